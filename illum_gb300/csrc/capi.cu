@@ -1,0 +1,596 @@
+// capi.cu — the C ABI of include/illum_gb300.h: context lifecycle, the
+// drop-in entry points for the reference's illum_context / thermal_model /
+// conduction calls, and the fused time-step loop of do_radiosity_task
+// (src/cpp/illum_cli.cpp:403-468), optionally captured as a CUDA graph.
+#include <stdarg.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "geom.h"
+#include "internal.cuh"
+
+struct ilg_ctx {
+  ilg::Context c;
+};
+
+namespace ilg {
+
+static thread_local std::string g_err;
+
+void set_error(const char* fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+}
+
+Context::~Context() {
+  if (graph) cudaGraphExecDestroy(graph);
+  for (auto& e : ev)
+    if (e) cudaEventDestroy(e);
+  if (pinned_aux) cudaFreeHost(pinned_aux);
+  if (pinned_tsurf) cudaFreeHost(pinned_tsurf);
+  if (stream) cudaStreamDestroy(stream);
+}
+
+int read_device_errors(Context& c) {
+  int h[DERR_COUNT];
+  ILG_CUDA(cudaMemcpyAsync(h, c.derr.p, sizeof(h), cudaMemcpyDeviceToHost, c.stream));
+  ILG_CUDA(cudaStreamSynchronize(c.stream));
+  bool any = false;
+  for (int i = 0; i < DERR_COUNT; ++i) any |= h[i] != 0;
+  if (!any) return ILG_OK;
+  ILG_CUDA(cudaMemsetAsync(c.derr.p, 0, sizeof(h), c.stream));
+  ILG_CUDA(cudaStreamSynchronize(c.stream));
+  if (h[DERR_NAN]) { set_error("computed a NaN form factor"); return ILG_ERR_NAN; }
+  if (h[DERR_PIVOT]) { set_error("zero pivot in a conduction column"); return ILG_ERR_PIVOT; }
+  if (h[DERR_STACK]) { set_error("BVH traversal stack overflow"); return ILG_ERR_DEVICE; }
+  if (h[DERR_BARRIER]) { set_error("radiosity grid barrier wait exceeded its limit"); return ILG_ERR_DEVICE; }
+  if (h[DERR_HORIZON]) { set_error("horizon bisection deeper than its table"); return ILG_ERR_DEVICE; }
+  set_error("device error flags set");
+  return ILG_ERR_DEVICE;
+}
+
+static int set_disk(Context& c, const double* disk_xy, int ndisk) {
+  if (!disk_xy || ndisk < 2) { set_error("disk_xy needs at least 2 rows"); return ILG_ERR_ARG; }
+  std::vector<double> h(disk_xy, disk_xy + 2 * (size_t)ndisk);
+  double rmax = 0.0;
+  for (int s = 0; s < ndisk - 1; ++s) rmax = std::max(rmax, std::sqrt(h[s] * h[s] + h[ndisk + s] * h[ndisk + s]));
+  ILG_TRY(c.disk.alloc(2 * (size_t)ndisk));
+  ILG_CUDA(cudaMemcpyAsync(c.disk.p, h.data(), h.size() * 8, cudaMemcpyHostToDevice, c.stream));
+  ILG_CUDA(cudaStreamSynchronize(c.stream));
+  c.ndisk = ndisk;
+  c.disk_rmax = rmax;
+  return ILG_OK;
+}
+
+static void invalidate_graph(Context& c) {
+  if (c.graph) cudaGraphExecDestroy(c.graph);
+  c.graph = nullptr;
+  for (int& k : c.graph_key) k = -1;
+}
+
+__global__ void k_advance(int* counters) {
+  counters[1] += 1;   // sun index
+  counters[2] += 1;   // frame
+}
+
+// One step on c.stream. suns_dev: SunAux table indexed by counters[1]
+// (from_counter) or a single entry. When the radiosity solve is off the
+// direct kernel writes rad directly.
+static int enqueue_step(Context& c, const ilg_run_opts& o, const void* suns_dev, int from_counter, bool timing) {
+  bool rad_on = o.use_radiosity && c.have_F && c.n_active > 0;
+  if (timing) ILG_CUDA(cudaEventRecord(c.ev[0], c.stream));
+  ILG_TRY(direct_launch_aux(c, suns_dev, from_counter, c.Fsurf.p, rad_on ? c.E.p : c.rad.p));
+  if (timing) ILG_CUDA(cudaEventRecord(c.ev[1], c.stream));
+  if (rad_on) ILG_TRY(radiosity_launch(c, c.E.p, c.rad.p, o.tol, o.max_sweeps, o.precision, true));
+  if (timing) ILG_CUDA(cudaEventRecord(c.ev[2], c.stream));
+  ILG_TRY(conduction_launch(c, c.rad.p, o.precision, true));
+  if (timing) ILG_CUDA(cudaEventRecord(c.ev[3], c.stream));
+  k_advance<<<1, 1, 0, c.stream>>>(c.counters.p);
+  ILG_CUDA(cudaGetLastError());
+  return ILG_OK;
+}
+
+static int ensure_pinned(Context& c) {
+  if (!c.pinned_aux) ILG_CUDA(cudaMallocHost((void**)&c.pinned_aux, 256));
+  if (!c.pinned_tsurf) ILG_CUDA(cudaMallocHost((void**)&c.pinned_tsurf, (size_t)c.nt * 8));
+  ILG_TRY(c.host_sun_aux.reserve(256));
+  return ILG_OK;
+}
+
+static int check_run(Context& c, const ilg_run_opts* o) {
+  if (!o) { set_error("opts is NULL"); return ILG_ERR_ARG; }
+  if (!c.have_thermal) { set_error("ilg_thermal_init has not been called"); return ILG_ERR_ARG; }
+  if (!c.H.p || c.nphi < 2) { set_error("horizons are not set"); return ILG_ERR_ARG; }
+  if (c.ndisk < 2) { set_error("sun disk samples are not set (ilg_set_suns)"); return ILG_ERR_ARG; }
+  if (!(o->dt > 0.0)) { set_error("dt must be > 0"); return ILG_ERR_ARG; }
+  if (o->precision != ILG_PREC_FP64 && o->precision != ILG_PREC_MIXED) { set_error("bad precision"); return ILG_ERR_ARG; }
+  if (o->use_radiosity && !c.have_F) { set_error("use_radiosity set but no form factors"); return ILG_ERR_ARG; }
+  if (o->precision == ILG_PREC_MIXED && o->use_radiosity && !c.have_bf16) { set_error("no bf16 form factors"); return ILG_ERR_ARG; }
+  ILG_TRY(conduction_prepare(c, o->dt, o->precision));
+  ILG_TRY(conduction_state_convert(c, o->precision));
+  if (o->use_radiosity && c.have_F && c.n_active > 0) ILG_TRY(radiosity_setup(c, o->precision));
+  ILG_TRY(ensure_pinned(c));
+  return ILG_OK;
+}
+
+// Graph of one step (kernels only). key identifies what was captured.
+static int get_graph(Context& c, const ilg_run_opts& o, const void* suns_dev, int from_counter, bool with_copies,
+                     cudaGraphExec_t* out) {
+  int key[4] = {o.precision * 2 + (o.use_radiosity ? 1 : 0), from_counter, with_copies ? 1 : 0,
+                (int)(((uintptr_t)suns_dev >> 4) & 0x7fffffff)};
+  if (c.graph && std::equal(key, key + 4, c.graph_key)) { *out = c.graph; return ILG_OK; }
+  invalidate_graph(c);
+  cudaGraph_t g;
+  ILG_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
+  int rc = ILG_OK;
+  if (with_copies)
+    if (cudaMemcpyAsync(c.host_sun_aux.p, c.pinned_aux, sun_aux_bytes(), cudaMemcpyHostToDevice, c.stream) != cudaSuccess)
+      rc = ILG_ERR_CUDA;
+  if (rc == ILG_OK) rc = enqueue_step(c, o, suns_dev, from_counter, false);
+  if (rc == ILG_OK && with_copies)
+    if (cudaMemcpyAsync(c.pinned_tsurf, c.Tsurf.p, (size_t)c.nt * 8, cudaMemcpyDeviceToHost, c.stream) != cudaSuccess)
+      rc = ILG_ERR_CUDA;
+  cudaError_t e = cudaStreamEndCapture(c.stream, &g);
+  if (rc != ILG_OK || e != cudaSuccess) {
+    cudaGetLastError();
+    if (e == cudaSuccess) cudaGraphDestroy(g);
+    set_error("step capture failed: %s", cudaGetErrorString(e));
+    return rc != ILG_OK ? rc : ILG_ERR_CUDA;
+  }
+  cudaError_t ei = cudaGraphInstantiate(&c.graph, g, 0);
+  cudaGraphDestroy(g);
+  if (ei != cudaSuccess) {
+    c.graph = nullptr;
+    set_error("graph instantiation failed: %s", cudaGetErrorString(ei));
+    return ILG_ERR_CUDA;
+  }
+  std::copy(key, key + 4, c.graph_key);
+  *out = c.graph;
+  return ILG_OK;
+}
+
+static int collect_stats(Context& c, bool timing) {
+  int h[4];
+  ILG_CUDA(cudaMemcpyAsync(h, c.counters.p, sizeof(h), cudaMemcpyDeviceToHost, c.stream));
+  ILG_CUDA(cudaStreamSynchronize(c.stream));
+  c.stats_ambiguous += h[0];
+  c.stats_sweeps += h[3];
+  if (timing) {
+    float a, b, d;
+    ILG_CUDA(cudaEventElapsedTime(&a, c.ev[0], c.ev[1]));
+    ILG_CUDA(cudaEventElapsedTime(&b, c.ev[1], c.ev[2]));
+    ILG_CUDA(cudaEventElapsedTime(&d, c.ev[2], c.ev[3]));
+    c.ms_direct += a;
+    c.ms_rad += b;
+    c.ms_cond += d;
+  }
+  return ILG_OK;
+}
+
+}  // namespace ilg
+
+using namespace ilg;
+
+extern "C" {
+
+const char* ilg_last_error(void) { return g_err.c_str(); }
+int ilg_version(void) { return 10000; }
+
+int ilg_ctx_create(const float* verts, int nv, const int32_t* tris, int nt, const float* normals, ilg_ctx** out) {
+  if (!out || !verts || !tris || nv < 3 || nt < 1) { set_error("invalid mesh arguments"); return ILG_ERR_ARG; }
+  *out = nullptr;
+  ilg_ctx* h = new ilg_ctx();
+  Context& c = h->c;
+  c.nt = nt;
+  int rc = ILG_OK;
+  if (cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) != cudaSuccess) {
+    set_error("cudaStreamCreate failed");
+    delete h;
+    return ILG_ERR_CUDA;
+  }
+  for (auto& e : c.ev)
+    if (cudaEventCreate(&e) != cudaSuccess) { set_error("cudaEventCreate failed"); delete h; return ILG_ERR_CUDA; }
+  if ((rc = c.derr.alloc(DERR_COUNT)) || (rc = c.counters.alloc(8)) || (rc = c.work.alloc(nt)) ||
+      (rc = c.barrier.alloc(2))) {
+    delete h;
+    return rc;
+  }
+  cudaMemsetAsync(c.derr.p, 0, DERR_COUNT * sizeof(int), c.stream);
+  cudaMemsetAsync(c.counters.p, 0, 8 * sizeof(int), c.stream);
+  rc = bvh_build(c, verts, nv, tris, normals);
+  if (rc == ILG_OK) rc = read_device_errors(c);
+  if (rc != ILG_OK) { delete h; return rc; }
+  *out = h;
+  return ILG_OK;
+}
+
+int ilg_ctx_destroy(ilg_ctx* ctx) {
+  delete ctx;
+  return ILG_OK;
+}
+
+int ilg_ctx_num_faces(const ilg_ctx* ctx) { return ctx ? ctx->c.nt : 0; }
+
+int ilg_ctx_info(const ilg_ctx* ctx, int64_t* bvh_nodes, int* bvh_depth) {
+  if (!ctx) { set_error("ctx is NULL"); return ILG_ERR_ARG; }
+  if (bvh_nodes) *bvh_nodes = ctx->c.bvh_nodes;
+  if (bvh_depth) *bvh_depth = ctx->c.bvh_depth;
+  return ILG_OK;
+}
+
+int ilg_trace(ilg_ctx* ctx, int nrays, const float* orig, const float* dir, int any_hit, int32_t* hit, double* t) {
+  if (!ctx || nrays < 0 || (nrays > 0 && (!orig || !dir || !hit))) { set_error("invalid trace arguments"); return ILG_ERR_ARG; }
+  return bvh_trace(ctx->c, nrays, orig, dir, any_hit, hit, t);
+}
+
+int ilg_compute_F(ilg_ctx* ctx, const double* albedo, double albedo_scalar, double offset, int64_t* nnz, int64_t* rays) {
+  if (!ctx) { set_error("ctx is NULL"); return ILG_ERR_ARG; }
+  invalidate_graph(ctx->c);
+  ILG_TRY(form_factors_build(ctx->c, albedo, albedo_scalar, offset, rays));
+  if (nnz) *nnz = ctx->c.nnz;
+  return ILG_OK;
+}
+
+int ilg_get_F(ilg_ctx* ctx, int64_t* rowptr, int32_t* col, double* val) {
+  if (!ctx || !ctx->c.have_F) { set_error("no form factors"); return ILG_ERR_ARG; }
+  Context& c = ctx->c;
+  if (rowptr) ILG_CUDA(cudaMemcpyAsync(rowptr, c.rowptr.p, ((size_t)c.nt + 1) * 8, cudaMemcpyDeviceToHost, c.stream));
+  if (c.nnz > 0) {
+    if (col) ILG_CUDA(cudaMemcpyAsync(col, c.col.p, (size_t)c.nnz * 4, cudaMemcpyDeviceToHost, c.stream));
+    if (val) ILG_CUDA(cudaMemcpyAsync(val, c.val.p, (size_t)c.nnz * 8, cudaMemcpyDeviceToHost, c.stream));
+  }
+  ILG_CUDA(cudaStreamSynchronize(c.stream));
+  return ILG_OK;
+}
+
+int ilg_set_F(ilg_ctx* ctx, int64_t nnz, const int64_t* rowptr, const int32_t* col, const double* val) {
+  if (!ctx || nnz < 0 || !rowptr || (nnz > 0 && (!col || !val))) { set_error("invalid F arguments"); return ILG_ERR_ARG; }
+  Context& c = ctx->c;
+  if (rowptr[0] != 0 || rowptr[c.nt] != nnz) { set_error("rowptr does not span nnz"); return ILG_ERR_ARG; }
+  for (int i = 0; i < c.nt; ++i)
+    if (rowptr[i + 1] < rowptr[i]) { set_error("rowptr decreases at row %d", i); return ILG_ERR_ARG; }
+  for (int64_t k = 0; k < nnz; ++k)
+    if (col[k] < 0 || col[k] >= c.nt) { set_error("column index out of range at %lld", (long long)k); return ILG_ERR_ARG; }
+  invalidate_graph(c);
+  ILG_TRY(c.rowptr.alloc((size_t)c.nt + 1));
+  ILG_TRY(c.col.alloc(nnz > 0 ? nnz : 1));
+  ILG_TRY(c.val.alloc(nnz > 0 ? nnz : 1));
+  ILG_CUDA(cudaMemcpyAsync(c.rowptr.p, rowptr, ((size_t)c.nt + 1) * 8, cudaMemcpyHostToDevice, c.stream));
+  if (nnz > 0) {
+    ILG_CUDA(cudaMemcpyAsync(c.col.p, col, (size_t)nnz * 4, cudaMemcpyHostToDevice, c.stream));
+    ILG_CUDA(cudaMemcpyAsync(c.val.p, val, (size_t)nnz * 8, cudaMemcpyHostToDevice, c.stream));
+  }
+  c.nnz = nnz;
+  c.have_F = true;
+  return radiosity_prepare(c);
+}
+
+int ilg_make_horizons(ilg_ctx* ctx, int nphi, double theta_eps, double offset) {
+  if (!ctx) { set_error("ctx is NULL"); return ILG_ERR_ARG; }
+  invalidate_graph(ctx->c);
+  return horizons_build(ctx->c, nphi, theta_eps, offset);
+}
+
+int ilg_get_horizons(ilg_ctx* ctx, double* out) {
+  if (!ctx || !ctx->c.H.p || !out) { set_error("no horizons"); return ILG_ERR_ARG; }
+  Context& c = ctx->c;
+  ILG_CUDA(cudaMemcpyAsync(out, c.H.p, (size_t)c.nt * c.nphi * 8, cudaMemcpyDeviceToHost, c.stream));
+  ILG_CUDA(cudaStreamSynchronize(c.stream));
+  return ILG_OK;
+}
+
+int ilg_set_horizons(ilg_ctx* ctx, int nphi, const double* h) {
+  if (!ctx || nphi < 2 || !h) { set_error("invalid horizon arguments"); return ILG_ERR_ARG; }
+  Context& c = ctx->c;
+  invalidate_graph(c);
+  size_t n = (size_t)c.nt * nphi;
+  std::vector<double> lo(c.nt), hi(c.nt);
+  for (int f = 0; f < c.nt; ++f) {
+    const double* col = h + (size_t)f * nphi;
+    double a = col[0], b = col[0];
+    for (int k = 1; k < nphi; ++k) { a = std::min(a, col[k]); b = std::max(b, col[k]); }
+    if (!(a == a) || !(b == b)) { set_error("horizon column %d holds NaN", f); return ILG_ERR_ARG; }
+    lo[f] = a;
+    hi[f] = b;
+  }
+  ILG_TRY(c.H.alloc(n));
+  ILG_TRY(c.hmin.alloc(c.nt));
+  ILG_TRY(c.hmax.alloc(c.nt));
+  ILG_CUDA(cudaMemcpyAsync(c.H.p, h, n * 8, cudaMemcpyHostToDevice, c.stream));
+  ILG_CUDA(cudaMemcpyAsync(c.hmin.p, lo.data(), (size_t)c.nt * 8, cudaMemcpyHostToDevice, c.stream));
+  ILG_CUDA(cudaMemcpyAsync(c.hmax.p, hi.data(), (size_t)c.nt * 8, cudaMemcpyHostToDevice, c.stream));
+  ILG_CUDA(cudaStreamSynchronize(c.stream));
+  c.nphi = nphi;
+  c.dphi = TWO_PI / (double)(nphi - 1);
+  return ILG_OK;
+}
+
+int ilg_set_insolation(ilg_ctx* ctx, int norm_mode, int interp, double solar_const) {
+  if (!ctx || (norm_mode != 0 && norm_mode != 1) || (interp != 0 && interp != 1) || !(solar_const >= 0.0)) {
+    set_error("invalid insolation options");
+    return ILG_ERR_ARG;
+  }
+  Context& c = ctx->c;
+  invalidate_graph(c);
+  c.norm_mode = norm_mode;
+  c.interp = interp;
+  c.solar_const = solar_const;
+  if (c.nsun > 0 && c.sun_aux.p) {   // flux is baked into the per-sun table: rebuild
+    std::vector<double> s((size_t)c.nsun * 3);
+    ILG_CUDA(cudaMemcpy(s.data(), c.suns.p, s.size() * 8, cudaMemcpyDeviceToHost));
+    std::vector<unsigned char> aux((size_t)c.nsun * sun_aux_bytes());
+    sun_aux_fill(c, s.data(), c.nsun, aux.data());
+    ILG_CUDA(cudaMemcpy(c.sun_aux.p, aux.data(), aux.size(), cudaMemcpyHostToDevice));
+  }
+  return ILG_OK;
+}
+
+void ilg_fib_spiral(double* xy, int n) {
+  if (xy && n > 0) fib_spiral(xy, n);
+}
+
+int ilg_direct_radiosity(ilg_ctx* ctx, const double* sun, const double* disk_xy, int ndisk, double* out) {
+  if (!ctx || !sun || !out) { set_error("invalid direct arguments"); return ILG_ERR_ARG; }
+  Context& c = ctx->c;
+  ILG_TRY(set_disk(c, disk_xy, ndisk));
+  ILG_TRY(ensure_pinned(c));
+  ILG_TRY(c.E.reserve(c.nt));
+  sun_aux_fill(c, sun, 1, c.pinned_aux);
+  ILG_CUDA(cudaMemcpyAsync(c.host_sun_aux.p, c.pinned_aux, sun_aux_bytes(), cudaMemcpyHostToDevice, c.stream));
+  ILG_TRY(direct_launch_aux(c, c.host_sun_aux.p, 0, nullptr, c.E.p));
+  ILG_CUDA(cudaMemcpyAsync(out, c.E.p, (size_t)c.nt * 8, cudaMemcpyDeviceToHost, c.stream));
+  ILG_CUDA(cudaStreamSynchronize(c.stream));
+  return read_device_errors(c);
+}
+
+int ilg_radiosity_solve(ilg_ctx* ctx, const double* E, double tol, int max_sweeps, double* x, double* res, int* sweeps) {
+  if (!ctx || !E || !x || max_sweeps < 1 || !(tol >= 0.0)) { set_error("invalid radiosity arguments"); return ILG_ERR_ARG; }
+  Context& c = ctx->c;
+  if (!c.have_F) { set_error("no form factors"); return ILG_ERR_ARG; }
+  ILG_TRY(c.E.reserve(c.nt));
+  ILG_TRY(c.Q.reserve(c.nt));
+  ILG_CUDA(cudaMemcpyAsync(c.E.p, E, (size_t)c.nt * 8, cudaMemcpyHostToDevice, c.stream));
+  if (c.n_active == 0) {
+    std::memcpy(x, E, (size_t)c.nt * 8);
+    if (res) *res = 0.0;
+    if (sweeps) *sweeps = 0;
+    return ILG_OK;
+  }
+  ILG_CUDA(cudaMemsetAsync(c.counters.p + 3, 0, sizeof(int), c.stream));
+  ILG_TRY(radiosity_launch(c, c.E.p, c.Q.p, tol, max_sweeps, ILG_PREC_FP64, false));
+  double r2 = 0.0;
+  int sw = 0;
+  ILG_CUDA(cudaMemcpyAsync(x, c.Q.p, (size_t)c.nt * 8, cudaMemcpyDeviceToHost, c.stream));
+  ILG_CUDA(cudaMemcpyAsync(&r2, c.partials.p + 2 * c.rad_grid, 8, cudaMemcpyDeviceToHost, c.stream));
+  ILG_CUDA(cudaMemcpyAsync(&sw, c.counters.p + 3, 4, cudaMemcpyDeviceToHost, c.stream));
+  ILG_CUDA(cudaStreamSynchronize(c.stream));
+  ILG_TRY(read_device_errors(c));
+  if (res) *res = std::sqrt(r2);
+  if (sweeps) *sweeps = sw;
+  if (r2 > tol * tol) { set_error("radiosity residual %g above tol after %d sweeps", std::sqrt(r2), sw); return ILG_ERR_NOTCONV; }
+  return ILG_OK;
+}
+
+int ilg_thermal_init(ilg_ctx* ctx, int nz, const double* z, const double* ti, const double* rhoc, double T0,
+                     const double* T0_full, double emissivity, double Fgeotherm, int bc_mode, int precision) {
+  if (!ctx || nz < 2 || !z || !ti || !rhoc) { set_error("invalid thermal arguments"); return ILG_ERR_ARG; }
+  if (bc_mode != ILG_BC_LINEARISED && bc_mode != ILG_BC_NEWTON) { set_error("bad bc_mode"); return ILG_ERR_ARG; }
+  if (precision != ILG_PREC_FP64 && precision != ILG_PREC_MIXED) { set_error("bad precision"); return ILG_ERR_ARG; }
+  Context& c = ctx->c;
+  invalidate_graph(c);
+  int nt = c.nt;
+  c.nz = nz;
+  c.z_h.assign(z, z + nz);
+  c.ti_h.assign(ti, ti + nz);
+  c.rhoc_h.assign(rhoc, rhoc + nz);
+  c.emiss = emissivity;
+  c.Fgeo = Fgeotherm;
+  c.bc_mode = bc_mode;
+  c.coef_dt = -1.0;
+  c.coef_prec = -1;
+  size_t n = (size_t)nz * nt;
+  std::vector<double> Tl(n), ts(nt);
+  for (int f = 0; f < nt; ++f) {
+    ts[f] = T0_full ? T0_full[(size_t)f * (nz + 1)] : T0;
+    for (int i = 0; i < nz; ++i) Tl[(size_t)i * nt + f] = T0_full ? T0_full[(size_t)f * (nz + 1) + 1 + i] : T0;
+  }
+  ILG_TRY(c.T64.alloc(n));
+  ILG_TRY(c.Tsurf.alloc(nt));
+  ILG_TRY(c.Fsurf.alloc(nt));
+  ILG_TRY(c.Qprev.alloc(nt));
+  ILG_TRY(c.rad.alloc(nt));
+  ILG_TRY(c.rad_avg.alloc(nt));
+  ILG_TRY(c.therm_avg.alloc(nt));
+  ILG_TRY(c.therm_max.alloc(nt));
+  ILG_TRY(c.E.reserve(nt));
+  ILG_TRY(c.Q.reserve(nt));
+  ILG_CUDA(cudaMemcpyAsync(c.T64.p, Tl.data(), n * 8, cudaMemcpyHostToDevice, c.stream));
+  ILG_CUDA(cudaMemcpyAsync(c.Tsurf.p, ts.data(), (size_t)nt * 8, cudaMemcpyHostToDevice, c.stream));
+  for (double* p : {c.Fsurf.p, c.Qprev.p, c.rad.p, c.rad_avg.p, c.therm_avg.p, c.therm_max.p})
+    ILG_CUDA(cudaMemsetAsync(p, 0, (size_t)nt * 8, c.stream));
+  ILG_CUDA(cudaMemsetAsync(c.counters.p, 0, 8 * sizeof(int), c.stream));
+  ILG_CUDA(cudaStreamSynchronize(c.stream));
+  c.state_prec = ILG_PREC_FP64;
+  c.frame_no = 0;
+  c.have_thermal = true;
+  return conduction_state_convert(c, precision);
+}
+
+int ilg_thermal_step(ilg_ctx* ctx, double dt, const double* Q) {
+  if (!ctx || !Q || !(dt > 0.0)) { set_error("invalid thermal step arguments"); return ILG_ERR_ARG; }
+  Context& c = ctx->c;
+  if (!c.have_thermal) { set_error("ilg_thermal_init has not been called"); return ILG_ERR_ARG; }
+  ILG_TRY(conduction_prepare(c, dt, c.state_prec));
+  ILG_CUDA(cudaMemcpyAsync(c.Q.p, Q, (size_t)c.nt * 8, cudaMemcpyHostToDevice, c.stream));
+  ILG_TRY(conduction_launch(c, c.Q.p, c.state_prec, false));
+  ILG_CUDA(cudaStreamSynchronize(c.stream));
+  return read_device_errors(c);
+}
+
+int ilg_thermal_get(ilg_ctx* ctx, double* T, double* Fsurf, double* Qprev) {
+  if (!ctx) { set_error("ctx is NULL"); return ILG_ERR_ARG; }
+  Context& c = ctx->c;
+  if (!c.have_thermal) { set_error("ilg_thermal_init has not been called"); return ILG_ERR_ARG; }
+  int nt = c.nt, nz = c.nz;
+  if (T) {
+    size_t n = (size_t)nz * nt;
+    std::vector<double> Tl(n), ts(nt);
+    if (c.state_prec == ILG_PREC_MIXED) {
+      std::vector<float> t32(n);
+      ILG_CUDA(cudaMemcpyAsync(t32.data(), c.T32.p, n * 4, cudaMemcpyDeviceToHost, c.stream));
+      ILG_CUDA(cudaStreamSynchronize(c.stream));
+      for (size_t i = 0; i < n; ++i) Tl[i] = t32[i];
+    } else {
+      ILG_CUDA(cudaMemcpyAsync(Tl.data(), c.T64.p, n * 8, cudaMemcpyDeviceToHost, c.stream));
+    }
+    ILG_CUDA(cudaMemcpyAsync(ts.data(), c.Tsurf.p, (size_t)nt * 8, cudaMemcpyDeviceToHost, c.stream));
+    ILG_CUDA(cudaStreamSynchronize(c.stream));
+    for (int f = 0; f < nt; ++f) {
+      T[(size_t)f * (nz + 1)] = ts[f];
+      for (int i = 0; i < nz; ++i) T[(size_t)f * (nz + 1) + 1 + i] = Tl[(size_t)i * nt + f];
+    }
+  }
+  if (Fsurf) ILG_CUDA(cudaMemcpyAsync(Fsurf, c.Fsurf.p, (size_t)nt * 8, cudaMemcpyDeviceToHost, c.stream));
+  if (Qprev) ILG_CUDA(cudaMemcpyAsync(Qprev, c.Qprev.p, (size_t)nt * 8, cudaMemcpyDeviceToHost, c.stream));
+  ILG_CUDA(cudaStreamSynchronize(c.stream));
+  return ILG_OK;
+}
+
+int ilg_set_suns(ilg_ctx* ctx, int nsun, const double* suns, const double* disk_xy, int ndisk) {
+  if (!ctx || nsun < 1 || !suns) { set_error("invalid sun arguments"); return ILG_ERR_ARG; }
+  Context& c = ctx->c;
+  invalidate_graph(c);
+  ILG_TRY(set_disk(c, disk_xy, ndisk));
+  std::vector<unsigned char> aux((size_t)nsun * sun_aux_bytes());
+  sun_aux_fill(c, suns, nsun, aux.data());
+  ILG_TRY(c.sun_aux.alloc(aux.size()));
+  ILG_TRY(c.suns.alloc((size_t)nsun * 3));
+  ILG_CUDA(cudaMemcpyAsync(c.sun_aux.p, aux.data(), aux.size(), cudaMemcpyHostToDevice, c.stream));
+  ILG_CUDA(cudaMemcpyAsync(c.suns.p, suns, (size_t)nsun * 24, cudaMemcpyHostToDevice, c.stream));
+  ILG_CUDA(cudaStreamSynchronize(c.stream));
+  c.nsun = nsun;
+  return ILG_OK;
+}
+
+int ilg_run_steps(ilg_ctx* ctx, const ilg_run_opts* opts, int first_sun, int nsteps, double* tsurf_out) {
+  if (!ctx) { set_error("ctx is NULL"); return ILG_ERR_ARG; }
+  Context& c = ctx->c;
+  ILG_TRY(check_run(c, opts));
+  if (nsteps < 0 || first_sun < 0 || first_sun + nsteps > c.nsun) { set_error("sun range out of bounds"); return ILG_ERR_ARG; }
+  const ilg_run_opts& o = *opts;
+  int h2[2] = {first_sun, c.frame_no};
+  ILG_CUDA(cudaMemcpyAsync(c.counters.p + 1, h2, sizeof(h2), cudaMemcpyHostToDevice, c.stream));
+  ILG_CUDA(cudaStreamSynchronize(c.stream));
+  bool timing = c.timing;
+  cudaGraphExec_t g = nullptr;
+  if (o.use_graph && !timing && !c.graph_broken)
+    if (get_graph(c, o, c.sun_aux.p, 1, false, &g) != ILG_OK) { c.graph_broken = true; g = nullptr; cudaGetLastError(); }
+  if (tsurf_out) ILG_TRY(ensure_pinned(c));
+  for (int s = 0; s < nsteps; ++s) {
+    if (g) ILG_CUDA(cudaGraphLaunch(g, c.stream));
+    else ILG_TRY(enqueue_step(c, o, c.sun_aux.p, 1, timing));
+    if (timing) ILG_TRY(collect_stats(c, true));
+    if (tsurf_out) {
+      ILG_CUDA(cudaMemcpyAsync(c.pinned_tsurf, c.Tsurf.p, (size_t)c.nt * 8, cudaMemcpyDeviceToHost, c.stream));
+      ILG_CUDA(cudaStreamSynchronize(c.stream));
+      std::memcpy(tsurf_out + (size_t)s * c.nt, c.pinned_tsurf, (size_t)c.nt * 8);
+    }
+  }
+  ILG_CUDA(cudaStreamSynchronize(c.stream));
+  c.frame_no += nsteps;
+  return read_device_errors(c);
+}
+
+int ilg_run_steps_host(ilg_ctx* ctx, const ilg_run_opts* opts, int nsteps, const double* suns, double* tsurf_out) {
+  if (!ctx || (nsteps > 0 && !suns)) { set_error("invalid arguments"); return ILG_ERR_ARG; }
+  Context& c = ctx->c;
+  ILG_TRY(check_run(c, opts));
+  ILG_TRY(ensure_pinned(c));
+  const ilg_run_opts& o = *opts;
+  int h2[2] = {0, c.frame_no};
+  ILG_CUDA(cudaMemcpyAsync(c.counters.p + 1, h2, sizeof(h2), cudaMemcpyHostToDevice, c.stream));
+  ILG_CUDA(cudaStreamSynchronize(c.stream));
+  bool timing = c.timing;
+  cudaGraphExec_t g = nullptr;
+  if (o.use_graph && !timing && !c.graph_broken)
+    if (get_graph(c, o, c.host_sun_aux.p, 0, true, &g) != ILG_OK) { c.graph_broken = true; g = nullptr; cudaGetLastError(); }
+  for (int s = 0; s < nsteps; ++s) {
+    sun_aux_fill(c, suns + 3 * (size_t)s, 1, c.pinned_aux);
+    if (g) {
+      ILG_CUDA(cudaGraphLaunch(g, c.stream));
+    } else {
+      ILG_CUDA(cudaMemcpyAsync(c.host_sun_aux.p, c.pinned_aux, sun_aux_bytes(), cudaMemcpyHostToDevice, c.stream));
+      ILG_TRY(enqueue_step(c, o, c.host_sun_aux.p, 0, timing));
+      ILG_CUDA(cudaMemcpyAsync(c.pinned_tsurf, c.Tsurf.p, (size_t)c.nt * 8, cudaMemcpyDeviceToHost, c.stream));
+    }
+    ILG_CUDA(cudaStreamSynchronize(c.stream));
+    if (timing) ILG_TRY(collect_stats(c, true));
+    if (tsurf_out) std::memcpy(tsurf_out + (size_t)s * c.nt, c.pinned_tsurf, (size_t)c.nt * 8);
+  }
+  c.frame_no += nsteps;
+  return read_device_errors(c);
+}
+
+int ilg_get_outputs(ilg_ctx* ctx, double* rad, double* rad_avg, double* therm_avg, double* therm_max) {
+  if (!ctx) { set_error("ctx is NULL"); return ILG_ERR_ARG; }
+  Context& c = ctx->c;
+  if (!c.have_thermal) { set_error("ilg_thermal_init has not been called"); return ILG_ERR_ARG; }
+  size_t b = (size_t)c.nt * 8;
+  if (rad) ILG_CUDA(cudaMemcpyAsync(rad, c.rad.p, b, cudaMemcpyDeviceToHost, c.stream));
+  if (rad_avg) ILG_CUDA(cudaMemcpyAsync(rad_avg, c.rad_avg.p, b, cudaMemcpyDeviceToHost, c.stream));
+  if (therm_avg) ILG_CUDA(cudaMemcpyAsync(therm_avg, c.therm_avg.p, b, cudaMemcpyDeviceToHost, c.stream));
+  if (therm_max) ILG_CUDA(cudaMemcpyAsync(therm_max, c.therm_max.p, b, cudaMemcpyDeviceToHost, c.stream));
+  ILG_CUDA(cudaStreamSynchronize(c.stream));
+  return ILG_OK;
+}
+
+int ilg_set_timing(ilg_ctx* ctx, int enable) {
+  if (!ctx) { set_error("ctx is NULL"); return ILG_ERR_ARG; }
+  Context& c = ctx->c;
+  c.timing = enable != 0;
+  c.ms_direct = c.ms_rad = c.ms_cond = 0.f;
+  c.stats_ambiguous = c.stats_sweeps = 0;
+  return ILG_OK;
+}
+
+int ilg_get_stats(ilg_ctx* ctx, double* ms_direct, double* ms_radiosity, double* ms_conduction, int64_t* ambiguous,
+                  int64_t* sweeps) {
+  if (!ctx) { set_error("ctx is NULL"); return ILG_ERR_ARG; }
+  Context& c = ctx->c;
+  if (ms_direct) *ms_direct = c.ms_direct;
+  if (ms_radiosity) *ms_radiosity = c.ms_rad;
+  if (ms_conduction) *ms_conduction = c.ms_cond;
+  if (ambiguous) *ambiguous = c.stats_ambiguous;
+  if (sweeps) *sweeps = c.stats_sweeps;
+  return ILG_OK;
+}
+
+void conductionq_(int* nz, const double z[], double* dt, double* Qn, double* Qnp1, double T[], const double ti[],
+                  const double rhoc[], double* emiss, double* Tsurf, double* Fgeotherm, double* Fsurf) {
+  int rc = conduction_batch_host(1, *nz, z, *dt, Qn, Qnp1, T, ti, rhoc, *emiss, Tsurf, *Fgeotherm, Fsurf,
+                                 ILG_BC_LINEARISED);
+  if (rc != ILG_OK) fprintf(stderr, "conductionq_: %s\n", g_err.c_str());
+}
+
+void conductiont_(int* nz, const double z[], double* dt, double T[], double* Tsurf, double* Tsurfp1, const double ti[],
+                  const double rhoc[], double* Fgeotherm, double* Fsurf) {
+  int rc = conductiont_host(*nz, z, *dt, T, *Tsurf, *Tsurfp1, ti, rhoc, *Fgeotherm, Fsurf);
+  if (rc != ILG_OK) fprintf(stderr, "conductiont_: %s\n", g_err.c_str());
+}
+
+int ilg_conductionq_batch(int ncol, int nz, const double* z, double dt, const double* Qn, const double* Qnp1, double* T,
+                          const double* ti, const double* rhoc, double emiss, double* Tsurf, double Fgeotherm,
+                          double* Fsurf, int bc_mode) {
+  if (ncol < 0 || !z || !Qnp1 || !T || !ti || !rhoc || !Tsurf || !Fsurf) { set_error("invalid arguments"); return ILG_ERR_ARG; }
+  return conduction_batch_host(ncol, nz, z, dt, Qn, Qnp1, T, ti, rhoc, emiss, Tsurf, Fgeotherm, Fsurf, bc_mode);
+}
+
+}  // extern "C"

@@ -1,0 +1,343 @@
+// conduction.cu — batched Crank-Nicolson conduction, one thread per facet
+// column: conductionQ.f (src/cpp/conductionQ.f:1-99) as driven by
+// thermal_model::step (src/cpp/thermal.hpp:65-83), plus conductionT.f
+// (src/cpp/conductionT.f:1-71) for the ABI.
+//
+// The reference rebuilds every coefficient and runs a full Thomas solve per
+// facet per step. Here the depth profile (z, ti, rho*c) is shared by all
+// facets of a mesh, so rows 2..nz of the tridiagonal matrix are the same for
+// every column: their bottom-up elimination factors (1/beta_i and
+// c_i/beta_{i+1}) are computed once per (mesh, dt) on the host. Per column
+// and step only the right-hand side changes:
+//   upward pass:   rho_i = r_i - (c_i/beta_{i+1}) rho_{i+1}   (i = nz..2)
+//   top row:       the surface boundary, linearised as in conductionQ.f:76-82
+//                  or solved by Newton's method for emiss*sigma*Ts^4
+//                  (T1 is affine in Ts once rows 2..nz are eliminated, so the
+//                  Newton iteration is scalar)
+//   downward pass: T_i = (rho_i + gamma_i T_{i-1}) / beta_i
+// rho is staged in shared memory ([layer][thread], conflict-free). The
+// temperature state is layer-major [nz][N], so every layer access of a warp
+// is one coalesced 256-byte (fp64) or 128-byte (fp32) transaction.
+#include <cmath>
+#include <vector>
+
+#include "geom.h"
+#include "internal.cuh"
+
+namespace ilg {
+
+namespace {
+
+constexpr int COND_THREADS = 128;
+constexpr int TAB_W = 5;            // g, m, al, f, inv_beta per layer
+constexpr size_t SMEM_LIMIT = 160 * 1024;
+
+template <class R, bool SMEM>
+__global__ void __launch_bounds__(COND_THREADS)
+k_conduct(const R* __restrict__ tab, CondScalars cs, int nt, R* __restrict__ T, double* __restrict__ Tsurf,
+          double* __restrict__ Fsurf, double* __restrict__ Qprev, const double* __restrict__ Qnp1,
+          R* __restrict__ rho_g, int upd, double* __restrict__ rad_avg, double* __restrict__ therm_avg,
+          double* __restrict__ therm_max, const int* __restrict__ frame_ptr, int frame_host,
+          int* __restrict__ derr) {
+  extern __shared__ unsigned char smem_raw[];
+  R* rho_s = reinterpret_cast<R*>(smem_raw);
+  int f = blockIdx.x * COND_THREADS + threadIdx.x;
+  if (f >= nt) return;
+  const int nz = cs.nz;
+  const size_t N = (size_t)nt;
+#define RHO(i) (SMEM ? rho_s[(size_t)(i) * COND_THREADS + threadIdx.x] : rho_g[(size_t)(i) * N + f])
+  // upward pass
+  R Tip1 = T[(size_t)(nz - 1) * N + f];
+  R Ti = T[(size_t)(nz - 2) * N + f];
+  const R* cb = tab + (size_t)(nz - 1) * TAB_W;
+  R rho_next = cb[0] * Ti + cb[1] * Tip1 + (R)cs.cgeo;
+  RHO(nz - 1) = rho_next;
+  for (int i = nz - 2; i >= 1; --i) {
+    R Tim1 = T[(size_t)(i - 1) * N + f];
+    const R* c = tab + (size_t)i * TAB_W;
+    R r = c[0] * Tim1 + c[1] * Ti + c[2] * Tip1;
+    R rh = r - c[3] * rho_next;
+    RHO(i) = rh;
+    rho_next = rh;
+    Tip1 = Ti;
+    Ti = Tim1;
+  }
+  // top row (Ti = T_1, Tip1 = T_2 in the Fortran's numbering)
+  double T0 = (double)Ti, T1 = (double)Tip1, rho1 = (double)rho_next;
+  double Ts = Tsurf[f];
+  double Q = Qnp1[f];
+  double T0n, Tsn;
+  if (cs.bc == 0) {
+    double Qn = Qprev[f];
+    double Tr3 = Ts * Ts * Ts;
+    double arad = -3.0 * cs.es * Tr3 * Ts;
+    double brad = 2.0 * cs.es * Tr3;
+    double den = cs.k1 + brad;
+    double ann = (Qn - arad) / den, annp1 = (Q - arad) / den, bn = (cs.k1 - brad) / den;
+    double b0 = 1.0 + cs.alpha0 + cs.gamma0 - cs.gamma0 * bn;
+    double r0 = cs.gamma0 * (annp1 + ann) + (1.0 - cs.alpha0 - cs.gamma0 + cs.gamma0 * bn) * T0 + cs.alpha0 * T1;
+    double piv = b0 + cs.f0 * cs.gamma1;
+    if (piv == 0.0) { atomicExch(&derr[DERR_PIVOT], 1); return; }
+    T0n = (r0 - cs.f0 * rho1) / piv;
+    Tsn = 0.5 * (annp1 + bn * T0n + T0n);
+  } else if (cs.bc == 1) {
+    double R0 = (1.0 - cs.alpha0 - cs.gamma0) * T0 + cs.alpha0 * T1 + cs.gamma0 * (2.0 * Ts - T0);
+    double P = (R0 - cs.f0 * rho1) / cs.Ap;
+    double S = 2.0 * cs.gamma0 / cs.Ap;
+    double x = Ts;
+    double tolr = sizeof(R) == 8 ? 1e-13 : 1e-9;
+    for (int it = 0; it < 30; ++it) {
+      double x3 = x * x * x;
+      double g = Q + 2.0 * cs.k1 * (P + (S - 1.0) * x) - cs.es * x3 * x;
+      double dg = 2.0 * cs.k1 * (S - 1.0) - 4.0 * cs.es * x3;
+      double dT = g / dg;
+      x -= dT;
+      if (fabs(dT) <= tolr * fabs(x)) break;
+    }
+    Tsn = x;
+    T0n = P + S * Tsn;
+  } else {
+    // prescribed surface temperature: Ts at n, Q holds Ts at n+1
+    double b0 = 1.0 + cs.alpha0 + cs.gamma0;
+    double r0 = cs.alpha0 * T1 + (1.0 - cs.alpha0 - cs.gamma0) * T0 + cs.gamma0 * (Ts + Q);
+    T0n = (r0 - cs.f0 * rho1) / (b0 + cs.f0 * cs.gamma1);
+    Tsn = Q;
+  }
+  double Fs = -cs.k0 * (T0n - Tsn) / cs.z0;
+  // downward pass
+  R prev = (R)T0n;
+  T[f] = prev;
+  for (int i = 1; i < nz; ++i) {
+    const R* c = tab + (size_t)i * TAB_W;
+    R t = (RHO(i) + c[0] * prev) * c[4];
+    T[(size_t)i * N + f] = t;
+    prev = t;
+  }
+#undef RHO
+  Fsurf[f] = Fs;
+  if (cs.bc != 2) {
+    Tsurf[f] = Tsn;
+    Qprev[f] = Q;
+  }
+  if (upd) {
+    int frame = frame_ptr ? *frame_ptr : frame_host;
+    double inv = (double)(frame + 1);
+    rad_avg[f] += (Q - rad_avg[f]) / inv;
+    therm_avg[f] += (Tsn - therm_avg[f]) / inv;
+    if (frame > 50) therm_max[f] = fmax(therm_max[f], Tsn);
+  }
+}
+
+template <class A, class B>
+__global__ void k_convert(const A* __restrict__ in, B* __restrict__ out, size_t n) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (B)in[i];
+}
+
+// Coefficients of conductionQ.f:50-73 / conductionT.f:28-45 and the shared
+// elimination factors. tab: nz x TAB_W.
+int build_tables(int nz, const double* z, const double* ti, const double* rhoc, double dt, double emiss, double Fgeo,
+                 int bc, std::vector<double>& tab, CondScalars& cs) {
+  if (nz < 2) { set_error("conduction needs nz >= 2 (got %d)", nz); return ILG_ERR_ARG; }
+  std::vector<double> k(nz), alpha(nz, 0.0), gamma(nz, 0.0), a(nz), b(nz), c(nz), beta(nz, 0.0);
+  for (int i = 0; i < nz; ++i) {
+    if (!(rhoc[i] > 0.0)) { set_error("rhoc[%d] must be > 0", i); return ILG_ERR_ARG; }
+    k[i] = ti[i] * ti[i] / rhoc[i];
+  }
+  for (int i = 1; i < nz; ++i)
+    if (!(z[i] > z[i - 1])) { set_error("depths must increase (z[%d] <= z[%d])", i, i - 1); return ILG_ERR_ARG; }
+  if (!(z[0] > 0.0)) { set_error("z[0] must be > 0"); return ILG_ERR_ARG; }
+  double dz = 2.0 * z[0];
+  if (bc == 2) {
+    alpha[0] = k[1] * dt / rhoc[0] / (z[1] - z[0]) / z[1];
+    gamma[0] = k[0] * dt / rhoc[0] / z[0] / z[1];
+  } else {
+    double bt = dt / rhoc[0] / (2.0 * dz * dz);
+    alpha[0] = bt * k[1];
+    gamma[0] = bt * k[0];
+  }
+  for (int i = 1; i < nz - 1; ++i) {
+    double buf = dt / (z[i + 1] - z[i - 1]);
+    alpha[i] = 2.0 * k[i + 1] * buf / (rhoc[i] + rhoc[i + 1]) / (z[i + 1] - z[i]);
+    gamma[i] = 2.0 * k[i] * buf / (rhoc[i] + rhoc[i + 1]) / (z[i] - z[i - 1]);
+  }
+  double buf = dt / ((z[nz - 1] - z[nz - 2]) * (z[nz - 1] - z[nz - 2]));
+  gamma[nz - 1] = k[nz - 1] * buf / (2.0 * rhoc[nz - 1]);
+  for (int i = 0; i < nz; ++i) {
+    a[i] = -gamma[i];
+    b[i] = 1.0 + alpha[i] + gamma[i];
+    c[i] = -alpha[i];
+  }
+  b[nz - 1] = 1.0 + gamma[nz - 1];
+  beta[nz - 1] = b[nz - 1];
+  for (int i = nz - 2; i >= 1; --i) {
+    if (beta[i + 1] == 0.0) { set_error("zero pivot in the conduction matrix"); return ILG_ERR_PIVOT; }
+    beta[i] = b[i] - c[i] * a[i + 1] / beta[i + 1];
+  }
+  if (beta[1] == 0.0) { set_error("zero pivot in the conduction matrix"); return ILG_ERR_PIVOT; }
+  tab.assign((size_t)nz * TAB_W, 0.0);
+  for (int i = 0; i < nz; ++i) {
+    double* t = &tab[(size_t)i * TAB_W];
+    t[0] = gamma[i];
+    t[1] = (i == nz - 1) ? 1.0 - gamma[i] : 1.0 - alpha[i] - gamma[i];
+    t[2] = alpha[i];
+    t[3] = (i <= nz - 2) ? c[i] / beta[i + 1] : 0.0;
+    t[4] = (i >= 1) ? 1.0 / beta[i] : 0.0;
+  }
+  cs.alpha0 = alpha[0];
+  cs.gamma0 = gamma[0];
+  cs.k1 = k[0] / dz;
+  cs.f0 = c[0] / beta[1];
+  cs.gamma1 = gamma[1];
+  cs.Ap = (1.0 + alpha[0] + 2.0 * gamma[0]) + cs.f0 * gamma[1];
+  cs.k0 = k[0];
+  cs.z0 = z[0];
+  cs.cgeo = dt / rhoc[nz - 1] * Fgeo / (z[nz - 1] - z[nz - 2]);
+  cs.es = emiss * SIGMA_SB;
+  cs.nz = nz;
+  cs.bc = bc;
+  return ILG_OK;
+}
+
+template <class R>
+int launch_conduct(const R* tab, const CondScalars& cs, int nt, R* T, double* Tsurf, double* Fsurf, double* Qprev,
+                   const double* Qnp1, dbuf<R>& rho_scratch, int upd, double* rad_avg, double* therm_avg,
+                   double* therm_max, const int* frame_ptr, int frame_host, int* derr, cudaStream_t s) {
+  size_t smem = (size_t)cs.nz * COND_THREADS * sizeof(R);
+  int grid = div_up(nt, COND_THREADS);
+  if (smem <= SMEM_LIMIT) {
+    k_conduct<R, true><<<grid, COND_THREADS, smem, s>>>(tab, cs, nt, T, Tsurf, Fsurf, Qprev, Qnp1, nullptr, upd,
+                                                        rad_avg, therm_avg, therm_max, frame_ptr, frame_host, derr);
+  } else {
+    ILG_TRY(rho_scratch.reserve((size_t)cs.nz * nt));
+    k_conduct<R, false><<<grid, COND_THREADS, 0, s>>>(tab, cs, nt, T, Tsurf, Fsurf, Qprev, Qnp1, rho_scratch.p, upd,
+                                                      rad_avg, therm_avg, therm_max, frame_ptr, frame_host, derr);
+  }
+  ILG_CUDA(cudaGetLastError());
+  return ILG_OK;
+}
+
+}  // namespace
+
+// Opt the shared-memory kernels into SMEM_LIMIT bytes (once per process,
+// before any capture).
+int conduction_setup() {
+  static bool done = false;
+  if (done) return ILG_OK;
+  ILG_CUDA(cudaFuncSetAttribute(k_conduct<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_LIMIT));
+  ILG_CUDA(cudaFuncSetAttribute(k_conduct<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_LIMIT));
+  done = true;
+  return ILG_OK;
+}
+
+int conduction_prepare(Context& c, double dt, int precision) {
+  if (!c.have_thermal) { set_error("thermal model not initialised"); return ILG_ERR_ARG; }
+  ILG_TRY(conduction_setup());
+  if (c.coef_dt == dt && c.coef_prec == precision) return ILG_OK;
+  std::vector<double> tab;
+  CondScalars cs;
+  ILG_TRY(build_tables(c.nz, c.z_h.data(), c.ti_h.data(), c.rhoc_h.data(), dt, c.emiss, c.Fgeo, c.bc_mode, tab, cs));
+  if (precision == ILG_PREC_MIXED) {
+    std::vector<float> t32(tab.size());
+    for (size_t i = 0; i < tab.size(); ++i) t32[i] = (float)tab[i];
+    ILG_TRY(c.coef32.alloc(t32.size()));
+    ILG_CUDA(cudaMemcpy(c.coef32.p, t32.data(), t32.size() * 4, cudaMemcpyHostToDevice));
+  } else {
+    ILG_TRY(c.coef64.alloc(tab.size()));
+    ILG_CUDA(cudaMemcpy(c.coef64.p, tab.data(), tab.size() * 8, cudaMemcpyHostToDevice));
+  }
+  c.cond_cs = cs;
+  c.coef_dt = dt;
+  c.coef_prec = precision;
+  return ILG_OK;
+}
+
+// Move the layer state between fp64 and fp32 storage.
+int conduction_state_convert(Context& c, int precision) {
+  if (c.state_prec == precision) return ILG_OK;
+  size_t n = (size_t)c.nz * c.nt;
+  if (precision == ILG_PREC_MIXED) {
+    ILG_TRY(c.T32.alloc(n));
+    k_convert<double, float><<<div_up(n, 256), 256, 0, c.stream>>>(c.T64.p, c.T32.p, n);
+  } else {
+    ILG_TRY(c.T64.alloc(n));
+    k_convert<float, double><<<div_up(n, 256), 256, 0, c.stream>>>(c.T32.p, c.T64.p, n);
+  }
+  ILG_CUDA(cudaGetLastError());
+  c.state_prec = precision;
+  return ILG_OK;
+}
+
+int conduction_launch(Context& c, const double* Q_dev, int precision, bool update_outputs) {
+  const CondScalars& cs = c.cond_cs;
+  ILG_TRY(conduction_state_convert(c, precision));
+  if (precision == ILG_PREC_MIXED)
+    return launch_conduct<float>(c.coef32.p, cs, c.nt, c.T32.p, c.Tsurf.p, c.Fsurf.p, c.Qprev.p, Q_dev, c.rho32,
+                                 update_outputs ? 1 : 0, c.rad_avg.p, c.therm_avg.p, c.therm_max.p,
+                                 c.counters.p + 2, 0, c.derr.p, c.stream);
+  return launch_conduct<double>(c.coef64.p, cs, c.nt, c.T64.p, c.Tsurf.p, c.Fsurf.p, c.Qprev.p, Q_dev, c.rho64,
+                                update_outputs ? 1 : 0, c.rad_avg.p, c.therm_avg.p, c.therm_max.p,
+                                c.counters.p + 2, 0, c.derr.p, c.stream);
+}
+
+// Standalone batched columns (host arrays, reference layout: column-major
+// nz x ncol). Runs on the current device with a private stream.
+static int run_columns(int ncol, int nz, const double* z, double dt, const double* Qn, const double* Qnp1, double* T,
+                       const double* ti, const double* rhoc, double emiss, double* Tsurf, double Fgeo,
+                       double* Fsurf, int bc) {
+  if (ncol <= 0) return ILG_OK;
+  std::vector<double> tab;
+  CondScalars cs;
+  ILG_TRY(build_tables(nz, z, ti, rhoc, dt, emiss, Fgeo, bc, tab, cs));
+  ILG_TRY(conduction_setup());
+  cudaStream_t s;
+  ILG_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  struct StreamGuard { cudaStream_t s; ~StreamGuard() { cudaStreamDestroy(s); } } guard{s};
+  dbuf<double> dtab, dT, dTs, dFs, dQn, dQ;
+  dbuf<int> derr;
+  dbuf<double> rho;
+  ILG_TRY(dtab.alloc(tab.size()));
+  ILG_TRY(dT.alloc((size_t)nz * ncol));
+  ILG_TRY(dTs.alloc(ncol));
+  ILG_TRY(dFs.alloc(ncol));
+  ILG_TRY(dQn.alloc(ncol));
+  ILG_TRY(dQ.alloc(ncol));
+  ILG_TRY(derr.alloc(DERR_COUNT));
+  std::vector<double> Tl((size_t)nz * ncol);
+  for (int f = 0; f < ncol; ++f)
+    for (int i = 0; i < nz; ++i) Tl[(size_t)i * ncol + f] = T[(size_t)f * nz + i];
+  ILG_CUDA(cudaMemcpyAsync(dtab.p, tab.data(), tab.size() * 8, cudaMemcpyHostToDevice, s));
+  ILG_CUDA(cudaMemcpyAsync(dT.p, Tl.data(), Tl.size() * 8, cudaMemcpyHostToDevice, s));
+  ILG_CUDA(cudaMemcpyAsync(dTs.p, Tsurf, (size_t)ncol * 8, cudaMemcpyHostToDevice, s));
+  ILG_CUDA(cudaMemcpyAsync(dQ.p, Qnp1, (size_t)ncol * 8, cudaMemcpyHostToDevice, s));
+  if (Qn) ILG_CUDA(cudaMemcpyAsync(dQn.p, Qn, (size_t)ncol * 8, cudaMemcpyHostToDevice, s));
+  else ILG_CUDA(cudaMemsetAsync(dQn.p, 0, (size_t)ncol * 8, s));
+  ILG_CUDA(cudaMemsetAsync(derr.p, 0, DERR_COUNT * sizeof(int), s));
+  ILG_TRY(launch_conduct<double>(dtab.p, cs, ncol, dT.p, dTs.p, dFs.p, dQn.p, dQ.p, rho, 0, nullptr, nullptr, nullptr,
+                                 nullptr, 0, derr.p, s));
+  int herr[DERR_COUNT];
+  ILG_CUDA(cudaMemcpyAsync(Tl.data(), dT.p, Tl.size() * 8, cudaMemcpyDeviceToHost, s));
+  if (bc != 2) ILG_CUDA(cudaMemcpyAsync(Tsurf, dTs.p, (size_t)ncol * 8, cudaMemcpyDeviceToHost, s));
+  ILG_CUDA(cudaMemcpyAsync(Fsurf, dFs.p, (size_t)ncol * 8, cudaMemcpyDeviceToHost, s));
+  ILG_CUDA(cudaMemcpyAsync(herr, derr.p, sizeof(herr), cudaMemcpyDeviceToHost, s));
+  ILG_CUDA(cudaStreamSynchronize(s));
+  if (herr[DERR_PIVOT]) { set_error("zero pivot in a conduction column"); return ILG_ERR_PIVOT; }
+  for (int f = 0; f < ncol; ++f)
+    for (int i = 0; i < nz; ++i) T[(size_t)f * nz + i] = Tl[(size_t)i * ncol + f];
+  return ILG_OK;
+}
+
+int conduction_batch_host(int ncol, int nz, const double* z, double dt, const double* Qn, const double* Qnp1,
+                          double* T, const double* ti, const double* rhoc, double emiss, double* Tsurf, double Fgeo,
+                          double* Fsurf, int bc_mode) {
+  if (bc_mode != ILG_BC_LINEARISED && bc_mode != ILG_BC_NEWTON) { set_error("bad bc_mode %d", bc_mode); return ILG_ERR_ARG; }
+  return run_columns(ncol, nz, z, dt, Qn, Qnp1, T, ti, rhoc, emiss, Tsurf, Fgeo, Fsurf, bc_mode);
+}
+
+int conductiont_host(int nz, const double* z, double dt, double* T, double Tsurf, double Tsurfp1, const double* ti,
+                     const double* rhoc, double Fgeo, double* Fsurf) {
+  double ts = Tsurf;
+  return run_columns(1, nz, z, dt, nullptr, &Tsurfp1, T, ti, rhoc, 1.0, &ts, Fgeo, Fsurf, 2);
+}
+
+}  // namespace ilg

@@ -1,0 +1,191 @@
+/*
+ * illum_gb300.h — C ABI of the GB300-native illumination + thermal library.
+ *
+ * Each entry point replaces one piece of sampotter/illum's path (paths are
+ * relative to the reference project's root):
+ *
+ *   ilg_ctx_create          illum_context::illum_context(obj_path)
+ *                           (src/cpp/illum.cpp:22-27, src/cpp/illum.hpp:9-10):
+ *                           triangles in, acceleration structure (here an LBVH
+ *                           on the GPU) built.
+ *   ilg_compute_F/_get_F    illum_context::compute_F (src/cpp/illum.cpp:31-237,
+ *                           src/cpp/illum.hpp:18-20)
+ *   ilg_set_F               loading form_factors_file (src/cpp/illum_cli.cpp:385-389)
+ *   ilg_make_horizons       illum_context::make_horizons (src/cpp/illum.cpp:326-363)
+ *   ilg_get/set_horizons    save_horizons / load_horizons (src/cpp/illum.cpp:365-375)
+ *   ilg_direct_radiosity    illum_context::get_direct_radiosity
+ *                           (src/cpp/illum.cpp:382-466)
+ *   ilg_fib_spiral          fib_spiral (src/cpp/illum.cpp:468-483)
+ *   ilg_radiosity_solve     arma_util::forward_solve + the Gauss-Seidel loop
+ *                           (src/cpp/arma_util.cpp:4-17, src/cpp/illum_cli.cpp:425-440)
+ *   ilg_thermal_init/_step/_get
+ *                           thermal_model ctor / step / T, F members
+ *                           (src/cpp/thermal.hpp:17-105)
+ *   ilg_run_steps           the time-step loop of do_radiosity_task
+ *                           (src/cpp/illum_cli.cpp:403-468)
+ *   ilg_trace               BVH::getIntersection (call sites src/cpp/illum.cpp:73,301)
+ *   conductionq_/conductiont_
+ *                           the Fortran subroutines' exact C symbols
+ *                           (src/cpp/conduction.cpp:3-6,17-20)
+ *   ilg_conductionq_batch   many conductionQ columns in one call
+ *
+ * Conventions: every ilg_* function returns ILG_OK (0) or a negative status;
+ * ilg_last_error() gives the message of the calling thread's last failure.
+ * All array arguments are HOST pointers owned by the caller (device state is
+ * owned by the context). Dense matrices use the reference's column-major
+ * (Armadillo) layout. A context is not thread-safe; separate contexts are
+ * independent. Lengths are in the mesh's unit (km by default, as the
+ * reference), temperatures in K, fluxes in W/m^2.
+ */
+#ifndef ILLUM_GB300_H
+#define ILLUM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ILG_OK 0
+#define ILG_ERR_ARG (-1)      /* invalid argument or call order */
+#define ILG_ERR_CUDA (-2)     /* CUDA runtime error */
+#define ILG_ERR_NAN (-3)      /* NaN form factor (reference throws, illum.cpp:121-123) */
+#define ILG_ERR_PIVOT (-4)    /* zero pivot in a tridiagonal solve (tridag.for stops) */
+#define ILG_ERR_NOMEM (-5)    /* device allocation failed */
+#define ILG_ERR_DEVICE (-6)   /* a kernel reported an error (stack overflow, wait limit) */
+#define ILG_ERR_NOTCONV (-7)  /* radiosity did not reach the tolerance in max_sweeps */
+
+typedef struct ilg_ctx ilg_ctx;
+
+/* Precision of the time-step loop. */
+#define ILG_PREC_FP64 0       /* plain method: FP64 radiosity and conduction */
+#define ILG_PREC_MIXED 1      /* BF16 form factors + FP32 conduction, FP64 residual refinement */
+
+/* Surface boundary of the conduction step. */
+#define ILG_BC_LINEARISED 0   /* conductionQ.f:76-82 (one-shot linearisation) */
+#define ILG_BC_NEWTON 1       /* Newton solve of emiss*sigma*Ts^4 at the new time level */
+
+const char* ilg_last_error(void);
+int ilg_version(void);
+
+/* ---- context (illum_context) ------------------------------------------- */
+/* verts: nv x 3 float (row-major xyz); tris: nt x 3 int32 vertex indices;
+ * normals: nt x 3 float face normals, or NULL to use the normalised
+ * (v1-v0)x(v2-v0) of each face. */
+int ilg_ctx_create(const float* verts, int nv, const int32_t* tris, int nt,
+                   const float* normals, ilg_ctx** out);
+int ilg_ctx_destroy(ilg_ctx* ctx);
+int ilg_ctx_num_faces(const ilg_ctx* ctx);
+int ilg_ctx_info(const ilg_ctx* ctx, int64_t* bvh_nodes, int* bvh_depth);
+
+/* ---- closest / any hit (BVH::getIntersection) ----------------------------- */
+/* hit[r] = index of the closest triangle hit by ray r (or the first found
+ * with any_hit != 0), -1 for none; t[r] its ray parameter (may be NULL). */
+int ilg_trace(ilg_ctx* ctx, int nrays, const float* orig, const float* dir, int any_hit,
+              int32_t* hit, double* t);
+
+/* ---- form factors (compute_F) -------------------------------------------- */
+/* Visibility + form factors, rows scaled by albedo (albedo: nt values, or
+ * NULL to use albedo_scalar). Result stays on the device as CSR by receiver
+ * row; *nnz receives its size and *rays the number of visibility rays. */
+int ilg_compute_F(ilg_ctx* ctx, const double* albedo, double albedo_scalar, double offset,
+                  int64_t* nnz, int64_t* rays);
+/* rowptr: nt+1, col: nnz, val: nnz */
+int ilg_get_F(ilg_ctx* ctx, int64_t* rowptr, int32_t* col, double* val);
+int ilg_set_F(ilg_ctx* ctx, int64_t nnz, const int64_t* rowptr, const int32_t* col,
+              const double* val);
+
+/* ---- horizons ----------------------------------------------------------- */
+int ilg_make_horizons(ilg_ctx* ctx, int nphi, double theta_eps, double offset);
+/* out: nphi x nt column-major (nphi zenith angles per facet) */
+int ilg_get_horizons(ilg_ctx* ctx, double* out);
+int ilg_set_horizons(ilg_ctx* ctx, int nphi, const double* h);
+
+/* ---- direct insolation -------------------------------------------------- */
+/* Insolation options: norm_mode 0 divides the lit count by nphi - 1 as the
+ * reference does (illum.cpp:441), 1 by the number of samples used;
+ * interp 0 keeps the reference's threshold h[k] + t*dphi (illum.cpp:434),
+ * 1 interpolates h[k]..h[k+1]; solar_const is the flux at 1 AU
+ * (1372 in illum.cpp:451). */
+int ilg_set_insolation(ilg_ctx* ctx, int norm_mode, int interp, double solar_const);
+void ilg_fib_spiral(double* xy /* n x 2 column-major */, int n);
+/* sun: 3 doubles (km); disk_xy: ndisk x 2 column-major (ndisk-1 samples
+ * used); out: nt doubles. */
+int ilg_direct_radiosity(ilg_ctx* ctx, const double* sun, const double* disk_xy, int ndisk,
+                         double* out);
+
+/* ---- radiosity ---------------------------------------------------------- */
+/* Solves (I - F) x = E for the context's F to ||(I-F)x - E||_2 <= tol
+ * (at most max_sweeps sweeps). x: nt doubles out; *res the residual bound
+ * and *sweeps the sweeps used (either may be NULL). */
+int ilg_radiosity_solve(ilg_ctx* ctx, const double* E, double tol, int max_sweeps, double* x,
+                        double* res, int* sweeps);
+
+/* ---- thermal model -------------------------------------------------------- */
+/* z, ti, rhoc: nz per-layer values (the reference shares one profile across
+ * facets, thermal.hpp:23-42); T0: uniform start temperature, or T0_full
+ * ((nz+1) x nt column-major, row 0 = surface) when non-NULL. */
+int ilg_thermal_init(ilg_ctx* ctx, int nz, const double* z, const double* ti, const double* rhoc,
+                     double T0, const double* T0_full, double emissivity, double Fgeotherm,
+                     int bc_mode, int precision);
+/* thermal_model::step(dt, Q): Q is nt doubles (host). */
+int ilg_thermal_step(ilg_ctx* ctx, double dt, const double* Q);
+/* T: (nz+1) x nt column-major (row 0 = surface temperature); Fsurf, Qprev: nt.
+ * Any pointer may be NULL. */
+int ilg_thermal_get(ilg_ctx* ctx, double* T, double* Fsurf, double* Qprev);
+
+/* ---- fused time-step loop (do_radiosity_task's step lambda) ---------------- */
+/* Run-level options for ilg_run_steps. */
+typedef struct ilg_run_opts {
+  double dt;               /* s */
+  double tol;              /* radiosity tolerance (2-norm of the residual) */
+  int max_sweeps;          /* radiosity sweep limit */
+  int use_radiosity;       /* 0: rad = E (no F) */
+  int use_graph;           /* capture the step in a CUDA graph */
+  int precision;           /* ILG_PREC_FP64 / ILG_PREC_MIXED */
+} ilg_run_opts;
+
+/* Upload sun positions (nsun x 3, row-major, km) kept on the device for
+ * ilg_run_steps; disk_xy as in ilg_direct_radiosity. */
+int ilg_set_suns(ilg_ctx* ctx, int nsun, const double* suns, const double* disk_xy, int ndisk);
+/* Advance nsteps steps using device-resident sun positions starting at
+ * index first_sun. tsurf_out: nsteps x nt host array (NULL: none) receiving
+ * the surface temperature after every step. */
+int ilg_run_steps(ilg_ctx* ctx, const ilg_run_opts* opts, int first_sun, int nsteps,
+                  double* tsurf_out);
+/* Same, with the sun position of each step passed from the host: suns is
+ * nsteps x 3. */
+int ilg_run_steps_host(ilg_ctx* ctx, const ilg_run_opts* opts, int nsteps, const double* suns,
+                       double* tsurf_out);
+/* rad, rad_avg, therm_avg, therm_max: nt doubles each (any may be NULL). */
+int ilg_get_outputs(ilg_ctx* ctx, double* rad, double* rad_avg, double* therm_avg,
+                    double* therm_max);
+/* Per-phase device times (ms) of the last ilg_run_steps call with timing
+ * enabled, and per-call counters. */
+int ilg_set_timing(ilg_ctx* ctx, int enable);
+int ilg_get_stats(ilg_ctx* ctx, double* ms_direct, double* ms_radiosity, double* ms_conduction,
+                  int64_t* ambiguous_facets, int64_t* radiosity_sweeps);
+
+/* ---- conduction (Fortran ABI) -------------------------------------------- */
+/* Exact symbols of conductionQ.f / conductionT.f as the reference's C++
+ * wrapper declares them (conduction.cpp:3-6,17-20). Each runs one column on
+ * the GPU; errors are reported on stderr (the Fortran has no status). */
+void conductionq_(int* nz, const double z[], double* dt, double* Qn, double* Qnp1, double T[],
+                  const double ti[], const double rhoc[], double* emiss, double* Tsurf,
+                  double* Fgeotherm, double* Fsurf);
+void conductiont_(int* nz, const double z[], double* dt, double T[], double* Tsurf,
+                  double* Tsurfp1, const double ti[], const double rhoc[], double* Fgeotherm,
+                  double* Fsurf);
+/* ncol columns sharing z/ti/rhoc: T is nz x ncol column-major (each column's
+ * nz layer temperatures contiguous); Qn, Qnp1, Tsurf, Fsurf are ncol values.
+ * bc_mode as in ilg_thermal_init (Qn unused for ILG_BC_NEWTON). */
+int ilg_conductionq_batch(int ncol, int nz, const double* z, double dt, const double* Qn,
+                          const double* Qnp1, double* T, const double* ti, const double* rhoc,
+                          double emiss, double* Tsurf, double Fgeotherm, double* Fsurf,
+                          int bc_mode);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ILLUM_GB300_H */

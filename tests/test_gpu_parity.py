@@ -1,0 +1,330 @@
+"""GPU parity: every CUDA path through the C ABI against the CPU oracle.
+
+Exactness bars: ray hits, horizons, visibility sets, form-factor values and
+direct insolation are compared bit for bit; radiosity to the solve
+tolerance; temperatures of the FP64 path to 1e-9 K; the mixed-precision path
+to 0.05 K.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from illum_gb300 import meshgen
+
+pytestmark = pytest.mark.gpu
+
+TOL_T_FP64 = 1e-9      # K
+TOL_T_MIXED = 0.05     # K
+
+
+@pytest.fixture(scope="module")
+def mesh_l4():
+    return meshgen.icosphere_craters(4, seed=0)          # 5,120 facets (the CPU-runnable configuration)
+
+
+@pytest.fixture(scope="module")
+def mesh_l3():
+    return meshgen.icosphere_craters(3, seed=3, n_craters=12, dmin_m=150.0, dmax_m=450.0)
+
+
+def _rays(oracle_mod, v, f, n, seed):
+    c, nn, r, a = oracle_mod.facet_geometry(v, f)
+    rng = np.random.default_rng(seed)
+    idx = rng.integers(0, len(f), n)
+    o = (c[idx] + 1e-5 * nn[idx]).astype(np.float32)
+    d = rng.normal(size=(n, 3))
+    d = (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(np.float32)
+    return o, d
+
+
+def test_trace_bit_exact(ilg, oracle_mod, mesh_l3):
+    v, f = mesh_l3
+    ctx = ilg.IllumContext(v, f)
+    o, d = _rays(oracle_mod, v, f, 20000, 1)
+    hg, tg = ctx.trace(o, d)
+    ho, to = oracle_mod.trace(v, f, o, d)
+    assert np.array_equal(hg, ho)
+    assert np.array_equal(tg[hg >= 0], to[ho >= 0])
+    ag, _ = ctx.trace(o, d, any_hit=True)
+    ao, _ = oracle_mod.trace(v, f, o, d, any_hit=True)
+    assert np.array_equal(ag >= 0, ao >= 0)
+
+
+def test_trace_grazing_rays_bit_exact(ilg, oracle_mod, mesh_l3):
+    """Rays aimed at triangle vertices and edge midpoints (where the float
+    filter must defer to the double-precision predicate)."""
+    v, f = mesh_l3
+    ctx = ilg.IllumContext(v, f)
+    rng = np.random.default_rng(7)
+    tgt_f = rng.integers(0, len(f), 4000)
+    w = rng.integers(0, 3, 4000)
+    tv = v[f[tgt_f, w]].astype(np.float64)
+    tv2 = v[f[tgt_f, (w + 1) % 3]].astype(np.float64)
+    tgt = np.where((np.arange(4000) % 2 == 0)[:, None], tv, 0.5 * (tv + tv2))
+    src = rng.normal(size=(4000, 3))
+    src = 2.0 * src / np.linalg.norm(src, axis=1, keepdims=True)
+    d = tgt - src
+    d = (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(np.float32)
+    o = src.astype(np.float32)
+    hg, tg = ctx.trace(o, d)
+    ho, to = oracle_mod.trace(v, f, o, d, brute=True)
+    assert np.array_equal(hg, ho)
+    assert np.array_equal(tg[hg >= 0], to[ho >= 0])
+
+
+def test_horizons_bit_exact(ilg, oracle_mod, mesh_l4):
+    v, f = mesh_l4
+    ctx = ilg.IllumContext(v, f)
+    ctx.make_horizons(nphi=32, theta_eps=1e-3, offset=1e-5)
+    Hg = ctx.horizons
+    Ho = oracle_mod.horizons(v, f, 32, 1e-3, 1e-5).T
+    assert Hg.shape == (32, f.shape[0])
+    assert np.array_equal(Hg, Ho)
+
+
+def test_horizons_other_eps_bit_exact(ilg, oracle_mod, mesh_l3):
+    v, f = mesh_l3
+    ctx = ilg.IllumContext(v, f)
+    for nphi, eps in ((9, 1e-2), (17, 3e-4)):
+        ctx.make_horizons(nphi=nphi, theta_eps=eps)
+        assert np.array_equal(ctx.horizons, oracle_mod.horizons(v, f, nphi, eps).T)
+
+
+def test_form_factors_bit_exact(ilg, oracle_mod, mesh_l4):
+    v, f = mesh_l4
+    ctx = ilg.IllumContext(v, f)
+    rowptr, col, val = ctx.compute_F(albedo=0.1)
+    ro, co, vo, rays = oracle_mod.form_factors(v, f, albedo_scalar=0.1)
+    rp, c, x = oracle_mod.coo_to_csr(f.shape[0], ro, co, vo)
+    assert ctx.visibility_rays == rays
+    assert np.array_equal(rowptr, rp) and np.array_equal(col, c) and np.array_equal(val, x)
+
+
+def test_form_factors_per_facet_albedo(ilg, oracle_mod, mesh_l3):
+    v, f = mesh_l3
+    alb = np.random.default_rng(2).uniform(0.05, 0.3, f.shape[0])
+    ctx = ilg.IllumContext(v, f)
+    rowptr, col, val = ctx.compute_F(albedo=alb)
+    ro, co, vo, _ = oracle_mod.form_factors(v, f, albedo=alb)
+    rp, c, x = oracle_mod.coo_to_csr(f.shape[0], ro, co, vo)
+    assert np.array_equal(rowptr, rp) and np.array_equal(col, c) and np.array_equal(val, x)
+
+
+@pytest.mark.parametrize("norm_mode,interp", [(0, 0), (1, 0), (1, 1)])
+def test_direct_bit_exact(ilg, oracle_mod, mesh_l4, norm_mode, interp):
+    v, f = mesh_l4
+    ctx = ilg.IllumContext(v, f)
+    ctx.make_horizons(nphi=32)
+    H = ctx.horizons
+    ctx.set_insolation(norm_mode, interp, 1361.0)
+    disk = ilg.fib_spiral(100)
+    suns = meshgen.spin_sun_positions(24, 6 * 3600.0, 900.0)
+    for s in suns:
+        dg = ctx.get_direct_radiosity(s, disk)
+        do, _ = oracle_mod.direct(v, f, H.T, s, disk, norm_mode, interp, 1361.0)
+        assert np.array_equal(dg, do)
+
+
+def test_radiosity_converges_to_oracle(ilg, oracle_mod, mesh_l4):
+    v, f = mesh_l4
+    n = f.shape[0]
+    ctx = ilg.IllumContext(v, f)
+    rowptr, col, val = ctx.compute_F(albedo=0.1)
+    E = np.random.default_rng(3).uniform(0, 600, n)
+    x, res, sweeps = ctx.radiosity_solve(E, tol=1e-10, max_sweeps=200)
+    xo, reso, _ = oracle_mod.gauss_seidel(rowptr, col, val, E, mode=1, tol=1e-12)
+    assert res <= 1e-10 and sweeps >= 1
+    assert np.abs(x - xo).max() <= 1e-10
+    # residual computed independently
+    A_x = x.copy()
+    for i in range(n):
+        A_x[i] -= val[rowptr[i]:rowptr[i + 1]] @ x[col[rowptr[i]:rowptr[i + 1]]]
+    assert np.linalg.norm(A_x - E) <= 1e-10
+
+
+def test_set_F_round_trip(ilg, oracle_mod, mesh_l3):
+    v, f = mesh_l3
+    ctx = ilg.IllumContext(v, f)
+    rp, c, x = ctx.compute_F(albedo=0.1)
+    ctx2 = ilg.IllumContext(v, f)
+    ctx2.set_F(rp, c, x)
+    E = np.linspace(0, 500, f.shape[0])
+    a, _, _ = ctx.radiosity_solve(E)
+    b, _, _ = ctx2.radiosity_solve(E)
+    assert np.array_equal(a, b)
+
+
+# ------------------------------------------------------------ conduction
+def _profile(nz):
+    return meshgen.geometric_depths(nz), np.full(nz, 300.0), np.full(nz, 1.05e6)
+
+
+@pytest.mark.parametrize("bc_mode", [0, 1])
+def test_conduction_batch_vs_oracle(ilg, oracle_mod, bc_mode):
+    nz, ncol = 40, 777
+    z, ti, rhoc = _profile(nz)
+    rng = np.random.default_rng(4)
+    T = rng.uniform(180, 320, (nz, ncol))
+    Ts = rng.uniform(180, 320, ncol)
+    Qn = rng.uniform(0, 800, ncol)
+    Qp = rng.uniform(0, 800, ncol)
+    Tg, Tsg, Fsg = ilg.conductionQ_batch(z, 30.0, Qn, Qp, T, ti, rhoc, 0.95, Ts, bc_mode=bc_mode)
+    for k in range(ncol):
+        if bc_mode == 0:
+            To, tso, fso = oracle_mod.conductionq(z, 30.0, Qn[k], Qp[k], T[:, k], ti, rhoc, 0.95, Ts[k])
+        else:
+            To, tso, fso, _ = oracle_mod.conductionq_newton(z, 30.0, Qp[k], T[:, k], ti, rhoc, 0.95, Ts[k])
+        assert np.abs(Tg[:, k] - To).max() <= 1e-9
+        assert abs(Tsg[k] - tso) <= 1e-9
+        assert abs(Fsg[k] - fso) <= 1e-9 * max(1.0, abs(fso))
+
+
+def test_fortran_abi_symbols(ilg, oracle_mod):
+    """conductionq_ / conductiont_ with the reference's exact signatures."""
+    z, ti, rhoc = _profile(25)
+    T = np.linspace(260, 210, 25)
+    Tg, tsg, fsg = ilg.conductionQ(z, 60.0, 100.0, 450.0, T, ti, rhoc, 0.999, 255.0)
+    To, tso, fso = oracle_mod.conductionq(z, 60.0, 100.0, 450.0, T, ti, rhoc, 0.999, 255.0)
+    assert np.abs(Tg - To).max() <= 1e-9 and abs(tsg - tso) <= 1e-9
+    Tg2, fg2 = ilg.conductionT(z, 60.0, T, 255.0, 270.0, ti, rhoc)
+    To2, fo2 = oracle_mod.conductiont(z, 60.0, T, 255.0, 270.0, ti, rhoc)
+    assert np.abs(Tg2 - To2).max() <= 1e-9 and abs(fg2 - fo2) <= 1e-9 * max(1, abs(fo2))
+
+
+def test_thermal_model_step_vs_oracle(ilg, oracle_mod, mesh_l3):
+    v, f = mesh_l3
+    n = f.shape[0]
+    ctx = ilg.IllumContext(v, f)
+    z, ti, rhoc = _profile(30)
+    tm = ilg.ThermalModel(ctx, z, 300.0, 1.05e6, 233.0)
+    T = np.full((n, 31), 233.0)
+    Qprev = np.zeros(n)
+    Fs = np.zeros(n)
+    rng = np.random.default_rng(5)
+    for step in range(5):
+        Q = rng.uniform(0, 700, n)
+        tm.step(600.0, Q)
+        for k in range(n):
+            T[k, 1:], T[k, 0], Fs[k] = oracle_mod.conductionq(z, 600.0, Qprev[k], Q[k], T[k, 1:], ti, rhoc, 0.999,
+                                                              T[k, 0])
+        Qprev = Q
+    assert np.abs(tm.T - T.T).max() <= TOL_T_FP64
+    assert np.abs(tm.get_radiosity() + Fs).max() <= 1e-9 * max(1, np.abs(Fs).max())
+
+
+# ------------------------------------------------------------ fused loop
+def _setup_run(ilg, oracle_mod, v, f, nphi, nz, nsteps, period=6 * 3600.0, steps_per_rot=360, use_graph=1,
+               precision=0, bc_mode=1):
+    ctx = ilg.IllumContext(v, f)
+    ctx.make_horizons(nphi=nphi)
+    ctx.set_insolation(1, 0, 1361.0)
+    rp, c, x = ctx.compute_F(albedo=0.1)
+    dt = period / steps_per_rot
+    suns = meshgen.spin_sun_positions(nsteps, period, dt)
+    disk = ilg.fib_spiral(100)
+    ctx.set_suns(suns, disk)
+    z, ti, rhoc = _profile(nz)
+    tm = ilg.ThermalModel(ctx, z, 300.0, 1.05e6, 200.0, emissivity=0.95, bc_mode=bc_mode, precision=precision)
+    opts = ilg.RunOpts(dt=dt, tol=1e-10, max_sweeps=200, use_radiosity=1, use_graph=use_graph, precision=precision)
+    return ctx, tm, opts, (rp, c, x), suns, disk, (z, ti, rhoc), dt
+
+
+def test_run_steps_vs_oracle_fp64(ilg, oracle_mod, mesh_l4):
+    """C0-shaped run (L4, 32 azimuths, 40 layers, Newton boundary, radiosity
+    to 1e-10): surface and subsurface temperatures within 1e-9 K."""
+    v, f = mesh_l4
+    nsteps = 120
+    ctx, tm, opts, csr, suns, disk, (z, ti, rhoc), dt = _setup_run(ilg, oracle_mod, v, f, 32, 40, nsteps)
+    hist = ctx.run_steps(opts, 0, nsteps, record_tsurf=True)
+    st = oracle_mod.thermal_run(v, f, ctx.horizons.T, suns, disk, csr, z, ti, rhoc, dt=dt, T0=200.0, emiss=0.95,
+                                solar_const=1361.0, norm_mode=1, bc_mode=1, rad_mode=1, tol=1e-10,
+                                record_tsurf=True)
+    assert np.abs(hist - st["tsurf_hist"]).max() <= TOL_T_FP64
+    assert np.abs(tm.T - st["T"].T).max() <= TOL_T_FP64
+    out = ctx.outputs()
+    assert np.abs(out["therm_avg"] - st["therm_avg"]).max() <= TOL_T_FP64
+    assert np.abs(out["rad_avg"] - st["rad_avg"]).max() <= 1e-8
+
+
+def test_run_steps_reference_boundary(ilg, oracle_mod, mesh_l3):
+    v, f = mesh_l3
+    nsteps = 60
+    ctx, tm, opts, csr, suns, disk, (z, ti, rhoc), dt = _setup_run(ilg, oracle_mod, v, f, 16, 30, nsteps, bc_mode=0)
+    ctx.run_steps(opts, 0, nsteps)
+    st = oracle_mod.thermal_run(v, f, ctx.horizons.T, suns, disk, csr, z, ti, rhoc, dt=dt, T0=200.0, emiss=0.95,
+                                solar_const=1361.0, norm_mode=1, bc_mode=0, rad_mode=1, tol=1e-10)
+    assert np.abs(tm.T - st["T"].T).max() <= TOL_T_FP64
+
+
+def test_graph_equals_eager_and_host_driven(ilg, oracle_mod, mesh_l3):
+    v, f = mesh_l3
+    runs = []
+    for mode in ("graph", "eager", "host"):
+        ctx, tm, opts, csr, suns, disk, _, _ = _setup_run(ilg, oracle_mod, v, f, 16, 30, 40,
+                                                          use_graph=0 if mode == "eager" else 1)
+        if mode == "host":
+            h = ctx.run_steps_host(opts, suns)
+        else:
+            h = ctx.run_steps(opts, 0, 40, record_tsurf=True)
+        runs.append((h, tm.T))
+    for h, T in runs[1:]:
+        assert np.array_equal(h, runs[0][0]) and np.array_equal(T, runs[0][1])
+
+
+def test_split_runs_equal_one_run(ilg, oracle_mod, mesh_l3):
+    v, f = mesh_l3
+    a = _setup_run(ilg, oracle_mod, v, f, 16, 30, 30)
+    a[0].run_steps(a[2], 0, 30)
+    b = _setup_run(ilg, oracle_mod, v, f, 16, 30, 30)
+    b[0].run_steps(b[2], 0, 10)
+    b[0].run_steps(b[2], 10, 20)
+    assert np.array_equal(a[1].T, b[1].T)
+
+
+def test_mixed_precision_within_tolerance(ilg, oracle_mod, mesh_l4):
+    v, f = mesh_l4
+    nsteps = 360
+    ref = _setup_run(ilg, oracle_mod, v, f, 32, 40, nsteps, precision=0)
+    mix = _setup_run(ilg, oracle_mod, v, f, 32, 40, nsteps, precision=1)
+    ha = ref[0].run_steps(ref[2], 0, nsteps, record_tsurf=True)
+    hb = mix[0].run_steps(mix[2], 0, nsteps, record_tsurf=True)
+    err_s = np.abs(ha - hb).max()
+    err_t = np.abs(ref[1].T - mix[1].T).max()
+    assert err_s <= TOL_T_MIXED and err_t <= TOL_T_MIXED, (err_s, err_t)
+
+
+# ------------------------------------------------------------ edge cases
+def test_single_triangle_and_no_form_factors(ilg, oracle_mod):
+    v = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32)
+    f = np.array([[0, 1, 2]], np.int32)
+    ctx = ilg.IllumContext(v, f)
+    rp, c, x = ctx.compute_F(albedo=0.1)
+    assert rp.tolist() == [0, 0] and len(x) == 0
+    ctx.make_horizons(nphi=8)
+    assert np.array_equal(ctx.horizons, oracle_mod.horizons(v, f, 8).T)
+    E = np.array([5.0])
+    xs, res, sw = ctx.radiosity_solve(E)
+    assert xs.tolist() == [5.0]
+
+
+def test_convex_sphere_has_empty_F(ilg, oracle_mod):
+    v, f = meshgen.icosphere_craters(3, 0, n_craters=0, sigma_m=0.0)
+    ctx = ilg.IllumContext(v, f)
+    rp, c, x = ctx.compute_F()
+    ro, co, vo, rays = oracle_mod.form_factors(v, f)
+    assert len(x) == len(vo) == 0 and ctx.visibility_rays == rays
+
+
+def test_errors_are_reported(ilg):
+    v = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32)
+    with pytest.raises(ilg.IlgError):
+        ilg.IllumContext(v, np.array([[0, 1, 5]], np.int32))
+    ctx = ilg.IllumContext(v, np.array([[0, 1, 2]], np.int32))
+    with pytest.raises(ilg.IlgError):
+        ctx.make_horizons(nphi=1)
+    with pytest.raises(ilg.IlgError):
+        ctx.radiosity_solve(np.zeros(1))        # no form factors yet
+    with pytest.raises(ilg.IlgError):
+        ilg.conductionQ_batch(np.array([0.1]), 1.0, None, np.zeros(1), np.zeros((1, 1)), np.ones(1), np.ones(1),
+                              1.0, np.zeros(1))   # nz < 2
