@@ -1,0 +1,331 @@
+"""Benchmark of the illumination + thermal time-step loop on one GB300.
+
+Workload (default): icosphere level 6 (81,920 facets), seed 1, 200 craters
+of 30-300 m on a 1 km body, 64 horizon azimuths, form factors with albedo
+0.1, radiosity to 1e-10, 60-layer conduction column (geometric 1.1 to 0.5 m,
+thermal inertia 300, rho*c 1.05e6, emissivity 0.95, Newton surface
+boundary), sun 1361 W/m^2 at 1.5 AU, spin period 6 h, sub-solar latitude
+10 deg, 720 steps per rotation (dt = 30 s). Synthetic seeded mesh (the
+reference's shape models are not distributed).
+
+A step = direct insolation + radiosity solve + conduction for all facets
+(src/cpp/illum_cli.cpp:403-456). value = facet-steps/s of the plain FP64
+path with device-resident inputs, device time of each step measured with
+CUDA events on the library's stream, L2 (129 MB) flushed by a 256 MB write
+before every step. e2e = the same metric through ilg_run_steps_host: the
+step's sun position copied host->device and the surface temperatures copied
+device->host every step, host wall clock.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+N > 1 runs independent replicas (one process per GPU; the path has no
+cross-GPU exchange): value is the sum over ranks of facets*steps divided by
+the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "facet-steps/s at <=0.05 K max err vs FP64; visibility rays/s; serve p50/p99 ms"
+UNIT = "facet-steps/s"
+
+CFG = dict(level=6, seed=1, n_craters=200, dmin_m=30.0, dmax_m=300.0, nphi=64, theta_eps=1e-3, offset=1e-5,
+           albedo=0.1, nz=60, ti=300.0, rhoc=1500.0 * 700.0, emiss=0.95, T0=200.0, solar=1361.0, dist_au=1.5,
+           period_s=6 * 3600.0, steps_per_rot=720, rotations=10, tol=1e-10, lat_deg=10.0)
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=2)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1])); mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def build_workload(ig, meshgen, precision=0):
+    c = CFG
+    v, f = meshgen.icosphere_craters(c["level"], c["seed"], n_craters=c["n_craters"], dmin_m=c["dmin_m"],
+                                     dmax_m=c["dmax_m"])
+    t0 = time.perf_counter()
+    ctx = ig.IllumContext(v, f)
+    t_bvh = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    ctx.make_horizons(nphi=c["nphi"], theta_eps=c["theta_eps"], offset=c["offset"])
+    t_hor = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    csr = ctx.compute_F(albedo=c["albedo"], offset=c["offset"])
+    t_ff = time.perf_counter() - t0
+    ctx.set_insolation(1, 0, c["solar"])
+    dt = c["period_s"] / c["steps_per_rot"]
+    nsun = c["steps_per_rot"] * c["rotations"]
+    suns = meshgen.spin_sun_positions(nsun, c["period_s"], dt, c["lat_deg"], c["dist_au"])
+    disk = ig.fib_spiral(100)
+    ctx.set_suns(suns, disk)
+    z = meshgen.geometric_depths(c["nz"])
+    tm = ig.ThermalModel(ctx, z, c["ti"], c["rhoc"], c["T0"], emissivity=c["emiss"], bc_mode=ig.BC_NEWTON,
+                         precision=precision)
+    setup = {"bvh_s": t_bvh, "horizons_s": t_hor, "form_factors_s": t_ff,
+             "horizon_rays": int(f.shape[0] * c["nphi"] * 11), "visibility_rays": int(ctx.visibility_rays),
+             "nnz": int(ctx.nnz)}
+    return dict(v=v, f=f, ctx=ctx, tm=tm, csr=csr, suns=suns, disk=disk, z=z, dt=dt, nsun=nsun, setup=setup)
+
+
+def run_chunks(fn, first, n, nsun):
+    """Call fn(first_sun, count) over [first, first+n) wrapping the sun table."""
+    out = []
+    s = first % nsun
+    left = n
+    while left > 0:
+        k = min(left, nsun - s)
+        out.append(fn(s, k))
+        left -= k
+        s = (s + k) % nsun
+    return out
+
+
+def cpu_baseline(W, steps, threads):
+    """The CPU oracle (a restatement of the reference path; the reference
+    itself cannot be built here) on the host cores: a bounded sample of
+    time steps of the same workload."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.set_threads(threads)
+    c = CFG
+    H = W["ctx"].horizons.T
+    z = W["z"]
+    nz = len(z)
+    t0 = time.perf_counter()
+    O.thermal_run(W["v"], W["f"], H, W["suns"][:steps], W["disk"], W["csr"], z, np.full(nz, c["ti"]),
+                  np.full(nz, c["rhoc"]), dt=W["dt"], T0=c["T0"], emiss=c["emiss"], solar_const=c["solar"],
+                  norm_mode=1, bc_mode=1, rad_mode=1, tol=c["tol"])
+    el = time.perf_counter() - t0
+    return W["f"].shape[0] * steps / el, el
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1440)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-steps", type=int, default=12)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
+
+    import __graft_entry__
+    __graft_entry__.build()
+    import illum_gb300 as ig
+    from illum_gb300 import meshgen
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        threads = os.cpu_count() or 1
+        W = build_workload(ig, meshgen)
+        per = []
+        for _ in range(args.warmup):
+            pass
+        for _ in range(max(1, args.steps if args.steps <= 50 else 3)):
+            v, el = cpu_baseline(W, args.cpu_steps, threads)
+            per.append(el)
+        value = W["f"].shape[0] * args.cpu_steps * len(per) / sum(per)
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": len(per),
+                "warmup": 0, "ms_per_step": 1000.0 * sum(per) / (len(per) * args.cpu_steps),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic", "impl": "reference",
+                "config": {"workload": "icosphere L6 81,920 facets, 200 craters, nphi 64, nz 60, dt 30 s, "
+                                       "radiosity tol 1e-10, Newton boundary (C1)", "facets": int(W["f"].shape[0])},
+                "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                                 "sample": f"{len(per)} x {args.cpu_steps} time steps of the workload"},
+                "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    W = build_workload(ig, meshgen)
+    ctx = W["ctx"]
+    N = W["f"].shape[0]
+    nsun = W["nsun"]
+    c = CFG
+    opts = ig.RunOpts(dt=W["dt"], tol=c["tol"], max_sweeps=200, use_radiosity=1, use_graph=1,
+                      precision=ig.PREC_FP64)
+    # warm-up (graph capture included)
+    run_chunks(lambda s, k: ctx.bench_steps(opts, s, k, 256.0), 0, args.warmup, nsun)
+    sun_pos = args.warmup
+    if dist is not None:
+        dist.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    res = run_chunks(lambda s, k: ctx.bench_steps(opts, s, k, 256.0), sun_pos, args.steps, nsun)
+    step_ms = np.concatenate([r[0] for r in res])
+    sun_pos += args.steps
+    clk = clocks.stop()
+    total_ms = float(step_ms.sum())
+    if dist is not None:
+        import torch
+        t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * N * args.steps / (total_ms / 1000.0)
+
+    # per-phase breakdown (eager launches with events between phases)
+    eager = ig.RunOpts(dt=W["dt"], tol=c["tol"], max_sweeps=200, use_radiosity=1, use_graph=0,
+                       precision=ig.PREC_FP64)
+    ctx.set_timing(True)
+    nph = min(args.steps, 720)
+    res = run_chunks(lambda s, k: ctx.bench_steps(eager, s, k, 256.0), sun_pos, nph, nsun)
+    sun_pos += nph
+    ph = {k: sum(r[1][k] for r in res) / nph for k in ("direct", "radiosity", "conduction")}
+    st = ctx.stats()
+    ctx.set_timing(False)
+    sweeps_per_step = st["radiosity_sweeps"] / nph
+    amb_per_step = st["ambiguous_facets"] / nph
+    nz = c["nz"]
+    peak, peak_kind = _peaks()
+    bytes_cond = N * (2 * nz * 8 + 6 * 8)
+    nnz = W["setup"]["nnz"]
+    bytes_rad = sweeps_per_step * (nnz * (8 + 4) + N * (4 + 8 + 8 + 8))
+    kern = {"conduction": (bytes_cond, ph["conduction"]), "radiosity": (bytes_rad, ph["radiosity"])}
+    dom = max(kern, key=lambda k: kern[k][1])
+    b, ms = kern[dom]
+    achieved = b / (ms / 1000.0) / 1e9
+    roofline = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+                "algorithmic_bytes": b, "avg_ms": ms}
+
+    # mixed precision on a second context from the same initial state
+    mixed = None
+    try:
+        Wm = build_workload(ig, meshgen, precision=ig.PREC_MIXED)
+        Wf = build_workload(ig, meshgen, precision=ig.PREC_FP64)
+        mopts = ig.RunOpts(dt=W["dt"], tol=c["tol"], max_sweeps=200, use_radiosity=1, use_graph=1,
+                           precision=ig.PREC_MIXED)
+        nchk = 720
+        Wf["ctx"].run_steps(opts, 0, nchk)
+        mres = Wm["ctx"].bench_steps(mopts, 0, nchk, 256.0)
+        err = float(np.abs(Wf["tm"].T - Wm["tm"].T).max())
+        mval = N * nchk / (mres[0].sum() / 1000.0)
+        mixed = {"value": mval, "unit": UNIT, "steps": nchk, "max_err_K": err, "speedup_vs_fp64": mval / value * world}
+        del Wm, Wf
+    except Exception as e:  # reported, not hidden
+        mixed = {"error": str(e)}
+
+    e2e = None
+    if not args.no_e2e:
+        nE = min(args.steps, 720)
+        suns = np.array([W["suns"][(sun_pos + i) % nsun] for i in range(nE)])
+        out = np.zeros(N)
+        t_tot = 0.0
+        for i in range(nE):
+            t0 = time.perf_counter()
+            o = ctx.run_steps_host(opts, suns[i:i + 1], record_tsurf=True)
+            t_tot += time.perf_counter() - t0
+            out += o[0]
+        e2e = {"value": world * N * nE / t_tot, "unit": UNIT, "h2d_bytes_per_step": 56,
+               "d2h_bytes_per_step": 8 * N, "steps": nE, "note": "ilg_run_steps_host per step, host wall clock"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        cv, el = cpu_baseline(W, args.cpu_steps, threads)
+        cpu = {"value": cv, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{args.cpu_steps} time steps of the workload ({el:.1f} s); direct insolation threaded, "
+                         f"Gauss-Seidel and conduction serial as in the reference"}
+    su = W["setup"]
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": "icosphere L6 81,920 facets, 200 craters 30-300 m, nphi 64, nz 60, "
+                                       "dt 30 s, radiosity tol 1e-10, Newton boundary (C1, plain FP64 path)",
+                           "facets": N, "nnz": nnz, "l2": "256 MB flush before every timed step",
+                           "parallelism": f"replicas x{world}"},
+                "e2e": e2e, "gpu_launches": 5 * args.steps, "roofline": roofline, "cpu_baseline": cpu,
+                "clocks": clk,
+                "phases_ms_per_step": ph, "radiosity_sweeps_per_step": sweeps_per_step,
+                "ambiguous_facets_per_step": amb_per_step,
+                "visibility_rays_per_s": su["visibility_rays"] / su["form_factors_s"],
+                "horizon_rays_per_s": su["horizon_rays"] / su["horizons_s"],
+                "setup_s": {k: su[k] for k in ("bvh_s", "horizons_s", "form_factors_s")},
+                "mixed": mixed}
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -75,6 +75,8 @@ _SIGS = {
     "ilg_set_suns": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int]),
     "ilg_run_steps": (C.c_int, [C.c_void_p, C.POINTER(RunOpts), C.c_int, C.c_int, C.c_void_p]),
     "ilg_run_steps_host": (C.c_int, [C.c_void_p, C.POINTER(RunOpts), C.c_int, C.c_void_p, C.c_void_p]),
+    "ilg_bench_steps": (C.c_int, [C.c_void_p, C.POINTER(RunOpts), C.c_int, C.c_int, C.c_double, C.c_void_p,
+                                  C.c_void_p]),
     "ilg_get_outputs": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "ilg_set_timing": (C.c_int, [C.c_void_p, C.c_int]),
     "ilg_get_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double),
@@ -256,6 +258,14 @@ class IllumContext:
         out = np.zeros((s.shape[0], self.num_faces), np.float64) if record_tsurf else None
         _check(lib().ilg_run_steps_host(self._h, C.byref(opts), s.shape[0], _p(s), _p(out)))
         return out
+
+    def bench_steps(self, opts: RunOpts, first_sun: int, nsteps: int, flush_mb=256.0):
+        """Per-step device times (ms) with an L2 flush before each step; with
+        opts.use_graph == 0 also the summed per-phase times."""
+        ms = np.zeros(nsteps, np.float64)
+        ph = np.zeros(3, np.float64)
+        _check(lib().ilg_bench_steps(self._h, C.byref(opts), first_sun, nsteps, flush_mb, _p(ms), _p(ph)))
+        return ms, {"direct": ph[0], "radiosity": ph[1], "conduction": ph[2]}
 
     def outputs(self):
         n = self.num_faces

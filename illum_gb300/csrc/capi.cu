@@ -76,6 +76,12 @@ static void invalidate_graph(Context& c) {
   for (int& k : c.graph_key) k = -1;
 }
 
+__global__ void k_flush(float4* buf, size_t n, unsigned salt) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x, st = (size_t)gridDim.x * blockDim.x;
+  float v = (float)salt;
+  for (; i < n; i += st) buf[i] = make_float4(v, v, v, v);
+}
+
 __global__ void k_advance(int* counters) {
   counters[1] += 1;   // sun index
   counters[2] += 1;   // frame
@@ -535,6 +541,56 @@ int ilg_run_steps_host(ilg_ctx* ctx, const ilg_run_opts* opts, int nsteps, const
     if (timing) ILG_TRY(collect_stats(c, true));
     if (tsurf_out) std::memcpy(tsurf_out + (size_t)s * c.nt, c.pinned_tsurf, (size_t)c.nt * 8);
   }
+  c.frame_no += nsteps;
+  return read_device_errors(c);
+}
+
+// Benchmark loop: before every step a kernel overwrites flush_mb MB (evicting
+// the 129 MB L2), then the step runs between two events on the context's
+// stream. step_ms[s] receives each step's device time; with use_graph == 0
+// the steps run eagerly and phase_ms[0..2] accumulates the direct,
+// radiosity and conduction phases.
+int ilg_bench_steps(ilg_ctx* ctx, const ilg_run_opts* opts, int first_sun, int nsteps, double flush_mb,
+                    double* step_ms, double* phase_ms) {
+  if (!ctx || !step_ms) { set_error("invalid arguments"); return ILG_ERR_ARG; }
+  Context& c = ctx->c;
+  ILG_TRY(check_run(c, opts));
+  if (nsteps < 0 || first_sun < 0 || first_sun + nsteps > c.nsun) { set_error("sun range out of bounds"); return ILG_ERR_ARG; }
+  const ilg_run_opts& o = *opts;
+  size_t nflush = flush_mb > 0 ? (size_t)(flush_mb * 1048576.0 / 16.0) : 0;
+  if (nflush) ILG_TRY(c.flush.reserve(nflush));
+  int h2[2] = {first_sun, c.frame_no};
+  ILG_CUDA(cudaMemcpyAsync(c.counters.p + 1, h2, sizeof(h2), cudaMemcpyHostToDevice, c.stream));
+  cudaGraphExec_t g = nullptr;
+  if (o.use_graph && !c.graph_broken)
+    if (get_graph(c, o, c.sun_aux.p, 1, false, &g) != ILG_OK) { c.graph_broken = true; g = nullptr; cudaGetLastError(); }
+  cudaEvent_t a = c.ev[0], b = c.ev[3];
+  if (phase_ms) phase_ms[0] = phase_ms[1] = phase_ms[2] = 0.0;
+  for (int s = 0; s < nsteps; ++s) {
+    if (nflush) {
+      k_flush<<<4 * 152, 256, 0, c.stream>>>(c.flush.p, nflush, (unsigned)s);
+      ILG_CUDA(cudaGetLastError());
+    }
+    if (g) {
+      ILG_CUDA(cudaEventRecord(a, c.stream));
+      ILG_CUDA(cudaGraphLaunch(g, c.stream));
+      ILG_CUDA(cudaEventRecord(b, c.stream));
+    } else {
+      ILG_TRY(enqueue_step(c, o, c.sun_aux.p, 1, true));
+    }
+    ILG_CUDA(cudaEventSynchronize(b));
+    float ms = 0.f;
+    ILG_CUDA(cudaEventElapsedTime(&ms, a, b));
+    step_ms[s] = ms;
+    if (!g) {
+      float p0, p1, p2;
+      ILG_CUDA(cudaEventElapsedTime(&p0, c.ev[0], c.ev[1]));
+      ILG_CUDA(cudaEventElapsedTime(&p1, c.ev[1], c.ev[2]));
+      ILG_CUDA(cudaEventElapsedTime(&p2, c.ev[2], c.ev[3]));
+      if (phase_ms) { phase_ms[0] += p0; phase_ms[1] += p1; phase_ms[2] += p2; }
+    }
+  }
+  ILG_CUDA(cudaStreamSynchronize(c.stream));
   c.frame_no += nsteps;
   return read_device_errors(c);
 }

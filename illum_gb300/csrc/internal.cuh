@@ -125,6 +125,8 @@ struct Context {
   int graph_key[4] = {-1, -1, -1, -1};
   bool graph_broken = false;      // capture failed once: launch eagerly
 
+  dbuf<float4> flush;              // L2-eviction buffer of the benchmark loop
+
   // scratch
   ScanScratch scan;
   SortScratch sort;

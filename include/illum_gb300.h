@@ -157,6 +157,13 @@ int ilg_run_steps(ilg_ctx* ctx, const ilg_run_opts* opts, int first_sun, int nst
  * nsteps x 3. */
 int ilg_run_steps_host(ilg_ctx* ctx, const ilg_run_opts* opts, int nsteps, const double* suns,
                        double* tsurf_out);
+/* Measurement loop over device-resident suns: before every step a kernel
+ * overwrites flush_mb MB of device memory (evicting L2), then the step runs
+ * between two CUDA events on the context's stream. step_ms: nsteps device
+ * times; with opts->use_graph == 0 phase_ms (3 values, may be NULL) receives
+ * the summed direct / radiosity / conduction phase times. */
+int ilg_bench_steps(ilg_ctx* ctx, const ilg_run_opts* opts, int first_sun, int nsteps, double flush_mb,
+                    double* step_ms, double* phase_ms);
 /* rad, rad_avg, therm_avg, therm_max: nt doubles each (any may be NULL). */
 int ilg_get_outputs(ilg_ctx* ctx, double* rad, double* rad_avg, double* therm_avg,
                     double* therm_max);
