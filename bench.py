@@ -160,7 +160,7 @@ def cpu_baseline(W, steps, threads):
     t0 = time.perf_counter()
     O.thermal_run(W["v"], W["f"], H, W["suns"][:steps], W["disk"], W["csr"], z, np.full(nz, c["ti"]),
                   np.full(nz, c["rhoc"]), dt=W["dt"], T0=c["T0"], emiss=c["emiss"], solar_const=c["solar"],
-                  norm_mode=1, bc_mode=1, rad_mode=1, tol=c["tol"])
+                  norm_mode=1, bc_mode=1, rad_mode=1, tol=c["tol"], coupling=1)
     el = time.perf_counter() - t0
     return W["f"].shape[0] * steps / el, el
 
@@ -222,7 +222,7 @@ def main():
     nsun = W["nsun"]
     c = CFG
     opts = ig.RunOpts(dt=W["dt"], tol=c["tol"], max_sweeps=200, use_radiosity=1, use_graph=1,
-                      precision=ig.PREC_FP64)
+                      precision=ig.PREC_FP64, coupling=ig.COUPLE_DIRECT)
     # warm-up (graph capture included)
     run_chunks(lambda s, k: ctx.bench_steps(opts, s, k, 256.0), 0, args.warmup, nsun)
     sun_pos = args.warmup
@@ -244,8 +244,8 @@ def main():
 
     # per-phase breakdown (eager launches with events between phases)
     eager = ig.RunOpts(dt=W["dt"], tol=c["tol"], max_sweeps=200, use_radiosity=1, use_graph=0,
-                       precision=ig.PREC_FP64)
-    ctx.set_timing(True)
+                       precision=ig.PREC_FP64, coupling=ig.COUPLE_DIRECT)
+    ctx.set_timing(True)    # resets the counters read by ctx.stats()
     nph = min(args.steps, 720)
     res = run_chunks(lambda s, k: ctx.bench_steps(eager, s, k, 256.0), sun_pos, nph, nsun)
     sun_pos += nph
@@ -273,7 +273,7 @@ def main():
         Wm = build_workload(ig, meshgen, precision=ig.PREC_MIXED)
         Wf = build_workload(ig, meshgen, precision=ig.PREC_FP64)
         mopts = ig.RunOpts(dt=W["dt"], tol=c["tol"], max_sweeps=200, use_radiosity=1, use_graph=1,
-                           precision=ig.PREC_MIXED)
+                           precision=ig.PREC_MIXED, coupling=ig.COUPLE_DIRECT)
         nchk = 720
         Wf["ctx"].run_steps(opts, 0, nchk)
         mres = Wm["ctx"].bench_steps(mopts, 0, nchk, 256.0)
@@ -311,7 +311,7 @@ def main():
                 "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
                 "config": {"workload": "icosphere L6 81,920 facets, 200 craters 30-300 m, nphi 64, nz 60, "
-                                       "dt 30 s, radiosity tol 1e-10, Newton boundary (C1, plain FP64 path)",
+                                       "dt 30 s, radiosity tol 1e-10, Newton boundary, E = direct coupling (C1, plain FP64 path)",
                            "facets": N, "nnz": nnz, "l2": "256 MB flush before every timed step",
                            "parallelism": f"replicas x{world}"},
                 "e2e": e2e, "gpu_launches": 5 * args.steps, "roofline": roofline, "cpu_baseline": cpu,

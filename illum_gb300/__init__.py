@@ -22,13 +22,15 @@ import os
 import numpy as np
 
 __all__ = ["IllumContext", "ThermalModel", "IlgError", "fib_spiral", "conductionQ", "conductionQ_batch", "lib",
-           "library_path", "RunOpts", "PREC_FP64", "PREC_MIXED", "BC_LINEARISED", "BC_NEWTON"]
+           "library_path", "RunOpts", "PREC_FP64", "PREC_MIXED", "BC_LINEARISED", "BC_NEWTON",
+           "COUPLE_REFERENCE", "COUPLE_DIRECT"]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _SO = os.path.join(_HERE, "libillum_gb300.so")
 
 PREC_FP64, PREC_MIXED = 0, 1
 BC_LINEARISED, BC_NEWTON = 0, 1
+COUPLE_REFERENCE, COUPLE_DIRECT = 0, 1
 
 ERRORS = {-1: "ILG_ERR_ARG", -2: "ILG_ERR_CUDA", -3: "ILG_ERR_NAN", -4: "ILG_ERR_PIVOT", -5: "ILG_ERR_NOMEM",
           -6: "ILG_ERR_DEVICE", -7: "ILG_ERR_NOTCONV"}
@@ -42,7 +44,7 @@ class IlgError(RuntimeError):
 
 class RunOpts(C.Structure):
     _fields_ = [("dt", C.c_double), ("tol", C.c_double), ("max_sweeps", C.c_int), ("use_radiosity", C.c_int),
-                ("use_graph", C.c_int), ("precision", C.c_int)]
+                ("use_graph", C.c_int), ("precision", C.c_int), ("coupling", C.c_int)]
 
 
 _lib = None

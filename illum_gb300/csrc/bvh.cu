@@ -21,7 +21,7 @@ __device__ __forceinline__ f3 f3of(float4 a) { return mk(a.x, a.y, a.z); }
 // ------------------------------------------------------------------ build
 __global__ void k_prepare(const float* __restrict__ verts, const int32_t* __restrict__ tris,
                           const float* __restrict__ normals, int nt, float4* tri_o, float4* cen, float4* nrm,
-                          double* area, double* frame) {
+                          double* area, double* frame, float4* frame32) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nt) return;
   const float* a = verts + 3 * (int64_t)tris[3 * t];
@@ -42,6 +42,9 @@ __global__ void k_prepare(const float* __restrict__ verts, const int32_t* __rest
   fr[0] = F.b.x; fr[1] = F.b.y; fr[2] = F.b.z;
   fr[3] = F.t.x; fr[4] = F.t.y; fr[5] = F.t.z;
   fr[6] = F.n.x; fr[7] = F.n.y; fr[8] = F.n.z;
+  frame32[3 * t] = make_float4((float)F.b.x, (float)F.b.y, (float)F.b.z, 0.f);
+  frame32[3 * t + 1] = make_float4((float)F.t.x, (float)F.t.y, (float)F.t.z, 0.f);
+  frame32[3 * t + 2] = make_float4((float)F.n.x, (float)F.n.y, (float)F.n.z, 0.f);
 }
 
 __device__ __forceinline__ u64 spread3(u64 x) {   // 21 bits -> every third bit
@@ -483,8 +486,9 @@ int bvh_build(Context& c, const float* verts_h, int nv, const int32_t* tris_h, c
   ILG_TRY(c.nrm.alloc(nt));
   ILG_TRY(c.area.alloc(nt));
   ILG_TRY(c.frame.alloc((size_t)nt * 9));
+  ILG_TRY(c.frame32.alloc((size_t)nt * 3));
   k_prepare<<<div_up(nt, 256), 256, 0, s>>>(dverts.p, dtris.p, dnormals.p, nt, c.tri_o.p, c.cen.p, c.nrm.p,
-                                            c.area.p, c.frame.p);
+                                            c.area.p, c.frame.p, c.frame32.p);
   ILG_CUDA(cudaGetLastError());
 
   // r_max on the host copy of the radii

@@ -93,7 +93,8 @@ __global__ void k_advance(int* counters) {
 static int enqueue_step(Context& c, const ilg_run_opts& o, const void* suns_dev, int from_counter, bool timing) {
   bool rad_on = o.use_radiosity && c.have_F && c.n_active > 0;
   if (timing) ILG_CUDA(cudaEventRecord(c.ev[0], c.stream));
-  ILG_TRY(direct_launch_aux(c, suns_dev, from_counter, c.Fsurf.p, rad_on ? c.E.p : c.rad.p));
+  const double* base = o.coupling == ILG_COUPLE_REFERENCE ? c.Fsurf.p : nullptr;
+  ILG_TRY(direct_launch_aux(c, suns_dev, from_counter, base, rad_on ? c.E.p : c.rad.p));
   if (timing) ILG_CUDA(cudaEventRecord(c.ev[1], c.stream));
   if (rad_on) ILG_TRY(radiosity_launch(c, c.E.p, c.rad.p, o.tol, o.max_sweeps, o.precision, true));
   if (timing) ILG_CUDA(cudaEventRecord(c.ev[2], c.stream));
@@ -118,6 +119,7 @@ static int check_run(Context& c, const ilg_run_opts* o) {
   if (c.ndisk < 2) { set_error("sun disk samples are not set (ilg_set_suns)"); return ILG_ERR_ARG; }
   if (!(o->dt > 0.0)) { set_error("dt must be > 0"); return ILG_ERR_ARG; }
   if (o->precision != ILG_PREC_FP64 && o->precision != ILG_PREC_MIXED) { set_error("bad precision"); return ILG_ERR_ARG; }
+  if (o->coupling != ILG_COUPLE_REFERENCE && o->coupling != ILG_COUPLE_DIRECT) { set_error("bad coupling"); return ILG_ERR_ARG; }
   if (o->use_radiosity && !c.have_F) { set_error("use_radiosity set but no form factors"); return ILG_ERR_ARG; }
   if (o->precision == ILG_PREC_MIXED && o->use_radiosity && !c.have_bf16) { set_error("no bf16 form factors"); return ILG_ERR_ARG; }
   ILG_TRY(conduction_prepare(c, o->dt, o->precision));
@@ -130,7 +132,7 @@ static int check_run(Context& c, const ilg_run_opts* o) {
 // Graph of one step (kernels only). key identifies what was captured.
 static int get_graph(Context& c, const ilg_run_opts& o, const void* suns_dev, int from_counter, bool with_copies,
                      cudaGraphExec_t* out) {
-  int key[4] = {o.precision * 2 + (o.use_radiosity ? 1 : 0), from_counter, with_copies ? 1 : 0,
+  int key[4] = {o.precision * 4 + o.coupling * 2 + (o.use_radiosity ? 1 : 0), from_counter, with_copies ? 1 : 0,
                 (int)(((uintptr_t)suns_dev >> 4) & 0x7fffffff)};
   if (c.graph && std::equal(key, key + 4, c.graph_key)) { *out = c.graph; return ILG_OK; }
   invalidate_graph(c);
@@ -423,6 +425,7 @@ int ilg_thermal_init(ilg_ctx* ctx, int nz, const double* z, const double* ti, co
   for (double* p : {c.Fsurf.p, c.Qprev.p, c.rad.p, c.rad_avg.p, c.therm_avg.p, c.therm_max.p})
     ILG_CUDA(cudaMemsetAsync(p, 0, (size_t)nt * 8, c.stream));
   ILG_CUDA(cudaMemsetAsync(c.counters.p, 0, 8 * sizeof(int), c.stream));
+  if (c.xprev.p) ILG_CUDA(cudaMemsetAsync(c.xprev.p, 0, c.xprev.n * 8, c.stream));
   ILG_CUDA(cudaStreamSynchronize(c.stream));
   c.state_prec = ILG_PREC_FP64;
   c.frame_no = 0;
@@ -582,6 +585,10 @@ int ilg_bench_steps(ilg_ctx* ctx, const ilg_run_opts* opts, int first_sun, int n
     float ms = 0.f;
     ILG_CUDA(cudaEventElapsedTime(&ms, a, b));
     step_ms[s] = ms;
+    int hc[4];
+    ILG_CUDA(cudaMemcpy(hc, c.counters.p, sizeof(hc), cudaMemcpyDeviceToHost));
+    c.stats_ambiguous += hc[0];
+    c.stats_sweeps += hc[3];
     if (!g) {
       float p0, p1, p2;
       ILG_CUDA(cudaEventElapsedTime(&p0, c.ev[0], c.ev[1]));

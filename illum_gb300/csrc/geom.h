@@ -352,6 +352,14 @@ ILG_HD void sun_frame(d3 N, d3* T, d3* B) {
   *B = cross(*T, N);
 }
 
+// Cosine between the sun-centre direction seen from p and the facet normal n
+// (src/cpp/illum.cpp:405,446: dot(normalise(sun - p), n)), written as
+// dot(sun - p, n) / |sun - p| (one division instead of three).
+ILG_HD double sun_mu(d3 S, d3 p, d3 n) {
+  d3 v = sub(S, p);
+  return dot(v, n) / norm(v);
+}
+
 // One sun-disk sample of src/cpp/illum.cpp:422-436: returns 1 when the sample
 // direction lies above the horizon. h points at the facet's nphi horizon
 // zenith angles. interp = 0 keeps the reference's threshold

@@ -50,6 +50,7 @@ struct Context {
 
   dbuf<float4> tri_o, cen, nrm;
   dbuf<double> area, frame;
+  dbuf<float4> frame32;           // float copy of the frame (3 x float4)
   dbuf<float4> nodes, tri_s;
   int root = 0;             // child code of the root (0, or ~0 for one facet)
   int64_t bvh_nodes = 0;
@@ -76,6 +77,13 @@ struct Context {
   dbuf<__nv_bfloat16> val_bf16;   // mixed precision copy
   dbuf<float> row_scale;
   bool have_bf16 = false;
+  // SELL-32 copy of the active rows for the sweeps (radiosity.cu)
+  int sell_nslices = 0;
+  int64_t sell_elems = 0;
+  dbuf<int64_t> sell_ptr;
+  dbuf<int32_t> sell_len, sell_split, sell_row, sell_m, sell_col;
+  dbuf<double> sell_val;
+  dbuf<__nv_bfloat16> sell_vbf;
 
   // thermal
   bool have_thermal = false;
@@ -95,6 +103,7 @@ struct Context {
   int state_prec = 0;             // which of T64 / T32 holds the state
   dbuf<double> Tsurf, Fsurf, Qprev;
   dbuf<double> rad, rad_avg, therm_avg, therm_max, E, xtmp, Q;
+  dbuf<double> xprev;             // radiosity solution of the step before
   int frame_no = 0;
 
   // suns and step machinery

@@ -23,6 +23,7 @@
 #include <cooperative_groups.h>
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <vector>
 
 #include "internal.cuh"
@@ -31,10 +32,20 @@ namespace ilg {
 
 namespace {
 
-constexpr int RAD_THREADS = 256;
+constexpr int RAD_THREADS = 512;
 constexpr int RAD_WARPS = RAD_THREADS / 32;
 
 struct RadArgs {
+  // SELL-32 copy of the active rows (see radiosity_prepare)
+  const int64_t* sl_ptr;    // per slice: offset of its first element
+  const int32_t* sl_len;    // per slice: elements per lane (multiple of 4)
+  const int32_t* sl_split;  // per slice: largest chunk count of its rows (1: no split rows)
+  const int32_t* ln_row;    // per lane: row, or -1 (padding lane)
+  const int32_t* ln_m;      // per lane: chunks of its row if it is the row's first lane, else 0
+  const int32_t* s_col;
+  const double* s_val;
+  const __nv_bfloat16* s_vbf;
+  int nslices;
   const int64_t* rowptr;
   const int32_t* col;
   const double* val;
@@ -45,6 +56,7 @@ struct RadArgs {
   const double* E;
   double* x;       // result (and warm start)
   double* xt;      // second iterate buffer
+  double* xprev;   // solution of the step before (extrapolated warm start)
   float* x32a;     // fp32 iterate buffers (mixed)
   float* x32b;
   float* r32;      // fp32 correction right-hand side (mixed)
@@ -108,8 +120,70 @@ __device__ __forceinline__ double grid_total(const double* part, int nb, double*
   return block_sum(v, sh);
 }
 
+// sum_k val[k] * x[col[k]] over one row, lanes strided, four independent
+// loads per lane in flight; fixed summation order (deterministic).
+template <class V, class X, class Acc>
+__device__ __forceinline__ Acc row_dot(const int32_t* __restrict__ col, const V* __restrict__ val,
+                                       const X* __restrict__ x, int64_t b, int64_t e, int lane) {
+  Acc s = 0;
+  for (int64_t k0 = b; k0 < e; k0 += 128) {
+    int c[4];
+    V v[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      int64_t k = k0 + lane + 32 * j;
+      bool ok = k < e;
+      c[j] = ok ? __ldg(col + k) : 0;
+      v[j] = ok ? __ldg(val + k) : V(0);
+    }
+    X xv[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) xv[j] = x[c[j]];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) s += (Acc)v[j] * (Acc)xv[j];
+  }
+  for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  return s;
+}
+
+// One SELL-32 slice: lane l accumulates its (chunk of a) row sequentially
+// (four independent loads in flight), then rows split into several chunks
+// are combined into their first lane in a fixed order.
+template <class V, class X, class Acc>
+__device__ __forceinline__ Acc slice_dot(const RadArgs& a, const V* __restrict__ sval, const X* __restrict__ x,
+                                         int sl, int lane) {
+  int64_t base = a.sl_ptr[sl] + lane;
+  int len = a.sl_len[sl];
+  Acc p = 0;
+  for (int k = 0; k < len; k += 4) {
+    int c[4];
+    V v[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      c[j] = __ldg(a.s_col + base + (int64_t)(k + j) * 32);
+      v[j] = __ldg(sval + base + (int64_t)(k + j) * 32);
+    }
+    X xv[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) xv[j] = x[c[j]];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) p += (Acc)v[j] * (Acc)xv[j];
+  }
+  int mmax = a.sl_split[sl];
+  if (mmax > 1) {
+    int m = a.ln_m[(int64_t)sl * 32 + lane];
+    Acc tot = p;
+    for (int j = 1; j < mmax; ++j) {
+      Acc q = __shfl_down_sync(0xffffffffu, p, j);
+      if (j < m) tot += q;
+    }
+    p = tot;
+  }
+  return p;
+}
+
 // FP64 Jacobi to tolerance.
-__global__ void __launch_bounds__(RAD_THREADS) k_radiosity64(RadArgs a) {
+__global__ void __launch_bounds__(RAD_THREADS, 2) k_radiosity64(RadArgs a) {
   __shared__ double sh[RAD_WARPS];
   const int lane = threadIdx.x & 31;
   const int gw = (blockIdx.x * RAD_THREADS + threadIdx.x) >> 5;
@@ -118,15 +192,19 @@ __global__ void __launch_bounds__(RAD_THREADS) k_radiosity64(RadArgs a) {
   const int nthreads = gridDim.x * RAD_THREADS;
   // all rows: both buffers start at E (inactive rows keep it); active rows
   // of x keep the previous solution when warm-starting
+  // warm start: x_{n-1} (or 2 x_{n-1} - x_{n-2} once two solutions exist)
+  const bool extrap = a.warm && a.counters[2] >= 2;
   for (int i = gt; i < a.nt; i += nthreads) {
     double e = a.E[i];
     a.xt[i] = e;
-    if (!a.warm) a.x[i] = e;
-  }
-  if (a.warm) {
-    // inactive rows of x must hold the new E
-    for (int i = gt; i < a.nt; i += nthreads)
-      if (a.rowptr[i + 1] == a.rowptr[i]) a.x[i] = a.E[i];
+    bool act = a.rowptr[i + 1] != a.rowptr[i];
+    if (!a.warm || !act) {
+      a.x[i] = e;
+    } else {
+      double xn = a.x[i];
+      if (extrap) a.x[i] = 2.0 * xn - a.xprev[i];
+      a.xprev[i] = xn;
+    }
   }
   if (!grid_barrier(a.bar, gridDim.x, a.derr)) return;
   double* cur = a.x;
@@ -134,13 +212,11 @@ __global__ void __launch_bounds__(RAD_THREADS) k_radiosity64(RadArgs a) {
   int sweeps = 0;
   for (;;) {
     double d2 = 0.0;
-    for (int w = gw; w < a.n_active; w += nwarps) {
-      int i = a.active[w];
-      int64_t b = a.rowptr[i], e = a.rowptr[i + 1];
-      double s = 0.0;
-      for (int64_t k = b + lane; k < e; k += 32) s += a.val[k] * cur[a.col[k]];
-      for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-      if (lane == 0) {
+    for (int sl = gw; sl < a.nslices; sl += nwarps) {
+      double s = slice_dot<double, double, double>(a, a.s_val, cur, sl, lane);
+      int64_t li = (int64_t)sl * 32 + lane;
+      if (a.ln_m[li] > 0) {
+        int i = a.ln_row[li];
         double xn = a.E[i] + s;
         double df = xn - cur[i];
         nxt[i] = xn;
@@ -174,16 +250,23 @@ __global__ void __launch_bounds__(RAD_THREADS) k_radiosity64(RadArgs a) {
 // Mixed precision: outer refinement with an fp64 residual r = E - (I - F) x
 // (fp64 values), inner fp32 Jacobi on (I - F~) d = r with bf16 F~, x += d.
 // The outer loop stops when ||r||_2 <= tol.
-__global__ void __launch_bounds__(RAD_THREADS) k_radiosity_mixed(RadArgs a) {
+__global__ void __launch_bounds__(RAD_THREADS, 2) k_radiosity_mixed(RadArgs a) {
   __shared__ double sh[RAD_WARPS];
   const int lane = threadIdx.x & 31;
   const int gw = (blockIdx.x * RAD_THREADS + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * RAD_THREADS) >> 5;
   const int gt = blockIdx.x * RAD_THREADS + threadIdx.x;
   const int nthreads = gridDim.x * RAD_THREADS;
+  const bool extrap = a.warm && a.counters[2] >= 2;
   for (int i = gt; i < a.nt; i += nthreads) {
     bool act = a.rowptr[i + 1] != a.rowptr[i];
-    if (!a.warm || !act) a.x[i] = a.E[i];
+    if (!a.warm || !act) {
+      a.x[i] = a.E[i];
+    } else {
+      double xn = a.x[i];
+      if (extrap) a.x[i] = 2.0 * xn - a.xprev[i];
+      a.xprev[i] = xn;
+    }
     a.x32a[i] = 0.f;
     a.x32b[i] = 0.f;
   }
@@ -192,13 +275,11 @@ __global__ void __launch_bounds__(RAD_THREADS) k_radiosity_mixed(RadArgs a) {
   for (;;) {
     // fp64 residual on active rows (inactive rows are exact)
     double r2 = 0.0;
-    for (int w = gw; w < a.n_active; w += nwarps) {
-      int i = a.active[w];
-      int64_t b = a.rowptr[i], e = a.rowptr[i + 1];
-      double s = 0.0;
-      for (int64_t k = b + lane; k < e; k += 32) s += a.val[k] * a.x[a.col[k]];
-      for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-      if (lane == 0) {
+    for (int sl = gw; sl < a.nslices; sl += nwarps) {
+      double s = slice_dot<double, double, double>(a, a.s_val, a.x, sl, lane);
+      int64_t li = (int64_t)sl * 32 + lane;
+      if (a.ln_m[li] > 0) {
+        int i = a.ln_row[li];
         double r = a.E[i] + s - a.x[i];
         a.r32[i] = (float)r;
         a.x32a[i] = (float)r;     // inner start: d0 = r
@@ -222,13 +303,13 @@ __global__ void __launch_bounds__(RAD_THREADS) k_radiosity_mixed(RadArgs a) {
     float* cur = a.x32a;
     float* nxt = a.x32b;
     for (int it = 0; it < 4; ++it) {
-      for (int w = gw; w < a.n_active; w += nwarps) {
-        int i = a.active[w];
-        int64_t b = a.rowptr[i], e = a.rowptr[i + 1];
-        float s = 0.f;
-        for (int64_t k = b + lane; k < e; k += 32) s += __bfloat162float(a.vbf[k]) * cur[a.col[k]];
-        for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-        if (lane == 0) nxt[i] = a.r32[i] + a.rscale[i] * s;
+      for (int sl = gw; sl < a.nslices; sl += nwarps) {
+        float s = slice_dot<__nv_bfloat16, float, float>(a, a.s_vbf, cur, sl, lane);
+        int64_t li = (int64_t)sl * 32 + lane;
+        if (a.ln_m[li] > 0) {
+          int i = a.ln_row[li];
+          nxt[i] = a.r32[i] + a.rscale[i] * s;
+        }
       }
       ++sweeps;
       if (!grid_barrier(a.bar, gridDim.x, a.derr)) return;
@@ -250,6 +331,37 @@ __global__ void k_active_compact(const uint32_t* __restrict__ flag, const unsign
                                  int nt, int32_t* active) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < nt && flag[i]) active[pos[i]] = i;
+}
+
+// SELL fill: lane (slice, l) copies elements [first, first + cnt) of its row
+// into column k of the slice; the rest of the slice column is padding
+// (column = 0, value = 0).
+__global__ void k_sell_fill(const int64_t* __restrict__ sl_ptr, const int32_t* __restrict__ sl_len,
+                            const int64_t* __restrict__ ln_first, const int32_t* __restrict__ ln_cnt,
+                            const int32_t* __restrict__ ln_row, const int32_t* __restrict__ col,
+                            const double* __restrict__ val, const float* __restrict__ rscale, int nslices,
+                            int32_t* s_col, double* s_val, __nv_bfloat16* s_vbf) {
+  int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= (int64_t)nslices * 32) return;
+  int sl = (int)(g >> 5), lane = (int)(g & 31);
+  int len = sl_len[sl];
+  int64_t base = sl_ptr[sl] + lane;
+  int64_t first = ln_first[g];
+  int cnt = ln_cnt[g];
+  int row = ln_row[g];
+  float sc = row >= 0 ? rscale[row] : 1.f;
+  for (int k = 0; k < len; ++k) {
+    int64_t o = base + (int64_t)k * 32;
+    if (k < cnt) {
+      s_col[o] = col[first + k];
+      s_val[o] = val[first + k];
+      s_vbf[o] = __float2bfloat16_rn((float)(val[first + k] / (double)sc));
+    } else {
+      s_col[o] = 0;
+      s_val[o] = 0.0;
+      s_vbf[o] = __float2bfloat16_rn(0.f);
+    }
+  }
 }
 
 // Per-row fp32 scale = max |F_ij| of the row; values stored as bf16(F/scale).
@@ -292,7 +404,90 @@ int radiosity_prepare(Context& c) {
   k_to_bf16<<<div_up(nt, 256), 256, 0, s>>>(c.rowptr.p, c.val.p, nt, c.val_bf16.p, c.row_scale.p);
   ILG_CUDA(cudaGetLastError());
   c.have_bf16 = true;
+
+  // SELL-32 layout of the active rows: rows sorted by length (longest
+  // first), rows longer than L split into chunks of at most L placed in
+  // adjacent lanes of one slice, each slice column-major and padded to the
+  // longest chunk (rounded up to 4).
+  std::vector<int64_t> rp((size_t)nt + 1);
+  ILG_CUDA(cudaMemcpyAsync(rp.data(), c.rowptr.p, rp.size() * 8, cudaMemcpyDeviceToHost, s));
   ILG_CUDA(cudaStreamSynchronize(s));
+  std::vector<int> rows;
+  int64_t maxlen = 0;
+  for (int i = 0; i < nt; ++i)
+    if (rp[i + 1] > rp[i]) { rows.push_back(i); maxlen = std::max<int64_t>(maxlen, rp[i + 1] - rp[i]); }
+  std::stable_sort(rows.begin(), rows.end(), [&](int p, int q) { return rp[p + 1] - rp[p] > rp[q + 1] - rp[q]; });
+  int64_t L = 32;                 // chunk length: bounds the per-sweep critical path
+  while ((maxlen + L - 1) / L > 32) L *= 2;
+  std::vector<int64_t> sl_ptr;
+  std::vector<int32_t> sl_len, sl_split, ln_row, ln_m, ln_cnt;
+  std::vector<int64_t> ln_first;
+  int lane = 32;   // force a new slice first
+  int64_t off = 0;
+  auto close_slice = [&]() {
+    if (sl_len.empty()) return;
+    while (lane < 32) {          // pad lanes
+      ln_row.push_back(-1); ln_m.push_back(-1); ln_cnt.push_back(0); ln_first.push_back(0);
+      ++lane;
+    }
+    int len = (sl_len.back() + 3) & ~3;
+    sl_len.back() = len;
+    off += (int64_t)len * 32;
+  };
+  for (int i : rows) {
+    int64_t len = rp[i + 1] - rp[i];
+    int m = (int)((len + L - 1) / L);
+    if (lane + m > 32) {
+      close_slice();
+      sl_ptr.push_back(off);
+      sl_len.push_back(0);
+      sl_split.push_back(1);
+      lane = 0;
+    }
+    for (int k = 0; k < m; ++k) {
+      int64_t first = rp[i] + (int64_t)k * L;
+      int cnt = (int)std::min<int64_t>(L, rp[i + 1] - first);
+      ln_row.push_back(i);
+      ln_m.push_back(k == 0 ? m : 0);
+      ln_cnt.push_back(cnt);
+      ln_first.push_back(first);
+      sl_len.back() = std::max(sl_len.back(), cnt);
+      ++lane;
+    }
+    sl_split.back() = std::max(sl_split.back(), m);
+  }
+  close_slice();
+  c.sell_nslices = (int)sl_len.size();
+  int ns = c.sell_nslices > 0 ? c.sell_nslices : 1;
+  int64_t nel = off > 0 ? off : 1;
+  ILG_TRY(c.sell_ptr.alloc(ns));
+  ILG_TRY(c.sell_len.alloc(ns));
+  ILG_TRY(c.sell_split.alloc(ns));
+  ILG_TRY(c.sell_row.alloc((size_t)ns * 32));
+  ILG_TRY(c.sell_m.alloc((size_t)ns * 32));
+  ILG_TRY(c.sell_col.alloc(nel));
+  ILG_TRY(c.sell_val.alloc(nel));
+  ILG_TRY(c.sell_vbf.alloc(nel));
+  if (c.sell_nslices > 0) {
+    dbuf<int64_t> dfirst;
+    dbuf<int32_t> dcnt;
+    ILG_TRY(dfirst.alloc(ln_first.size()));
+    ILG_TRY(dcnt.alloc(ln_cnt.size()));
+    ILG_CUDA(cudaMemcpyAsync(c.sell_ptr.p, sl_ptr.data(), sl_ptr.size() * 8, cudaMemcpyHostToDevice, s));
+    ILG_CUDA(cudaMemcpyAsync(c.sell_len.p, sl_len.data(), sl_len.size() * 4, cudaMemcpyHostToDevice, s));
+    ILG_CUDA(cudaMemcpyAsync(c.sell_split.p, sl_split.data(), sl_split.size() * 4, cudaMemcpyHostToDevice, s));
+    ILG_CUDA(cudaMemcpyAsync(c.sell_row.p, ln_row.data(), ln_row.size() * 4, cudaMemcpyHostToDevice, s));
+    ILG_CUDA(cudaMemcpyAsync(c.sell_m.p, ln_m.data(), ln_m.size() * 4, cudaMemcpyHostToDevice, s));
+    ILG_CUDA(cudaMemcpyAsync(dfirst.p, ln_first.data(), ln_first.size() * 8, cudaMemcpyHostToDevice, s));
+    ILG_CUDA(cudaMemcpyAsync(dcnt.p, ln_cnt.data(), ln_cnt.size() * 4, cudaMemcpyHostToDevice, s));
+    int64_t nl = (int64_t)c.sell_nslices * 32;
+    k_sell_fill<<<div_up(nl, 256), 256, 0, s>>>(c.sell_ptr.p, c.sell_len.p, dfirst.p, dcnt.p, c.sell_row.p, c.col.p,
+                                               c.val.p, c.row_scale.p, c.sell_nslices, c.sell_col.p, c.sell_val.p,
+                                               c.sell_vbf.p);
+    ILG_CUDA(cudaGetLastError());
+    ILG_CUDA(cudaStreamSynchronize(s));
+  }
+  c.sell_elems = off;
   return ILG_OK;
 }
 
@@ -309,12 +504,16 @@ int radiosity_setup(Context& c, int precision) {
   }
   bool mixed = precision == ILG_PREC_MIXED;
   int per_sm = mixed ? per_smm : per_sm64;
-  int want = div_up((int64_t)(c.n_active > 0 ? c.n_active : 1) * 32, RAD_THREADS);
+  int want = div_up((int64_t)(c.sell_nslices > 0 ? c.sell_nslices : 1) * 32, RAD_THREADS);
   int grid = per_sm * nsm;
   if (want < grid) grid = want;
   if (grid < 1) grid = 1;
   ILG_TRY(c.partials.reserve((size_t)2 * grid + 2));
   ILG_TRY(c.xtmp.reserve(c.nt));
+  if (c.xprev.n < (size_t)c.nt) {
+    ILG_TRY(c.xprev.alloc(c.nt));
+    ILG_CUDA(cudaMemset(c.xprev.p, 0, (size_t)c.nt * 8));
+  }
   if (mixed) ILG_TRY(c.x32.reserve((size_t)3 * c.nt));
   c.rad_grid = grid;
   c.rad_grid_prec = precision;
@@ -330,9 +529,12 @@ int radiosity_launch(Context& c, const double* E_dev, double* x_dev, double tol,
   bool mixed = precision == ILG_PREC_MIXED;
   int grid = c.rad_grid;
   RadArgs a;
+  a.sl_ptr = c.sell_ptr.p; a.sl_len = c.sell_len.p; a.sl_split = c.sell_split.p; a.ln_row = c.sell_row.p;
+  a.ln_m = c.sell_m.p; a.s_col = c.sell_col.p; a.s_val = c.sell_val.p; a.s_vbf = c.sell_vbf.p;
+  a.nslices = c.sell_nslices;
   a.rowptr = c.rowptr.p; a.col = c.col.p; a.val = c.val.p; a.vbf = c.val_bf16.p; a.rscale = c.row_scale.p;
   a.active = c.active.p; a.n_active = c.n_active; a.nt = c.nt;
-  a.E = E_dev; a.x = x_dev; a.xt = c.xtmp.p;
+  a.E = E_dev; a.x = x_dev; a.xt = c.xtmp.p; a.xprev = c.xprev.p;
   a.x32a = mixed ? c.x32.p : nullptr;
   a.x32b = mixed ? c.x32.p + c.nt : nullptr;
   a.r32 = mixed ? c.x32.p + 2 * (size_t)c.nt : nullptr;

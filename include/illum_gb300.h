@@ -143,7 +143,19 @@ typedef struct ilg_run_opts {
   int use_radiosity;       /* 0: rad = E (no F) */
   int use_graph;           /* capture the step in a CUDA graph */
   int precision;           /* ILG_PREC_FP64 / ILG_PREC_MIXED */
+  int coupling;            /* ILG_COUPLE_REFERENCE / ILG_COUPLE_DIRECT */
 } ilg_run_opts;
+
+/* What the radiosity solve of a step starts from. ILG_COUPLE_REFERENCE is
+ * the reference's E = -Fsurf + direct (src/cpp/illum_cli.cpp:411-421): the
+ * conductive surface flux of the previous step is fed back through the
+ * radiosity solve. With a thin top layer that loop has a gain above one for
+ * mutually visible facets and the run oscillates and diverges (the CPU
+ * restatement does the same). ILG_COUPLE_DIRECT starts from the direct
+ * insolation alone (E = direct), so the radiosity solve redistributes
+ * scattered sunlight and the conduction step receives it. */
+#define ILG_COUPLE_REFERENCE 0
+#define ILG_COUPLE_DIRECT 1
 
 /* Upload sun positions (nsun x 3, row-major, km) kept on the device for
  * ilg_run_steps; disk_xy as in ilg_direct_radiosity. */

@@ -17,7 +17,7 @@
 // insolation without any fast path, natural-order serial Gauss-Seidel, and a
 // top-down Thomas solve per facet column with coefficients rebuilt per call.
 //
-// Build: oracle/build.sh (g++ -O2 -ffp-contract=off -pthread -shared).
+// Build: oracle/Makefile (g++ -O2 -ffp-contract=off -pthread -shared).
 #include "../illum_gb300/csrc/geom.h"
 
 #include <algorithm>
@@ -384,7 +384,7 @@ void orc_direct(const float* verts, const int32_t* tris, int nt, const double* h
     }
     double denom = norm_mode == 0 ? (double)(nphi - 1) : (double)nsamp;
     double dv = (double)count / denom;
-    double mu = dot(N, BTN.n);
+    double mu = sun_mu(S, p, BTN.n);
     dv *= (mu > 0.0 ? mu : 0.0);
     dv *= flux;
     out[f] = dv;
@@ -593,8 +593,11 @@ int orc_conductiont(int nz, const double* z, double dt, double* T, double Tsurf,
 // T: (nz+1) x nt column-major in/out (row 0 = surface), the reference's
 // layout (src/cpp/thermal.hpp:48). bc_mode 0 = conductionQ, 1 = Newton.
 // rad_mode: 0 = reference sweeps (1 + gs_steps), 1 = to tolerance.
+// coupling: 0 = E = -Fsurf + direct (src/cpp/illum_cli.cpp:411-421),
+// 1 = E = direct.
 struct orc_run_params {
-  int nt, nz, nsteps, nphi, ndisk, norm_mode, interp, bc_mode, rad_mode, gs_steps, max_sweeps, use_radiosity;
+  int nt, nz, nsteps, nphi, ndisk, norm_mode, interp, bc_mode, rad_mode, gs_steps, max_sweeps, use_radiosity,
+      coupling;
   double dt, emiss, solar_const, tol, Fgeo;
 };
 
@@ -614,7 +617,10 @@ int orc_thermal_run(const orc_run_params* P, const float* verts, const int32_t* 
       orc_direct(verts, tris, nt, horizons, P->nphi, sun + 3 * s, disk_xy, P->ndisk, P->norm_mode,
                  P->interp, P->solar_const, direct.data(), cnt.data());
     }
-    for (int i = 0; i < nt; ++i) E[i] = -Fsurf[i] + direct[i];
+    if (P->coupling == 0)
+      for (int i = 0; i < nt; ++i) E[i] = -Fsurf[i] + direct[i];
+    else
+      for (int i = 0; i < nt; ++i) E[i] = direct[i];
     if (P->use_radiosity) {
       double res;
       orc_gauss_seidel(nt, rowptr, col, val, E.data(), P->rad_mode, P->gs_steps, P->tol,

@@ -167,13 +167,14 @@ def conductiont(z, dt, T, Tsurf, Tsurfp1, ti, rhoc, Fgeo=0.0):
 
 class RunParams(C.Structure):
     _fields_ = [(n, C.c_int) for n in ("nt", "nz", "nsteps", "nphi", "ndisk", "norm_mode", "interp", "bc_mode",
-                                       "rad_mode", "gs_steps", "max_sweeps", "use_radiosity")] + \
+                                       "rad_mode", "gs_steps", "max_sweeps", "use_radiosity", "coupling")] + \
                [(n, C.c_double) for n in ("dt", "emiss", "solar_const", "tol", "Fgeo")]
 
 
 def thermal_run(verts, faces, hor, suns, disk_xy, csr, z, ti, rhoc, *, dt, T0, emiss=0.999,
                 solar_const=1372.0, norm_mode=0, interp=0, bc_mode=0, rad_mode=1, gs_steps=1,
-                tol=1e-10, max_sweeps=200, state=None, frame0=0, record_tsurf=False, direct_all=None):
+                tol=1e-10, max_sweeps=200, state=None, frame0=0, record_tsurf=False, direct_all=None,
+                coupling=0):
     """Time-step loop of src/cpp/illum_cli.cpp:403-468. Returns a dict of the
     final state (T is (nz+1) x N column-major as a [N, nz+1] array)."""
     verts = np.ascontiguousarray(verts, np.float32)
@@ -186,7 +187,7 @@ def thermal_run(verts, faces, hor, suns, disk_xy, csr, z, ti, rhoc, *, dt, T0, e
     dxy = np.ascontiguousarray(np.asarray(disk_xy, np.float64).T)
     P = RunParams(nt=nt, nz=nz, nsteps=nsteps, nphi=hor.shape[1], ndisk=disk_xy.shape[0], norm_mode=norm_mode,
                   interp=interp, bc_mode=bc_mode, rad_mode=rad_mode, gs_steps=gs_steps, max_sweeps=max_sweeps,
-                  use_radiosity=int(csr is not None), dt=dt, emiss=emiss, solar_const=solar_const, tol=tol, Fgeo=0.0)
+                  use_radiosity=int(csr is not None), coupling=coupling, dt=dt, emiss=emiss, solar_const=solar_const, tol=tol, Fgeo=0.0)
     if state is None:
         state = dict(T=np.full((nt, nz + 1), T0, np.float64), Qprev=np.zeros(nt), Fsurf=np.zeros(nt),
                      rad=np.zeros(nt), rad_avg=np.zeros(nt), therm_avg=np.zeros(nt), therm_max=np.zeros(nt))

@@ -215,7 +215,7 @@ def test_thermal_model_step_vs_oracle(ilg, oracle_mod, mesh_l3):
 
 # ------------------------------------------------------------ fused loop
 def _setup_run(ilg, oracle_mod, v, f, nphi, nz, nsteps, period=6 * 3600.0, steps_per_rot=360, use_graph=1,
-               precision=0, bc_mode=1):
+               precision=0, bc_mode=1, coupling=1):
     ctx = ilg.IllumContext(v, f)
     ctx.make_horizons(nphi=nphi)
     ctx.set_insolation(1, 0, 1361.0)
@@ -226,20 +226,23 @@ def _setup_run(ilg, oracle_mod, v, f, nphi, nz, nsteps, period=6 * 3600.0, steps
     ctx.set_suns(suns, disk)
     z, ti, rhoc = _profile(nz)
     tm = ilg.ThermalModel(ctx, z, 300.0, 1.05e6, 200.0, emissivity=0.95, bc_mode=bc_mode, precision=precision)
-    opts = ilg.RunOpts(dt=dt, tol=1e-10, max_sweeps=200, use_radiosity=1, use_graph=use_graph, precision=precision)
+    opts = ilg.RunOpts(dt=dt, tol=1e-10, max_sweeps=200, use_radiosity=1, use_graph=use_graph, precision=precision,
+                       coupling=coupling)
     return ctx, tm, opts, (rp, c, x), suns, disk, (z, ti, rhoc), dt
 
 
-def test_run_steps_vs_oracle_fp64(ilg, oracle_mod, mesh_l4):
+@pytest.mark.parametrize("coupling,nsteps", [(0, 120), (1, 360)])
+def test_run_steps_vs_oracle_fp64(ilg, oracle_mod, mesh_l4, coupling, nsteps):
     """C0-shaped run (L4, 32 azimuths, 40 layers, Newton boundary, radiosity
-    to 1e-10): surface and subsurface temperatures within 1e-9 K."""
+    to 1e-10): surface and subsurface temperatures within 1e-9 K, with the
+    reference's E = -Fsurf + direct coupling and with E = direct."""
     v, f = mesh_l4
-    nsteps = 120
-    ctx, tm, opts, csr, suns, disk, (z, ti, rhoc), dt = _setup_run(ilg, oracle_mod, v, f, 32, 40, nsteps)
+    ctx, tm, opts, csr, suns, disk, (z, ti, rhoc), dt = _setup_run(ilg, oracle_mod, v, f, 32, 40, nsteps,
+                                                                   coupling=coupling)
     hist = ctx.run_steps(opts, 0, nsteps, record_tsurf=True)
     st = oracle_mod.thermal_run(v, f, ctx.horizons.T, suns, disk, csr, z, ti, rhoc, dt=dt, T0=200.0, emiss=0.95,
                                 solar_const=1361.0, norm_mode=1, bc_mode=1, rad_mode=1, tol=1e-10,
-                                record_tsurf=True)
+                                record_tsurf=True, coupling=coupling)
     assert np.abs(hist - st["tsurf_hist"]).max() <= TOL_T_FP64
     assert np.abs(tm.T - st["T"].T).max() <= TOL_T_FP64
     out = ctx.outputs()
@@ -250,10 +253,11 @@ def test_run_steps_vs_oracle_fp64(ilg, oracle_mod, mesh_l4):
 def test_run_steps_reference_boundary(ilg, oracle_mod, mesh_l3):
     v, f = mesh_l3
     nsteps = 60
-    ctx, tm, opts, csr, suns, disk, (z, ti, rhoc), dt = _setup_run(ilg, oracle_mod, v, f, 16, 30, nsteps, bc_mode=0)
+    ctx, tm, opts, csr, suns, disk, (z, ti, rhoc), dt = _setup_run(ilg, oracle_mod, v, f, 16, 30, nsteps, bc_mode=0,
+                                                                   coupling=0)
     ctx.run_steps(opts, 0, nsteps)
     st = oracle_mod.thermal_run(v, f, ctx.horizons.T, suns, disk, csr, z, ti, rhoc, dt=dt, T0=200.0, emiss=0.95,
-                                solar_const=1361.0, norm_mode=1, bc_mode=0, rad_mode=1, tol=1e-10)
+                                solar_const=1361.0, norm_mode=1, bc_mode=0, rad_mode=1, tol=1e-10, coupling=0)
     assert np.abs(tm.T - st["T"].T).max() <= TOL_T_FP64
 
 
