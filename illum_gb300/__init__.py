@@ -21,7 +21,7 @@ import os
 
 import numpy as np
 
-__all__ = ["IllumContext", "ThermalModel", "IlgError", "fib_spiral", "conductionQ", "conductionQ_batch", "lib",
+__all__ = ["IllumContext", "ThermalModel", "Batch", "IlgError", "fib_spiral", "conductionQ", "conductionQ_batch", "lib",
            "library_path", "RunOpts", "PREC_FP64", "PREC_MIXED", "BC_LINEARISED", "BC_NEWTON",
            "COUPLE_REFERENCE", "COUPLE_DIRECT"]
 
@@ -83,6 +83,14 @@ _SIGS = {
     "ilg_set_timing": (C.c_int, [C.c_void_p, C.c_int]),
     "ilg_get_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double),
                                 C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    "ilg_batch_create": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.POINTER(C.c_void_p)]),
+    "ilg_batch_destroy": (C.c_int, [C.c_void_p]),
+    "ilg_batch_run": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "ilg_batch_bench": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_void_p]),
+    "ilg_batch_status": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "ilg_batch_set_active": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "ilg_batch_get_tsurf": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    "ilg_batch_sync": (C.c_int, [C.c_void_p]),
     "conductionq_": (None, [C.POINTER(C.c_int), C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double),
                             C.POINTER(C.c_double), C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_double),
                             C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double)]),
@@ -327,6 +335,56 @@ class ThermalModel:
 
     def get_radiosity(self):
         return -self.get_F()
+
+
+class Batch:
+    """Several contexts stepped together (ilg_batch_*): one launch per phase
+    for all members; each member keeps its own RunOpts (same precision)."""
+
+    def __init__(self, contexts, opts):
+        self.contexts = list(contexts)
+        n = len(self.contexts)
+        arr = (RunOpts * n)(*opts)
+        hs = (C.c_void_p * n)(*[c._h for c in self.contexts])
+        h = C.c_void_p()
+        _check(lib().ilg_batch_create(hs, n, arr, C.byref(h)))
+        self._h = h
+        self.n = n
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().ilg_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def run(self, nsteps, use_graph=True):
+        _check(lib().ilg_batch_run(self._h, nsteps, int(use_graph)))
+
+    def bench(self, nsteps, flush_mb=256.0):
+        ms = np.zeros(nsteps)
+        _check(lib().ilg_batch_bench(self._h, nsteps, flush_mb, _p(ms)))
+        return ms
+
+    def status(self):
+        a = np.zeros(self.n, np.int32); d = np.zeros(self.n, np.int32); w = np.zeros(self.n, np.int32)
+        _check(lib().ilg_batch_status(self._h, _p(a), _p(d), _p(w)))
+        return a, d, w
+
+    def set_active(self, member, active):
+        _check(lib().ilg_batch_set_active(self._h, member, int(active)))
+
+    def tsurf(self, member):
+        out = np.zeros(self.contexts[member].num_faces)
+        _check(lib().ilg_batch_get_tsurf(self._h, member, _p(out)))
+        return out
+
+    def sync(self):
+        _check(lib().ilg_batch_sync(self._h))
 
 
 def conductionQ(z, dt, Qn, Qnp1, T, ti, rhoc, emiss, Tsurf, Fgeotherm=0.0):

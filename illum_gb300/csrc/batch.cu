@@ -1,0 +1,430 @@
+// batch.cu — many meshes stepped together: ilg_batch_* of include/illum_gb300.h.
+//
+// A batch concatenates its member contexts into one scene: facet arrays,
+// horizons, layer blocks ([nz][N] per mesh), conduction tables, sun tables
+// and the radiosity SELL slices (columns and rows shifted by the mesh's
+// first facet), plus a mesh table (MeshDesc) that every step kernel reads.
+// One step is then one launch per phase for all active meshes. Each mesh
+// keeps its own dt, layer count, thermal profile, sun table, coupling and
+// radiosity tolerance; meshes switch off after their last sun position.
+// Radiosity convergence is decided per mesh with fixed-order reductions,
+// so a mesh's results are bitwise the same alone and in any mix.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "internal.cuh"
+
+namespace ilg {
+
+namespace {
+
+__global__ void k_fill_int(int* a, int64_t n, int v) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) a[i] = v;
+}
+
+// shift non-negative entries by off (columns / rows of a member's slices)
+__global__ void k_shift(int32_t* a, int64_t n, int off) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n && a[i] >= 0) a[i] += off;
+}
+
+__global__ void k_shift64(int64_t* a, int64_t n, int64_t off) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) a[i] += off;
+}
+
+}  // namespace
+
+struct Batch {
+  std::vector<ilg_ctx*> members;
+  std::vector<ilg_run_opts> opts;
+  std::vector<MeshDesc> mh;
+  int nt = 0, precision = 0, nz_max = 0, nslices = 0;
+  int64_t nel = 0;
+  cudaStream_t stream = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  bool graph_broken = false;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  StepView v{};
+  StepPlan plan{};
+  // owned scene arrays
+  dbuf<MeshDesc> md;
+  dbuf<int> mesh_of;
+  dbuf<int2> cblocks;
+  dbuf<float4> cen, nrm, frame32;
+  dbuf<double> frame, H, hmin, hmax, disk;
+  dbuf<SunAux> suns;
+  dbuf<double> Tsurf, Fsurf, Qprev, rad, rad_avg, therm_avg, therm_max, E, xtmp, xprev;
+  dbuf<float> x32;
+  dbuf<double> T64, coef64;
+  dbuf<float> T32, coef32;
+  dbuf<int64_t> sl_ptr;
+  dbuf<int32_t> sl_len, sl_split, sl_mesh, ln_row, ln_m, s_col;
+  dbuf<double> s_val;
+  dbuf<__nv_bfloat16> s_vbf;
+  dbuf<float> rscale;
+  dbuf<uint8_t> row_act;
+  dbuf<int> work, counters, derr, mesh_flag;
+  dbuf<double> sl_d2, ch_d2;
+  dbuf<int4> chunks;
+  int nchunks = 0;
+  dbuf<unsigned> barrier;
+  dbuf<float4> flush;
+  ~Batch() {
+    if (graph) cudaGraphExecDestroy(graph);
+    for (auto& e : ev)
+      if (e) cudaEventDestroy(e);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+template <class T>
+static int cat(dbuf<T>& dst, size_t off, const T* src, size_t n, cudaStream_t s) {
+  if (n == 0 || !src) return ILG_OK;
+  ILG_CUDA(cudaMemcpyAsync(dst.p + off, src, n * sizeof(T), cudaMemcpyDeviceToDevice, s));
+  return ILG_OK;
+}
+
+static int build(Batch& b) {
+  int n = (int)b.members.size();
+  cudaStream_t s = b.stream;
+  // sizes and offsets
+  int64_t nt = 0, nH = 0, nT = 0, ncoef = 0, nsun = 0, nsl = 0, nel = 0, ncb = 0, nch = 0;
+  b.mh.assign(n, MeshDesc{});
+  b.nz_max = 0;
+  int ndisk = -1;
+  for (int i = 0; i < n; ++i) {
+    Context& c = b.members[i]->c;
+    const ilg_run_opts& o = b.opts[i];
+    ILG_TRY(check_run(c, &o, false));
+    ILG_CUDA(cudaStreamSynchronize(c.stream));
+    if (ndisk < 0) ndisk = c.ndisk;
+    if (c.ndisk != ndisk) { set_error("batch members must share the sun-disk samples"); return ILG_ERR_ARG; }
+    MeshDesc M = solo_desc(c, &o, 0);
+    M.facet0 = (int)nt;
+    M.H0 = nH;
+    M.T0 = nT;
+    M.coef0 = (int)ncoef;
+    M.sun0 = (int)nsun;
+    M.host_slot = (int)(nsun + c.nsun);
+    M.slice0 = (int)nsl;
+    M.chunk0 = (int)nch;
+    b.mh[i] = M;
+    nt += c.nt;
+    nH += (int64_t)c.nt * c.nphi;
+    nT += (int64_t)c.nt * c.nz;
+    ncoef += (int64_t)c.nz * 5;
+    nsun += c.nsun + 1;
+    nsl += M.nslices;
+    nch += M.nchunks;
+    if (M.nslices) nel += c.sell_elems;
+    ncb += div_up(c.nt, 128);
+    b.nz_max = std::max(b.nz_max, c.nz);
+  }
+  b.nt = (int)nt;
+  b.nslices = (int)nsl;
+  b.nchunks = (int)nch;
+  b.nel = nel;
+  bool mixed = b.precision == ILG_PREC_MIXED;
+  // allocations
+  ILG_TRY(b.md.alloc(n));
+  ILG_TRY(b.mesh_of.alloc(nt));
+  ILG_TRY(b.cblocks.alloc(ncb));
+  ILG_TRY(b.cen.alloc(nt)); ILG_TRY(b.nrm.alloc(nt)); ILG_TRY(b.frame32.alloc(3 * nt));
+  ILG_TRY(b.frame.alloc(9 * nt)); ILG_TRY(b.H.alloc(nH)); ILG_TRY(b.hmin.alloc(nt)); ILG_TRY(b.hmax.alloc(nt));
+  ILG_TRY(b.disk.alloc(2 * (size_t)ndisk));
+  ILG_TRY(b.suns.alloc(nsun));
+  for (dbuf<double>* d : {&b.Tsurf, &b.Fsurf, &b.Qprev, &b.rad, &b.rad_avg, &b.therm_avg, &b.therm_max, &b.E, &b.xtmp,
+                          &b.xprev})
+    ILG_TRY(d->alloc(nt));
+  if (mixed) {
+    ILG_TRY(b.x32.alloc(3 * nt));
+    ILG_TRY(b.T32.alloc(nT));
+    ILG_TRY(b.coef32.alloc(ncoef));
+  } else {
+    ILG_TRY(b.T64.alloc(nT));
+    ILG_TRY(b.coef64.alloc(ncoef));
+  }
+  int64_t nsl1 = nsl > 0 ? nsl : 1, nel1 = nel > 0 ? nel : 1;
+  ILG_TRY(b.sl_ptr.alloc(nsl1)); ILG_TRY(b.sl_len.alloc(nsl1)); ILG_TRY(b.sl_split.alloc(nsl1));
+  ILG_TRY(b.sl_mesh.alloc(nsl1)); ILG_TRY(b.ln_row.alloc(32 * nsl1)); ILG_TRY(b.ln_m.alloc(32 * nsl1));
+  ILG_TRY(b.s_col.alloc(nel1)); ILG_TRY(b.s_val.alloc(nel1)); ILG_TRY(b.s_vbf.alloc(nel1));
+  ILG_TRY(b.rscale.alloc(nt)); ILG_TRY(b.row_act.alloc(nt));
+  ILG_TRY(b.work.alloc(nt)); ILG_TRY(b.counters.alloc(8)); ILG_TRY(b.derr.alloc(DERR_COUNT));
+  ILG_TRY(b.mesh_flag.alloc(n)); ILG_TRY(b.sl_d2.alloc(nsl1)); ILG_TRY(b.barrier.alloc(2));
+  ILG_TRY(b.ch_d2.alloc(nch > 0 ? nch : 1));
+  std::vector<int4> chh;
+  for (int i = 0; i < n; ++i) {
+    const MeshDesc& M = b.mh[i];
+    int C = radiosity_chunk();
+    for (int k = 0; k < M.nchunks; ++k)
+      chh.push_back(make_int4(M.slice0 + k * C, std::min(C, M.nslices - k * C), i, 0));
+  }
+  ILG_TRY(b.chunks.alloc(chh.empty() ? 1 : chh.size()));
+  if (!chh.empty())
+    ILG_CUDA(cudaMemcpyAsync(b.chunks.p, chh.data(), chh.size() * sizeof(int4), cudaMemcpyHostToDevice, s));
+  ILG_CUDA(cudaMemsetAsync(b.row_act.p, 0, nt, s));
+  ILG_CUDA(cudaMemsetAsync(b.counters.p, 0, 8 * sizeof(int), s));
+  ILG_CUDA(cudaMemsetAsync(b.derr.p, 0, DERR_COUNT * sizeof(int), s));
+  // copies
+  std::vector<int2> cbh;
+  int64_t el = 0;
+  for (int i = 0; i < n; ++i) {
+    Context& c = b.members[i]->c;
+    MeshDesc& M = b.mh[i];
+    size_t f0 = M.facet0, N = c.nt;
+    ILG_TRY(cat(b.cen, f0, c.cen.p, N, s));
+    ILG_TRY(cat(b.nrm, f0, c.nrm.p, N, s));
+    ILG_TRY(cat(b.frame32, 3 * f0, c.frame32.p, 3 * N, s));
+    ILG_TRY(cat(b.frame, 9 * f0, c.frame.p, 9 * N, s));
+    ILG_TRY(cat(b.H, (size_t)M.H0, c.H.p, N * c.nphi, s));
+    ILG_TRY(cat(b.hmin, f0, c.hmin.p, N, s));
+    ILG_TRY(cat(b.hmax, f0, c.hmax.p, N, s));
+    ILG_TRY(cat(b.suns, (size_t)M.sun0, c.sun_aux.p, (size_t)c.nsun + 1, s));
+    ILG_TRY(cat(b.Tsurf, f0, c.Tsurf.p, N, s));
+    ILG_TRY(cat(b.Fsurf, f0, c.Fsurf.p, N, s));
+    ILG_TRY(cat(b.Qprev, f0, c.Qprev.p, N, s));
+    ILG_TRY(cat(b.rad, f0, c.rad.p, N, s));
+    ILG_TRY(cat(b.rad_avg, f0, c.rad_avg.p, N, s));
+    ILG_TRY(cat(b.therm_avg, f0, c.therm_avg.p, N, s));
+    ILG_TRY(cat(b.therm_max, f0, c.therm_max.p, N, s));
+    ILG_TRY(cat(b.xprev, f0, c.xprev.p, N, s));
+    if (mixed) {
+      ILG_TRY(cat(b.T32, (size_t)M.T0, c.T32.p, N * c.nz, s));
+      ILG_TRY(cat(b.coef32, (size_t)M.coef0, c.coef32.p, (size_t)c.nz * 5, s));
+    } else {
+      ILG_TRY(cat(b.T64, (size_t)M.T0, c.T64.p, N * c.nz, s));
+      ILG_TRY(cat(b.coef64, (size_t)M.coef0, c.coef64.p, (size_t)c.nz * 5, s));
+    }
+    if (c.have_F) {
+      ILG_TRY(cat(b.rscale, f0, c.row_scale.p, N, s));
+      ILG_TRY(cat(b.row_act, f0, c.row_act.p, N, s));
+    }
+    if (M.nslices > 0) {
+      size_t s0 = M.slice0, ns = M.nslices;
+      ILG_TRY(cat(b.sl_ptr, s0, c.sell_ptr.p, ns, s));
+      ILG_TRY(cat(b.sl_len, s0, c.sell_len.p, ns, s));
+      ILG_TRY(cat(b.sl_split, s0, c.sell_split.p, ns, s));
+      ILG_TRY(cat(b.ln_row, 32 * s0, c.sell_row.p, 32 * ns, s));
+      ILG_TRY(cat(b.ln_m, 32 * s0, c.sell_m.p, 32 * ns, s));
+      ILG_TRY(cat(b.s_col, (size_t)el, c.sell_col.p, (size_t)c.sell_elems, s));
+      ILG_TRY(cat(b.s_val, (size_t)el, c.sell_val.p, (size_t)c.sell_elems, s));
+      ILG_TRY(cat(b.s_vbf, (size_t)el, c.sell_vbf.p, (size_t)c.sell_elems, s));
+      k_shift64<<<div_up(ns, 256), 256, 0, s>>>(b.sl_ptr.p + s0, ns, el);
+      k_shift<<<div_up(32 * ns, 256), 256, 0, s>>>(b.ln_row.p + 32 * s0, 32 * ns, (int)f0);
+      k_shift<<<div_up(c.sell_elems, 256), 256, 0, s>>>(b.s_col.p + el, c.sell_elems, (int)f0);
+      k_fill_int<<<div_up(ns, 256), 256, 0, s>>>(b.sl_mesh.p + s0, ns, i);
+      ILG_CUDA(cudaGetLastError());
+      el += c.sell_elems;
+    }
+    k_fill_int<<<div_up(N, 256), 256, 0, s>>>(b.mesh_of.p + f0, N, i);
+    ILG_CUDA(cudaGetLastError());
+    for (int k = 0; k < div_up(c.nt, 128); ++k) cbh.push_back(make_int2(i, k * 128));
+  }
+  ILG_TRY(cat(b.disk, 0, b.members[0]->c.disk.p, 2 * (size_t)ndisk, s));
+  ILG_CUDA(cudaMemcpyAsync(b.cblocks.p, cbh.data(), cbh.size() * sizeof(int2), cudaMemcpyHostToDevice, s));
+  ILG_CUDA(cudaMemcpyAsync(b.md.p, b.mh.data(), n * sizeof(MeshDesc), cudaMemcpyHostToDevice, s));
+  ILG_CUDA(cudaStreamSynchronize(s));
+  // view
+  StepView& v = b.v;
+  v = StepView{};
+  v.nt = b.nt; v.nmesh = n; v.md = b.md.p; v.mesh_of = b.mesh_of.p;
+  v.cen = b.cen.p; v.nrm = b.nrm.p; v.frame32 = b.frame32.p; v.frame = b.frame.p; v.H = b.H.p;
+  v.hmin = b.hmin.p; v.hmax = b.hmax.p; v.disk = b.disk.p; v.ndisk = ndisk; v.suns = b.suns.p;
+  v.Tsurf = b.Tsurf.p; v.Fsurf = b.Fsurf.p; v.Qprev = b.Qprev.p; v.rad = b.rad.p; v.rad_avg = b.rad_avg.p;
+  v.therm_avg = b.therm_avg.p; v.therm_max = b.therm_max.p; v.E = b.E.p; v.xtmp = b.xtmp.p; v.xprev = b.xprev.p;
+  v.x32 = b.x32.p; v.T64 = b.T64.p; v.T32 = b.T32.p; v.coef64 = b.coef64.p; v.coef32 = b.coef32.p;
+  v.sl_ptr = b.sl_ptr.p; v.sl_len = b.sl_len.p; v.sl_split = b.sl_split.p; v.sl_mesh = b.sl_mesh.p;
+  v.ln_row = b.ln_row.p; v.ln_m = b.ln_m.p; v.s_col = b.s_col.p; v.s_val = b.s_val.p; v.s_vbf = b.s_vbf.p;
+  v.rscale = b.rscale.p; v.row_act = b.row_act.p; v.nslices = b.nslices;
+  v.cblocks = b.cblocks.p; v.ncblocks = (int)ncb;
+  v.chunks = b.chunks.p; v.nchunks = b.nchunks;
+  v.work = b.work.p; v.counters = b.counters.p; v.derr = b.derr.p; v.mesh_flag = b.mesh_flag.p;
+  v.sl_d2 = b.sl_d2.p; v.ch_d2 = b.ch_d2.p; v.barrier = b.barrier.p;
+  b.plan.precision = b.precision;
+  b.plan.rad_on = b.nslices > 0;
+  b.plan.rad_grid = b.plan.rad_on ? radiosity_grid(b.nslices, b.precision) : 1;
+  b.plan.nz_max = b.nz_max;
+  return ILG_OK;
+}
+
+static int batch_errors(Batch& b) {
+  int h[DERR_COUNT];
+  ILG_CUDA(cudaMemcpyAsync(h, b.derr.p, sizeof(h), cudaMemcpyDeviceToHost, b.stream));
+  ILG_CUDA(cudaStreamSynchronize(b.stream));
+  for (int i = 0; i < DERR_COUNT; ++i)
+    if (h[i]) {
+      ILG_CUDA(cudaMemsetAsync(b.derr.p, 0, sizeof(h), b.stream));
+      set_error("device error flag %d set during a batch step", i);
+      return i == DERR_PIVOT ? ILG_ERR_PIVOT : ILG_ERR_DEVICE;
+    }
+  return ILG_OK;
+}
+
+static int batch_graph(Batch& b, cudaGraphExec_t* out) {
+  if (b.graph) { *out = b.graph; return ILG_OK; }
+  cudaGraph_t g;
+  ILG_CUDA(cudaStreamBeginCapture(b.stream, cudaStreamCaptureModeThreadLocal));
+  int rc = enqueue_step(b.v, b.plan, b.stream, nullptr);
+  cudaError_t e = cudaStreamEndCapture(b.stream, &g);
+  if (rc != ILG_OK || e != cudaSuccess) {
+    cudaGetLastError();
+    if (e == cudaSuccess) cudaGraphDestroy(g);
+    set_error("batch step capture failed: %s", cudaGetErrorString(e));
+    return rc != ILG_OK ? rc : ILG_ERR_CUDA;
+  }
+  cudaError_t ei = cudaGraphInstantiate(&b.graph, g, 0);
+  cudaGraphDestroy(g);
+  if (ei != cudaSuccess) { b.graph = nullptr; set_error("graph instantiation failed"); return ILG_ERR_CUDA; }
+  *out = b.graph;
+  return ILG_OK;
+}
+
+}  // namespace ilg
+
+using namespace ilg;
+
+struct ilg_batch {
+  Batch b;
+};
+
+extern "C" {
+
+int ilg_batch_create(ilg_ctx** members, int n, const ilg_run_opts* opts, ilg_batch** out) {
+  if (!members || n < 1 || !opts || !out) { set_error("invalid batch arguments"); return ILG_ERR_ARG; }
+  if (n > radiosity_max_meshes()) { set_error("a batch holds at most %d meshes", radiosity_max_meshes()); return ILG_ERR_ARG; }
+  for (int i = 1; i < n; ++i)
+    if (opts[i].precision != opts[0].precision) { set_error("batch members must share one precision"); return ILG_ERR_ARG; }
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < i; ++j)
+      if (members[i] == members[j]) { set_error("a context appears twice in the batch"); return ILG_ERR_ARG; }
+  *out = nullptr;
+  ilg_batch* h = new ilg_batch();
+  Batch& b = h->b;
+  b.members.assign(members, members + n);
+  b.opts.assign(opts, opts + n);
+  b.precision = opts[0].precision;
+  if (cudaStreamCreateWithFlags(&b.stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete h;
+    set_error("cudaStreamCreate failed");
+    return ILG_ERR_CUDA;
+  }
+  for (auto& e : b.ev)
+    if (cudaEventCreate(&e) != cudaSuccess) { delete h; set_error("cudaEventCreate failed"); return ILG_ERR_CUDA; }
+  int rc = build(b);
+  if (rc != ILG_OK) { delete h; return rc; }
+  *out = h;
+  return ILG_OK;
+}
+
+int ilg_batch_destroy(ilg_batch* batch) {
+  delete batch;
+  return ILG_OK;
+}
+
+int ilg_batch_run(ilg_batch* batch, int nsteps, int use_graph) {
+  if (!batch || nsteps < 0) { set_error("invalid arguments"); return ILG_ERR_ARG; }
+  Batch& b = batch->b;
+  cudaGraphExec_t g = nullptr;
+  if (use_graph && !b.graph_broken)
+    if (batch_graph(b, &g) != ILG_OK) { b.graph_broken = true; g = nullptr; cudaGetLastError(); }
+  for (int s = 0; s < nsteps; ++s) {
+    if (g) ILG_CUDA(cudaGraphLaunch(g, b.stream));
+    else ILG_TRY(enqueue_step(b.v, b.plan, b.stream, nullptr));
+  }
+  ILG_CUDA(cudaStreamSynchronize(b.stream));
+  return batch_errors(b);
+}
+
+int ilg_batch_bench(ilg_batch* batch, int nsteps, double flush_mb, double* step_ms) {
+  if (!batch || nsteps < 0 || !step_ms) { set_error("invalid arguments"); return ILG_ERR_ARG; }
+  Batch& b = batch->b;
+  size_t nflush = flush_mb > 0 ? (size_t)(flush_mb * 1048576.0 / 16.0) : 0;
+  if (nflush) ILG_TRY(b.flush.reserve(nflush));
+  cudaGraphExec_t g = nullptr;
+  if (!b.graph_broken)
+    if (batch_graph(b, &g) != ILG_OK) { b.graph_broken = true; g = nullptr; cudaGetLastError(); }
+  for (int s = 0; s < nsteps; ++s) {
+    if (nflush) ILG_TRY(flush_launch(b.flush.p, nflush, (unsigned)s, b.stream));
+    ILG_CUDA(cudaEventRecord(b.ev[0], b.stream));
+    if (g) ILG_CUDA(cudaGraphLaunch(g, b.stream));
+    else ILG_TRY(enqueue_step(b.v, b.plan, b.stream, nullptr));
+    ILG_CUDA(cudaEventRecord(b.ev[3], b.stream));
+    ILG_CUDA(cudaEventSynchronize(b.ev[3]));
+    float ms = 0.f;
+    ILG_CUDA(cudaEventElapsedTime(&ms, b.ev[0], b.ev[3]));
+    step_ms[s] = ms;
+  }
+  return batch_errors(b);
+}
+
+int ilg_batch_status(ilg_batch* batch, int* active, int* steps_done, int* sweeps) {
+  if (!batch) { set_error("batch is NULL"); return ILG_ERR_ARG; }
+  Batch& b = batch->b;
+  int n = (int)b.members.size();
+  std::vector<MeshDesc> m(n);
+  ILG_CUDA(cudaMemcpyAsync(m.data(), b.md.p, n * sizeof(MeshDesc), cudaMemcpyDeviceToHost, b.stream));
+  ILG_CUDA(cudaStreamSynchronize(b.stream));
+  for (int i = 0; i < n; ++i) {
+    if (active) active[i] = m[i].active;
+    if (steps_done) steps_done[i] = m[i].done_steps;
+    if (sweeps) sweeps[i] = m[i].sweeps;
+  }
+  return ILG_OK;
+}
+
+int ilg_batch_set_active(ilg_batch* batch, int member, int active) {
+  if (!batch || member < 0 || member >= (int)batch->b.members.size()) { set_error("invalid member"); return ILG_ERR_ARG; }
+  Batch& b = batch->b;
+  MeshDesc* d = b.md.p + member;
+  int a = active ? 1 : 0;
+  ILG_CUDA(cudaMemcpyAsync(&d->active, &a, sizeof(int), cudaMemcpyHostToDevice, b.stream));
+  ILG_CUDA(cudaStreamSynchronize(b.stream));
+  return ILG_OK;
+}
+
+int ilg_batch_get_tsurf(ilg_batch* batch, int member, double* out) {
+  if (!batch || !out || member < 0 || member >= (int)batch->b.members.size()) { set_error("invalid member"); return ILG_ERR_ARG; }
+  Batch& b = batch->b;
+  const MeshDesc& M = b.mh[member];
+  ILG_CUDA(cudaMemcpyAsync(out, b.Tsurf.p + M.facet0, (size_t)M.nfacet * 8, cudaMemcpyDeviceToHost, b.stream));
+  ILG_CUDA(cudaStreamSynchronize(b.stream));
+  return ILG_OK;
+}
+
+// Copy every member's state back into its context (temperatures, fluxes,
+// averages, radiosity history, frame counter).
+int ilg_batch_sync(ilg_batch* batch) {
+  if (!batch) { set_error("batch is NULL"); return ILG_ERR_ARG; }
+  Batch& b = batch->b;
+  int n = (int)b.members.size();
+  std::vector<MeshDesc> m(n);
+  ILG_CUDA(cudaMemcpyAsync(m.data(), b.md.p, n * sizeof(MeshDesc), cudaMemcpyDeviceToHost, b.stream));
+  ILG_CUDA(cudaStreamSynchronize(b.stream));
+  bool mixed = b.precision == ILG_PREC_MIXED;
+  for (int i = 0; i < n; ++i) {
+    Context& c = b.members[i]->c;
+    const MeshDesc& M = b.mh[i];
+    size_t f0 = M.facet0, N = c.nt, bytes = N * 8;
+    cudaStream_t s = b.stream;
+    ILG_CUDA(cudaMemcpyAsync(c.Tsurf.p, b.Tsurf.p + f0, bytes, cudaMemcpyDeviceToDevice, s));
+    ILG_CUDA(cudaMemcpyAsync(c.Fsurf.p, b.Fsurf.p + f0, bytes, cudaMemcpyDeviceToDevice, s));
+    ILG_CUDA(cudaMemcpyAsync(c.Qprev.p, b.Qprev.p + f0, bytes, cudaMemcpyDeviceToDevice, s));
+    ILG_CUDA(cudaMemcpyAsync(c.rad.p, b.rad.p + f0, bytes, cudaMemcpyDeviceToDevice, s));
+    ILG_CUDA(cudaMemcpyAsync(c.rad_avg.p, b.rad_avg.p + f0, bytes, cudaMemcpyDeviceToDevice, s));
+    ILG_CUDA(cudaMemcpyAsync(c.therm_avg.p, b.therm_avg.p + f0, bytes, cudaMemcpyDeviceToDevice, s));
+    ILG_CUDA(cudaMemcpyAsync(c.therm_max.p, b.therm_max.p + f0, bytes, cudaMemcpyDeviceToDevice, s));
+    ILG_CUDA(cudaMemcpyAsync(c.xprev.p, b.xprev.p + f0, bytes, cudaMemcpyDeviceToDevice, s));
+    if (mixed)
+      ILG_CUDA(cudaMemcpyAsync(c.T32.p, b.T32.p + M.T0, N * c.nz * 4, cudaMemcpyDeviceToDevice, s));
+    else
+      ILG_CUDA(cudaMemcpyAsync(c.T64.p, b.T64.p + M.T0, N * c.nz * 8, cudaMemcpyDeviceToDevice, s));
+    c.frame_no = m[i].frame;
+  }
+  ILG_CUDA(cudaStreamSynchronize(b.stream));
+  return ILG_OK;
+}
+
+}  // extern "C"

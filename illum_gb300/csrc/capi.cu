@@ -13,10 +13,6 @@
 #include "geom.h"
 #include "internal.cuh"
 
-struct ilg_ctx {
-  ilg::Context c;
-};
-
 namespace ilg {
 
 static thread_local std::string g_err;
@@ -82,67 +78,180 @@ __global__ void k_flush(float4* buf, size_t n, unsigned salt) {
   for (; i < n; i += st) buf[i] = make_float4(v, v, v, v);
 }
 
-__global__ void k_advance(int* counters) {
-  counters[1] += 1;   // sun index
-  counters[2] += 1;   // frame
+// Advance every active mesh by one step; a mesh driven from its sun table
+// switches itself off after its last sun position.
+__global__ void k_advance(MeshDesc* md, int nmesh) {
+  int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= nmesh) return;
+  MeshDesc& M = md[m];
+  if (!M.active) return;
+  M.sun_idx += 1;
+  M.frame += 1;
+  M.done_steps += 1;
+  if (!M.host_sun && M.sun_idx >= M.nsun) M.active = 0;
 }
 
-// One step on c.stream. suns_dev: SunAux table indexed by counters[1]
-// (from_counter) or a single entry. When the radiosity solve is off the
-// direct kernel writes rad directly.
-static int enqueue_step(Context& c, const ilg_run_opts& o, const void* suns_dev, int from_counter, bool timing) {
-  bool rad_on = o.use_radiosity && c.have_F && c.n_active > 0;
-  if (timing) ILG_CUDA(cudaEventRecord(c.ev[0], c.stream));
-  const double* base = o.coupling == ILG_COUPLE_REFERENCE ? c.Fsurf.p : nullptr;
-  ILG_TRY(direct_launch_aux(c, suns_dev, from_counter, base, rad_on ? c.E.p : c.rad.p));
-  if (timing) ILG_CUDA(cudaEventRecord(c.ev[1], c.stream));
-  if (rad_on) ILG_TRY(radiosity_launch(c, c.E.p, c.rad.p, o.tol, o.max_sweeps, o.precision, true));
-  if (timing) ILG_CUDA(cudaEventRecord(c.ev[2], c.stream));
-  ILG_TRY(conduction_launch(c, c.rad.p, o.precision, true));
-  if (timing) ILG_CUDA(cudaEventRecord(c.ev[3], c.stream));
-  k_advance<<<1, 1, 0, c.stream>>>(c.counters.p);
+int advance_launch(const StepView& v, cudaStream_t s) {
+  k_advance<<<div_up(v.nmesh, 128), 128, 0, s>>>(v.md, v.nmesh);
   ILG_CUDA(cudaGetLastError());
   return ILG_OK;
 }
 
-static int ensure_pinned(Context& c) {
-  if (!c.pinned_aux) ILG_CUDA(cudaMallocHost((void**)&c.pinned_aux, 256));
-  if (!c.pinned_tsurf) ILG_CUDA(cudaMallocHost((void**)&c.pinned_tsurf, (size_t)c.nt * 8));
-  ILG_TRY(c.host_sun_aux.reserve(256));
+int flush_launch(float4* buf, size_t n, unsigned salt, cudaStream_t s) {
+  k_flush<<<4 * 152, 256, 0, s>>>(buf, n, salt);
+  ILG_CUDA(cudaGetLastError());
   return ILG_OK;
 }
 
-static int check_run(Context& c, const ilg_run_opts* o) {
+// One step of a view: direct -> radiosity -> conduction -> advance. With
+// ev (4 events), the phase boundaries are recorded.
+int enqueue_step(const StepView& v, const StepPlan& p, cudaStream_t s, cudaEvent_t* ev) {
+  if (ev) ILG_CUDA(cudaEventRecord(ev[0], s));
+  ILG_TRY(direct_launch(v, 0, s));
+  if (ev) ILG_CUDA(cudaEventRecord(ev[1], s));
+  if (p.rad_on) ILG_TRY(radiosity_launch(v, v.rad, 1, p.precision, p.rad_grid, s));
+  if (ev) ILG_CUDA(cudaEventRecord(ev[2], s));
+  ILG_TRY(conduction_launch(v, v.rad, p.precision, 1, p.nz_max, s));
+  if (ev) ILG_CUDA(cudaEventRecord(ev[3], s));
+  return advance_launch(v, s);
+}
+
+static int ensure_pinned(Context& c) {
+  if (!c.pinned_aux) ILG_CUDA(cudaMallocHost((void**)&c.pinned_aux, sizeof(SunAux)));
+  if (!c.pinned_tsurf) ILG_CUDA(cudaMallocHost((void**)&c.pinned_tsurf, (size_t)c.nt * 8));
+  return ILG_OK;
+}
+
+// The context as a one-mesh view (device pointers of its own buffers).
+static StepView solo_view(Context& c, int precision) {
+  StepView v{};
+  v.nt = c.nt;
+  v.nmesh = 1;
+  v.md = c.md.p;
+  v.mesh_of = nullptr;
+  v.cen = c.cen.p; v.nrm = c.nrm.p; v.frame32 = c.frame32.p;
+  v.frame = c.frame.p; v.H = c.H.p; v.hmin = c.hmin.p; v.hmax = c.hmax.p; v.disk = c.disk.p;
+  v.ndisk = c.ndisk;
+  v.suns = c.sun_aux.p;
+  v.Tsurf = c.Tsurf.p; v.Fsurf = c.Fsurf.p; v.Qprev = c.Qprev.p; v.rad = c.rad.p; v.rad_avg = c.rad_avg.p;
+  v.therm_avg = c.therm_avg.p; v.therm_max = c.therm_max.p; v.E = c.E.p; v.xtmp = c.xtmp.p; v.xprev = c.xprev.p;
+  v.x32 = c.x32.p;
+  v.T64 = c.T64.p; v.T32 = c.T32.p;
+  v.coef64 = c.coef64.p; v.coef32 = c.coef32.p;
+  v.sl_ptr = c.sell_ptr.p; v.sl_len = c.sell_len.p; v.sl_split = c.sell_split.p; v.sl_mesh = nullptr;
+  v.ln_row = c.sell_row.p; v.ln_m = c.sell_m.p; v.s_col = c.sell_col.p; v.s_val = c.sell_val.p;
+  v.s_vbf = c.sell_vbf.p; v.rscale = c.row_scale.p; v.row_act = c.row_act.p;
+  v.nslices = c.have_F ? c.sell_nslices : 0;
+  v.cblocks = nullptr; v.ncblocks = 0;
+  v.chunks = c.chunks.p; v.nchunks = c.have_F ? c.nchunks : 0;
+  v.work = c.work.p; v.counters = c.counters.p; v.derr = c.derr.p; v.mesh_flag = c.mesh_flag.p;
+  v.sl_d2 = c.sl_d2.p; v.ch_d2 = c.ch_d2.p; v.barrier = c.barrier.p;
+  v.rho64 = nullptr; v.rho32 = nullptr;
+  (void)precision;
+  return v;
+}
+
+// Host mirror of the context's mesh descriptor for a run (or a drop-in call).
+MeshDesc solo_desc(const Context& c, const ilg_run_opts* o, int first_sun) {
+  MeshDesc M{};
+  M.facet0 = 0;
+  M.nfacet = c.nt;
+  M.nphi = c.nphi;
+  M.interp = c.interp;
+  M.H0 = 0;
+  M.dphi = c.dphi;
+  M.denom = c.norm_mode == 0 ? (double)(c.nphi - 1) : (double)(c.ndisk - 1);
+  M.nsamp = c.ndisk - 1;
+  M.coupling = o ? o->coupling : ILG_COUPLE_DIRECT;
+  M.sun0 = 0;
+  M.nsun = c.nsun;
+  M.sun_idx = first_sun;
+  M.frame = c.frame_no;
+  M.host_sun = 0;
+  M.host_slot = c.nsun;
+  M.nz = c.nz;
+  M.coef0 = 0;
+  M.T0 = 0;
+  M.cs = c.cond_cs;
+  M.slice0 = 0;
+  M.nslices = (o && o->use_radiosity && c.have_F) ? c.sell_nslices : 0;
+  M.chunk0 = 0;
+  M.nchunks = M.nslices > 0 ? c.nchunks : 0;
+  M.tol2 = o ? o->tol * o->tol : 0.0;
+  M.max_sweeps = o ? o->max_sweeps : 1;
+  M.active = 1;
+  return M;
+}
+
+static int upload_desc(Context& c, const MeshDesc& M) {
+  c.mh = M;
+  ILG_CUDA(cudaMemcpyAsync(c.md.p, &c.mh, sizeof(MeshDesc), cudaMemcpyHostToDevice, c.stream));
+  ILG_CUDA(cudaStreamSynchronize(c.stream));
+  return ILG_OK;
+}
+
+// Per-context scratch of the step kernels, sized before any capture.
+static int ensure_step_buffers(Context& c, int precision) {
+  ILG_TRY(c.E.reserve(c.nt));
+  ILG_TRY(c.Q.reserve(c.nt));
+  ILG_TRY(c.xtmp.reserve(c.nt));
+  if (c.xprev.n < (size_t)c.nt) {
+    ILG_TRY(c.xprev.alloc(c.nt));
+    ILG_CUDA(cudaMemset(c.xprev.p, 0, (size_t)c.nt * 8));
+  }
+  if (precision == ILG_PREC_MIXED) ILG_TRY(c.x32.reserve((size_t)3 * c.nt));
+  ILG_TRY(c.sl_d2.reserve(c.sell_nslices > 0 ? c.sell_nslices : 1));
+  ILG_TRY(c.md.reserve(1));
+  ILG_TRY(c.mesh_flag.reserve(1));
+  return ILG_OK;
+}
+
+// host_driven: the sun of each step comes from the host slot, so no sun
+// table is needed.
+int check_run(Context& c, const ilg_run_opts* o, bool host_driven) {
   if (!o) { set_error("opts is NULL"); return ILG_ERR_ARG; }
   if (!c.have_thermal) { set_error("ilg_thermal_init has not been called"); return ILG_ERR_ARG; }
   if (!c.H.p || c.nphi < 2) { set_error("horizons are not set"); return ILG_ERR_ARG; }
   if (c.ndisk < 2) { set_error("sun disk samples are not set (ilg_set_suns)"); return ILG_ERR_ARG; }
+  if (!host_driven && c.nsun < 1) { set_error("sun positions are not set (ilg_set_suns)"); return ILG_ERR_ARG; }
   if (!(o->dt > 0.0)) { set_error("dt must be > 0"); return ILG_ERR_ARG; }
   if (o->precision != ILG_PREC_FP64 && o->precision != ILG_PREC_MIXED) { set_error("bad precision"); return ILG_ERR_ARG; }
   if (o->coupling != ILG_COUPLE_REFERENCE && o->coupling != ILG_COUPLE_DIRECT) { set_error("bad coupling"); return ILG_ERR_ARG; }
   if (o->use_radiosity && !c.have_F) { set_error("use_radiosity set but no form factors"); return ILG_ERR_ARG; }
-  if (o->precision == ILG_PREC_MIXED && o->use_radiosity && !c.have_bf16) { set_error("no bf16 form factors"); return ILG_ERR_ARG; }
+  if (o->max_sweeps < 1) { set_error("max_sweeps must be >= 1"); return ILG_ERR_ARG; }
   ILG_TRY(conduction_prepare(c, o->dt, o->precision));
   ILG_TRY(conduction_state_convert(c, o->precision));
-  if (o->use_radiosity && c.have_F && c.n_active > 0) ILG_TRY(radiosity_setup(c, o->precision));
+  ILG_TRY(ensure_step_buffers(c, o->precision));
   ILG_TRY(ensure_pinned(c));
   return ILG_OK;
 }
 
-// Graph of one step (kernels only). key identifies what was captured.
-static int get_graph(Context& c, const ilg_run_opts& o, const void* suns_dev, int from_counter, bool with_copies,
-                     cudaGraphExec_t* out) {
-  int key[4] = {o.precision * 4 + o.coupling * 2 + (o.use_radiosity ? 1 : 0), from_counter, with_copies ? 1 : 0,
-                (int)(((uintptr_t)suns_dev >> 4) & 0x7fffffff)};
+static StepPlan solo_plan(Context& c, const ilg_run_opts& o) {
+  StepPlan p;
+  p.precision = o.precision;
+  p.rad_on = o.use_radiosity && c.have_F && c.sell_nslices > 0;
+  p.rad_grid = p.rad_on ? radiosity_grid(c.sell_nslices, o.precision) : 1;
+  p.nz_max = c.nz;
+  return p;
+}
+
+// Graph of one step. with_copies adds the host sun upload before and the
+// surface-temperature download after the step (host-driven steps).
+static int get_graph(Context& c, const ilg_run_opts& o, bool with_copies, cudaGraphExec_t* out) {
+  int key[4] = {o.precision * 4 + o.coupling * 2 + (o.use_radiosity ? 1 : 0), with_copies ? 1 : 0, c.nz,
+                c.sell_nslices};
   if (c.graph && std::equal(key, key + 4, c.graph_key)) { *out = c.graph; return ILG_OK; }
   invalidate_graph(c);
+  StepView v = solo_view(c, o.precision);
+  StepPlan p = solo_plan(c, o);
   cudaGraph_t g;
   ILG_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
   int rc = ILG_OK;
   if (with_copies)
-    if (cudaMemcpyAsync(c.host_sun_aux.p, c.pinned_aux, sun_aux_bytes(), cudaMemcpyHostToDevice, c.stream) != cudaSuccess)
+    if (cudaMemcpyAsync(c.sun_aux.p + c.nsun, c.pinned_aux, sizeof(SunAux), cudaMemcpyHostToDevice, c.stream) !=
+        cudaSuccess)
       rc = ILG_ERR_CUDA;
-  if (rc == ILG_OK) rc = enqueue_step(c, o, suns_dev, from_counter, false);
+  if (rc == ILG_OK) rc = enqueue_step(v, p, c.stream, nullptr);
   if (rc == ILG_OK && with_copies)
     if (cudaMemcpyAsync(c.pinned_tsurf, c.Tsurf.p, (size_t)c.nt * 8, cudaMemcpyDeviceToHost, c.stream) != cudaSuccess)
       rc = ILG_ERR_CUDA;
@@ -165,13 +274,15 @@ static int get_graph(Context& c, const ilg_run_opts& o, const void* suns_dev, in
   return ILG_OK;
 }
 
-static int collect_stats(Context& c, bool timing) {
-  int h[4];
-  ILG_CUDA(cudaMemcpyAsync(h, c.counters.p, sizeof(h), cudaMemcpyDeviceToHost, c.stream));
+static int collect_stats(Context& c, bool phases) {
+  int h0 = 0;
+  MeshDesc md;
+  ILG_CUDA(cudaMemcpyAsync(&h0, c.counters.p, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+  ILG_CUDA(cudaMemcpyAsync(&md, c.md.p, sizeof(md), cudaMemcpyDeviceToHost, c.stream));
   ILG_CUDA(cudaStreamSynchronize(c.stream));
-  c.stats_ambiguous += h[0];
-  c.stats_sweeps += h[3];
-  if (timing) {
+  c.stats_ambiguous += h0;
+  c.stats_sweeps += md.sweeps;
+  if (phases) {
     float a, b, d;
     ILG_CUDA(cudaEventElapsedTime(&a, c.ev[0], c.ev[1]));
     ILG_CUDA(cudaEventElapsedTime(&b, c.ev[1], c.ev[2]));
@@ -180,6 +291,32 @@ static int collect_stats(Context& c, bool timing) {
     c.ms_rad += b;
     c.ms_cond += d;
   }
+  return ILG_OK;
+}
+
+// Sun positions of the context: a SunAux table of nsun entries plus one
+// host slot (index nsun) for host-driven steps and drop-in calls.
+static int upload_suns(Context& c, const double* suns, int nsun) {
+  std::vector<SunAux> aux((size_t)nsun + 1);
+  for (int i = 0; i < nsun; ++i) aux[i] = make_sun_aux(suns + 3 * (size_t)i, c.solar_const, c.scene_mag, c.disk_rmax);
+  aux[nsun] = aux[nsun > 0 ? nsun - 1 : 0];
+  ILG_TRY(c.sun_aux.alloc(aux.size()));
+  ILG_CUDA(cudaMemcpyAsync(c.sun_aux.p, aux.data(), aux.size() * sizeof(SunAux), cudaMemcpyHostToDevice, c.stream));
+  ILG_CUDA(cudaStreamSynchronize(c.stream));
+  c.nsun = nsun;
+  return ILG_OK;
+}
+
+// Put one sun position into the host slot (allocating a one-entry table
+// when no sun table exists yet).
+static int set_host_sun(Context& c, const double* sun) {
+  ILG_TRY(ensure_pinned(c));
+  if (!c.sun_aux.p) {
+    ILG_TRY(c.sun_aux.alloc(1));
+    c.nsun = 0;
+  }
+  *(SunAux*)c.pinned_aux = make_sun_aux(sun, c.solar_const, c.scene_mag, c.disk_rmax);
+  ILG_CUDA(cudaMemcpyAsync(c.sun_aux.p + c.nsun, c.pinned_aux, sizeof(SunAux), cudaMemcpyHostToDevice, c.stream));
   return ILG_OK;
 }
 
@@ -207,7 +344,7 @@ int ilg_ctx_create(const float* verts, int nv, const int32_t* tris, int nt, cons
   for (auto& e : c.ev)
     if (cudaEventCreate(&e) != cudaSuccess) { set_error("cudaEventCreate failed"); delete h; return ILG_ERR_CUDA; }
   if ((rc = c.derr.alloc(DERR_COUNT)) || (rc = c.counters.alloc(8)) || (rc = c.work.alloc(nt)) ||
-      (rc = c.barrier.alloc(2))) {
+      (rc = c.barrier.alloc(2)) || (rc = c.md.alloc(1)) || (rc = c.mesh_flag.alloc(1))) {
     delete h;
     return rc;
   }
@@ -331,13 +468,7 @@ int ilg_set_insolation(ilg_ctx* ctx, int norm_mode, int interp, double solar_con
   c.norm_mode = norm_mode;
   c.interp = interp;
   c.solar_const = solar_const;
-  if (c.nsun > 0 && c.sun_aux.p) {   // flux is baked into the per-sun table: rebuild
-    std::vector<double> s((size_t)c.nsun * 3);
-    ILG_CUDA(cudaMemcpy(s.data(), c.suns.p, s.size() * 8, cudaMemcpyDeviceToHost));
-    std::vector<unsigned char> aux((size_t)c.nsun * sun_aux_bytes());
-    sun_aux_fill(c, s.data(), c.nsun, aux.data());
-    ILG_CUDA(cudaMemcpy(c.sun_aux.p, aux.data(), aux.size(), cudaMemcpyHostToDevice));
-  }
+  if (c.nsun > 0) ILG_TRY(upload_suns(c, c.suns_h.data(), c.nsun));   // flux is baked into the table
   return ILG_OK;
 }
 
@@ -348,12 +479,14 @@ void ilg_fib_spiral(double* xy, int n) {
 int ilg_direct_radiosity(ilg_ctx* ctx, const double* sun, const double* disk_xy, int ndisk, double* out) {
   if (!ctx || !sun || !out) { set_error("invalid direct arguments"); return ILG_ERR_ARG; }
   Context& c = ctx->c;
+  if (!c.H.p || c.nphi < 2) { set_error("horizons are not set"); return ILG_ERR_ARG; }
   ILG_TRY(set_disk(c, disk_xy, ndisk));
-  ILG_TRY(ensure_pinned(c));
-  ILG_TRY(c.E.reserve(c.nt));
-  sun_aux_fill(c, sun, 1, c.pinned_aux);
-  ILG_CUDA(cudaMemcpyAsync(c.host_sun_aux.p, c.pinned_aux, sun_aux_bytes(), cudaMemcpyHostToDevice, c.stream));
-  ILG_TRY(direct_launch_aux(c, c.host_sun_aux.p, 0, nullptr, c.E.p));
+  ILG_TRY(ensure_step_buffers(c, ILG_PREC_FP64));
+  ILG_TRY(set_host_sun(c, sun));
+  MeshDesc M = solo_desc(c, nullptr, 0);
+  M.host_sun = 1;
+  ILG_TRY(upload_desc(c, M));
+  ILG_TRY(direct_launch(solo_view(c, ILG_PREC_FP64), 1, c.stream));
   ILG_CUDA(cudaMemcpyAsync(out, c.E.p, (size_t)c.nt * 8, cudaMemcpyDeviceToHost, c.stream));
   ILG_CUDA(cudaStreamSynchronize(c.stream));
   return read_device_errors(c);
@@ -363,27 +496,33 @@ int ilg_radiosity_solve(ilg_ctx* ctx, const double* E, double tol, int max_sweep
   if (!ctx || !E || !x || max_sweeps < 1 || !(tol >= 0.0)) { set_error("invalid radiosity arguments"); return ILG_ERR_ARG; }
   Context& c = ctx->c;
   if (!c.have_F) { set_error("no form factors"); return ILG_ERR_ARG; }
-  ILG_TRY(c.E.reserve(c.nt));
-  ILG_TRY(c.Q.reserve(c.nt));
-  ILG_CUDA(cudaMemcpyAsync(c.E.p, E, (size_t)c.nt * 8, cudaMemcpyHostToDevice, c.stream));
-  if (c.n_active == 0) {
+  if (c.sell_nslices == 0) {
     std::memcpy(x, E, (size_t)c.nt * 8);
     if (res) *res = 0.0;
     if (sweeps) *sweeps = 0;
     return ILG_OK;
   }
-  ILG_CUDA(cudaMemsetAsync(c.counters.p + 3, 0, sizeof(int), c.stream));
-  ILG_TRY(radiosity_launch(c, c.E.p, c.Q.p, tol, max_sweeps, ILG_PREC_FP64, false));
-  double r2 = 0.0;
-  int sw = 0;
+  ILG_TRY(ensure_step_buffers(c, ILG_PREC_FP64));
+  ilg_run_opts o{};
+  o.tol = tol;
+  o.max_sweeps = max_sweeps;
+  o.use_radiosity = 1;
+  MeshDesc M = solo_desc(c, &o, 0);
+  ILG_TRY(upload_desc(c, M));
+  ILG_CUDA(cudaMemcpyAsync(c.E.p, E, (size_t)c.nt * 8, cudaMemcpyHostToDevice, c.stream));
+  StepView v = solo_view(c, ILG_PREC_FP64);
+  ILG_TRY(radiosity_launch(v, c.Q.p, 0, ILG_PREC_FP64, radiosity_grid(c.sell_nslices, ILG_PREC_FP64), c.stream));
+  MeshDesc out;
   ILG_CUDA(cudaMemcpyAsync(x, c.Q.p, (size_t)c.nt * 8, cudaMemcpyDeviceToHost, c.stream));
-  ILG_CUDA(cudaMemcpyAsync(&r2, c.partials.p + 2 * c.rad_grid, 8, cudaMemcpyDeviceToHost, c.stream));
-  ILG_CUDA(cudaMemcpyAsync(&sw, c.counters.p + 3, 4, cudaMemcpyDeviceToHost, c.stream));
+  ILG_CUDA(cudaMemcpyAsync(&out, c.md.p, sizeof(out), cudaMemcpyDeviceToHost, c.stream));
   ILG_CUDA(cudaStreamSynchronize(c.stream));
   ILG_TRY(read_device_errors(c));
-  if (res) *res = std::sqrt(r2);
-  if (sweeps) *sweeps = sw;
-  if (r2 > tol * tol) { set_error("radiosity residual %g above tol after %d sweeps", std::sqrt(r2), sw); return ILG_ERR_NOTCONV; }
+  if (res) *res = std::sqrt(out.res2);
+  if (sweeps) *sweeps = out.sweeps;
+  if (out.res2 > tol * tol) {
+    set_error("radiosity residual %g above tol after %d sweeps", std::sqrt(out.res2), out.sweeps);
+    return ILG_ERR_NOTCONV;
+  }
   return ILG_OK;
 }
 
@@ -426,6 +565,7 @@ int ilg_thermal_init(ilg_ctx* ctx, int nz, const double* z, const double* ti, co
     ILG_CUDA(cudaMemsetAsync(p, 0, (size_t)nt * 8, c.stream));
   ILG_CUDA(cudaMemsetAsync(c.counters.p, 0, 8 * sizeof(int), c.stream));
   if (c.xprev.p) ILG_CUDA(cudaMemsetAsync(c.xprev.p, 0, c.xprev.n * 8, c.stream));
+  invalidate_graph(c);
   ILG_CUDA(cudaStreamSynchronize(c.stream));
   c.state_prec = ILG_PREC_FP64;
   c.frame_no = 0;
@@ -438,8 +578,11 @@ int ilg_thermal_step(ilg_ctx* ctx, double dt, const double* Q) {
   Context& c = ctx->c;
   if (!c.have_thermal) { set_error("ilg_thermal_init has not been called"); return ILG_ERR_ARG; }
   ILG_TRY(conduction_prepare(c, dt, c.state_prec));
+  ILG_TRY(ensure_step_buffers(c, c.state_prec));
+  MeshDesc M = solo_desc(c, nullptr, 0);
+  ILG_TRY(upload_desc(c, M));
   ILG_CUDA(cudaMemcpyAsync(c.Q.p, Q, (size_t)c.nt * 8, cudaMemcpyHostToDevice, c.stream));
-  ILG_TRY(conduction_launch(c, c.Q.p, c.state_prec, false));
+  ILG_TRY(conduction_launch(solo_view(c, c.state_prec), c.Q.p, c.state_prec, 0, c.nz, c.stream));
   ILG_CUDA(cudaStreamSynchronize(c.stream));
   return read_device_errors(c);
 }
@@ -478,34 +621,26 @@ int ilg_set_suns(ilg_ctx* ctx, int nsun, const double* suns, const double* disk_
   Context& c = ctx->c;
   invalidate_graph(c);
   ILG_TRY(set_disk(c, disk_xy, ndisk));
-  std::vector<unsigned char> aux((size_t)nsun * sun_aux_bytes());
-  sun_aux_fill(c, suns, nsun, aux.data());
-  ILG_TRY(c.sun_aux.alloc(aux.size()));
-  ILG_TRY(c.suns.alloc((size_t)nsun * 3));
-  ILG_CUDA(cudaMemcpyAsync(c.sun_aux.p, aux.data(), aux.size(), cudaMemcpyHostToDevice, c.stream));
-  ILG_CUDA(cudaMemcpyAsync(c.suns.p, suns, (size_t)nsun * 24, cudaMemcpyHostToDevice, c.stream));
-  ILG_CUDA(cudaStreamSynchronize(c.stream));
-  c.nsun = nsun;
-  return ILG_OK;
+  c.suns_h.assign(suns, suns + 3 * (size_t)nsun);
+  return upload_suns(c, suns, nsun);
 }
 
 int ilg_run_steps(ilg_ctx* ctx, const ilg_run_opts* opts, int first_sun, int nsteps, double* tsurf_out) {
   if (!ctx) { set_error("ctx is NULL"); return ILG_ERR_ARG; }
   Context& c = ctx->c;
-  ILG_TRY(check_run(c, opts));
+  ILG_TRY(check_run(c, opts, false));
   if (nsteps < 0 || first_sun < 0 || first_sun + nsteps > c.nsun) { set_error("sun range out of bounds"); return ILG_ERR_ARG; }
   const ilg_run_opts& o = *opts;
-  int h2[2] = {first_sun, c.frame_no};
-  ILG_CUDA(cudaMemcpyAsync(c.counters.p + 1, h2, sizeof(h2), cudaMemcpyHostToDevice, c.stream));
-  ILG_CUDA(cudaStreamSynchronize(c.stream));
+  ILG_TRY(upload_desc(c, solo_desc(c, &o, first_sun)));
   bool timing = c.timing;
   cudaGraphExec_t g = nullptr;
   if (o.use_graph && !timing && !c.graph_broken)
-    if (get_graph(c, o, c.sun_aux.p, 1, false, &g) != ILG_OK) { c.graph_broken = true; g = nullptr; cudaGetLastError(); }
-  if (tsurf_out) ILG_TRY(ensure_pinned(c));
+    if (get_graph(c, o, false, &g) != ILG_OK) { c.graph_broken = true; g = nullptr; cudaGetLastError(); }
+  StepView v = solo_view(c, o.precision);
+  StepPlan p = solo_plan(c, o);
   for (int s = 0; s < nsteps; ++s) {
     if (g) ILG_CUDA(cudaGraphLaunch(g, c.stream));
-    else ILG_TRY(enqueue_step(c, o, c.sun_aux.p, 1, timing));
+    else ILG_TRY(enqueue_step(v, p, c.stream, timing ? c.ev : nullptr));
     if (timing) ILG_TRY(collect_stats(c, true));
     if (tsurf_out) {
       ILG_CUDA(cudaMemcpyAsync(c.pinned_tsurf, c.Tsurf.p, (size_t)c.nt * 8, cudaMemcpyDeviceToHost, c.stream));
@@ -521,23 +656,27 @@ int ilg_run_steps(ilg_ctx* ctx, const ilg_run_opts* opts, int first_sun, int nst
 int ilg_run_steps_host(ilg_ctx* ctx, const ilg_run_opts* opts, int nsteps, const double* suns, double* tsurf_out) {
   if (!ctx || (nsteps > 0 && !suns)) { set_error("invalid arguments"); return ILG_ERR_ARG; }
   Context& c = ctx->c;
-  ILG_TRY(check_run(c, opts));
-  ILG_TRY(ensure_pinned(c));
+  if (!opts) { set_error("opts is NULL"); return ILG_ERR_ARG; }
+  if (c.ndisk < 2) { set_error("sun disk samples are not set (ilg_set_suns)"); return ILG_ERR_ARG; }
+  if (!c.sun_aux.p) { ILG_TRY(c.sun_aux.alloc(1)); c.nsun = 0; }
+  ILG_TRY(check_run(c, opts, true));
   const ilg_run_opts& o = *opts;
-  int h2[2] = {0, c.frame_no};
-  ILG_CUDA(cudaMemcpyAsync(c.counters.p + 1, h2, sizeof(h2), cudaMemcpyHostToDevice, c.stream));
-  ILG_CUDA(cudaStreamSynchronize(c.stream));
+  MeshDesc M = solo_desc(c, &o, 0);
+  M.host_sun = 1;
+  ILG_TRY(upload_desc(c, M));
   bool timing = c.timing;
   cudaGraphExec_t g = nullptr;
   if (o.use_graph && !timing && !c.graph_broken)
-    if (get_graph(c, o, c.host_sun_aux.p, 0, true, &g) != ILG_OK) { c.graph_broken = true; g = nullptr; cudaGetLastError(); }
+    if (get_graph(c, o, true, &g) != ILG_OK) { c.graph_broken = true; g = nullptr; cudaGetLastError(); }
+  StepView v = solo_view(c, o.precision);
+  StepPlan p = solo_plan(c, o);
   for (int s = 0; s < nsteps; ++s) {
-    sun_aux_fill(c, suns + 3 * (size_t)s, 1, c.pinned_aux);
+    *(SunAux*)c.pinned_aux = make_sun_aux(suns + 3 * (size_t)s, c.solar_const, c.scene_mag, c.disk_rmax);
     if (g) {
       ILG_CUDA(cudaGraphLaunch(g, c.stream));
     } else {
-      ILG_CUDA(cudaMemcpyAsync(c.host_sun_aux.p, c.pinned_aux, sun_aux_bytes(), cudaMemcpyHostToDevice, c.stream));
-      ILG_TRY(enqueue_step(c, o, c.host_sun_aux.p, 0, timing));
+      ILG_CUDA(cudaMemcpyAsync(c.sun_aux.p + c.nsun, c.pinned_aux, sizeof(SunAux), cudaMemcpyHostToDevice, c.stream));
+      ILG_TRY(enqueue_step(v, p, c.stream, timing ? c.ev : nullptr));
       ILG_CUDA(cudaMemcpyAsync(c.pinned_tsurf, c.Tsurf.p, (size_t)c.nt * 8, cudaMemcpyDeviceToHost, c.stream));
     }
     ILG_CUDA(cudaStreamSynchronize(c.stream));
@@ -557,38 +696,32 @@ int ilg_bench_steps(ilg_ctx* ctx, const ilg_run_opts* opts, int first_sun, int n
                     double* step_ms, double* phase_ms) {
   if (!ctx || !step_ms) { set_error("invalid arguments"); return ILG_ERR_ARG; }
   Context& c = ctx->c;
-  ILG_TRY(check_run(c, opts));
+  ILG_TRY(check_run(c, opts, false));
   if (nsteps < 0 || first_sun < 0 || first_sun + nsteps > c.nsun) { set_error("sun range out of bounds"); return ILG_ERR_ARG; }
   const ilg_run_opts& o = *opts;
   size_t nflush = flush_mb > 0 ? (size_t)(flush_mb * 1048576.0 / 16.0) : 0;
   if (nflush) ILG_TRY(c.flush.reserve(nflush));
-  int h2[2] = {first_sun, c.frame_no};
-  ILG_CUDA(cudaMemcpyAsync(c.counters.p + 1, h2, sizeof(h2), cudaMemcpyHostToDevice, c.stream));
+  ILG_TRY(upload_desc(c, solo_desc(c, &o, first_sun)));
   cudaGraphExec_t g = nullptr;
   if (o.use_graph && !c.graph_broken)
-    if (get_graph(c, o, c.sun_aux.p, 1, false, &g) != ILG_OK) { c.graph_broken = true; g = nullptr; cudaGetLastError(); }
+    if (get_graph(c, o, false, &g) != ILG_OK) { c.graph_broken = true; g = nullptr; cudaGetLastError(); }
+  StepView v = solo_view(c, o.precision);
+  StepPlan p = solo_plan(c, o);
   cudaEvent_t a = c.ev[0], b = c.ev[3];
   if (phase_ms) phase_ms[0] = phase_ms[1] = phase_ms[2] = 0.0;
   for (int s = 0; s < nsteps; ++s) {
-    if (nflush) {
-      k_flush<<<4 * 152, 256, 0, c.stream>>>(c.flush.p, nflush, (unsigned)s);
-      ILG_CUDA(cudaGetLastError());
-    }
+    if (nflush) ILG_TRY(flush_launch(c.flush.p, nflush, (unsigned)s, c.stream));
     if (g) {
       ILG_CUDA(cudaEventRecord(a, c.stream));
       ILG_CUDA(cudaGraphLaunch(g, c.stream));
       ILG_CUDA(cudaEventRecord(b, c.stream));
     } else {
-      ILG_TRY(enqueue_step(c, o, c.sun_aux.p, 1, true));
+      ILG_TRY(enqueue_step(v, p, c.stream, c.ev));
     }
     ILG_CUDA(cudaEventSynchronize(b));
     float ms = 0.f;
     ILG_CUDA(cudaEventElapsedTime(&ms, a, b));
     step_ms[s] = ms;
-    int hc[4];
-    ILG_CUDA(cudaMemcpy(hc, c.counters.p, sizeof(hc), cudaMemcpyDeviceToHost));
-    c.stats_ambiguous += hc[0];
-    c.stats_sweeps += hc[3];
     if (!g) {
       float p0, p1, p2;
       ILG_CUDA(cudaEventElapsedTime(&p0, c.ev[0], c.ev[1]));
@@ -596,6 +729,7 @@ int ilg_bench_steps(ilg_ctx* ctx, const ilg_run_opts* opts, int first_sun, int n
       ILG_CUDA(cudaEventElapsedTime(&p2, c.ev[2], c.ev[3]));
       if (phase_ms) { phase_ms[0] += p0; phase_ms[1] += p1; phase_ms[2] += p2; }
     }
+    ILG_TRY(collect_stats(c, false));
   }
   ILG_CUDA(cudaStreamSynchronize(c.stream));
   c.frame_no += nsteps;

@@ -32,28 +32,48 @@ constexpr int COND_THREADS = 128;
 constexpr int TAB_W = 5;            // g, m, al, f, inv_beta per layer
 constexpr size_t SMEM_LIMIT = 160 * 1024;
 
+template <class R> R* rho_scratch_host(const StepView& v);
+template <> double* rho_scratch_host<double>(const StepView& v) { return v.rho64; }
+template <> float* rho_scratch_host<float>(const StepView& v) { return v.rho32; }
+
+template <class R> __device__ __forceinline__ R* state_T(const StepView& v);
+template <> __device__ __forceinline__ double* state_T<double>(const StepView& v) { return v.T64; }
+template <> __device__ __forceinline__ float* state_T<float>(const StepView& v) { return v.T32; }
+template <class R> __device__ __forceinline__ const R* coef_tab(const StepView& v);
+template <> __device__ __forceinline__ const double* coef_tab<double>(const StepView& v) { return v.coef64; }
+template <> __device__ __forceinline__ const float* coef_tab<float>(const StepView& v) { return v.coef32; }
+template <class R> __device__ __forceinline__ R* rho_scratch(const StepView& v);
+template <> __device__ __forceinline__ double* rho_scratch<double>(const StepView& v) { return v.rho64; }
+template <> __device__ __forceinline__ float* rho_scratch<float>(const StepView& v) { return v.rho32; }
+
+// One thread per facet column. Block b covers facets [cb.y, cb.y + 128) of
+// mesh cb.x. Q: the new time level's flux per facet.
 template <class R, bool SMEM>
 __global__ void __launch_bounds__(COND_THREADS)
-k_conduct(const R* __restrict__ tab, CondScalars cs, int nt, R* __restrict__ T, double* __restrict__ Tsurf,
-          double* __restrict__ Fsurf, double* __restrict__ Qprev, const double* __restrict__ Qnp1,
-          R* __restrict__ rho_g, int upd, double* __restrict__ rad_avg, double* __restrict__ therm_avg,
-          double* __restrict__ therm_max, const int* __restrict__ frame_ptr, int frame_host,
-          int* __restrict__ derr) {
+k_conduct(StepView v, const double* __restrict__ Qnp1, int upd) {
   extern __shared__ unsigned char smem_raw[];
   R* rho_s = reinterpret_cast<R*>(smem_raw);
-  int f = blockIdx.x * COND_THREADS + threadIdx.x;
-  if (f >= nt) return;
+  int2 cb = v.cblocks ? v.cblocks[blockIdx.x] : make_int2(0, blockIdx.x * COND_THREADS);
+  const MeshDesc& M = v.md[cb.x];
+  if (!M.active) return;
+  int fl = cb.y + threadIdx.x;
+  if (fl >= M.nfacet) return;
+  const int g = M.facet0 + fl;
+  const CondScalars cs = M.cs;
   const int nz = cs.nz;
-  const size_t N = (size_t)nt;
-#define RHO(i) (SMEM ? rho_s[(size_t)(i) * COND_THREADS + threadIdx.x] : rho_g[(size_t)(i) * N + f])
+  const size_t N = (size_t)M.nfacet;
+  R* __restrict__ T = state_T<R>(v) + M.T0 + fl;
+  const R* __restrict__ tab = coef_tab<R>(v) + M.coef0;
+  R* __restrict__ rho_g = SMEM ? nullptr : rho_scratch<R>(v) + g;
+#define RHO(i) (SMEM ? rho_s[(size_t)(i) * COND_THREADS + threadIdx.x] : rho_g[(size_t)(i) * v.nt])
   // upward pass
-  R Tip1 = T[(size_t)(nz - 1) * N + f];
-  R Ti = T[(size_t)(nz - 2) * N + f];
-  const R* cb = tab + (size_t)(nz - 1) * TAB_W;
-  R rho_next = cb[0] * Ti + cb[1] * Tip1 + (R)cs.cgeo;
+  R Tip1 = T[(size_t)(nz - 1) * N];
+  R Ti = T[(size_t)(nz - 2) * N];
+  const R* cb_t = tab + (size_t)(nz - 1) * TAB_W;
+  R rho_next = cb_t[0] * Ti + cb_t[1] * Tip1 + (R)cs.cgeo;
   RHO(nz - 1) = rho_next;
   for (int i = nz - 2; i >= 1; --i) {
-    R Tim1 = T[(size_t)(i - 1) * N + f];
+    R Tim1 = T[(size_t)(i - 1) * N];
     const R* c = tab + (size_t)i * TAB_W;
     R r = c[0] * Tim1 + c[1] * Ti + c[2] * Tip1;
     R rh = r - c[3] * rho_next;
@@ -64,11 +84,11 @@ k_conduct(const R* __restrict__ tab, CondScalars cs, int nt, R* __restrict__ T, 
   }
   // top row (Ti = T_1, Tip1 = T_2 in the Fortran's numbering)
   double T0 = (double)Ti, T1 = (double)Tip1, rho1 = (double)rho_next;
-  double Ts = Tsurf[f];
-  double Q = Qnp1[f];
+  double Ts = v.Tsurf[g];
+  double Q = Qnp1[g];
   double T0n, Tsn;
   if (cs.bc == 0) {
-    double Qn = Qprev[f];
+    double Qn = v.Qprev[g];
     double Tr3 = Ts * Ts * Ts;
     double arad = -3.0 * cs.es * Tr3 * Ts;
     double brad = 2.0 * cs.es * Tr3;
@@ -77,7 +97,7 @@ k_conduct(const R* __restrict__ tab, CondScalars cs, int nt, R* __restrict__ T, 
     double b0 = 1.0 + cs.alpha0 + cs.gamma0 - cs.gamma0 * bn;
     double r0 = cs.gamma0 * (annp1 + ann) + (1.0 - cs.alpha0 - cs.gamma0 + cs.gamma0 * bn) * T0 + cs.alpha0 * T1;
     double piv = b0 + cs.f0 * cs.gamma1;
-    if (piv == 0.0) { atomicExch(&derr[DERR_PIVOT], 1); return; }
+    if (piv == 0.0) { atomicExch(&v.derr[DERR_PIVOT], 1); return; }
     T0n = (r0 - cs.f0 * rho1) / piv;
     Tsn = 0.5 * (annp1 + bn * T0n + T0n);
   } else if (cs.bc == 1) {
@@ -88,9 +108,9 @@ k_conduct(const R* __restrict__ tab, CondScalars cs, int nt, R* __restrict__ T, 
     double tolr = sizeof(R) == 8 ? 1e-13 : 1e-9;
     for (int it = 0; it < 30; ++it) {
       double x3 = x * x * x;
-      double g = Q + 2.0 * cs.k1 * (P + (S - 1.0) * x) - cs.es * x3 * x;
+      double gx = Q + 2.0 * cs.k1 * (P + (S - 1.0) * x) - cs.es * x3 * x;
       double dg = 2.0 * cs.k1 * (S - 1.0) - 4.0 * cs.es * x3;
-      double dT = g / dg;
+      double dT = gx / dg;
       x -= dT;
       if (fabs(dT) <= tolr * fabs(x)) break;
     }
@@ -106,25 +126,24 @@ k_conduct(const R* __restrict__ tab, CondScalars cs, int nt, R* __restrict__ T, 
   double Fs = -cs.k0 * (T0n - Tsn) / cs.z0;
   // downward pass
   R prev = (R)T0n;
-  T[f] = prev;
+  T[0] = prev;
   for (int i = 1; i < nz; ++i) {
     const R* c = tab + (size_t)i * TAB_W;
     R t = (RHO(i) + c[0] * prev) * c[4];
-    T[(size_t)i * N + f] = t;
+    T[(size_t)i * N] = t;
     prev = t;
   }
 #undef RHO
-  Fsurf[f] = Fs;
+  v.Fsurf[g] = Fs;
   if (cs.bc != 2) {
-    Tsurf[f] = Tsn;
-    Qprev[f] = Q;
+    v.Tsurf[g] = Tsn;
+    v.Qprev[g] = Q;
   }
   if (upd) {
-    int frame = frame_ptr ? *frame_ptr : frame_host;
-    double inv = (double)(frame + 1);
-    rad_avg[f] += (Q - rad_avg[f]) / inv;
-    therm_avg[f] += (Tsn - therm_avg[f]) / inv;
-    if (frame > 50) therm_max[f] = fmax(therm_max[f], Tsn);
+    double inv = (double)(M.frame + 1);
+    v.rad_avg[g] += (Q - v.rad_avg[g]) / inv;
+    v.therm_avg[g] += (Tsn - v.therm_avg[g]) / inv;
+    if (M.frame > 50) v.therm_max[g] = fmax(v.therm_max[g], Tsn);
   }
 }
 
@@ -200,18 +219,15 @@ int build_tables(int nz, const double* z, const double* ti, const double* rhoc, 
 }
 
 template <class R>
-int launch_conduct(const R* tab, const CondScalars& cs, int nt, R* T, double* Tsurf, double* Fsurf, double* Qprev,
-                   const double* Qnp1, dbuf<R>& rho_scratch, int upd, double* rad_avg, double* therm_avg,
-                   double* therm_max, const int* frame_ptr, int frame_host, int* derr, cudaStream_t s) {
-  size_t smem = (size_t)cs.nz * COND_THREADS * sizeof(R);
-  int grid = div_up(nt, COND_THREADS);
+int launch_conduct(const StepView& v, const double* Q, int upd, int nz_max, cudaStream_t s) {
+  size_t smem = (size_t)nz_max * COND_THREADS * sizeof(R);
+  int grid = v.cblocks ? v.ncblocks : div_up(v.nt, COND_THREADS);
+  if (grid <= 0) return ILG_OK;
   if (smem <= SMEM_LIMIT) {
-    k_conduct<R, true><<<grid, COND_THREADS, smem, s>>>(tab, cs, nt, T, Tsurf, Fsurf, Qprev, Qnp1, nullptr, upd,
-                                                        rad_avg, therm_avg, therm_max, frame_ptr, frame_host, derr);
+    k_conduct<R, true><<<grid, COND_THREADS, smem, s>>>(v, Q, upd);
   } else {
-    ILG_TRY(rho_scratch.reserve((size_t)cs.nz * nt));
-    k_conduct<R, false><<<grid, COND_THREADS, 0, s>>>(tab, cs, nt, T, Tsurf, Fsurf, Qprev, Qnp1, rho_scratch.p, upd,
-                                                      rad_avg, therm_avg, therm_max, frame_ptr, frame_host, derr);
+    if (!rho_scratch_host<R>(v)) { set_error("conduction: %d layers need the deep-column scratch", nz_max); return ILG_ERR_ARG; }
+    k_conduct<R, false><<<grid, COND_THREADS, 0, s>>>(v, Q, upd);
   }
   ILG_CUDA(cudaGetLastError());
   return ILG_OK;
@@ -268,16 +284,9 @@ int conduction_state_convert(Context& c, int precision) {
   return ILG_OK;
 }
 
-int conduction_launch(Context& c, const double* Q_dev, int precision, bool update_outputs) {
-  const CondScalars& cs = c.cond_cs;
-  ILG_TRY(conduction_state_convert(c, precision));
-  if (precision == ILG_PREC_MIXED)
-    return launch_conduct<float>(c.coef32.p, cs, c.nt, c.T32.p, c.Tsurf.p, c.Fsurf.p, c.Qprev.p, Q_dev, c.rho32,
-                                 update_outputs ? 1 : 0, c.rad_avg.p, c.therm_avg.p, c.therm_max.p,
-                                 c.counters.p + 2, 0, c.derr.p, c.stream);
-  return launch_conduct<double>(c.coef64.p, cs, c.nt, c.T64.p, c.Tsurf.p, c.Fsurf.p, c.Qprev.p, Q_dev, c.rho64,
-                                update_outputs ? 1 : 0, c.rad_avg.p, c.therm_avg.p, c.therm_max.p,
-                                c.counters.p + 2, 0, c.derr.p, c.stream);
+int conduction_launch(const StepView& v, const double* Q, int precision, int upd, int nz_max, cudaStream_t s) {
+  if (precision == ILG_PREC_MIXED) return launch_conduct<float>(v, Q, upd, nz_max, s);
+  return launch_conduct<double>(v, Q, upd, nz_max, s);
 }
 
 // Standalone batched columns (host arrays, reference layout: column-major
@@ -293,9 +302,9 @@ static int run_columns(int ncol, int nz, const double* z, double dt, const doubl
   cudaStream_t s;
   ILG_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
   struct StreamGuard { cudaStream_t s; ~StreamGuard() { cudaStreamDestroy(s); } } guard{s};
-  dbuf<double> dtab, dT, dTs, dFs, dQn, dQ;
+  dbuf<double> dtab, dT, dTs, dFs, dQn, dQ, rho;
   dbuf<int> derr;
-  dbuf<double> rho;
+  dbuf<MeshDesc> dmd;
   ILG_TRY(dtab.alloc(tab.size()));
   ILG_TRY(dT.alloc((size_t)nz * ncol));
   ILG_TRY(dTs.alloc(ncol));
@@ -303,9 +312,15 @@ static int run_columns(int ncol, int nz, const double* z, double dt, const doubl
   ILG_TRY(dQn.alloc(ncol));
   ILG_TRY(dQ.alloc(ncol));
   ILG_TRY(derr.alloc(DERR_COUNT));
+  ILG_TRY(dmd.alloc(1));
+  size_t smem = (size_t)nz * 128 * sizeof(double);
+  if (smem > SMEM_LIMIT) ILG_TRY(rho.alloc((size_t)nz * ncol));
+  MeshDesc md{};
+  md.facet0 = 0; md.nfacet = ncol; md.nz = nz; md.coef0 = 0; md.T0 = 0; md.cs = cs; md.active = 1;
   std::vector<double> Tl((size_t)nz * ncol);
   for (int f = 0; f < ncol; ++f)
     for (int i = 0; i < nz; ++i) Tl[(size_t)i * ncol + f] = T[(size_t)f * nz + i];
+  ILG_CUDA(cudaMemcpyAsync(dmd.p, &md, sizeof(md), cudaMemcpyHostToDevice, s));
   ILG_CUDA(cudaMemcpyAsync(dtab.p, tab.data(), tab.size() * 8, cudaMemcpyHostToDevice, s));
   ILG_CUDA(cudaMemcpyAsync(dT.p, Tl.data(), Tl.size() * 8, cudaMemcpyHostToDevice, s));
   ILG_CUDA(cudaMemcpyAsync(dTs.p, Tsurf, (size_t)ncol * 8, cudaMemcpyHostToDevice, s));
@@ -313,8 +328,11 @@ static int run_columns(int ncol, int nz, const double* z, double dt, const doubl
   if (Qn) ILG_CUDA(cudaMemcpyAsync(dQn.p, Qn, (size_t)ncol * 8, cudaMemcpyHostToDevice, s));
   else ILG_CUDA(cudaMemsetAsync(dQn.p, 0, (size_t)ncol * 8, s));
   ILG_CUDA(cudaMemsetAsync(derr.p, 0, DERR_COUNT * sizeof(int), s));
-  ILG_TRY(launch_conduct<double>(dtab.p, cs, ncol, dT.p, dTs.p, dFs.p, dQn.p, dQ.p, rho, 0, nullptr, nullptr, nullptr,
-                                 nullptr, 0, derr.p, s));
+  StepView v{};
+  v.nt = ncol; v.nmesh = 1; v.md = dmd.p;
+  v.Tsurf = dTs.p; v.Fsurf = dFs.p; v.Qprev = dQn.p; v.T64 = dT.p; v.coef64 = dtab.p; v.rho64 = rho.p;
+  v.derr = derr.p;
+  ILG_TRY(launch_conduct<double>(v, dQ.p, 0, nz, s));
   int herr[DERR_COUNT];
   ILG_CUDA(cudaMemcpyAsync(Tl.data(), dT.p, Tl.size() * 8, cudaMemcpyDeviceToHost, s));
   if (bc != 2) ILG_CUDA(cudaMemcpyAsync(Tsurf, dTs.p, (size_t)ncol * 8, cudaMemcpyDeviceToHost, s));

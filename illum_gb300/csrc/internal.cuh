@@ -42,6 +42,79 @@ struct CondScalars {
   int nz, bc;                        // bc: 0 linearised, 1 Newton, 2 prescribed Ts (conductionT)
 };
 
+// Per sun position, precomputed on the host (direct.cu make_sun_aux).
+struct SunAux {
+  double sx, sy, sz;     // position (km)
+  double flux;           // solar_const * (AU / |S|)^2
+  float ux, uy, uz;      // unit direction S / |S|
+  float alpha;           // bound on the disk samples' angular offset
+  float mu_eps;          // bound on |mu32 - mu64|
+  float ang_eps;         // bound on the angle between S/|S| and S - p
+};
+
+// One mesh of a scene: where its facets, horizons, layers, suns and
+// radiosity slices live in the scene's arrays, and its run state. The step
+// kernels read it from device memory, so a captured step graph stays valid
+// while meshes advance, finish or are switched off.
+struct MeshDesc {
+  int facet0, nfacet;          // facet range in the scene
+  int nphi, interp;
+  int64_t H0;                  // offset of the mesh's horizons (nphi per facet)
+  double dphi, denom;          // azimuth step; lit-count divisor
+  int nsamp, coupling;         // sun-disk samples used; ILG_COUPLE_*
+  int sun0, nsun;              // the mesh's sun table in the scene's table
+  int sun_idx, frame;          // current sun index and frame (advanced per step)
+  int host_sun, host_slot;     // 1: take the sun from host_slot (host-driven steps)
+  int nz, coef0;               // layers; offset of the conduction table
+  int64_t T0;                  // offset of the mesh's [nz][nfacet] layer block
+  CondScalars cs;
+  int slice0, nslices;         // radiosity SELL slices
+  int chunk0, nchunks;         // residual-reduction chunks of the slices
+  double tol2;                 // squared residual tolerance
+  int max_sweeps;
+  int sweeps;                  // out: sweeps of the last solve
+  double res2;                 // out: squared residual bound of the last solve
+  int active;                  // 0: skipped by the step kernels
+  int done_steps;              // steps taken since the run started
+};
+
+// Everything a step kernel touches, as plain device pointers.
+struct StepView {
+  int nt, nmesh;
+  MeshDesc* md;
+  const int* mesh_of;          // per facet, or nullptr for a single mesh
+  const float4 *cen, *nrm, *frame32;
+  const double *frame, *H, *hmin, *hmax, *disk;
+  int ndisk;
+  const SunAux* suns;
+  double *Tsurf, *Fsurf, *Qprev, *rad, *rad_avg, *therm_avg, *therm_max, *E, *xtmp, *xprev;
+  float* x32;                  // 3 x nt (mixed radiosity)
+  double* T64;
+  float* T32;
+  const double* coef64;
+  const float* coef32;
+  // radiosity SELL-32
+  const int64_t* sl_ptr;
+  const int32_t *sl_len, *sl_split, *sl_mesh, *ln_row, *ln_m, *s_col;
+  const double* s_val;
+  const __nv_bfloat16* s_vbf;
+  const float* rscale;
+  const uint8_t* row_act;      // per facet: its row has entries
+  int nslices;
+  // conduction blocks: (mesh, first local facet), or nullptr for a single mesh
+  const int2* cblocks;
+  int ncblocks;
+  // residual-reduction chunks: (first slice, count, mesh, 0)
+  const int4* chunks;
+  int nchunks;
+  // scratch
+  int *work, *counters, *derr, *mesh_flag;
+  double *sl_d2, *ch_d2;
+  unsigned* barrier;
+  double* rho64;               // deep-column conduction scratch [nz][nt] (or nullptr)
+  float* rho32;
+};
+
 struct Context {
   int nt = 0;
   cudaStream_t stream = nullptr;
@@ -84,6 +157,7 @@ struct Context {
   dbuf<int32_t> sell_len, sell_split, sell_row, sell_m, sell_col;
   dbuf<double> sell_val;
   dbuf<__nv_bfloat16> sell_vbf;
+  dbuf<uint8_t> row_act;
 
   // thermal
   bool have_thermal = false;
@@ -108,21 +182,23 @@ struct Context {
 
   // suns and step machinery
   int nsun = 0;
-  dbuf<double> suns;              // nsun x 3
+  std::vector<double> suns_h;     // nsun x 3 positions (to rebuild the table)
   dbuf<double> disk;              // ndisk x 2 column-major
   int ndisk = 0;
   double disk_rmax = 0.0;
   dbuf<int> work;                 // ambiguous facets
   dbuf<int> counters;             // [0] work count, [1] step (sun index), [2] frame, [3] sweeps
   dbuf<int> derr;                 // DERR_COUNT error flags
-  dbuf<double> partials;          // radiosity residual partials (2 x grid + 1)
   dbuf<unsigned> barrier;         // grid barrier state of the radiosity kernel
   dbuf<float> x32;                // mixed-precision radiosity iterates (3 x N)
-  int rad_grid = 0;
-  int rad_grid_prec = -1;
-  dbuf<unsigned char> sun_aux;    // per-sun precomputed data (direct.cu SunAux)
-  dbuf<unsigned char> host_sun_aux;  // one entry for host-driven steps
+  dbuf<SunAux> sun_aux;           // nsun entries + the host slot
   unsigned char* pinned_aux = nullptr;
+  MeshDesc mh{};                  // host mirror of the one-mesh descriptor
+  dbuf<MeshDesc> md;
+  dbuf<int> mesh_flag;
+  dbuf<double> sl_d2, ch_d2;
+  dbuf<int4> chunks;
+  int nchunks = 0;
   double* pinned_tsurf = nullptr;
   int64_t stats_ambiguous = 0, stats_sweeps = 0;
   bool timing = false;
@@ -143,6 +219,14 @@ struct Context {
   ~Context();
 };
 
+// What one step launches (capi.cu enqueue_step).
+struct StepPlan {
+  int precision;
+  bool rad_on;
+  int rad_grid;
+  int nz_max;
+};
+
 // ---- bvh.cu ----
 int bvh_build(Context& c, const float* verts_h, int nv, const int32_t* tris_h, const float* normals_h);
 int bvh_trace(Context& c, int nrays, const float* orig_h, const float* dir_h, int any_hit, int32_t* hit_h,
@@ -152,24 +236,30 @@ int form_factors_build(Context& c, const double* albedo_h, double albedo_scalar,
                        int64_t* rays_out);
 
 // ---- direct.cu ----
-int sun_aux_bytes();
-int sun_aux_fill(const Context& c, const double* suns_h, int nsun, void* out_h);
-int direct_launch_aux(Context& c, const void* suns_dev, int from_counter, const double* base_neg,
-                      double* out_dev);
+SunAux make_sun_aux(const double* s, double solar_const, double scene_mag, double disk_rmax);
+int direct_launch(const StepView& v, int dropin, cudaStream_t s);
 
 // ---- radiosity.cu ----
 int radiosity_prepare(Context& c);
-int radiosity_setup(Context& c, int precision);
-int radiosity_launch(Context& c, const double* E_dev, double* x_dev, double tol, int max_sweeps,
-                     int precision, bool warm_start);
+int radiosity_grid(int nslices, int precision);
+int radiosity_chunk();
+int radiosity_max_meshes();
+int radiosity_launch(const StepView& v, double* x, int warm, int precision, int grid, cudaStream_t s);
 
 // ---- capi.cu ----
 int read_device_errors(Context& c);
+int check_run(Context& c, const ilg_run_opts* o, bool host_driven);
+MeshDesc solo_desc(const Context& c, const ilg_run_opts* o, int first_sun);
+int enqueue_step(const StepView& v, const StepPlan& p, cudaStream_t s, cudaEvent_t* ev);
+int advance_launch(const StepView& v, cudaStream_t s);
+int flush_launch(float4* buf, size_t n, unsigned salt, cudaStream_t s);
 
 // ---- conduction.cu ----
 int conduction_prepare(Context& c, double dt, int precision);
 int conduction_setup();
-int conduction_launch(Context& c, const double* Q_dev, int precision, bool update_outputs);
+// Q: heat flux at the new time level per facet (global index); upd: also
+// update rad_avg / therm_avg / therm_max; nz_max: deepest mesh of the view.
+int conduction_launch(const StepView& v, const double* Q, int precision, int upd, int nz_max, cudaStream_t s);
 int conduction_state_convert(Context& c, int precision);
 int conduction_batch_host(int ncol, int nz, const double* z, double dt, const double* Qn, const double* Qnp1,
                           double* T, const double* ti, const double* rhoc, double emiss, double* Tsurf,
@@ -178,3 +268,7 @@ int conductiont_host(int nz, const double* z, double dt, double* T, double Tsurf
                      const double* ti, const double* rhoc, double Fgeo, double* Fsurf);
 
 }  // namespace ilg
+
+struct ilg_ctx {
+  ilg::Context c;
+};

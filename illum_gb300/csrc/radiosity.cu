@@ -32,43 +32,7 @@ namespace ilg {
 
 namespace {
 
-constexpr int RAD_THREADS = 512;
-constexpr int RAD_WARPS = RAD_THREADS / 32;
-
-struct RadArgs {
-  // SELL-32 copy of the active rows (see radiosity_prepare)
-  const int64_t* sl_ptr;    // per slice: offset of its first element
-  const int32_t* sl_len;    // per slice: elements per lane (multiple of 4)
-  const int32_t* sl_split;  // per slice: largest chunk count of its rows (1: no split rows)
-  const int32_t* ln_row;    // per lane: row, or -1 (padding lane)
-  const int32_t* ln_m;      // per lane: chunks of its row if it is the row's first lane, else 0
-  const int32_t* s_col;
-  const double* s_val;
-  const __nv_bfloat16* s_vbf;
-  int nslices;
-  const int64_t* rowptr;
-  const int32_t* col;
-  const double* val;
-  const __nv_bfloat16* vbf;
-  const float* rscale;
-  const int32_t* active;
-  int n_active, nt;
-  const double* E;
-  double* x;       // result (and warm start)
-  double* xt;      // second iterate buffer
-  double* xprev;   // solution of the step before (extrapolated warm start)
-  float* x32a;     // fp32 iterate buffers (mixed)
-  float* x32b;
-  float* r32;      // fp32 correction right-hand side (mixed)
-  double tol2;
-  int max_sweeps;
-  int warm;
-  int mixed;
-  double* partials;   // 2 x gridDim.x
-  unsigned* bar;      // [0] arrival count, [1] generation
-  int* counters;
-  int* derr;
-};
+constexpr int RAD_THREADS = 1024;
 
 // Grid barrier for a cooperative launch (all blocks co-resident). The wait
 // is bounded: after ~2^26 polls it records DERR_BARRIER and returns false.
@@ -101,77 +65,50 @@ __device__ bool grid_barrier(unsigned* bar, unsigned nblocks, int* derr) {
   return ok != 0;
 }
 
-__device__ __forceinline__ double block_sum(double v, double* sh) {
-  for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  __syncthreads();
-  if (lane == 0) sh[w] = v;
-  __syncthreads();
-  double t = 0.0;
-  for (int i = 0; i < RAD_WARPS; ++i) t += sh[i];
-  return t;
-}
-
-// Sum of the grid's partials in a fixed order (same value in every block).
-__device__ __forceinline__ double grid_total(const double* part, int nb, double* sh) {
-  double v = 0.0;
-  for (int b = threadIdx.x; b < nb; b += RAD_THREADS) v += part[b];
-  // fixed-order tree: warp shuffles then warps in order
-  return block_sum(v, sh);
-}
-
-// sum_k val[k] * x[col[k]] over one row, lanes strided, four independent
-// loads per lane in flight; fixed summation order (deterministic).
-template <class V, class X, class Acc>
-__device__ __forceinline__ Acc row_dot(const int32_t* __restrict__ col, const V* __restrict__ val,
-                                       const X* __restrict__ x, int64_t b, int64_t e, int lane) {
-  Acc s = 0;
-  for (int64_t k0 = b; k0 < e; k0 += 128) {
-    int c[4];
-    V v[4];
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      int64_t k = k0 + lane + 32 * j;
-      bool ok = k < e;
-      c[j] = ok ? __ldg(col + k) : 0;
-      v[j] = ok ? __ldg(val + k) : V(0);
-    }
-    X xv[4];
-#pragma unroll
-    for (int j = 0; j < 4; ++j) xv[j] = x[c[j]];
-#pragma unroll
-    for (int j = 0; j < 4; ++j) s += (Acc)v[j] * (Acc)xv[j];
-  }
-  for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-  return s;
-}
+__device__ __forceinline__ int mesh_of_facet(const StepView& v, int g) { return v.mesh_of ? v.mesh_of[g] : 0; }
+__device__ __forceinline__ int mesh_of_slice(const StepView& v, int sl) { return v.sl_mesh ? v.sl_mesh[sl] : 0; }
 
 // One SELL-32 slice: lane l accumulates its (chunk of a) row sequentially
 // (four independent loads in flight), then rows split into several chunks
 // are combined into their first lane in a fixed order.
 template <class V, class X, class Acc>
-__device__ __forceinline__ Acc slice_dot(const RadArgs& a, const V* __restrict__ sval, const X* __restrict__ x,
+__device__ __forceinline__ Acc slice_dot(const StepView& v, const V* __restrict__ sval, const X* __restrict__ x,
                                          int sl, int lane) {
-  int64_t base = a.sl_ptr[sl] + lane;
-  int len = a.sl_len[sl];
+  int64_t base = v.sl_ptr[sl] + lane;
+  int len = v.sl_len[sl];
   Acc p = 0;
-  for (int k = 0; k < len; k += 4) {
+  int k = 0;
+  for (; k + 8 <= len; k += 8) {
+    int c[8];
+    V w[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      c[j] = __ldg(v.s_col + base + (int64_t)(k + j) * 32);
+      w[j] = __ldg(sval + base + (int64_t)(k + j) * 32);
+    }
+    X xv[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) xv[j] = x[c[j]];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) p += (Acc)w[j] * (Acc)xv[j];
+  }
+  if (k < len) {   // len is a multiple of 4
     int c[4];
-    V v[4];
+    V w[4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-      c[j] = __ldg(a.s_col + base + (int64_t)(k + j) * 32);
-      v[j] = __ldg(sval + base + (int64_t)(k + j) * 32);
+      c[j] = __ldg(v.s_col + base + (int64_t)(k + j) * 32);
+      w[j] = __ldg(sval + base + (int64_t)(k + j) * 32);
     }
     X xv[4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) xv[j] = x[c[j]];
 #pragma unroll
-    for (int j = 0; j < 4; ++j) p += (Acc)v[j] * (Acc)xv[j];
+    for (int j = 0; j < 4; ++j) p += (Acc)w[j] * (Acc)xv[j];
   }
-  int mmax = a.sl_split[sl];
+  int mmax = v.sl_split[sl];
   if (mmax > 1) {
-    int m = a.ln_m[(int64_t)sl * 32 + lane];
+    int m = v.ln_m[(int64_t)sl * 32 + lane];
     Acc tot = p;
     for (int j = 1; j < mmax; ++j) {
       Acc q = __shfl_down_sync(0xffffffffu, p, j);
@@ -182,144 +119,202 @@ __device__ __forceinline__ Acc slice_dot(const RadArgs& a, const V* __restrict__
   return p;
 }
 
-// FP64 Jacobi to tolerance.
-__global__ void __launch_bounds__(RAD_THREADS, 2) k_radiosity64(RadArgs a) {
-  __shared__ double sh[RAD_WARPS];
-  const int lane = threadIdx.x & 31;
-  const int gw = (blockIdx.x * RAD_THREADS + threadIdx.x) >> 5;
-  const int nwarps = (gridDim.x * RAD_THREADS) >> 5;
-  const int gt = blockIdx.x * RAD_THREADS + threadIdx.x;
-  const int nthreads = gridDim.x * RAD_THREADS;
-  // all rows: both buffers start at E (inactive rows keep it); active rows
-  // of x keep the previous solution when warm-starting
-  // warm start: x_{n-1} (or 2 x_{n-1} - x_{n-2} once two solutions exist)
-  const bool extrap = a.warm && a.counters[2] >= 2;
-  for (int i = gt; i < a.nt; i += nthreads) {
-    double e = a.E[i];
-    a.xt[i] = e;
-    bool act = a.rowptr[i + 1] != a.rowptr[i];
-    if (!a.warm || !act) {
-      a.x[i] = e;
+__device__ __forceinline__ double warp_sum(double x) {
+  for (int o = 16; o; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+  return x;
+}
+
+// Per-mesh convergence. Residual partials are reduced in a fixed order that
+// depends only on the mesh's own slices: each slice's partial (warp sum),
+// then chunks of RAD_CHUNK consecutive slices of the mesh (one warp per
+// chunk), then the mesh's chunks in order. Every block repeats the last
+// stage for every mesh and keeps the stop flags in shared memory, so all
+// blocks take the same decisions without another barrier, and a mesh's
+// decisions are the same alone and in a batch.
+constexpr int RAD_CHUNK = 256;
+constexpr int RAD_MAX_MESH = 1024;
+
+struct MeshState {
+  int done[RAD_MAX_MESH];
+  int sweeps[RAD_MAX_MESH];
+};
+
+__device__ __forceinline__ void init_meshes(const StepView& v, MeshState& st) {
+  for (int m = threadIdx.x; m < v.nmesh; m += blockDim.x) {
+    const MeshDesc& M = v.md[m];
+    st.done[m] = (M.active && M.nslices > 0) ? 0 : 1;
+    st.sweeps[m] = 0;
+  }
+}
+
+// chunk sums of all meshes still running (one warp per chunk)
+__device__ __forceinline__ void chunk_sums(const StepView& v, const MeshState& st, int gw, int nwarps, int lane) {
+  for (int k = gw; k < v.nchunks; k += nwarps) {
+    int4 ch = v.chunks[k];   // (first slice, count, mesh, -)
+    if (st.done[ch.z]) continue;
+    double t = 0.0;
+    for (int j = lane; j < ch.y; j += 32) t += v.sl_d2[ch.x + j];
+    t = warp_sum(t);
+    if (lane == 0) v.ch_d2[k] = t;
+  }
+}
+
+// Every block: totals per running mesh (its chunks in order), stop
+// decisions, and the number of meshes still running. Block 0 records the
+// sweep counts and residuals in the mesh table.
+__device__ __forceinline__ int decide_meshes(const StepView& v, MeshState& st, int inc, int first) {
+  __syncthreads();
+  for (int m = threadIdx.x; m < v.nmesh; m += blockDim.x) {
+    if (st.done[m]) continue;
+    const MeshDesc& M = v.md[m];
+    double t = 0.0;
+    for (int c = 0; c < M.nchunks; ++c) t += v.ch_d2[M.chunk0 + c];
+    int sw = st.sweeps[m] + (first ? 0 : inc);
+    st.sweeps[m] = sw;
+    bool stop = t <= M.tol2 || sw >= M.max_sweeps;
+    if (stop) st.done[m] = 1;
+    if (blockIdx.x == 0) {
+      v.md[m].sweeps = sw;
+      v.md[m].res2 = t;
+    }
+  }
+  __syncthreads();
+  int running = 0;
+  for (int m0 = 0; m0 < v.nmesh; m0 += blockDim.x) {
+    int m = m0 + threadIdx.x;
+    running += __syncthreads_count(m < v.nmesh && !st.done[m]);
+  }
+  return running;
+}
+
+// Start values: rows without entries are x = E exactly; the others start at
+// E (cold) or at the mesh's previous solution, extrapolated linearly once two
+// solutions exist (warm).
+__device__ __forceinline__ void init_x(const StepView& v, double* x, int warm, int gt, int nthreads) {
+  for (int g = gt; g < v.nt; g += nthreads) {
+    const MeshDesc& M = v.md[mesh_of_facet(v, g)];
+    if (!M.active || M.nslices == 0) continue;
+    double e = v.E[g];
+    v.xtmp[g] = e;
+    if (!warm || !v.row_act[g]) {
+      x[g] = e;
     } else {
-      double xn = a.x[i];
-      if (extrap) a.x[i] = 2.0 * xn - a.xprev[i];
-      a.xprev[i] = xn;
+      double xn = x[g];
+      if (M.frame >= 2) x[g] = 2.0 * xn - v.xprev[g];
+      v.xprev[g] = xn;
     }
-  }
-  if (!grid_barrier(a.bar, gridDim.x, a.derr)) return;
-  double* cur = a.x;
-  double* nxt = a.xt;
-  int sweeps = 0;
-  for (;;) {
-    double d2 = 0.0;
-    for (int sl = gw; sl < a.nslices; sl += nwarps) {
-      double s = slice_dot<double, double, double>(a, a.s_val, cur, sl, lane);
-      int64_t li = (int64_t)sl * 32 + lane;
-      if (a.ln_m[li] > 0) {
-        int i = a.ln_row[li];
-        double xn = a.E[i] + s;
-        double df = xn - cur[i];
-        nxt[i] = xn;
-        d2 += df * df;
-      }
-    }
-    ++sweeps;
-    double bs = block_sum(d2, sh);
-    double* part = a.partials + (sweeps & 1) * gridDim.x;
-    if (threadIdx.x == 0) part[blockIdx.x] = bs;
-    if (!grid_barrier(a.bar, gridDim.x, a.derr)) return;
-    double tot = grid_total(part, gridDim.x, sh);
-    double* t = cur; cur = nxt; nxt = t;
-    if (tot <= a.tol2 || sweeps >= a.max_sweeps) {
-      if (blockIdx.x == 0 && threadIdx.x == 0) {
-        a.counters[3] = sweeps;
-        a.partials[2 * gridDim.x] = tot;
-      }
-      break;
-    }
-  }
-  // make sure the final iterate is in x
-  if (cur != a.x) {
-    for (int w = gt; w < a.n_active; w += nthreads) {
-      int i = a.active[w];
-      a.x[i] = cur[i];
+    if (v.x32) {
+      v.x32[g] = 0.f;
+      v.x32[v.nt + g] = 0.f;
     }
   }
 }
 
-// Mixed precision: outer refinement with an fp64 residual r = E - (I - F) x
-// (fp64 values), inner fp32 Jacobi on (I - F~) d = r with bf16 F~, x += d.
-// The outer loop stops when ||r||_2 <= tol.
-__global__ void __launch_bounds__(RAD_THREADS, 2) k_radiosity_mixed(RadArgs a) {
-  __shared__ double sh[RAD_WARPS];
+// FP64 Jacobi to each mesh's tolerance. x: solution (and warm start).
+__global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity64(StepView v, double* x, int warm) {
+  __shared__ MeshState st;
   const int lane = threadIdx.x & 31;
   const int gw = (blockIdx.x * RAD_THREADS + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * RAD_THREADS) >> 5;
   const int gt = blockIdx.x * RAD_THREADS + threadIdx.x;
   const int nthreads = gridDim.x * RAD_THREADS;
-  const bool extrap = a.warm && a.counters[2] >= 2;
-  for (int i = gt; i < a.nt; i += nthreads) {
-    bool act = a.rowptr[i + 1] != a.rowptr[i];
-    if (!a.warm || !act) {
-      a.x[i] = a.E[i];
-    } else {
-      double xn = a.x[i];
-      if (extrap) a.x[i] = 2.0 * xn - a.xprev[i];
-      a.xprev[i] = xn;
-    }
-    a.x32a[i] = 0.f;
-    a.x32b[i] = 0.f;
-  }
-  if (!grid_barrier(a.bar, gridDim.x, a.derr)) return;
-  int sweeps = 0, outer = 0;
+  init_meshes(v, st);
+  init_x(v, x, warm, gt, nthreads);
+  if (!grid_barrier(v.barrier, gridDim.x, v.derr)) return;
+  double* cur = x;
+  double* nxt = v.xtmp;
   for (;;) {
-    // fp64 residual on active rows (inactive rows are exact)
-    double r2 = 0.0;
-    for (int sl = gw; sl < a.nslices; sl += nwarps) {
-      double s = slice_dot<double, double, double>(a, a.s_val, a.x, sl, lane);
+    for (int sl = gw; sl < v.nslices; sl += nwarps) {
+      if (st.done[mesh_of_slice(v, sl)]) continue;
+      double s = slice_dot<double, double, double>(v, v.s_val, cur, sl, lane);
       int64_t li = (int64_t)sl * 32 + lane;
-      if (a.ln_m[li] > 0) {
-        int i = a.ln_row[li];
-        double r = a.E[i] + s - a.x[i];
-        a.r32[i] = (float)r;
-        a.x32a[i] = (float)r;     // inner start: d0 = r
-        r2 += r * r;
+      double d2 = 0.0;
+      if (v.ln_m[li] > 0) {
+        int i = v.ln_row[li];
+        double xn = v.E[i] + s;
+        double df = xn - cur[i];
+        nxt[i] = xn;
+        d2 = df * df;
       }
+      d2 = warp_sum(d2);
+      if (lane == 0) v.sl_d2[sl] = d2;
     }
-    double bs = block_sum(r2, sh);
-    double* part = a.partials + (outer & 1) * gridDim.x;
-    if (threadIdx.x == 0) part[blockIdx.x] = bs;
-    if (!grid_barrier(a.bar, gridDim.x, a.derr)) return;
-    double tot = grid_total(part, gridDim.x, sh);
-    ++outer;
-    if (tot <= a.tol2 || sweeps >= a.max_sweeps) {
-      if (blockIdx.x == 0 && threadIdx.x == 0) {
-        a.counters[3] = sweeps;
-        a.partials[2 * gridDim.x] = tot;
+    if (!grid_barrier(v.barrier, gridDim.x, v.derr)) return;
+    chunk_sums(v, st, gw, nwarps, lane);
+    if (!grid_barrier(v.barrier, gridDim.x, v.derr)) return;
+    double* t = cur; cur = nxt; nxt = t;
+    if (decide_meshes(v, st, 1, 0) == 0) break;
+  }
+  // a mesh that stopped after an odd number of sweeps has its last iterate
+  // in xtmp
+  for (int sl = gw; sl < v.nslices; sl += nwarps) {
+    int m = mesh_of_slice(v, sl);
+    if (!v.md[m].active || !(st.sweeps[m] & 1)) continue;
+    int64_t li = (int64_t)sl * 32 + lane;
+    if (v.ln_m[li] > 0) x[v.ln_row[li]] = v.xtmp[v.ln_row[li]];
+  }
+}
+
+// Mixed precision: outer refinement with an fp64 residual r = E - (I - F) x
+// (fp64 values), inner fp32 Jacobi on (I - F~) d = r with bf16 F~ (4 sweeps),
+// x += d. A mesh stops when ||r||_2 <= tol.
+__global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity_mixed(StepView v, double* x, int warm) {
+  __shared__ MeshState st;
+  const int lane = threadIdx.x & 31;
+  const int gw = (blockIdx.x * RAD_THREADS + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * RAD_THREADS) >> 5;
+  const int gt = blockIdx.x * RAD_THREADS + threadIdx.x;
+  const int nthreads = gridDim.x * RAD_THREADS;
+  float* xa = v.x32;
+  float* xb = v.x32 + v.nt;
+  float* r32 = v.x32 + 2 * (size_t)v.nt;
+  init_meshes(v, st);
+  init_x(v, x, warm, gt, nthreads);
+  if (!grid_barrier(v.barrier, gridDim.x, v.derr)) return;
+  int first = 1;
+  for (;;) {
+    for (int sl = gw; sl < v.nslices; sl += nwarps) {
+      if (st.done[mesh_of_slice(v, sl)]) continue;
+      double s = slice_dot<double, double, double>(v, v.s_val, x, sl, lane);
+      int64_t li = (int64_t)sl * 32 + lane;
+      double r2 = 0.0;
+      if (v.ln_m[li] > 0) {
+        int i = v.ln_row[li];
+        double r = v.E[i] + s - x[i];
+        r32[i] = (float)r;
+        xa[i] = (float)r;     // inner start: d0 = r
+        r2 = r * r;
       }
-      return;
+      r2 = warp_sum(r2);
+      if (lane == 0) v.sl_d2[sl] = r2;
     }
-    // inner fp32 Jacobi: d <- r + F~ d, a fixed 4 sweeps (each gains ~1.5 digits)
-    float* cur = a.x32a;
-    float* nxt = a.x32b;
+    if (!grid_barrier(v.barrier, gridDim.x, v.derr)) return;
+    chunk_sums(v, st, gw, nwarps, lane);
+    if (!grid_barrier(v.barrier, gridDim.x, v.derr)) return;
+    int running = decide_meshes(v, st, 4, first);
+    first = 0;
+    if (running == 0) break;
+    float* cur = xa;
+    float* nxt = xb;
     for (int it = 0; it < 4; ++it) {
-      for (int sl = gw; sl < a.nslices; sl += nwarps) {
-        float s = slice_dot<__nv_bfloat16, float, float>(a, a.s_vbf, cur, sl, lane);
+      for (int sl = gw; sl < v.nslices; sl += nwarps) {
+        if (st.done[mesh_of_slice(v, sl)]) continue;
+        float s = slice_dot<__nv_bfloat16, float, float>(v, v.s_vbf, cur, sl, lane);
         int64_t li = (int64_t)sl * 32 + lane;
-        if (a.ln_m[li] > 0) {
-          int i = a.ln_row[li];
-          nxt[i] = a.r32[i] + a.rscale[i] * s;
+        if (v.ln_m[li] > 0) {
+          int i = v.ln_row[li];
+          nxt[i] = r32[i] + v.rscale[i] * s;
         }
       }
-      ++sweeps;
-      if (!grid_barrier(a.bar, gridDim.x, a.derr)) return;
+      if (!grid_barrier(v.barrier, gridDim.x, v.derr)) return;
       float* t = cur; cur = nxt; nxt = t;
     }
-    for (int w = gt; w < a.n_active; w += nthreads) {
-      int i = a.active[w];
-      a.x[i] += (double)cur[i];
+    for (int sl = gw; sl < v.nslices; sl += nwarps) {
+      if (st.done[mesh_of_slice(v, sl)]) continue;
+      int64_t li = (int64_t)sl * 32 + lane;
+      if (v.ln_m[li] > 0) x[v.ln_row[li]] += (double)cur[v.ln_row[li]];
     }
-    if (!grid_barrier(a.bar, gridDim.x, a.derr)) return;
+    if (!grid_barrier(v.barrier, gridDim.x, v.derr)) return;
   }
 }
 
@@ -417,7 +412,7 @@ int radiosity_prepare(Context& c) {
   for (int i = 0; i < nt; ++i)
     if (rp[i + 1] > rp[i]) { rows.push_back(i); maxlen = std::max<int64_t>(maxlen, rp[i + 1] - rp[i]); }
   std::stable_sort(rows.begin(), rows.end(), [&](int p, int q) { return rp[p + 1] - rp[p] > rp[q + 1] - rp[q]; });
-  int64_t L = 32;                 // chunk length: bounds the per-sweep critical path
+  int64_t L = 64;                 // chunk length: bounds the per-sweep critical path
   while ((maxlen + L - 1) / L > 32) L *= 2;
   std::vector<int64_t> sl_ptr;
   std::vector<int32_t> sl_len, sl_split, ln_row, ln_m, ln_cnt;
@@ -488,73 +483,68 @@ int radiosity_prepare(Context& c) {
     ILG_CUDA(cudaStreamSynchronize(s));
   }
   c.sell_elems = off;
+  // residual-reduction chunks of the slices
+  {
+    int ns = c.sell_nslices;
+    int nch = (ns + RAD_CHUNK - 1) / RAD_CHUNK;
+    std::vector<int4> ch(nch > 0 ? nch : 1);
+    for (int k = 0; k < nch; ++k) ch[k] = make_int4(k * RAD_CHUNK, std::min(RAD_CHUNK, ns - k * RAD_CHUNK), 0, 0);
+    ILG_TRY(c.chunks.alloc(ch.size()));
+    ILG_TRY(c.ch_d2.alloc(ch.size()));
+    ILG_CUDA(cudaMemcpyAsync(c.chunks.p, ch.data(), ch.size() * sizeof(int4), cudaMemcpyHostToDevice, s));
+    c.nchunks = nch;
+  }
+  // per-facet flag: the row has entries
+  std::vector<uint8_t> act((size_t)nt, 0);
+  for (int i : rows) act[i] = 1;
+  ILG_TRY(c.row_act.alloc(nt));
+  ILG_CUDA(cudaMemcpyAsync(c.row_act.p, act.data(), (size_t)nt, cudaMemcpyHostToDevice, s));
+  ILG_CUDA(cudaStreamSynchronize(s));
   return ILG_OK;
 }
 
-// Sizes the cooperative grid and reserves the solve's buffers. Called
-// before any stream capture (no allocation may happen while capturing).
-int radiosity_setup(Context& c, int precision) {
+// Cooperative grid size for nslices slices (at most the co-resident blocks).
+int radiosity_chunk() { return RAD_CHUNK; }
+int radiosity_max_meshes() { return RAD_MAX_MESH; }
+
+int radiosity_grid(int nslices, int precision) {
   static int nsm = 0, per_sm64 = 0, per_smm = 0;
   if (!nsm) {
     int dev;
-    ILG_CUDA(cudaGetDevice(&dev));
-    ILG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    ILG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm64, k_radiosity64, RAD_THREADS, 0));
-    ILG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_smm, k_radiosity_mixed, RAD_THREADS, 0));
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm64, k_radiosity64, RAD_THREADS, 0) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_smm, k_radiosity_mixed, RAD_THREADS, 0) != cudaSuccess) {
+      nsm = 0;
+      return 1;
+    }
   }
-  bool mixed = precision == ILG_PREC_MIXED;
-  int per_sm = mixed ? per_smm : per_sm64;
-  int want = div_up((int64_t)(c.sell_nslices > 0 ? c.sell_nslices : 1) * 32, RAD_THREADS);
+  int per_sm = precision == ILG_PREC_MIXED ? per_smm : per_sm64;
+  int want = div_up((int64_t)(nslices > 0 ? nslices : 1) * 32, RAD_THREADS);
   int grid = per_sm * nsm;
   if (want < grid) grid = want;
-  if (grid < 1) grid = 1;
-  ILG_TRY(c.partials.reserve((size_t)2 * grid + 2));
-  ILG_TRY(c.xtmp.reserve(c.nt));
-  if (c.xprev.n < (size_t)c.nt) {
-    ILG_TRY(c.xprev.alloc(c.nt));
-    ILG_CUDA(cudaMemset(c.xprev.p, 0, (size_t)c.nt * 8));
-  }
-  if (mixed) ILG_TRY(c.x32.reserve((size_t)3 * c.nt));
-  c.rad_grid = grid;
-  c.rad_grid_prec = precision;
-  return ILG_OK;
+  return grid < 1 ? 1 : grid;
 }
 
-// Launches the cooperative solve on c.stream. x_dev: result (also the warm
-// start when warm_start). Sweep count lands in counters[3] and the final
-// squared residual in partials[2*grid].
-int radiosity_launch(Context& c, const double* E_dev, double* x_dev, double tol, int max_sweeps, int precision,
-                     bool warm_start) {
-  if (c.rad_grid_prec != precision || c.rad_grid < 1) ILG_TRY(radiosity_setup(c, precision));
-  bool mixed = precision == ILG_PREC_MIXED;
-  int grid = c.rad_grid;
-  RadArgs a;
-  a.sl_ptr = c.sell_ptr.p; a.sl_len = c.sell_len.p; a.sl_split = c.sell_split.p; a.ln_row = c.sell_row.p;
-  a.ln_m = c.sell_m.p; a.s_col = c.sell_col.p; a.s_val = c.sell_val.p; a.s_vbf = c.sell_vbf.p;
-  a.nslices = c.sell_nslices;
-  a.rowptr = c.rowptr.p; a.col = c.col.p; a.val = c.val.p; a.vbf = c.val_bf16.p; a.rscale = c.row_scale.p;
-  a.active = c.active.p; a.n_active = c.n_active; a.nt = c.nt;
-  a.E = E_dev; a.x = x_dev; a.xt = c.xtmp.p; a.xprev = c.xprev.p;
-  a.x32a = mixed ? c.x32.p : nullptr;
-  a.x32b = mixed ? c.x32.p + c.nt : nullptr;
-  a.r32 = mixed ? c.x32.p + 2 * (size_t)c.nt : nullptr;
-  a.tol2 = tol * tol; a.max_sweeps = max_sweeps; a.warm = warm_start ? 1 : 0; a.mixed = mixed ? 1 : 0;
-  a.partials = c.partials.p; a.bar = (unsigned*)c.barrier.p; a.counters = c.counters.p; a.derr = c.derr.p;
-  ILG_CUDA(cudaMemsetAsync(c.barrier.p, 0, 2 * sizeof(unsigned), c.stream));
+// Launches the cooperative solve for every active mesh of the view with
+// slices. x: result (also the warm start when warm). Per-mesh sweep counts
+// and residuals land in the mesh table.
+int radiosity_launch(const StepView& v, double* x, int warm, int precision, int grid, cudaStream_t s) {
+  ILG_CUDA(cudaMemsetAsync(v.barrier, 0, 2 * sizeof(unsigned), s));
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(grid);
   cfg.blockDim = dim3(RAD_THREADS);
   cfg.dynamicSmemBytes = 0;
-  cfg.stream = c.stream;
+  cfg.stream = s;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeCooperative;   // all blocks co-resident: the grid barrier is safe
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  if (mixed)
-    ILG_CUDA(cudaLaunchKernelEx(&cfg, k_radiosity_mixed, a));
+  if (precision == ILG_PREC_MIXED)
+    ILG_CUDA(cudaLaunchKernelEx(&cfg, k_radiosity_mixed, v, x, warm));
   else
-    ILG_CUDA(cudaLaunchKernelEx(&cfg, k_radiosity64, a));
+    ILG_CUDA(cudaLaunchKernelEx(&cfg, k_radiosity64, v, x, warm));
   return ILG_OK;
 }
 

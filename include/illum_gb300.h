@@ -185,6 +185,29 @@ int ilg_set_timing(ilg_ctx* ctx, int enable);
 int ilg_get_stats(ilg_ctx* ctx, double* ms_direct, double* ms_radiosity, double* ms_conduction,
                   int64_t* ambiguous_facets, int64_t* radiosity_sweeps);
 
+/* ---- batches: many meshes stepped together ---------------------------------- */
+/* A batch steps its member contexts (each with horizons, suns set by
+ * ilg_set_suns and an initialised thermal model) together: one launch per
+ * phase for all members, each with its own opts (dt, tolerance, coupling,
+ * radiosity on/off; the precision must be the same for all). Members start
+ * at their first sun position and switch off after their last one. The
+ * batch owns a copy of the members' state; ilg_batch_sync writes it back to
+ * the contexts. A member's results are bitwise the same as when it runs
+ * alone (per-mesh radiosity convergence, no cross-mesh reductions). */
+typedef struct ilg_batch ilg_batch;
+int ilg_batch_create(ilg_ctx** members, int n, const ilg_run_opts* opts, ilg_batch** out);
+int ilg_batch_destroy(ilg_batch* batch);
+int ilg_batch_run(ilg_batch* batch, int nsteps, int use_graph);
+/* nsteps timed steps (L2 flushed by a flush_mb write before each);
+ * step_ms: nsteps device times. */
+int ilg_batch_bench(ilg_batch* batch, int nsteps, double flush_mb, double* step_ms);
+/* per member (arrays of n, any may be NULL): still active, steps done,
+ * radiosity sweeps of the last step */
+int ilg_batch_status(ilg_batch* batch, int* active, int* steps_done, int* sweeps);
+int ilg_batch_set_active(ilg_batch* batch, int member, int active);
+int ilg_batch_get_tsurf(ilg_batch* batch, int member, double* out);
+int ilg_batch_sync(ilg_batch* batch);
+
 /* ---- conduction (Fortran ABI) -------------------------------------------- */
 /* Exact symbols of conductionQ.f / conductionT.f as the reference's C++
  * wrapper declares them (conduction.cpp:3-6,17-20). Each runs one column on
