@@ -102,7 +102,10 @@ static int build(Batch& b) {
     ILG_CUDA(cudaStreamSynchronize(c.stream));
     if (ndisk < 0) ndisk = c.ndisk;
     if (c.ndisk != ndisk) { set_error("batch members must share the sun-disk samples"); return ILG_ERR_ARG; }
-    MeshDesc M = solo_desc(c, &o, 0);
+    // a member resumes at its own frame: the sun table covers its whole run
+    MeshDesc M = solo_desc(c, &o, c.frame_no);
+    M.done_steps = c.frame_no;
+    M.active = c.frame_no < c.nsun ? 1 : 0;
     M.facet0 = (int)nt;
     M.H0 = nH;
     M.T0 = nT;

@@ -66,23 +66,29 @@ k_conduct(StepView v, const double* __restrict__ Qnp1, int upd) {
   const R* __restrict__ tab = coef_tab<R>(v) + M.coef0;
   R* __restrict__ rho_g = SMEM ? nullptr : rho_scratch<R>(v) + g;
 #define RHO(i) (SMEM ? rho_s[(size_t)(i) * COND_THREADS + threadIdx.x] : rho_g[(size_t)(i) * v.nt])
+  // FP64 solves for T(n+1) directly (the reference's rows); FP32 solves for
+  // the increment dT = T(n+1) - T(n), whose right-hand side
+  // 2 gamma (T(i-1) - T(i)) + 2 alpha (T(i+1) - T(i)) carries no large
+  // cancellation when the diffusion numbers alpha, gamma are large.
+  constexpr bool INC = sizeof(R) == 4;
   // upward pass
   R Tip1 = T[(size_t)(nz - 1) * N];
   R Ti = T[(size_t)(nz - 2) * N];
   const R* cb_t = tab + (size_t)(nz - 1) * TAB_W;
-  R rho_next = cb_t[0] * Ti + cb_t[1] * Tip1 + (R)cs.cgeo;
+  R rho_next = INC ? (R)2 * cb_t[0] * (Ti - Tip1) + (R)cs.cgeo : cb_t[0] * Ti + cb_t[1] * Tip1 + (R)cs.cgeo;
   RHO(nz - 1) = rho_next;
   for (int i = nz - 2; i >= 1; --i) {
     R Tim1 = T[(size_t)(i - 1) * N];
     const R* c = tab + (size_t)i * TAB_W;
-    R r = c[0] * Tim1 + c[1] * Ti + c[2] * Tip1;
+    R r = INC ? (R)2 * (c[0] * (Tim1 - Ti) + c[2] * (Tip1 - Ti)) : c[0] * Tim1 + c[1] * Ti + c[2] * Tip1;
     R rh = r - c[3] * rho_next;
     RHO(i) = rh;
     rho_next = rh;
     Tip1 = Ti;
     Ti = Tim1;
   }
-  // top row (Ti = T_1, Tip1 = T_2 in the Fortran's numbering)
+  // top row (Ti = T_1, Tip1 = T_2 in the Fortran's numbering). In increment
+  // form rho1 is the increment's; T1(n+1) = T0 + (increment) below.
   double T0 = (double)Ti, T1 = (double)Tip1, rho1 = (double)rho_next;
   double Ts = v.Tsurf[g];
   double Q = Qnp1[g];
@@ -98,14 +104,18 @@ k_conduct(StepView v, const double* __restrict__ Qnp1, int upd) {
     double r0 = cs.gamma0 * (annp1 + ann) + (1.0 - cs.alpha0 - cs.gamma0 + cs.gamma0 * bn) * T0 + cs.alpha0 * T1;
     double piv = b0 + cs.f0 * cs.gamma1;
     if (piv == 0.0) { atomicExch(&v.derr[DERR_PIVOT], 1); return; }
+    if (INC) r0 -= b0 * T0 - cs.alpha0 * T1;   // the row applied to T(n)
     T0n = (r0 - cs.f0 * rho1) / piv;
+    if (INC) T0n += T0;
     Tsn = 0.5 * (annp1 + bn * T0n + T0n);
   } else if (cs.bc == 1) {
     double R0 = (1.0 - cs.alpha0 - cs.gamma0) * T0 + cs.alpha0 * T1 + cs.gamma0 * (2.0 * Ts - T0);
+    if (INC) R0 = 2.0 * cs.alpha0 * (T1 - T0) + 4.0 * cs.gamma0 * (Ts - T0) - 2.0 * cs.gamma0 * Ts;
     double P = (R0 - cs.f0 * rho1) / cs.Ap;
+    if (INC) P += T0;
     double S = 2.0 * cs.gamma0 / cs.Ap;
     double x = Ts;
-    double tolr = sizeof(R) == 8 ? 1e-13 : 1e-9;
+    double tolr = sizeof(R) == 8 ? 1e-13 : 1e-12;
     for (int it = 0; it < 30; ++it) {
       double x3 = x * x * x;
       double gx = Q + 2.0 * cs.k1 * (P + (S - 1.0) * x) - cs.es * x3 * x;
@@ -120,18 +130,31 @@ k_conduct(StepView v, const double* __restrict__ Qnp1, int upd) {
     // prescribed surface temperature: Ts at n, Q holds Ts at n+1
     double b0 = 1.0 + cs.alpha0 + cs.gamma0;
     double r0 = cs.alpha0 * T1 + (1.0 - cs.alpha0 - cs.gamma0) * T0 + cs.gamma0 * (Ts + Q);
+    if (INC) r0 -= b0 * T0 - cs.alpha0 * T1;
     T0n = (r0 - cs.f0 * rho1) / (b0 + cs.f0 * cs.gamma1);
+    if (INC) T0n += T0;
     Tsn = Q;
   }
   double Fs = -cs.k0 * (T0n - Tsn) / cs.z0;
   // downward pass
-  R prev = (R)T0n;
-  T[0] = prev;
-  for (int i = 1; i < nz; ++i) {
-    const R* c = tab + (size_t)i * TAB_W;
-    R t = (RHO(i) + c[0] * prev) * c[4];
-    T[(size_t)i * N] = t;
-    prev = t;
+  if (INC) {
+    R dprev = (R)(T0n - T0);
+    T[0] = (R)T0n;
+    for (int i = 1; i < nz; ++i) {
+      const R* c = tab + (size_t)i * TAB_W;
+      R d = (RHO(i) + c[0] * dprev) * c[4];
+      T[(size_t)i * N] += d;
+      dprev = d;
+    }
+  } else {
+    R prev = (R)T0n;
+    T[0] = prev;
+    for (int i = 1; i < nz; ++i) {
+      const R* c = tab + (size_t)i * TAB_W;
+      R t = (RHO(i) + c[0] * prev) * c[4];
+      T[(size_t)i * N] = t;
+      prev = t;
+    }
   }
 #undef RHO
   v.Fsurf[g] = Fs;

@@ -193,7 +193,9 @@ int ilg_get_stats(ilg_ctx* ctx, double* ms_direct, double* ms_radiosity, double*
  * at their first sun position and switch off after their last one. The
  * batch owns a copy of the members' state; ilg_batch_sync writes it back to
  * the contexts. A member's results are bitwise the same as when it runs
- * alone (per-mesh radiosity convergence, no cross-mesh reductions). */
+ * alone (per-mesh radiosity convergence, no cross-mesh reductions). A
+ * member resumes at its context's frame count (sun index = frames done), so
+ * after ilg_batch_sync the contexts can be regrouped into a new batch. */
 typedef struct ilg_batch ilg_batch;
 int ilg_batch_create(ilg_ctx** members, int n, const ilg_run_opts* opts, ilg_batch** out);
 int ilg_batch_destroy(ilg_batch* batch);
@@ -201,8 +203,8 @@ int ilg_batch_run(ilg_batch* batch, int nsteps, int use_graph);
 /* nsteps timed steps (L2 flushed by a flush_mb write before each);
  * step_ms: nsteps device times. */
 int ilg_batch_bench(ilg_batch* batch, int nsteps, double flush_mb, double* step_ms);
-/* per member (arrays of n, any may be NULL): still active, steps done,
- * radiosity sweeps of the last step */
+/* per member (arrays of n, any may be NULL): still active, steps done in
+ * total (including before this batch), radiosity sweeps of the last step */
 int ilg_batch_status(ilg_batch* batch, int* active, int* steps_done, int* sweeps);
 int ilg_batch_set_active(ilg_batch* batch, int member, int active);
 int ilg_batch_get_tsurf(ilg_batch* batch, int member, double* out);

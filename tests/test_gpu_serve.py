@@ -1,0 +1,34 @@
+"""Serving loop: jobs admitted over time, co-batched, each result the same
+as the job run alone."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_serving_results_equal_alone(ilg):
+    from illum_gb300 import serve
+    reqs = serve.request_stream(8, rate_hz=200.0, levels=(2, 3), rotations=(1, 2), steps_per_rot=(40, 60))
+    srv = serve.Server(budget_bytes=int(2e9), chunk_steps=7)
+    done = srv.run(reqs)
+    assert len(done) == len(reqs) and srv.rebuilds >= 2
+    for j in done:
+        alone = srv.build_job(j.req)
+        h = alone.ctx.run_steps(alone.opts, 0, j.req.nsteps, record_tsurf=True)
+        assert np.array_equal(h[-1], j.tsurf), j.req.rid
+
+
+def test_admission_respects_budget(ilg):
+    from illum_gb300 import serve
+    reqs = serve.request_stream(4, rate_hz=1000.0, levels=(3,), rotations=(1, 1), steps_per_rot=(30, 31))
+    one = serve.footprint_bytes(3, 80, 32, ilg.PREC_MIXED)
+    srv = serve.Server(budget_bytes=int(1.5 * one), chunk_steps=10)
+    seen = []
+    orig = srv.build_job
+
+    def spy(r):
+        seen.append(srv.used)
+        return orig(r)
+    srv.build_job = spy
+    done = srv.run(reqs)
+    assert len(done) == 4 and max(seen) <= srv.budget
