@@ -429,7 +429,7 @@ def main():
                 "visibility_rays_per_s": su["visibility_rays"] / su["form_factors_s"],
                 "horizon_rays_per_s": su["horizon_rays"] / su["horizons_s"],
                 "setup_s": {k: su[k] for k in ("bvh_s", "horizons_s", "form_factors_s")},
-                "mixed": mixed}
+                "mixed": mixed, "F": ctx.F_info()}
         print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()

@@ -62,6 +62,8 @@ _SIGS = {
                                 C.POINTER(C.c_int64)]),
     "ilg_get_F": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "ilg_set_F": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "ilg_F_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int),
+                             C.POINTER(C.c_int)]),
     "ilg_make_horizons": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_double]),
     "ilg_get_horizons": (C.c_int, [C.c_void_p, C.c_void_p]),
     "ilg_set_horizons": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
@@ -206,6 +208,12 @@ class IllumContext:
         col = np.zeros(max(self.nnz, 1), np.int32); val = np.zeros(max(self.nnz, 1), np.float64)
         _check(lib().ilg_get_F(self._h, _p(rowptr), _p(col), _p(val)))
         return rowptr, col[:self.nnz], val[:self.nnz]
+
+    def F_info(self):
+        a, b = C.c_int64(), C.c_int64()
+        c, d = C.c_int(), C.c_int()
+        _check(lib().ilg_F_info(self._h, C.byref(a), C.byref(b), C.byref(c), C.byref(d)))
+        return {"nnz": a.value, "sell_elems": b.value, "sell_slices": c.value, "active_rows": d.value}
 
     def set_F(self, rowptr, col, val):
         rowptr = np.ascontiguousarray(rowptr, np.int64); col = np.ascontiguousarray(col, np.int32); val = _f64(val)

@@ -72,10 +72,17 @@ static void invalidate_graph(Context& c) {
   for (int& k : c.graph_key) k = -1;
 }
 
+// L2 eviction between benchmark steps: writes n float4 with the evict-last
+// policy the radiosity sweeps use for the form-factor matrix, so lines kept
+// at that priority are displaced too (the buffer is twice the L2).
 __global__ void k_flush(float4* buf, size_t n, unsigned salt) {
   size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x, st = (size_t)gridDim.x * blockDim.x;
   float v = (float)salt;
-  for (; i < n; i += st) buf[i] = make_float4(v, v, v, v);
+  uint64_t pol;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+  for (; i < n; i += st)
+    asm volatile("st.global.L2::cache_hint.v4.f32 [%0], {%1, %1, %1, %1}, %2;" ::"l"(buf + i), "f"(v), "l"(pol)
+                 : "memory");
 }
 
 // Advance every active mesh by one step; a mesh driven from its sun table
@@ -368,6 +375,16 @@ int ilg_ctx_info(const ilg_ctx* ctx, int64_t* bvh_nodes, int* bvh_depth) {
   if (!ctx) { set_error("ctx is NULL"); return ILG_ERR_ARG; }
   if (bvh_nodes) *bvh_nodes = ctx->c.bvh_nodes;
   if (bvh_depth) *bvh_depth = ctx->c.bvh_depth;
+  return ILG_OK;
+}
+
+int ilg_F_info(const ilg_ctx* ctx, int64_t* nnz, int64_t* sell_elems, int* sell_slices, int* active_rows) {
+  if (!ctx || !ctx->c.have_F) { set_error("no form factors"); return ILG_ERR_ARG; }
+  const Context& c = ctx->c;
+  if (nnz) *nnz = c.nnz;
+  if (sell_elems) *sell_elems = c.sell_elems;
+  if (sell_slices) *sell_slices = c.sell_nslices;
+  if (active_rows) *active_rows = c.n_active;
   return ILG_OK;
 }
 

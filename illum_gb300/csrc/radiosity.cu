@@ -68,6 +68,33 @@ __device__ bool grid_barrier(unsigned* bar, unsigned nblocks, int* derr) {
 __device__ __forceinline__ int mesh_of_facet(const StepView& v, int g) { return v.mesh_of ? v.mesh_of[g] : 0; }
 __device__ __forceinline__ int mesh_of_slice(const StepView& v, int sl) { return v.sl_mesh ? v.sl_mesh[sl] : 0; }
 
+// Loads of the matrix carry an L2 evict-last policy on a fraction of the
+// lines: the SELL arrays (~12-16 B per entry) are re-read by every sweep of
+// a solve, and when they are about as large as GB300's 126 MB L2 a plain
+// cyclic scan would evict every line before its reuse. Keeping 3/4 of the
+// lines at evict-last lets sweeps after the first hit L2 for most of the
+// matrix while the rest streams from HBM.
+__device__ __forceinline__ uint64_t l2_keep_policy() {
+  uint64_t pol;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 0.75;" : "=l"(pol));
+  return pol;
+}
+__device__ __forceinline__ int ld_keep(const int32_t* p, uint64_t pol) {
+  int v;
+  asm volatile("ld.global.nc.L2::cache_hint.b32 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ double ld_keep(const double* p, uint64_t pol) {
+  double v;
+  asm volatile("ld.global.nc.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(p), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ __nv_bfloat16 ld_keep(const __nv_bfloat16* p, uint64_t pol) {
+  unsigned short v;
+  asm volatile("ld.global.nc.L2::cache_hint.b16 %0, [%1], %2;" : "=h"(v) : "l"(p), "l"(pol));
+  return __ushort_as_bfloat16(v);
+}
+
 // One SELL-32 slice: lane l accumulates its (chunk of a) row sequentially
 // (four independent loads in flight), then rows split into several chunks
 // are combined into their first lane in a fixed order.
@@ -76,6 +103,7 @@ __device__ __forceinline__ Acc slice_dot(const StepView& v, const V* __restrict_
                                          int sl, int lane) {
   int64_t base = v.sl_ptr[sl] + lane;
   int len = v.sl_len[sl];
+  const uint64_t pol = l2_keep_policy();
   Acc p = 0;
   int k = 0;
   for (; k + 8 <= len; k += 8) {
@@ -83,8 +111,8 @@ __device__ __forceinline__ Acc slice_dot(const StepView& v, const V* __restrict_
     V w[8];
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
-      c[j] = __ldg(v.s_col + base + (int64_t)(k + j) * 32);
-      w[j] = __ldg(sval + base + (int64_t)(k + j) * 32);
+      c[j] = ld_keep(v.s_col + base + (int64_t)(k + j) * 32, pol);
+      w[j] = ld_keep(sval + base + (int64_t)(k + j) * 32, pol);
     }
     X xv[8];
 #pragma unroll
@@ -97,8 +125,8 @@ __device__ __forceinline__ Acc slice_dot(const StepView& v, const V* __restrict_
     V w[4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-      c[j] = __ldg(v.s_col + base + (int64_t)(k + j) * 32);
-      w[j] = __ldg(sval + base + (int64_t)(k + j) * 32);
+      c[j] = ld_keep(v.s_col + base + (int64_t)(k + j) * 32, pol);
+      w[j] = ld_keep(sval + base + (int64_t)(k + j) * 32, pol);
     }
     X xv[4];
 #pragma unroll
@@ -152,8 +180,15 @@ __device__ __forceinline__ void chunk_sums(const StepView& v, const MeshState& s
   for (int k = gw; k < v.nchunks; k += nwarps) {
     int4 ch = v.chunks[k];   // (first slice, count, mesh, -)
     if (st.done[ch.z]) continue;
+    double w[RAD_CHUNK / 32];
+#pragma unroll
+    for (int j = 0; j < RAD_CHUNK / 32; ++j) {
+      int idx = lane + 32 * j;
+      w[j] = idx < ch.y ? v.sl_d2[ch.x + idx] : 0.0;
+    }
     double t = 0.0;
-    for (int j = lane; j < ch.y; j += 32) t += v.sl_d2[ch.x + j];
+#pragma unroll
+    for (int j = 0; j < RAD_CHUNK / 32; ++j) t += w[j];
     t = warp_sum(t);
     if (lane == 0) v.ch_d2[k] = t;
   }
@@ -168,7 +203,13 @@ __device__ __forceinline__ int decide_meshes(const StepView& v, MeshState& st, i
     if (st.done[m]) continue;
     const MeshDesc& M = v.md[m];
     double t = 0.0;
-    for (int c = 0; c < M.nchunks; ++c) t += v.ch_d2[M.chunk0 + c];
+    for (int c0 = 0; c0 < M.nchunks; c0 += 8) {   // loads issued together, summed in order
+      double w[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) w[j] = c0 + j < M.nchunks ? v.ch_d2[M.chunk0 + c0 + j] : 0.0;
+#pragma unroll
+      for (int j = 0; j < 8; ++j) t += w[j];
+    }
     int sw = st.sweeps[m] + (first ? 0 : inc);
     st.sweeps[m] = sw;
     bool stop = t <= M.tol2 || sw >= M.max_sweeps;
@@ -432,6 +473,7 @@ int radiosity_prepare(Context& c) {
   for (int i : rows) {
     int64_t len = rp[i + 1] - rp[i];
     int m = (int)((len + L - 1) / L);
+    int64_t csz = (len + m - 1) / m;   // nearly equal chunks: little padding next to similar rows
     if (lane + m > 32) {
       close_slice();
       sl_ptr.push_back(off);
@@ -440,8 +482,8 @@ int radiosity_prepare(Context& c) {
       lane = 0;
     }
     for (int k = 0; k < m; ++k) {
-      int64_t first = rp[i] + (int64_t)k * L;
-      int cnt = (int)std::min<int64_t>(L, rp[i + 1] - first);
+      int64_t first = rp[i] + (int64_t)k * csz;
+      int cnt = (int)std::max<int64_t>(0, std::min<int64_t>(csz, rp[i + 1] - first));
       ln_row.push_back(i);
       ln_m.push_back(k == 0 ? m : 0);
       ln_cnt.push_back(cnt);
