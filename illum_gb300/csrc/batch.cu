@@ -30,6 +30,11 @@ __global__ void k_shift(int32_t* a, int64_t n, int off) {
   if (i < n && a[i] >= 0) a[i] += off;
 }
 
+__global__ void k_iota(uint32_t* a, int64_t n, int off) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) a[i] = (uint32_t)(off + i);
+}
+
 __global__ void k_shift64(int64_t* a, int64_t n, int64_t off) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) a[i] += off;
@@ -66,6 +71,7 @@ struct Batch {
   dbuf<__nv_bfloat16> s_vbf;
   dbuf<float> rscale;
   dbuf<uint8_t> row_act;
+  dbuf<uint32_t> rperm;
   dbuf<int> work, counters, derr, mesh_flag;
   dbuf<double> sl_d2, ch_d2;
   dbuf<int4> chunks;
@@ -139,9 +145,11 @@ static int build(Batch& b) {
   ILG_TRY(b.frame.alloc(9 * nt)); ILG_TRY(b.H.alloc(nH)); ILG_TRY(b.hmin.alloc(nt)); ILG_TRY(b.hmax.alloc(nt));
   ILG_TRY(b.disk.alloc(2 * (size_t)ndisk));
   ILG_TRY(b.suns.alloc(nsun));
-  for (dbuf<double>* d : {&b.Tsurf, &b.Fsurf, &b.Qprev, &b.rad, &b.rad_avg, &b.therm_avg, &b.therm_max, &b.E, &b.xtmp,
+  for (dbuf<double>* d : {&b.Tsurf, &b.Fsurf, &b.Qprev, &b.rad, &b.rad_avg, &b.therm_avg, &b.therm_max, &b.E,
                           &b.xprev})
     ILG_TRY(d->alloc(nt));
+  ILG_TRY(b.xtmp.alloc(3 * nt));
+  ILG_TRY(b.rperm.alloc(nt));
   if (mixed) {
     ILG_TRY(b.x32.alloc(3 * nt));
     ILG_TRY(b.T32.alloc(nT));
@@ -204,6 +212,10 @@ static int build(Batch& b) {
     if (c.have_F) {
       ILG_TRY(cat(b.rscale, f0, c.row_scale.p, N, s));
       ILG_TRY(cat(b.row_act, f0, c.row_act.p, N, s));
+      ILG_TRY(cat(b.rperm, f0, c.rperm.p, N, s));
+      k_shift<<<div_up(N, 256), 256, 0, s>>>((int32_t*)(b.rperm.p + f0), N, (int)f0);
+    } else {
+      k_iota<<<div_up(N, 256), 256, 0, s>>>(b.rperm.p + f0, N, (int)f0);
     }
     if (M.nslices > 0) {
       size_t s0 = M.slice0, ns = M.nslices;
@@ -237,11 +249,12 @@ static int build(Batch& b) {
   v.cen = b.cen.p; v.nrm = b.nrm.p; v.frame32 = b.frame32.p; v.frame = b.frame.p; v.H = b.H.p;
   v.hmin = b.hmin.p; v.hmax = b.hmax.p; v.disk = b.disk.p; v.ndisk = ndisk; v.suns = b.suns.p;
   v.Tsurf = b.Tsurf.p; v.Fsurf = b.Fsurf.p; v.Qprev = b.Qprev.p; v.rad = b.rad.p; v.rad_avg = b.rad_avg.p;
-  v.therm_avg = b.therm_avg.p; v.therm_max = b.therm_max.p; v.E = b.E.p; v.xtmp = b.xtmp.p; v.xprev = b.xprev.p;
+  v.therm_avg = b.therm_avg.p; v.therm_max = b.therm_max.p; v.E = b.E.p; v.xprev = b.xprev.p;
   v.x32 = b.x32.p; v.T64 = b.T64.p; v.T32 = b.T32.p; v.coef64 = b.coef64.p; v.coef32 = b.coef32.p;
   v.sl_ptr = b.sl_ptr.p; v.sl_len = b.sl_len.p; v.sl_split = b.sl_split.p; v.sl_mesh = b.sl_mesh.p;
   v.ln_row = b.ln_row.p; v.ln_m = b.ln_m.p; v.s_col = b.s_col.p; v.s_val = b.s_val.p; v.s_vbf = b.s_vbf.p;
   v.rscale = b.rscale.p; v.row_act = b.row_act.p; v.nslices = b.nslices;
+  v.rperm = b.rperm.p; v.rbuf = b.xtmp.p;
   v.cblocks = b.cblocks.p; v.ncblocks = (int)ncb;
   v.chunks = b.chunks.p; v.nchunks = b.nchunks;
   v.work = b.work.p; v.counters = b.counters.p; v.derr = b.derr.p; v.mesh_flag = b.mesh_flag.p;

@@ -500,7 +500,7 @@ int bvh_build(Context& c, const float* verts_h, int nv, const int32_t* tris_h, c
   c.r_max = rmax;
 
   dbuf<unsigned long long> keys;
-  dbuf<uint32_t> order;
+  dbuf<uint32_t>& order = c.morton_order;   // kept: facets in Morton order
   ILG_TRY(keys.alloc(nt));
   ILG_TRY(order.alloc(nt));
   float3 blo = make_float3(lo[0], lo[1], lo[2]);

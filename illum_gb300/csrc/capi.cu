@@ -141,13 +141,14 @@ static StepView solo_view(Context& c, int precision) {
   v.ndisk = c.ndisk;
   v.suns = c.sun_aux.p;
   v.Tsurf = c.Tsurf.p; v.Fsurf = c.Fsurf.p; v.Qprev = c.Qprev.p; v.rad = c.rad.p; v.rad_avg = c.rad_avg.p;
-  v.therm_avg = c.therm_avg.p; v.therm_max = c.therm_max.p; v.E = c.E.p; v.xtmp = c.xtmp.p; v.xprev = c.xprev.p;
+  v.therm_avg = c.therm_avg.p; v.therm_max = c.therm_max.p; v.E = c.E.p; v.xprev = c.xprev.p;
   v.x32 = c.x32.p;
   v.T64 = c.T64.p; v.T32 = c.T32.p;
   v.coef64 = c.coef64.p; v.coef32 = c.coef32.p;
   v.sl_ptr = c.sell_ptr.p; v.sl_len = c.sell_len.p; v.sl_split = c.sell_split.p; v.sl_mesh = nullptr;
   v.ln_row = c.sell_row.p; v.ln_m = c.sell_m.p; v.s_col = c.sell_col.p; v.s_val = c.sell_val.p;
-  v.s_vbf = c.sell_vbf.p; v.rscale = c.row_scale.p; v.row_act = c.row_act.p;
+  v.s_vbf = c.sell_vbf.p; v.rscale = c.row_scale.p; v.row_act = c.row_act.p; v.rperm = c.rperm.p;
+  v.rbuf = c.xtmp.p;
   v.nslices = c.have_F ? c.sell_nslices : 0;
   v.cblocks = nullptr; v.ncblocks = 0;
   v.chunks = c.chunks.p; v.nchunks = c.have_F ? c.nchunks : 0;
@@ -201,7 +202,7 @@ static int upload_desc(Context& c, const MeshDesc& M) {
 static int ensure_step_buffers(Context& c, int precision) {
   ILG_TRY(c.E.reserve(c.nt));
   ILG_TRY(c.Q.reserve(c.nt));
-  ILG_TRY(c.xtmp.reserve(c.nt));
+  ILG_TRY(c.xtmp.reserve((size_t)3 * c.nt));   // radiosity E + two iterates (Morton positions)
   if (c.xprev.n < (size_t)c.nt) {
     ILG_TRY(c.xprev.alloc(c.nt));
     ILG_CUDA(cudaMemset(c.xprev.p, 0, (size_t)c.nt * 8));

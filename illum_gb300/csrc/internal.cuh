@@ -87,7 +87,7 @@ struct StepView {
   const double *frame, *H, *hmin, *hmax, *disk;
   int ndisk;
   const SunAux* suns;
-  double *Tsurf, *Fsurf, *Qprev, *rad, *rad_avg, *therm_avg, *therm_max, *E, *xtmp, *xprev;
+  double *Tsurf, *Fsurf, *Qprev, *rad, *rad_avg, *therm_avg, *therm_max, *E, *xprev;
   float* x32;                  // 3 x nt (mixed radiosity)
   double* T64;
   float* T32;
@@ -100,6 +100,8 @@ struct StepView {
   const __nv_bfloat16* s_vbf;
   const float* rscale;
   const uint8_t* row_act;      // per facet: its row has entries
+  const uint32_t* rperm;       // radiosity position -> facet (Morton order within each mesh)
+  double* rbuf;                // 3 x nt: E, and two iterates, in radiosity positions
   int nslices;
   // conduction blocks: (mesh, first local facet), or nullptr for a single mesh
   const int2* cblocks;
@@ -126,6 +128,7 @@ struct Context {
   dbuf<float4> frame32;           // float copy of the frame (3 x float4)
   dbuf<float4> nodes, tri_s;
   int root = 0;             // child code of the root (0, or ~0 for one facet)
+  dbuf<uint32_t> morton_order;   // facet at each position of the LBVH's Morton order
   int64_t bvh_nodes = 0;
   int bvh_depth = 0;
 
@@ -158,6 +161,7 @@ struct Context {
   dbuf<double> sell_val;
   dbuf<__nv_bfloat16> sell_vbf;
   dbuf<uint8_t> row_act;
+  dbuf<uint32_t> rperm;           // Morton position -> facet (radiosity's internal order)
 
   // thermal
   bool have_thermal = false;

@@ -4,11 +4,13 @@
 // src/cpp/illum_cli.cpp:425-440).
 //
 // GPU scheme: Jacobi sweeps x <- E + F x over the rows that have entries
-// (rows without entries are x = E exactly), one warp per row with a fixed
-// lane-strided summation order, inside ONE persistent cooperative kernel:
-// a grid barrier separates sweeps and every block reduces the per-block
-// residual partials in the same order, so all blocks take the same stop
-// decision and results are run-to-run deterministic. The residual of
+// (rows without entries are x = E exactly) inside ONE persistent cooperative
+// kernel. The matrix is stored as SELL-32 (slices of 32 rows, column-major,
+// one lane per row or row chunk, fixed summation order) and the solve works
+// on facets renumbered in the LBVH's Morton order, so the gathers of x hit
+// few cache lines. A grid barrier separates sweeps and every block reduces
+// the residual partials in the same fixed order, so all blocks take the same
+// stop decision and results are run-to-run deterministic. The residual of
 // iterate x_k is E - (I - F) x_k = x_{k+1} - x_k, so it comes for free
 // with the next sweep; iteration stops once its 2-norm is <= tol.
 // With albedo-scaled form factors the iteration matrix has spectral radius
@@ -24,6 +26,7 @@
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <cmath>
 #include <vector>
 
 #include "internal.cuh"
@@ -228,26 +231,47 @@ __device__ __forceinline__ int decide_meshes(const StepView& v, MeshState& st, i
   return running;
 }
 
-// Start values: rows without entries are x = E exactly; the others start at
-// E (cold) or at the mesh's previous solution, extrapolated linearly once two
-// solutions exist (warm).
-__device__ __forceinline__ void init_x(const StepView& v, double* x, int warm, int gt, int nthreads) {
-  for (int g = gt; g < v.nt; g += nthreads) {
+// The solve works on radiosity positions (Morton order within each mesh):
+// EP = E, P0 / P1 = iterates, gathered through rperm at entry. Start values:
+// rows without entries are x = E exactly; the others start at E (cold) or
+// at the mesh's previous solution, extrapolated linearly once two solutions
+// exist (warm).
+__device__ __forceinline__ void init_x(const StepView& v, const double* x, int warm, int gt, int nthreads) {
+  double* EP = v.rbuf;
+  double* P0 = v.rbuf + v.nt;
+  double* P1 = v.rbuf + 2 * (size_t)v.nt;
+  for (int p = gt; p < v.nt; p += nthreads) {
+    int g = (int)v.rperm[p];
     const MeshDesc& M = v.md[mesh_of_facet(v, g)];
     if (!M.active || M.nslices == 0) continue;
     double e = v.E[g];
-    v.xtmp[g] = e;
+    EP[p] = e;
+    P1[p] = e;
     if (!warm || !v.row_act[g]) {
-      x[g] = e;
+      P0[p] = e;
     } else {
       double xn = x[g];
-      if (M.frame >= 2) x[g] = 2.0 * xn - v.xprev[g];
+      P0[p] = M.frame >= 2 ? 2.0 * xn - v.xprev[g] : xn;
       v.xprev[g] = xn;
     }
     if (v.x32) {
-      v.x32[g] = 0.f;
-      v.x32[v.nt + g] = 0.f;
+      v.x32[p] = 0.f;
+      v.x32[v.nt + p] = 0.f;
     }
+  }
+}
+
+// Scatter the solved meshes' last iterate back to facet order.
+__device__ __forceinline__ void scatter_x(const StepView& v, const MeshState& st, double* x, int gt, int nthreads,
+                                          bool mixed) {
+  const double* P0 = v.rbuf + v.nt;
+  const double* P1 = v.rbuf + 2 * (size_t)v.nt;
+  for (int p = gt; p < v.nt; p += nthreads) {
+    int g = (int)v.rperm[p];
+    int m = mesh_of_facet(v, g);
+    const MeshDesc& M = v.md[m];
+    if (!M.active || M.nslices == 0) continue;
+    x[g] = (!mixed && (st.sweeps[m] & 1)) ? P1[p] : P0[p];
   }
 }
 
@@ -262,8 +286,9 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity64(StepView v, doub
   init_meshes(v, st);
   init_x(v, x, warm, gt, nthreads);
   if (!grid_barrier(v.barrier, gridDim.x, v.derr)) return;
-  double* cur = x;
-  double* nxt = v.xtmp;
+  const double* EP = v.rbuf;
+  double* cur = v.rbuf + v.nt;
+  double* nxt = v.rbuf + 2 * (size_t)v.nt;
   for (;;) {
     for (int sl = gw; sl < v.nslices; sl += nwarps) {
       if (st.done[mesh_of_slice(v, sl)]) continue;
@@ -272,7 +297,7 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity64(StepView v, doub
       double d2 = 0.0;
       if (v.ln_m[li] > 0) {
         int i = v.ln_row[li];
-        double xn = v.E[i] + s;
+        double xn = EP[i] + s;
         double df = xn - cur[i];
         nxt[i] = xn;
         d2 = df * df;
@@ -286,14 +311,7 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity64(StepView v, doub
     double* t = cur; cur = nxt; nxt = t;
     if (decide_meshes(v, st, 1, 0) == 0) break;
   }
-  // a mesh that stopped after an odd number of sweeps has its last iterate
-  // in xtmp
-  for (int sl = gw; sl < v.nslices; sl += nwarps) {
-    int m = mesh_of_slice(v, sl);
-    if (!v.md[m].active || !(st.sweeps[m] & 1)) continue;
-    int64_t li = (int64_t)sl * 32 + lane;
-    if (v.ln_m[li] > 0) x[v.ln_row[li]] = v.xtmp[v.ln_row[li]];
-  }
+  scatter_x(v, st, x, gt, nthreads, false);
 }
 
 // Mixed precision: outer refinement with an fp64 residual r = E - (I - F) x
@@ -312,16 +330,18 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity_mixed(StepView v, 
   init_meshes(v, st);
   init_x(v, x, warm, gt, nthreads);
   if (!grid_barrier(v.barrier, gridDim.x, v.derr)) return;
+  const double* EP = v.rbuf;
+  double* X = v.rbuf + v.nt;          // the fp64 iterate (radiosity positions)
   int first = 1;
   for (;;) {
     for (int sl = gw; sl < v.nslices; sl += nwarps) {
       if (st.done[mesh_of_slice(v, sl)]) continue;
-      double s = slice_dot<double, double, double>(v, v.s_val, x, sl, lane);
+      double s = slice_dot<double, double, double>(v, v.s_val, X, sl, lane);
       int64_t li = (int64_t)sl * 32 + lane;
       double r2 = 0.0;
       if (v.ln_m[li] > 0) {
         int i = v.ln_row[li];
-        double r = v.E[i] + s - x[i];
+        double r = EP[i] + s - X[i];
         r32[i] = (float)r;
         xa[i] = (float)r;     // inner start: d0 = r
         r2 = r * r;
@@ -334,7 +354,7 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity_mixed(StepView v, 
     if (!grid_barrier(v.barrier, gridDim.x, v.derr)) return;
     int running = decide_meshes(v, st, 4, first);
     first = 0;
-    if (running == 0) break;
+    if (running == 0) break;   // scatter below
     float* cur = xa;
     float* nxt = xb;
     for (int it = 0; it < 4; ++it) {
@@ -344,7 +364,7 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity_mixed(StepView v, 
         int64_t li = (int64_t)sl * 32 + lane;
         if (v.ln_m[li] > 0) {
           int i = v.ln_row[li];
-          nxt[i] = r32[i] + v.rscale[i] * s;
+          nxt[i] = r32[i] + v.rscale[v.rperm[i]] * s;
         }
       }
       if (!grid_barrier(v.barrier, gridDim.x, v.derr)) return;
@@ -353,10 +373,11 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity_mixed(StepView v, 
     for (int sl = gw; sl < v.nslices; sl += nwarps) {
       if (st.done[mesh_of_slice(v, sl)]) continue;
       int64_t li = (int64_t)sl * 32 + lane;
-      if (v.ln_m[li] > 0) x[v.ln_row[li]] += (double)cur[v.ln_row[li]];
+      if (v.ln_m[li] > 0) X[v.ln_row[li]] += (double)cur[v.ln_row[li]];
     }
     if (!grid_barrier(v.barrier, gridDim.x, v.derr)) return;
   }
+  scatter_x(v, st, x, gt, nthreads, true);
 }
 
 __global__ void k_active_rows(const int64_t* __restrict__ rowptr, int nt, uint32_t* flag) {
@@ -369,34 +390,48 @@ __global__ void k_active_compact(const uint32_t* __restrict__ flag, const unsign
   if (i < nt && flag[i]) active[pos[i]] = i;
 }
 
-// SELL fill: lane (slice, l) copies elements [first, first + cnt) of its row
-// into column k of the slice; the rest of the slice column is padding
-// (column = 0, value = 0).
-__global__ void k_sell_fill(const int64_t* __restrict__ sl_ptr, const int32_t* __restrict__ sl_len,
-                            const int64_t* __restrict__ ln_first, const int32_t* __restrict__ ln_cnt,
-                            const int32_t* __restrict__ ln_row, const int32_t* __restrict__ col,
-                            const double* __restrict__ val, const float* __restrict__ rscale, int nslices,
-                            int32_t* s_col, double* s_val, __nv_bfloat16* s_vbf) {
-  int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= (int64_t)nslices * 32) return;
-  int sl = (int)(g >> 5), lane = (int)(g & 31);
-  int len = sl_len[sl];
-  int64_t base = sl_ptr[sl] + lane;
-  int64_t first = ln_first[g];
-  int cnt = ln_cnt[g];
-  int row = ln_row[g];
-  float sc = row >= 0 ? rscale[row] : 1.f;
-  for (int k = 0; k < len; ++k) {
-    int64_t o = base + (int64_t)k * 32;
-    if (k < cnt) {
-      s_col[o] = col[first + k];
-      s_val[o] = val[first + k];
-      s_vbf[o] = __float2bfloat16_rn((float)(val[first + k] / (double)sc));
-    } else {
-      s_col[o] = 0;
-      s_val[o] = 0.0;
-      s_vbf[o] = __float2bfloat16_rn(0.f);
-    }
+// SELL fill: element e takes CSR entry src[e] (value, and its bf16 copy
+// scaled by its row's scale), or zero for padding (src < 0).
+__global__ void k_sell_fill(const int64_t* __restrict__ src, int64_t nel, const int64_t* __restrict__ sl_ptr,
+                            int nslices, const int32_t* __restrict__ ln_row, const uint32_t* __restrict__ rperm,
+                            const double* __restrict__ val, const float* __restrict__ rscale, double* s_val,
+                            __nv_bfloat16* s_vbf) {
+  int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nel) return;
+  int64_t k = src[e];
+  if (k < 0) {
+    s_val[e] = 0.0;
+    s_vbf[e] = __float2bfloat16_rn(0.f);
+    return;
+  }
+  // the element's slice and lane give its row (Morton position -> facet)
+  int lo = 0, hi = nslices - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (sl_ptr[mid] <= e) lo = mid; else hi = mid - 1;
+  }
+  int lane = (int)((e - sl_ptr[lo]) & 31);
+  int row = (int)rperm[ln_row[(int64_t)lo * 32 + lane]];
+  double v = val[k];
+  s_val[e] = v;
+  s_vbf[e] = __float2bfloat16_rn((float)(v / (double)rscale[row]));
+}
+
+__global__ void k_rank(const uint32_t* __restrict__ order, int nt, uint32_t* rank) {
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p < nt) rank[order[p]] = (uint32_t)p;
+}
+
+// key = row << rb | Morton position of the column; value = CSR entry.
+__global__ void k_row_keys(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+                           const uint32_t* __restrict__ rank, int nt, int rb, unsigned long long* key,
+                           uint32_t* src) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nt) return;
+  unsigned long long hi = (unsigned long long)i << rb;
+  for (int64_t k = rowptr[i]; k < rowptr[i + 1]; ++k) {
+    key[k] = hi | rank[col[k]];
+    src[k] = (uint32_t)k;
   }
 }
 
@@ -441,23 +476,74 @@ int radiosity_prepare(Context& c) {
   ILG_CUDA(cudaGetLastError());
   c.have_bf16 = true;
 
-  // SELL-32 layout of the active rows: rows sorted by length (longest
-  // first), rows longer than L split into chunks of at most L placed in
-  // adjacent lanes of one slice, each slice column-major and padded to the
-  // longest chunk (rounded up to 4).
+  // SELL-32 layout of the active rows, in Morton order. Inside the solve a
+  // facet is addressed by its position in the LBVH's Morton order, so
+  // facets near each other in space are near each other in memory. Rows are
+  // grouped by length class (half octaves, longest first) and by Morton
+  // position within a class; each row's entries are sorted by their
+  // column's Morton position. Neighbouring lanes of a slice are then
+  // neighbouring facets whose visible sets overlap, so the k-th columns of a
+  // slice's 32 lanes fall in few cache lines. Rows longer than L are split
+  // into nearly equal chunks in adjacent lanes of one slice; each slice is
+  // column-major and padded to its longest chunk (rounded up to 4).
+  // Per-row columns in Morton order, sorted on the device: key = (row,
+  // Morton position of the column), value = CSR entry.
+  int rb = 1;
+  while ((1 << rb) < nt) ++rb;
+  int64_t nnz = c.nnz;
   std::vector<int64_t> rp((size_t)nt + 1);
+  std::vector<unsigned long long> skey((size_t)(nnz > 0 ? nnz : 1));
+  std::vector<uint32_t> ssrc32((size_t)(nnz > 0 ? nnz : 1));
+  std::vector<uint32_t> order((size_t)nt);
   ILG_CUDA(cudaMemcpyAsync(rp.data(), c.rowptr.p, rp.size() * 8, cudaMemcpyDeviceToHost, s));
+  ILG_CUDA(cudaMemcpyAsync(order.data(), c.morton_order.p, (size_t)nt * 4, cudaMemcpyDeviceToHost, s));
+  if (nnz > 0) {
+    dbuf<uint32_t> drank, dsv;
+    dbuf<unsigned long long> dkey;
+    ILG_TRY(drank.alloc(nt));
+    ILG_TRY(dkey.alloc(nnz));
+    ILG_TRY(dsv.alloc(nnz));
+    k_rank<<<div_up(nt, 256), 256, 0, s>>>(c.morton_order.p, nt, drank.p);
+    ILG_CUDA(cudaGetLastError());
+    k_row_keys<<<div_up(nt, 256), 256, 0, s>>>(c.rowptr.p, c.col.p, drank.p, nt, rb, dkey.p, dsv.p);
+    ILG_CUDA(cudaGetLastError());
+    ILG_TRY(radix_sort_u64(dkey.p, dsv.p, nnz, 2 * rb, c.sort, s));
+    ILG_CUDA(cudaMemcpyAsync(skey.data(), dkey.p, (size_t)nnz * 8, cudaMemcpyDeviceToHost, s));
+    ILG_CUDA(cudaMemcpyAsync(ssrc32.data(), dsv.p, (size_t)nnz * 4, cudaMemcpyDeviceToHost, s));
+    ILG_CUDA(cudaStreamSynchronize(s));
+  }
   ILG_CUDA(cudaStreamSynchronize(s));
+  const unsigned long long cmask = (1ull << rb) - 1;
+  std::vector<int32_t> rank((size_t)nt);
+  for (int p = 0; p < nt; ++p) rank[order[p]] = p;
   std::vector<int> rows;
   int64_t maxlen = 0;
   for (int i = 0; i < nt; ++i)
     if (rp[i + 1] > rp[i]) { rows.push_back(i); maxlen = std::max<int64_t>(maxlen, rp[i + 1] - rp[i]); }
-  std::stable_sort(rows.begin(), rows.end(), [&](int p, int q) { return rp[p + 1] - rp[p] > rp[q + 1] - rp[q]; });
+  auto len_class = [&](int i) {
+    double l = (double)(rp[i + 1] - rp[i]);
+    return (int)std::floor(2.0 * std::log2(l));
+  };
+  std::sort(rows.begin(), rows.end(), [&](int p, int q) {
+    int cp = len_class(p), cq = len_class(q);
+    return cp != cq ? cp > cq : rank[p] < rank[q];
+  });
+  // Inside windows of 256 Morton-consecutive rows of one class, longest
+  // first: the slices cut from a window keep their spatial neighbourhood but
+  // pad less.
+  for (size_t a = 0; a < rows.size();) {
+    size_t b = a;
+    int ca = len_class(rows[a]);
+    while (b < rows.size() && b - a < 256 && len_class(rows[b]) == ca) ++b;
+    std::stable_sort(rows.begin() + a, rows.begin() + b,
+                     [&](int p, int q) { return rp[p + 1] - rp[p] > rp[q + 1] - rp[q]; });
+    a = b;
+  }
   int64_t L = 64;                 // chunk length: bounds the per-sweep critical path
   while ((maxlen + L - 1) / L > 32) L *= 2;
   std::vector<int64_t> sl_ptr;
   std::vector<int32_t> sl_len, sl_split, ln_row, ln_m, ln_cnt;
-  std::vector<int64_t> ln_first;
+  std::vector<int64_t> ln_first;   // offset of the lane's chunk in the sorted entries
   int lane = 32;   // force a new slice first
   int64_t off = 0;
   auto close_slice = [&]() {
@@ -472,6 +558,7 @@ int radiosity_prepare(Context& c) {
   };
   for (int i : rows) {
     int64_t len = rp[i + 1] - rp[i];
+    int64_t row0 = rp[i];   // the row's sorted entries: skey/ssrc32[rp[i], rp[i+1])
     int m = (int)((len + L - 1) / L);
     int64_t csz = (len + m - 1) / m;   // nearly equal chunks: little padding next to similar rows
     if (lane + m > 32) {
@@ -482,12 +569,12 @@ int radiosity_prepare(Context& c) {
       lane = 0;
     }
     for (int k = 0; k < m; ++k) {
-      int64_t first = rp[i] + (int64_t)k * csz;
-      int cnt = (int)std::max<int64_t>(0, std::min<int64_t>(csz, rp[i + 1] - first));
-      ln_row.push_back(i);
+      int64_t first = (int64_t)k * csz;
+      int cnt = (int)std::max<int64_t>(0, std::min<int64_t>(csz, len - first));
+      ln_row.push_back(rank[i]);
       ln_m.push_back(k == 0 ? m : 0);
       ln_cnt.push_back(cnt);
-      ln_first.push_back(first);
+      ln_first.push_back(row0 + first);
       sl_len.back() = std::max(sl_len.back(), cnt);
       ++lane;
     }
@@ -497,6 +584,18 @@ int radiosity_prepare(Context& c) {
   c.sell_nslices = (int)sl_len.size();
   int ns = c.sell_nslices > 0 ? c.sell_nslices : 1;
   int64_t nel = off > 0 ? off : 1;
+  // element arrays built on the host: column position and CSR source
+  std::vector<int32_t> ecol((size_t)nel, 0);
+  std::vector<int64_t> esrc((size_t)nel, -1);
+  for (int sl = 0; sl < c.sell_nslices; ++sl)
+    for (int l = 0; l < 32; ++l) {
+      size_t li = (size_t)sl * 32 + l;
+      for (int k = 0; k < ln_cnt[li]; ++k) {
+        size_t o = (size_t)sl_ptr[sl] + (size_t)k * 32 + l;
+        ecol[o] = (int32_t)(skey[ln_first[li] + k] & cmask);
+        esrc[o] = (int64_t)ssrc32[ln_first[li] + k];
+      }
+    }
   ILG_TRY(c.sell_ptr.alloc(ns));
   ILG_TRY(c.sell_len.alloc(ns));
   ILG_TRY(c.sell_split.alloc(ns));
@@ -505,22 +604,20 @@ int radiosity_prepare(Context& c) {
   ILG_TRY(c.sell_col.alloc(nel));
   ILG_TRY(c.sell_val.alloc(nel));
   ILG_TRY(c.sell_vbf.alloc(nel));
+  ILG_TRY(c.rperm.alloc(nt));
+  ILG_CUDA(cudaMemcpyAsync(c.rperm.p, order.data(), (size_t)nt * 4, cudaMemcpyHostToDevice, s));
   if (c.sell_nslices > 0) {
-    dbuf<int64_t> dfirst;
-    dbuf<int32_t> dcnt;
-    ILG_TRY(dfirst.alloc(ln_first.size()));
-    ILG_TRY(dcnt.alloc(ln_cnt.size()));
+    dbuf<int64_t> dsrc;
+    ILG_TRY(dsrc.alloc(nel));
     ILG_CUDA(cudaMemcpyAsync(c.sell_ptr.p, sl_ptr.data(), sl_ptr.size() * 8, cudaMemcpyHostToDevice, s));
     ILG_CUDA(cudaMemcpyAsync(c.sell_len.p, sl_len.data(), sl_len.size() * 4, cudaMemcpyHostToDevice, s));
     ILG_CUDA(cudaMemcpyAsync(c.sell_split.p, sl_split.data(), sl_split.size() * 4, cudaMemcpyHostToDevice, s));
     ILG_CUDA(cudaMemcpyAsync(c.sell_row.p, ln_row.data(), ln_row.size() * 4, cudaMemcpyHostToDevice, s));
     ILG_CUDA(cudaMemcpyAsync(c.sell_m.p, ln_m.data(), ln_m.size() * 4, cudaMemcpyHostToDevice, s));
-    ILG_CUDA(cudaMemcpyAsync(dfirst.p, ln_first.data(), ln_first.size() * 8, cudaMemcpyHostToDevice, s));
-    ILG_CUDA(cudaMemcpyAsync(dcnt.p, ln_cnt.data(), ln_cnt.size() * 4, cudaMemcpyHostToDevice, s));
-    int64_t nl = (int64_t)c.sell_nslices * 32;
-    k_sell_fill<<<div_up(nl, 256), 256, 0, s>>>(c.sell_ptr.p, c.sell_len.p, dfirst.p, dcnt.p, c.sell_row.p, c.col.p,
-                                               c.val.p, c.row_scale.p, c.sell_nslices, c.sell_col.p, c.sell_val.p,
-                                               c.sell_vbf.p);
+    ILG_CUDA(cudaMemcpyAsync(c.sell_col.p, ecol.data(), (size_t)nel * 4, cudaMemcpyHostToDevice, s));
+    ILG_CUDA(cudaMemcpyAsync(dsrc.p, esrc.data(), (size_t)nel * 8, cudaMemcpyHostToDevice, s));
+    k_sell_fill<<<div_up(nel, 256), 256, 0, s>>>(dsrc.p, nel, c.sell_ptr.p, c.sell_nslices, c.sell_row.p,
+                                                c.rperm.p, c.val.p, c.row_scale.p, c.sell_val.p, c.sell_vbf.p);
     ILG_CUDA(cudaGetLastError());
     ILG_CUDA(cudaStreamSynchronize(s));
   }
