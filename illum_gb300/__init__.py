@@ -102,6 +102,9 @@ _SIGS = {
     "ilg_conductionq_batch": (C.c_int, [C.c_int, C.c_int, C.c_void_p, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p,
                                         C.c_void_p, C.c_void_p, C.c_double, C.c_void_p, C.c_double, C.c_void_p,
                                         C.c_int]),
+    "ilg_conductionq_batch_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_void_p, C.c_double, C.c_void_p, C.c_void_p,
+                                                C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_void_p,
+                                                C.c_double, C.c_void_p, C.c_int, C.c_void_p]),
 }
 
 

@@ -19,6 +19,7 @@
 // temperature state is layer-major [nz][N], so every layer access of a warp
 // is one coalesced 256-byte (fp64) or 128-byte (fp32) transaction.
 #include <cmath>
+#include <mutex>
 #include <vector>
 
 #include "geom.h"
@@ -381,4 +382,123 @@ int conductiont_host(int nz, const double* z, double dt, double* T, double Tsurf
   return run_columns(1, nz, z, dt, nullptr, &Tsurfp1, T, ti, rhoc, 1.0, &ts, Fgeo, Fsurf, 2);
 }
 
+// ---- conduction columns without allocation ----------------------------------
+//
+// ilg_conductionq_batch_noalloc runs the same k_conduct kernel as the
+// allocating entry point on caller-owned device arrays. Its device scratch is
+// one fixed file-scope array, sized once at library load, so the call itself
+// never allocates device memory. It serves callers that cannot call
+// cudaMalloc at the time they step the columns: code running inside another
+// framework's caching allocator (whose memory it must not fragment or
+// double-count), host code under a memory budget that is already spent, and
+// callers that must not stall on the driver's allocation lock.
+//
+// Scratch layout (each region starts on a 256-byte boundary):
+//   error flags   DERR_COUNT ints; zeroed by every call before its launch
+//   mesh record   one MeshDesc, written by every call
+//   layer table   nz x 5 doubles, written by every call
+//   Qn copy       ncol doubles (Qn, or zeros), written by every call; the
+//                 kernel replaces it with Qnp1 as the allocating path does
+//   rho           nz x ncol doubles, only for columns deeper than the
+//                 shared-memory stage holds (nz > 160); written before read
+// Only the error flags must start at zero, and each call clears them itself.
+// All calls share the one array: two calls that overlap on the device would
+// race on it. Calls therefore take a process-wide lock and return only after
+// their work has finished, so calls from one process never overlap.
+
+constexpr size_t NOALLOC_SCRATCH_BYTES = (size_t)ILG_NOALLOC_SCRATCH_MB << 20;
+static __device__ __align__(256) unsigned char g_cond_scratch[NOALLOC_SCRATCH_BYTES];
+
+namespace {
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[NOALLOC_MAX_DEVICES];   // scratch address per device (set-up done when non-null)
+
+size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+struct NoallocLayout {
+  size_t flags, md, tab, qprev, rho, total;
+};
+
+NoallocLayout noalloc_layout(int ncol, int nz, bool deep) {
+  NoallocLayout L;
+  L.flags = 0;
+  L.md = L.flags + align256(DERR_COUNT * sizeof(int));
+  L.tab = L.md + align256(sizeof(MeshDesc));
+  L.qprev = L.tab + align256((size_t)nz * TAB_W * sizeof(double));
+  L.rho = L.qprev + align256((size_t)ncol * sizeof(double));
+  L.total = L.rho + (deep ? align256((size_t)nz * ncol * sizeof(double)) : 0);
+  return L;
+}
+
+// Once per device, with that device current: the scratch's device address
+// and the shared-memory opt-in of the kernel.
+int noalloc_setup(unsigned char** out) {
+  int dev = 0;
+  ILG_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) { set_error("device %d out of range", dev); return ILG_ERR_ARG; }
+  if (!g_noalloc_ptr[dev]) {
+    void* ptr = nullptr;
+    ILG_CUDA(cudaGetSymbolAddress(&ptr, g_cond_scratch));
+    ILG_CUDA(cudaFuncSetAttribute(k_conduct<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)SMEM_LIMIT));
+    g_noalloc_ptr[dev] = ptr;
+  }
+  *out = static_cast<unsigned char*>(g_noalloc_ptr[dev]);
+  return ILG_OK;
+}
+
+}  // namespace
+
 }  // namespace ilg
+
+extern "C" int ilg_conductionq_batch_noalloc(int ncol, int nz, const double* z, double dt, const double* Qn,
+                                             const double* Qnp1, double* T, const double* ti, const double* rhoc,
+                                             double emiss, double* Tsurf, double Fgeotherm, double* Fsurf,
+                                             int bc_mode, void* stream) {
+  using namespace ilg;
+  if (ncol < 0 || nz < 2) { set_error("invalid sizes (ncol %d, nz %d)", ncol, nz); return ILG_ERR_ARG; }
+  const bool deep = (size_t)nz * COND_THREADS * sizeof(double) > SMEM_LIMIT;
+  const NoallocLayout L = noalloc_layout(ncol, nz, deep);
+  if (L.total > NOALLOC_SCRATCH_BYTES) {
+    set_error("%d columns of %d layers need %zu bytes of scratch; the fixed scratch holds %zu "
+              "(split the columns into smaller calls)", ncol, nz, L.total, NOALLOC_SCRATCH_BYTES);
+    return ILG_ERR_ARG;
+  }
+  if (bc_mode != ILG_BC_LINEARISED && bc_mode != ILG_BC_NEWTON) { set_error("bad bc_mode %d", bc_mode); return ILG_ERR_ARG; }
+  if (!z || !ti || !rhoc || (ncol > 0 && (!Qnp1 || !T || !Tsurf || !Fsurf))) {
+    set_error("invalid arguments");
+    return ILG_ERR_ARG;
+  }
+  std::vector<double> tab;
+  CondScalars cs;
+  ILG_TRY(build_tables(nz, z, ti, rhoc, dt, emiss, Fgeotherm, bc_mode, tab, cs));
+  if (ncol == 0) return ILG_OK;
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  unsigned char* base = nullptr;
+  ILG_TRY(noalloc_setup(&base));
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  MeshDesc md{};
+  md.facet0 = 0; md.nfacet = ncol; md.nz = nz; md.coef0 = 0; md.T0 = 0; md.cs = cs; md.active = 1;
+  int* flags = reinterpret_cast<int*>(base + L.flags);
+  MeshDesc* dmd = reinterpret_cast<MeshDesc*>(base + L.md);
+  double* dtab = reinterpret_cast<double*>(base + L.tab);
+  double* qprev = reinterpret_cast<double*>(base + L.qprev);
+  ILG_CUDA(cudaMemsetAsync(flags, 0, DERR_COUNT * sizeof(int), s));
+  ILG_CUDA(cudaMemcpyAsync(dmd, &md, sizeof(md), cudaMemcpyHostToDevice, s));
+  ILG_CUDA(cudaMemcpyAsync(dtab, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice, s));
+  if (Qn) ILG_CUDA(cudaMemcpyAsync(qprev, Qn, (size_t)ncol * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  else ILG_CUDA(cudaMemsetAsync(qprev, 0, (size_t)ncol * sizeof(double), s));
+  StepView v{};
+  v.nt = ncol; v.nmesh = 1; v.md = dmd;
+  v.Tsurf = Tsurf; v.Fsurf = Fsurf; v.Qprev = qprev; v.T64 = T; v.coef64 = dtab;
+  v.rho64 = deep ? reinterpret_cast<double*>(base + L.rho) : nullptr;
+  v.derr = flags;
+  ILG_TRY(launch_conduct<double>(v, Qnp1, 0, nz, s));
+  int herr[DERR_COUNT];
+  ILG_CUDA(cudaMemcpyAsync(herr, flags, sizeof(herr), cudaMemcpyDeviceToHost, s));
+  ILG_CUDA(cudaStreamSynchronize(s));
+  if (herr[DERR_PIVOT]) { set_error("zero pivot in a conduction column"); return ILG_ERR_PIVOT; }
+  return ILG_OK;
+}

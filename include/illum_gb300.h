@@ -232,6 +232,35 @@ int ilg_conductionq_batch(int ncol, int nz, const double* z, double dt, const do
                           double emiss, double* Tsurf, double Fgeotherm, double* Fsurf,
                           int bc_mode);
 
+/* ---- conduction columns without allocation -------------------------------- */
+/* No counterpart in the reference (which has no device code): a variant of
+ * ilg_conductionq_batch for callers that cannot call cudaMalloc when they
+ * step their columns, e.g. code whose device memory belongs to another
+ * framework's caching allocator, or that runs under an exhausted memory
+ * budget. It allocates no device memory: its scratch is one fixed
+ * ILG_NOALLOC_SCRATCH_MB MiB array in the library, shared by all calls.
+ *
+ * T, Qn, Qnp1, Tsurf and Fsurf are DEVICE arrays of the current device; T is
+ * layer-major (T[i * ncol + f], layer i of column f), the transpose of
+ * ilg_conductionq_batch's host layout. z, ti, rhoc are nz host values. Qn
+ * may be NULL (zero; unused for ILG_BC_NEWTON). Work is queued on `stream`
+ * (a cudaStream_t; NULL = the legacy default stream) and the call returns
+ * once it has finished.
+ *
+ * Scratch needed: about 8*ncol + 40*nz bytes, plus 8*nz*ncol for columns
+ * deeper than 160 layers; a call needing more than the fixed array returns
+ * ILG_ERR_ARG without touching the device (split the columns into smaller
+ * calls). The first call on each device sets up the scratch's address for
+ * that device; make it before capturing a stream into a graph. Calls share
+ * the scratch: overlapping calls would race on it, so calls serialise on a
+ * process-wide lock. */
+#define ILG_NOALLOC_SCRATCH_MB 16
+int ilg_conductionq_batch_noalloc(int ncol, int nz, const double* z, double dt,
+                                  const double* Qn, const double* Qnp1, double* T,
+                                  const double* ti, const double* rhoc, double emiss,
+                                  double* Tsurf, double Fgeotherm, double* Fsurf, int bc_mode,
+                                  void* stream);
+
 #ifdef __cplusplus
 }
 #endif
