@@ -216,7 +216,7 @@ class IllumContext:
         a, b = C.c_int64(), C.c_int64()
         c, d = C.c_int(), C.c_int()
         _check(lib().ilg_F_info(self._h, C.byref(a), C.byref(b), C.byref(c), C.byref(d)))
-        return {"nnz": a.value, "sell_elems": b.value, "sell_slices": c.value, "active_rows": d.value}
+        return {"nnz": a.value, "stored_entries": b.value, "row_tiles": c.value, "active_rows": d.value}
 
     def set_F(self, rowptr, col, val):
         rowptr = np.ascontiguousarray(rowptr, np.int64); col = np.ascontiguousarray(col, np.int32); val = _f64(val)

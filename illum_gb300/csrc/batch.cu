@@ -24,7 +24,7 @@ __global__ void k_fill_int(int* a, int64_t n, int v) {
   if (i < n) a[i] = v;
 }
 
-// shift non-negative entries by off (columns / rows of a member's slices)
+// shift non-negative entries by off (a member's facet positions)
 __global__ void k_shift(int32_t* a, int64_t n, int off) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n && a[i] >= 0) a[i] += off;
@@ -35,18 +35,13 @@ __global__ void k_iota(uint32_t* a, int64_t n, int off) {
   if (i < n) a[i] = (uint32_t)(off + i);
 }
 
-__global__ void k_shift64(int64_t* a, int64_t n, int64_t off) {
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) a[i] += off;
-}
-
 }  // namespace
 
 struct Batch {
   std::vector<ilg_ctx*> members;
   std::vector<ilg_run_opts> opts;
   std::vector<MeshDesc> mh;
-  int nt = 0, precision = 0, nz_max = 0, nslices = 0;
+  int nt = 0, precision = 0, nz_max = 0, ntiles = 0;
   int64_t nel = 0;
   cudaStream_t stream = nullptr;
   cudaGraphExec_t graph = nullptr;
@@ -65,17 +60,16 @@ struct Batch {
   dbuf<float> x32;
   dbuf<double> T64, coef64;
   dbuf<float> T32, coef32;
-  dbuf<int64_t> sl_ptr;
-  dbuf<int32_t> sl_len, sl_split, sl_mesh, ln_row, ln_m, s_col;
-  dbuf<double> s_val;
-  dbuf<__nv_bfloat16> s_vbf;
-  dbuf<float> rscale;
+  dbuf<RowTile> tiles;
+  dbuf<uint16_t> t_cf;
+  dbuf<float2> t_val;
+  dbuf<double> tile_d2;
+  dbuf<__nv_bfloat16> t_vbf;
+  dbuf<uint32_t> t_row, t_halo, t_start;
+  dbuf<float> t_scale;
   dbuf<uint8_t> row_act;
   dbuf<uint32_t> rperm;
   dbuf<int> work, counters, derr, mesh_flag;
-  dbuf<double> sl_d2, ch_d2;
-  dbuf<int4> chunks;
-  int nchunks = 0;
   dbuf<unsigned> barrier;
   dbuf<float4> flush;
   ~Batch() {
@@ -97,7 +91,7 @@ static int build(Batch& b) {
   int n = (int)b.members.size();
   cudaStream_t s = b.stream;
   // sizes and offsets
-  int64_t nt = 0, nH = 0, nT = 0, ncoef = 0, nsun = 0, nsl = 0, nel = 0, ncb = 0, nch = 0;
+  int64_t nt = 0, nH = 0, nT = 0, ncoef = 0, nsun = 0, ntl = 0, nel = 0, ncb = 0, nrow = 0, nhal = 0;
   b.mh.assign(n, MeshDesc{});
   b.nz_max = 0;
   int ndisk = -1;
@@ -118,23 +112,24 @@ static int build(Batch& b) {
     M.coef0 = (int)ncoef;
     M.sun0 = (int)nsun;
     M.host_slot = (int)(nsun + c.nsun);
-    M.slice0 = (int)nsl;
-    M.chunk0 = (int)nch;
+    M.tile0 = (int)ntl;
     b.mh[i] = M;
     nt += c.nt;
     nH += (int64_t)c.nt * c.nphi;
     nT += (int64_t)c.nt * c.nz;
     ncoef += (int64_t)c.nz * 5;
     nsun += c.nsun + 1;
-    nsl += M.nslices;
-    nch += M.nchunks;
-    if (M.nslices) nel += c.sell_elems;
+    ntl += M.ntiles;
+    if (M.ntiles) {
+      nel += c.tile_elems;
+      nrow += c.n_active;
+      for (const RowTile& T : c.tiles_h) nhal += T.nhalo;
+    }
     ncb += div_up(c.nt, 128);
     b.nz_max = std::max(b.nz_max, c.nz);
   }
   b.nt = (int)nt;
-  b.nslices = (int)nsl;
-  b.nchunks = (int)nch;
+  b.ntiles = (int)ntl;
   b.nel = nel;
   bool mixed = b.precision == ILG_PREC_MIXED;
   // allocations
@@ -158,30 +153,43 @@ static int build(Batch& b) {
     ILG_TRY(b.T64.alloc(nT));
     ILG_TRY(b.coef64.alloc(ncoef));
   }
-  int64_t nsl1 = nsl > 0 ? nsl : 1, nel1 = nel > 0 ? nel : 1;
-  ILG_TRY(b.sl_ptr.alloc(nsl1)); ILG_TRY(b.sl_len.alloc(nsl1)); ILG_TRY(b.sl_split.alloc(nsl1));
-  ILG_TRY(b.sl_mesh.alloc(nsl1)); ILG_TRY(b.ln_row.alloc(32 * nsl1)); ILG_TRY(b.ln_m.alloc(32 * nsl1));
-  ILG_TRY(b.s_col.alloc(nel1)); ILG_TRY(b.s_val.alloc(nel1)); ILG_TRY(b.s_vbf.alloc(nel1));
-  ILG_TRY(b.rscale.alloc(nt)); ILG_TRY(b.row_act.alloc(nt));
+  const int RT = radiosity_threads();
+  int64_t ntl1 = ntl > 0 ? ntl : 1, nel1 = nel > 0 ? nel : 1;
+  ILG_TRY(b.tiles.alloc(ntl1)); ILG_TRY(b.tile_d2.alloc(2 * ntl1)); ILG_TRY(b.t_start.alloc(ntl1 * RT));
+  ILG_TRY(b.t_cf.alloc(nel1)); ILG_TRY(b.t_val.alloc(nel1)); ILG_TRY(b.t_vbf.alloc(nel1));
+  ILG_TRY(b.t_row.alloc(nrow > 0 ? nrow : 1)); ILG_TRY(b.t_scale.alloc(nrow > 0 ? nrow : 1));
+  ILG_TRY(b.t_halo.alloc(nhal > 0 ? nhal : 1));
+  ILG_TRY(b.row_act.alloc(nt));
   ILG_TRY(b.work.alloc(nt)); ILG_TRY(b.counters.alloc(8)); ILG_TRY(b.derr.alloc(DERR_COUNT));
-  ILG_TRY(b.mesh_flag.alloc(n)); ILG_TRY(b.sl_d2.alloc(nsl1)); ILG_TRY(b.barrier.alloc(2));
-  ILG_TRY(b.ch_d2.alloc(nch > 0 ? nch : 1));
-  std::vector<int4> chh;
-  for (int i = 0; i < n; ++i) {
-    const MeshDesc& M = b.mh[i];
-    int C = radiosity_chunk();
-    for (int k = 0; k < M.nchunks; ++k)
-      chh.push_back(make_int4(M.slice0 + k * C, std::min(C, M.nslices - k * C), i, 0));
+  ILG_TRY(b.mesh_flag.alloc(n)); ILG_TRY(b.barrier.alloc(2));
+  // the members' tiles, shifted to the scene's arrays
+  std::vector<RowTile> th;
+  {
+    int64_t e_off = 0, r_off = 0, h_off = 0;
+    for (int i = 0; i < n; ++i) {
+      Context& c = b.members[i]->c;
+      if (!b.mh[i].ntiles) continue;
+      for (RowTile T : c.tiles_h) {
+        T.e0 += e_off;
+        T.r0 += (int)r_off;
+        T.h0 += (int)h_off;
+        T.mesh = i;
+        th.push_back(T);
+      }
+      e_off += c.tile_elems;
+      r_off += c.n_active;
+      for (const RowTile& T : c.tiles_h) h_off += T.nhalo;
+    }
+    if (r_off > INT32_MAX || h_off > INT32_MAX) { set_error("batch too large for the radiosity tiles"); return ILG_ERR_ARG; }
   }
-  ILG_TRY(b.chunks.alloc(chh.empty() ? 1 : chh.size()));
-  if (!chh.empty())
-    ILG_CUDA(cudaMemcpyAsync(b.chunks.p, chh.data(), chh.size() * sizeof(int4), cudaMemcpyHostToDevice, s));
+  if (!th.empty())
+    ILG_CUDA(cudaMemcpyAsync(b.tiles.p, th.data(), th.size() * sizeof(RowTile), cudaMemcpyHostToDevice, s));
   ILG_CUDA(cudaMemsetAsync(b.row_act.p, 0, nt, s));
   ILG_CUDA(cudaMemsetAsync(b.counters.p, 0, 8 * sizeof(int), s));
   ILG_CUDA(cudaMemsetAsync(b.derr.p, 0, DERR_COUNT * sizeof(int), s));
   // copies
   std::vector<int2> cbh;
-  int64_t el = 0;
+  int64_t el = 0, ro = 0, ho = 0, to = 0;
   for (int i = 0; i < n; ++i) {
     Context& c = b.members[i]->c;
     MeshDesc& M = b.mh[i];
@@ -210,29 +218,29 @@ static int build(Batch& b) {
       ILG_TRY(cat(b.coef64, (size_t)M.coef0, c.coef64.p, (size_t)c.nz * 5, s));
     }
     if (c.have_F) {
-      ILG_TRY(cat(b.rscale, f0, c.row_scale.p, N, s));
       ILG_TRY(cat(b.row_act, f0, c.row_act.p, N, s));
       ILG_TRY(cat(b.rperm, f0, c.rperm.p, N, s));
       k_shift<<<div_up(N, 256), 256, 0, s>>>((int32_t*)(b.rperm.p + f0), N, (int)f0);
     } else {
       k_iota<<<div_up(N, 256), 256, 0, s>>>(b.rperm.p + f0, N, (int)f0);
     }
-    if (M.nslices > 0) {
-      size_t s0 = M.slice0, ns = M.nslices;
-      ILG_TRY(cat(b.sl_ptr, s0, c.sell_ptr.p, ns, s));
-      ILG_TRY(cat(b.sl_len, s0, c.sell_len.p, ns, s));
-      ILG_TRY(cat(b.sl_split, s0, c.sell_split.p, ns, s));
-      ILG_TRY(cat(b.ln_row, 32 * s0, c.sell_row.p, 32 * ns, s));
-      ILG_TRY(cat(b.ln_m, 32 * s0, c.sell_m.p, 32 * ns, s));
-      ILG_TRY(cat(b.s_col, (size_t)el, c.sell_col.p, (size_t)c.sell_elems, s));
-      ILG_TRY(cat(b.s_val, (size_t)el, c.sell_val.p, (size_t)c.sell_elems, s));
-      ILG_TRY(cat(b.s_vbf, (size_t)el, c.sell_vbf.p, (size_t)c.sell_elems, s));
-      k_shift64<<<div_up(ns, 256), 256, 0, s>>>(b.sl_ptr.p + s0, ns, el);
-      k_shift<<<div_up(32 * ns, 256), 256, 0, s>>>(b.ln_row.p + 32 * s0, 32 * ns, (int)f0);
-      k_shift<<<div_up(c.sell_elems, 256), 256, 0, s>>>(b.s_col.p + el, c.sell_elems, (int)f0);
-      k_fill_int<<<div_up(ns, 256), 256, 0, s>>>(b.sl_mesh.p + s0, ns, i);
+    if (M.ntiles > 0) {
+      int64_t nh = 0;
+      for (const RowTile& T : c.tiles_h) nh += T.nhalo;
+      ILG_TRY(cat(b.t_cf, (size_t)el, c.t_cf.p, (size_t)c.tile_elems, s));
+      ILG_TRY(cat(b.t_val, (size_t)el, c.t_val.p, (size_t)c.tile_elems, s));
+      ILG_TRY(cat(b.t_vbf, (size_t)el, c.t_vbf.p, (size_t)c.tile_elems, s));
+      ILG_TRY(cat(b.t_start, (size_t)to * RT, c.t_start.p, (size_t)M.ntiles * RT, s));
+      ILG_TRY(cat(b.t_row, (size_t)ro, c.t_row.p, (size_t)c.n_active, s));
+      ILG_TRY(cat(b.t_scale, (size_t)ro, c.t_scale.p, (size_t)c.n_active, s));
+      ILG_TRY(cat(b.t_halo, (size_t)ho, c.t_halo.p, (size_t)nh, s));
+      k_shift<<<div_up(c.n_active, 256), 256, 0, s>>>((int32_t*)(b.t_row.p + ro), c.n_active, (int)f0);
+      k_shift<<<div_up(nh, 256), 256, 0, s>>>((int32_t*)(b.t_halo.p + ho), nh, (int)f0);
       ILG_CUDA(cudaGetLastError());
-      el += c.sell_elems;
+      el += c.tile_elems;
+      ro += c.n_active;
+      ho += nh;
+      to += M.ntiles;
     }
     k_fill_int<<<div_up(N, 256), 256, 0, s>>>(b.mesh_of.p + f0, N, i);
     ILG_CUDA(cudaGetLastError());
@@ -251,17 +259,18 @@ static int build(Batch& b) {
   v.Tsurf = b.Tsurf.p; v.Fsurf = b.Fsurf.p; v.Qprev = b.Qprev.p; v.rad = b.rad.p; v.rad_avg = b.rad_avg.p;
   v.therm_avg = b.therm_avg.p; v.therm_max = b.therm_max.p; v.E = b.E.p; v.xprev = b.xprev.p;
   v.x32 = b.x32.p; v.T64 = b.T64.p; v.T32 = b.T32.p; v.coef64 = b.coef64.p; v.coef32 = b.coef32.p;
-  v.sl_ptr = b.sl_ptr.p; v.sl_len = b.sl_len.p; v.sl_split = b.sl_split.p; v.sl_mesh = b.sl_mesh.p;
-  v.ln_row = b.ln_row.p; v.ln_m = b.ln_m.p; v.s_col = b.s_col.p; v.s_val = b.s_val.p; v.s_vbf = b.s_vbf.p;
-  v.rscale = b.rscale.p; v.row_act = b.row_act.p; v.nslices = b.nslices;
+  v.tiles = b.tiles.p; v.ntiles = b.ntiles;
+  v.t_cf = b.t_cf.p; v.t_val = b.t_val.p; v.t_vbf = b.t_vbf.p;
+  v.t_row = b.t_row.p; v.t_halo = b.t_halo.p; v.t_start = b.t_start.p; v.t_scale = b.t_scale.p;
+  v.tile_d2 = b.tile_d2.p;
+  v.row_act = b.row_act.p;
   v.rperm = b.rperm.p; v.rbuf = b.xtmp.p;
   v.cblocks = b.cblocks.p; v.ncblocks = (int)ncb;
-  v.chunks = b.chunks.p; v.nchunks = b.nchunks;
   v.work = b.work.p; v.counters = b.counters.p; v.derr = b.derr.p; v.mesh_flag = b.mesh_flag.p;
-  v.sl_d2 = b.sl_d2.p; v.ch_d2 = b.ch_d2.p; v.barrier = b.barrier.p;
+  v.barrier = b.barrier.p;
   b.plan.precision = b.precision;
-  b.plan.rad_on = b.nslices > 0;
-  b.plan.rad_grid = b.plan.rad_on ? radiosity_grid(b.nslices, b.precision) : 1;
+  b.plan.rad_on = b.ntiles > 0;
+  b.plan.rad_grid = b.plan.rad_on ? radiosity_grid(b.ntiles, b.precision) : 1;
   b.plan.nz_max = b.nz_max;
   return ILG_OK;
 }

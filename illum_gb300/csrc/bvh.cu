@@ -687,7 +687,7 @@ int form_factors_build(Context& c, const double* albedo_h, double albedo_scalar,
   ILG_TRY(cj.alloc(npairs > 0 ? npairs : 1));
   ILG_TRY(keys.alloc(npairs > 0 ? npairs : 1));
   c.have_F = false;
-  c.have_bf16 = false;
+  c.ntiles = 0;
   if (npairs > 0) {
     k_candidates<true><<<div_up(nt, 128), 128, 0, s>>>(c.nodes.p, c.tri_s.p, c.root, c.cen.p, c.nrm.p, nt, c.r_max,
                                                        slack, nullptr, offs.p, ci.p, cj.p, c.derr.p);

@@ -145,15 +145,15 @@ static StepView solo_view(Context& c, int precision) {
   v.x32 = c.x32.p;
   v.T64 = c.T64.p; v.T32 = c.T32.p;
   v.coef64 = c.coef64.p; v.coef32 = c.coef32.p;
-  v.sl_ptr = c.sell_ptr.p; v.sl_len = c.sell_len.p; v.sl_split = c.sell_split.p; v.sl_mesh = nullptr;
-  v.ln_row = c.sell_row.p; v.ln_m = c.sell_m.p; v.s_col = c.sell_col.p; v.s_val = c.sell_val.p;
-  v.s_vbf = c.sell_vbf.p; v.rscale = c.row_scale.p; v.row_act = c.row_act.p; v.rperm = c.rperm.p;
+  v.tiles = c.tiles.p; v.ntiles = c.have_F ? c.ntiles : 0;
+  v.t_cf = c.t_cf.p; v.t_val = c.t_val.p; v.t_vbf = c.t_vbf.p;
+  v.t_row = c.t_row.p; v.t_halo = c.t_halo.p; v.t_start = c.t_start.p; v.t_scale = c.t_scale.p;
+  v.tile_d2 = c.tile_d2.p;
+  v.row_act = c.row_act.p; v.rperm = c.rperm.p;
   v.rbuf = c.xtmp.p;
-  v.nslices = c.have_F ? c.sell_nslices : 0;
   v.cblocks = nullptr; v.ncblocks = 0;
-  v.chunks = c.chunks.p; v.nchunks = c.have_F ? c.nchunks : 0;
   v.work = c.work.p; v.counters = c.counters.p; v.derr = c.derr.p; v.mesh_flag = c.mesh_flag.p;
-  v.sl_d2 = c.sl_d2.p; v.ch_d2 = c.ch_d2.p; v.barrier = c.barrier.p;
+  v.barrier = c.barrier.p;
   v.rho64 = nullptr; v.rho32 = nullptr;
   (void)precision;
   return v;
@@ -181,10 +181,8 @@ MeshDesc solo_desc(const Context& c, const ilg_run_opts* o, int first_sun) {
   M.coef0 = 0;
   M.T0 = 0;
   M.cs = c.cond_cs;
-  M.slice0 = 0;
-  M.nslices = (o && o->use_radiosity && c.have_F) ? c.sell_nslices : 0;
-  M.chunk0 = 0;
-  M.nchunks = M.nslices > 0 ? c.nchunks : 0;
+  M.tile0 = 0;
+  M.ntiles = (o && o->use_radiosity && c.have_F) ? c.ntiles : 0;
   M.tol2 = o ? o->tol * o->tol : 0.0;
   M.max_sweeps = o ? o->max_sweeps : 1;
   M.active = 1;
@@ -208,7 +206,6 @@ static int ensure_step_buffers(Context& c, int precision) {
     ILG_CUDA(cudaMemset(c.xprev.p, 0, (size_t)c.nt * 8));
   }
   if (precision == ILG_PREC_MIXED) ILG_TRY(c.x32.reserve((size_t)3 * c.nt));
-  ILG_TRY(c.sl_d2.reserve(c.sell_nslices > 0 ? c.sell_nslices : 1));
   ILG_TRY(c.md.reserve(1));
   ILG_TRY(c.mesh_flag.reserve(1));
   return ILG_OK;
@@ -237,8 +234,8 @@ int check_run(Context& c, const ilg_run_opts* o, bool host_driven) {
 static StepPlan solo_plan(Context& c, const ilg_run_opts& o) {
   StepPlan p;
   p.precision = o.precision;
-  p.rad_on = o.use_radiosity && c.have_F && c.sell_nslices > 0;
-  p.rad_grid = p.rad_on ? radiosity_grid(c.sell_nslices, o.precision) : 1;
+  p.rad_on = o.use_radiosity && c.have_F && c.ntiles > 0;
+  p.rad_grid = p.rad_on ? radiosity_grid(c.ntiles, o.precision) : 1;
   p.nz_max = c.nz;
   return p;
 }
@@ -247,7 +244,7 @@ static StepPlan solo_plan(Context& c, const ilg_run_opts& o) {
 // surface-temperature download after the step (host-driven steps).
 static int get_graph(Context& c, const ilg_run_opts& o, bool with_copies, cudaGraphExec_t* out) {
   int key[4] = {o.precision * 4 + o.coupling * 2 + (o.use_radiosity ? 1 : 0), with_copies ? 1 : 0, c.nz,
-                c.sell_nslices};
+                c.ntiles};
   if (c.graph && std::equal(key, key + 4, c.graph_key)) { *out = c.graph; return ILG_OK; }
   invalidate_graph(c);
   StepView v = solo_view(c, o.precision);
@@ -379,12 +376,12 @@ int ilg_ctx_info(const ilg_ctx* ctx, int64_t* bvh_nodes, int* bvh_depth) {
   return ILG_OK;
 }
 
-int ilg_F_info(const ilg_ctx* ctx, int64_t* nnz, int64_t* sell_elems, int* sell_slices, int* active_rows) {
+int ilg_F_info(const ilg_ctx* ctx, int64_t* nnz, int64_t* stored_entries, int* row_tiles, int* active_rows) {
   if (!ctx || !ctx->c.have_F) { set_error("no form factors"); return ILG_ERR_ARG; }
   const Context& c = ctx->c;
   if (nnz) *nnz = c.nnz;
-  if (sell_elems) *sell_elems = c.sell_elems;
-  if (sell_slices) *sell_slices = c.sell_nslices;
+  if (stored_entries) *stored_entries = c.tile_elems;
+  if (row_tiles) *row_tiles = c.ntiles;
   if (active_rows) *active_rows = c.n_active;
   return ILG_OK;
 }
@@ -514,7 +511,7 @@ int ilg_radiosity_solve(ilg_ctx* ctx, const double* E, double tol, int max_sweep
   if (!ctx || !E || !x || max_sweeps < 1 || !(tol >= 0.0)) { set_error("invalid radiosity arguments"); return ILG_ERR_ARG; }
   Context& c = ctx->c;
   if (!c.have_F) { set_error("no form factors"); return ILG_ERR_ARG; }
-  if (c.sell_nslices == 0) {
+  if (c.ntiles == 0) {
     std::memcpy(x, E, (size_t)c.nt * 8);
     if (res) *res = 0.0;
     if (sweeps) *sweeps = 0;
@@ -529,7 +526,7 @@ int ilg_radiosity_solve(ilg_ctx* ctx, const double* E, double tol, int max_sweep
   ILG_TRY(upload_desc(c, M));
   ILG_CUDA(cudaMemcpyAsync(c.E.p, E, (size_t)c.nt * 8, cudaMemcpyHostToDevice, c.stream));
   StepView v = solo_view(c, ILG_PREC_FP64);
-  ILG_TRY(radiosity_launch(v, c.Q.p, 0, ILG_PREC_FP64, radiosity_grid(c.sell_nslices, ILG_PREC_FP64), c.stream));
+  ILG_TRY(radiosity_launch(v, c.Q.p, 0, ILG_PREC_FP64, radiosity_grid(c.ntiles, ILG_PREC_FP64), c.stream));
   MeshDesc out;
   ILG_CUDA(cudaMemcpyAsync(x, c.Q.p, (size_t)c.nt * 8, cudaMemcpyDeviceToHost, c.stream));
   ILG_CUDA(cudaMemcpyAsync(&out, c.md.p, sizeof(out), cudaMemcpyDeviceToHost, c.stream));

@@ -40,7 +40,7 @@ __device__ __forceinline__ const SunAux* mesh_sun(const StepView& v, const MeshD
 __device__ __forceinline__ void store_direct(const StepView& v, const MeshDesc& M, int g, double dv, int dropin) {
   if (dropin) { v.E[g] = dv; return; }
   double e = M.coupling == ILG_COUPLE_REFERENCE ? (-v.Fsurf[g] + dv) : dv;
-  if (M.nslices > 0) v.E[g] = e; else v.rad[g] = e;
+  if (M.ntiles > 0) v.E[g] = e; else v.rad[g] = e;
 }
 
 // Range of the horizon threshold of src/cpp/illum.cpp:431-434 over the

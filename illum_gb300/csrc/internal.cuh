@@ -52,8 +52,20 @@ struct SunAux {
   float ang_eps;         // bound on the angle between S/|S| and S - p
 };
 
+// A run of Morton-consecutive rows of the form-factor matrix solved by one
+// block (radiosity.cu): its entries, split evenly over the block's threads,
+// and the compact set of facets its rows see (the halo).
+struct RowTile {
+  int64_t e0;                  // first stored entry (lam x 1024 entries)
+  int lam;                     // entries per thread (multiple of 4)
+  int nrows;                   // rows (all with entries)
+  int r0;                      // first row in t_row / t_scale
+  int h0, nhalo;               // halo entries in t_halo
+  int mesh;
+};
+
 // One mesh of a scene: where its facets, horizons, layers, suns and
-// radiosity slices live in the scene's arrays, and its run state. The step
+// radiosity tiles live in the scene's arrays, and its run state. The step
 // kernels read it from device memory, so a captured step graph stays valid
 // while meshes advance, finish or are switched off.
 struct MeshDesc {
@@ -68,8 +80,7 @@ struct MeshDesc {
   int nz, coef0;               // layers; offset of the conduction table
   int64_t T0;                  // offset of the mesh's [nz][nfacet] layer block
   CondScalars cs;
-  int slice0, nslices;         // radiosity SELL slices
-  int chunk0, nchunks;         // residual-reduction chunks of the slices
+  int tile0, ntiles;           // radiosity row tiles (0: no radiosity)
   double tol2;                 // squared residual tolerance
   int max_sweeps;
   int sweeps;                  // out: sweeps of the last solve
@@ -93,25 +104,23 @@ struct StepView {
   float* T32;
   const double* coef64;
   const float* coef32;
-  // radiosity SELL-32
-  const int64_t* sl_ptr;
-  const int32_t *sl_len, *sl_split, *sl_mesh, *ln_row, *ln_m, *s_col;
-  const double* s_val;
-  const __nv_bfloat16* s_vbf;
-  const float* rscale;
+  // radiosity row tiles
+  const RowTile* tiles;
+  int ntiles;
+  const uint16_t* t_cf;        // per stored entry: halo index | row end << 15
+  const float2* t_val;         // double-float values (hi, lo)
+  const __nv_bfloat16* t_vbf;  // value / row scale
+  const uint32_t *t_row, *t_halo, *t_start;   // tile rows and halos (positions); per-thread first row
+  const float* t_scale;        // per tile row: bf16 scale
+  double* tile_d2;             // 2 x ntiles residual partials
   const uint8_t* row_act;      // per facet: its row has entries
   const uint32_t* rperm;       // radiosity position -> facet (Morton order within each mesh)
   double* rbuf;                // 3 x nt: E, and two iterates, in radiosity positions
-  int nslices;
   // conduction blocks: (mesh, first local facet), or nullptr for a single mesh
   const int2* cblocks;
   int ncblocks;
-  // residual-reduction chunks: (first slice, count, mesh, 0)
-  const int4* chunks;
-  int nchunks;
   // scratch
   int *work, *counters, *derr, *mesh_flag;
-  double *sl_d2, *ch_d2;
   unsigned* barrier;
   double* rho64;               // deep-column conduction scratch [nz][nt] (or nullptr)
   float* rho32;
@@ -148,18 +157,19 @@ struct Context {
   dbuf<int64_t> rowptr;
   dbuf<int32_t> col;
   dbuf<double> val;
-  dbuf<int32_t> active;           // rows with at least one entry
-  int n_active = 0;
-  dbuf<__nv_bfloat16> val_bf16;   // mixed precision copy
-  dbuf<float> row_scale;
-  bool have_bf16 = false;
-  // SELL-32 copy of the active rows for the sweeps (radiosity.cu)
-  int sell_nslices = 0;
-  int64_t sell_elems = 0;
-  dbuf<int64_t> sell_ptr;
-  dbuf<int32_t> sell_len, sell_split, sell_row, sell_m, sell_col;
-  dbuf<double> sell_val;
-  dbuf<__nv_bfloat16> sell_vbf;
+  int n_active = 0;               // rows with at least one entry
+  dbuf<float> row_scale;          // per facet: max |F_ij| of its row
+  // row tiles of the active rows for the sweeps (radiosity.cu)
+  int ntiles = 0;
+  int64_t tile_elems = 0;
+  std::vector<RowTile> tiles_h;
+  dbuf<RowTile> tiles;
+  dbuf<uint16_t> t_cf;
+  dbuf<float2> t_val;
+  dbuf<__nv_bfloat16> t_vbf;
+  dbuf<uint32_t> t_row, t_halo, t_start;
+  dbuf<float> t_scale;
+  dbuf<double> tile_d2;
   dbuf<uint8_t> row_act;
   dbuf<uint32_t> rperm;           // Morton position -> facet (radiosity's internal order)
 
@@ -200,9 +210,6 @@ struct Context {
   MeshDesc mh{};                  // host mirror of the one-mesh descriptor
   dbuf<MeshDesc> md;
   dbuf<int> mesh_flag;
-  dbuf<double> sl_d2, ch_d2;
-  dbuf<int4> chunks;
-  int nchunks = 0;
   double* pinned_tsurf = nullptr;
   int64_t stats_ambiguous = 0, stats_sweeps = 0;
   bool timing = false;
@@ -245,9 +252,9 @@ int direct_launch(const StepView& v, int dropin, cudaStream_t s);
 
 // ---- radiosity.cu ----
 int radiosity_prepare(Context& c);
-int radiosity_grid(int nslices, int precision);
-int radiosity_chunk();
+int radiosity_grid(int ntiles, int precision);
 int radiosity_max_meshes();
+int radiosity_threads();
 int radiosity_launch(const StepView& v, double* x, int warm, int precision, int grid, cudaStream_t s);
 
 // ---- capi.cu ----

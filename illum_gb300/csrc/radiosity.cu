@@ -5,24 +5,39 @@
 //
 // GPU scheme: Jacobi sweeps x <- E + F x over the rows that have entries
 // (rows without entries are x = E exactly) inside ONE persistent cooperative
-// kernel. The matrix is stored as SELL-32 (slices of 32 rows, column-major,
-// one lane per row or row chunk, fixed summation order) and the solve works
-// on facets renumbered in the LBVH's Morton order, so the gathers of x hit
-// few cache lines. A grid barrier separates sweeps and every block reduces
-// the residual partials in the same fixed order, so all blocks take the same
-// stop decision and results are run-to-run deterministic. The residual of
-// iterate x_k is E - (I - F) x_k = x_{k+1} - x_k, so it comes for free
-// with the next sweep; iteration stops once its 2-norm is <= tol.
+// kernel, one grid barrier per sweep. The solve works on facets renumbered in
+// the LBVH's Morton order, and the matrix is cut into row tiles: runs of
+// Morton-consecutive rows with about nnz / (co-resident blocks) entries each.
+// A tile's rows see a compact set of facets (its halo), so a block first
+// gathers the halo's x values into shared memory and then streams the tile's
+// entries, each a 16-bit halo index (plus a row-end bit) and a value. The
+// tile's entries, row after row, are split into equal runs, one per thread
+// (entries of a row that straddles threads are combined in a fixed order),
+// so every thread of every block does the same amount of work whatever the
+// row lengths. Every block reduces the per-tile residual partials in the
+// same fixed order, so all blocks take the same stop decisions and results
+// are run-to-run deterministic. The residual of iterate x_k is
+// E - (I - F) x_k = x_{k+1} - x_k, so it comes for free with the next sweep;
+// iteration stops once its 2-norm is <= tol.
 // With albedo-scaled form factors the iteration matrix has spectral radius
 // well below 1, so Jacobi converges in a handful of sweeps; a multicolour
 // Gauss-Seidel would need one grid barrier per colour, and the cliques of
 // mutually visible crater facets force hundreds of colours.
 //
+// FP64 arithmetic runs at about one fused multiply-add per clock per SM on
+// GB300, so the double-precision sweeps evaluate their dot products in
+// FP32-pair ("double-float") arithmetic on the FP32 pipes instead: each
+// value and each x is split into hi + lo floats (48 significant bits), the
+// product hi*hi is taken exactly with an FMA, the cross terms are added,
+// and the running sum is kept as an unevaluated float pair by TwoSum
+// (Dekker 1971; Knuth TAOCP vol. 2, 4.2.2). The relative error of a row sum
+// is ~2^-46 (vs 2^-53 for FP64), orders of magnitude below the solve
+// tolerance; everything per row (residual, iterate, convergence) is FP64.
+//
 // Mixed precision: values stored as bf16 with a per-row fp32 scale, fp32
-// accumulation for the sweeps, and an outer refinement whose residual is
-// evaluated with the fp64 values in fp64 (so the fixed point is the fp64
-// system's).
-#include <cooperative_groups.h>
+// accumulation for the inner sweeps, and an outer refinement whose residual
+// is evaluated with the double-float dot products above (so the fixed point
+// is the fp64 system's).
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -36,9 +51,17 @@ namespace ilg {
 namespace {
 
 constexpr int RAD_THREADS = 1024;
+constexpr int RAD_HALO = 16384;          // halo values per tile (double-float: 128 KB of shared memory)
+constexpr int RAD_ROWS = 6144;           // rows per tile (their sums: 48 KB of shared memory)
+constexpr int RAD_MAX_MESH = 1024;
+constexpr int64_t RAD_MIN_TILE = 16384;  // entries: smaller tiles cost more in staging than they balance
+constexpr size_t RAD_SMEM =
+    (size_t)RAD_HALO * sizeof(float2) + RAD_THREADS * sizeof(float2) + RAD_ROWS * sizeof(double) + RAD_THREADS;
 
 // Grid barrier for a cooperative launch (all blocks co-resident). The wait
 // is bounded: after ~2^26 polls it records DERR_BARRIER and returns false.
+// The fences make the iterates written before the barrier visible to the
+// loads after it.
 __device__ bool grid_barrier(unsigned* bar, unsigned nblocks, int* derr) {
   __shared__ int ok;
   __syncthreads();
@@ -69,85 +92,34 @@ __device__ bool grid_barrier(unsigned* bar, unsigned nblocks, int* derr) {
 }
 
 __device__ __forceinline__ int mesh_of_facet(const StepView& v, int g) { return v.mesh_of ? v.mesh_of[g] : 0; }
-__device__ __forceinline__ int mesh_of_slice(const StepView& v, int sl) { return v.sl_mesh ? v.sl_mesh[sl] : 0; }
 
-// Loads of the matrix carry an L2 evict-last policy on a fraction of the
-// lines: the SELL arrays (~12-16 B per entry) are re-read by every sweep of
-// a solve, and when they are about as large as GB300's 126 MB L2 a plain
-// cyclic scan would evict every line before its reuse. Keeping 3/4 of the
-// lines at evict-last lets sweeps after the first hit L2 for most of the
-// matrix while the rest streams from HBM.
+// Matrix loads: read-only for the whole solve, so the non-coherent path, no
+// L1 allocation (each entry is used once per sweep), and an L2 evict-last
+// policy on 3/4 of the lines so that repeated sweeps find most of the
+// matrix in L2 when it is about as large as L2.
 __device__ __forceinline__ uint64_t l2_keep_policy() {
   uint64_t pol;
   asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 0.75;" : "=l"(pol));
   return pol;
 }
-__device__ __forceinline__ int ld_keep(const int32_t* p, uint64_t pol) {
-  int v;
-  asm volatile("ld.global.nc.L2::cache_hint.b32 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol));
-  return v;
+__device__ __forceinline__ uint2 ld_mat(const uint2* p, uint64_t pol) {
+  uint2 r;
+  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v2.u32 {%0, %1}, [%2], %3;"
+               : "=r"(r.x), "=r"(r.y) : "l"(p), "l"(pol));
+  return r;
 }
-__device__ __forceinline__ double ld_keep(const double* p, uint64_t pol) {
-  double v;
-  asm volatile("ld.global.nc.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(p), "l"(pol));
-  return v;
+__device__ __forceinline__ void ld_mat4(const float2* p, float2 (&w)[4], uint64_t pol) {
+  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
+               : "=f"(w[0].x), "=f"(w[0].y), "=f"(w[1].x), "=f"(w[1].y) : "l"(p), "l"(pol));
+  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
+               : "=f"(w[2].x), "=f"(w[2].y), "=f"(w[3].x), "=f"(w[3].y) : "l"(p + 2), "l"(pol));
 }
-__device__ __forceinline__ __nv_bfloat16 ld_keep(const __nv_bfloat16* p, uint64_t pol) {
-  unsigned short v;
-  asm volatile("ld.global.nc.L2::cache_hint.b16 %0, [%1], %2;" : "=h"(v) : "l"(p), "l"(pol));
-  return __ushort_as_bfloat16(v);
-}
-
-// One SELL-32 slice: lane l accumulates its (chunk of a) row sequentially
-// (four independent loads in flight), then rows split into several chunks
-// are combined into their first lane in a fixed order.
-template <class V, class X, class Acc>
-__device__ __forceinline__ Acc slice_dot(const StepView& v, const V* __restrict__ sval, const X* __restrict__ x,
-                                         int sl, int lane) {
-  int64_t base = v.sl_ptr[sl] + lane;
-  int len = v.sl_len[sl];
-  const uint64_t pol = l2_keep_policy();
-  Acc p = 0;
-  int k = 0;
-  for (; k + 8 <= len; k += 8) {
-    int c[8];
-    V w[8];
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      c[j] = ld_keep(v.s_col + base + (int64_t)(k + j) * 32, pol);
-      w[j] = ld_keep(sval + base + (int64_t)(k + j) * 32, pol);
-    }
-    X xv[8];
-#pragma unroll
-    for (int j = 0; j < 8; ++j) xv[j] = x[c[j]];
-#pragma unroll
-    for (int j = 0; j < 8; ++j) p += (Acc)w[j] * (Acc)xv[j];
-  }
-  if (k < len) {   // len is a multiple of 4
-    int c[4];
-    V w[4];
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      c[j] = ld_keep(v.s_col + base + (int64_t)(k + j) * 32, pol);
-      w[j] = ld_keep(sval + base + (int64_t)(k + j) * 32, pol);
-    }
-    X xv[4];
-#pragma unroll
-    for (int j = 0; j < 4; ++j) xv[j] = x[c[j]];
-#pragma unroll
-    for (int j = 0; j < 4; ++j) p += (Acc)w[j] * (Acc)xv[j];
-  }
-  int mmax = v.sl_split[sl];
-  if (mmax > 1) {
-    int m = v.ln_m[(int64_t)sl * 32 + lane];
-    Acc tot = p;
-    for (int j = 1; j < mmax; ++j) {
-      Acc q = __shfl_down_sync(0xffffffffu, p, j);
-      if (j < m) tot += q;
-    }
-    p = tot;
-  }
-  return p;
+__device__ __forceinline__ void ld_mat4(const __nv_bfloat16* p, float (&w)[4], uint64_t pol) {
+  uint2 r = ld_mat(reinterpret_cast<const uint2*>(p), pol);
+  w[0] = __uint_as_float(r.x << 16);
+  w[1] = __uint_as_float(r.x & 0xffff0000u);
+  w[2] = __uint_as_float(r.y << 16);
+  w[3] = __uint_as_float(r.y & 0xffff0000u);
 }
 
 __device__ __forceinline__ double warp_sum(double x) {
@@ -155,16 +127,193 @@ __device__ __forceinline__ double warp_sum(double x) {
   return x;
 }
 
-// Per-mesh convergence. Residual partials are reduced in a fixed order that
-// depends only on the mesh's own slices: each slice's partial (warp sum),
-// then chunks of RAD_CHUNK consecutive slices of the mesh (one warp per
-// chunk), then the mesh's chunks in order. Every block repeats the last
-// stage for every mesh and keeps the stop flags in shared memory, so all
-// blocks take the same decisions without another barrier, and a mesh's
-// decisions are the same alone and in a batch.
-constexpr int RAD_CHUNK = 256;
-constexpr int RAD_MAX_MESH = 1024;
+// Double-float: v = hi + lo with hi = fl(v), lo = fl(v - hi).
+__device__ __forceinline__ float2 split_df(double x) {
+  float h = __double2float_rn(x);
+  return make_float2(h, __double2float_rn(x - (double)h));
+}
 
+// Running sum of double-float products. add(): p + e = w.hi * x.hi exactly
+// (FMA), plus the cross terms w.hi * x.lo + w.lo * x.hi in e; (h, l) += p
+// by TwoSum, l += e. Intrinsics keep the compiler from contracting or
+// reassociating the error-free steps.
+struct AccDF {
+  typedef float2 W;
+  typedef float2 X;
+  typedef float2 Part;
+  typedef double Sum;
+  float h, l;
+  __device__ __forceinline__ void zero() { h = 0.f; l = 0.f; }
+  __device__ __forceinline__ void two_sum(float p) {
+    float t = __fadd_rn(h, p);
+    float bp = __fsub_rn(t, h);
+    float err = __fadd_rn(__fsub_rn(h, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+    h = t;
+    l = __fadd_rn(l, err);
+  }
+  __device__ __forceinline__ void add(float2 w, float2 x) {
+    float p = __fmul_rn(w.x, x.x);
+    float e = __fmaf_rn(w.x, x.x, -p);
+    e = __fmaf_rn(w.x, x.y, e);
+    e = __fmaf_rn(w.y, x.x, e);
+    two_sum(p);
+    l = __fadd_rn(l, e);
+  }
+  __device__ __forceinline__ Part part() const { return make_float2(h, l); }
+  __device__ __forceinline__ void merge(Part q) {
+    two_sum(q.x);
+    l = __fadd_rn(l, q.y);
+  }
+  __device__ __forceinline__ double get() const { return (double)h + (double)l; }
+};
+
+// Plain fp32 sum (mixed inner sweeps: bf16 values, fp32 iterates).
+struct AccF32 {
+  typedef float W;
+  typedef float X;
+  typedef float Part;
+  typedef float Sum;
+  float s;
+  __device__ __forceinline__ void zero() { s = 0.f; }
+  __device__ __forceinline__ void add(float w, float x) { s = fmaf(w, x, s); }
+  __device__ __forceinline__ Part part() const { return s; }
+  __device__ __forceinline__ void merge(Part q) { s += q; }
+  __device__ __forceinline__ float get() const { return s; }
+};
+
+__device__ __forceinline__ float2 to_halo(double x, float2*) { return split_df(x); }
+__device__ __forceinline__ float to_halo(float x, float*) { return x; }
+
+// Iterates written by other blocks during the solve are read at L2 (never
+// from a possibly stale L1 line).
+__device__ __forceinline__ double ld_it(const double* p) { return __ldcg(p); }
+__device__ __forceinline__ float ld_it(const float* p) { return __ldcg(p); }
+
+// Gather the tile's halo values x[halo[h]] into shared memory.
+template <class XS, class XG>
+__device__ __forceinline__ void stage_halo(const StepView& v, const RowTile& T, const XG* xg, XS* sx) {
+  const uint32_t* hp = v.t_halo + T.h0;
+  int h = threadIdx.x;
+  for (; h + 3 * RAD_THREADS < T.nhalo; h += 4 * RAD_THREADS) {
+    uint32_t a = __ldg(hp + h), b = __ldg(hp + h + RAD_THREADS), c = __ldg(hp + h + 2 * RAD_THREADS),
+             d = __ldg(hp + h + 3 * RAD_THREADS);
+    XG xa = ld_it(xg + a), xb = ld_it(xg + b), xc = ld_it(xg + c), xd = ld_it(xg + d);
+    sx[h] = to_halo(xa, sx);
+    sx[h + RAD_THREADS] = to_halo(xb, sx);
+    sx[h + 2 * RAD_THREADS] = to_halo(xc, sx);
+    sx[h + 3 * RAD_THREADS] = to_halo(xd, sx);
+  }
+  for (; h < T.nhalo; h += RAD_THREADS) sx[h] = to_halo(ld_it(xg + __ldg(hp + h)), sx);
+  __syncthreads();
+}
+
+// One tile: thread t owns entries [t*lam, (t+1)*lam) of the tile's entry
+// stream (rows in order, each row's entries in column order), stored so that
+// a warp's loads are contiguous: entry k of thread t at e0 + (k/4)*4096 +
+// 4t + k%4. Each thread accumulates sequentially (two groups of four
+// entries in flight ahead of the one being summed) and stores the sum of
+// every row that starts and ends in its run in rs[row] (shared memory). A
+// row that began in an earlier thread is completed by the thread where it
+// ends: the partial sums of the threads it spans, in thread order, then its
+// own part. Ends with a block barrier: rs holds every row sum of the tile.
+template <class Acc, class V>
+__device__ __forceinline__ void tile_rows(const StepView& v, const RowTile& T, int t, const V* vals,
+                                          const typename Acc::X* sx, typename Acc::Part* tail, unsigned char* tnew,
+                                          typename Acc::Sum* rs, uint64_t pol) {
+  typedef typename Acc::W W;
+  const int tid = threadIdx.x;
+  const uint32_t s0 = __ldg(v.t_start + (size_t)t * RAD_THREADS + tid);
+  int r = (int)(s0 & 0x7fffffffu);
+  const bool cont = (s0 >> 31) != 0;
+  bool any = false, has_head = false;
+  int head_row = 0;
+  Acc acc, head;
+  acc.zero();
+  head.zero();
+  const uint2* cfp = reinterpret_cast<const uint2*>(v.t_cf + T.e0) + tid;
+  const V* vp = vals + T.e0 + 4 * tid;
+  const int ng = T.lam >> 2;
+  auto elem = [&](uint32_t c, W w) {
+    acc.add(w, sx[c & 0x7fffu]);
+    if (c & 0x8000u) {
+      if (cont && !any) {
+        head = acc;
+        head_row = r;
+        has_head = true;
+      } else {
+        rs[r] = acc.get();
+      }
+      ++r;
+      acc.zero();
+      any = true;
+    }
+  };
+  uint2 c0 = ld_mat(cfp, pol), c1 = c0;
+  W w0[4], w1[4];
+  ld_mat4(vp, w0, pol);
+  if (ng > 1) {
+    c1 = ld_mat(cfp + RAD_THREADS, pol);
+    ld_mat4(vp + 4 * RAD_THREADS, w1, pol);
+  } else {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) w1[j] = w0[j];
+  }
+  for (int g = 0; g < ng; ++g) {
+    uint2 c2 = c1;
+    W w2[4];
+    if (g + 2 < ng) {
+      c2 = ld_mat(cfp + (size_t)(g + 2) * RAD_THREADS, pol);
+      ld_mat4(vp + (size_t)(g + 2) * 4 * RAD_THREADS, w2, pol);
+    } else {
+#pragma unroll
+      for (int j = 0; j < 4; ++j) w2[j] = w1[j];
+    }
+    elem(c0.x & 0xffffu, w0[0]);
+    elem(c0.x >> 16, w0[1]);
+    elem(c0.y & 0xffffu, w0[2]);
+    elem(c0.y >> 16, w0[3]);
+    c0 = c1;
+    c1 = c2;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      w0[j] = w1[j];
+      w1[j] = w2[j];
+    }
+  }
+  tail[tid] = acc.part();
+  tnew[tid] = (any || !cont) ? 1 : 0;
+  __syncthreads();
+  if (has_head) {
+    int u = tid - 1;
+    while (!tnew[u]) --u;   // thread 0 starts a row, so this stops
+    Acc s;
+    s.zero();
+    for (; u < tid; ++u) s.merge(tail[u]);
+    s.merge(head.part());
+    rs[head_row] = s.get();
+  }
+  __syncthreads();
+}
+
+// Block sum in a fixed order; thread 0 stores it. Ends with a block barrier
+// (the tile's shared arrays are free again).
+__device__ __forceinline__ void block_sum_store(double d, double* red, double* out) {
+  d = warp_sum(d);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = d;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double t = warp_sum(red[threadIdx.x]);
+    if (threadIdx.x == 0) *out = t;
+  }
+  __syncthreads();
+}
+
+// Per-mesh convergence: a mesh's residual is the sum of its tiles' partials
+// (lane-strided over the tiles, then a fixed warp tree), computed by every
+// block for every running mesh, so all blocks take the same decisions
+// without another barrier, and a mesh's decisions are the same alone and in
+// a batch. Tile partials are double-buffered by sweep parity: a block that
+// runs ahead into the next sweep writes the other buffer.
 struct MeshState {
   int done[RAD_MAX_MESH];
   int sweeps[RAD_MAX_MESH];
@@ -173,53 +322,32 @@ struct MeshState {
 __device__ __forceinline__ void init_meshes(const StepView& v, MeshState& st) {
   for (int m = threadIdx.x; m < v.nmesh; m += blockDim.x) {
     const MeshDesc& M = v.md[m];
-    st.done[m] = (M.active && M.nslices > 0) ? 0 : 1;
+    st.done[m] = (M.active && M.ntiles > 0) ? 0 : 1;
     st.sweeps[m] = 0;
   }
 }
 
-// chunk sums of all meshes still running (one warp per chunk)
-__device__ __forceinline__ void chunk_sums(const StepView& v, const MeshState& st, int gw, int nwarps, int lane) {
-  for (int k = gw; k < v.nchunks; k += nwarps) {
-    int4 ch = v.chunks[k];   // (first slice, count, mesh, -)
-    if (st.done[ch.z]) continue;
-    double w[RAD_CHUNK / 32];
-#pragma unroll
-    for (int j = 0; j < RAD_CHUNK / 32; ++j) {
-      int idx = lane + 32 * j;
-      w[j] = idx < ch.y ? v.sl_d2[ch.x + idx] : 0.0;
-    }
-    double t = 0.0;
-#pragma unroll
-    for (int j = 0; j < RAD_CHUNK / 32; ++j) t += w[j];
-    t = warp_sum(t);
-    if (lane == 0) v.ch_d2[k] = t;
-  }
-}
-
-// Every block: totals per running mesh (its chunks in order), stop
-// decisions, and the number of meshes still running. Block 0 records the
-// sweep counts and residuals in the mesh table.
-__device__ __forceinline__ int decide_meshes(const StepView& v, MeshState& st, int inc, int first) {
+// Every block: totals per running mesh, stop decisions, and the number of
+// meshes still running. Block 0 records the sweep counts and residuals in
+// the mesh table.
+__device__ __forceinline__ int decide_meshes(const StepView& v, MeshState& st, int inc, int first, int par) {
   __syncthreads();
-  for (int m = threadIdx.x; m < v.nmesh; m += blockDim.x) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const double* d2 = v.tile_d2 + (size_t)par * v.ntiles;
+  for (int m = warp; m < v.nmesh; m += RAD_THREADS / 32) {
     if (st.done[m]) continue;
     const MeshDesc& M = v.md[m];
     double t = 0.0;
-    for (int c0 = 0; c0 < M.nchunks; c0 += 8) {   // loads issued together, summed in order
-      double w[8];
-#pragma unroll
-      for (int j = 0; j < 8; ++j) w[j] = c0 + j < M.nchunks ? v.ch_d2[M.chunk0 + c0 + j] : 0.0;
-#pragma unroll
-      for (int j = 0; j < 8; ++j) t += w[j];
-    }
-    int sw = st.sweeps[m] + (first ? 0 : inc);
-    st.sweeps[m] = sw;
-    bool stop = t <= M.tol2 || sw >= M.max_sweeps;
-    if (stop) st.done[m] = 1;
-    if (blockIdx.x == 0) {
-      v.md[m].sweeps = sw;
-      v.md[m].res2 = t;
+    for (int j = lane; j < M.ntiles; j += 32) t += ld_it(d2 + M.tile0 + j);
+    t = warp_sum(t);
+    if (lane == 0) {
+      int sw = st.sweeps[m] + (first ? 0 : inc);
+      st.sweeps[m] = sw;
+      if (t <= M.tol2 || sw >= M.max_sweeps) st.done[m] = 1;
+      if (blockIdx.x == 0) {
+        v.md[m].sweeps = sw;
+        v.md[m].res2 = t;
+      }
     }
   }
   __syncthreads();
@@ -243,7 +371,7 @@ __device__ __forceinline__ void init_x(const StepView& v, const double* x, int w
   for (int p = gt; p < v.nt; p += nthreads) {
     int g = (int)v.rperm[p];
     const MeshDesc& M = v.md[mesh_of_facet(v, g)];
-    if (!M.active || M.nslices == 0) continue;
+    if (!M.active || M.ntiles == 0) continue;
     double e = v.E[g];
     EP[p] = e;
     P1[p] = e;
@@ -270,46 +398,62 @@ __device__ __forceinline__ void scatter_x(const StepView& v, const MeshState& st
     int g = (int)v.rperm[p];
     int m = mesh_of_facet(v, g);
     const MeshDesc& M = v.md[m];
-    if (!M.active || M.nslices == 0) continue;
-    x[g] = (!mixed && (st.sweeps[m] & 1)) ? P1[p] : P0[p];
+    if (!M.active || M.ntiles == 0) continue;
+    x[g] = (!mixed && (st.sweeps[m] & 1)) ? ld_it(P1 + p) : ld_it(P0 + p);
   }
+}
+
+struct RadSmem {
+  float2* sx;            // halo values (RAD_HALO double-floats, or floats)
+  float2* tail;          // per-thread open-row partials
+  double* rs;            // row sums of the tile (RAD_ROWS, or floats)
+  unsigned char* tnew;   // per thread: its last open row began in its run
+};
+
+__device__ __forceinline__ RadSmem rad_smem() {
+  extern __shared__ __align__(16) unsigned char rad_dyn[];
+  RadSmem m;
+  m.sx = reinterpret_cast<float2*>(rad_dyn);
+  m.tail = m.sx + RAD_HALO;
+  m.rs = reinterpret_cast<double*>(m.tail + RAD_THREADS);
+  m.tnew = reinterpret_cast<unsigned char*>(m.rs + RAD_ROWS);
+  return m;
 }
 
 // FP64 Jacobi to each mesh's tolerance. x: solution (and warm start).
 __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity64(StepView v, double* x, int warm) {
   __shared__ MeshState st;
-  const int lane = threadIdx.x & 31;
-  const int gw = (blockIdx.x * RAD_THREADS + threadIdx.x) >> 5;
-  const int nwarps = (gridDim.x * RAD_THREADS) >> 5;
+  __shared__ double red[32];
+  const RadSmem sm = rad_smem();
   const int gt = blockIdx.x * RAD_THREADS + threadIdx.x;
   const int nthreads = gridDim.x * RAD_THREADS;
   init_meshes(v, st);
   init_x(v, x, warm, gt, nthreads);
   if (!grid_barrier(v.barrier, gridDim.x, v.derr)) return;
+  const uint64_t pol = l2_keep_policy();
   const double* EP = v.rbuf;
   double* cur = v.rbuf + v.nt;
   double* nxt = v.rbuf + 2 * (size_t)v.nt;
-  for (;;) {
-    for (int sl = gw; sl < v.nslices; sl += nwarps) {
-      if (st.done[mesh_of_slice(v, sl)]) continue;
-      double s = slice_dot<double, double, double>(v, v.s_val, cur, sl, lane);
-      int64_t li = (int64_t)sl * 32 + lane;
+  for (int par = 0;; par ^= 1) {
+    for (int t = blockIdx.x; t < v.ntiles; t += gridDim.x) {
+      const RowTile T = v.tiles[t];
+      if (st.done[T.mesh]) continue;
+      stage_halo(v, T, cur, sm.sx);
+      tile_rows<AccDF>(v, T, t, v.t_val, sm.sx, sm.tail, sm.tnew, sm.rs, pol);
+      const uint32_t* rows = v.t_row + T.r0;
       double d2 = 0.0;
-      if (v.ln_m[li] > 0) {
-        int i = v.ln_row[li];
-        double xn = EP[i] + s;
-        double df = xn - cur[i];
+      for (int r = threadIdx.x; r < T.nrows; r += RAD_THREADS) {
+        uint32_t i = __ldg(rows + r);
+        double xn = __ldg(EP + i) + sm.rs[r];
+        double df = xn - ld_it(cur + i);
         nxt[i] = xn;
-        d2 = df * df;
+        d2 += df * df;
       }
-      d2 = warp_sum(d2);
-      if (lane == 0) v.sl_d2[sl] = d2;
+      block_sum_store(d2, red, v.tile_d2 + (size_t)par * v.ntiles + t);
     }
     if (!grid_barrier(v.barrier, gridDim.x, v.derr)) return;
-    chunk_sums(v, st, gw, nwarps, lane);
-    if (!grid_barrier(v.barrier, gridDim.x, v.derr)) return;
-    double* t = cur; cur = nxt; nxt = t;
-    if (decide_meshes(v, st, 1, 0) == 0) break;
+    double* tmp = cur; cur = nxt; nxt = tmp;
+    if (decide_meshes(v, st, 1, 0, par) == 0) break;
   }
   scatter_x(v, st, x, gt, nthreads, false);
 }
@@ -319,9 +463,11 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity64(StepView v, doub
 // x += d. A mesh stops when ||r||_2 <= tol.
 __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity_mixed(StepView v, double* x, int warm) {
   __shared__ MeshState st;
-  const int lane = threadIdx.x & 31;
-  const int gw = (blockIdx.x * RAD_THREADS + threadIdx.x) >> 5;
-  const int nwarps = (gridDim.x * RAD_THREADS) >> 5;
+  __shared__ double red[32];
+  const RadSmem sm = rad_smem();
+  float* sxf = reinterpret_cast<float*>(sm.sx);
+  float* tailf = reinterpret_cast<float*>(sm.tail);
+  float* rsf = reinterpret_cast<float*>(sm.rs);
   const int gt = blockIdx.x * RAD_THREADS + threadIdx.x;
   const int nthreads = gridDim.x * RAD_THREADS;
   float* xa = v.x32;
@@ -330,91 +476,72 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity_mixed(StepView v, 
   init_meshes(v, st);
   init_x(v, x, warm, gt, nthreads);
   if (!grid_barrier(v.barrier, gridDim.x, v.derr)) return;
+  const uint64_t pol = l2_keep_policy();
   const double* EP = v.rbuf;
   double* X = v.rbuf + v.nt;          // the fp64 iterate (radiosity positions)
   int first = 1;
-  for (;;) {
-    for (int sl = gw; sl < v.nslices; sl += nwarps) {
-      if (st.done[mesh_of_slice(v, sl)]) continue;
-      double s = slice_dot<double, double, double>(v, v.s_val, X, sl, lane);
-      int64_t li = (int64_t)sl * 32 + lane;
-      double r2 = 0.0;
-      if (v.ln_m[li] > 0) {
-        int i = v.ln_row[li];
-        double r = EP[i] + s - X[i];
-        r32[i] = (float)r;
-        xa[i] = (float)r;     // inner start: d0 = r
-        r2 = r * r;
+  for (int par = 0;; par ^= 1) {
+    for (int t = blockIdx.x; t < v.ntiles; t += gridDim.x) {
+      const RowTile T = v.tiles[t];
+      if (st.done[T.mesh]) continue;
+      stage_halo(v, T, X, sm.sx);
+      tile_rows<AccDF>(v, T, t, v.t_val, sm.sx, sm.tail, sm.tnew, sm.rs, pol);
+      const uint32_t* rows = v.t_row + T.r0;
+      double d2 = 0.0;
+      for (int r = threadIdx.x; r < T.nrows; r += RAD_THREADS) {
+        uint32_t i = __ldg(rows + r);
+        double res = __ldg(EP + i) + sm.rs[r] - ld_it(X + i);
+        r32[i] = (float)res;
+        xa[i] = (float)res;     // inner start: d0 = r
+        d2 += res * res;
       }
-      r2 = warp_sum(r2);
-      if (lane == 0) v.sl_d2[sl] = r2;
+      block_sum_store(d2, red, v.tile_d2 + (size_t)par * v.ntiles + t);
     }
     if (!grid_barrier(v.barrier, gridDim.x, v.derr)) return;
-    chunk_sums(v, st, gw, nwarps, lane);
-    if (!grid_barrier(v.barrier, gridDim.x, v.derr)) return;
-    int running = decide_meshes(v, st, 4, first);
+    int running = decide_meshes(v, st, 4, first, par);
     first = 0;
     if (running == 0) break;   // scatter below
     float* cur = xa;
     float* nxt = xb;
     for (int it = 0; it < 4; ++it) {
-      for (int sl = gw; sl < v.nslices; sl += nwarps) {
-        if (st.done[mesh_of_slice(v, sl)]) continue;
-        float s = slice_dot<__nv_bfloat16, float, float>(v, v.s_vbf, cur, sl, lane);
-        int64_t li = (int64_t)sl * 32 + lane;
-        if (v.ln_m[li] > 0) {
-          int i = v.ln_row[li];
-          nxt[i] = r32[i] + v.rscale[v.rperm[i]] * s;
+      for (int t = blockIdx.x; t < v.ntiles; t += gridDim.x) {
+        const RowTile T = v.tiles[t];
+        if (st.done[T.mesh]) continue;
+        stage_halo(v, T, cur, sxf);
+        tile_rows<AccF32>(v, T, t, v.t_vbf, sxf, tailf, sm.tnew, rsf, pol);
+        const uint32_t* rows = v.t_row + T.r0;
+        const float* scale = v.t_scale + T.r0;
+        for (int r = threadIdx.x; r < T.nrows; r += RAD_THREADS) {
+          uint32_t i = __ldg(rows + r);
+          nxt[i] = ld_it(r32 + i) + __ldg(scale + r) * rsf[r];
         }
+        __syncthreads();
       }
       if (!grid_barrier(v.barrier, gridDim.x, v.derr)) return;
-      float* t = cur; cur = nxt; nxt = t;
+      float* tmp = cur; cur = nxt; nxt = tmp;
     }
-    for (int sl = gw; sl < v.nslices; sl += nwarps) {
-      if (st.done[mesh_of_slice(v, sl)]) continue;
-      int64_t li = (int64_t)sl * 32 + lane;
-      if (v.ln_m[li] > 0) X[v.ln_row[li]] += (double)cur[v.ln_row[li]];
+    for (int t = blockIdx.x; t < v.ntiles; t += gridDim.x) {
+      const RowTile T = v.tiles[t];
+      if (st.done[T.mesh]) continue;
+      const uint32_t* rows = v.t_row + T.r0;
+      for (int r = threadIdx.x; r < T.nrows; r += RAD_THREADS) {
+        uint32_t i = __ldg(rows + r);
+        X[i] += (double)ld_it(cur + i);
+      }
     }
     if (!grid_barrier(v.barrier, gridDim.x, v.derr)) return;
   }
   scatter_x(v, st, x, gt, nthreads, true);
 }
 
-__global__ void k_active_rows(const int64_t* __restrict__ rowptr, int nt, uint32_t* flag) {
+// Per-row fp32 scale = max |F_ij| of the row (the bf16 copy stores F/scale).
+__global__ void k_row_scale(const int64_t* __restrict__ rowptr, const double* __restrict__ val, int nt,
+                            float* rscale) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < nt) flag[i] = rowptr[i + 1] != rowptr[i] ? 1u : 0u;
-}
-__global__ void k_active_compact(const uint32_t* __restrict__ flag, const unsigned long long* __restrict__ pos,
-                                 int nt, int32_t* active) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < nt && flag[i]) active[pos[i]] = i;
-}
-
-// SELL fill: element e takes CSR entry src[e] (value, and its bf16 copy
-// scaled by its row's scale), or zero for padding (src < 0).
-__global__ void k_sell_fill(const int64_t* __restrict__ src, int64_t nel, const int64_t* __restrict__ sl_ptr,
-                            int nslices, const int32_t* __restrict__ ln_row, const uint32_t* __restrict__ rperm,
-                            const double* __restrict__ val, const float* __restrict__ rscale, double* s_val,
-                            __nv_bfloat16* s_vbf) {
-  int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= nel) return;
-  int64_t k = src[e];
-  if (k < 0) {
-    s_val[e] = 0.0;
-    s_vbf[e] = __float2bfloat16_rn(0.f);
-    return;
-  }
-  // the element's slice and lane give its row (Morton position -> facet)
-  int lo = 0, hi = nslices - 1;
-  while (lo < hi) {
-    int mid = (lo + hi + 1) >> 1;
-    if (sl_ptr[mid] <= e) lo = mid; else hi = mid - 1;
-  }
-  int lane = (int)((e - sl_ptr[lo]) & 31);
-  int row = (int)rperm[ln_row[(int64_t)lo * 32 + lane]];
-  double v = val[k];
-  s_val[e] = v;
-  s_vbf[e] = __float2bfloat16_rn((float)(v / (double)rscale[row]));
+  if (i >= nt) return;
+  double m = 0.0;
+  for (int64_t k = rowptr[i]; k < rowptr[i + 1]; ++k) m = fmax(m, fabs(val[k]));
+  rscale[i] = m > 0.0 ? (float)m : 1.f;
 }
 
 __global__ void k_rank(const uint32_t* __restrict__ order, int nt, uint32_t* rank) {
@@ -435,65 +562,67 @@ __global__ void k_row_keys(const int64_t* __restrict__ rowptr, const int32_t* __
   }
 }
 
-// Per-row fp32 scale = max |F_ij| of the row; values stored as bf16(F/scale).
-__global__ void k_to_bf16(const int64_t* __restrict__ rowptr, const double* __restrict__ val, int nt,
-                          __nv_bfloat16* vbf, float* rscale) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nt) return;
-  int64_t b = rowptr[i], e = rowptr[i + 1];
-  double m = 0.0;
-  for (int64_t k = b; k < e; ++k) m = fmax(m, fabs(val[k]));
-  float sc = m > 0.0 ? (float)m : 1.f;
-  rscale[i] = sc;
-  for (int64_t k = b; k < e; ++k) vbf[k] = __float2bfloat16_rn((float)(val[k] / (double)sc));
+// Stored entry e takes CSR entry src[e] (value as a double-float, and its
+// bf16 copy scaled by its row's scale), or zero for padding (src = ~0).
+__global__ void k_tile_fill(const uint32_t* __restrict__ src, const uint32_t* __restrict__ fac, int64_t n,
+                            const double* __restrict__ val, const float* __restrict__ rscale, float2* t_val,
+                            __nv_bfloat16* t_vbf) {
+  int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  uint32_t k = src[e];
+  double w = k == 0xffffffffu ? 0.0 : val[k];
+  t_val[e] = split_df(w);
+  t_vbf[e] = __float2bfloat16_rn(k == 0xffffffffu ? 0.f : (float)(w / (double)rscale[fac[e]]));
+}
+
+__global__ void k_tile_scale(const uint32_t* __restrict__ t_row, const uint32_t* __restrict__ rperm, int n,
+                             const float* __restrict__ rscale, float* t_scale) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) t_scale[k] = rscale[rperm[t_row[k]]];
+}
+
+int g_rad_nsm = 0, g_rad_per_sm64 = 0, g_rad_per_smm = 0;
+
+// Once per process, before any capture: the kernels' shared-memory opt-in
+// and their co-residency.
+int radiosity_setup() {
+  if (g_rad_nsm) return ILG_OK;
+  int dev, nsm;
+  ILG_CUDA(cudaGetDevice(&dev));
+  ILG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  ILG_CUDA(cudaFuncSetAttribute(k_radiosity64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RAD_SMEM));
+  ILG_CUDA(cudaFuncSetAttribute(k_radiosity_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RAD_SMEM));
+  ILG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_rad_per_sm64, k_radiosity64, RAD_THREADS, RAD_SMEM));
+  ILG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_rad_per_smm, k_radiosity_mixed, RAD_THREADS, RAD_SMEM));
+  if (g_rad_per_sm64 < 1 || g_rad_per_smm < 1) { set_error("radiosity kernel cannot be resident"); return ILG_ERR_CUDA; }
+  g_rad_nsm = nsm;
+  return ILG_OK;
 }
 
 }  // namespace
 
+// Row tiles of the form-factor matrix in Morton order (see the top of the
+// file). Tile sizes target nnz / (co-resident blocks) entries, at least
+// RAD_MIN_TILE, and a tile closes early when its halo would exceed RAD_HALO
+// or its rows RAD_ROWS.
 int radiosity_prepare(Context& c) {
+  ILG_TRY(radiosity_setup());
   cudaStream_t s = c.stream;
-  int nt = c.nt;
-  dbuf<uint32_t> flag;
-  dbuf<unsigned long long> pos;
-  ILG_TRY(flag.alloc(nt));
-  ILG_TRY(pos.alloc(nt));
-  k_active_rows<<<div_up(nt, 256), 256, 0, s>>>(c.rowptr.p, nt, flag.p);
-  ILG_CUDA(cudaGetLastError());
-  ILG_TRY(scan_exclusive_u32_to_u64(flag.p, pos.p, nt, c.scan, s));
-  unsigned long long lp = 0;
-  uint32_t lf = 0;
-  ILG_CUDA(cudaMemcpyAsync(&lp, pos.p + (nt - 1), 8, cudaMemcpyDeviceToHost, s));
-  ILG_CUDA(cudaMemcpyAsync(&lf, flag.p + (nt - 1), 4, cudaMemcpyDeviceToHost, s));
-  ILG_CUDA(cudaStreamSynchronize(s));
-  c.n_active = (int)(lp + lf);
-  ILG_TRY(c.active.alloc(c.n_active > 0 ? c.n_active : 1));
-  k_active_compact<<<div_up(nt, 256), 256, 0, s>>>(flag.p, pos.p, nt, c.active.p);
-  ILG_CUDA(cudaGetLastError());
-  // mixed-precision copy
-  ILG_TRY(c.val_bf16.alloc(c.nnz > 0 ? c.nnz : 1));
+  const int nt = c.nt;
+  const int64_t nnz = c.nnz;
   ILG_TRY(c.row_scale.alloc(nt));
-  k_to_bf16<<<div_up(nt, 256), 256, 0, s>>>(c.rowptr.p, c.val.p, nt, c.val_bf16.p, c.row_scale.p);
+  k_row_scale<<<div_up(nt, 256), 256, 0, s>>>(c.rowptr.p, c.val.p, nt, c.row_scale.p);
   ILG_CUDA(cudaGetLastError());
-  c.have_bf16 = true;
+  ILG_TRY(c.rperm.alloc(nt));
+  ILG_CUDA(cudaMemcpyAsync(c.rperm.p, c.morton_order.p, (size_t)nt * 4, cudaMemcpyDeviceToDevice, s));
 
-  // SELL-32 layout of the active rows, in Morton order. Inside the solve a
-  // facet is addressed by its position in the LBVH's Morton order, so
-  // facets near each other in space are near each other in memory. Rows are
-  // grouped by length class (half octaves, longest first) and by Morton
-  // position within a class; each row's entries are sorted by their
-  // column's Morton position. Neighbouring lanes of a slice are then
-  // neighbouring facets whose visible sets overlap, so the k-th columns of a
-  // slice's 32 lanes fall in few cache lines. Rows longer than L are split
-  // into nearly equal chunks in adjacent lanes of one slice; each slice is
-  // column-major and padded to its longest chunk (rounded up to 4).
-  // Per-row columns in Morton order, sorted on the device: key = (row,
-  // Morton position of the column), value = CSR entry.
+  // Each row's entries in Morton order of their columns, sorted on the
+  // device: key = (row, Morton position of the column), value = CSR entry.
   int rb = 1;
   while ((1 << rb) < nt) ++rb;
-  int64_t nnz = c.nnz;
   std::vector<int64_t> rp((size_t)nt + 1);
   std::vector<unsigned long long> skey((size_t)(nnz > 0 ? nnz : 1));
-  std::vector<uint32_t> ssrc32((size_t)(nnz > 0 ? nnz : 1));
+  std::vector<uint32_t> ssrc((size_t)(nnz > 0 ? nnz : 1));
   std::vector<uint32_t> order((size_t)nt);
   ILG_CUDA(cudaMemcpyAsync(rp.data(), c.rowptr.p, rp.size() * 8, cudaMemcpyDeviceToHost, s));
   ILG_CUDA(cudaMemcpyAsync(order.data(), c.morton_order.p, (size_t)nt * 4, cudaMemcpyDeviceToHost, s));
@@ -509,171 +638,163 @@ int radiosity_prepare(Context& c) {
     ILG_CUDA(cudaGetLastError());
     ILG_TRY(radix_sort_u64(dkey.p, dsv.p, nnz, 2 * rb, c.sort, s));
     ILG_CUDA(cudaMemcpyAsync(skey.data(), dkey.p, (size_t)nnz * 8, cudaMemcpyDeviceToHost, s));
-    ILG_CUDA(cudaMemcpyAsync(ssrc32.data(), dsv.p, (size_t)nnz * 4, cudaMemcpyDeviceToHost, s));
+    ILG_CUDA(cudaMemcpyAsync(ssrc.data(), dsv.p, (size_t)nnz * 4, cudaMemcpyDeviceToHost, s));
     ILG_CUDA(cudaStreamSynchronize(s));
   }
   ILG_CUDA(cudaStreamSynchronize(s));
   const unsigned long long cmask = (1ull << rb) - 1;
-  std::vector<int32_t> rank((size_t)nt);
-  for (int p = 0; p < nt; ++p) rank[order[p]] = p;
-  std::vector<int> rows;
-  int64_t maxlen = 0;
-  for (int i = 0; i < nt; ++i)
-    if (rp[i + 1] > rp[i]) { rows.push_back(i); maxlen = std::max<int64_t>(maxlen, rp[i + 1] - rp[i]); }
-  auto len_class = [&](int i) {
-    double l = (double)(rp[i + 1] - rp[i]);
-    return (int)std::floor(2.0 * std::log2(l));
-  };
-  std::sort(rows.begin(), rows.end(), [&](int p, int q) {
-    int cp = len_class(p), cq = len_class(q);
-    return cp != cq ? cp > cq : rank[p] < rank[q];
-  });
-  // Inside windows of 256 Morton-consecutive rows of one class, longest
-  // first: the slices cut from a window keep their spatial neighbourhood but
-  // pad less.
-  for (size_t a = 0; a < rows.size();) {
+
+  // active rows (with entries) in Morton order
+  std::vector<uint8_t> act((size_t)nt, 0);
+  std::vector<int> arow;   // positions
+  for (int p = 0; p < nt; ++p) {
+    int g = (int)order[p];
+    int64_t len = rp[g + 1] - rp[g];
+    if (len > 0) {
+      if (len > RAD_HALO) {
+        set_error("facet %d sees %lld facets; the radiosity solve supports at most %d per facet", g,
+                  (long long)len, RAD_HALO);
+        return ILG_ERR_ARG;
+      }
+      act[g] = 1;
+      arow.push_back(p);
+    }
+  }
+  c.n_active = (int)arow.size();
+
+  // tile cuts: cumulative entry targets, halo cap
+  const int G = g_rad_nsm * std::min(g_rad_per_sm64, g_rad_per_smm);
+  int64_t ntarget = std::max<int64_t>(1, std::min<int64_t>(G, (nnz + RAD_MIN_TILE - 1) / RAD_MIN_TILE));
+  std::vector<int> stamp((size_t)nt, -1);
+  std::vector<int> loc((size_t)nt, 0);
+  std::vector<RowTile> tiles;
+  std::vector<uint16_t> cf;
+  std::vector<uint32_t> esrc, efac, trow, thalo, tstart;
+  int64_t done_entries = 0;
+  size_t a = 0;
+  while (a < arow.size()) {
+    // rows [a, b) form the next tile
+    const int tid = (int)tiles.size();
+    int64_t bound = (int64_t)((double)nnz * (double)(tid + 1) / (double)ntarget);
+    int nhalo = 0;
     size_t b = a;
-    int ca = len_class(rows[a]);
-    while (b < rows.size() && b - a < 256 && len_class(rows[b]) == ca) ++b;
-    std::stable_sort(rows.begin() + a, rows.begin() + b,
-                     [&](int p, int q) { return rp[p + 1] - rp[p] > rp[q + 1] - rp[q]; });
-    a = b;
-  }
-  int64_t L = 64;                 // chunk length: bounds the per-sweep critical path
-  while ((maxlen + L - 1) / L > 32) L *= 2;
-  std::vector<int64_t> sl_ptr;
-  std::vector<int32_t> sl_len, sl_split, ln_row, ln_m, ln_cnt;
-  std::vector<int64_t> ln_first;   // offset of the lane's chunk in the sorted entries
-  int lane = 32;   // force a new slice first
-  int64_t off = 0;
-  auto close_slice = [&]() {
-    if (sl_len.empty()) return;
-    while (lane < 32) {          // pad lanes
-      ln_row.push_back(-1); ln_m.push_back(-1); ln_cnt.push_back(0); ln_first.push_back(0);
-      ++lane;
+    int64_t ne = 0;
+    std::vector<uint32_t> halo;
+    while (b < arow.size()) {
+      int g = (int)order[arow[b]];
+      int fresh = 0;
+      for (int64_t k = rp[g]; k < rp[g + 1]; ++k)
+        if (stamp[skey[k] & cmask] != tid) ++fresh;
+      if (b > a && (nhalo + fresh > RAD_HALO || (int64_t)(b - a) >= RAD_ROWS)) break;
+      for (int64_t k = rp[g]; k < rp[g + 1]; ++k) {
+        uint32_t cpos = (uint32_t)(skey[k] & cmask);
+        if (stamp[cpos] != tid) { stamp[cpos] = tid; halo.push_back(cpos); }
+      }
+      nhalo += fresh;
+      ne += rp[g + 1] - rp[g];
+      ++b;
+      if (done_entries + ne >= bound && tid + 1 < ntarget) break;
     }
-    int len = (sl_len.back() + 3) & ~3;
-    sl_len.back() = len;
-    off += (int64_t)len * 32;
-  };
-  for (int i : rows) {
-    int64_t len = rp[i + 1] - rp[i];
-    int64_t row0 = rp[i];   // the row's sorted entries: skey/ssrc32[rp[i], rp[i+1])
-    int m = (int)((len + L - 1) / L);
-    int64_t csz = (len + m - 1) / m;   // nearly equal chunks: little padding next to similar rows
-    if (lane + m > 32) {
-      close_slice();
-      sl_ptr.push_back(off);
-      sl_len.push_back(0);
-      sl_split.push_back(1);
-      lane = 0;
-    }
-    for (int k = 0; k < m; ++k) {
-      int64_t first = (int64_t)k * csz;
-      int cnt = (int)std::max<int64_t>(0, std::min<int64_t>(csz, len - first));
-      ln_row.push_back(rank[i]);
-      ln_m.push_back(k == 0 ? m : 0);
-      ln_cnt.push_back(cnt);
-      ln_first.push_back(row0 + first);
-      sl_len.back() = std::max(sl_len.back(), cnt);
-      ++lane;
-    }
-    sl_split.back() = std::max(sl_split.back(), m);
-  }
-  close_slice();
-  c.sell_nslices = (int)sl_len.size();
-  int ns = c.sell_nslices > 0 ? c.sell_nslices : 1;
-  int64_t nel = off > 0 ? off : 1;
-  // element arrays built on the host: column position and CSR source
-  std::vector<int32_t> ecol((size_t)nel, 0);
-  std::vector<int64_t> esrc((size_t)nel, -1);
-  for (int sl = 0; sl < c.sell_nslices; ++sl)
-    for (int l = 0; l < 32; ++l) {
-      size_t li = (size_t)sl * 32 + l;
-      for (int k = 0; k < ln_cnt[li]; ++k) {
-        size_t o = (size_t)sl_ptr[sl] + (size_t)k * 32 + l;
-        ecol[o] = (int32_t)(skey[ln_first[li] + k] & cmask);
-        esrc[o] = (int64_t)ssrc32[ln_first[li] + k];
+    std::sort(halo.begin(), halo.end());
+    for (int h = 0; h < (int)halo.size(); ++h) loc[halo[h]] = h;
+    RowTile T{};
+    T.e0 = (int64_t)cf.size();
+    T.lam = (int)(((ne + RAD_THREADS - 1) / RAD_THREADS + 3) & ~(int64_t)3);
+    T.nrows = (int)(b - a);
+    T.r0 = (int)trow.size();
+    T.h0 = (int)thalo.size();
+    T.nhalo = (int)halo.size();
+    T.mesh = 0;
+    const int64_t stored = (int64_t)T.lam * RAD_THREADS;
+    cf.resize(cf.size() + stored, 0);
+    esrc.resize(esrc.size() + stored, 0xffffffffu);
+    efac.resize(efac.size() + stored, 0);
+    std::vector<int64_t> row_first;
+    int64_t j = 0;
+    for (size_t q = a; q < b; ++q) {
+      int p = arow[q];
+      int g = (int)order[p];
+      row_first.push_back(j);
+      trow.push_back((uint32_t)p);
+      for (int64_t k = rp[g]; k < rp[g + 1]; ++k, ++j) {
+        int64_t t = j / T.lam, kk = j % T.lam;
+        int64_t off = T.e0 + (kk >> 2) * 4 * RAD_THREADS + 4 * t + (kk & 3);
+        cf[off] = (uint16_t)(loc[skey[k] & cmask] | (k + 1 == rp[g + 1] ? 0x8000 : 0));
+        esrc[off] = ssrc[k];
+        efac[off] = (uint32_t)g;
       }
     }
-  ILG_TRY(c.sell_ptr.alloc(ns));
-  ILG_TRY(c.sell_len.alloc(ns));
-  ILG_TRY(c.sell_split.alloc(ns));
-  ILG_TRY(c.sell_row.alloc((size_t)ns * 32));
-  ILG_TRY(c.sell_m.alloc((size_t)ns * 32));
-  ILG_TRY(c.sell_col.alloc(nel));
-  ILG_TRY(c.sell_val.alloc(nel));
-  ILG_TRY(c.sell_vbf.alloc(nel));
-  ILG_TRY(c.rperm.alloc(nt));
-  ILG_CUDA(cudaMemcpyAsync(c.rperm.p, order.data(), (size_t)nt * 4, cudaMemcpyHostToDevice, s));
-  if (c.sell_nslices > 0) {
-    dbuf<int64_t> dsrc;
-    ILG_TRY(dsrc.alloc(nel));
-    ILG_CUDA(cudaMemcpyAsync(c.sell_ptr.p, sl_ptr.data(), sl_ptr.size() * 8, cudaMemcpyHostToDevice, s));
-    ILG_CUDA(cudaMemcpyAsync(c.sell_len.p, sl_len.data(), sl_len.size() * 4, cudaMemcpyHostToDevice, s));
-    ILG_CUDA(cudaMemcpyAsync(c.sell_split.p, sl_split.data(), sl_split.size() * 4, cudaMemcpyHostToDevice, s));
-    ILG_CUDA(cudaMemcpyAsync(c.sell_row.p, ln_row.data(), ln_row.size() * 4, cudaMemcpyHostToDevice, s));
-    ILG_CUDA(cudaMemcpyAsync(c.sell_m.p, ln_m.data(), ln_m.size() * 4, cudaMemcpyHostToDevice, s));
-    ILG_CUDA(cudaMemcpyAsync(c.sell_col.p, ecol.data(), (size_t)nel * 4, cudaMemcpyHostToDevice, s));
-    ILG_CUDA(cudaMemcpyAsync(dsrc.p, esrc.data(), (size_t)nel * 8, cudaMemcpyHostToDevice, s));
-    k_sell_fill<<<div_up(nel, 256), 256, 0, s>>>(dsrc.p, nel, c.sell_ptr.p, c.sell_nslices, c.sell_row.p,
-                                                c.rperm.p, c.val.p, c.row_scale.p, c.sell_val.p, c.sell_vbf.p);
+    for (int t = 0; t < RAD_THREADS; ++t) {
+      int64_t j0 = (int64_t)t * T.lam;
+      if (j0 >= ne) { tstart.push_back((uint32_t)T.nrows); continue; }
+      int r = (int)(std::upper_bound(row_first.begin(), row_first.end(), j0) - row_first.begin()) - 1;
+      tstart.push_back((uint32_t)r | (row_first[r] != j0 ? 0x80000000u : 0u));
+    }
+    thalo.insert(thalo.end(), halo.begin(), halo.end());
+    tiles.push_back(T);
+    done_entries += ne;
+    a = b;
+  }
+  c.ntiles = (int)tiles.size();
+  c.tile_elems = (int64_t)cf.size();
+  c.tiles_h = tiles;
+  const int64_t ns = c.tile_elems > 0 ? c.tile_elems : 1;
+  const int ntl = c.ntiles > 0 ? c.ntiles : 1;
+  ILG_TRY(c.tiles.alloc(ntl));
+  ILG_TRY(c.t_cf.alloc(ns));
+  ILG_TRY(c.t_val.alloc(ns));
+  ILG_TRY(c.t_vbf.alloc(ns));
+  ILG_TRY(c.t_row.alloc(trow.empty() ? 1 : trow.size()));
+  ILG_TRY(c.t_scale.alloc(trow.empty() ? 1 : trow.size()));
+  ILG_TRY(c.t_halo.alloc(thalo.empty() ? 1 : thalo.size()));
+  ILG_TRY(c.t_start.alloc((size_t)ntl * RAD_THREADS));
+  ILG_TRY(c.tile_d2.alloc(2 * (size_t)ntl));
+  if (c.ntiles > 0) {
+    dbuf<uint32_t> dsrc, dfac;
+    ILG_TRY(dsrc.alloc(ns));
+    ILG_TRY(dfac.alloc(ns));
+    ILG_CUDA(cudaMemcpyAsync(c.tiles.p, tiles.data(), tiles.size() * sizeof(RowTile), cudaMemcpyHostToDevice, s));
+    ILG_CUDA(cudaMemcpyAsync(c.t_cf.p, cf.data(), cf.size() * 2, cudaMemcpyHostToDevice, s));
+    ILG_CUDA(cudaMemcpyAsync(c.t_row.p, trow.data(), trow.size() * 4, cudaMemcpyHostToDevice, s));
+    ILG_CUDA(cudaMemcpyAsync(c.t_halo.p, thalo.data(), thalo.size() * 4, cudaMemcpyHostToDevice, s));
+    ILG_CUDA(cudaMemcpyAsync(c.t_start.p, tstart.data(), tstart.size() * 4, cudaMemcpyHostToDevice, s));
+    ILG_CUDA(cudaMemcpyAsync(dsrc.p, esrc.data(), esrc.size() * 4, cudaMemcpyHostToDevice, s));
+    ILG_CUDA(cudaMemcpyAsync(dfac.p, efac.data(), efac.size() * 4, cudaMemcpyHostToDevice, s));
+    k_tile_fill<<<div_up(ns, 256), 256, 0, s>>>(dsrc.p, dfac.p, ns, c.val.p, c.row_scale.p, c.t_val.p, c.t_vbf.p);
+    ILG_CUDA(cudaGetLastError());
+    k_tile_scale<<<div_up((int64_t)trow.size(), 256), 256, 0, s>>>(c.t_row.p, c.rperm.p, (int)trow.size(),
+                                                                  c.row_scale.p, c.t_scale.p);
     ILG_CUDA(cudaGetLastError());
     ILG_CUDA(cudaStreamSynchronize(s));
   }
-  c.sell_elems = off;
-  // residual-reduction chunks of the slices
-  {
-    int ns = c.sell_nslices;
-    int nch = (ns + RAD_CHUNK - 1) / RAD_CHUNK;
-    std::vector<int4> ch(nch > 0 ? nch : 1);
-    for (int k = 0; k < nch; ++k) ch[k] = make_int4(k * RAD_CHUNK, std::min(RAD_CHUNK, ns - k * RAD_CHUNK), 0, 0);
-    ILG_TRY(c.chunks.alloc(ch.size()));
-    ILG_TRY(c.ch_d2.alloc(ch.size()));
-    ILG_CUDA(cudaMemcpyAsync(c.chunks.p, ch.data(), ch.size() * sizeof(int4), cudaMemcpyHostToDevice, s));
-    c.nchunks = nch;
-  }
-  // per-facet flag: the row has entries
-  std::vector<uint8_t> act((size_t)nt, 0);
-  for (int i : rows) act[i] = 1;
   ILG_TRY(c.row_act.alloc(nt));
   ILG_CUDA(cudaMemcpyAsync(c.row_act.p, act.data(), (size_t)nt, cudaMemcpyHostToDevice, s));
   ILG_CUDA(cudaStreamSynchronize(s));
   return ILG_OK;
 }
 
-// Cooperative grid size for nslices slices (at most the co-resident blocks).
-int radiosity_chunk() { return RAD_CHUNK; }
 int radiosity_max_meshes() { return RAD_MAX_MESH; }
+int radiosity_threads() { return RAD_THREADS; }
 
-int radiosity_grid(int nslices, int precision) {
-  static int nsm = 0, per_sm64 = 0, per_smm = 0;
-  if (!nsm) {
-    int dev;
-    if (cudaGetDevice(&dev) != cudaSuccess ||
-        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm64, k_radiosity64, RAD_THREADS, 0) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_smm, k_radiosity_mixed, RAD_THREADS, 0) != cudaSuccess) {
-      nsm = 0;
-      return 1;
-    }
-  }
-  int per_sm = precision == ILG_PREC_MIXED ? per_smm : per_sm64;
-  int want = div_up((int64_t)(nslices > 0 ? nslices : 1) * 32, RAD_THREADS);
-  int grid = per_sm * nsm;
-  if (want < grid) grid = want;
+// Cooperative grid size for ntiles tiles (at most the co-resident blocks).
+int radiosity_grid(int ntiles, int precision) {
+  if (radiosity_setup() != ILG_OK) return 1;
+  int per_sm = precision == ILG_PREC_MIXED ? g_rad_per_smm : g_rad_per_sm64;
+  int grid = per_sm * g_rad_nsm;
+  if (ntiles < grid) grid = ntiles;
   return grid < 1 ? 1 : grid;
 }
 
 // Launches the cooperative solve for every active mesh of the view with
-// slices. x: result (also the warm start when warm). Per-mesh sweep counts
+// tiles. x: result (also the warm start when warm). Per-mesh sweep counts
 // and residuals land in the mesh table.
 int radiosity_launch(const StepView& v, double* x, int warm, int precision, int grid, cudaStream_t s) {
+  ILG_TRY(radiosity_setup());
   ILG_CUDA(cudaMemsetAsync(v.barrier, 0, 2 * sizeof(unsigned), s));
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(grid);
   cfg.blockDim = dim3(RAD_THREADS);
-  cfg.dynamicSmemBytes = 0;
+  cfg.dynamicSmemBytes = RAD_SMEM;
   cfg.stream = s;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeCooperative;   // all blocks co-resident: the grid barrier is safe

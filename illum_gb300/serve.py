@@ -86,7 +86,7 @@ def footprint_bytes(level: int, nz: int, nphi: int, precision: int) -> int:
     """Device bytes a job holds while it runs (its context plus its copy in a
     batch): geometry + LBVH + horizons ~ (400 + 8 nphi) B per facet, layer
     state nz * (4|8) B twice, ~12 facet arrays of 8 B twice, and form factors
-    estimated at 150 entries per facet * 30 B (CSR, SELL and bf16 copies)."""
+    estimated at 150 entries per facet * 30 B (CSR, row-tile and bf16 copies)."""
     n = 20 * 4 ** level
     s_t = 4 if precision == ig.PREC_MIXED else 8
     return int(n * (400 + 8 * nphi + 2 * nz * s_t + 2 * 12 * 8 + 150 * 30))

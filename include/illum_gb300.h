@@ -94,9 +94,10 @@ int ilg_compute_F(ilg_ctx* ctx, const double* albedo, double albedo_scalar, doub
 int ilg_get_F(ilg_ctx* ctx, int64_t* rowptr, int32_t* col, double* val);
 int ilg_set_F(ilg_ctx* ctx, int64_t nnz, const int64_t* rowptr, const int32_t* col,
               const double* val);
-/* Sizes of the device copy: entries, padded SELL-32 entries used by the
- * radiosity sweeps, SELL slices, rows with entries (any may be NULL). */
-int ilg_F_info(const ilg_ctx* ctx, int64_t* nnz, int64_t* sell_elems, int* sell_slices,
+/* Sizes of the device copy: entries, entries stored for the radiosity
+ * sweeps (row tiles padded to whole thread runs), row tiles, rows with
+ * entries (any may be NULL). */
+int ilg_F_info(const ilg_ctx* ctx, int64_t* nnz, int64_t* stored_entries, int* row_tiles,
                int* active_rows);
 
 /* ---- horizons ----------------------------------------------------------- */
