@@ -56,7 +56,7 @@ constexpr int RAD_ROWS = 6144;           // rows per tile (their sums: 48 KB of 
 constexpr int RAD_MAX_MESH = 1024;
 constexpr int64_t RAD_MIN_TILE = 16384;  // entries: smaller tiles cost more in staging than they balance
 constexpr size_t RAD_SMEM =
-    (size_t)RAD_HALO * sizeof(float2) + RAD_THREADS * sizeof(float2) + RAD_ROWS * sizeof(double) + RAD_THREADS;
+    (size_t)RAD_HALO * sizeof(float2) + RAD_THREADS * sizeof(float2) + RAD_ROWS * sizeof(float2) + RAD_THREADS;
 
 // Grid barrier for a cooperative launch (all blocks co-resident). The wait
 // is bounded: after ~2^26 polls it records DERR_BARRIER and returns false.
@@ -141,7 +141,7 @@ struct AccDF {
   typedef float2 W;
   typedef float2 X;
   typedef float2 Part;
-  typedef double Sum;
+  typedef float2 Sum;
   float h, l;
   __device__ __forceinline__ void zero() { h = 0.f; l = 0.f; }
   __device__ __forceinline__ void two_sum(float p) {
@@ -164,8 +164,10 @@ struct AccDF {
     two_sum(q.x);
     l = __fadd_rn(l, q.y);
   }
-  __device__ __forceinline__ double get() const { return (double)h + (double)l; }
+  __device__ __forceinline__ float2 get() const { return make_float2(h, l); }
 };
+
+__device__ __forceinline__ double df_value(float2 s) { return (double)s.x + (double)s.y; }
 
 // Plain fp32 sum (mixed inner sweeps: bf16 values, fp32 iterates).
 struct AccF32 {
@@ -181,13 +183,14 @@ struct AccF32 {
   __device__ __forceinline__ float get() const { return s; }
 };
 
-__device__ __forceinline__ float2 to_halo(double x, float2*) { return split_df(x); }
+__device__ __forceinline__ float2 to_halo(float2 x, float2*) { return x; }
 __device__ __forceinline__ float to_halo(float x, float*) { return x; }
 
 // Iterates written by other blocks during the solve are read at L2 (never
 // from a possibly stale L1 line).
 __device__ __forceinline__ double ld_it(const double* p) { return __ldcg(p); }
 __device__ __forceinline__ float ld_it(const float* p) { return __ldcg(p); }
+__device__ __forceinline__ float2 ld_it(const float2* p) { return __ldcg(p); }
 
 // Gather the tile's halo values x[halo[h]] into shared memory.
 template <class XS, class XG>
@@ -360,7 +363,8 @@ __device__ __forceinline__ int decide_meshes(const StepView& v, MeshState& st, i
 }
 
 // The solve works on radiosity positions (Morton order within each mesh):
-// EP = E, P0 / P1 = iterates, gathered through rperm at entry. Start values:
+// EP = E, P0 / P1 = iterates, gathered through rperm at entry, and H0 / H1
+// the iterates' double-float copies (what the halos gather). Start values:
 // rows without entries are x = E exactly; the others start at E (cold) or
 // at the mesh's previous solution, extrapolated linearly once two solutions
 // exist (warm).
@@ -368,20 +372,24 @@ __device__ __forceinline__ void init_x(const StepView& v, const double* x, int w
   double* EP = v.rbuf;
   double* P0 = v.rbuf + v.nt;
   double* P1 = v.rbuf + 2 * (size_t)v.nt;
+  float2* H0 = reinterpret_cast<float2*>(v.rbuf + 3 * (size_t)v.nt);
+  float2* H1 = H0 + v.nt;
   for (int p = gt; p < v.nt; p += nthreads) {
     int g = (int)v.rperm[p];
     const MeshDesc& M = v.md[mesh_of_facet(v, g)];
     if (!M.active || M.ntiles == 0) continue;
     double e = v.E[g];
-    EP[p] = e;
-    P1[p] = e;
-    if (!warm || !v.row_act[g]) {
-      P0[p] = e;
-    } else {
+    double x0 = e;
+    if (warm && v.row_act[g]) {
       double xn = x[g];
-      P0[p] = M.frame >= 2 ? 2.0 * xn - v.xprev[g] : xn;
+      x0 = M.frame >= 2 ? 2.0 * xn - v.xprev[g] : xn;
       v.xprev[g] = xn;
     }
+    EP[p] = e;
+    P0[p] = x0;
+    P1[p] = e;
+    H0[p] = split_df(x0);
+    H1[p] = split_df(e);
     if (v.x32) {
       v.x32[p] = 0.f;
       v.x32[v.nt + p] = 0.f;
@@ -406,7 +414,7 @@ __device__ __forceinline__ void scatter_x(const StepView& v, const MeshState& st
 struct RadSmem {
   float2* sx;            // halo values (RAD_HALO double-floats, or floats)
   float2* tail;          // per-thread open-row partials
-  double* rs;            // row sums of the tile (RAD_ROWS, or floats)
+  float2* rs;            // row sums of the tile (RAD_ROWS double-floats, or floats)
   unsigned char* tnew;   // per thread: its last open row began in its run
 };
 
@@ -415,7 +423,7 @@ __device__ __forceinline__ RadSmem rad_smem() {
   RadSmem m;
   m.sx = reinterpret_cast<float2*>(rad_dyn);
   m.tail = m.sx + RAD_HALO;
-  m.rs = reinterpret_cast<double*>(m.tail + RAD_THREADS);
+  m.rs = m.tail + RAD_THREADS;
   m.tnew = reinterpret_cast<unsigned char*>(m.rs + RAD_ROWS);
   return m;
 }
@@ -434,25 +442,29 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity64(StepView v, doub
   const double* EP = v.rbuf;
   double* cur = v.rbuf + v.nt;
   double* nxt = v.rbuf + 2 * (size_t)v.nt;
+  float2* curh = reinterpret_cast<float2*>(v.rbuf + 3 * (size_t)v.nt);
+  float2* nxth = curh + v.nt;
   for (int par = 0;; par ^= 1) {
     for (int t = blockIdx.x; t < v.ntiles; t += gridDim.x) {
       const RowTile T = v.tiles[t];
       if (st.done[T.mesh]) continue;
-      stage_halo(v, T, cur, sm.sx);
+      stage_halo(v, T, curh, sm.sx);
       tile_rows<AccDF>(v, T, t, v.t_val, sm.sx, sm.tail, sm.tnew, sm.rs, pol);
       const uint32_t* rows = v.t_row + T.r0;
       double d2 = 0.0;
       for (int r = threadIdx.x; r < T.nrows; r += RAD_THREADS) {
         uint32_t i = __ldg(rows + r);
-        double xn = __ldg(EP + i) + sm.rs[r];
+        double xn = __ldg(EP + i) + df_value(sm.rs[r]);
         double df = xn - ld_it(cur + i);
         nxt[i] = xn;
+        nxth[i] = split_df(xn);
         d2 += df * df;
       }
       block_sum_store(d2, red, v.tile_d2 + (size_t)par * v.ntiles + t);
     }
     if (!grid_barrier(v.barrier, gridDim.x, v.derr)) return;
     double* tmp = cur; cur = nxt; nxt = tmp;
+    float2* tmph = curh; curh = nxth; nxth = tmph;
     if (decide_meshes(v, st, 1, 0, par) == 0) break;
   }
   scatter_x(v, st, x, gt, nthreads, false);
@@ -479,18 +491,19 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity_mixed(StepView v, 
   const uint64_t pol = l2_keep_policy();
   const double* EP = v.rbuf;
   double* X = v.rbuf + v.nt;          // the fp64 iterate (radiosity positions)
+  float2* XH = reinterpret_cast<float2*>(v.rbuf + 3 * (size_t)v.nt);   // its double-float copy
   int first = 1;
   for (int par = 0;; par ^= 1) {
     for (int t = blockIdx.x; t < v.ntiles; t += gridDim.x) {
       const RowTile T = v.tiles[t];
       if (st.done[T.mesh]) continue;
-      stage_halo(v, T, X, sm.sx);
+      stage_halo(v, T, XH, sm.sx);
       tile_rows<AccDF>(v, T, t, v.t_val, sm.sx, sm.tail, sm.tnew, sm.rs, pol);
       const uint32_t* rows = v.t_row + T.r0;
       double d2 = 0.0;
       for (int r = threadIdx.x; r < T.nrows; r += RAD_THREADS) {
         uint32_t i = __ldg(rows + r);
-        double res = __ldg(EP + i) + sm.rs[r] - ld_it(X + i);
+        double res = __ldg(EP + i) + df_value(sm.rs[r]) - ld_it(X + i);
         r32[i] = (float)res;
         xa[i] = (float)res;     // inner start: d0 = r
         d2 += res * res;
@@ -526,7 +539,9 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity_mixed(StepView v, 
       const uint32_t* rows = v.t_row + T.r0;
       for (int r = threadIdx.x; r < T.nrows; r += RAD_THREADS) {
         uint32_t i = __ldg(rows + r);
-        X[i] += (double)ld_it(cur + i);
+        double xi = X[i] + (double)ld_it(cur + i);
+        X[i] = xi;
+        XH[i] = split_df(xi);
       }
     }
     if (!grid_barrier(v.barrier, gridDim.x, v.derr)) return;
