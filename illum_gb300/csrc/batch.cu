@@ -58,7 +58,7 @@ struct Batch {
   dbuf<SunAux> suns;
   dbuf<double> Tsurf, Fsurf, Qprev, rad, rad_avg, therm_avg, therm_max, E, xtmp, xprev;
   dbuf<float> x32;
-  dbuf<double> T64, coef64;
+  dbuf<float2> Tdf, coefdf;
   dbuf<float> T32, coef32;
   dbuf<RowTile> tiles;
   dbuf<uint16_t> t_cf;
@@ -125,7 +125,7 @@ static int build(Batch& b) {
       nrow += c.n_active;
       for (const RowTile& T : c.tiles_h) nhal += T.nhalo;
     }
-    ncb += div_up(c.nt, 128);
+    ncb += div_up(c.nt, conduction_step_threads());
     b.nz_max = std::max(b.nz_max, c.nz);
   }
   b.nt = (int)nt;
@@ -150,8 +150,8 @@ static int build(Batch& b) {
     ILG_TRY(b.T32.alloc(nT));
     ILG_TRY(b.coef32.alloc(ncoef));
   } else {
-    ILG_TRY(b.T64.alloc(nT));
-    ILG_TRY(b.coef64.alloc(ncoef));
+    ILG_TRY(b.Tdf.alloc(nT));
+    ILG_TRY(b.coefdf.alloc(ncoef));
   }
   const int RT = radiosity_threads();
   int64_t ntl1 = ntl > 0 ? ntl : 1, nel1 = nel > 0 ? nel : 1;
@@ -214,8 +214,8 @@ static int build(Batch& b) {
       ILG_TRY(cat(b.T32, (size_t)M.T0, c.T32.p, N * c.nz, s));
       ILG_TRY(cat(b.coef32, (size_t)M.coef0, c.coef32.p, (size_t)c.nz * 5, s));
     } else {
-      ILG_TRY(cat(b.T64, (size_t)M.T0, c.T64.p, N * c.nz, s));
-      ILG_TRY(cat(b.coef64, (size_t)M.coef0, c.coef64.p, (size_t)c.nz * 5, s));
+      ILG_TRY(cat(b.Tdf, (size_t)M.T0, c.Tdf.p, N * c.nz, s));
+      ILG_TRY(cat(b.coefdf, (size_t)M.coef0, c.coefdf.p, (size_t)c.nz * 5, s));
     }
     if (c.have_F) {
       ILG_TRY(cat(b.row_act, f0, c.row_act.p, N, s));
@@ -244,7 +244,8 @@ static int build(Batch& b) {
     }
     k_fill_int<<<div_up(N, 256), 256, 0, s>>>(b.mesh_of.p + f0, N, i);
     ILG_CUDA(cudaGetLastError());
-    for (int k = 0; k < div_up(c.nt, 128); ++k) cbh.push_back(make_int2(i, k * 128));
+    const int cbs = conduction_step_threads();
+    for (int k = 0; k < div_up(c.nt, cbs); ++k) cbh.push_back(make_int2(i, k * cbs));
   }
   ILG_TRY(cat(b.disk, 0, b.members[0]->c.disk.p, 2 * (size_t)ndisk, s));
   ILG_CUDA(cudaMemcpyAsync(b.cblocks.p, cbh.data(), cbh.size() * sizeof(int2), cudaMemcpyHostToDevice, s));
@@ -258,7 +259,7 @@ static int build(Batch& b) {
   v.hmin = b.hmin.p; v.hmax = b.hmax.p; v.disk = b.disk.p; v.ndisk = ndisk; v.suns = b.suns.p;
   v.Tsurf = b.Tsurf.p; v.Fsurf = b.Fsurf.p; v.Qprev = b.Qprev.p; v.rad = b.rad.p; v.rad_avg = b.rad_avg.p;
   v.therm_avg = b.therm_avg.p; v.therm_max = b.therm_max.p; v.E = b.E.p; v.xprev = b.xprev.p;
-  v.x32 = b.x32.p; v.T64 = b.T64.p; v.T32 = b.T32.p; v.coef64 = b.coef64.p; v.coef32 = b.coef32.p;
+  v.x32 = b.x32.p; v.Tdf = b.Tdf.p; v.T32 = b.T32.p; v.coefdf = b.coefdf.p; v.coef32 = b.coef32.p;
   v.tiles = b.tiles.p; v.ntiles = b.ntiles;
   v.t_cf = b.t_cf.p; v.t_val = b.t_val.p; v.t_vbf = b.t_vbf.p;
   v.t_row = b.t_row.p; v.t_halo = b.t_halo.p; v.t_start = b.t_start.p; v.t_scale = b.t_scale.p;
@@ -445,7 +446,7 @@ int ilg_batch_sync(ilg_batch* batch) {
     if (mixed)
       ILG_CUDA(cudaMemcpyAsync(c.T32.p, b.T32.p + M.T0, N * c.nz * 4, cudaMemcpyDeviceToDevice, s));
     else
-      ILG_CUDA(cudaMemcpyAsync(c.T64.p, b.T64.p + M.T0, N * c.nz * 8, cudaMemcpyDeviceToDevice, s));
+      ILG_CUDA(cudaMemcpyAsync(c.Tdf.p, b.Tdf.p + M.T0, N * c.nz * 8, cudaMemcpyDeviceToDevice, s));
     c.frame_no = m[i].frame;
   }
   ILG_CUDA(cudaStreamSynchronize(b.stream));

@@ -143,8 +143,8 @@ static StepView solo_view(Context& c, int precision) {
   v.Tsurf = c.Tsurf.p; v.Fsurf = c.Fsurf.p; v.Qprev = c.Qprev.p; v.rad = c.rad.p; v.rad_avg = c.rad_avg.p;
   v.therm_avg = c.therm_avg.p; v.therm_max = c.therm_max.p; v.E = c.E.p; v.xprev = c.xprev.p;
   v.x32 = c.x32.p;
-  v.T64 = c.T64.p; v.T32 = c.T32.p;
-  v.coef64 = c.coef64.p; v.coef32 = c.coef32.p;
+  v.T64 = nullptr; v.Tdf = c.Tdf.p; v.T32 = c.T32.p;
+  v.coef64 = nullptr; v.coefdf = c.coefdf.p; v.coef32 = c.coef32.p;
   v.tiles = c.tiles.p; v.ntiles = c.have_F ? c.ntiles : 0;
   v.t_cf = c.t_cf.p; v.t_val = c.t_val.p; v.t_vbf = c.t_vbf.p;
   v.t_row = c.t_row.p; v.t_halo = c.t_halo.p; v.t_start = c.t_start.p; v.t_scale = c.t_scale.p;
@@ -559,12 +559,14 @@ int ilg_thermal_init(ilg_ctx* ctx, int nz, const double* z, const double* ti, co
   c.coef_dt = -1.0;
   c.coef_prec = -1;
   size_t n = (size_t)nz * nt;
-  std::vector<double> Tl(n), ts(nt);
+  std::vector<float2> Tl(n);
+  std::vector<double> ts(nt);
   for (int f = 0; f < nt; ++f) {
     ts[f] = T0_full ? T0_full[(size_t)f * (nz + 1)] : T0;
-    for (int i = 0; i < nz; ++i) Tl[(size_t)i * nt + f] = T0_full ? T0_full[(size_t)f * (nz + 1) + 1 + i] : T0;
+    for (int i = 0; i < nz; ++i)
+      Tl[(size_t)i * nt + f] = split_df_host(T0_full ? T0_full[(size_t)f * (nz + 1) + 1 + i] : T0);
   }
-  ILG_TRY(c.T64.alloc(n));
+  ILG_TRY(c.Tdf.alloc(n));
   ILG_TRY(c.Tsurf.alloc(nt));
   ILG_TRY(c.Fsurf.alloc(nt));
   ILG_TRY(c.Qprev.alloc(nt));
@@ -574,7 +576,7 @@ int ilg_thermal_init(ilg_ctx* ctx, int nz, const double* z, const double* ti, co
   ILG_TRY(c.therm_max.alloc(nt));
   ILG_TRY(c.E.reserve(nt));
   ILG_TRY(c.Q.reserve(nt));
-  ILG_CUDA(cudaMemcpyAsync(c.T64.p, Tl.data(), n * 8, cudaMemcpyHostToDevice, c.stream));
+  ILG_CUDA(cudaMemcpyAsync(c.Tdf.p, Tl.data(), n * 8, cudaMemcpyHostToDevice, c.stream));
   ILG_CUDA(cudaMemcpyAsync(c.Tsurf.p, ts.data(), (size_t)nt * 8, cudaMemcpyHostToDevice, c.stream));
   for (double* p : {c.Fsurf.p, c.Qprev.p, c.rad.p, c.rad_avg.p, c.therm_avg.p, c.therm_max.p})
     ILG_CUDA(cudaMemsetAsync(p, 0, (size_t)nt * 8, c.stream));
@@ -616,7 +618,10 @@ int ilg_thermal_get(ilg_ctx* ctx, double* T, double* Fsurf, double* Qprev) {
       ILG_CUDA(cudaStreamSynchronize(c.stream));
       for (size_t i = 0; i < n; ++i) Tl[i] = t32[i];
     } else {
-      ILG_CUDA(cudaMemcpyAsync(Tl.data(), c.T64.p, n * 8, cudaMemcpyDeviceToHost, c.stream));
+      std::vector<float2> tdf(n);
+      ILG_CUDA(cudaMemcpyAsync(tdf.data(), c.Tdf.p, n * 8, cudaMemcpyDeviceToHost, c.stream));
+      ILG_CUDA(cudaStreamSynchronize(c.stream));
+      for (size_t i = 0; i < n; ++i) Tl[i] = (double)tdf[i].x + (double)tdf[i].y;
     }
     ILG_CUDA(cudaMemcpyAsync(ts.data(), c.Tsurf.p, (size_t)nt * 8, cudaMemcpyDeviceToHost, c.stream));
     ILG_CUDA(cudaStreamSynchronize(c.stream));

@@ -75,6 +75,12 @@ struct dbuf {
 
 inline int div_up(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
 
+// Double-float split on the host: x = hi + lo, hi = fl32(x), lo = fl32(x - hi).
+inline float2 split_df_host(double x) {
+  float h = (float)x;
+  return make_float2(h, (float)(x - (double)h));
+}
+
 // Device error flags written by kernels (bounded waits that gave up, stack
 // overflows, NaN form factors). One int per kind.
 enum DevErr : int {

@@ -17,9 +17,23 @@
 //   downward pass: T_i = (rho_i + gamma_i T_{i-1}) / beta_i
 // rho is staged in shared memory ([layer][thread], conflict-free). The
 // temperature state is layer-major [nz][N], so every layer access of a warp
-// is one coalesced 256-byte (fp64) or 128-byte (fp32) transaction.
+// is one coalesced 256-byte (8-byte values) or 128-byte (fp32) transaction.
+//
+// Arithmetic: GB300 executes FP64 at about one fused multiply-add per clock
+// per SM, so the FP64 step of a scene keeps its layers as double-float
+// pairs (hi + lo floats, 48 significant bits) and runs the layer recurrences
+// in double-float arithmetic on the FP32 pipes (error-free products by FMA,
+// TwoSum additions; Dekker 1971). It solves for the increment
+// dT = T(n+1) - T(n), whose right-hand side 2 gamma (T(i-1) - T(i)) +
+// 2 alpha (T(i+1) - T(i)) carries no large cancellation when the diffusion
+// numbers are large, so rounding stays relative to the increment and the
+// stored state is within ~1e-12 K of FP64 per step. The surface boundary
+// (linearised or Newton) is solved in FP64. The mixed step uses the same
+// increment form in plain FP32; the standalone column entry points
+// (conductionq_, ilg_conductionq_batch) run the reference's rows in FP64.
 #include <cmath>
 #include <mutex>
+#include <type_traits>
 #include <vector>
 
 #include "geom.h"
@@ -29,32 +43,86 @@ namespace ilg {
 
 namespace {
 
-constexpr int COND_THREADS = 128;
+constexpr int COND_THREADS = 128;       // standalone column entry points
+constexpr int COND_STEP_THREADS = 64;   // scene steps: 7 blocks of 60-layer columns per SM
 constexpr int TAB_W = 5;            // g, m, al, f, inv_beta per layer
 constexpr size_t SMEM_LIMIT = 160 * 1024;
+
+// Double-float number: value = h + l with |l| <= ulp(h) / 2. The
+// intrinsics keep the compiler from contracting or reassociating the
+// error-free steps.
+struct dfloat {
+  float h, l;
+  __host__ __device__ __forceinline__ dfloat() {}
+  __device__ __forceinline__ dfloat(float a, float b) : h(a), l(b) {}
+  __device__ __forceinline__ explicit dfloat(double x) {
+    h = __double2float_rn(x);
+    l = __double2float_rn(x - (double)h);
+  }
+  __device__ __forceinline__ explicit dfloat(int x) : h((float)x), l(0.f) {}
+  __device__ __forceinline__ explicit operator double() const { return (double)h + (double)l; }
+};
+// s + e renormalised, |s| >= |e| (Fast2Sum)
+__device__ __forceinline__ dfloat df_norm(float s, float e) {
+  float t = __fadd_rn(s, e);
+  return dfloat(t, __fsub_rn(e, __fsub_rn(t, s)));
+}
+__device__ __forceinline__ dfloat operator+(dfloat a, dfloat b) {
+  float s = __fadd_rn(a.h, b.h);
+  float bb = __fsub_rn(s, a.h);
+  float e = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, bb)), __fsub_rn(b.h, bb));   // TwoSum error
+  return df_norm(s, __fadd_rn(e, __fadd_rn(a.l, b.l)));
+}
+__device__ __forceinline__ dfloat operator-(dfloat a) { return dfloat(-a.h, -a.l); }
+__device__ __forceinline__ dfloat operator-(dfloat a, dfloat b) { return a + (-b); }
+__device__ __forceinline__ dfloat operator*(dfloat a, dfloat b) {
+  float p = __fmul_rn(a.h, b.h);
+  float e = __fmaf_rn(a.h, b.h, -p);   // exact error of the product
+  e = __fmaf_rn(a.h, b.l, e);
+  e = __fmaf_rn(a.l, b.h, e);
+  return df_norm(p, e);
+}
+
+// Layer loads bypass L1 (each value is read once per pass), so the small
+// per-layer coefficient table, read by every thread at every layer, stays
+// L1-resident next to the shared-memory rho arrays.
+__device__ __forceinline__ double ld_layer(const double* p) { return __ldcg(p); }
+__device__ __forceinline__ float ld_layer(const float* p) { return __ldcg(p); }
+__device__ __forceinline__ dfloat ld_layer(const dfloat* p) {
+  float2 t = __ldcg(reinterpret_cast<const float2*>(p));
+  return dfloat(t.x, t.y);
+}
 
 template <class R> R* rho_scratch_host(const StepView& v);
 template <> double* rho_scratch_host<double>(const StepView& v) { return v.rho64; }
 template <> float* rho_scratch_host<float>(const StepView& v) { return v.rho32; }
+template <> dfloat* rho_scratch_host<dfloat>(const StepView&) { return nullptr; }
 
 template <class R> __device__ __forceinline__ R* state_T(const StepView& v);
 template <> __device__ __forceinline__ double* state_T<double>(const StepView& v) { return v.T64; }
 template <> __device__ __forceinline__ float* state_T<float>(const StepView& v) { return v.T32; }
+template <> __device__ __forceinline__ dfloat* state_T<dfloat>(const StepView& v) {
+  return reinterpret_cast<dfloat*>(v.Tdf);
+}
 template <class R> __device__ __forceinline__ const R* coef_tab(const StepView& v);
 template <> __device__ __forceinline__ const double* coef_tab<double>(const StepView& v) { return v.coef64; }
 template <> __device__ __forceinline__ const float* coef_tab<float>(const StepView& v) { return v.coef32; }
+template <> __device__ __forceinline__ const dfloat* coef_tab<dfloat>(const StepView& v) {
+  return reinterpret_cast<const dfloat*>(v.coefdf);
+}
 template <class R> __device__ __forceinline__ R* rho_scratch(const StepView& v);
 template <> __device__ __forceinline__ double* rho_scratch<double>(const StepView& v) { return v.rho64; }
 template <> __device__ __forceinline__ float* rho_scratch<float>(const StepView& v) { return v.rho32; }
+template <> __device__ __forceinline__ dfloat* rho_scratch<dfloat>(const StepView&) { return nullptr; }
 
-// One thread per facet column. Block b covers facets [cb.y, cb.y + 128) of
+// One thread per facet column. Block b covers facets [cb.y, cb.y + BS) of
 // mesh cb.x. Q: the new time level's flux per facet.
-template <class R, bool SMEM>
-__global__ void __launch_bounds__(COND_THREADS)
+template <class R, bool SMEM, int BS>
+__global__ void __launch_bounds__(BS)
 k_conduct(StepView v, const double* __restrict__ Qnp1, int upd) {
   extern __shared__ unsigned char smem_raw[];
   R* rho_s = reinterpret_cast<R*>(smem_raw);
-  int2 cb = v.cblocks ? v.cblocks[blockIdx.x] : make_int2(0, blockIdx.x * COND_THREADS);
+  int2 cb = v.cblocks ? v.cblocks[blockIdx.x] : make_int2(0, blockIdx.x * BS);
   const MeshDesc& M = v.md[cb.x];
   if (!M.active) return;
   int fl = cb.y + threadIdx.x;
@@ -66,20 +134,33 @@ k_conduct(StepView v, const double* __restrict__ Qnp1, int upd) {
   R* __restrict__ T = state_T<R>(v) + M.T0 + fl;
   const R* __restrict__ tab = coef_tab<R>(v) + M.coef0;
   R* __restrict__ rho_g = SMEM ? nullptr : rho_scratch<R>(v) + g;
-#define RHO(i) (SMEM ? rho_s[(size_t)(i) * COND_THREADS + threadIdx.x] : rho_g[(size_t)(i) * v.nt])
-  // FP64 solves for T(n+1) directly (the reference's rows); FP32 solves for
-  // the increment dT = T(n+1) - T(n), whose right-hand side
-  // 2 gamma (T(i-1) - T(i)) + 2 alpha (T(i+1) - T(i)) carries no large
-  // cancellation when the diffusion numbers alpha, gamma are large.
-  constexpr bool INC = sizeof(R) == 4;
+#define RHO(i) (SMEM ? rho_s[(size_t)(i) * BS + threadIdx.x] : rho_g[(size_t)(i) * v.nt])
+  // FP64 solves for T(n+1) directly (the reference's rows); FP32 and
+  // double-float solve for the increment dT = T(n+1) - T(n), whose
+  // right-hand side 2 gamma (T(i-1) - T(i)) + 2 alpha (T(i+1) - T(i))
+  // carries no large cancellation when the diffusion numbers alpha, gamma
+  // are large.
+  constexpr bool INC = !std::is_same<R, double>::value;
+  // Stage the column in the rho slots (slot i <- T_i), eight loads in
+  // flight at a time: the upward pass then reads T from shared memory and
+  // overwrites slot i with rho_i once T_i is in registers.
+  for (int i0 = 0; i0 < nz; i0 += 8) {
+    R t[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+      if (i0 + j < nz) t[j] = ld_layer(T + (size_t)(i0 + j) * N);
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+      if (i0 + j < nz) RHO(i0 + j) = t[j];
+  }
   // upward pass
-  R Tip1 = T[(size_t)(nz - 1) * N];
-  R Ti = T[(size_t)(nz - 2) * N];
+  R Tip1 = RHO(nz - 1);
+  R Ti = RHO(nz - 2);
   const R* cb_t = tab + (size_t)(nz - 1) * TAB_W;
   R rho_next = INC ? (R)2 * cb_t[0] * (Ti - Tip1) + (R)cs.cgeo : cb_t[0] * Ti + cb_t[1] * Tip1 + (R)cs.cgeo;
   RHO(nz - 1) = rho_next;
   for (int i = nz - 2; i >= 1; --i) {
-    R Tim1 = T[(size_t)(i - 1) * N];
+    R Tim1 = RHO(i - 1);
     const R* c = tab + (size_t)i * TAB_W;
     R r = INC ? (R)2 * (c[0] * (Tim1 - Ti) + c[2] * (Tip1 - Ti)) : c[0] * Tim1 + c[1] * Ti + c[2] * Tip1;
     R rh = r - c[3] * rho_next;
@@ -112,21 +193,34 @@ k_conduct(StepView v, const double* __restrict__ Qnp1, int upd) {
   } else if (cs.bc == 1) {
     double R0 = (1.0 - cs.alpha0 - cs.gamma0) * T0 + cs.alpha0 * T1 + cs.gamma0 * (2.0 * Ts - T0);
     if (INC) R0 = 2.0 * cs.alpha0 * (T1 - T0) + 4.0 * cs.gamma0 * (Ts - T0) - 2.0 * cs.gamma0 * Ts;
-    double P = (R0 - cs.f0 * rho1) / cs.Ap;
+    double P = (R0 - cs.f0 * rho1) * cs.inv_Ap;
     if (INC) P += T0;
-    double S = 2.0 * cs.gamma0 / cs.Ap;
-    double x = Ts;
-    double tolr = sizeof(R) == 8 ? 1e-13 : 1e-12;
-    for (int it = 0; it < 30; ++it) {
+    // Root of g(x) = Q + 2 k1 (P + (S - 1) x) - es x^4 = A + B x - es x^4
+    // (g' = B - 4 es x^3 < 0): Newton in FP32 to ~1e-6, then FP64 steps
+    // whose g is exact to FP64 and whose step uses an FP32 reciprocal of
+    // g' (each step gains ~7 digits, so two reach the FP64 tolerance).
+    const double A = Q + 2.0 * cs.k1 * P;
+    float xf = (float)Ts;
+    {
+      const float Af = (float)A, Bf = (float)cs.B_top, esf = (float)cs.es;
+      for (int it = 0; it < 30; ++it) {
+        float x3 = xf * xf * xf;
+        float dT = (Af + Bf * xf - esf * x3 * xf) / (Bf - 4.f * esf * x3);
+        xf -= dT;
+        if (fabsf(dT) <= 1e-6f * fabsf(xf)) break;
+      }
+    }
+    double x = (double)xf;
+    double tolr = std::is_same<R, float>::value ? 1e-12 : 1e-13;
+    for (int it = 0; it < 8; ++it) {
       double x3 = x * x * x;
-      double gx = Q + 2.0 * cs.k1 * (P + (S - 1.0) * x) - cs.es * x3 * x;
-      double dg = 2.0 * cs.k1 * (S - 1.0) - 4.0 * cs.es * x3;
-      double dT = gx / dg;
+      double gx = A + cs.B_top * x - cs.es * x3 * x;
+      double dT = gx * (double)__frcp_rn((float)(cs.B_top - 4.0 * cs.es * x3));
       x -= dT;
       if (fabs(dT) <= tolr * fabs(x)) break;
     }
     Tsn = x;
-    T0n = P + S * Tsn;
+    T0n = P + cs.S_top * Tsn;
   } else {
     // prescribed surface temperature: Ts at n, Q holds Ts at n+1
     double b0 = 1.0 + cs.alpha0 + cs.gamma0;
@@ -136,16 +230,26 @@ k_conduct(StepView v, const double* __restrict__ Qnp1, int upd) {
     if (INC) T0n += T0;
     Tsn = Q;
   }
-  double Fs = -cs.k0 * (T0n - Tsn) / cs.z0;
+  double Fs = -(T0n - Tsn) * cs.kz;
   // downward pass
   if (INC) {
     R dprev = (R)(T0n - T0);
     T[0] = (R)T0n;
-    for (int i = 1; i < nz; ++i) {
-      const R* c = tab + (size_t)i * TAB_W;
-      R d = (RHO(i) + c[0] * dprev) * c[4];
-      T[(size_t)i * N] += d;
-      dprev = d;
+    for (int i0 = 1; i0 < nz; i0 += 8) {   // T(n) re-read eight layers at a time
+      R t[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j)
+        if (i0 + j < nz) t[j] = ld_layer(T + (size_t)(i0 + j) * N);
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const int i = i0 + j;
+        if (i < nz) {
+          const R* c = tab + (size_t)i * TAB_W;
+          R d = (RHO(i) + c[0] * dprev) * c[4];
+          T[(size_t)i * N] = t[j] + d;
+          dprev = d;
+        }
+      }
     }
   } else {
     R prev = (R)T0n;
@@ -164,17 +268,25 @@ k_conduct(StepView v, const double* __restrict__ Qnp1, int upd) {
     v.Qprev[g] = Q;
   }
   if (upd) {
-    double inv = (double)(M.frame + 1);
-    v.rad_avg[g] += (Q - v.rad_avg[g]) / inv;
-    v.therm_avg[g] += (Tsn - v.therm_avg[g]) / inv;
+    // running means: 1/(frame + 1) by an FP32 reciprocal and two FP64
+    // Newton steps (no FP64 division)
+    const double n = (double)(M.frame + 1);
+    double rn = (double)__frcp_rn((float)n);
+    rn = rn * (2.0 - n * rn);
+    rn = rn * (2.0 - n * rn);
+    v.rad_avg[g] += (Q - v.rad_avg[g]) * rn;
+    v.therm_avg[g] += (Tsn - v.therm_avg[g]) * rn;
     if (M.frame > 50) v.therm_max[g] = fmax(v.therm_max[g], Tsn);
   }
 }
 
-template <class A, class B>
-__global__ void k_convert(const A* __restrict__ in, B* __restrict__ out, size_t n) {
+__global__ void k_df_to_f(const float2* __restrict__ in, float* __restrict__ out, size_t n) {
   size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) out[i] = (B)in[i];
+  if (i < n) out[i] = (float)((double)in[i].x + (double)in[i].y);
+}
+__global__ void k_f_to_df(const float* __restrict__ in, float2* __restrict__ out, size_t n) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = make_float2(in[i], 0.f);
 }
 
 // Coefficients of conductionQ.f:50-73 / conductionT.f:28-45 and the shared
@@ -235,6 +347,10 @@ int build_tables(int nz, const double* z, const double* ti, const double* rhoc, 
   cs.Ap = (1.0 + alpha[0] + 2.0 * gamma[0]) + cs.f0 * gamma[1];
   cs.k0 = k[0];
   cs.z0 = z[0];
+  cs.inv_Ap = 1.0 / cs.Ap;
+  cs.S_top = 2.0 * gamma[0] / cs.Ap;
+  cs.B_top = 2.0 * cs.k1 * (cs.S_top - 1.0);
+  cs.kz = k[0] / z[0];
   cs.cgeo = dt / rhoc[nz - 1] * Fgeo / (z[nz - 1] - z[nz - 2]);
   cs.es = emiss * SIGMA_SB;
   cs.nz = nz;
@@ -242,16 +358,16 @@ int build_tables(int nz, const double* z, const double* ti, const double* rhoc, 
   return ILG_OK;
 }
 
-template <class R>
+template <class R, int BS>
 int launch_conduct(const StepView& v, const double* Q, int upd, int nz_max, cudaStream_t s) {
-  size_t smem = (size_t)nz_max * COND_THREADS * sizeof(R);
-  int grid = v.cblocks ? v.ncblocks : div_up(v.nt, COND_THREADS);
+  size_t smem = (size_t)nz_max * BS * sizeof(R);
+  int grid = v.cblocks ? v.ncblocks : div_up(v.nt, BS);
   if (grid <= 0) return ILG_OK;
   if (smem <= SMEM_LIMIT) {
-    k_conduct<R, true><<<grid, COND_THREADS, smem, s>>>(v, Q, upd);
+    k_conduct<R, true, BS><<<grid, BS, smem, s>>>(v, Q, upd);
   } else {
     if (!rho_scratch_host<R>(v)) { set_error("conduction: %d layers need the deep-column scratch", nz_max); return ILG_ERR_ARG; }
-    k_conduct<R, false><<<grid, COND_THREADS, 0, s>>>(v, Q, upd);
+    k_conduct<R, false, BS><<<grid, BS, 0, s>>>(v, Q, upd);
   }
   ILG_CUDA(cudaGetLastError());
   return ILG_OK;
@@ -261,11 +377,17 @@ int launch_conduct(const StepView& v, const double* Q, int upd, int nz_max, cuda
 
 // Opt the shared-memory kernels into SMEM_LIMIT bytes (once per process,
 // before any capture).
+int conduction_step_threads() { return COND_STEP_THREADS; }
+
 int conduction_setup() {
   static bool done = false;
   if (done) return ILG_OK;
-  ILG_CUDA(cudaFuncSetAttribute(k_conduct<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_LIMIT));
-  ILG_CUDA(cudaFuncSetAttribute(k_conduct<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_LIMIT));
+  ILG_CUDA(cudaFuncSetAttribute(k_conduct<double, true, COND_THREADS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)SMEM_LIMIT));
+  ILG_CUDA(cudaFuncSetAttribute(k_conduct<dfloat, true, COND_STEP_THREADS>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_LIMIT));
+  ILG_CUDA(cudaFuncSetAttribute(k_conduct<float, true, COND_STEP_THREADS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)SMEM_LIMIT));
   done = true;
   return ILG_OK;
 }
@@ -283,8 +405,10 @@ int conduction_prepare(Context& c, double dt, int precision) {
     ILG_TRY(c.coef32.alloc(t32.size()));
     ILG_CUDA(cudaMemcpy(c.coef32.p, t32.data(), t32.size() * 4, cudaMemcpyHostToDevice));
   } else {
-    ILG_TRY(c.coef64.alloc(tab.size()));
-    ILG_CUDA(cudaMemcpy(c.coef64.p, tab.data(), tab.size() * 8, cudaMemcpyHostToDevice));
+    std::vector<float2> tdf(tab.size());
+    for (size_t i = 0; i < tab.size(); ++i) tdf[i] = split_df_host(tab[i]);
+    ILG_TRY(c.coefdf.alloc(tdf.size()));
+    ILG_CUDA(cudaMemcpy(c.coefdf.p, tdf.data(), tdf.size() * 8, cudaMemcpyHostToDevice));
   }
   c.cond_cs = cs;
   c.coef_dt = dt;
@@ -292,16 +416,16 @@ int conduction_prepare(Context& c, double dt, int precision) {
   return ILG_OK;
 }
 
-// Move the layer state between fp64 and fp32 storage.
+// Move the layer state between double-float and fp32 storage.
 int conduction_state_convert(Context& c, int precision) {
   if (c.state_prec == precision) return ILG_OK;
   size_t n = (size_t)c.nz * c.nt;
   if (precision == ILG_PREC_MIXED) {
     ILG_TRY(c.T32.alloc(n));
-    k_convert<double, float><<<div_up(n, 256), 256, 0, c.stream>>>(c.T64.p, c.T32.p, n);
+    k_df_to_f<<<div_up(n, 256), 256, 0, c.stream>>>(c.Tdf.p, c.T32.p, n);
   } else {
-    ILG_TRY(c.T64.alloc(n));
-    k_convert<float, double><<<div_up(n, 256), 256, 0, c.stream>>>(c.T32.p, c.T64.p, n);
+    ILG_TRY(c.Tdf.alloc(n));
+    k_f_to_df<<<div_up(n, 256), 256, 0, c.stream>>>(c.T32.p, c.Tdf.p, n);
   }
   ILG_CUDA(cudaGetLastError());
   c.state_prec = precision;
@@ -309,8 +433,8 @@ int conduction_state_convert(Context& c, int precision) {
 }
 
 int conduction_launch(const StepView& v, const double* Q, int precision, int upd, int nz_max, cudaStream_t s) {
-  if (precision == ILG_PREC_MIXED) return launch_conduct<float>(v, Q, upd, nz_max, s);
-  return launch_conduct<double>(v, Q, upd, nz_max, s);
+  if (precision == ILG_PREC_MIXED) return launch_conduct<float, COND_STEP_THREADS>(v, Q, upd, nz_max, s);
+  return launch_conduct<dfloat, COND_STEP_THREADS>(v, Q, upd, nz_max, s);
 }
 
 // Standalone batched columns (host arrays, reference layout: column-major
@@ -356,7 +480,7 @@ static int run_columns(int ncol, int nz, const double* z, double dt, const doubl
   v.nt = ncol; v.nmesh = 1; v.md = dmd.p;
   v.Tsurf = dTs.p; v.Fsurf = dFs.p; v.Qprev = dQn.p; v.T64 = dT.p; v.coef64 = dtab.p; v.rho64 = rho.p;
   v.derr = derr.p;
-  ILG_TRY(launch_conduct<double>(v, dQ.p, 0, nz, s));
+  ILG_TRY((launch_conduct<double, COND_THREADS>(v, dQ.p, 0, nz, s)));
   int herr[DERR_COUNT];
   ILG_CUDA(cudaMemcpyAsync(Tl.data(), dT.p, Tl.size() * 8, cudaMemcpyDeviceToHost, s));
   if (bc != 2) ILG_CUDA(cudaMemcpyAsync(Tsurf, dTs.p, (size_t)ncol * 8, cudaMemcpyDeviceToHost, s));
@@ -441,7 +565,7 @@ int noalloc_setup(unsigned char** out) {
   if (!g_noalloc_ptr[dev]) {
     void* ptr = nullptr;
     ILG_CUDA(cudaGetSymbolAddress(&ptr, g_cond_scratch));
-    ILG_CUDA(cudaFuncSetAttribute(k_conduct<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    ILG_CUDA(cudaFuncSetAttribute(k_conduct<double, true, COND_THREADS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)SMEM_LIMIT));
     g_noalloc_ptr[dev] = ptr;
   }
@@ -495,7 +619,7 @@ extern "C" int ilg_conductionq_batch_noalloc(int ncol, int nz, const double* z, 
   v.Tsurf = Tsurf; v.Fsurf = Fsurf; v.Qprev = qprev; v.T64 = T; v.coef64 = dtab;
   v.rho64 = deep ? reinterpret_cast<double*>(base + L.rho) : nullptr;
   v.derr = flags;
-  ILG_TRY(launch_conduct<double>(v, Qnp1, 0, nz, s));
+  ILG_TRY((launch_conduct<double, COND_THREADS>(v, Qnp1, 0, nz, s)));
   int herr[DERR_COUNT];
   ILG_CUDA(cudaMemcpyAsync(herr, flags, sizeof(herr), cudaMemcpyDeviceToHost, s));
   ILG_CUDA(cudaStreamSynchronize(s));

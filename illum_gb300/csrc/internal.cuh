@@ -39,6 +39,7 @@ struct HorizonNode {   // one node of the zenith-angle bisection tree
 // Scalars of a conduction table set (conduction.cu build_tables).
 struct CondScalars {
   double alpha0, gamma0, k1, f0, gamma1, Ap, k0, z0, cgeo, es;
+  double inv_Ap, S_top, B_top, kz;   // 1/Ap, 2 gamma0/Ap, 2 k1 (S_top - 1), k0/z0
   int nz, bc;                        // bc: 0 linearised, 1 Newton, 2 prescribed Ts (conductionT)
 };
 
@@ -100,9 +101,11 @@ struct StepView {
   const SunAux* suns;
   double *Tsurf, *Fsurf, *Qprev, *rad, *rad_avg, *therm_avg, *therm_max, *E, *xprev;
   float* x32;                  // 3 x nt (mixed radiosity)
-  double* T64;
-  float* T32;
+  double* T64;                 // [nz][nt] fp64 layers (standalone column entry points)
+  float2* Tdf;                 // [nz][nt] double-float layers (the FP64 step)
+  float* T32;                  // [nz][nt] fp32 layers (the mixed step)
   const double* coef64;
+  const float2* coefdf;
   const float* coef32;
   // radiosity row tiles
   const RowTile* tiles;
@@ -181,14 +184,14 @@ struct Context {
   std::vector<double> z_h, ti_h, rhoc_h;
   double coef_dt = -1.0;          // dt the coefficient tables were built for
   int coef_prec = -1;
-  dbuf<double> coef64;            // per-layer tables (see conduction.cu)
+  dbuf<float2> coefdf;            // per-layer tables (see conduction.cu)
   dbuf<float> coef32;
   CondScalars cond_cs{};
   dbuf<double> rho64;             // deep-column fallback scratch
   dbuf<float> rho32;
-  dbuf<double> T64;               // [nz][N]
-  dbuf<float> T32;
-  int state_prec = 0;             // which of T64 / T32 holds the state
+  dbuf<float2> Tdf;               // [nz][N] double-float layers (FP64 precision)
+  dbuf<float> T32;                // [nz][N] fp32 layers (mixed precision)
+  int state_prec = 0;             // which of Tdf / T32 holds the state
   dbuf<double> Tsurf, Fsurf, Qprev;
   dbuf<double> rad, rad_avg, therm_avg, therm_max, E, xtmp, Q;
   dbuf<double> xprev;             // radiosity solution of the step before
@@ -268,6 +271,7 @@ int flush_launch(float4* buf, size_t n, unsigned salt, cudaStream_t s);
 // ---- conduction.cu ----
 int conduction_prepare(Context& c, double dt, int precision);
 int conduction_setup();
+int conduction_step_threads();   // facets per conduction block of a scene step
 // Q: heat flux at the new time level per facet (global index); upd: also
 // update rad_avg / therm_avg / therm_max; nz_max: deepest mesh of the view.
 int conduction_launch(const StepView& v, const double* Q, int precision, int upd, int nz_max, cudaStream_t s);
