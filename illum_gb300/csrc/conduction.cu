@@ -83,6 +83,11 @@ __device__ __forceinline__ dfloat operator*(dfloat a, dfloat b) {
   return df_norm(p, e);
 }
 
+// 2x, exact
+__device__ __forceinline__ double twice(double a) { return 2.0 * a; }
+__device__ __forceinline__ float twice(float a) { return 2.f * a; }
+__device__ __forceinline__ dfloat twice(dfloat a) { return dfloat(2.f * a.h, 2.f * a.l); }
+
 // Layer loads bypass L1 (each value is read once per pass), so the small
 // per-layer coefficient table, read by every thread at every layer, stays
 // L1-resident next to the shared-memory rho arrays.
@@ -141,28 +146,49 @@ k_conduct(StepView v, const double* __restrict__ Qnp1, int upd) {
   // carries no large cancellation when the diffusion numbers alpha, gamma
   // are large.
   constexpr bool INC = !std::is_same<R, double>::value;
-  // Stage the column in the rho slots (slot i <- T_i), eight loads in
-  // flight at a time: the upward pass then reads T from shared memory and
-  // overwrites slot i with rho_i once T_i is in registers.
-  for (int i0 = 0; i0 < nz; i0 += 8) {
-    R t[8];
+  // Stage the column in the rho slots (slot i <- T_i): the upward pass then
+  // reads T from shared memory and overwrites slot i with rho_i once T_i is
+  // in registers. In shared memory the copies are asynchronous (cp.async,
+  // every layer in flight at once; each thread waits for its own copies).
+  if (SMEM) {
+    for (int i = 0; i < nz; ++i) {
+      unsigned sa = (unsigned)__cvta_generic_to_shared(&rho_s[(size_t)i * BS + threadIdx.x]);
+      const R* ga = T + (size_t)i * N;
+      if (sizeof(R) == 8)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(sa), "l"(ga) : "memory");
+      else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(sa), "l"(ga) : "memory");
+    }
+    asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+  } else {
+    for (int i0 = 0; i0 < nz; i0 += 8) {
+      R t[8];
 #pragma unroll
-    for (int j = 0; j < 8; ++j)
-      if (i0 + j < nz) t[j] = ld_layer(T + (size_t)(i0 + j) * N);
+      for (int j = 0; j < 8; ++j)
+        if (i0 + j < nz) t[j] = ld_layer(T + (size_t)(i0 + j) * N);
 #pragma unroll
-    for (int j = 0; j < 8; ++j)
-      if (i0 + j < nz) RHO(i0 + j) = t[j];
+      for (int j = 0; j < 8; ++j)
+        if (i0 + j < nz) RHO(i0 + j) = t[j];
+    }
   }
   // upward pass
   R Tip1 = RHO(nz - 1);
   R Ti = RHO(nz - 2);
   const R* cb_t = tab + (size_t)(nz - 1) * TAB_W;
-  R rho_next = INC ? (R)2 * cb_t[0] * (Ti - Tip1) + (R)cs.cgeo : cb_t[0] * Ti + cb_t[1] * Tip1 + (R)cs.cgeo;
+  R dn = Ti - Tip1;   // increment form: layer differences d_i = T(i-1) - T(i), each formed once
+  R rho_next = INC ? twice(cb_t[0] * dn) + (R)cs.cgeo : cb_t[0] * Ti + cb_t[1] * Tip1 + (R)cs.cgeo;
   RHO(nz - 1) = rho_next;
   for (int i = nz - 2; i >= 1; --i) {
     R Tim1 = RHO(i - 1);
     const R* c = tab + (size_t)i * TAB_W;
-    R r = INC ? (R)2 * (c[0] * (Tim1 - Ti) + c[2] * (Tip1 - Ti)) : c[0] * Tim1 + c[1] * Ti + c[2] * Tip1;
+    R r;
+    if (INC) {
+      R dm = Tim1 - Ti;
+      r = twice(c[0] * dm - c[2] * dn);
+      dn = dm;
+    } else {
+      r = c[0] * Tim1 + c[1] * Ti + c[2] * Tip1;
+    }
     R rh = r - c[3] * rho_next;
     RHO(i) = rh;
     rho_next = rh;
@@ -235,21 +261,20 @@ k_conduct(StepView v, const double* __restrict__ Qnp1, int upd) {
   if (INC) {
     R dprev = (R)(T0n - T0);
     T[0] = (R)T0n;
-    for (int i0 = 1; i0 < nz; i0 += 8) {   // T(n) re-read eight layers at a time
-      R t[8];
+    for (int i = 1; i < nz; ++i) {   // the increments, into the rho slots
+      const R* c = tab + (size_t)i * TAB_W;
+      R d = (RHO(i) + c[0] * dprev) * c[4];
+      RHO(i) = d;
+      dprev = d;
+    }
+    for (int i0 = 1; i0 < nz; i0 += 16) {   // T(n+1) = T(n) + dT, sixteen layers in flight
+      R t[16];
 #pragma unroll
-      for (int j = 0; j < 8; ++j)
+      for (int j = 0; j < 16; ++j)
         if (i0 + j < nz) t[j] = ld_layer(T + (size_t)(i0 + j) * N);
 #pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        const int i = i0 + j;
-        if (i < nz) {
-          const R* c = tab + (size_t)i * TAB_W;
-          R d = (RHO(i) + c[0] * dprev) * c[4];
-          T[(size_t)i * N] = t[j] + d;
-          dprev = d;
-        }
-      }
+      for (int j = 0; j < 16; ++j)
+        if (i0 + j < nz) T[(size_t)(i0 + j) * N] = t[j] + RHO(i0 + j);
     }
   } else {
     R prev = (R)T0n;
