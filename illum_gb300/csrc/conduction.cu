@@ -178,6 +178,7 @@ k_conduct(StepView v, const double* __restrict__ Qnp1, int upd) {
   R dn = Ti - Tip1;   // increment form: layer differences d_i = T(i-1) - T(i), each formed once
   R rho_next = INC ? twice(cb_t[0] * dn) + (R)cs.cgeo : cb_t[0] * Ti + cb_t[1] * Tip1 + (R)cs.cgeo;
   RHO(nz - 1) = rho_next;
+#pragma unroll 4
   for (int i = nz - 2; i >= 1; --i) {
     R Tim1 = RHO(i - 1);
     const R* c = tab + (size_t)i * TAB_W;
@@ -261,6 +262,7 @@ k_conduct(StepView v, const double* __restrict__ Qnp1, int upd) {
   if (INC) {
     R dprev = (R)(T0n - T0);
     T[0] = (R)T0n;
+#pragma unroll 4
     for (int i = 1; i < nz; ++i) {   // the increments, into the rho slots
       const R* c = tab + (size_t)i * TAB_W;
       R d = (RHO(i) + c[0] * dprev) * c[4];
