@@ -418,6 +418,8 @@ def main():
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "arithmetic": "FP64 state, iterates, residuals and surface boundary; radiosity dot products and "
+                              "conduction layer recurrences in double-float (FP32 pairs, ~2^-46 relative)",
                 "config": {"workload": "icosphere L6 81,920 facets, 200 craters 30-300 m, nphi 64, nz 60, "
                                        "dt 30 s, radiosity tol 1e-10, Newton boundary, E = direct coupling (C1, plain FP64 path)",
                            "facets": N, "nnz": nnz, "l2": "256 MB flush before every timed step",
