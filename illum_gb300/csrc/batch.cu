@@ -54,7 +54,9 @@ struct Batch {
   dbuf<int> mesh_of;
   dbuf<int2> cblocks;
   dbuf<float4> cen, nrm, frame32;
-  dbuf<double> frame, H, hmin, hmax, disk;
+  dbuf<double> frame, H, disk;
+  dbuf<float> H32, disk32;
+  dbuf<float2> hmm32;
   dbuf<SunAux> suns;
   dbuf<double> Tsurf, Fsurf, Qprev, rad, rad_avg, therm_avg, therm_max, E, xtmp, xprev;
   dbuf<float> x32;
@@ -137,8 +139,9 @@ static int build(Batch& b) {
   ILG_TRY(b.mesh_of.alloc(nt));
   ILG_TRY(b.cblocks.alloc(ncb));
   ILG_TRY(b.cen.alloc(nt)); ILG_TRY(b.nrm.alloc(nt)); ILG_TRY(b.frame32.alloc(3 * nt));
-  ILG_TRY(b.frame.alloc(9 * nt)); ILG_TRY(b.H.alloc(nH)); ILG_TRY(b.hmin.alloc(nt)); ILG_TRY(b.hmax.alloc(nt));
+  ILG_TRY(b.frame.alloc(9 * nt)); ILG_TRY(b.H.alloc(nH)); ILG_TRY(b.H32.alloc(nH)); ILG_TRY(b.hmm32.alloc(nt));
   ILG_TRY(b.disk.alloc(2 * (size_t)ndisk));
+  ILG_TRY(b.disk32.alloc(2 * (size_t)ndisk));
   ILG_TRY(b.suns.alloc(nsun));
   for (dbuf<double>* d : {&b.Tsurf, &b.Fsurf, &b.Qprev, &b.rad, &b.rad_avg, &b.therm_avg, &b.therm_max, &b.E,
                           &b.xprev})
@@ -199,8 +202,8 @@ static int build(Batch& b) {
     ILG_TRY(cat(b.frame32, 3 * f0, c.frame32.p, 3 * N, s));
     ILG_TRY(cat(b.frame, 9 * f0, c.frame.p, 9 * N, s));
     ILG_TRY(cat(b.H, (size_t)M.H0, c.H.p, N * c.nphi, s));
-    ILG_TRY(cat(b.hmin, f0, c.hmin.p, N, s));
-    ILG_TRY(cat(b.hmax, f0, c.hmax.p, N, s));
+    ILG_TRY(cat(b.H32, (size_t)M.H0, c.H32.p, N * c.nphi, s));
+    ILG_TRY(cat(b.hmm32, f0, c.hmm32.p, N, s));
     ILG_TRY(cat(b.suns, (size_t)M.sun0, c.sun_aux.p, (size_t)c.nsun + 1, s));
     ILG_TRY(cat(b.Tsurf, f0, c.Tsurf.p, N, s));
     ILG_TRY(cat(b.Fsurf, f0, c.Fsurf.p, N, s));
@@ -248,6 +251,7 @@ static int build(Batch& b) {
     for (int k = 0; k < div_up(c.nt, cbs); ++k) cbh.push_back(make_int2(i, k * cbs));
   }
   ILG_TRY(cat(b.disk, 0, b.members[0]->c.disk.p, 2 * (size_t)ndisk, s));
+  ILG_TRY(cat(b.disk32, 0, b.members[0]->c.disk32.p, 2 * (size_t)ndisk, s));
   ILG_CUDA(cudaMemcpyAsync(b.cblocks.p, cbh.data(), cbh.size() * sizeof(int2), cudaMemcpyHostToDevice, s));
   ILG_CUDA(cudaMemcpyAsync(b.md.p, b.mh.data(), n * sizeof(MeshDesc), cudaMemcpyHostToDevice, s));
   ILG_CUDA(cudaStreamSynchronize(s));
@@ -256,7 +260,8 @@ static int build(Batch& b) {
   v = StepView{};
   v.nt = b.nt; v.nmesh = n; v.md = b.md.p; v.mesh_of = b.mesh_of.p;
   v.cen = b.cen.p; v.nrm = b.nrm.p; v.frame32 = b.frame32.p; v.frame = b.frame.p; v.H = b.H.p;
-  v.hmin = b.hmin.p; v.hmax = b.hmax.p; v.disk = b.disk.p; v.ndisk = ndisk; v.suns = b.suns.p;
+  v.H32 = b.H32.p; v.hmm32 = b.hmm32.p; v.disk = b.disk.p; v.disk32 = b.disk32.p; v.ndisk = ndisk;
+  v.suns = b.suns.p;
   v.Tsurf = b.Tsurf.p; v.Fsurf = b.Fsurf.p; v.Qprev = b.Qprev.p; v.rad = b.rad.p; v.rad_avg = b.rad_avg.p;
   v.therm_avg = b.therm_avg.p; v.therm_max = b.therm_max.p; v.E = b.E.p; v.xprev = b.xprev.p;
   v.x32 = b.x32.p; v.Tdf = b.Tdf.p; v.T32 = b.T32.p; v.coefdf = b.coefdf.p; v.coef32 = b.coef32.p;

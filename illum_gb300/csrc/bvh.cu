@@ -313,14 +313,20 @@ __global__ void k_horizons(const float4* __restrict__ nodes, const float4* __res
   }
 }
 
-__global__ void k_hminmax(const double* __restrict__ H, int nt, int nphi, double* hmin, double* hmax) {
+// fp32 copies of a facet's horizon and of its min / max (the insolation
+// filters compare in fp32 with margins).
+__global__ void k_horizon_f32(const double* __restrict__ H, int nt, int nphi, float* H32, float2* hmm) {
   int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= nt) return;
   const double* h = H + (int64_t)f * nphi;
+  float* h32 = H32 + (int64_t)f * nphi;
   double lo = h[0], hi = h[0];
-  for (int k = 1; k < nphi; ++k) { lo = fmin(lo, h[k]); hi = fmax(hi, h[k]); }
-  hmin[f] = lo;
-  hmax[f] = hi;
+  for (int k = 0; k < nphi; ++k) {
+    lo = fmin(lo, h[k]);
+    hi = fmax(hi, h[k]);
+    h32[k] = (float)h[k];
+  }
+  hmm[f] = make_float2((float)lo, (float)hi);
 }
 
 // ------------------------------------------------------------------ visibility
@@ -645,19 +651,24 @@ int horizons_build(Context& c, int nphi, double theta_eps, double offset) {
   ILG_CUDA(cudaMemcpyAsync(dc.p, cph.data(), nphi * 8, cudaMemcpyHostToDevice, s));
   ILG_CUDA(cudaMemcpyAsync(ds.p, sph.data(), nphi * 8, cudaMemcpyHostToDevice, s));
   ILG_TRY(c.H.alloc((size_t)c.nt * nphi));
-  ILG_TRY(c.hmin.alloc(c.nt));
-  ILG_TRY(c.hmax.alloc(c.nt));
   int64_t total = (int64_t)c.nt * nphi;
   k_horizons<<<div_up(total, 128), 128, 0, s>>>(c.nodes.p, c.tri_s.p, c.root, c.tri_o.p, c.cen.p, c.nrm.p, c.nt,
                                                 nphi, dc.p, ds.p, dtree.p, (int)tree.size(), (float)offset, c.H.p,
                                                 c.derr.p);
   ILG_CUDA(cudaGetLastError());
-  k_hminmax<<<div_up(c.nt, 256), 256, 0, s>>>(c.H.p, c.nt, nphi, c.hmin.p, c.hmax.p);
-  ILG_CUDA(cudaGetLastError());
-  ILG_CUDA(cudaStreamSynchronize(s));
   c.nphi = nphi;
   c.dphi = dphi;
+  ILG_TRY(horizons_f32(c));
   return read_device_errors(c);
+}
+
+int horizons_f32(Context& c) {
+  ILG_TRY(c.H32.alloc((size_t)c.nt * c.nphi));
+  ILG_TRY(c.hmm32.alloc(c.nt));
+  k_horizon_f32<<<div_up(c.nt, 256), 256, 0, c.stream>>>(c.H.p, c.nt, c.nphi, c.H32.p, c.hmm32.p);
+  ILG_CUDA(cudaGetLastError());
+  ILG_CUDA(cudaStreamSynchronize(c.stream));
+  return ILG_OK;
 }
 
 int form_factors_build(Context& c, const double* albedo_h, double albedo_scalar, double offset, int64_t* rays_out) {

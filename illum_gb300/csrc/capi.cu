@@ -58,8 +58,11 @@ static int set_disk(Context& c, const double* disk_xy, int ndisk) {
   std::vector<double> h(disk_xy, disk_xy + 2 * (size_t)ndisk);
   double rmax = 0.0;
   for (int s = 0; s < ndisk - 1; ++s) rmax = std::max(rmax, std::sqrt(h[s] * h[s] + h[ndisk + s] * h[ndisk + s]));
+  std::vector<float> h32(h.begin(), h.end());
   ILG_TRY(c.disk.alloc(2 * (size_t)ndisk));
+  ILG_TRY(c.disk32.alloc(2 * (size_t)ndisk));
   ILG_CUDA(cudaMemcpyAsync(c.disk.p, h.data(), h.size() * 8, cudaMemcpyHostToDevice, c.stream));
+  ILG_CUDA(cudaMemcpyAsync(c.disk32.p, h32.data(), h32.size() * 4, cudaMemcpyHostToDevice, c.stream));
   ILG_CUDA(cudaStreamSynchronize(c.stream));
   c.ndisk = ndisk;
   c.disk_rmax = rmax;
@@ -137,7 +140,8 @@ static StepView solo_view(Context& c, int precision) {
   v.md = c.md.p;
   v.mesh_of = nullptr;
   v.cen = c.cen.p; v.nrm = c.nrm.p; v.frame32 = c.frame32.p;
-  v.frame = c.frame.p; v.H = c.H.p; v.hmin = c.hmin.p; v.hmax = c.hmax.p; v.disk = c.disk.p;
+  v.frame = c.frame.p; v.H = c.H.p; v.H32 = c.H32.p; v.hmm32 = c.hmm32.p; v.disk = c.disk.p;
+  v.disk32 = c.disk32.p;
   v.ndisk = c.ndisk;
   v.suns = c.sun_aux.p;
   v.Tsurf = c.Tsurf.p; v.Fsurf = c.Fsurf.p; v.Qprev = c.Qprev.p; v.rad = c.rad.p; v.rad_avg = c.rad_avg.p;
@@ -168,8 +172,10 @@ MeshDesc solo_desc(const Context& c, const ilg_run_opts* o, int first_sun) {
   M.interp = c.interp;
   M.H0 = 0;
   M.dphi = c.dphi;
+  M.dphi32 = (float)c.dphi;
   M.denom = c.norm_mode == 0 ? (double)(c.nphi - 1) : (double)(c.ndisk - 1);
   M.nsamp = c.ndisk - 1;
+  M.lit_all = (double)M.nsamp / M.denom;
   M.coupling = o ? o->coupling : ILG_COUPLE_DIRECT;
   M.sun0 = 0;
   M.nsun = c.nsun;
@@ -452,25 +458,13 @@ int ilg_set_horizons(ilg_ctx* ctx, int nphi, const double* h) {
   Context& c = ctx->c;
   invalidate_graph(c);
   size_t n = (size_t)c.nt * nphi;
-  std::vector<double> lo(c.nt), hi(c.nt);
-  for (int f = 0; f < c.nt; ++f) {
-    const double* col = h + (size_t)f * nphi;
-    double a = col[0], b = col[0];
-    for (int k = 1; k < nphi; ++k) { a = std::min(a, col[k]); b = std::max(b, col[k]); }
-    if (!(a == a) || !(b == b)) { set_error("horizon column %d holds NaN", f); return ILG_ERR_ARG; }
-    lo[f] = a;
-    hi[f] = b;
-  }
+  for (size_t k = 0; k < n; ++k)
+    if (!(h[k] == h[k])) { set_error("horizon column %d holds NaN", (int)(k / nphi)); return ILG_ERR_ARG; }
   ILG_TRY(c.H.alloc(n));
-  ILG_TRY(c.hmin.alloc(c.nt));
-  ILG_TRY(c.hmax.alloc(c.nt));
   ILG_CUDA(cudaMemcpyAsync(c.H.p, h, n * 8, cudaMemcpyHostToDevice, c.stream));
-  ILG_CUDA(cudaMemcpyAsync(c.hmin.p, lo.data(), (size_t)c.nt * 8, cudaMemcpyHostToDevice, c.stream));
-  ILG_CUDA(cudaMemcpyAsync(c.hmax.p, hi.data(), (size_t)c.nt * 8, cudaMemcpyHostToDevice, c.stream));
-  ILG_CUDA(cudaStreamSynchronize(c.stream));
   c.nphi = nphi;
   c.dphi = TWO_PI / (double)(nphi - 1);
-  return ILG_OK;
+  return horizons_f32(c);
 }
 
 int ilg_set_insolation(ilg_ctx* ctx, int norm_mode, int interp, double solar_const) {

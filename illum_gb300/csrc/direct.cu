@@ -45,7 +45,7 @@ __device__ __forceinline__ void store_direct(const StepView& v, const MeshDesc& 
 
 // Range of the horizon threshold of src/cpp/illum.cpp:431-434 over the
 // azimuth interval [a, b] (0 <= a <= b <= 2 pi), bins of width dphi.
-__device__ __forceinline__ bool thr_range(const double* __restrict__ h, int nphi, float dphi, int interp, float a,
+__device__ __forceinline__ bool thr_range(const float* __restrict__ h, int nphi, float dphi, int interp, float a,
                                           float b, float& tmin, float& tmax) {
   int k0 = (int)floorf(a / dphi), k1 = (int)floorf(b / dphi);
   k0 = max(0, min(k0, nphi - 1));
@@ -54,13 +54,13 @@ __device__ __forceinline__ bool thr_range(const double* __restrict__ h, int nphi
   for (int k = k0; k <= k1; ++k) {
     float lo = fmaxf(a, (float)k * dphi), hi = fminf(b, (float)(k + 1) * dphi);
     if (hi < lo) hi = lo;
-    float hk = (float)h[k];
+    float hk = h[k];
     float v0, v1;
     if (interp == 0) {
       v0 = hk + (lo - (float)k * dphi);
       v1 = hk + (hi - (float)k * dphi);
     } else {
-      float hk1 = (float)h[k + 1 < nphi ? k + 1 : nphi - 1];
+      float hk1 = h[k + 1 < nphi ? k + 1 : nphi - 1];
       v0 = hk + (lo - (float)k * dphi) / dphi * (hk1 - hk);
       v1 = hk + (hi - (float)k * dphi) / dphi * (hk1 - hk);
     }
@@ -89,8 +89,9 @@ __global__ void k_direct_classify(StepView v, int dropin) {
       decided = 1;                   // facing away: max(0, mu) = 0
     } else {
       const float MARG = 1e-6f, CEPS = 1e-6f;
-      float alo = (float)v.hmin[f] - S->alpha - MARG;
-      float ahi = (float)v.hmax[f] + (float)M.dphi + S->alpha + MARG;
+      const float2 hmm = v.hmm32[f];
+      float alo = hmm.x - S->alpha - MARG;
+      float ahi = hmm.y + M.dphi32 + S->alpha + MARG;
       if (alo > 0.f && (mu32 - eps) > cosf(alo) + CEPS) decided = 2;
       else if (ahi < 3.14159f && (mu32 + eps) < cosf(ahi) - CEPS) decided = 1;
       else {
@@ -111,8 +112,8 @@ __global__ void k_direct_classify(StepView v, int dropin) {
             float ph = atan2f(dy, dx);
             const float TWO_PI_F = 6.2831853f;
             if (ph < 0.f) ph += TWO_PI_F;
-            float dphi = (float)M.dphi;
-            const double* h = v.H + M.H0 + (size_t)(f - M.facet0) * M.nphi;
+            float dphi = M.dphi32;
+            const float* h = v.H32 + M.H0 + (size_t)(f - M.facet0) * M.nphi;
             float tmin = 3e38f, tmax = -3e38f;
             float lo = ph - dp, hi = ph + dp;
             bool ok = true;
@@ -141,7 +142,7 @@ __global__ void k_direct_classify(StepView v, int dropin) {
         d3 p = mkd((double)c4.x, (double)c4.y, (double)c4.z);
         const double* fr = v.frame + 9 * (int64_t)f;
         double mu = sun_mu(mkd(S->sx, S->sy, S->sz), p, mkd(fr[6], fr[7], fr[8]));
-        dv = (double)M.nsamp / M.denom;
+        dv = M.lit_all;   // (double)nsamp / denom
         dv *= (mu > 0.0 ? mu : 0.0);
         dv *= S->flux;
       }
@@ -161,77 +162,189 @@ __global__ void k_direct_classify(StepView v, int dropin) {
   }
 }
 
-// Pass 2: one warp per undecided facet. Each sample is first classified
-// in FP32 (direction N + kappa (x T + y B) in the facet frame, atan2f);
-// only samples within MT of the threshold or MP of a bin edge, or facets
-// with the sun near the zenith, are evaluated with the exact FP64
-// sample_lit. MT and MP dominate the FP32 errors (~1e-6 rad).
-__global__ void k_direct_exact(StepView v, int dropin) {
-  int nw = v.counters[0];
-  int lane = threadIdx.x & 31;
-  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  int nwarps = (gridDim.x * blockDim.x) >> 5;
+// Pass 2: blocks of DX_FACETS undecided facets. The GPU's FP64 pipe is slow
+// per instruction, so FP64 runs one lane per facet or per ambiguous
+// sample, and the FP64 set-up overlaps the FP32 filter:
+//   warp 0, one lane per facet: the sun frame (T, B) of geom.h sun_frame and
+//     the cosine mu in FP64 (the values the exact test and the flux need);
+//   warps 1.., concurrently: an FP32 set-up per facet (direction N, frame,
+//     kappa), then one thread per (facet, sample): the sample is classified
+//     in FP32 (direction N + kappa (x T + y B) in the facet frame, atan2f);
+//     lit samples count, samples within MT of the threshold or MP of a bin
+//     edge (or with the sun near the zenith) are listed;
+//   all threads: the listed samples with the exact FP64 sample_lit,
+//     bit-identical to the CPU oracle;
+//   warp 0: count / denom * mu * flux as the reference.
+// The FP32 set-up differs from the rounded FP64 one by ~1e-7 rad (p is
+// negligible next to |S|), far below MT and MP, which dominate the FP32
+// errors; a facet whose sun-frame axis choice is within rounding of a tie
+// lists all its samples. Counts are integer sums, so the result does not
+// depend on the order.
+constexpr int DX_FACETS = 32;
+constexpr int DX_THREADS = 512;
+constexpr int DX_LIST = 4096;   // (facet, sample) pairs per round of the filter
+
+struct DxFacet {
+  double Tx, Ty, Tz, Bx, By, Bz;   // sun frame (FP64, for sample_lit)
+  double mu;                       // cosine of the sun centre (FP64)
+  float4 fb, ft, fn;               // facet frame (FP32)
+  float Nx, Ny, Nz, Tfx, Tfy, Tfz, Bfx, Bfy, Bfz, kap;
+  int f, mesh, all_amb, count;
+};
+
+__device__ __forceinline__ int dx_classify(const StepView& v, const MeshDesc& M, const DxFacet& F, int s) {
   const float MT = 2e-5f, MP = 2e-5f;
-  for (int w = warp; w < nw; w += nwarps) {
-    int f = v.work[w];
-    const MeshDesc& M = v.md[v.mesh_of ? v.mesh_of[f] : 0];
-    const SunAux* S = mesh_sun(v, M);
-    d3 Sv = mkd(S->sx, S->sy, S->sz);
-    const float dphi = (float)M.dphi;
-    float4 c4 = v.cen[f];
-    d3 p = mkd((double)c4.x, (double)c4.y, (double)c4.z);
-    d3 SP = sub(Sv, p);
-    double dist = norm(SP);
-    d3 N = mkd(SP.x / dist, SP.y / dist, SP.z / dist);   // = geom.h normalise(S - p)
-    d3 T, B;
-    sun_frame(N, &T, &B);
-    frame3 BTN = load_frame(v.frame + 9 * (int64_t)f);
-    const double* h = v.H + M.H0 + (int64_t)(f - M.facet0) * M.nphi;
-    auto hl = [&](int k) { return h[k]; };
-    const float4* F4 = v.frame32 + 3 * (size_t)f;
-    float4 fb = F4[0], ft = F4[1], fn = F4[2];
-    float kap = (float)(SUN_RADIUS_KM / dist);
-    float Nx = (float)N.x, Ny = (float)N.y, Nz = (float)N.z;
-    float Tx = (float)T.x, Ty = (float)T.y, Tz = (float)T.z;
-    float Bx = (float)B.x, By = (float)B.y, Bz = (float)B.z;
-    int count = 0;
-    for (int s = lane; s < M.nsamp; s += 32) {
-      double x = v.disk[s], y = v.disk[v.ndisk + s];
-      float xf = kap * (float)x, yf = kap * (float)y;
-      float vx = Nx + (xf * Tx + yf * Bx), vy = Ny + (xf * Ty + yf * By), vz = Nz + (xf * Tz + yf * Bz);
-      float lx = (fb.x * vx + fb.y * vy) + fb.z * vz;
-      float ly = (ft.x * vx + ft.y * vy) + ft.z * vz;
-      float lz = (fn.x * vx + fn.y * vy) + fn.z * vz;
-      float th = atan2f(sqrtf(lx * lx + ly * ly), lz);
-      int lit = -1;
-      if (th > 0.05f) {
-        float ph = atan2f(ly, lx);
-        if (ph < 0.f) ph += 6.2831853f;
-        int k = (int)floorf(ph / dphi);
-        float edge = fminf(ph - (float)k * dphi, (float)(k + 1) * dphi - ph);
-        if (k >= 0 && k < M.nphi - 1 && edge > MP) {
-          float hk = (float)h[k];
-          float thr = M.interp == 0 ? hk + (ph - (float)k * dphi)
-                                    : hk + (ph - (float)k * dphi) / dphi * ((float)h[k + 1] - hk);
-          float dlt = th - thr;
-          if (dlt < -MT) lit = 1;
-          else if (dlt > MT) lit = 0;
-        }
-      }
-      if (lit < 0) {
-        d3 disk = add(Sv, scl(add(scl(T, x), scl(B, y)), SUN_RADIUS_KM));
-        lit = sample_lit(p, disk, BTN, hl, M.nphi, M.dphi, M.interp);
-      }
-      count += lit;
+  if (F.all_amb) return -1;
+  const float dphi = M.dphi32;
+  float xf = F.kap * v.disk32[s], yf = F.kap * v.disk32[v.ndisk + s];
+  float vx = F.Nx + (xf * F.Tfx + yf * F.Bfx), vy = F.Ny + (xf * F.Tfy + yf * F.Bfy),
+        vz = F.Nz + (xf * F.Tfz + yf * F.Bfz);
+  float lx = (F.fb.x * vx + F.fb.y * vy) + F.fb.z * vz;
+  float ly = (F.ft.x * vx + F.ft.y * vy) + F.ft.z * vz;
+  float lz = (F.fn.x * vx + F.fn.y * vy) + F.fn.z * vz;
+  float th = atan2f(sqrtf(lx * lx + ly * ly), lz);
+  if (th > 0.05f) {
+    float ph = atan2f(ly, lx);
+    if (ph < 0.f) ph += 6.2831853f;
+    int k = (int)floorf(ph / dphi);
+    float edge = fminf(ph - (float)k * dphi, (float)(k + 1) * dphi - ph);
+    if (k >= 0 && k < M.nphi - 1 && edge > MP) {
+      const float* h = v.H32 + M.H0 + (int64_t)(F.f - M.facet0) * M.nphi;
+      float hk = h[k];
+      float thr = M.interp == 0 ? hk + (ph - (float)k * dphi)
+                                : hk + (ph - (float)k * dphi) / dphi * (h[k + 1] - hk);
+      float dlt = th - thr;
+      if (dlt < -MT) return 1;
+      if (dlt > MT) return 0;
     }
-    for (int o = 16; o; o >>= 1) count += __shfl_xor_sync(0xffffffffu, count, o);
-    if (lane == 0) {
-      double dv = (double)count / M.denom;
-      double mu = sun_mu(Sv, p, BTN.n);
+  }
+  return -1;
+}
+
+// FP32 sun direction, frame and kappa of one facet; all_amb when the axis
+// choice of sun_frame is within rounding of a tie.
+__device__ __forceinline__ void dx_setup32(const StepView& v, DxFacet& F, int f) {
+  const MeshDesc& M = v.md[v.mesh_of ? v.mesh_of[f] : 0];
+  const SunAux* S = mesh_sun(v, M);
+  float4 c4 = v.cen[f];
+  float sx = (float)S->sx - c4.x, sy = (float)S->sy - c4.y, sz = (float)S->sz - c4.z;
+  float dist = sqrtf(sx * sx + sy * sy + sz * sz);
+  float nx = sx / dist, ny = sy / dist, nz = sz / dist;
+  float ax = fabsf(nx), ay = fabsf(ny), az = fabsf(nz);
+  const float TIE = 1e-5f;
+  F.all_amb = (fabsf(ax - ay) < TIE || fabsf(ax - az) < TIE || fabsf(ay - az) < TIE) ? 1 : 0;
+  float ex = 0.f, ey = 0.f, ez = 0.f;
+  if (ax <= ay && ax <= az) ex = 1.f;
+  else if (ay <= az) ey = 1.f;
+  else ez = 1.f;
+  float ne = nx * ex + ny * ey + nz * ez;
+  float tx = ex - nx * ne, ty = ey - ny * ne, tz = ez - nz * ne;
+  float tl = sqrtf(tx * tx + ty * ty + tz * tz);
+  tx /= tl; ty /= tl; tz /= tl;
+  F.Nx = nx; F.Ny = ny; F.Nz = nz;
+  F.Tfx = tx; F.Tfy = ty; F.Tfz = tz;
+  F.Bfx = ty * nz - tz * ny; F.Bfy = tz * nx - tx * nz; F.Bfz = tx * ny - ty * nx;   // T x N
+  F.kap = (float)SUN_RADIUS_KM / dist;
+  const float4* F4 = v.frame32 + 3 * (size_t)f;
+  F.fb = F4[0]; F.ft = F4[1]; F.fn = F4[2];
+  F.f = f;
+  F.mesh = v.mesh_of ? v.mesh_of[f] : 0;
+  F.count = 0;
+}
+
+__device__ __forceinline__ void dx_exact_sample(const StepView& v, DxFacet& F, int s) {
+  const MeshDesc& M = v.md[F.mesh];
+  const SunAux* S = mesh_sun(v, M);
+  d3 Sv = mkd(S->sx, S->sy, S->sz);
+  float4 c4 = v.cen[F.f];
+  d3 p = mkd((double)c4.x, (double)c4.y, (double)c4.z);
+  d3 T = mkd(F.Tx, F.Ty, F.Tz), B = mkd(F.Bx, F.By, F.Bz);
+  double x = v.disk[s], y = v.disk[v.ndisk + s];
+  d3 disk = add(Sv, scl(add(scl(T, x), scl(B, y)), SUN_RADIUS_KM));
+  frame3 BTN = load_frame(v.frame + 9 * (int64_t)F.f);
+  const double* h = v.H + M.H0 + (int64_t)(F.f - M.facet0) * M.nphi;
+  auto hl = [&](int k) { return h[k]; };
+  if (sample_lit(p, disk, BTN, hl, M.nphi, M.dphi, M.interp)) atomicAdd(&F.count, 1);
+}
+
+__global__ void __launch_bounds__(DX_THREADS) k_direct_exact(StepView v, int dropin) {
+  __shared__ DxFacet fs[DX_FACETS];
+  __shared__ int list[DX_LIST];
+  __shared__ int nlist;
+  const int nw = v.counters[0];
+  const int nsamp = v.ndisk - 1;   // samples per facet (the meshes of a view share the disk)
+  const int FT = DX_THREADS - 32;  // filter threads (warps 1..)
+  for (int base = blockIdx.x * DX_FACETS; base < nw; base += gridDim.x * DX_FACETS) {
+    const int nf = min(DX_FACETS, nw - base);
+    const int total = nf * nsamp;
+    if (threadIdx.x < 32) {
+      // FP64 set-up, one lane per facet (overlaps the filter below)
+      if (threadIdx.x < nf) {
+        DxFacet& F = fs[threadIdx.x];
+        int f = v.work[base + threadIdx.x];
+        const MeshDesc& M = v.md[v.mesh_of ? v.mesh_of[f] : 0];
+        const SunAux* S = mesh_sun(v, M);
+        float4 c4 = v.cen[f];
+        d3 p = mkd((double)c4.x, (double)c4.y, (double)c4.z);
+        d3 Sv = mkd(S->sx, S->sy, S->sz);
+        d3 SP = sub(Sv, p);
+        double dist = norm(SP);
+        d3 N = mkd(SP.x / dist, SP.y / dist, SP.z / dist);   // = geom.h normalise(S - p)
+        d3 T, B;
+        sun_frame(N, &T, &B);
+        F.Tx = T.x; F.Ty = T.y; F.Tz = T.z;
+        F.Bx = B.x; F.By = B.y; F.Bz = B.z;
+        const double* fr = v.frame + 9 * (int64_t)f;
+        F.mu = sun_mu(Sv, p, mkd(fr[6], fr[7], fr[8]));
+      }
+    } else {
+      if (threadIdx.x - 32 < nf) dx_setup32(v, fs[threadIdx.x - 32], v.work[base + threadIdx.x - 32]);
+      if (threadIdx.x == 32) nlist = 0;
+      asm volatile("bar.sync 1, %0;" ::"r"(FT));   // the filter warps only
+      const int q1 = min(total, DX_LIST);
+      for (int q = threadIdx.x - 32; q < q1; q += FT) {
+        const int j = q / nsamp, s = q - j * nsamp;
+        int lit = dx_classify(v, v.md[fs[j].mesh], fs[j], s);
+        if (lit == 1) atomicAdd(&fs[j].count, 1);
+        if (lit < 0) list[atomicAdd(&nlist, 1)] = q;
+      }
+    }
+    __syncthreads();
+    for (int q0 = 0;;) {
+      const int nl = nlist;
+      for (int a = threadIdx.x; a < nl; a += DX_THREADS) {
+        const int q = list[a];
+        const int j = q / nsamp;
+        dx_exact_sample(v, fs[j], q - j * nsamp);
+      }
+      q0 += DX_LIST;
+      if (q0 >= total) break;
+      // more pairs than one round holds (more than DX_LIST / DX_FACETS samples per facet)
+      __syncthreads();
+      if (threadIdx.x == 0) nlist = 0;
+      __syncthreads();
+      const int q1 = min(total, q0 + DX_LIST);
+      for (int q = q0 + threadIdx.x; q < q1; q += DX_THREADS) {
+        const int j = q / nsamp, s = q - j * nsamp;
+        int lit = dx_classify(v, v.md[fs[j].mesh], fs[j], s);
+        if (lit == 1) atomicAdd(&fs[j].count, 1);
+        if (lit < 0) list[atomicAdd(&nlist, 1) ] = q;
+      }
+      __syncthreads();
+    }
+    __syncthreads();
+    // the facet's flux, one thread per facet
+    if (threadIdx.x < nf) {
+      const DxFacet& F = fs[threadIdx.x];
+      const MeshDesc& M = v.md[F.mesh];
+      const SunAux* S = mesh_sun(v, M);
+      double dv = (double)F.count / M.denom;
+      double mu = F.mu;
       dv *= (mu > 0.0 ? mu : 0.0);
       dv *= S->flux;
-      store_direct(v, M, f, dv, dropin);
+      store_direct(v, M, F.f, dv, dropin);
     }
+    __syncthreads();
   }
 }
 
@@ -266,7 +379,7 @@ int direct_launch(const StepView& v, int dropin, cudaStream_t s) {
   ILG_CUDA(cudaMemsetAsync(v.counters, 0, sizeof(int), s));
   k_direct_classify<<<div_up(v.nt, 256), 256, 0, s>>>(v, dropin);
   ILG_CUDA(cudaGetLastError());
-  k_direct_exact<<<152 * 4, 256, 0, s>>>(v, dropin);
+  k_direct_exact<<<152 * 4, DX_THREADS, 0, s>>>(v, dropin);
   ILG_CUDA(cudaGetLastError());
   return ILG_OK;
 }

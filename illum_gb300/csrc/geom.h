@@ -11,7 +11,8 @@
 //                  default) and without -ffast-math;
 //   * no flush-to-zero (nvcc default without --use_fast_math).
 // Transcendentals (sin, cos, atan2, acos) are implemented here from their
-// Taylor / half-angle series instead of calling libm or CUDA's math library,
+// Taylor series (with quadrant reduction for sin / cos and a table of
+// atan(k/16) for atan2) instead of calling libm or CUDA's math library,
 // whose last-ulp results differ between platforms.
 //
 // Reference semantics mirrored (sampotter/illum, paths relative to its root):
@@ -128,28 +129,54 @@ ILG_HD void sincos_x(double x, double* s, double* c) {
   }
 }
 
-// atan(z) for z in [0, 1]: two half-angle reductions
-// atan(z) = 2 atan(z / (1 + sqrt(1 + z^2))) bring z below 0.199, then the
-// alternating series sum_k (-1)^k w^(2k+1)/(2k+1) to k = 13 (error < 1e-18).
-ILG_HD double atan01(double z) {
-  double w = z / (1.0 + sqrt(1.0 + z * z));
-  w = w / (1.0 + sqrt(1.0 + w * w));
-  double y = w * w;
-  double p = 0.037037037037037035;            //  1/27
-  p = -0.04 + y * p;                          // -1/25
-  p = 0.043478260869565216 + y * p;           //  1/23
-  p = -0.047619047619047616 + y * p;          // -1/21
-  p = 0.05263157894736842 + y * p;            //  1/19
-  p = -0.058823529411764705 + y * p;          // -1/17
-  p = 0.06666666666666667 + y * p;            //  1/15
-  p = -0.07692307692307693 + y * p;           // -1/13
-  p = 0.09090909090909091 + y * p;            //  1/11
-  p = -0.1111111111111111 + y * p;            // -1/9
-  p = 0.14285714285714285 + y * p;            //  1/7
-  p = -0.2 + y * p;                           // -1/5
-  p = 0.3333333333333333 + y * p;             //  1/3
-  double a = w - (w * y) * p;
-  return 4.0 * a;
+// atan(k/16), k = 0..16, correctly rounded (computed to 60 digits).
+ILG_HD double atan_tab16(int k) {
+  switch (k) {
+    case 0: return 0.0;
+    case 1: return 0.06241880999595735;
+    case 2: return 0.12435499454676144;
+    case 3: return 0.18534794999569476;
+    case 4: return 0.24497866312686414;
+    case 5: return 0.3028848683749714;
+    case 6: return 0.35877067027057225;
+    case 7: return 0.4124104415973873;
+    case 8: return 0.4636476090008061;
+    case 9: return 0.5123894603107377;
+    case 10: return 0.5585993153435624;
+    case 11: return 0.6022873461349642;
+    case 12: return 0.6435011087932844;
+    case 13: return 0.6823165548747481;
+    case 14: return 0.7188299996216245;
+    case 15: return 0.7531512809621944;
+    default: return 0.7853981633974483;
+  }
+}
+
+// atan(n / d) for 0 <= n <= d, d > 0, by a table reduction:
+// atan(n/d) = atan(c) + atan(u), c = k/16 near n/d (k from an fp32 estimate,
+// correctly rounded on every IEEE platform, so CPU and GPU pick the same k),
+// u = (n - c d) / (d + c n), |u| <= ~1/32, and the series
+// atan(u) = u + u y (-1/3 + y/5 - y^2/7 + y^3/9 - y^4/11 + y^5/13), y = u^2,
+// evaluated in Estrin form (truncation < 1e-19 relative). One division and a
+// short dependent chain: the FP64 pipe of the GPU is slow per instruction.
+ILG_HD double atan_ratio(double n, double d) {
+  if (d < 7.888609052210118e-31) {   // 2^-100: keep the fp32 estimate in range (exact scaling)
+    n *= 1.6069380442589903e60;      // 2^200
+    d *= 1.6069380442589903e60;
+  }
+  float rf = (float)n / (float)d;
+  int k = (int)(rf * 16.0f + 0.5f);
+  if (k < 0) k = 0;
+  if (k > 16) k = 16;
+  double c = (double)k * 0.0625;
+  double u = (n - c * d) / (d + c * n);
+  double y = u * u;
+  double y2 = y * y;
+  double p01 = -0.3333333333333333 + 0.2 * y;
+  double p23 = -0.14285714285714285 + 0.1111111111111111 * y;
+  double p45 = -0.09090909090909091 + 0.07692307692307693 * y;
+  double p = p01 + y2 * (p23 + y2 * p45);
+  return atan_tab16(k) + (u + (u * y) * p);
 }
 
 // atan2 with the usual quadrant conventions; atan2(0, 0) = 0.
@@ -157,8 +184,7 @@ ILG_HD double atan2_x(double y, double x) {
   double ax = fabs(x), ay = fabs(y);
   if (ax == 0.0 && ay == 0.0) return 0.0;
   bool swap = ay > ax;
-  double z = swap ? ax / ay : ay / ax;
-  double a = atan01(z);
+  double a = swap ? atan_ratio(ax, ay) : atan_ratio(ay, ax);
   if (swap) a = HALF_PI - a;
   if (x < 0.0) a = PI - a;
   return (y < 0.0) ? -a : a;
@@ -364,17 +390,24 @@ ILG_HD double sun_mu(d3 S, d3 p, d3 n) {
 // direction lies above the horizon. h points at the facet's nphi horizon
 // zenith angles. interp = 0 keeps the reference's threshold
 // h[k] + t*dphi; interp = 1 interpolates h[k] .. h[k+1] linearly.
+//
+// The reference takes acos of the normalised direction's z; with the
+// orthonormal frame the same angles come from the unnormalised direction,
+// theta = atan2(|(x, y)|, z) and phi = atan2(y, x), which drops the
+// normalisation's square root and three divisions from the dependent chain
+// (FP64 latency dominates this test on the GPU). The bin and its fraction
+// come from one division, q = phi / dphi.
 template <class HLoad>
 ILG_HD int sample_lit(d3 p, d3 disk, const frame3& BTN, HLoad h, int nphi, double dphi, int interp) {
-  d3 n_sun = normalise(sub(disk, p));
-  d3 dir = frame_apply_t(BTN, n_sun);
-  double theta = acos_x(dir.z);
+  d3 dir = frame_apply_t(BTN, sub(disk, p));
+  double theta = atan2_x(sqrt(dir.x * dir.x + dir.y * dir.y), dir.z);
   double phi = atan2_x(dir.y, dir.x);
   if (phi < 0.0) phi += TWO_PI;
-  int k = (int)floor(phi / dphi);
+  double q = phi / dphi;
+  int k = (int)floor(q);
   if (k < 0) k = 0;
   if (k > nphi - 1) k = nphi - 1;
-  double t = (phi - (double)k * dphi) / dphi;
+  double t = q - (double)k;
   double thr;
   if (interp == 0) {
     thr = h(k) + t * dphi;

@@ -74,7 +74,9 @@ struct MeshDesc {
   int nphi, interp;
   int64_t H0;                  // offset of the mesh's horizons (nphi per facet)
   double dphi, denom;          // azimuth step; lit-count divisor
+  double lit_all;              // nsamp / denom (every sample lit), as the device would divide
   int nsamp, coupling;         // sun-disk samples used; ILG_COUPLE_*
+  float dphi32;                // fp32 copy of dphi
   int sun0, nsun;              // the mesh's sun table in the scene's table
   int sun_idx, frame;          // current sun index and frame (advanced per step)
   int host_sun, host_slot;     // 1: take the sun from host_slot (host-driven steps)
@@ -96,7 +98,10 @@ struct StepView {
   MeshDesc* md;
   const int* mesh_of;          // per facet, or nullptr for a single mesh
   const float4 *cen, *nrm, *frame32;
-  const double *frame, *H, *hmin, *hmax, *disk;
+  const double *frame, *H, *disk;
+  const float* H32;            // fp32 copy of H
+  const float2* hmm32;         // per facet: fp32 min and max of its horizon
+  const float* disk32;         // fp32 copy of the disk samples
   int ndisk;
   const SunAux* suns;
   double *Tsurf, *Fsurf, *Qprev, *rad, *rad_avg, *therm_avg, *therm_max, *E, *xprev;
@@ -148,7 +153,8 @@ struct Context {
   int nphi = 0;
   double dphi = 0.0;
   dbuf<double> H;
-  dbuf<double> hmin, hmax;  // per facet: min_k H, max_k H
+  dbuf<float> H32;          // fp32 copy (the insolation filters run in fp32)
+  dbuf<float2> hmm32;       // per facet: (min_k H, max_k H) in fp32
 
   // insolation options
   int norm_mode = 0, interp = 0;
@@ -201,6 +207,7 @@ struct Context {
   int nsun = 0;
   std::vector<double> suns_h;     // nsun x 3 positions (to rebuild the table)
   dbuf<double> disk;              // ndisk x 2 column-major
+  dbuf<float> disk32;
   int ndisk = 0;
   double disk_rmax = 0.0;
   dbuf<int> work;                 // ambiguous facets
@@ -246,6 +253,7 @@ int bvh_build(Context& c, const float* verts_h, int nv, const int32_t* tris_h, c
 int bvh_trace(Context& c, int nrays, const float* orig_h, const float* dir_h, int any_hit, int32_t* hit_h,
               double* t_h);
 int horizons_build(Context& c, int nphi, double theta_eps, double offset);
+int horizons_f32(Context& c);   // H32 and hmm32 from H
 int form_factors_build(Context& c, const double* albedo_h, double albedo_scalar, double offset,
                        int64_t* rays_out);
 
