@@ -146,7 +146,7 @@ static int build(Batch& b) {
   for (dbuf<double>* d : {&b.Tsurf, &b.Fsurf, &b.Qprev, &b.rad, &b.rad_avg, &b.therm_avg, &b.therm_max, &b.E,
                           &b.xprev})
     ILG_TRY(d->alloc(nt));
-  ILG_TRY(b.xtmp.alloc(5 * nt));
+  ILG_TRY(b.xtmp.alloc(6 * nt));
   ILG_TRY(b.rperm.alloc(nt));
   if (mixed) {
     ILG_TRY(b.x32.alloc(3 * nt));

@@ -206,7 +206,7 @@ static int upload_desc(Context& c, const MeshDesc& M) {
 static int ensure_step_buffers(Context& c, int precision) {
   ILG_TRY(c.E.reserve(c.nt));
   ILG_TRY(c.Q.reserve(c.nt));
-  ILG_TRY(c.xtmp.reserve((size_t)5 * c.nt));   // radiosity E, two iterates, their double-float copies
+  ILG_TRY(c.xtmp.reserve((size_t)6 * c.nt));   // radiosity E, two iterates, double-float copies of both and of E
   if (c.xprev.n < (size_t)c.nt) {
     ILG_TRY(c.xprev.alloc(c.nt));
     ILG_CUDA(cudaMemset(c.xprev.p, 0, (size_t)c.nt * 8));

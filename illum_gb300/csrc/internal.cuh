@@ -123,7 +123,7 @@ struct StepView {
   double* tile_d2;             // 2 x ntiles residual partials
   const uint8_t* row_act;      // per facet: its row has entries
   const uint32_t* rperm;       // radiosity position -> facet (Morton order within each mesh)
-  double* rbuf;                // 5 x nt: E, two iterates, their double-float copies (radiosity positions)
+  double* rbuf;                // 6 x nt: E, two iterates, double-float copies of both and of E (radiosity positions)
   // conduction blocks: (mesh, first local facet), or nullptr for a single mesh
   const int2* cblocks;
   int ncblocks;

@@ -55,6 +55,7 @@ constexpr int RAD_HALO = 16384;          // halo values per tile (double-float: 
 constexpr int RAD_ROWS = 6144;           // rows per tile (their sums: 48 KB of shared memory)
 constexpr int RAD_MAX_MESH = 1024;
 constexpr int64_t RAD_MIN_TILE = 16384;  // entries: smaller tiles cost more in staging than they balance
+constexpr int64_t RAD_ROW_COST = 32;     // a row's finishing work, in entries (tile balance)
 constexpr size_t RAD_SMEM =
     (size_t)RAD_HALO * sizeof(float2) + RAD_THREADS * sizeof(float2) + RAD_ROWS * sizeof(float2) + RAD_THREADS;
 
@@ -168,6 +169,17 @@ struct AccDF {
 };
 
 __device__ __forceinline__ double df_value(float2 s) { return (double)s.x + (double)s.y; }
+
+// Double-float sum a + b (TwoSum of the high parts, then renormalised),
+// FP32 operations only.
+__device__ __forceinline__ float2 df_add(float2 a, float2 b) {
+  float s = __fadd_rn(a.x, b.x);
+  float bb = __fsub_rn(s, a.x);
+  float e = __fadd_rn(__fsub_rn(a.x, __fsub_rn(s, bb)), __fsub_rn(b.x, bb));
+  e = __fadd_rn(e, __fadd_rn(a.y, b.y));
+  float t = __fadd_rn(s, e);
+  return make_float2(t, __fsub_rn(e, __fsub_rn(t, s)));
+}
 
 // Plain fp32 sum (mixed inner sweeps: bf16 values, fp32 iterates).
 struct AccF32 {
@@ -363,8 +375,9 @@ __device__ __forceinline__ int decide_meshes(const StepView& v, MeshState& st, i
 }
 
 // The solve works on radiosity positions (Morton order within each mesh):
-// EP = E, P0 / P1 = iterates, gathered through rperm at entry, and H0 / H1
-// the iterates' double-float copies (what the halos gather). Start values:
+// EP = E, P0 / P1 = iterates, gathered through rperm at entry, H0 / H1 the
+// iterates' double-float copies (what the halos gather) and EH = E as a
+// double-float (the copies are updated in FP32 arithmetic). Start values:
 // rows without entries are x = E exactly; the others start at E (cold) or
 // at the mesh's previous solution, extrapolated linearly once two solutions
 // exist (warm).
@@ -374,6 +387,7 @@ __device__ __forceinline__ void init_x(const StepView& v, const double* x, int w
   double* P1 = v.rbuf + 2 * (size_t)v.nt;
   float2* H0 = reinterpret_cast<float2*>(v.rbuf + 3 * (size_t)v.nt);
   float2* H1 = H0 + v.nt;
+  float2* EH = H1 + v.nt;
   for (int p = gt; p < v.nt; p += nthreads) {
     int g = (int)v.rperm[p];
     const MeshDesc& M = v.md[mesh_of_facet(v, g)];
@@ -390,6 +404,7 @@ __device__ __forceinline__ void init_x(const StepView& v, const double* x, int w
     P1[p] = e;
     H0[p] = split_df(x0);
     H1[p] = split_df(e);
+    EH[p] = H1[p];
     if (v.x32) {
       v.x32[p] = 0.f;
       v.x32[v.nt + p] = 0.f;
@@ -444,6 +459,7 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity64(StepView v, doub
   double* nxt = v.rbuf + 2 * (size_t)v.nt;
   float2* curh = reinterpret_cast<float2*>(v.rbuf + 3 * (size_t)v.nt);
   float2* nxth = curh + v.nt;
+  const float2* EH = nxth + v.nt;
   for (int par = 0;; par ^= 1) {
     for (int t = blockIdx.x; t < v.ntiles; t += gridDim.x) {
       const RowTile T = v.tiles[t];
@@ -454,10 +470,11 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity64(StepView v, doub
       double d2 = 0.0;
       for (int r = threadIdx.x; r < T.nrows; r += RAD_THREADS) {
         uint32_t i = __ldg(rows + r);
-        double xn = __ldg(EP + i) + df_value(sm.rs[r]);
+        const float2 sr = sm.rs[r];
+        double xn = __ldg(EP + i) + df_value(sr);
         double df = xn - ld_it(cur + i);
         nxt[i] = xn;
-        nxth[i] = split_df(xn);
+        nxth[i] = df_add(__ldg(EH + i), sr);
         d2 += df * df;
       }
       block_sum_store(d2, red, v.tile_d2 + (size_t)par * v.ntiles + t);
@@ -539,9 +556,9 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity_mixed(StepView v, 
       const uint32_t* rows = v.t_row + T.r0;
       for (int r = threadIdx.x; r < T.nrows; r += RAD_THREADS) {
         uint32_t i = __ldg(rows + r);
-        double xi = X[i] + (double)ld_it(cur + i);
-        X[i] = xi;
-        XH[i] = split_df(xi);
+        const float d = ld_it(cur + i);
+        X[i] = ld_it(X + i) + (double)d;
+        XH[i] = df_add(ld_it(XH + i), make_float2(d, 0.f));
       }
     }
     if (!grid_barrier(v.barrier, gridDim.x, v.derr)) return;
@@ -677,20 +694,22 @@ int radiosity_prepare(Context& c) {
   }
   c.n_active = (int)arow.size();
 
-  // tile cuts: cumulative entry targets, halo cap
+  // tile cuts: equal shares of the estimated work (entries + RAD_ROW_COST
+  // per row), halo and row caps
   const int G = g_rad_nsm * std::min(g_rad_per_sm64, g_rad_per_smm);
   int64_t ntarget = std::max<int64_t>(1, std::min<int64_t>(G, (nnz + RAD_MIN_TILE - 1) / RAD_MIN_TILE));
+  const int64_t total_cost = nnz + RAD_ROW_COST * (int64_t)arow.size();
   std::vector<int> stamp((size_t)nt, -1);
   std::vector<int> loc((size_t)nt, 0);
   std::vector<RowTile> tiles;
   std::vector<uint16_t> cf;
   std::vector<uint32_t> esrc, efac, trow, thalo, tstart;
-  int64_t done_entries = 0;
+  int64_t done_cost = 0;
   size_t a = 0;
   while (a < arow.size()) {
     // rows [a, b) form the next tile
     const int tid = (int)tiles.size();
-    int64_t bound = (int64_t)((double)nnz * (double)(tid + 1) / (double)ntarget);
+    int64_t bound = (int64_t)((double)total_cost * (double)(tid + 1) / (double)ntarget);
     int nhalo = 0;
     size_t b = a;
     int64_t ne = 0;
@@ -708,7 +727,7 @@ int radiosity_prepare(Context& c) {
       nhalo += fresh;
       ne += rp[g + 1] - rp[g];
       ++b;
-      if (done_entries + ne >= bound && tid + 1 < ntarget) break;
+      if (done_cost + ne + RAD_ROW_COST * (int64_t)(b - a) >= bound && tid + 1 < ntarget) break;
     }
     std::sort(halo.begin(), halo.end());
     for (int h = 0; h < (int)halo.size(); ++h) loc[halo[h]] = h;
@@ -747,7 +766,7 @@ int radiosity_prepare(Context& c) {
     }
     thalo.insert(thalo.end(), halo.begin(), halo.end());
     tiles.push_back(T);
-    done_entries += ne;
+    done_cost += ne + RAD_ROW_COST * (int64_t)(b - a);
     a = b;
   }
   c.ntiles = (int)tiles.size();
