@@ -58,7 +58,7 @@ struct Batch {
   dbuf<float> H32, disk32;
   dbuf<float2> hmm32;
   dbuf<SunAux> suns;
-  dbuf<double> Tsurf, Fsurf, Qprev, rad, rad_avg, therm_avg, therm_max, E, xtmp, xprev;
+  dbuf<double> Tsurf, Fsurf, Qprev, rad, rad_avg, therm_avg, therm_max, E, xtmp, sprev;
   dbuf<float> x32;
   dbuf<float2> Tdf, coefdf;
   dbuf<float> T32, coef32;
@@ -143,9 +143,9 @@ static int build(Batch& b) {
   ILG_TRY(b.disk.alloc(2 * (size_t)ndisk));
   ILG_TRY(b.disk32.alloc(2 * (size_t)ndisk));
   ILG_TRY(b.suns.alloc(nsun));
-  for (dbuf<double>* d : {&b.Tsurf, &b.Fsurf, &b.Qprev, &b.rad, &b.rad_avg, &b.therm_avg, &b.therm_max, &b.E,
-                          &b.xprev})
+  for (dbuf<double>* d : {&b.Tsurf, &b.Fsurf, &b.Qprev, &b.rad, &b.rad_avg, &b.therm_avg, &b.therm_max, &b.E})
     ILG_TRY(d->alloc(nt));
+  ILG_TRY(b.sprev.alloc(2 * nt));
   ILG_TRY(b.xtmp.alloc(6 * nt));
   ILG_TRY(b.rperm.alloc(nt));
   if (mixed) {
@@ -212,7 +212,8 @@ static int build(Batch& b) {
     ILG_TRY(cat(b.rad_avg, f0, c.rad_avg.p, N, s));
     ILG_TRY(cat(b.therm_avg, f0, c.therm_avg.p, N, s));
     ILG_TRY(cat(b.therm_max, f0, c.therm_max.p, N, s));
-    ILG_TRY(cat(b.xprev, f0, c.xprev.p, N, s));
+    ILG_TRY(cat(b.sprev, f0, c.sprev.p, N, s));
+    ILG_TRY(cat(b.sprev, (size_t)nt + f0, c.sprev.p + N, N, s));
     if (mixed) {
       ILG_TRY(cat(b.T32, (size_t)M.T0, c.T32.p, N * c.nz, s));
       ILG_TRY(cat(b.coef32, (size_t)M.coef0, c.coef32.p, (size_t)c.nz * 5, s));
@@ -263,7 +264,7 @@ static int build(Batch& b) {
   v.H32 = b.H32.p; v.hmm32 = b.hmm32.p; v.disk = b.disk.p; v.disk32 = b.disk32.p; v.ndisk = ndisk;
   v.suns = b.suns.p;
   v.Tsurf = b.Tsurf.p; v.Fsurf = b.Fsurf.p; v.Qprev = b.Qprev.p; v.rad = b.rad.p; v.rad_avg = b.rad_avg.p;
-  v.therm_avg = b.therm_avg.p; v.therm_max = b.therm_max.p; v.E = b.E.p; v.xprev = b.xprev.p;
+  v.therm_avg = b.therm_avg.p; v.therm_max = b.therm_max.p; v.E = b.E.p; v.sprev = b.sprev.p;
   v.x32 = b.x32.p; v.Tdf = b.Tdf.p; v.T32 = b.T32.p; v.coefdf = b.coefdf.p; v.coef32 = b.coef32.p;
   v.tiles = b.tiles.p; v.ntiles = b.ntiles;
   v.t_cf = b.t_cf.p; v.t_val = b.t_val.p; v.t_vbf = b.t_vbf.p;
@@ -447,7 +448,8 @@ int ilg_batch_sync(ilg_batch* batch) {
     ILG_CUDA(cudaMemcpyAsync(c.rad_avg.p, b.rad_avg.p + f0, bytes, cudaMemcpyDeviceToDevice, s));
     ILG_CUDA(cudaMemcpyAsync(c.therm_avg.p, b.therm_avg.p + f0, bytes, cudaMemcpyDeviceToDevice, s));
     ILG_CUDA(cudaMemcpyAsync(c.therm_max.p, b.therm_max.p + f0, bytes, cudaMemcpyDeviceToDevice, s));
-    ILG_CUDA(cudaMemcpyAsync(c.xprev.p, b.xprev.p + f0, bytes, cudaMemcpyDeviceToDevice, s));
+    ILG_CUDA(cudaMemcpyAsync(c.sprev.p, b.sprev.p + f0, bytes, cudaMemcpyDeviceToDevice, s));
+    ILG_CUDA(cudaMemcpyAsync(c.sprev.p + N, b.sprev.p + (size_t)b.nt + f0, bytes, cudaMemcpyDeviceToDevice, s));
     if (mixed)
       ILG_CUDA(cudaMemcpyAsync(c.T32.p, b.T32.p + M.T0, N * c.nz * 4, cudaMemcpyDeviceToDevice, s));
     else

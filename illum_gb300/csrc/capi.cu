@@ -145,7 +145,7 @@ static StepView solo_view(Context& c, int precision) {
   v.ndisk = c.ndisk;
   v.suns = c.sun_aux.p;
   v.Tsurf = c.Tsurf.p; v.Fsurf = c.Fsurf.p; v.Qprev = c.Qprev.p; v.rad = c.rad.p; v.rad_avg = c.rad_avg.p;
-  v.therm_avg = c.therm_avg.p; v.therm_max = c.therm_max.p; v.E = c.E.p; v.xprev = c.xprev.p;
+  v.therm_avg = c.therm_avg.p; v.therm_max = c.therm_max.p; v.E = c.E.p; v.sprev = c.sprev.p;
   v.x32 = c.x32.p;
   v.T64 = nullptr; v.Tdf = c.Tdf.p; v.T32 = c.T32.p;
   v.coef64 = nullptr; v.coefdf = c.coefdf.p; v.coef32 = c.coef32.p;
@@ -207,9 +207,9 @@ static int ensure_step_buffers(Context& c, int precision) {
   ILG_TRY(c.E.reserve(c.nt));
   ILG_TRY(c.Q.reserve(c.nt));
   ILG_TRY(c.xtmp.reserve((size_t)6 * c.nt));   // radiosity E, two iterates, double-float copies of both and of E
-  if (c.xprev.n < (size_t)c.nt) {
-    ILG_TRY(c.xprev.alloc(c.nt));
-    ILG_CUDA(cudaMemset(c.xprev.p, 0, (size_t)c.nt * 8));
+  if (c.sprev.n < 2 * (size_t)c.nt) {
+    ILG_TRY(c.sprev.alloc(2 * (size_t)c.nt));
+    ILG_CUDA(cudaMemset(c.sprev.p, 0, 2 * (size_t)c.nt * 8));
   }
   if (precision == ILG_PREC_MIXED) ILG_TRY(c.x32.reserve((size_t)3 * c.nt));
   ILG_TRY(c.md.reserve(1));
@@ -575,7 +575,7 @@ int ilg_thermal_init(ilg_ctx* ctx, int nz, const double* z, const double* ti, co
   for (double* p : {c.Fsurf.p, c.Qprev.p, c.rad.p, c.rad_avg.p, c.therm_avg.p, c.therm_max.p})
     ILG_CUDA(cudaMemsetAsync(p, 0, (size_t)nt * 8, c.stream));
   ILG_CUDA(cudaMemsetAsync(c.counters.p, 0, 8 * sizeof(int), c.stream));
-  if (c.xprev.p) ILG_CUDA(cudaMemsetAsync(c.xprev.p, 0, c.xprev.n * 8, c.stream));
+  if (c.sprev.p) ILG_CUDA(cudaMemsetAsync(c.sprev.p, 0, c.sprev.n * 8, c.stream));
   invalidate_graph(c);
   ILG_CUDA(cudaStreamSynchronize(c.stream));
   c.state_prec = ILG_PREC_FP64;

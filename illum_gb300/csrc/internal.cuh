@@ -104,7 +104,8 @@ struct StepView {
   const float* disk32;         // fp32 copy of the disk samples
   int ndisk;
   const SunAux* suns;
-  double *Tsurf, *Fsurf, *Qprev, *rad, *rad_avg, *therm_avg, *therm_max, *E, *xprev;
+  double *Tsurf, *Fsurf, *Qprev, *rad, *rad_avg, *therm_avg, *therm_max, *E;
+  double* sprev;               // 2 x nt: scattered radiosity x - E of the last solve, and its change
   float* x32;                  // 3 x nt (mixed radiosity)
   double* T64;                 // [nz][nt] fp64 layers (standalone column entry points)
   float2* Tdf;                 // [nz][nt] double-float layers (the FP64 step)
@@ -200,7 +201,7 @@ struct Context {
   int state_prec = 0;             // which of Tdf / T32 holds the state
   dbuf<double> Tsurf, Fsurf, Qprev;
   dbuf<double> rad, rad_avg, therm_avg, therm_max, E, xtmp, Q;
-  dbuf<double> xprev;             // radiosity solution of the step before
+  dbuf<double> sprev;             // 2 x N: x - E of the last radiosity solve, and its change
   int frame_no = 0;
 
   // suns and step machinery

@@ -380,7 +380,11 @@ __device__ __forceinline__ int decide_meshes(const StepView& v, MeshState& st, i
 // double-float (the copies are updated in FP32 arithmetic). Start values:
 // rows without entries are x = E exactly; the others start at E (cold) or
 // at the mesh's previous solution, extrapolated linearly once two solutions
-// exist (warm).
+// exist (warm). The warm start predicts the scattered part S = x - E and
+// takes the step's own E: x0 = E + S(n) + (S(n) - S(n-1)). E jumps where
+// a facet enters or leaves shadow; S = F x varies smoothly, so the start is
+// off by about F dE there instead of dE. sprev holds S(n) and, after it,
+// its last change.
 __device__ __forceinline__ void init_x(const StepView& v, const double* x, int warm, int gt, int nthreads) {
   double* EP = v.rbuf;
   double* P0 = v.rbuf + v.nt;
@@ -394,10 +398,9 @@ __device__ __forceinline__ void init_x(const StepView& v, const double* x, int w
     if (!M.active || M.ntiles == 0) continue;
     double e = v.E[g];
     double x0 = e;
-    if (warm && v.row_act[g]) {
-      double xn = x[g];
-      x0 = M.frame >= 2 ? 2.0 * xn - v.xprev[g] : xn;
-      v.xprev[g] = xn;
+    if (warm && v.row_act[g] && M.frame >= 1) {
+      x0 = e + v.sprev[g];
+      if (M.frame >= 2) x0 += v.sprev[v.nt + g];
     }
     EP[p] = e;
     P0[p] = x0;
@@ -412,9 +415,11 @@ __device__ __forceinline__ void init_x(const StepView& v, const double* x, int w
   }
 }
 
-// Scatter the solved meshes' last iterate back to facet order.
-__device__ __forceinline__ void scatter_x(const StepView& v, const MeshState& st, double* x, int gt, int nthreads,
-                                          bool mixed) {
+// Scatter the solved meshes' last iterate back to facet order; warm solves
+// also record S = x - E and its change for the next step's start.
+__device__ __forceinline__ void scatter_x(const StepView& v, const MeshState& st, double* x, int warm, int gt,
+                                          int nthreads, bool mixed) {
+  const double* EP = v.rbuf;
   const double* P0 = v.rbuf + v.nt;
   const double* P1 = v.rbuf + 2 * (size_t)v.nt;
   for (int p = gt; p < v.nt; p += nthreads) {
@@ -422,7 +427,13 @@ __device__ __forceinline__ void scatter_x(const StepView& v, const MeshState& st
     int m = mesh_of_facet(v, g);
     const MeshDesc& M = v.md[m];
     if (!M.active || M.ntiles == 0) continue;
-    x[g] = (!mixed && (st.sweeps[m] & 1)) ? ld_it(P1 + p) : ld_it(P0 + p);
+    double xs = (!mixed && (st.sweeps[m] & 1)) ? ld_it(P1 + p) : ld_it(P0 + p);
+    x[g] = xs;
+    if (warm) {
+      double s = xs - EP[p];
+      v.sprev[v.nt + g] = s - v.sprev[g];
+      v.sprev[g] = s;
+    }
   }
 }
 
@@ -484,7 +495,7 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity64(StepView v, doub
     float2* tmph = curh; curh = nxth; nxth = tmph;
     if (decide_meshes(v, st, 1, 0, par) == 0) break;
   }
-  scatter_x(v, st, x, gt, nthreads, false);
+  scatter_x(v, st, x, warm, gt, nthreads, false);
 }
 
 // Mixed precision: outer refinement with an fp64 residual r = E - (I - F) x
@@ -563,7 +574,7 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity_mixed(StepView v, 
     }
     if (!grid_barrier(v.barrier, gridDim.x, v.derr)) return;
   }
-  scatter_x(v, st, x, gt, nthreads, true);
+  scatter_x(v, st, x, warm, gt, nthreads, true);
 }
 
 // Per-row fp32 scale = max |F_ij| of the row (the bf16 copy stores F/scale).
