@@ -32,6 +32,8 @@ Context::~Context() {
     if (e) cudaEventDestroy(e);
   if (pinned_aux) cudaFreeHost(pinned_aux);
   if (pinned_tsurf) cudaFreeHost(pinned_tsurf);
+  for (cudaEvent_t e : slot_ev)
+    if (e) cudaEventDestroy(e);
   if (stream) cudaStreamDestroy(stream);
 }
 
@@ -71,7 +73,9 @@ static int set_disk(Context& c, const double* disk_xy, int ndisk) {
 
 static void invalidate_graph(Context& c) {
   if (c.graph) cudaGraphExecDestroy(c.graph);
+  if (c.graph_b) cudaGraphExecDestroy(c.graph_b);
   c.graph = nullptr;
+  c.graph_b = nullptr;
   for (int& k : c.graph_key) k = -1;
 }
 
@@ -127,8 +131,10 @@ int enqueue_step(const StepView& v, const StepPlan& p, cudaStream_t s, cudaEvent
 }
 
 static int ensure_pinned(Context& c) {
-  if (!c.pinned_aux) ILG_CUDA(cudaMallocHost((void**)&c.pinned_aux, sizeof(SunAux)));
-  if (!c.pinned_tsurf) ILG_CUDA(cudaMallocHost((void**)&c.pinned_tsurf, (size_t)c.nt * 8));
+  if (!c.pinned_aux) ILG_CUDA(cudaMallocHost((void**)&c.pinned_aux, 2 * sizeof(SunAux)));
+  if (!c.pinned_tsurf) ILG_CUDA(cudaMallocHost((void**)&c.pinned_tsurf, 2 * (size_t)c.nt * 8));
+  for (cudaEvent_t& e : c.slot_ev)
+    if (!e) ILG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   return ILG_OK;
 }
 
@@ -246,25 +252,23 @@ static StepPlan solo_plan(Context& c, const ilg_run_opts& o) {
   return p;
 }
 
-// Graph of one step. with_copies adds the host sun upload before and the
-// surface-temperature download after the step (host-driven steps).
-static int get_graph(Context& c, const ilg_run_opts& o, bool with_copies, cudaGraphExec_t* out) {
-  int key[4] = {o.precision * 4 + o.coupling * 2 + (o.use_radiosity ? 1 : 0), with_copies ? 1 : 0, c.nz,
-                c.ntiles};
-  if (c.graph && std::equal(key, key + 4, c.graph_key)) { *out = c.graph; return ILG_OK; }
-  invalidate_graph(c);
+// Captures one step; slot >= 0 adds the host sun upload from pinned slot
+// `slot` before and the surface-temperature download into that slot after
+// the step (host-driven steps).
+static int capture_step(Context& c, const ilg_run_opts& o, int slot, cudaGraphExec_t* out) {
   StepView v = solo_view(c, o.precision);
   StepPlan p = solo_plan(c, o);
   cudaGraph_t g;
   ILG_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
   int rc = ILG_OK;
-  if (with_copies)
-    if (cudaMemcpyAsync(c.sun_aux.p + c.nsun, c.pinned_aux, sizeof(SunAux), cudaMemcpyHostToDevice, c.stream) !=
-        cudaSuccess)
+  if (slot >= 0)
+    if (cudaMemcpyAsync(c.sun_aux.p + c.nsun, c.pinned_aux + slot * sizeof(SunAux), sizeof(SunAux),
+                        cudaMemcpyHostToDevice, c.stream) != cudaSuccess)
       rc = ILG_ERR_CUDA;
   if (rc == ILG_OK) rc = enqueue_step(v, p, c.stream, nullptr);
-  if (rc == ILG_OK && with_copies)
-    if (cudaMemcpyAsync(c.pinned_tsurf, c.Tsurf.p, (size_t)c.nt * 8, cudaMemcpyDeviceToHost, c.stream) != cudaSuccess)
+  if (rc == ILG_OK && slot >= 0)
+    if (cudaMemcpyAsync(c.pinned_tsurf + (size_t)slot * c.nt, c.Tsurf.p, (size_t)c.nt * 8, cudaMemcpyDeviceToHost,
+                        c.stream) != cudaSuccess)
       rc = ILG_ERR_CUDA;
   cudaError_t e = cudaStreamEndCapture(c.stream, &g);
   if (rc != ILG_OK || e != cudaSuccess) {
@@ -273,15 +277,35 @@ static int get_graph(Context& c, const ilg_run_opts& o, bool with_copies, cudaGr
     set_error("step capture failed: %s", cudaGetErrorString(e));
     return rc != ILG_OK ? rc : ILG_ERR_CUDA;
   }
-  cudaError_t ei = cudaGraphInstantiate(&c.graph, g, 0);
+  cudaError_t ei = cudaGraphInstantiate(out, g, 0);
   cudaGraphDestroy(g);
   if (ei != cudaSuccess) {
-    c.graph = nullptr;
+    *out = nullptr;
     set_error("graph instantiation failed: %s", cudaGetErrorString(ei));
     return ILG_ERR_CUDA;
   }
+  return ILG_OK;
+}
+
+// Graph of one step (with_copies: the two host-driven slot graphs, out[0]
+// and out[1]; otherwise out[0] only).
+static int get_graph(Context& c, const ilg_run_opts& o, bool with_copies, cudaGraphExec_t* out) {
+  int key[4] = {o.precision * 4 + o.coupling * 2 + (o.use_radiosity ? 1 : 0), with_copies ? 1 : 0, c.nz,
+                c.ntiles};
+  if (c.graph && std::equal(key, key + 4, c.graph_key)) {
+    out[0] = c.graph;
+    if (with_copies) out[1] = c.graph_b;
+    return ILG_OK;
+  }
+  invalidate_graph(c);
+  ILG_TRY(capture_step(c, o, with_copies ? 0 : -1, &c.graph));
+  if (with_copies) {
+    int rc = capture_step(c, o, 1, &c.graph_b);
+    if (rc != ILG_OK) { invalidate_graph(c); return rc; }
+    out[1] = c.graph_b;
+  }
   std::copy(key, key + 4, c.graph_key);
-  *out = c.graph;
+  out[0] = c.graph;
   return ILG_OK;
 }
 
@@ -679,23 +703,42 @@ int ilg_run_steps_host(ilg_ctx* ctx, const ilg_run_opts* opts, int nsteps, const
   M.host_sun = 1;
   ILG_TRY(upload_desc(c, M));
   bool timing = c.timing;
-  cudaGraphExec_t g = nullptr;
+  cudaGraphExec_t g[2] = {nullptr, nullptr};
   if (o.use_graph && !timing && !c.graph_broken)
-    if (get_graph(c, o, true, &g) != ILG_OK) { c.graph_broken = true; g = nullptr; cudaGetLastError(); }
-  StepView v = solo_view(c, o.precision);
-  StepPlan p = solo_plan(c, o);
-  for (int s = 0; s < nsteps; ++s) {
-    *(SunAux*)c.pinned_aux = make_sun_aux(suns + 3 * (size_t)s, c.solar_const, c.scene_mag, c.disk_rmax);
-    if (g) {
-      ILG_CUDA(cudaGraphLaunch(g, c.stream));
-    } else {
+    if (get_graph(c, o, true, g) != ILG_OK) { c.graph_broken = true; g[0] = g[1] = nullptr; cudaGetLastError(); }
+  SunAux* aux = reinterpret_cast<SunAux*>(c.pinned_aux);
+  if (g[0]) {
+    // Pipelined: step s+1 is queued (sun in slot (s+1)&1) before step s's
+    // surface temperatures are copied out of slot s&1, so the GPU runs the
+    // steps back to back. A slot is rewritten only after the step that last
+    // used it has completed.
+    if (nsteps > 0) {
+      aux[0] = make_sun_aux(suns, c.solar_const, c.scene_mag, c.disk_rmax);
+      ILG_CUDA(cudaGraphLaunch(g[0], c.stream));
+      ILG_CUDA(cudaEventRecord(c.slot_ev[0], c.stream));
+    }
+    for (int s = 0; s < nsteps; ++s) {
+      const int b = s & 1, nb = b ^ 1;
+      if (s + 1 < nsteps) {
+        aux[nb] = make_sun_aux(suns + 3 * (size_t)(s + 1), c.solar_const, c.scene_mag, c.disk_rmax);
+        ILG_CUDA(cudaGraphLaunch(g[nb], c.stream));
+        ILG_CUDA(cudaEventRecord(c.slot_ev[nb], c.stream));
+      }
+      ILG_CUDA(cudaEventSynchronize(c.slot_ev[b]));
+      if (tsurf_out) std::memcpy(tsurf_out + (size_t)s * c.nt, c.pinned_tsurf + (size_t)b * c.nt, (size_t)c.nt * 8);
+    }
+  } else {
+    StepView v = solo_view(c, o.precision);
+    StepPlan p = solo_plan(c, o);
+    for (int s = 0; s < nsteps; ++s) {
+      aux[0] = make_sun_aux(suns + 3 * (size_t)s, c.solar_const, c.scene_mag, c.disk_rmax);
       ILG_CUDA(cudaMemcpyAsync(c.sun_aux.p + c.nsun, c.pinned_aux, sizeof(SunAux), cudaMemcpyHostToDevice, c.stream));
       ILG_TRY(enqueue_step(v, p, c.stream, timing ? c.ev : nullptr));
       ILG_CUDA(cudaMemcpyAsync(c.pinned_tsurf, c.Tsurf.p, (size_t)c.nt * 8, cudaMemcpyDeviceToHost, c.stream));
+      ILG_CUDA(cudaStreamSynchronize(c.stream));
+      if (timing) ILG_TRY(collect_stats(c, true));
+      if (tsurf_out) std::memcpy(tsurf_out + (size_t)s * c.nt, c.pinned_tsurf, (size_t)c.nt * 8);
     }
-    ILG_CUDA(cudaStreamSynchronize(c.stream));
-    if (timing) ILG_TRY(collect_stats(c, true));
-    if (tsurf_out) std::memcpy(tsurf_out + (size_t)s * c.nt, c.pinned_tsurf, (size_t)c.nt * 8);
   }
   c.frame_no += nsteps;
   return read_device_errors(c);

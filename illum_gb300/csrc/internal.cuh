@@ -217,18 +217,20 @@ struct Context {
   dbuf<unsigned> barrier;         // grid barrier state of the radiosity kernel
   dbuf<float> x32;                // mixed-precision radiosity iterates (3 x N)
   dbuf<SunAux> sun_aux;           // nsun entries + the host slot
-  unsigned char* pinned_aux = nullptr;
+  unsigned char* pinned_aux = nullptr;   // 2 SunAux slots (host-driven steps alternate)
   MeshDesc mh{};                  // host mirror of the one-mesh descriptor
   dbuf<MeshDesc> md;
   dbuf<int> mesh_flag;
-  double* pinned_tsurf = nullptr;
+  double* pinned_tsurf = nullptr;        // 2 x N surface temperatures (alternating slots)
+  cudaEvent_t slot_ev[2] = {nullptr, nullptr};
   int64_t stats_ambiguous = 0, stats_sweeps = 0;
   bool timing = false;
   float ms_direct = 0, ms_rad = 0, ms_cond = 0;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
 
   // CUDA graph of one step
-  cudaGraphExec_t graph = nullptr;
+  cudaGraphExec_t graph = nullptr;       // without copies, or with the copies of slot 0
+  cudaGraphExec_t graph_b = nullptr;     // with the copies of slot 1
   int graph_key[4] = {-1, -1, -1, -1};
   bool graph_broken = false;      // capture failed once: launch eagerly
 
