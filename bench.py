@@ -431,6 +431,8 @@ def main():
                 "clocks": clk,
                 "phases_ms_per_step": ph, "radiosity_sweeps_per_step": sweeps_per_step,
                 "ambiguous_facets_per_step": amb_per_step,
+                "direct_samples_per_s": (N * (len(W["disk"]) - 1) / (ph["direct"] * 1e-3)
+                                         if ph.get("direct") else None),
                 "visibility_rays_per_s": su["visibility_rays"] / su["form_factors_s"],
                 "horizon_rays_per_s": su["horizon_rays"] / su["horizons_s"],
                 "setup_s": {k: su[k] for k in ("bvh_s", "horizons_s", "form_factors_s")},

@@ -43,3 +43,66 @@ def load(path: str, order: str = "F") -> np.ndarray:
     if len(dims) == 1:
         return data.copy()
     return data.reshape(dims, order=order).copy()
+
+
+def save_sparse(path: str, rowptr, col, val, n_cols: int | None = None) -> None:
+    """Write a CSR matrix (rows = receivers, as the library's F) as an
+    Armadillo sparse binary file, ARMA_SPM_BIN_FN008: header
+    ``ARMA_SPM_BIN_FN008\\n<n_rows> <n_cols> <n_nonzero>\\n``, then the values,
+    the row indices and the column pointers (u64) of the compressed-column
+    form, which is how Armadillo stores sp_mat (the reference's
+    form_factors.bin, src/cpp/illum_cli.cpp:282 through arma_util::save_mat,
+    src/cpp/arma_util.hpp:8-13)."""
+    rowptr = np.asarray(rowptr, np.int64)
+    col = np.asarray(col, np.int64)
+    val = np.asarray(val, np.float64)
+    n_rows = rowptr.size - 1
+    n_cols = n_rows if n_cols is None else int(n_cols)
+    rows = np.repeat(np.arange(n_rows, dtype=np.int64), np.diff(rowptr))
+    order = np.lexsort((rows, col))          # column-major: by column, then row
+    r, c, v = rows[order], col[order], val[order]
+    colptr = np.zeros(n_cols + 1, np.uint64)
+    np.add.at(colptr, c + 1, 1)
+    colptr = np.cumsum(colptr).astype(np.uint64)
+    with open(path, "wb") as f:
+        f.write(b"ARMA_SPM_BIN_FN008\n%d %d %d\n" % (n_rows, n_cols, v.size))
+        f.write(v.tobytes())
+        f.write(r.astype(np.uint64).tobytes())
+        f.write(colptr.tobytes())
+
+
+def load_sparse(path: str):
+    """Read an ARMA_SPM_BIN_FN008 file (64-bit indices) and return the matrix
+    as CSR (rowptr int64, col int32, val float64, n_cols), the layout
+    IllumContext.set_F takes."""
+    with open(path, "rb") as f:
+        head = f.readline().strip()
+        if head != b"ARMA_SPM_BIN_FN008":
+            raise ValueError("not an ARMA_SPM_BIN_FN008 file")
+        n_rows, n_cols, nnz = (int(x) for x in f.readline().split())
+        v = np.frombuffer(f.read(8 * nnz), np.float64)
+        r = np.frombuffer(f.read(8 * nnz), np.uint64).astype(np.int64)
+        colptr = np.frombuffer(f.read(8 * (n_cols + 1)), np.uint64).astype(np.int64)
+    if colptr[-1] != nnz:
+        raise ValueError("inconsistent column pointers")
+    c = np.repeat(np.arange(n_cols, dtype=np.int64), np.diff(colptr))
+    order = np.lexsort((c, r))
+    rowptr = np.zeros(n_rows + 1, np.int64)
+    np.add.at(rowptr, r + 1, 1)
+    return np.cumsum(rowptr), c[order].astype(np.int32), v[order].copy(), n_cols
+
+
+def load_sun_positions(path: str, unit: str = "km") -> np.ndarray:
+    """Sun positions from a whitespace-separated text file, one position per
+    line, columns beyond the third ignored, as the reference loads
+    sun_pos_file (src/cpp/illum_cli.cpp:325-345: raw ASCII, rows shed past 3,
+    metres rescaled to km when sun_unit is "m"). Returns n x 3 in km."""
+    if unit not in ("km", "m"):
+        raise ValueError("unit must be 'km' or 'm'")
+    S = np.loadtxt(path, dtype=np.float64, ndmin=2)
+    if S.shape[1] < 3:
+        raise ValueError("sun position file needs three columns")
+    S = S[:, :3].copy()
+    if unit == "m":
+        S /= 1000.0
+    return S

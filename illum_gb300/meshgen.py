@@ -197,3 +197,49 @@ def geometric_depths(nz: int, zmax_m: float = 0.5, ratio: float = 1.1) -> np.nda
     kk = np.arange(1, nz + 1, dtype=np.float64)
     dz1 = zmax_m * (ratio - 1.0) / (ratio ** nz - 1.0)
     return dz1 * (ratio ** kk - 1.0) / (ratio - 1.0)
+
+
+def load_obj(path: str, shape_index: int = 0, scale: float = 0.01):
+    """Triangles of one OBJ shape as the reference ingests them
+    (src/cpp/obj_util.cpp:9-96): faces in file order (polygons fan-split),
+    vertices multiplied by `scale` (the reference divides by 100), and each
+    face normal normalise((v1-v0) x (v2-v0)) flipped when it disagrees with
+    the sum of the three vertex normals. Like the reference, vertex normals
+    are looked up by vertex index. Returns (verts float32 n x 3, faces int32
+    m x 3, normals float32 m x 3) for IllumContext(verts, faces, normals)."""
+    V, N, shapes = [], [], [[]]
+    with open(path) as f:
+        for line in f:
+            t = line.split()
+            if not t:
+                continue
+            if t[0] == "v":
+                V.append([float(x) for x in t[1:4]])
+            elif t[0] == "vn":
+                N.append([float(x) for x in t[1:4]])
+            elif t[0] in ("o", "g") and shapes[-1]:
+                shapes.append([])
+            elif t[0] == "f":
+                idx = []
+                for tok in t[1:]:
+                    k = int(tok.split("/")[0])
+                    idx.append(k - 1 if k > 0 else len(V) + k)
+                for j in range(1, len(idx) - 1):
+                    shapes[-1].append((idx[0], idx[j], idx[j + 1]))
+    shapes = [s for s in shapes if s]
+    if shape_index >= len(shapes):
+        raise ValueError(f"{path} has {len(shapes)} shapes")
+    F = np.asarray(shapes[shape_index], np.int64)
+    V = np.asarray(V, np.float32)
+    v0, v1, v2 = V[F[:, 0]], V[F[:, 1]], V[F[:, 2]]
+    n = np.cross(v1 - v0, v2 - v0).astype(np.float32)
+    n /= np.linalg.norm(n, axis=1, keepdims=True).astype(np.float32)
+    if N:
+        Nv = np.asarray(N, np.float32)
+        if Nv.shape[0] < V.shape[0]:
+            raise ValueError("vertex normals are looked up by vertex index and there are fewer of them")
+        s = Nv[F[:, 0]] + Nv[F[:, 1]] + Nv[F[:, 2]]
+        flip = np.sum(n * s, axis=1) < 0
+        n[flip] = -n[flip]
+    Vs = (V * np.float32(scale)).astype(np.float32)
+    return Vs, F.astype(np.int32), n
