@@ -187,6 +187,80 @@ def build_c2(ig, meshgen, precision, nmesh=None, nsteps=None):
     return members
 
 
+TERRAIN = dict(seed=7, spacing_m=2.0, hurst=0.8, rms_m=25.0, n_bowls=2000, dmin_m=10.0, dmax_m=400.0, nphi=128,
+               albedo=0.1, rel_tol=1e-8, nz=40, ti=300.0, rhoc=1500.0 * 700.0, emiss=0.95, T0=200.0,
+               period_s=6 * 3600.0, steps_per_rot=360, site_lat_deg=0.0)
+
+
+def bench_terrain(args, ig, meshgen):
+    """C3 shape: fBm heightmap patch with power-law bowls, form factors within
+    a distance cutoff, 128 horizon azimuths, mixed-precision radiosity refined
+    to rel_tol of ||E|| (absolute tolerance rel_tol * ||E|| at noon), C0
+    materials. value = facet-steps/s of the mixed path (device time, L2
+    flushed per step); max_err_K and radiance errors against the same steps
+    in FP64."""
+    c = TERRAIN
+    n = args.terrain_n
+    t0 = time.perf_counter()
+    v, f = meshgen.heightmap_terrain(n=n, spacing_m=c["spacing_m"], seed=c["seed"], hurst=c["hurst"],
+                                     rms_m=c["rms_m"], n_bowls=c["n_bowls"] * (n * n) // (1024 * 1024),
+                                     dmin_m=c["dmin_m"], dmax_m=c["dmax_m"])
+    t_mesh = time.perf_counter() - t0
+    N = f.shape[0]
+    dt = c["period_s"] / c["steps_per_rot"]
+    nsun = c["steps_per_rot"]
+    suns = meshgen.site_sun_positions(nsun, c["period_s"], dt, c["site_lat_deg"])
+    disk = ig.fib_spiral(100)
+    z = meshgen.geometric_depths(c["nz"])
+    res = {}
+    for prec in (ig.PREC_MIXED, ig.PREC_FP64):
+        t0 = time.perf_counter()
+        ctx = ig.IllumContext(v, f)
+        t_bvh = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        ctx.make_horizons(nphi=c["nphi"])
+        t_hor = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        ctx.compute_F(albedo=c["albedo"], cutoff=args.terrain_cutoff_m / 1000.0, fetch=False)
+        t_ff = time.perf_counter() - t0
+        ctx.set_insolation(1, 0, CFG["solar"])
+        ctx.set_suns(suns, disk)
+        E = ctx.get_direct_radiosity(suns[0], disk)
+        tol = c["rel_tol"] * float(np.linalg.norm(E))
+        tm = ig.ThermalModel(ctx, z, c["ti"], c["rhoc"], c["T0"], emissivity=c["emiss"], bc_mode=ig.BC_NEWTON,
+                             precision=prec)
+        opts = ig.RunOpts(dt=dt, tol=tol, max_sweeps=400, use_radiosity=1, use_graph=1, precision=prec,
+                          coupling=ig.COUPLE_DIRECT)
+        W = max(3, args.warmup)
+        K = min(args.steps, nsun - W)
+        ctx.run_steps(opts, 0, W)
+        clk = ClockSampler(0)
+        clk.start()
+        ms, _ = ctx.bench_steps(opts, W, K, flush_mb=256.0)
+        cl = clk.stop()
+        out = ctx.outputs()
+        st = ctx.stats()
+        res[prec] = dict(ms=float(np.sum(ms)), K=K, T=tm.T.copy(), rad=out["rad"].copy(), clocks=cl,
+                         setup={"mesh_s": t_mesh, "bvh_s": t_bvh, "horizons_s": t_hor, "form_factors_s": t_ff},
+                         rays=int(ctx.visibility_rays), F=ctx.F_info(), tol=tol, stats=st)
+        del tm, ctx
+    m, d = res[ig.PREC_MIXED], res[ig.PREC_FP64]
+    err_K = float(np.abs(m["T"] - d["T"]).max())
+    rad_rel = float(np.abs(m["rad"] - d["rad"]).max() / max(1e-300, np.abs(d["rad"]).max()))
+    line = {"metric": METRIC, "value": N * m["K"] / (m["ms"] * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": m["K"],
+            "warmup": W, "ms_per_step": m["ms"] / m["K"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "bf16 F + fp32 conduction (fp64 residual)", "data": "synthetic",
+            "config": {"workload": f"heightmap {n}x{n} at {c['spacing_m']} m ({N} facets), fBm H {c['hurst']} "
+                                   f"RMS {c['rms_m']} m, power-law bowls, form factors within "
+                                   f"{args.terrain_cutoff_m} m, nphi {c['nphi']}, radiosity to {c['rel_tol']} of "
+                                   f"||E||, nz {c['nz']} (C3 shape at reduced size and cutoff)",
+                       "facets": N, "l2": "256 MB flush before every timed step"},
+            "fp64_value": N * d["K"] / (d["ms"] * 1e-3), "max_err_K_vs_fp64": err_K,
+            "max_rel_radiance_err_vs_fp64": rad_rel, "radiosity_tol": m["tol"], "F": m["F"],
+            "visibility_rays": m["rays"], "setup_s": m["setup"], "clocks": m["clocks"], "gpu_launches": 5 * m["K"]}
+    print(json.dumps(line))
+
+
 def bench_batch(args, ig, meshgen):
     """C2: 64 meshes stepped as one batch (mixed precision, one launch per
     phase, CUDA graph). value = facet-steps/s over steps where every member
@@ -268,8 +342,11 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=12)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--workload", default="c1", choices=["c1", "batch", "serve"],
-                    help="c1: one 81,920-facet mesh (default); batch: 64 meshes as one batch; serve: request loop")
+    ap.add_argument("--workload", default="c1", choices=["c1", "batch", "serve", "terrain"],
+                    help="c1: one 81,920-facet mesh (default); batch: 64 meshes as one batch; serve: request "
+                         "loop; terrain: heightmap patch with a form-factor cutoff, mixed precision")
+    ap.add_argument("--terrain-n", type=int, default=512, help="terrain grid points per side (the C3 shape: 1024)")
+    ap.add_argument("--terrain-cutoff-m", type=float, default=30.0, help="form-factor cutoff (C3 states 2000 m)")
     ap.add_argument("--serve-requests", type=int, default=120)
     ap.add_argument("--serve-scale", type=float, default=0.05, help="step-count scale of the serving sample")
     args = ap.parse_args()
@@ -293,6 +370,10 @@ def main():
     if args.workload == "batch" and args.impl == "ours":
         if rank == 0:
             bench_batch(args, ig, meshgen)
+        return
+    if args.workload == "terrain" and args.impl == "ours":
+        if rank == 0:
+            bench_terrain(args, ig, meshgen)
         return
     if args.workload == "serve" and args.impl == "ours":
         if rank == 0:

@@ -60,6 +60,8 @@ _SIGS = {
     "ilg_trace": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
     "ilg_compute_F": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.POINTER(C.c_int64),
                                 C.POINTER(C.c_int64)]),
+    "ilg_compute_F_cutoff": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_double,
+                                       C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "ilg_get_F": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "ilg_set_F": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]),
     "ilg_F_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int),
@@ -192,8 +194,10 @@ class IllumContext:
         return hit, t
 
     # -- form factors
-    def compute_F(self, albedo=1.0, offset=1e-5):
-        """Returns the form-factor matrix as (rowptr, col, val) CSR by receiver row."""
+    def compute_F(self, albedo=1.0, offset=1e-5, cutoff=None, fetch=True):
+        """Returns the form-factor matrix as (rowptr, col, val) CSR by receiver
+        row (None with fetch=False: it stays on the device). cutoff: keep
+        only pairs whose centroids are at most this far apart."""
         alb = None
         scalar = 1.0
         if np.isscalar(albedo):
@@ -201,9 +205,15 @@ class IllumContext:
         else:
             alb = _f64(albedo)
         nnz = C.c_int64(); rays = C.c_int64()
-        _check(lib().ilg_compute_F(self._h, _p(alb), scalar, offset, C.byref(nnz), C.byref(rays)))
+        if cutoff is None:
+            _check(lib().ilg_compute_F(self._h, _p(alb), scalar, offset, C.byref(nnz), C.byref(rays)))
+        else:
+            _check(lib().ilg_compute_F_cutoff(self._h, _p(alb), scalar, offset, float(cutoff), C.byref(nnz),
+                                              C.byref(rays)))
         self.nnz = nnz.value
         self.visibility_rays = rays.value
+        if not fetch:
+            return None
         return self.get_F()
 
     def get_F(self):

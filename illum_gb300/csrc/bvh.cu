@@ -331,13 +331,23 @@ __global__ void k_horizon_f32(const double* __restrict__ H, int nt, int nphi, fl
 
 // ------------------------------------------------------------------ visibility
 // Candidate enumeration for source j: every i != j passing the facing test
-// of src/cpp/illum.cpp:65-68, found by a half-space query over the BVH
-// (boxes whose farthest point along n_j is below -r_max are skipped).
+// of src/cpp/illum.cpp:65-68 (and the optional distance cutoff), found by a
+// half-space query over the BVH (boxes whose farthest point along n_j is
+// below -r_max are skipped, and with a cutoff boxes farther than it plus
+// r_max).
+__device__ __forceinline__ float box_dist2(f3 p, f3 lo, f3 hi) {
+  float dx = fmaxf(fmaxf(lo.x - p.x, p.x - hi.x), 0.f);
+  float dy = fmaxf(fmaxf(lo.y - p.y, p.y - hi.y), 0.f);
+  float dz = fmaxf(fmaxf(lo.z - p.z, p.z - hi.z), 0.f);
+  return dx * dx + dy * dy + dz * dz;
+}
+
 template <bool FILL>
 __global__ void k_candidates(const float4* __restrict__ nodes, const float4* __restrict__ tri_s, int root,
                              const float4* __restrict__ cen, const float4* __restrict__ nrm, int nt, float r_max,
-                             float slack, uint32_t* count, const unsigned long long* __restrict__ offs,
-                             int32_t* cand_i, int32_t* cand_j, int* derr) {
+                             float slack, float cut2, float box_cut2, uint32_t* count,
+                             const unsigned long long* __restrict__ offs, int32_t* cand_i, int32_t* cand_j,
+                             int* derr) {
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= nt) return;
   float4 cj4 = cen[j], nj4 = nrm[j];
@@ -354,7 +364,7 @@ __global__ void k_candidates(const float4* __restrict__ nodes, const float4* __r
       int i = __float_as_int(__ldg(&tri_s[3 * k]).w);
       if (i != j) {
         float4 ci4 = __ldg(&cen[i]);
-        if (facing(f3of(ci4), ci4.w, p_j, n_j)) {
+        if (facing(f3of(ci4), ci4.w, p_j, n_j) && within_cutoff(f3of(ci4), p_j, cut2)) {
           if (FILL) { cand_i[base + cnt] = i; cand_j[base + cnt] = j; }
           ++cnt;
         }
@@ -371,6 +381,10 @@ __global__ void k_candidates(const float4* __restrict__ nodes, const float4* __r
                (n_j.y >= 0.f ? (nb.rhi.y - p_j.y) * n_j.y : (nb.rlo.y - p_j.y) * n_j.y) +
                (n_j.z >= 0.f ? (nb.rhi.z - p_j.z) * n_j.z : (nb.rlo.z - p_j.z) * n_j.z);
     bool hl = ml > lim, hr = mr > lim;
+    if (cut2 >= 0.f) {   // boxes are around triangles, centroids lie inside them
+      hl = hl && box_dist2(p_j, nb.llo, nb.lhi) <= box_cut2;
+      hr = hr && box_dist2(p_j, nb.rlo, nb.rhi) <= box_cut2;
+    }
     if (hl && hr) {
       if (sp == TRACE_STACK) { atomicExch(&derr[DERR_STACK], 1); break; }
       stack[sp++] = nb.right;
@@ -671,7 +685,8 @@ int horizons_f32(Context& c) {
   return ILG_OK;
 }
 
-int form_factors_build(Context& c, const double* albedo_h, double albedo_scalar, double offset, int64_t* rays_out) {
+int form_factors_build(Context& c, const double* albedo_h, double albedo_scalar, double offset, double cutoff,
+                       int64_t* rays_out) {
   cudaStream_t s = c.stream;
   int nt = c.nt;
   dbuf<uint32_t> cnt;
@@ -679,8 +694,15 @@ int form_factors_build(Context& c, const double* albedo_h, double albedo_scalar,
   ILG_TRY(cnt.alloc(nt));
   ILG_TRY(offs.alloc((size_t)nt + 1));
   float slack = 1e-5f * c.scene_mag;
+  const float cut2 = cutoff > 0.0 ? (float)(cutoff * cutoff) : -1.0f;
+  // box test: the squared distance to a box is computed in float with at
+  // most a few ulps of error; the margin keeps every centroid within the
+  // cutoff reachable
+  const float box_cut2 = cutoff > 0.0 ? (float)((cutoff + 1e-5 * c.scene_mag) * (cutoff + 1e-5 * c.scene_mag)) * 1.0001f
+                                      : -1.0f;
   k_candidates<false><<<div_up(nt, 128), 128, 0, s>>>(c.nodes.p, c.tri_s.p, c.root, c.cen.p, c.nrm.p, nt, c.r_max,
-                                                      slack, cnt.p, nullptr, nullptr, nullptr, c.derr.p);
+                                                      slack, cut2, box_cut2, cnt.p, nullptr, nullptr, nullptr,
+                                                      c.derr.p);
   ILG_CUDA(cudaGetLastError());
   ILG_TRY(scan_exclusive_u32_to_u64(cnt.p, offs.p, nt, c.scan, s));
   unsigned long long last_off = 0;
@@ -701,7 +723,8 @@ int form_factors_build(Context& c, const double* albedo_h, double albedo_scalar,
   c.ntiles = 0;
   if (npairs > 0) {
     k_candidates<true><<<div_up(nt, 128), 128, 0, s>>>(c.nodes.p, c.tri_s.p, c.root, c.cen.p, c.nrm.p, nt, c.r_max,
-                                                       slack, nullptr, offs.p, ci.p, cj.p, c.derr.p);
+                                                       slack, cut2, box_cut2, nullptr, offs.p, ci.p, cj.p,
+                                                       c.derr.p);
     ILG_CUDA(cudaGetLastError());
     k_vis_rays<<<div_up(npairs, 128), 128, 0, s>>>(c.nodes.p, c.tri_s.p, c.root, c.cen.p, c.nrm.p, npairs, ci.p,
                                                    cj.p, (float)offset, bits, nt, keys.p, c.derr.p);

@@ -424,7 +424,17 @@ int ilg_trace(ilg_ctx* ctx, int nrays, const float* orig, const float* dir, int 
 int ilg_compute_F(ilg_ctx* ctx, const double* albedo, double albedo_scalar, double offset, int64_t* nnz, int64_t* rays) {
   if (!ctx) { set_error("ctx is NULL"); return ILG_ERR_ARG; }
   invalidate_graph(ctx->c);
-  ILG_TRY(form_factors_build(ctx->c, albedo, albedo_scalar, offset, rays));
+  ILG_TRY(form_factors_build(ctx->c, albedo, albedo_scalar, offset, 0.0, rays));
+  if (nnz) *nnz = ctx->c.nnz;
+  return ILG_OK;
+}
+
+int ilg_compute_F_cutoff(ilg_ctx* ctx, const double* albedo, double albedo_scalar, double offset, double cutoff,
+                         int64_t* nnz, int64_t* rays) {
+  if (!ctx) { set_error("ctx is NULL"); return ILG_ERR_ARG; }
+  if (!(cutoff > 0.0)) { set_error("cutoff must be > 0"); return ILG_ERR_ARG; }
+  invalidate_graph(ctx->c);
+  ILG_TRY(form_factors_build(ctx->c, albedo, albedo_scalar, offset, cutoff, rays));
   if (nnz) *nnz = ctx->c.nnz;
   return ILG_OK;
 }

@@ -228,6 +228,15 @@ ILG_HD bool facing(f3 p_i, float r_i, f3 p_j, f3 n_j) {
   return !(dot(sub(p_i, p_j), n_j) <= -r_i);
 }
 
+// Distance cutoff of the visibility pairs (not in the reference, which has
+// none; a cutoff makes terrain patches tractable): |p_i - p_j|^2 <= cut2 in
+// float, cut2 < 0 meaning no cutoff.
+ILG_HD bool within_cutoff(f3 p_i, f3 p_j, float cut2) {
+  if (cut2 < 0.0f) return true;
+  f3 d = sub(p_i, p_j);
+  return dot(d, d) <= cut2;
+}
+
 // Form factor F_ij of src/cpp/illum.cpp:108-119. Returns 0 for the
 // zero-distance case (the reference skips it).
 ILG_HD double form_factor(f3 p_i, f3 n_i, f3 p_j, f3 n_j, double A_j) {

@@ -258,7 +258,7 @@ int bvh_trace(Context& c, int nrays, const float* orig_h, const float* dir_h, in
 int horizons_build(Context& c, int nphi, double theta_eps, double offset);
 int horizons_f32(Context& c);   // H32 and hmm32 from H
 int form_factors_build(Context& c, const double* albedo_h, double albedo_scalar, double offset,
-                       int64_t* rays_out);
+                       double cutoff, int64_t* rays_out);
 
 // ---- direct.cu ----
 SunAux make_sun_aux(const double* s, double solar_const, double scene_mag, double disk_rmax);

@@ -192,6 +192,22 @@ def spin_sun_positions(nsteps: int, period_s: float, dt_s: float, subsolar_lat_d
                      np.full(nsteps, d * np.sin(lat))], 1)
 
 
+def site_sun_positions(nsteps: int, period_s: float, dt_s: float, site_lat_deg: float = 0.0,
+                       subsolar_lat_deg: float = 10.0, distance_au: float = 1.5, t0_s: float = 0.0) -> np.ndarray:
+    """Sun positions in km in the local frame of a surface patch (x east,
+    y north, z up) at latitude site_lat_deg on a body spinning with the given
+    period; the sun crosses the meridian at t = 0. Returns [nsteps, 3]."""
+    t = t0_s + dt_s * np.arange(nsteps)
+    h = 2.0 * np.pi * t / period_s
+    dec = np.deg2rad(subsolar_lat_deg)
+    phi = np.deg2rad(site_lat_deg)
+    d = distance_au * AU_KM
+    east = -np.cos(dec) * np.sin(h)
+    north = np.cos(phi) * np.sin(dec) - np.sin(phi) * np.cos(dec) * np.cos(h)
+    up = np.sin(phi) * np.sin(dec) + np.cos(phi) * np.cos(dec) * np.cos(h)
+    return d * np.stack([east, north, up], 1)
+
+
 def geometric_depths(nz: int, zmax_m: float = 0.5, ratio: float = 1.1) -> np.ndarray:
     """Layer depths z_1..z_nz (m) with z_k = dz1 (ratio^k - 1)/(ratio - 1), z_nz = zmax."""
     kk = np.arange(1, nz + 1, dtype=np.float64)

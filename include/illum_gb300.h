@@ -90,6 +90,11 @@ int ilg_trace(ilg_ctx* ctx, int nrays, const float* orig, const float* dir, int 
  * row; *nnz receives its size and *rays the number of visibility rays. */
 int ilg_compute_F(ilg_ctx* ctx, const double* albedo, double albedo_scalar, double offset,
                   int64_t* nnz, int64_t* rays);
+/* As ilg_compute_F, keeping only pairs whose centroids are at most `cutoff`
+ * apart (mesh units). The reference has no cutoff; it makes large terrain
+ * patches tractable (a facet then sees O(cutoff^2) facets, not O(N)). */
+int ilg_compute_F_cutoff(ilg_ctx* ctx, const double* albedo, double albedo_scalar, double offset,
+                         double cutoff, int64_t* nnz, int64_t* rays);
 /* rowptr: nt+1, col: nnz, val: nnz */
 int ilg_get_F(ilg_ctx* ctx, int64_t* rowptr, int32_t* col, double* val);
 int ilg_set_F(ilg_ctx* ctx, int64_t nnz, const int64_t* rowptr, const int32_t* col,

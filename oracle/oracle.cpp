@@ -258,7 +258,7 @@ static std::vector<double> s_f;
 static int64_t s_rays = 0;
 
 int64_t orc_form_factors(const float* verts, const int32_t* tris, int nt, double offset,
-                         const double* albedo, double albedo_scalar,
+                         const double* albedo, double albedo_scalar, double cutoff,
                          int32_t* rows, int32_t* cols, double* vals) {
   if (rows) {
     std::memcpy(rows, s_i.data(), s_i.size() * 4);
@@ -273,6 +273,7 @@ int64_t orc_form_factors(const float* verts, const int32_t* tris, int nt, double
   std::vector<std::vector<double>> f_of(nt);
   std::atomic<int64_t> rays{0};
   std::atomic<int> bad{0};
+  const float cut2 = cutoff > 0.0 ? (float)(cutoff * cutoff) : -1.0f;
   parallel_for(nt, [&](int64_t jj) {
     int j = (int)jj;
     f3 p_j = m.c[j], n_j = m.n[j];
@@ -282,6 +283,7 @@ int64_t orc_form_factors(const float* verts, const int32_t* tris, int nt, double
     for (int i = 0; i < nt; ++i) {
       if (i == j) continue;
       if (!facing(m.c[i], m.r[i], p_j, n_j)) continue;
+      if (!within_cutoff(m.c[i], p_j, cut2)) continue;
       f3 d = normalize(sub(m.c[i], q_j));
       ++nr;
       int h = bvh.trace(q_j, d, false, nullptr);

@@ -65,19 +65,21 @@ def trace(verts, faces, orig, dirs, any_hit=False, brute=False):
     return hit, t
 
 
-def form_factors(verts, faces, offset=1e-5, albedo=None, albedo_scalar=1.0):
+def form_factors(verts, faces, offset=1e-5, albedo=None, albedo_scalar=1.0, cutoff=0.0):
     """Returns (rows, cols, vals) in the reference's column-major order and the
-    number of visibility rays cast."""
+    number of visibility rays cast. cutoff > 0 keeps only pairs whose
+    centroids are at most that far apart (not in the reference)."""
     verts = np.ascontiguousarray(verts, np.float32)
     faces = np.ascontiguousarray(faces, np.int32)
     alb = None if albedo is None else np.ascontiguousarray(albedo, np.float64)
     L = lib()
     nnz = L.orc_form_factors(_p(verts), _p(faces), C.c_int(faces.shape[0]), C.c_double(offset), _p(alb),
-                             C.c_double(albedo_scalar), None, None, None)
+                             C.c_double(albedo_scalar), C.c_double(cutoff), None, None, None)
     if nnz < 0:
         raise RuntimeError("computed a NaN form factor")
     rows = np.zeros(nnz, np.int32); cols = np.zeros(nnz, np.int32); vals = np.zeros(nnz, np.float64)
-    L.orc_form_factors(None, None, C.c_int(0), C.c_double(0), None, C.c_double(0), _p(rows), _p(cols), _p(vals))
+    L.orc_form_factors(None, None, C.c_int(0), C.c_double(0), None, C.c_double(0), C.c_double(0), _p(rows),
+                       _p(cols), _p(vals))
     return rows, cols, vals, int(L.orc_last_visibility_rays())
 
 

@@ -111,6 +111,20 @@ def test_form_factors_per_facet_albedo(ilg, oracle_mod, mesh_l3):
     assert np.array_equal(rowptr, rp) and np.array_equal(col, c) and np.array_equal(val, x)
 
 
+@pytest.mark.parametrize("cutoff_m", [15.0, 40.0])
+def test_form_factors_cutoff_bit_exact(ilg, oracle_mod, cutoff_m):
+    """Terrain patch with the distance cutoff: same pairs, rays and values as
+    the oracle's brute-force loop with the same cutoff test."""
+    v, f = meshgen.heightmap_terrain(n=40, n_bowls=6, seed=3)
+    ctx = ilg.IllumContext(v, f)
+    rowptr, col, val = ctx.compute_F(albedo=0.1, cutoff=cutoff_m / 1000.0)
+    ro, co, vo, rays = oracle_mod.form_factors(v, f, albedo_scalar=0.1, cutoff=cutoff_m / 1000.0)
+    rp, c, x = oracle_mod.coo_to_csr(f.shape[0], ro, co, vo)
+    assert ctx.visibility_rays == rays
+    assert np.array_equal(rowptr, rp) and np.array_equal(col, c) and np.array_equal(val, x)
+    assert len(val) > 0
+
+
 @pytest.mark.parametrize("norm_mode,interp", [(0, 0), (1, 0), (1, 1)])
 def test_direct_bit_exact(ilg, oracle_mod, mesh_l4, norm_mode, interp):
     v, f = mesh_l4
