@@ -63,6 +63,8 @@ _SIGS = {
     "ilg_compute_F_cutoff": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_double,
                                        C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "ilg_get_F": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "ilg_record_thermal": (C.c_int, [C.c_void_p, C.c_int]),
+    "ilg_get_thermal_records": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_int)]),
     "ilg_set_F": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]),
     "ilg_F_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int),
                              C.POINTER(C.c_int)]),
@@ -303,6 +305,22 @@ class IllumContext:
         r, ra, ta, tm = (np.zeros(n) for _ in range(4))
         _check(lib().ilg_get_outputs(self._h, _p(r), _p(ra), _p(ta), _p(tm)))
         return {"rad": r, "rad_avg": ra, "therm_avg": ta, "therm_max": tm}
+
+    RECORD_COLUMNS = ("Tmax", "Tmin", "Tavg", "Tstd", "Tmax_top", "Tmin_top", "Tavg_top", "Tstd_top",
+                      "Tmax_bot", "Tmin_bot", "Tavg_bot", "Tstd_bot", "E_absorbed", "E_emitted", "E_conducted")
+
+    def record_thermal(self, capacity: int):
+        """Record per-step temperature statistics and FP64 energy sums for the
+        next `capacity` steps (columns RECORD_COLUMNS); 0 stops."""
+        _check(lib().ilg_record_thermal(self._h, int(capacity)))
+
+    def thermal_records(self):
+        n = C.c_int()
+        _check(lib().ilg_get_thermal_records(self._h, None, C.byref(n)))
+        out = np.zeros((n.value, 15), np.float64)
+        if n.value:
+            _check(lib().ilg_get_thermal_records(self._h, _p(out), C.byref(n)))
+        return out
 
     def set_timing(self, enable=True):
         _check(lib().ilg_set_timing(self._h, int(enable)))

@@ -54,7 +54,7 @@ struct Batch {
   dbuf<int> mesh_of;
   dbuf<int2> cblocks;
   dbuf<float4> cen, nrm, frame32;
-  dbuf<double> frame, H, disk;
+  dbuf<double> frame, H, disk, area, rec, rec_part;
   dbuf<float> H32, disk32;
   dbuf<float2> hmm32;
   dbuf<SunAux> suns;
@@ -93,7 +93,7 @@ static int build(Batch& b) {
   int n = (int)b.members.size();
   cudaStream_t s = b.stream;
   // sizes and offsets
-  int64_t nt = 0, nH = 0, nT = 0, ncoef = 0, nsun = 0, ntl = 0, nel = 0, ncb = 0, nrow = 0, nhal = 0;
+  int64_t nt = 0, nH = 0, nT = 0, ncoef = 0, nsun = 0, ntl = 0, nel = 0, ncb = 0, nrow = 0, nhal = 0, nrec = 0;
   b.mh.assign(n, MeshDesc{});
   b.nz_max = 0;
   int ndisk = -1;
@@ -115,6 +115,9 @@ static int build(Batch& b) {
     M.sun0 = (int)nsun;
     M.host_slot = (int)(nsun + c.nsun);
     M.tile0 = (int)ntl;
+    M.cb0 = (int)ncb;
+    M.rec0 = (int)nrec;
+    nrec += M.rec_cap;
     b.mh[i] = M;
     nt += c.nt;
     nH += (int64_t)c.nt * c.nphi;
@@ -139,6 +142,9 @@ static int build(Batch& b) {
   ILG_TRY(b.mesh_of.alloc(nt));
   ILG_TRY(b.cblocks.alloc(ncb));
   ILG_TRY(b.cen.alloc(nt)); ILG_TRY(b.nrm.alloc(nt)); ILG_TRY(b.frame32.alloc(3 * nt));
+  ILG_TRY(b.area.alloc(nt));
+  ILG_TRY(b.rec.alloc(nrec > 0 ? nrec * REC_W : 1));
+  ILG_TRY(b.rec_part.alloc((ncb > 0 ? ncb : 1) * REC_PART));
   ILG_TRY(b.frame.alloc(9 * nt)); ILG_TRY(b.H.alloc(nH)); ILG_TRY(b.H32.alloc(nH)); ILG_TRY(b.hmm32.alloc(nt));
   ILG_TRY(b.disk.alloc(2 * (size_t)ndisk));
   ILG_TRY(b.disk32.alloc(2 * (size_t)ndisk));
@@ -201,6 +207,8 @@ static int build(Batch& b) {
     ILG_TRY(cat(b.nrm, f0, c.nrm.p, N, s));
     ILG_TRY(cat(b.frame32, 3 * f0, c.frame32.p, 3 * N, s));
     ILG_TRY(cat(b.frame, 9 * f0, c.frame.p, 9 * N, s));
+    ILG_TRY(cat(b.area, f0, c.area.p, N, s));
+    if (M.rec_cap > 0) ILG_TRY(cat(b.rec, (size_t)M.rec0 * REC_W, c.rec.p, (size_t)M.rec_cap * REC_W, s));
     ILG_TRY(cat(b.H, (size_t)M.H0, c.H.p, N * c.nphi, s));
     ILG_TRY(cat(b.H32, (size_t)M.H0, c.H32.p, N * c.nphi, s));
     ILG_TRY(cat(b.hmm32, f0, c.hmm32.p, N, s));
@@ -262,6 +270,9 @@ static int build(Batch& b) {
   v.nt = b.nt; v.nmesh = n; v.md = b.md.p; v.mesh_of = b.mesh_of.p;
   v.cen = b.cen.p; v.nrm = b.nrm.p; v.frame32 = b.frame32.p; v.frame = b.frame.p; v.H = b.H.p;
   v.H32 = b.H32.p; v.hmm32 = b.hmm32.p; v.disk = b.disk.p; v.disk32 = b.disk32.p; v.ndisk = ndisk;
+  v.area = b.area.p;
+  v.rec = nrec > 0 ? b.rec.p : nullptr;
+  v.rec_part = b.rec_part.p;
   v.suns = b.suns.p;
   v.Tsurf = b.Tsurf.p; v.Fsurf = b.Fsurf.p; v.Qprev = b.Qprev.p; v.rad = b.rad.p; v.rad_avg = b.rad_avg.p;
   v.therm_avg = b.therm_avg.p; v.therm_max = b.therm_max.p; v.E = b.E.p; v.sprev = b.sprev.p;
@@ -277,6 +288,7 @@ static int build(Batch& b) {
   v.barrier = b.barrier.p;
   b.plan.precision = b.precision;
   b.plan.rad_on = b.ntiles > 0;
+  b.plan.rec_on = nrec > 0;
   b.plan.rad_grid = b.plan.rad_on ? radiosity_grid(b.ntiles, b.precision) : 1;
   b.plan.nz_max = b.nz_max;
   return ILG_OK;
@@ -454,6 +466,9 @@ int ilg_batch_sync(ilg_batch* batch) {
       ILG_CUDA(cudaMemcpyAsync(c.T32.p, b.T32.p + M.T0, N * c.nz * 4, cudaMemcpyDeviceToDevice, s));
     else
       ILG_CUDA(cudaMemcpyAsync(c.Tdf.p, b.Tdf.p + M.T0, N * c.nz * 8, cudaMemcpyDeviceToDevice, s));
+    if (M.rec_cap > 0)
+      ILG_CUDA(cudaMemcpyAsync(c.rec.p, b.rec.p + (size_t)M.rec0 * REC_W, (size_t)M.rec_cap * REC_W * 8,
+                               cudaMemcpyDeviceToDevice, s));
     c.frame_no = m[i].frame;
   }
   ILG_CUDA(cudaStreamSynchronize(b.stream));

@@ -126,6 +126,7 @@ int enqueue_step(const StepView& v, const StepPlan& p, cudaStream_t s, cudaEvent
   if (p.rad_on) ILG_TRY(radiosity_launch(v, v.rad, 1, p.precision, p.rad_grid, s));
   if (ev) ILG_CUDA(cudaEventRecord(ev[2], s));
   ILG_TRY(conduction_launch(v, v.rad, p.precision, 1, p.nz_max, s));
+  if (p.rec_on) ILG_TRY(record_launch(v, p.precision, v.cblocks ? v.ncblocks : div_up(v.nt, conduction_step_threads()), s));
   if (ev) ILG_CUDA(cudaEventRecord(ev[3], s));
   return advance_launch(v, s);
 }
@@ -146,7 +147,9 @@ static StepView solo_view(Context& c, int precision) {
   v.md = c.md.p;
   v.mesh_of = nullptr;
   v.cen = c.cen.p; v.nrm = c.nrm.p; v.frame32 = c.frame32.p;
-  v.frame = c.frame.p; v.H = c.H.p; v.H32 = c.H32.p; v.hmm32 = c.hmm32.p; v.disk = c.disk.p;
+  v.frame = c.frame.p; v.H = c.H.p; v.H32 = c.H32.p; v.hmm32 = c.hmm32.p; v.disk = c.disk.p; v.area = c.area.p;
+  v.rec = c.rec_cap > 0 ? c.rec.p : nullptr;
+  v.rec_part = c.rec_part.p;
   v.disk32 = c.disk32.p;
   v.ndisk = c.ndisk;
   v.suns = c.sun_aux.p;
@@ -195,6 +198,11 @@ MeshDesc solo_desc(const Context& c, const ilg_run_opts* o, int first_sun) {
   M.cs = c.cond_cs;
   M.tile0 = 0;
   M.ntiles = (o && o->use_radiosity && c.have_F) ? c.ntiles : 0;
+  M.cb0 = 0;
+  M.ncb = div_up(c.nt, conduction_step_threads());
+  M.rec0 = 0;
+  M.rec_cap = c.rec_cap;
+  M.rec_frame0 = c.rec_frame0;
   M.tol2 = o ? o->tol * o->tol : 0.0;
   M.max_sweeps = o ? o->max_sweeps : 1;
   M.active = 1;
@@ -249,6 +257,7 @@ static StepPlan solo_plan(Context& c, const ilg_run_opts& o) {
   p.rad_on = o.use_radiosity && c.have_F && c.ntiles > 0;
   p.rad_grid = p.rad_on ? radiosity_grid(c.ntiles, o.precision) : 1;
   p.nz_max = c.nz;
+  p.rec_on = c.rec_cap > 0;
   return p;
 }
 
@@ -290,8 +299,8 @@ static int capture_step(Context& c, const ilg_run_opts& o, int slot, cudaGraphEx
 // Graph of one step (with_copies: the two host-driven slot graphs, out[0]
 // and out[1]; otherwise out[0] only).
 static int get_graph(Context& c, const ilg_run_opts& o, bool with_copies, cudaGraphExec_t* out) {
-  int key[4] = {o.precision * 4 + o.coupling * 2 + (o.use_radiosity ? 1 : 0), with_copies ? 1 : 0, c.nz,
-                c.ntiles};
+  int key[4] = {o.precision * 4 + o.coupling * 2 + (o.use_radiosity ? 1 : 0), (with_copies ? 1 : 0) + 2 * c.rec_cap,
+                c.nz, c.ntiles};
   if (c.graph && std::equal(key, key + 4, c.graph_key)) {
     out[0] = c.graph;
     if (with_copies) out[1] = c.graph_b;
@@ -813,6 +822,31 @@ int ilg_get_outputs(ilg_ctx* ctx, double* rad, double* rad_avg, double* therm_av
   if (therm_avg) ILG_CUDA(cudaMemcpyAsync(therm_avg, c.therm_avg.p, b, cudaMemcpyDeviceToHost, c.stream));
   if (therm_max) ILG_CUDA(cudaMemcpyAsync(therm_max, c.therm_max.p, b, cudaMemcpyDeviceToHost, c.stream));
   ILG_CUDA(cudaStreamSynchronize(c.stream));
+  return ILG_OK;
+}
+
+int ilg_record_thermal(ilg_ctx* ctx, int capacity) {
+  if (!ctx || capacity < 0) { set_error("invalid arguments"); return ILG_ERR_ARG; }
+  Context& c = ctx->c;
+  invalidate_graph(c);
+  if (capacity == 0) { c.rec_cap = 0; return ILG_OK; }
+  ILG_TRY(c.rec.alloc((size_t)capacity * REC_W));
+  ILG_TRY(c.rec_part.alloc((size_t)div_up(c.nt, conduction_step_threads()) * REC_PART));
+  ILG_CUDA(cudaMemset(c.rec.p, 0, (size_t)capacity * REC_W * 8));
+  c.rec_cap = capacity;
+  c.rec_frame0 = c.frame_no;
+  return ILG_OK;
+}
+
+int ilg_get_thermal_records(ilg_ctx* ctx, double* out, int* count) {
+  if (!ctx || !count) { set_error("invalid arguments"); return ILG_ERR_ARG; }
+  Context& c = ctx->c;
+  int n = std::max(0, std::min(c.rec_cap, c.frame_no - c.rec_frame0));
+  *count = n;
+  if (out && n > 0) {
+    ILG_CUDA(cudaMemcpyAsync(out, c.rec.p, (size_t)n * REC_W * 8, cudaMemcpyDeviceToHost, c.stream));
+    ILG_CUDA(cudaStreamSynchronize(c.stream));
+  }
   return ILG_OK;
 }
 

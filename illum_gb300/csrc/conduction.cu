@@ -464,6 +464,131 @@ int conduction_launch(const StepView& v, const double* Q, int precision, int upd
   return launch_conduct<dfloat, COND_STEP_THREADS>(v, Q, upd, nz_max, s);
 }
 
+// ---- thermal records ----------------------------------------------------------
+namespace {
+
+// Sums of (T - REC_SHIFT) and of its square (the variance stays well
+// conditioned for temperatures of a few hundred K), minima and maxima, per
+// conduction block, then per mesh, both in a fixed order (deterministic).
+// Group g of a partial: [5g] min, [5g+1] max, [5g+2] count, [5g+3] sum,
+// [5g+4] sum of squares, for g = all layers and the surface, the surface
+// row, the bottom layer; [15..17] the energy sums.
+constexpr double REC_SHIFT = 250.0;
+
+__device__ __forceinline__ double layer_value(const double* T, size_t i) { return T[i]; }
+__device__ __forceinline__ double layer_value(const float* T, size_t i) { return (double)T[i]; }
+__device__ __forceinline__ double layer_value(const dfloat* T, size_t i) { return (double)T[i]; }
+
+__device__ __forceinline__ void rec_neutral(double* q) {
+  for (int g = 0; g < 3; ++g) {
+    q[5 * g] = INFINITY;
+    q[5 * g + 1] = -INFINITY;
+    q[5 * g + 2] = q[5 * g + 3] = q[5 * g + 4] = 0.0;
+  }
+  q[15] = q[16] = q[17] = 0.0;
+}
+__device__ __forceinline__ void rec_add(double* q, int g, double x) {
+  q[5 * g] = fmin(q[5 * g], x);
+  q[5 * g + 1] = fmax(q[5 * g + 1], x);
+  double d = x - REC_SHIFT;
+  q[5 * g + 2] += 1.0;
+  q[5 * g + 3] += d;
+  q[5 * g + 4] += d * d;
+}
+__device__ __forceinline__ void rec_merge(double* a, const double* b) {
+  for (int g = 0; g < 3; ++g) {
+    a[5 * g] = fmin(a[5 * g], b[5 * g]);
+    a[5 * g + 1] = fmax(a[5 * g + 1], b[5 * g + 1]);
+    a[5 * g + 2] += b[5 * g + 2];
+    a[5 * g + 3] += b[5 * g + 3];
+    a[5 * g + 4] += b[5 * g + 4];
+  }
+  a[15] += b[15];
+  a[16] += b[16];
+  a[17] += b[17];
+}
+
+template <class R>
+__global__ void __launch_bounds__(COND_STEP_THREADS) k_rec_partial(StepView v) {
+  __shared__ double sh[COND_STEP_THREADS][REC_PART];
+  int2 cb = v.cblocks ? v.cblocks[blockIdx.x] : make_int2(0, blockIdx.x * COND_STEP_THREADS);
+  const MeshDesc& M = v.md[cb.x];
+  double* q = sh[threadIdx.x];
+  rec_neutral(q);
+  const int fl = cb.y + threadIdx.x;
+  if (M.active && M.rec_cap > 0 && fl < M.nfacet) {
+    const int g = M.facet0 + fl;
+    const R* T = state_T<R>(v) + M.T0 + fl;
+    const size_t N = (size_t)M.nfacet;
+    const int nz = M.cs.nz;
+    double Ts = v.Tsurf[g];
+    rec_add(q, 0, Ts);
+    rec_add(q, 1, Ts);
+    for (int i = 0; i < nz; ++i) {
+      double x = layer_value(T, (size_t)i * N);
+      rec_add(q, 0, x);
+      if (i == nz - 1) rec_add(q, 2, x);
+    }
+    const double A = v.area[g];
+    double t2 = Ts * Ts;
+    q[15] = A * v.rad[g];
+    q[16] = A * (M.cs.es * (t2 * t2));
+    q[17] = A * v.Fsurf[g];
+  }
+  __syncthreads();
+  for (int off = COND_STEP_THREADS / 2; off; off >>= 1) {
+    if (threadIdx.x < off) rec_merge(sh[threadIdx.x], sh[threadIdx.x + off]);
+    __syncthreads();
+  }
+  if (threadIdx.x < REC_PART) v.rec_part[(size_t)blockIdx.x * REC_PART + threadIdx.x] = sh[0][threadIdx.x];
+}
+
+constexpr int REC_FINAL_THREADS = 128;
+
+__global__ void __launch_bounds__(REC_FINAL_THREADS) k_rec_final(StepView v) {
+  __shared__ double sh[REC_FINAL_THREADS][REC_PART];
+  const MeshDesc& M = v.md[blockIdx.x];
+  if (!M.active || M.rec_cap <= 0) return;
+  const int slot = M.frame - M.rec_frame0;
+  if (slot < 0 || slot >= M.rec_cap) return;
+  double* q = sh[threadIdx.x];
+  rec_neutral(q);
+  for (int b = M.cb0 + threadIdx.x; b < M.cb0 + M.ncb; b += REC_FINAL_THREADS)
+    rec_merge(q, v.rec_part + (size_t)b * REC_PART);
+  __syncthreads();
+  for (int off = REC_FINAL_THREADS / 2; off; off >>= 1) {
+    if (threadIdx.x < off) rec_merge(sh[threadIdx.x], sh[threadIdx.x + off]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double* r = sh[0];
+    double* out = v.rec + (size_t)(M.rec0 + slot) * REC_W;
+    for (int g = 0; g < 3; ++g) {   // the reference's column order: max, min, mean, std
+      double n = r[5 * g + 2], s1 = r[5 * g + 3], s2 = r[5 * g + 4];
+      double var = n > 1.0 ? (s2 - s1 * s1 / n) / (n - 1.0) : 0.0;
+      out[4 * g] = r[5 * g + 1];
+      out[4 * g + 1] = r[5 * g];
+      out[4 * g + 2] = REC_SHIFT + s1 / n;
+      out[4 * g + 3] = sqrt(fmax(var, 0.0));
+    }
+    out[12] = r[15];
+    out[13] = r[16];
+    out[14] = r[17];
+  }
+}
+
+}  // namespace
+
+int record_launch(const StepView& v, int precision, int ncblocks, cudaStream_t s) {
+  if (!v.rec || ncblocks <= 0) return ILG_OK;
+  if (precision == ILG_PREC_MIXED) k_rec_partial<float><<<ncblocks, COND_STEP_THREADS, 0, s>>>(v);
+  else k_rec_partial<dfloat><<<ncblocks, COND_STEP_THREADS, 0, s>>>(v);
+  ILG_CUDA(cudaGetLastError());
+  k_rec_final<<<v.nmesh, REC_FINAL_THREADS, 0, s>>>(v);
+  ILG_CUDA(cudaGetLastError());
+  return ILG_OK;
+}
+
 // Standalone batched columns (host arrays, reference layout: column-major
 // nz x ncol). Runs on the current device with a private stream.
 static int run_columns(int ncol, int nz, const double* z, double dt, const double* Qn, const double* Qnp1, double* T,

@@ -90,6 +90,9 @@ struct MeshDesc {
   double res2;                 // out: squared residual bound of the last solve
   int active;                  // 0: skipped by the step kernels
   int done_steps;              // steps taken since the run started
+  int cb0, ncb;                // the mesh's conduction blocks (thermal records)
+  int rec0, rec_cap;           // thermal records: offset (records) and capacity, 0 = not recording
+  int rec_frame0;              // frame of record 0
 };
 
 // Everything a step kernel touches, as plain device pointers.
@@ -98,7 +101,7 @@ struct StepView {
   MeshDesc* md;
   const int* mesh_of;          // per facet, or nullptr for a single mesh
   const float4 *cen, *nrm, *frame32;
-  const double *frame, *H, *disk;
+  const double *frame, *H, *disk, *area;
   const float* H32;            // fp32 copy of H
   const float2* hmm32;         // per facet: fp32 min and max of its horizon
   const float* disk32;         // fp32 copy of the disk samples
@@ -131,6 +134,8 @@ struct StepView {
   // scratch
   int *work, *counters, *derr, *mesh_flag;
   unsigned* barrier;
+  double* rec;                 // thermal records, REC_W doubles each (or nullptr)
+  double* rec_part;            // per conduction block: REC_PART doubles
   double* rho64;               // deep-column conduction scratch [nz][nt] (or nullptr)
   float* rho32;
 };
@@ -203,6 +208,8 @@ struct Context {
   dbuf<double> rad, rad_avg, therm_avg, therm_max, E, xtmp, Q;
   dbuf<double> sprev;             // 2 x N: x - E of the last radiosity solve, and its change
   int frame_no = 0;
+  int rec_cap = 0, rec_frame0 = 0;  // thermal records (ilg_record_thermal)
+  dbuf<double> rec, rec_part;
 
   // suns and step machinery
   int nsun = 0;
@@ -247,6 +254,7 @@ struct Context {
 struct StepPlan {
   int precision;
   bool rad_on;
+  bool rec_on;                 // thermal records after conduction
   int rad_grid;
   int nz_max;
 };
@@ -282,6 +290,14 @@ int flush_launch(float4* buf, size_t n, unsigned salt, cudaStream_t s);
 // ---- conduction.cu ----
 int conduction_prepare(Context& c, double dt, int precision);
 int conduction_setup();
+// Thermal records: per step and mesh, the reference's 12 temperature
+// statistics (thermal.hpp:86-126: max, min, mean, sample std over all
+// layers incl. the surface, over the surface row, over the bottom layer)
+// and three FP64 energy sums (area x absorbed flux, area x emitted flux
+// emiss sigma Ts^4, area x conducted flux Fsurf).
+constexpr int REC_W = 15;
+constexpr int REC_PART = 18;
+int record_launch(const StepView& v, int precision, int ncblocks, cudaStream_t s);
 int conduction_step_threads();   // facets per conduction block of a scene step
 // Q: heat flux at the new time level per facet (global index); upd: also
 // update rad_avg / therm_avg / therm_max; nz_max: deepest mesh of the view.

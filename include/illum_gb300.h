@@ -192,6 +192,19 @@ int ilg_get_outputs(ilg_ctx* ctx, double* rad, double* rad_avg, double* therm_av
 /* Per-phase device times (ms) of the last ilg_run_steps call with timing
  * enabled, and per-call counters. */
 int ilg_set_timing(ilg_ctx* ctx, int enable);
+
+/* ---- thermal records (thermal_model record_stats) ---------------------------- */
+/* Records, for each of the next `capacity` steps (ilg_run_steps,
+ * ilg_run_steps_host, or a batch holding the context), 15 FP64 values: the
+ * reference's 12 temperature statistics (thermal.hpp:86-126: Tmax, Tmin,
+ * Tavg, Tstd over all layers and the surface; the same over the surface
+ * row; the same over the bottom layer; std with N - 1) and three energy
+ * sums: sum of area x absorbed flux Q, of area x emitted emiss sigma Ts^4,
+ * of area x conducted Fsurf (area in the mesh's unit squared, fluxes in
+ * W/m^2). Adds a reduction per step. capacity 0 stops recording. */
+int ilg_record_thermal(ilg_ctx* ctx, int capacity);
+/* out: count x 15 row-major (may be NULL); count = steps recorded. */
+int ilg_get_thermal_records(ilg_ctx* ctx, double* out, int* count);
 int ilg_get_stats(ilg_ctx* ctx, double* ms_direct, double* ms_radiosity, double* ms_conduction,
                   int64_t* ambiguous_facets, int64_t* radiosity_sweeps);
 
