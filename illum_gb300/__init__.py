@@ -64,6 +64,7 @@ _SIGS = {
                                        C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "ilg_get_F": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "ilg_record_thermal": (C.c_int, [C.c_void_p, C.c_int]),
+    "ilg_render": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_int, C.c_int, C.c_void_p]),
     "ilg_get_thermal_records": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_int)]),
     "ilg_set_F": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]),
     "ilg_F_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int),

@@ -285,6 +285,42 @@ __global__ void k_trace(const float4* __restrict__ nodes, const float4* __restri
   }
 }
 
+// ------------------------------------------------------------------ renderer
+// One closest-hit ray per pixel of src/cpp/illum_renderer_cli.cpp:228-276:
+// mode 0 orthographic from direction (az, el) at distance 1.1 r_model,
+// mode 1 equal-area cylindrical map (rays from a sphere of radius
+// 1.1 r_model towards the model centre). out: facet index or -1.
+struct RenderCam {
+  int mode, width, height;
+  double rad, aspect, az, el;
+  float px, py, pz, ex, ey, ez, ux, uy, uz, rx, ry, rz;   // orthographic camera (float, as Vector3)
+  float cx, cy, cz;                                     // model centre
+};
+
+__global__ void k_render(const float4* __restrict__ nodes, const float4* __restrict__ tri_s, int root, RenderCam cam,
+                         int32_t* out, int* derr) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= (int64_t)cam.width * cam.height) return;
+  const int i = (int)(k / cam.width), j = (int)(k % cam.width);
+  f3 o, d;
+  if (cam.mode == 0) {
+    double y_eye = (2.0 * (1.0 - (double)i / (cam.height - 1)) - 1.0) * cam.rad;
+    double x_eye = (2.0 * (double)j / (cam.width - 1) - 1.0) * cam.aspect * cam.rad;
+    float ye = (float)y_eye, xe = (float)x_eye;
+    o = mk(cam.px + ye * cam.ux + xe * cam.rx, cam.py + ye * cam.uy + xe * cam.ry, cam.pz + ye * cam.uz + xe * cam.rz);
+    d = mk(cam.ex, cam.ey, cam.ez);
+  } else {
+    const double PI_D = 3.141592653589793;
+    double theta = asin(2.0 * (double)(i + 1) / (cam.height + 1) - 1.0) - cam.el;
+    double phi = 2.0 * PI_D * (double)j / cam.width - cam.az;
+    f3 p = mk((float)(cam.rad * cos(phi) * sin(theta)), (float)(cam.rad * sin(phi) * sin(theta)),
+              (float)(cam.rad * cos(theta)));
+    d = normalize(mk(-p.x, -p.y, -p.z));
+    o = mk(p.x + cam.cx, p.y + cam.cy, p.z + cam.cz);
+  }
+  out[k] = trace_closest(nodes, tri_s, root, o, d, nullptr, &derr[DERR_STACK]);
+}
+
 // ------------------------------------------------------------------ horizons
 // One thread per (facet, azimuth): walk the precomputed bisection tree of
 // src/cpp/illum.cpp:304-316 (hit -> hi = mid, miss -> lo = mid), one any-hit
@@ -591,6 +627,53 @@ int bvh_trace(Context& c, int nrays, const float* orig_h, const float* dir_h, in
   ILG_CUDA(cudaGetLastError());
   ILG_CUDA(cudaMemcpyAsync(hit_h, h.p, (size_t)nrays * 4, cudaMemcpyDeviceToHost, s));
   if (t_h) ILG_CUDA(cudaMemcpyAsync(t_h, t.p, (size_t)nrays * 8, cudaMemcpyDeviceToHost, s));
+  ILG_CUDA(cudaStreamSynchronize(s));
+  return read_device_errors(c);
+}
+
+int bvh_render(Context& c, int mode, double az_deg, double el_deg, int width, int height, int32_t* out_h) {
+  cudaStream_t s = c.stream;
+  std::vector<float4> cen((size_t)c.nt);
+  ILG_CUDA(cudaMemcpyAsync(cen.data(), c.cen.p, (size_t)c.nt * sizeof(float4), cudaMemcpyDeviceToHost, s));
+  ILG_CUDA(cudaStreamSynchronize(s));
+  double mx = 0, my = 0, mz = 0;
+  for (const float4& q : cen) { mx += q.x; my += q.y; mz += q.z; }
+  mx /= c.nt; my /= c.nt; mz /= c.nt;
+  double r_model = 0;
+  for (const float4& q : cen)
+    r_model = std::max(r_model, std::sqrt((q.x - mx) * (q.x - mx) + (q.y - my) * (q.y - my) + (q.z - mz) * (q.z - mz)));
+  RenderCam cam{};
+  cam.mode = mode; cam.width = width; cam.height = height;
+  cam.rad = 1.1 * r_model;
+  cam.aspect = (double)width / height;
+  const double D2R = 3.141592653589793 / 180.0;
+  cam.az = az_deg * D2R;
+  cam.el = el_deg * D2R;
+  cam.cx = (float)mx; cam.cy = (float)my; cam.cz = (float)mz;
+  if (mode == 0) {
+    auto sph = [](double phi, double theta, double r, float* v) {
+      v[0] = (float)(r * std::cos(phi) * std::sin(theta));
+      v[1] = (float)(r * std::sin(phi) * std::sin(theta));
+      v[2] = (float)(r * std::cos(theta));
+    };
+    float p[3], up[3];
+    sph(cam.az, cam.el, cam.rad, p);
+    sph(cam.az, cam.el - 3.141592653589793 / 2, 1.0, up);
+    float pl = std::sqrt(p[0] * p[0] + p[1] * p[1] + p[2] * p[2]);
+    float e[3] = {-p[0] / pl, -p[1] / pl, -p[2] / pl};
+    cam.ex = e[0]; cam.ey = e[1]; cam.ez = e[2];
+    cam.ux = up[0]; cam.uy = up[1]; cam.uz = up[2];
+    cam.rx = e[1] * up[2] - e[2] * up[1];   // n_eye x n_up
+    cam.ry = e[2] * up[0] - e[0] * up[2];
+    cam.rz = e[0] * up[1] - e[1] * up[0];
+    cam.px = p[0] + cam.cx; cam.py = p[1] + cam.cy; cam.pz = p[2] + cam.cz;
+  }
+  const int64_t npx = (int64_t)width * height;
+  dbuf<int32_t> dout;
+  ILG_TRY(dout.alloc(npx));
+  k_render<<<div_up(npx, 128), 128, 0, s>>>(c.nodes.p, c.tri_s.p, c.root, cam, dout.p, c.derr.p);
+  ILG_CUDA(cudaGetLastError());
+  ILG_CUDA(cudaMemcpyAsync(out_h, dout.p, (size_t)npx * 4, cudaMemcpyDeviceToHost, s));
   ILG_CUDA(cudaStreamSynchronize(s));
   return read_device_errors(c);
 }

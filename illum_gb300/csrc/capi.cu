@@ -430,6 +430,14 @@ int ilg_trace(ilg_ctx* ctx, int nrays, const float* orig, const float* dir, int 
   return bvh_trace(ctx->c, nrays, orig, dir, any_hit, hit, t);
 }
 
+int ilg_render(ilg_ctx* ctx, int mode, double az_deg, double el_deg, int width, int height, int32_t* facet_out) {
+  if (!ctx || !facet_out || (mode != 0 && mode != 1) || width < 2 || height < 2) {
+    set_error("invalid render arguments");
+    return ILG_ERR_ARG;
+  }
+  return bvh_render(ctx->c, mode, az_deg, el_deg, width, height, facet_out);
+}
+
 int ilg_compute_F(ilg_ctx* ctx, const double* albedo, double albedo_scalar, double offset, int64_t* nnz, int64_t* rays) {
   if (!ctx) { set_error("ctx is NULL"); return ILG_ERR_ARG; }
   invalidate_graph(ctx->c);

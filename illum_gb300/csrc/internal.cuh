@@ -265,6 +265,7 @@ int bvh_trace(Context& c, int nrays, const float* orig_h, const float* dir_h, in
               double* t_h);
 int horizons_build(Context& c, int nphi, double theta_eps, double offset);
 int horizons_f32(Context& c);   // H32 and hmm32 from H
+int bvh_render(Context& c, int mode, double az_deg, double el_deg, int width, int height, int32_t* out_h);
 int form_factors_build(Context& c, const double* albedo_h, double albedo_scalar, double offset,
                        double cutoff, int64_t* rays_out);
 

@@ -84,6 +84,15 @@ int ilg_ctx_info(const ilg_ctx* ctx, int64_t* bvh_nodes, int* bvh_depth);
 int ilg_trace(ilg_ctx* ctx, int nrays, const float* orig, const float* dir, int any_hit,
               int32_t* hit, double* t);
 
+/* ---- map renderer (illum_renderer_cli) ------------------------------------ */
+/* One closest-hit ray per pixel (src/cpp/illum_renderer_cli.cpp:228-276):
+ * mode 0 orthographic view from azimuth/elevation (degrees) at 1.1 x the
+ * model radius, mode 1 equal-area cylindrical map. facet_out: height x width
+ * row-major facet indices, -1 where no facet is hit. Colouring and the
+ * image file are the caller's (illum_gb300.render). */
+int ilg_render(ilg_ctx* ctx, int mode, double az_deg, double el_deg, int width, int height,
+               int32_t* facet_out);
+
 /* ---- form factors (compute_F) -------------------------------------------- */
 /* Visibility + form factors, rows scaled by albedo (albedo: nt values, or
  * NULL to use albedo_scalar). Result stays on the device as CSR by receiver
