@@ -77,3 +77,16 @@ def test_obj_normals_follow_vertex_normals_and_scale(tmp_path):
     assert F2.tolist() == [[4, 5, 6]]
     # (v1 - v0) x (v2 - v0) = (0,100,0) x (100,0,0) = -z; vertex normals +z: flipped
     assert np.allclose(N2, [[0, 0, 1]])
+
+
+def test_cli_yaml_config_and_overrides(tmp_path):
+    from illum_gb300 import cli
+    y = tmp_path / "job.yaml"
+    y.write_text("# thermal job\nnphi: 64\nthermal: true\nradiosity: yes\ndt: 120.5\n"
+                 "depths: [0.01, 0.02, 0.05]\nrhoc:\n  - 1.0e6\nT0: init.bin\nsun_unit: km\n")
+    cfg = cli.parse_yaml(y.read_text())
+    assert cfg == {"nphi": 64, "thermal": True, "radiosity": True, "dt": 120.5, "depths": [0.01, 0.02, 0.05],
+                   "rhoc": [1.0e6], "T0": "init.bin", "sun_unit": "km"}
+    a = cli.resolve(["--config", str(y), "--nphi", "32", "--task", "horizons"])
+    assert a.nphi == 32 and a.thermal is True and a.depths == [0.01, 0.02, 0.05] and a.rhoc == [1.0e6]
+    assert a.T0 == "init.bin" and a.sun_unit == "km" and a.task == "horizons"

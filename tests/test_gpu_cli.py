@@ -1,0 +1,52 @@
+"""The task front-end end to end on a small OBJ: horizons, form factors and
+a radiosity + thermal run write the reference's output files, with the
+values the library's API gives."""
+import numpy as np
+import pytest
+
+from illum_gb300 import armaio, meshgen
+
+pytestmark = pytest.mark.gpu
+
+
+def _write_obj(path, v, f):
+    n = v / np.linalg.norm(v, axis=1, keepdims=True)
+    with open(path, "w") as fh:
+        for p in v * 100.0:                     # the reader divides by 100
+            fh.write("v %.9g %.9g %.9g\n" % tuple(p))
+        for q in n:
+            fh.write("vn %.9g %.9g %.9g\n" % tuple(q))
+        for t in f + 1:
+            fh.write("f %d//%d %d//%d %d//%d\n" % (t[0], t[0], t[1], t[1], t[2], t[2]))
+
+
+def test_cli_tasks(ilg, tmp_path):
+    from illum_gb300 import cli
+    v, f = meshgen.icosphere_craters(2, seed=3, n_craters=4, dmin_m=150.0, dmax_m=400.0)
+    obj = tmp_path / "shape.obj"
+    _write_obj(str(obj), v.astype(np.float64), f)
+    out = tmp_path / "out"
+    cli.main(["--task", "horizons", "--path", str(obj), "--nphi", "16", "--output_dir", str(out)])
+    H = armaio.load(str(out / "horizons.bin"))
+    V, Fc, N = meshgen.load_obj(str(obj))
+    ctx = ilg.IllumContext(V, Fc, N)
+    ctx.make_horizons(nphi=16)
+    assert np.array_equal(H, ctx.horizons)
+    cli.main(["--task", "form_factors", "--path", str(obj), "--albedo", "0.1", "--output_dir", str(out)])
+    rp, c, x, _ = armaio.load_sparse(str(out / "form_factors.bin"))
+    rp2, c2, x2 = ctx.compute_F(albedo=0.1)
+    assert np.array_equal(rp, rp2) and np.array_equal(c, c2) and np.array_equal(x, x2)
+    suns = meshgen.spin_sun_positions(8, 6 * 3600.0, 600.0) * 1000.0     # metres, as sun_unit m
+    np.savetxt(str(tmp_path / "sun.txt"), suns)
+    cfg = tmp_path / "job.yaml"
+    cfg.write_text("radiosity: true\nthermal: true\nnphi: 16\ndt: 600\nti: 300\nrhoc: 1.05e6\nT0: 220\n"
+                   "depths: [0.002, 0.005, 0.01, 0.02, 0.05, 0.1]\nrecord_therm_stats: true\n"
+                   f"sun_pos_file: {tmp_path / 'sun.txt'}\nform_factors_file: {out / 'form_factors.bin'}\n"
+                   f"horizon_file: {out / 'horizons.bin'}\noutput_dir: {out}\n")
+    res = cli.main(["--task", "radiosity", "--path", str(obj), "--config", str(cfg)])
+    for name in ("rad", "rad_avg", "therm", "therm_avg", "therm_max", "therm_stats", "therm_energy"):
+        assert (out / (name + ".bin")).exists(), name
+    therm = armaio.load(str(out / "therm.bin")).ravel()
+    assert therm.shape == (Fc.shape[0],) and np.all(np.isfinite(therm))
+    assert armaio.load(str(out / "therm_stats.bin")).shape == (8, 12)
+    assert np.array_equal(res["therm"], therm)
