@@ -31,6 +31,7 @@
 // (linearised or Newton) is solved in FP64. The mixed step uses the same
 // increment form in plain FP32; the standalone column entry points
 // (conductionq_, ilg_conductionq_batch) run the reference's rows in FP64.
+#include <atomic>
 #include <cmath>
 #include <mutex>
 #include <type_traits>
@@ -407,15 +408,18 @@ int launch_conduct(const StepView& v, const double* Q, int upd, int nz_max, cuda
 int conduction_step_threads() { return COND_STEP_THREADS; }
 
 int conduction_setup() {
-  static bool done = false;
-  if (done) return ILG_OK;
+  static std::mutex mu;
+  static std::atomic<bool> done{false};
+  if (done.load(std::memory_order_acquire)) return ILG_OK;
+  std::lock_guard<std::mutex> lock(mu);
+  if (done.load(std::memory_order_relaxed)) return ILG_OK;
   ILG_CUDA(cudaFuncSetAttribute(k_conduct<double, true, COND_THREADS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)SMEM_LIMIT));
   ILG_CUDA(cudaFuncSetAttribute(k_conduct<dfloat, true, COND_STEP_THREADS>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_LIMIT));
   ILG_CUDA(cudaFuncSetAttribute(k_conduct<float, true, COND_STEP_THREADS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)SMEM_LIMIT));
-  done = true;
+  done.store(true, std::memory_order_release);
   return ILG_OK;
 }
 

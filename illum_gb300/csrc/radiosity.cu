@@ -41,7 +41,9 @@
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
+#include <mutex>
 #include <vector>
 
 #include "internal.cuh"
@@ -627,11 +629,15 @@ __global__ void k_tile_scale(const uint32_t* __restrict__ t_row, const uint32_t*
 }
 
 int g_rad_nsm = 0, g_rad_per_sm64 = 0, g_rad_per_smm = 0;
+std::atomic<bool> g_rad_ready{false};
+std::mutex g_rad_mu;
 
 // Once per process, before any capture: the kernels' shared-memory opt-in
-// and their co-residency.
+// and their co-residency. Safe to call from several host threads.
 int radiosity_setup() {
-  if (g_rad_nsm) return ILG_OK;
+  if (g_rad_ready.load(std::memory_order_acquire)) return ILG_OK;
+  std::lock_guard<std::mutex> lock(g_rad_mu);
+  if (g_rad_ready.load(std::memory_order_relaxed)) return ILG_OK;
   int dev, nsm;
   ILG_CUDA(cudaGetDevice(&dev));
   ILG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
@@ -641,6 +647,7 @@ int radiosity_setup() {
   ILG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_rad_per_smm, k_radiosity_mixed, RAD_THREADS, RAD_SMEM));
   if (g_rad_per_sm64 < 1 || g_rad_per_smm < 1) { set_error("radiosity kernel cannot be resident"); return ILG_ERR_CUDA; }
   g_rad_nsm = nsm;
+  g_rad_ready.store(true, std::memory_order_release);
   return ILG_OK;
 }
 

@@ -2,16 +2,19 @@
 
 A job is a shape model with a spin state and a material: its mesh is
 generated, its LBVH, horizons and form factors are built, and its time
-steps run until its last sun position. Requests arrive over time; a setup
-thread admits them in arrival order while the estimated device footprint of
-the admitted jobs stays under a budget, and builds each one on its own CUDA
-stream (overlapping the steps already running). The stepping loop keeps all
-admitted jobs in one batch (ilg_batch_*): one launch per phase steps every
-job, each at its own dt, depth grid and sun table. When jobs finish or new
-ones become ready, the batch state is written back to the jobs' contexts and
-a new batch is formed with the current set; finished jobs are read out and
-their memory released. A job's results do not depend on which other jobs
-shared its batch (bitwise, for a fixed precision).
+steps run until its last sun position. Requests arrive over time; an
+admission thread admits them in arrival order while the estimated device
+footprint of the admitted jobs stays under a budget and hands each to a pool
+of set-up workers, which build jobs concurrently, each context on its own
+CUDA stream (overlapping one another and the steps already running). The
+stepping loop keeps the admitted jobs in one batch (ilg_batch_*): one launch
+per phase steps every job, each at its own dt, depth grid and sun table. A
+job that finishes is read out and switched off in place; the batch is
+rebuilt (state written back to the contexts, a new batch formed, finished
+jobs' memory released) when new jobs are waiting, at most every
+min_rebuild_s, or when nothing in it is running. A job's results do not
+depend on which other jobs shared its batch (bitwise, for a fixed
+precision).
 """
 from __future__ import annotations
 
@@ -19,6 +22,7 @@ import math
 import queue
 import threading
 import time
+from concurrent.futures import ThreadPoolExecutor
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -55,6 +59,7 @@ class Job:
     t_ready: float = 0.0
     t_done: float = 0.0
     tsurf: np.ndarray = None
+    finished: bool = False
 
 
 def request_stream(n: int, rate_hz: float = 20.0, seed: int = 4242, levels=(3, 4, 5, 6, 7),
@@ -94,8 +99,10 @@ def footprint_bytes(level: int, nz: int, nphi: int, precision: int) -> int:
 
 class Server:
     def __init__(self, budget_bytes: int, precision: int = ig.PREC_MIXED, chunk_steps: int = 30, nphi: int = 32,
-                 tol: float = 1e-3, solar: float = 1361.0):
+                 tol: float = 1e-3, solar: float = 1361.0, setup_workers: int = 4, min_rebuild_s: float = 0.25):
         self.budget = budget_bytes
+        self.workers = max(1, setup_workers)
+        self.min_rebuild_s = min_rebuild_s
         self.precision = precision
         self.chunk = chunk_steps
         self.nphi = nphi
@@ -127,7 +134,18 @@ class Server:
                           precision=self.precision, coupling=ig.COUPLE_DIRECT)
         return Job(req=r, ctx=ctx, tm=tm, opts=opts, nfaces=f.shape[0])
 
+    def _build_one(self, r: Request, need: int):
+        try:
+            job = self.build_job(r)
+            job.footprint = need
+            job.t_ready = time.perf_counter() - self.t0
+            self.ready.put(job)
+        except Exception as e:   # surfaced by run()
+            self.error = e
+            self.ready.put(None)
+
     def _setup_loop(self, reqs):
+        pool = ThreadPoolExecutor(max_workers=self.workers)
         try:
             for r in reqs:
                 wait = r.arrival - (time.perf_counter() - self.t0)
@@ -138,75 +156,87 @@ class Server:
                     while self.used + need > self.budget and self.used > 0:
                         self.lock.wait()
                     self.used += need
-                job = self.build_job(r)
-                job.footprint = need
-                job.t_ready = time.perf_counter() - self.t0
-                self.ready.put(job)
+                if self.error:
+                    break
+                pool.submit(self._build_one, r, need)
         except Exception as e:   # surfaced by run()
             self.error = e
         finally:
+            pool.shutdown(wait=True)
             self.ready.put(None)
 
     # -------------------------------------------------------------- stepping
+    def _release(self, j: Job) -> None:
+        j.ctx.close()
+        j.ctx = j.tm = None
+        with self.lock:
+            self.used -= j.footprint
+            self.lock.notify_all()
+
     def run(self, reqs):
         """Serve the request stream; returns the finished jobs."""
         self.t0 = time.perf_counter()
         th = threading.Thread(target=self._setup_loop, args=(reqs,), daemon=True)
         th.start()
-        active: list = []
+        active: list = []          # jobs in the current batch (finished ones switched off)
+        pending: list = []         # built, waiting for the next batch
         batch = None
+        last_rebuild = -1e30
         setup_open = True
         self.rebuilds = 0
-        while setup_open or active:
-            changed = False
-            # take whatever is ready (block only when idle)
+        while True:
+            running = [j for j in active if not j.finished]
+            # take whatever is ready (block only when there is nothing to step)
             while True:
                 try:
-                    job = self.ready.get(block=not active and setup_open, timeout=0.05)
+                    job = self.ready.get(block=not running and not pending and setup_open, timeout=0.05)
                 except queue.Empty:
                     break
                 if job is None:
                     setup_open = False
                     break
-                active.append(job)
-                changed = True
-            if not active:
-                continue
-            if changed or batch is None:
+                pending.append(job)
+            if self.error:
+                break
+            now = time.perf_counter() - self.t0
+            if (pending and (not running or now - last_rebuild >= self.min_rebuild_s)) or \
+                    (batch is not None and not running):
                 if batch is not None:
                     batch.sync()
                     batch.close()
-                batch = ig.Batch([j.ctx for j in active], [j.opts for j in active])
-                self.rebuilds += 1
-            steps = min(self.chunk, max(1, min(j.req.nsteps - self._steps_done(j) for j in active)))
+                    batch = None
+                for j in active:
+                    if j.finished:
+                        self._release(j)
+                active = running + pending
+                pending = []
+                running = list(active)
+                if active:
+                    batch = ig.Batch([j.ctx for j in active], [j.opts for j in active])
+                    self.rebuilds += 1
+                    last_rebuild = now
+            if not running:
+                if not setup_open and not pending:
+                    break
+                continue
+            steps = min(self.chunk, max(1, min(j.req.nsteps - self._steps_done(j) for j in running)))
             batch.run(steps)
             act, done_steps, _ = batch.status()
-            finished = [k for k, j in enumerate(active) if done_steps[k] >= j.req.nsteps]
-            for j, d in zip(active, done_steps):
+            now = time.perf_counter() - self.t0
+            for k, (j, d) in enumerate(zip(active, done_steps)):
                 j._done = int(d)
-            if finished:
-                now = time.perf_counter() - self.t0
-                for k in finished:
-                    j = active[k]
+                if not j.finished and d >= j.req.nsteps:
                     j.tsurf = batch.tsurf(k)
                     j.t_done = now
-                batch.sync()
-                batch.close()
-                batch = None
-                keep = []
-                for k, j in enumerate(active):
-                    if k in finished:
-                        j.ctx.close()
-                        j.ctx = j.tm = None
-                        self.done.append(j)
-                        with self.lock:
-                            self.used -= j.footprint
-                            self.lock.notify_all()
-                    else:
-                        keep.append(j)
-                active = keep
+                    j.finished = True
+                    batch.set_active(k, False)
+                    self.done.append(j)
         if batch is not None:
+            batch.sync()
             batch.close()
+        for j in active:
+            if j.ctx is not None:
+                self._release(j)
         th.join()
         if self.error:
             raise self.error

@@ -6,12 +6,17 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def test_serving_results_equal_alone(ilg):
+@pytest.mark.parametrize("workers,min_rebuild_s", [(1, 0.0), (4, 0.25)])
+def test_serving_results_equal_alone(ilg, workers, min_rebuild_s):
+    """Jobs built concurrently, finished members switched off in place and
+    batches re-formed: every job's final surface temperature equals the
+    job run alone, bitwise."""
     from illum_gb300 import serve
     reqs = serve.request_stream(8, rate_hz=200.0, levels=(2, 3), rotations=(1, 2), steps_per_rot=(40, 60))
-    srv = serve.Server(budget_bytes=int(2e9), chunk_steps=7)
+    srv = serve.Server(budget_bytes=int(2e9), chunk_steps=7, setup_workers=workers, min_rebuild_s=min_rebuild_s)
     done = srv.run(reqs)
     assert len(done) == len(reqs) and srv.rebuilds >= 2
+    assert sorted(j.req.rid for j in done) == list(range(len(reqs)))
     for j in done:
         alone = srv.build_job(j.req)
         h = alone.ctx.run_steps(alone.opts, 0, j.req.nsteps, record_tsurf=True)
@@ -22,7 +27,7 @@ def test_admission_respects_budget(ilg):
     from illum_gb300 import serve
     reqs = serve.request_stream(4, rate_hz=1000.0, levels=(3,), rotations=(1, 1), steps_per_rot=(30, 31))
     one = serve.footprint_bytes(3, 80, 32, ilg.PREC_MIXED)
-    srv = serve.Server(budget_bytes=int(1.5 * one), chunk_steps=10)
+    srv = serve.Server(budget_bytes=int(1.5 * one), chunk_steps=10, setup_workers=4)
     seen = []
     orig = srv.build_job
 
