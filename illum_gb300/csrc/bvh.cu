@@ -173,13 +173,25 @@ __device__ __forceinline__ NodeBoxes load_node(const float4* __restrict__ nodes,
 }
 
 // Closest hit under geom.h's mt64 (smallest t, ties to the smaller original
-// index), with mt32_classify as a conservative filter. Returns the original
-// facet index or -1; sets *err on stack overflow.
+// index). Returns the original facet index or -1; sets *err on stack
+// overflow; *t_out (if given) receives the hit's mt64 t.
+//
+// The FP64 test runs only where single precision cannot decide. A leaf that
+// mt32_classify calls a certain hit comes with an enclosure [tlo, thi] of its
+// mt64 t; the best hit so far is kept as such an enclosure [blo, bhi] and
+// compared by intervals: tlo > bhi means certainly farther, thi < blo
+// certainly closer (so no tie is possible). Only when the intervals overlap,
+// or the leaf is undecided, are the exact t of both hits computed and
+// compared with the tie rule. The argmin of (t, index) over all mt64 hits is
+// therefore the one an all-FP64 traversal finds; rays aimed at facet
+// centroids almost never need the FP64 path.
 __device__ int trace_closest(const float4* __restrict__ nodes, const float4* __restrict__ tri_s, int root,
                              f3 o, f3 d, double* t_out, int* err) {
   ray_inv ri = make_ray_inv(o, d);
-  double best = 1e300;
-  int besti = -1;
+  int besti = -1, bk = 0;
+  float blo = 3.0e38f, bhi = 3.0e38f;   // encloses the best hit's mt64 t
+  double bt = 0.0;                      // that t, once computed (bex)
+  bool bex = false;
   float tmaxf = 3.0e38f;
   int stack[TRACE_STACK];
   int sp = 0;
@@ -192,13 +204,33 @@ __device__ int trace_closest(const float4* __restrict__ nodes, const float4* __r
       int idx = __float_as_int(a.w);
       float tlo, thi;
       int cls = mt32_classify(o, d, v0, v1, v2, &tlo, &thi);
-      if (cls != 0 && !(cls == 1 && (double)tlo > best)) {
+      bool take = false;
+      if (cls == 1 && (besti < 0 || thi < blo)) {
+        take = true;                    // certainly the closest so far
+        bex = false;
+        blo = tlo;
+        bhi = thi;
+      } else if (cls == 2 || (cls == 1 && !(tlo > bhi))) {
         double th;
-        if (mt64(o, d, v0, v1, v2, &th) && (th < best || (th == best && idx < besti))) {
-          best = th;
-          besti = idx;
-          tmaxf = (float)best * 1.000001f + 1e-30f;
+        if (mt64(o, d, v0, v1, v2, &th)) {
+          if (besti >= 0 && !bex) {     // exact t of the current best
+            float4 ba = __ldg(&tri_s[3 * bk]), bb = __ldg(&tri_s[3 * bk + 1]), bc = __ldg(&tri_s[3 * bk + 2]);
+            bex = mt64(o, d, f3of(ba), f3of(bb), f3of(bc), &bt);
+          }
+          if (besti < 0 || th < bt || (th == bt && idx < besti)) {
+            take = true;
+            bex = true;
+            bt = th;
+            float tf = (float)th;
+            blo = tf * (1.0f - 2.4e-7f);
+            bhi = tf * (1.0f + 2.4e-7f) + 1e-37f;
+          }
         }
+      }
+      if (take) {
+        besti = idx;
+        bk = k;
+        tmaxf = bhi * 1.000001f + 1e-30f;
       }
       if (sp == 0) break;
       node = stack[--sp];
@@ -221,7 +253,13 @@ __device__ int trace_closest(const float4* __restrict__ nodes, const float4* __r
       node = stack[--sp];
     }
   }
-  if (t_out) *t_out = best;
+  if (t_out) {
+    if (besti >= 0 && !bex) {
+      float4 ba = __ldg(&tri_s[3 * bk]), bb = __ldg(&tri_s[3 * bk + 1]), bc = __ldg(&tri_s[3 * bk + 2]);
+      mt64(o, d, f3of(ba), f3of(bb), f3of(bc), &bt);
+    }
+    *t_out = besti >= 0 ? bt : 1e300;
+  }
   return besti;
 }
 
