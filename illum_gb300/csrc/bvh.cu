@@ -416,22 +416,58 @@ __device__ __forceinline__ float box_dist2(f3 p, f3 lo, f3 hi) {
   return dx * dx + dy * dy + dz * dz;
 }
 
+// Up to FF_SPLIT disjoint subtrees covering every leaf (breadth-first from
+// the root), so that one source's query splits into FF_SPLIT work items.
+constexpr int FF_SPLIT = 32;
+
+__global__ void k_frontier(const float4* __restrict__ nodes, int root, int* front, int* nfront) {
+  int f[FF_SPLIT];
+  int n = 1;
+  f[0] = root;
+  bool grew = true;
+  while (grew) {
+    grew = false;
+    for (int k = 0; k < n && n < FF_SPLIT; ++k) {
+      if (f[k] < 0) continue;
+      float4 d = __ldg(&nodes[4 * f[k] + 3]);
+      f[k] = __float_as_int(d.x);
+      f[n++] = __float_as_int(d.y);
+      grew = true;
+    }
+  }
+  for (int k = 0; k < FF_SPLIT; ++k) front[k] = k < n ? f[k] : 0;
+  *nfront = n;
+}
+
+// Work item (source j, subtree sub), stored at t = (j - j0) FF_SPLIT + sub
+// so that a source's candidates are contiguous. Threads run subtree-major:
+// a warp holds consecutive sources on the same subtree (similar queries).
+// Counting writes count[t]; FILL writes the item's candidates from
+// offs[t] - base0 on.
 template <bool FILL>
-__global__ void k_candidates(const float4* __restrict__ nodes, const float4* __restrict__ tri_s, int root,
-                             const float4* __restrict__ cen, const float4* __restrict__ nrm, int nt, float r_max,
-                             float slack, float cut2, float box_cut2, uint32_t* count,
-                             const unsigned long long* __restrict__ offs, int32_t* cand_i, int32_t* cand_j,
-                             int* derr) {
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= nt) return;
+__global__ void k_candidates(const float4* __restrict__ nodes, const float4* __restrict__ tri_s,
+                             const int* __restrict__ front, const int* __restrict__ nfront,
+                             const float4* __restrict__ cen, const float4* __restrict__ nrm, int j0, int j1,
+                             float r_max, float slack, float cut2, float box_cut2, uint32_t* count,
+                             const unsigned long long* __restrict__ offs, unsigned long long base0, int32_t* cand_i,
+                             int32_t* cand_j, int* derr) {
+  const int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int nsrc = j1 - j0;
+  const int sub = (int)(u / nsrc), j = j0 + (int)(u % nsrc);
+  if (sub >= FF_SPLIT) return;
+  const int64_t t = (int64_t)(j - j0) * FF_SPLIT + sub;
+  uint32_t cnt = 0;
+  if (sub >= *nfront) {
+    if (!FILL) count[t] = 0;
+    return;
+  }
   float4 cj4 = cen[j], nj4 = nrm[j];
   f3 p_j = f3of(cj4), n_j = f3of(nj4);
   float lim = -r_max - slack;
-  uint32_t cnt = 0;
-  unsigned long long base = FILL ? offs[j] : 0ull;
+  unsigned long long base = FILL ? offs[t] - base0 : 0ull;
   int stack[TRACE_STACK];
   int sp = 0;
-  int node = root;
+  int node = front[sub];
   for (;;) {
     if (node < 0) {
       int k = ~node;
@@ -472,27 +508,39 @@ __global__ void k_candidates(const float4* __restrict__ nodes, const float4* __r
       node = stack[--sp];
     }
   }
-  if (!FILL) count[j] = cnt;
+  if (!FILL) count[t] = cnt;
 }
 
 // One visibility ray per candidate pair (src/cpp/illum.cpp:72-83): from the
-// offset centroid q_j towards p_i; the key packs (hit row, source column),
-// or the sentinel nt << bits when nothing but j (or nothing) is hit.
+// offset centroid q_j towards p_i. A ray that hits a facet h other than j
+// yields the key (h << bits) | j. Consecutive pairs share their source, so a
+// warp's keys repeat (rays stopped by the same occluder): each distinct key
+// of a warp is appended once to ukeys (one atomic per warp); the order of
+// ukeys is irrelevant, it is sorted and made unique afterwards. The launch
+// covers whole warps (no early exit before the warp-wide vote).
 __global__ void k_vis_rays(const float4* __restrict__ nodes, const float4* __restrict__ tri_s, int root,
                            const float4* __restrict__ cen, const float4* __restrict__ nrm, int64_t npairs,
                            const int32_t* __restrict__ cand_i, const int32_t* __restrict__ cand_j, float offset,
-                           int bits, int nt, unsigned long long* keys, int* derr) {
+                           int bits, unsigned long long* ukeys, unsigned long long* ucount, int* derr) {
   int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= npairs) return;
-  int i = cand_i[k], j = cand_j[k];
-  f3 p_j = f3of(cen[j]), n_j = f3of(nrm[j]);
-  f3 q_j = add(p_j, scl(n_j, offset));
-  f3 d = normalize(sub(f3of(cen[i]), q_j));
-  int h = trace_closest(nodes, tri_s, root, q_j, d, nullptr, &derr[DERR_STACK]);
-  unsigned long long key;
-  if (h < 0 || h == j) key = (unsigned long long)nt << bits;
-  else key = ((unsigned long long)h << bits) | (unsigned long long)j;
-  keys[k] = key;
+  const unsigned long long NONE = ~0ull;
+  unsigned long long key = NONE;
+  if (k < npairs) {
+    int i = cand_i[k], j = cand_j[k];
+    f3 p_j = f3of(cen[j]), n_j = f3of(nrm[j]);
+    f3 q_j = add(p_j, scl(n_j, offset));
+    f3 d = normalize(sub(f3of(cen[i]), q_j));
+    int h = trace_closest(nodes, tri_s, root, q_j, d, nullptr, &derr[DERR_STACK]);
+    if (h >= 0 && h != j) key = ((unsigned long long)h << bits) | (unsigned long long)j;
+  }
+  const int lane = threadIdx.x & 31;
+  unsigned same = __match_any_sync(0xffffffffu, key);
+  bool lead = key != NONE && (__ffs(same) - 1) == lane;
+  unsigned vote = __ballot_sync(0xffffffffu, lead);
+  unsigned long long base = 0;
+  if (lane == 0 && vote) base = atomicAdd(ucount, (unsigned long long)__popc(vote));
+  base = __shfl_sync(0xffffffffu, base, 0);
+  if (lead) ukeys[base + __popc(vote & ((1u << lane) - 1u))] = key;
 }
 
 // After sorting: first occurrence of each (row, col) -> form factor
@@ -508,7 +556,7 @@ __global__ void k_ff_values(const unsigned long long* __restrict__ keys, int64_t
   int i = (int)(key >> bits), j = (int)(key & mask);
   uint32_t kp = 0;
   double F = 0.0;
-  if (i < nt && (k == 0 || keys[k - 1] != key)) {
+  if (k == 0 || keys[k - 1] != key) {
     F = form_factor(f3of(cen[i]), f3of(nrm[i]), f3of(cen[j]), f3of(nrm[j]), area[j]);
     if (isnan(F)) {
       atomicExch(&derr[DERR_NAN], 1);
@@ -806,14 +854,17 @@ int horizons_f32(Context& c) {
   return ILG_OK;
 }
 
+// Candidate pairs held on the device at once (8 bytes each).
+constexpr int64_t FF_CHUNK = int64_t(1) << 29;
+
 int form_factors_build(Context& c, const double* albedo_h, double albedo_scalar, double offset, double cutoff,
                        int64_t* rays_out) {
   cudaStream_t s = c.stream;
   int nt = c.nt;
   dbuf<uint32_t> cnt;
   dbuf<unsigned long long> offs;
-  ILG_TRY(cnt.alloc(nt));
-  ILG_TRY(offs.alloc((size_t)nt + 1));
+  ILG_TRY(cnt.alloc((size_t)nt * FF_SPLIT));
+  ILG_TRY(offs.alloc((size_t)nt * FF_SPLIT));
   float slack = 1e-5f * c.scene_mag;
   const float cut2 = cutoff > 0.0 ? (float)(cutoff * cutoff) : -1.0f;
   // box test: the squared distance to a box is computed in float with at
@@ -821,44 +872,82 @@ int form_factors_build(Context& c, const double* albedo_h, double albedo_scalar,
   // cutoff reachable
   const float box_cut2 = cutoff > 0.0 ? (float)((cutoff + 1e-5 * c.scene_mag) * (cutoff + 1e-5 * c.scene_mag)) * 1.0001f
                                       : -1.0f;
-  k_candidates<false><<<div_up(nt, 128), 128, 0, s>>>(c.nodes.p, c.tri_s.p, c.root, c.cen.p, c.nrm.p, nt, c.r_max,
-                                                      slack, cut2, box_cut2, cnt.p, nullptr, nullptr, nullptr,
-                                                      c.derr.p);
+  const int64_t nitems = (int64_t)nt * FF_SPLIT;
+  dbuf<int> front;
+  ILG_TRY(front.alloc(FF_SPLIT + 1));
+  k_frontier<<<1, 1, 0, s>>>(c.nodes.p, c.root, front.p, front.p + FF_SPLIT);
   ILG_CUDA(cudaGetLastError());
-  ILG_TRY(scan_exclusive_u32_to_u64(cnt.p, offs.p, nt, c.scan, s));
-  unsigned long long last_off = 0;
+  k_candidates<false><<<div_up(nitems, 128), 128, 0, s>>>(c.nodes.p, c.tri_s.p, front.p, front.p + FF_SPLIT, c.cen.p,
+                                                          c.nrm.p, 0, nt, c.r_max, slack, cut2, box_cut2, cnt.p,
+                                                          nullptr, 0ull, nullptr, nullptr, c.derr.p);
+  ILG_CUDA(cudaGetLastError());
+  ILG_TRY(scan_exclusive_u32_to_u64(cnt.p, offs.p, nitems, c.scan, s));
+  // per-source offsets: every FF_SPLIT-th item offset, and the total
+  std::vector<unsigned long long> offs_h((size_t)nt + 1);
   uint32_t last_cnt = 0;
-  ILG_CUDA(cudaMemcpyAsync(&last_off, offs.p + (nt - 1), 8, cudaMemcpyDeviceToHost, s));
-  ILG_CUDA(cudaMemcpyAsync(&last_cnt, cnt.p + (nt - 1), 4, cudaMemcpyDeviceToHost, s));
+  unsigned long long last_off = 0;
+  ILG_CUDA(cudaMemcpy2DAsync(offs_h.data(), 8, offs.p, 8 * FF_SPLIT, 8, nt, cudaMemcpyDeviceToHost, s));
+  ILG_CUDA(cudaMemcpyAsync(&last_off, offs.p + (nitems - 1), 8, cudaMemcpyDeviceToHost, s));
+  ILG_CUDA(cudaMemcpyAsync(&last_cnt, cnt.p + (nitems - 1), 4, cudaMemcpyDeviceToHost, s));
   ILG_CUDA(cudaStreamSynchronize(s));
-  int64_t npairs = (int64_t)last_off + last_cnt;
+  offs_h[nt] = last_off + last_cnt;
+  const int64_t npairs = (int64_t)offs_h[nt];
   if (rays_out) *rays_out = npairs;
   int bits = 1;
-  while ((1LL << bits) <= nt) ++bits;   // row and column fields; row nt is the sentinel
-  dbuf<int32_t> ci, cj;
-  dbuf<unsigned long long> keys;
-  ILG_TRY(ci.alloc(npairs > 0 ? npairs : 1));
-  ILG_TRY(cj.alloc(npairs > 0 ? npairs : 1));
-  ILG_TRY(keys.alloc(npairs > 0 ? npairs : 1));
+  while ((1LL << bits) < nt) ++bits;   // row and column fields
+
+  // Sources in chunks of at most FF_CHUNK pairs (a source with more pairs is
+  // a chunk of its own): candidate pairs exist for one chunk at a time.
+  std::vector<int> cut{0};
+  int64_t cap = 1;
+  while (cut.back() < nt) {
+    int a = cut.back(), b = a + 1;
+    while (b < nt && (int64_t)(offs_h[b + 1] - offs_h[a]) <= FF_CHUNK) ++b;
+    cap = std::max<int64_t>(cap, (int64_t)(offs_h[b] - offs_h[a]));
+    cut.push_back(b);
+  }
   c.have_F = false;
   c.ntiles = 0;
-  if (npairs > 0) {
-    k_candidates<true><<<div_up(nt, 128), 128, 0, s>>>(c.nodes.p, c.tri_s.p, c.root, c.cen.p, c.nrm.p, nt, c.r_max,
-                                                       slack, cut2, box_cut2, nullptr, offs.p, ci.p, cj.p,
-                                                       c.derr.p);
+  dbuf<int32_t> ci, cj;
+  dbuf<unsigned long long> ukeys, ucount;
+  ILG_TRY(ci.alloc(cap));
+  ILG_TRY(cj.alloc(cap));
+  ILG_TRY(ucount.alloc(1));
+  ILG_CUDA(cudaMemsetAsync(ucount.p, 0, 8, s));
+  int64_t ucap = 0;   // ukeys capacity; kept >= keys so far + the next chunk's pairs
+  unsigned long long nkeys = 0;
+  for (size_t q = 0; q + 1 < cut.size(); ++q) {
+    const int a = cut[q], b = cut[q + 1];
+    const int64_t np = (int64_t)(offs_h[b] - offs_h[a]);
+    if (np == 0) continue;
+    if ((int64_t)nkeys + np > ucap) {
+      int64_t want = std::min<int64_t>(npairs, std::max<int64_t>(2 * ucap, (int64_t)nkeys + np));
+      dbuf<unsigned long long> grown;
+      ILG_TRY(grown.alloc(want));
+      if (nkeys > 0) ILG_CUDA(cudaMemcpyAsync(grown.p, ukeys.p, nkeys * 8, cudaMemcpyDeviceToDevice, s));
+      ILG_CUDA(cudaStreamSynchronize(s));
+      std::swap(ukeys, grown);
+      ucap = want;
+    }
+    k_candidates<true><<<div_up((int64_t)(b - a) * FF_SPLIT, 128), 128, 0, s>>>(
+        c.nodes.p, c.tri_s.p, front.p, front.p + FF_SPLIT, c.cen.p, c.nrm.p, a, b, c.r_max, slack, cut2, box_cut2,
+        nullptr, offs.p + (size_t)a * FF_SPLIT, offs_h[a], ci.p, cj.p, c.derr.p);
     ILG_CUDA(cudaGetLastError());
-    k_vis_rays<<<div_up(npairs, 128), 128, 0, s>>>(c.nodes.p, c.tri_s.p, c.root, c.cen.p, c.nrm.p, npairs, ci.p,
-                                                   cj.p, (float)offset, bits, nt, keys.p, c.derr.p);
+    k_vis_rays<<<div_up(np, 128), 128, 0, s>>>(c.nodes.p, c.tri_s.p, c.root, c.cen.p, c.nrm.p, np, ci.p, cj.p,
+                                               (float)offset, bits, ukeys.p, ucount.p, c.derr.p);
     ILG_CUDA(cudaGetLastError());
-    ILG_TRY(radix_sort_u64(keys.p, nullptr, npairs, 2 * bits, c.sort, s));
+    ILG_CUDA(cudaMemcpyAsync(&nkeys, ucount.p, 8, cudaMemcpyDeviceToHost, s));
+    ILG_CUDA(cudaStreamSynchronize(s));
   }
   ci.release();
   cj.release();
+  const int64_t n = (int64_t)nkeys;
+  if (n > 1) ILG_TRY(radix_sort_u64(ukeys.p, nullptr, n, 2 * bits, c.sort, s));
+  dbuf<unsigned long long>& keys = ukeys;
   dbuf<uint32_t> keep;
   dbuf<double> fval;
   dbuf<unsigned long long> pos;
   dbuf<double> alb;
-  int64_t n = npairs;
   ILG_TRY(keep.alloc(n > 0 ? n : 1));
   ILG_TRY(fval.alloc(n > 0 ? n : 1));
   ILG_TRY(pos.alloc(n > 0 ? n : 1));

@@ -44,6 +44,7 @@
 #include <atomic>
 #include <cmath>
 #include <mutex>
+#include <thread>
 #include <vector>
 
 #include "internal.cuh"
@@ -715,80 +716,125 @@ int radiosity_prepare(Context& c) {
   c.n_active = (int)arow.size();
 
   // tile cuts: equal shares of the estimated work (entries + RAD_ROW_COST
-  // per row), halo and row caps
+  // per row), halo and row caps. Sequential pass: a row is stamped into the
+  // current tile's halo and rolled back if it would overflow it.
   const int G = g_rad_nsm * std::min(g_rad_per_sm64, g_rad_per_smm);
   int64_t ntarget = std::max<int64_t>(1, std::min<int64_t>(G, (nnz + RAD_MIN_TILE - 1) / RAD_MIN_TILE));
   const int64_t total_cost = nnz + RAD_ROW_COST * (int64_t)arow.size();
-  std::vector<int> stamp((size_t)nt, -1);
-  std::vector<int> loc((size_t)nt, 0);
   std::vector<RowTile> tiles;
-  std::vector<uint16_t> cf;
-  std::vector<uint32_t> esrc, efac, trow, thalo, tstart;
-  int64_t done_cost = 0;
-  size_t a = 0;
-  while (a < arow.size()) {
-    // rows [a, b) form the next tile
-    const int tid = (int)tiles.size();
-    int64_t bound = (int64_t)((double)total_cost * (double)(tid + 1) / (double)ntarget);
-    int nhalo = 0;
-    size_t b = a;
-    int64_t ne = 0;
-    std::vector<uint32_t> halo;
-    while (b < arow.size()) {
-      int g = (int)order[arow[b]];
-      int fresh = 0;
-      for (int64_t k = rp[g]; k < rp[g + 1]; ++k)
-        if (stamp[skey[k] & cmask] != tid) ++fresh;
-      if (b > a && (nhalo + fresh > RAD_HALO || (int64_t)(b - a) >= RAD_ROWS)) break;
-      for (int64_t k = rp[g]; k < rp[g + 1]; ++k) {
-        uint32_t cpos = (uint32_t)(skey[k] & cmask);
-        if (stamp[cpos] != tid) { stamp[cpos] = tid; halo.push_back(cpos); }
+  std::vector<size_t> tile_a;   // first active row of each tile
+  {
+    std::vector<int> stamp((size_t)nt, -1);
+    std::vector<uint32_t> fresh;
+    int64_t done_cost = 0;
+    size_t a = 0;
+    while (a < arow.size()) {
+      const int tid = (int)tiles.size();
+      int64_t bound = (int64_t)((double)total_cost * (double)(tid + 1) / (double)ntarget);
+      int nhalo = 0;
+      size_t b = a;
+      int64_t ne = 0;
+      while (b < arow.size()) {
+        int g = (int)order[arow[b]];
+        if (b > a && (int64_t)(b - a) >= RAD_ROWS) break;
+        fresh.clear();
+        for (int64_t k = rp[g]; k < rp[g + 1]; ++k) {
+          uint32_t cpos = (uint32_t)(skey[k] & cmask);
+          if (stamp[cpos] != tid) { stamp[cpos] = tid; fresh.push_back(cpos); }
+        }
+        if (b > a && nhalo + (int)fresh.size() > RAD_HALO) {
+          for (uint32_t cpos : fresh) stamp[cpos] = -1;
+          break;
+        }
+        nhalo += (int)fresh.size();
+        ne += rp[g + 1] - rp[g];
+        ++b;
+        if (done_cost + ne + RAD_ROW_COST * (int64_t)(b - a) >= bound && tid + 1 < ntarget) break;
       }
-      nhalo += fresh;
-      ne += rp[g + 1] - rp[g];
-      ++b;
-      if (done_cost + ne + RAD_ROW_COST * (int64_t)(b - a) >= bound && tid + 1 < ntarget) break;
+      RowTile T{};
+      T.lam = (int)(((ne + RAD_THREADS - 1) / RAD_THREADS + 3) & ~(int64_t)3);
+      T.nrows = (int)(b - a);
+      T.nhalo = nhalo;
+      T.mesh = 0;
+      tiles.push_back(T);
+      tile_a.push_back(a);
+      done_cost += ne + RAD_ROW_COST * (int64_t)(b - a);
+      a = b;
     }
-    std::sort(halo.begin(), halo.end());
-    for (int h = 0; h < (int)halo.size(); ++h) loc[halo[h]] = h;
-    RowTile T{};
-    T.e0 = (int64_t)cf.size();
-    T.lam = (int)(((ne + RAD_THREADS - 1) / RAD_THREADS + 3) & ~(int64_t)3);
-    T.nrows = (int)(b - a);
-    T.r0 = (int)trow.size();
-    T.h0 = (int)thalo.size();
-    T.nhalo = (int)halo.size();
-    T.mesh = 0;
-    const int64_t stored = (int64_t)T.lam * RAD_THREADS;
-    cf.resize(cf.size() + stored, 0);
-    esrc.resize(esrc.size() + stored, 0xffffffffu);
-    efac.resize(efac.size() + stored, 0);
-    std::vector<int64_t> row_first;
-    int64_t j = 0;
-    for (size_t q = a; q < b; ++q) {
-      int p = arow[q];
-      int g = (int)order[p];
-      row_first.push_back(j);
-      trow.push_back((uint32_t)p);
-      for (int64_t k = rp[g]; k < rp[g + 1]; ++k, ++j) {
-        int64_t t = j / T.lam, kk = j % T.lam;
-        int64_t off = T.e0 + (kk >> 2) * 4 * RAD_THREADS + 4 * t + (kk & 3);
-        cf[off] = (uint16_t)(loc[skey[k] & cmask] | (k + 1 == rp[g + 1] ? 0x8000 : 0));
-        esrc[off] = ssrc[k];
-        efac[off] = (uint32_t)g;
-      }
-    }
-    for (int t = 0; t < RAD_THREADS; ++t) {
-      int64_t j0 = (int64_t)t * T.lam;
-      if (j0 >= ne) { tstart.push_back((uint32_t)T.nrows); continue; }
-      int r = (int)(std::upper_bound(row_first.begin(), row_first.end(), j0) - row_first.begin()) - 1;
-      tstart.push_back((uint32_t)r | (row_first[r] != j0 ? 0x80000000u : 0u));
-    }
-    thalo.insert(thalo.end(), halo.begin(), halo.end());
-    tiles.push_back(T);
-    done_cost += ne + RAD_ROW_COST * (int64_t)(b - a);
-    a = b;
   }
+  // offsets of each tile's slots, rows and halo
+  int64_t stored_total = 0, rows_total = 0, halo_total = 0;
+  for (RowTile& T : tiles) {
+    T.e0 = stored_total;
+    T.r0 = (int)rows_total;
+    T.h0 = (int)halo_total;
+    stored_total += (int64_t)T.lam * RAD_THREADS;
+    rows_total += T.nrows;
+    halo_total += T.nhalo;
+  }
+  std::vector<uint16_t> cf((size_t)stored_total, 0);
+  std::vector<uint32_t> esrc((size_t)stored_total, 0xffffffffu), efac((size_t)stored_total, 0);
+  std::vector<uint32_t> trow((size_t)rows_total), thalo((size_t)halo_total);
+  std::vector<uint32_t> tstart(tiles.size() * RAD_THREADS);
+  // Per tile, independently (host threads): sorted halo, entry slots
+  // (thread t holds entries [t lam, (t+1) lam) of the tile, interleaved by
+  // 4) and each thread's first row with its continuation bit.
+  std::atomic<int> next{0};
+  std::atomic<int> bad{0};
+  auto fill = [&]() {
+    std::vector<int> loc((size_t)nt, 0);
+    std::vector<int> seen((size_t)nt, -1);
+    std::vector<uint32_t> halo;
+    std::vector<int64_t> row_first;
+    for (int tid; (tid = next.fetch_add(1)) < (int)tiles.size();) {
+      const RowTile& T = tiles[tid];
+      const size_t a = tile_a[tid], b = a + T.nrows;
+      halo.clear();
+      int64_t ne = 0;
+      for (size_t q = a; q < b; ++q) {
+        int g = (int)order[arow[q]];
+        ne += rp[g + 1] - rp[g];
+        for (int64_t k = rp[g]; k < rp[g + 1]; ++k) {
+          uint32_t cpos = (uint32_t)(skey[k] & cmask);
+          if (seen[cpos] != tid) { seen[cpos] = tid; halo.push_back(cpos); }
+        }
+      }
+      if ((int)halo.size() != T.nhalo) { bad = 1; continue; }
+      std::sort(halo.begin(), halo.end());
+      for (int h = 0; h < (int)halo.size(); ++h) loc[halo[h]] = h;
+      std::copy(halo.begin(), halo.end(), thalo.begin() + T.h0);
+      row_first.clear();
+      int64_t j = 0;
+      for (size_t q = a; q < b; ++q) {
+        int p = arow[q];
+        int g = (int)order[p];
+        row_first.push_back(j);
+        trow[(size_t)T.r0 + (q - a)] = (uint32_t)p;
+        for (int64_t k = rp[g]; k < rp[g + 1]; ++k, ++j) {
+          int64_t t = j / T.lam, kk = j % T.lam;
+          int64_t off = T.e0 + (kk >> 2) * 4 * RAD_THREADS + 4 * t + (kk & 3);
+          cf[off] = (uint16_t)(loc[skey[k] & cmask] | (k + 1 == rp[g + 1] ? 0x8000 : 0));
+          esrc[off] = ssrc[k];
+          efac[off] = (uint32_t)g;
+        }
+      }
+      uint32_t* ts = tstart.data() + (size_t)tid * RAD_THREADS;
+      for (int t = 0; t < RAD_THREADS; ++t) {
+        int64_t j0 = (int64_t)t * T.lam;
+        if (j0 >= ne) { ts[t] = (uint32_t)T.nrows; continue; }
+        int r = (int)(std::upper_bound(row_first.begin(), row_first.end(), j0) - row_first.begin()) - 1;
+        ts[t] = (uint32_t)r | (row_first[r] != j0 ? 0x80000000u : 0u);
+      }
+    }
+  };
+  {
+    int nth = (int)std::min<size_t>(tiles.size(), std::max(1u, std::min(16u, std::thread::hardware_concurrency())));
+    std::vector<std::thread> pool;
+    for (int t = 1; t < nth; ++t) pool.emplace_back(fill);
+    fill();
+    for (auto& th : pool) th.join();
+  }
+  if (bad) { set_error("row tile halo mismatch"); return ILG_ERR_CUDA; }
   c.ntiles = (int)tiles.size();
   c.tile_elems = (int64_t)cf.size();
   c.tiles_h = tiles;
