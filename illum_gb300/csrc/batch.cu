@@ -64,7 +64,7 @@ struct Batch {
   dbuf<float> T32, coef32;
   dbuf<RowTile> tiles;
   dbuf<uint16_t> t_cf;
-  dbuf<float2> t_val;
+  dbuf<float> t_vhi, t_vlo;
   dbuf<double> tile_d2;
   dbuf<__nv_bfloat16> t_vbf;
   dbuf<uint32_t> t_row, t_halo, t_start;
@@ -165,7 +165,7 @@ static int build(Batch& b) {
   const int RT = radiosity_threads();
   int64_t ntl1 = ntl > 0 ? ntl : 1, nel1 = nel > 0 ? nel : 1;
   ILG_TRY(b.tiles.alloc(ntl1)); ILG_TRY(b.tile_d2.alloc(2 * ntl1)); ILG_TRY(b.t_start.alloc(ntl1 * RT));
-  ILG_TRY(b.t_cf.alloc(nel1)); ILG_TRY(b.t_val.alloc(nel1)); ILG_TRY(b.t_vbf.alloc(nel1));
+  ILG_TRY(b.t_cf.alloc(nel1)); ILG_TRY(b.t_vhi.alloc(nel1)); ILG_TRY(b.t_vlo.alloc(nel1)); ILG_TRY(b.t_vbf.alloc(nel1));
   ILG_TRY(b.t_row.alloc(nrow > 0 ? nrow : 1)); ILG_TRY(b.t_scale.alloc(nrow > 0 ? nrow : 1));
   ILG_TRY(b.t_halo.alloc(nhal > 0 ? nhal : 1));
   ILG_TRY(b.row_act.alloc(nt));
@@ -240,7 +240,8 @@ static int build(Batch& b) {
       int64_t nh = 0;
       for (const RowTile& T : c.tiles_h) nh += T.nhalo;
       ILG_TRY(cat(b.t_cf, (size_t)el, c.t_cf.p, (size_t)c.tile_elems, s));
-      ILG_TRY(cat(b.t_val, (size_t)el, c.t_val.p, (size_t)c.tile_elems, s));
+      ILG_TRY(cat(b.t_vhi, (size_t)el, c.t_vhi.p, (size_t)c.tile_elems, s));
+      ILG_TRY(cat(b.t_vlo, (size_t)el, c.t_vlo.p, (size_t)c.tile_elems, s));
       ILG_TRY(cat(b.t_vbf, (size_t)el, c.t_vbf.p, (size_t)c.tile_elems, s));
       ILG_TRY(cat(b.t_start, (size_t)to * RT, c.t_start.p, (size_t)M.ntiles * RT, s));
       ILG_TRY(cat(b.t_row, (size_t)ro, c.t_row.p, (size_t)c.n_active, s));
@@ -278,7 +279,7 @@ static int build(Batch& b) {
   v.therm_avg = b.therm_avg.p; v.therm_max = b.therm_max.p; v.E = b.E.p; v.sprev = b.sprev.p;
   v.x32 = b.x32.p; v.Tdf = b.Tdf.p; v.T32 = b.T32.p; v.coefdf = b.coefdf.p; v.coef32 = b.coef32.p;
   v.tiles = b.tiles.p; v.ntiles = b.ntiles;
-  v.t_cf = b.t_cf.p; v.t_val = b.t_val.p; v.t_vbf = b.t_vbf.p;
+  v.t_cf = b.t_cf.p; v.t_vhi = b.t_vhi.p; v.t_vlo = b.t_vlo.p; v.t_vbf = b.t_vbf.p;
   v.t_row = b.t_row.p; v.t_halo = b.t_halo.p; v.t_start = b.t_start.p; v.t_scale = b.t_scale.p;
   v.tile_d2 = b.tile_d2.p;
   v.row_act = b.row_act.p;

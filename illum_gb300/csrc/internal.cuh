@@ -120,7 +120,8 @@ struct StepView {
   const RowTile* tiles;
   int ntiles;
   const uint16_t* t_cf;        // per stored entry: halo index | row end << 15
-  const float2* t_val;         // double-float values (hi, lo)
+  const float* t_vhi;          // double-float values: hi = fl(F)
+  const float* t_vlo;          //   and lo = fl(F - hi)
   const __nv_bfloat16* t_vbf;  // value / row scale
   const uint32_t *t_row, *t_halo, *t_start;   // tile rows and halos (positions); per-thread first row
   const float* t_scale;        // per tile row: bf16 scale
@@ -180,7 +181,7 @@ struct Context {
   std::vector<RowTile> tiles_h;
   dbuf<RowTile> tiles;
   dbuf<uint16_t> t_cf;
-  dbuf<float2> t_val;
+  dbuf<float> t_vhi, t_vlo;
   dbuf<__nv_bfloat16> t_vbf;
   dbuf<uint32_t> t_row, t_halo, t_start;
   dbuf<float> t_scale;

@@ -34,10 +34,18 @@
 // is ~2^-46 (vs 2^-53 for FP64), orders of magnitude below the solve
 // tolerance; everything per row (residual, iterate, convergence) is FP64.
 //
+// The double-float values are stored as two arrays, hi = fl(F) and
+// lo = fl(F - hi).
+//
 // Mixed precision: values stored as bf16 with a per-row fp32 scale, fp32
 // accumulation for the inner sweeps, and an outer refinement whose residual
-// is evaluated with the double-float dot products above (so the fixed point
-// is the fp64 system's).
+// is accumulated in double-float from the fp32 values hi (x in double-float,
+// E and the residual in FP64): the fixed point is that of (I - fl(F)) x = E,
+// within ~1e-7 of the scattered flux of the fp64 system's. A mesh whose
+// sweep budget runs out in a refinement round stops after the round's update
+// without another residual pass, so max_sweeps = RAD_INNER gives one
+// refinement round per step (the next step's first residual includes what
+// is left).
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -57,8 +65,8 @@ constexpr int RAD_THREADS = 1024;
 constexpr int RAD_HALO = 16384;          // halo values per tile (double-float: 128 KB of shared memory)
 constexpr int RAD_ROWS = 6144;           // rows per tile (their sums: 48 KB of shared memory)
 constexpr int RAD_MAX_MESH = 1024;
-constexpr int RAD_INNER = 3;             // fp32 sweeps per refinement of the mixed solve (bf16 error ~4e-4 per
-                                         // refinement already dominates rho^(k+1); 2, 3, 4 measured, 3 fastest)
+constexpr int RAD_INNER = 2;             // fp32 sweeps per refinement of the mixed solve: the bf16 error
+                                         // (~4e-3 of the correction) already dominates rho^(k+1), rho ~ 0.013
 constexpr int64_t RAD_MIN_TILE = 16384;  // entries: smaller tiles cost more in staging than they balance
 constexpr int64_t RAD_ROW_COST = 32;     // a row's finishing work, in entries (tile balance)
 constexpr size_t RAD_SMEM =
@@ -114,14 +122,32 @@ __device__ __forceinline__ uint2 ld_mat(const uint2* p, uint64_t pol) {
                : "=r"(r.x), "=r"(r.y) : "l"(p), "l"(pol));
   return r;
 }
-__device__ __forceinline__ void ld_mat4(const float2* p, float2 (&w)[4], uint64_t pol) {
+__device__ __forceinline__ float4 ld_mat_f4(const float* p, uint64_t pol) {
+  float4 r;
   asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
-               : "=f"(w[0].x), "=f"(w[0].y), "=f"(w[1].x), "=f"(w[1].y) : "l"(p), "l"(pol));
-  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
-               : "=f"(w[2].x), "=f"(w[2].y), "=f"(w[3].x), "=f"(w[3].y) : "l"(p + 2), "l"(pol));
+               : "=f"(r.x), "=f"(r.y), "=f"(r.z), "=f"(r.w) : "l"(p), "l"(pol));
+  return r;
 }
-__device__ __forceinline__ void ld_mat4(const __nv_bfloat16* p, float (&w)[4], uint64_t pol) {
-  uint2 r = ld_mat(reinterpret_cast<const uint2*>(p), pol);
+// Value sources of tile_rows: four consecutive entries from offset off.
+struct ValsDF { const float* hi; const float* lo; };   // double-float (hi, lo)
+struct ValsHi { const float* hi; };                    // fl(F) as a double-float with lo = 0
+struct ValsBF { const __nv_bfloat16* v; };             // bf16, scaled per row
+__device__ __forceinline__ void ld_vals4(ValsDF s, size_t off, float2 (&w)[4], uint64_t pol) {
+  float4 h = ld_mat_f4(s.hi + off, pol), l = ld_mat_f4(s.lo + off, pol);
+  w[0] = make_float2(h.x, l.x);
+  w[1] = make_float2(h.y, l.y);
+  w[2] = make_float2(h.z, l.z);
+  w[3] = make_float2(h.w, l.w);
+}
+__device__ __forceinline__ void ld_vals4(ValsHi s, size_t off, float2 (&w)[4], uint64_t pol) {
+  float4 h = ld_mat_f4(s.hi + off, pol);
+  w[0] = make_float2(h.x, 0.f);
+  w[1] = make_float2(h.y, 0.f);
+  w[2] = make_float2(h.z, 0.f);
+  w[3] = make_float2(h.w, 0.f);
+}
+__device__ __forceinline__ void ld_vals4(ValsBF s, size_t off, float (&w)[4], uint64_t pol) {
+  uint2 r = ld_mat(reinterpret_cast<const uint2*>(s.v + off), pol);
   w[0] = __uint_as_float(r.x << 16);
   w[1] = __uint_as_float(r.x & 0xffff0000u);
   w[2] = __uint_as_float(r.y << 16);
@@ -237,7 +263,7 @@ __device__ __forceinline__ void stage_halo(const StepView& v, const RowTile& T, 
 // ends: the partial sums of the threads it spans, in thread order, then its
 // own part. Ends with a block barrier: rs holds every row sum of the tile.
 template <class Acc, class V>
-__device__ __forceinline__ void tile_rows(const StepView& v, const RowTile& T, int t, const V* vals,
+__device__ __forceinline__ void tile_rows(const StepView& v, const RowTile& T, int t, V vals,
                                           const typename Acc::X* sx, typename Acc::Part* tail, unsigned char* tnew,
                                           typename Acc::Sum* rs, uint64_t pol) {
   typedef typename Acc::W W;
@@ -251,7 +277,7 @@ __device__ __forceinline__ void tile_rows(const StepView& v, const RowTile& T, i
   acc.zero();
   head.zero();
   const uint2* cfp = reinterpret_cast<const uint2*>(v.t_cf + T.e0) + tid;
-  const V* vp = vals + T.e0 + 4 * tid;
+  const size_t vo = (size_t)T.e0 + 4 * tid;
   const int ng = T.lam >> 2;
   auto elem = [&](uint32_t c, W w) {
     acc.add(w, sx[c & 0x7fffu]);
@@ -270,10 +296,10 @@ __device__ __forceinline__ void tile_rows(const StepView& v, const RowTile& T, i
   };
   uint2 c0 = ld_mat(cfp, pol), c1 = c0;
   W w0[4], w1[4];
-  ld_mat4(vp, w0, pol);
+  ld_vals4(vals, vo, w0, pol);
   if (ng > 1) {
     c1 = ld_mat(cfp + RAD_THREADS, pol);
-    ld_mat4(vp + 4 * RAD_THREADS, w1, pol);
+    ld_vals4(vals, vo + 4 * RAD_THREADS, w1, pol);
   } else {
 #pragma unroll
     for (int j = 0; j < 4; ++j) w1[j] = w0[j];
@@ -283,7 +309,7 @@ __device__ __forceinline__ void tile_rows(const StepView& v, const RowTile& T, i
     W w2[4];
     if (g + 2 < ng) {
       c2 = ld_mat(cfp + (size_t)(g + 2) * RAD_THREADS, pol);
-      ld_mat4(vp + (size_t)(g + 2) * 4 * RAD_THREADS, w2, pol);
+      ld_vals4(vals, vo + (size_t)(g + 2) * 4 * RAD_THREADS, w2, pol);
     } else {
 #pragma unroll
       for (int j = 0; j < 4; ++j) w2[j] = w1[j];
@@ -481,7 +507,7 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity64(StepView v, doub
       const RowTile T = v.tiles[t];
       if (st.done[T.mesh]) continue;
       stage_halo(v, T, curh, sm.sx);
-      tile_rows<AccDF>(v, T, t, v.t_val, sm.sx, sm.tail, sm.tnew, sm.rs, pol);
+      tile_rows<AccDF>(v, T, t, ValsDF{v.t_vhi, v.t_vlo}, sm.sx, sm.tail, sm.tnew, sm.rs, pol);
       const uint32_t* rows = v.t_row + T.r0;
       double d2 = 0.0;
       for (int r = threadIdx.x; r < T.nrows; r += RAD_THREADS) {
@@ -503,9 +529,10 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity64(StepView v, doub
   scatter_x(v, st, x, warm, gt, nthreads, false);
 }
 
-// Mixed precision: outer refinement with an fp64 residual r = E - (I - F) x
-// (fp64 values), inner fp32 Jacobi on (I - F~) d = r with bf16 F~ (RAD_INNER sweeps),
-// x += d. A mesh stops when ||r||_2 <= tol.
+// Mixed precision: outer refinement with an fp64 residual r = E - (I - fl(F)) x
+// (double-float sums), inner fp32 Jacobi on (I - F~) d = r with bf16 F~
+// (RAD_INNER sweeps), x += d. A mesh stops when ||r||_2 <= tol, or after the
+// update of the round that reaches max_sweeps.
 __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity_mixed(StepView v, double* x, int warm) {
   __shared__ MeshState st;
   __shared__ double red[32];
@@ -531,7 +558,7 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity_mixed(StepView v, 
       const RowTile T = v.tiles[t];
       if (st.done[T.mesh]) continue;
       stage_halo(v, T, XH, sm.sx);
-      tile_rows<AccDF>(v, T, t, v.t_val, sm.sx, sm.tail, sm.tnew, sm.rs, pol);
+      tile_rows<AccDF>(v, T, t, ValsHi{v.t_vhi}, sm.sx, sm.tail, sm.tnew, sm.rs, pol);
       const uint32_t* rows = v.t_row + T.r0;
       double d2 = 0.0;
       for (int r = threadIdx.x; r < T.nrows; r += RAD_THREADS) {
@@ -554,30 +581,45 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity_mixed(StepView v, 
         const RowTile T = v.tiles[t];
         if (st.done[T.mesh]) continue;
         stage_halo(v, T, cur, sxf);
-        tile_rows<AccF32>(v, T, t, v.t_vbf, sxf, tailf, sm.tnew, rsf, pol);
+        tile_rows<AccF32>(v, T, t, ValsBF{v.t_vbf}, sxf, tailf, sm.tnew, rsf, pol);
         const uint32_t* rows = v.t_row + T.r0;
         const float* scale = v.t_scale + T.r0;
-        for (int r = threadIdx.x; r < T.nrows; r += RAD_THREADS) {
-          uint32_t i = __ldg(rows + r);
-          nxt[i] = ld_it(r32 + i) + __ldg(scale + r) * rsf[r];
+        if (it + 1 < RAD_INNER) {
+          for (int r = threadIdx.x; r < T.nrows; r += RAD_THREADS) {
+            uint32_t i = __ldg(rows + r);
+            nxt[i] = ld_it(r32 + i) + __ldg(scale + r) * rsf[r];
+          }
+        } else {   // last sweep: nobody reads d again, x += d directly
+          for (int r = threadIdx.x; r < T.nrows; r += RAD_THREADS) {
+            uint32_t i = __ldg(rows + r);
+            const float d = ld_it(r32 + i) + __ldg(scale + r) * rsf[r];
+            X[i] = ld_it(X + i) + (double)d;
+            XH[i] = df_add(ld_it(XH + i), make_float2(d, 0.f));
+          }
         }
         __syncthreads();
       }
-      if (!grid_barrier(v.barrier, gridDim.x, v.derr)) return;
-      float* tmp = cur; cur = nxt; nxt = tmp;
-    }
-    for (int t = blockIdx.x; t < v.ntiles; t += gridDim.x) {
-      const RowTile T = v.tiles[t];
-      if (st.done[T.mesh]) continue;
-      const uint32_t* rows = v.t_row + T.r0;
-      for (int r = threadIdx.x; r < T.nrows; r += RAD_THREADS) {
-        uint32_t i = __ldg(rows + r);
-        const float d = ld_it(cur + i);
-        X[i] = ld_it(X + i) + (double)d;
-        XH[i] = df_add(ld_it(XH + i), make_float2(d, 0.f));
+      if (it + 1 < RAD_INNER) {
+        if (!grid_barrier(v.barrier, gridDim.x, v.derr)) return;
+        float* tmp = cur; cur = nxt; nxt = tmp;
       }
     }
+    // meshes whose budget this round used up stop here (same decision in
+    // every block: it depends on the counts only)
+    int left = 0;
+    for (int m0 = 0; m0 < v.nmesh; m0 += blockDim.x) {
+      int m = m0 + threadIdx.x;
+      bool run = m < v.nmesh && !st.done[m];
+      if (run && st.sweeps[m] + RAD_INNER >= v.md[m].max_sweeps) {
+        st.done[m] = 1;
+        st.sweeps[m] += RAD_INNER;
+        if (blockIdx.x == 0) v.md[m].sweeps = st.sweeps[m];
+        run = false;
+      }
+      left += __syncthreads_count(run);
+    }
     if (!grid_barrier(v.barrier, gridDim.x, v.derr)) return;
+    if (left == 0) break;
   }
   scatter_x(v, st, x, warm, gt, nthreads, true);
 }
@@ -613,13 +655,15 @@ __global__ void k_row_keys(const int64_t* __restrict__ rowptr, const int32_t* __
 // Stored entry e takes CSR entry src[e] (value as a double-float, and its
 // bf16 copy scaled by its row's scale), or zero for padding (src = ~0).
 __global__ void k_tile_fill(const uint32_t* __restrict__ src, const uint32_t* __restrict__ fac, int64_t n,
-                            const double* __restrict__ val, const float* __restrict__ rscale, float2* t_val,
-                            __nv_bfloat16* t_vbf) {
+                            const double* __restrict__ val, const float* __restrict__ rscale, float* t_vhi,
+                            float* t_vlo, __nv_bfloat16* t_vbf) {
   int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= n) return;
   uint32_t k = src[e];
   double w = k == 0xffffffffu ? 0.0 : val[k];
-  t_val[e] = split_df(w);
+  float2 hl = split_df(w);
+  t_vhi[e] = hl.x;
+  t_vlo[e] = hl.y;
   t_vbf[e] = __float2bfloat16_rn(k == 0xffffffffu ? 0.f : (float)(w / (double)rscale[fac[e]]));
 }
 
@@ -842,7 +886,8 @@ int radiosity_prepare(Context& c) {
   const int ntl = c.ntiles > 0 ? c.ntiles : 1;
   ILG_TRY(c.tiles.alloc(ntl));
   ILG_TRY(c.t_cf.alloc(ns));
-  ILG_TRY(c.t_val.alloc(ns));
+  ILG_TRY(c.t_vhi.alloc(ns));
+  ILG_TRY(c.t_vlo.alloc(ns));
   ILG_TRY(c.t_vbf.alloc(ns));
   ILG_TRY(c.t_row.alloc(trow.empty() ? 1 : trow.size()));
   ILG_TRY(c.t_scale.alloc(trow.empty() ? 1 : trow.size()));
@@ -860,7 +905,8 @@ int radiosity_prepare(Context& c) {
     ILG_CUDA(cudaMemcpyAsync(c.t_start.p, tstart.data(), tstart.size() * 4, cudaMemcpyHostToDevice, s));
     ILG_CUDA(cudaMemcpyAsync(dsrc.p, esrc.data(), esrc.size() * 4, cudaMemcpyHostToDevice, s));
     ILG_CUDA(cudaMemcpyAsync(dfac.p, efac.data(), efac.size() * 4, cudaMemcpyHostToDevice, s));
-    k_tile_fill<<<div_up(ns, 256), 256, 0, s>>>(dsrc.p, dfac.p, ns, c.val.p, c.row_scale.p, c.t_val.p, c.t_vbf.p);
+    k_tile_fill<<<div_up(ns, 256), 256, 0, s>>>(dsrc.p, dfac.p, ns, c.val.p, c.row_scale.p, c.t_vhi.p, c.t_vlo.p,
+                                                c.t_vbf.p);
     ILG_CUDA(cudaGetLastError());
     k_tile_scale<<<div_up((int64_t)trow.size(), 256), 256, 0, s>>>(c.t_row.p, c.rperm.p, (int)trow.size(),
                                                                   c.row_scale.p, c.t_scale.p);

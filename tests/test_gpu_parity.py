@@ -300,11 +300,17 @@ def test_split_runs_equal_one_run(ilg, oracle_mod, mesh_l3):
     assert np.array_equal(a[1].T, b[1].T)
 
 
-def test_mixed_precision_within_tolerance(ilg, oracle_mod, mesh_l4):
+@pytest.mark.parametrize("tol,max_sweeps", [(1e-10, 200), (1e-3, 2)])
+def test_mixed_precision_within_tolerance(ilg, oracle_mod, mesh_l4, tol, max_sweeps):
+    """Mixed path (bf16 form factors, fp32 conduction) against the FP64 path:
+    solved to tolerance, and with one refinement round per step (the
+    two-sweep budget stops the solve after its first update)."""
     v, f = mesh_l4
     nsteps = 360
     ref = _setup_run(ilg, oracle_mod, v, f, 32, 40, nsteps, precision=0)
     mix = _setup_run(ilg, oracle_mod, v, f, 32, 40, nsteps, precision=1)
+    mix[2].tol = tol
+    mix[2].max_sweeps = max_sweeps
     ha = ref[0].run_steps(ref[2], 0, nsteps, record_tsurf=True)
     hb = mix[0].run_steps(mix[2], 0, nsteps, record_tsurf=True)
     err_s = np.abs(ha - hb).max()
