@@ -121,7 +121,7 @@ int flush_launch(float4* buf, size_t n, unsigned salt, cudaStream_t s) {
 // ev (4 events), the phase boundaries are recorded.
 int enqueue_step(const StepView& v, const StepPlan& p, cudaStream_t s, cudaEvent_t* ev) {
   if (ev) ILG_CUDA(cudaEventRecord(ev[0], s));
-  ILG_TRY(direct_launch(v, 0, s));
+  ILG_TRY(direct_launch(v, 0, p.precision == ILG_PREC_MIXED ? 1 : 0, s));
   if (ev) ILG_CUDA(cudaEventRecord(ev[1], s));
   if (p.rad_on) ILG_TRY(radiosity_launch(v, v.rad, 1, p.precision, p.rad_grid, s));
   if (ev) ILG_CUDA(cudaEventRecord(ev[2], s));
@@ -546,7 +546,7 @@ int ilg_direct_radiosity(ilg_ctx* ctx, const double* sun, const double* disk_xy,
   MeshDesc M = solo_desc(c, nullptr, 0);
   M.host_sun = 1;
   ILG_TRY(upload_desc(c, M));
-  ILG_TRY(direct_launch(solo_view(c, ILG_PREC_FP64), 1, c.stream));
+  ILG_TRY(direct_launch(solo_view(c, ILG_PREC_FP64), 1, 0, c.stream));
   ILG_CUDA(cudaMemcpyAsync(out, c.E.p, (size_t)c.nt * 8, cudaMemcpyDeviceToHost, c.stream));
   ILG_CUDA(cudaStreamSynchronize(c.stream));
   return read_device_errors(c);

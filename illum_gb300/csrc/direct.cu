@@ -70,7 +70,10 @@ __device__ __forceinline__ bool thr_range(const float* __restrict__ h, int nphi,
   return true;
 }
 
-__global__ void k_direct_classify(StepView v, int dropin) {
+// mu32: the cosine of the sun centre in FP32 (n . u, u the unit sun vector;
+// relative error ~2e-7) instead of the reference's FP64 value; the lit
+// sample count stays exact either way.
+__global__ void k_direct_classify(StepView v, int dropin, int mu32_flux) {
   int f = blockIdx.x * blockDim.x + threadIdx.x;
   bool amb = false;
   const MeshDesc* Mp = nullptr;
@@ -137,7 +140,9 @@ __global__ void k_direct_classify(StepView v, int dropin) {
     }
     if (decided) {
       double dv = 0.0;
-      if (decided == 2) {
+      if (decided == 2 && mu32_flux) {
+        dv = M.lit_all * S->flux * (double)fmaxf(mu32, 0.f);
+      } else if (decided == 2) {
         float4 c4 = v.cen[f];
         d3 p = mkd((double)c4.x, (double)c4.y, (double)c4.z);
         const double* fr = v.frame + 9 * (int64_t)f;
@@ -180,13 +185,13 @@ __global__ void k_direct_classify(StepView v, int dropin) {
 // errors; a facet whose sun-frame axis choice is within rounding of a tie
 // lists all its samples. Counts are integer sums, so the result does not
 // depend on the order.
-constexpr int DX_FACETS = 32;
+constexpr int DX_FACETS = 8;    // facets per block: spreads the FP64 work over the SMs
 constexpr int DX_THREADS = 512;
 constexpr int DX_LIST = 4096;   // (facet, sample) pairs per round of the filter
 
 struct DxFacet {
   double Tx, Ty, Tz, Bx, By, Bz;   // sun frame (FP64, for sample_lit)
-  double mu;                       // cosine of the sun centre (FP64)
+  double mu;                       // cosine of the sun centre (FP64, or FP32 with mu32_flux)
   float4 fb, ft, fn;               // facet frame (FP32)
   float Nx, Ny, Nz, Tfx, Tfy, Tfz, Bfx, Bfy, Bfz, kap;
   int f, mesh, all_amb, count;
@@ -267,7 +272,7 @@ __device__ __forceinline__ void dx_exact_sample(const StepView& v, DxFacet& F, i
   if (sample_lit(p, disk, BTN, hl, M.nphi, M.dphi, M.interp)) atomicAdd(&F.count, 1);
 }
 
-__global__ void __launch_bounds__(DX_THREADS) k_direct_exact(StepView v, int dropin) {
+__global__ void __launch_bounds__(DX_THREADS) k_direct_exact(StepView v, int dropin, int mu32_flux) {
   __shared__ DxFacet fs[DX_FACETS];
   __shared__ int list[DX_LIST];
   __shared__ int nlist;
@@ -294,8 +299,13 @@ __global__ void __launch_bounds__(DX_THREADS) k_direct_exact(StepView v, int dro
         sun_frame(N, &T, &B);
         F.Tx = T.x; F.Ty = T.y; F.Tz = T.z;
         F.Bx = B.x; F.By = B.y; F.Bz = B.z;
-        const double* fr = v.frame + 9 * (int64_t)f;
-        F.mu = sun_mu(Sv, p, mkd(fr[6], fr[7], fr[8]));
+        if (mu32_flux) {
+          float4 n4 = v.nrm[f];
+          F.mu = (double)((n4.x * S->ux + n4.y * S->uy) + n4.z * S->uz);
+        } else {
+          const double* fr = v.frame + 9 * (int64_t)f;
+          F.mu = sun_mu(Sv, p, mkd(fr[6], fr[7], fr[8]));
+        }
       }
     } else {
       if (threadIdx.x - 32 < nf) dx_setup32(v, fs[threadIdx.x - 32], v.work[base + threadIdx.x - 32]);
@@ -374,12 +384,13 @@ SunAux make_sun_aux(const double* s, double solar_const, double scene_mag, doubl
 }
 
 // Direct insolation for every active mesh of the view (dropin: E = direct
-// only). counters[0] is cleared first.
-int direct_launch(const StepView& v, int dropin, cudaStream_t s) {
+// only; mu32_flux: FP32 sun cosine in the flux). counters[0] is cleared
+// first.
+int direct_launch(const StepView& v, int dropin, int mu32_flux, cudaStream_t s) {
   ILG_CUDA(cudaMemsetAsync(v.counters, 0, sizeof(int), s));
-  k_direct_classify<<<div_up(v.nt, 256), 256, 0, s>>>(v, dropin);
+  k_direct_classify<<<div_up(v.nt, 256), 256, 0, s>>>(v, dropin, mu32_flux);
   ILG_CUDA(cudaGetLastError());
-  k_direct_exact<<<152 * 4, DX_THREADS, 0, s>>>(v, dropin);
+  k_direct_exact<<<152 * 4, DX_THREADS, 0, s>>>(v, dropin, mu32_flux);
   ILG_CUDA(cudaGetLastError());
   return ILG_OK;
 }

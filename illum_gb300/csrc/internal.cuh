@@ -272,7 +272,7 @@ int form_factors_build(Context& c, const double* albedo_h, double albedo_scalar,
 
 // ---- direct.cu ----
 SunAux make_sun_aux(const double* s, double solar_const, double scene_mag, double disk_rmax);
-int direct_launch(const StepView& v, int dropin, cudaStream_t s);
+int direct_launch(const StepView& v, int dropin, int mu32_flux, cudaStream_t s);
 
 // ---- radiosity.cu ----
 int radiosity_prepare(Context& c);
