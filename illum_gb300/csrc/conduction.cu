@@ -199,10 +199,57 @@ k_conduct(StepView v, const double* __restrict__ Qnp1, int upd) {
   }
   // top row (Ti = T_1, Tip1 = T_2 in the Fortran's numbering). In increment
   // form rho1 is the increment's; T1(n+1) = T0 + (increment) below.
+  const double Q = Qnp1[g];
+  double T0n, Tsn, Fs;
+  R top, dtop;   // T1(n+1) and its increment, in the state's type
+  if constexpr (std::is_same<R, float>::value) {
+    // fp32 state: the boundary rows in fp32 as well (Newton to ~2 ulp)
+    const float T0 = Ti, T1 = Tip1, rho1 = rho_next;
+    const float Ts = (float)v.Tsurf[g], Qf = (float)Q;
+    float t0n, tsn;
+    if (cs.bc == 0) {
+      const float Qn = (float)v.Qprev[g];
+      float Tr3 = Ts * Ts * Ts;
+      float arad = -3.f * cs.esf * Tr3 * Ts;
+      float brad = 2.f * cs.esf * Tr3;
+      float den = cs.k1f + brad;
+      float ann = (Qn - arad) / den, annp1 = (Qf - arad) / den, bn = (cs.k1f - brad) / den;
+      float b0 = 1.f + cs.alpha0f + cs.gamma0f - cs.gamma0f * bn;
+      float r0 = cs.gamma0f * (annp1 + ann) + (1.f - cs.alpha0f - cs.gamma0f + cs.gamma0f * bn) * T0 +
+                 cs.alpha0f * T1;
+      float piv = b0 + cs.f0f * cs.gamma1f;
+      if (piv == 0.f) { atomicExch(&v.derr[DERR_PIVOT], 1); return; }
+      r0 -= b0 * T0 - cs.alpha0f * T1;
+      t0n = (r0 - cs.f0f * rho1) / piv + T0;
+      tsn = 0.5f * (annp1 + bn * t0n + t0n);
+    } else if (cs.bc == 1) {
+      float R0 = 2.f * cs.alpha0f * (T1 - T0) + 4.f * cs.gamma0f * (Ts - T0) - 2.f * cs.gamma0f * Ts;
+      float P = (R0 - cs.f0f * rho1) * cs.inv_Apf + T0;
+      const float A = Qf + 2.f * cs.k1f * P;
+      float x = Ts;
+      for (int it = 0; it < 30; ++it) {
+        float x3 = x * x * x;
+        float dT = (A + cs.B_topf * x - cs.esf * x3 * x) / (cs.B_topf - 4.f * cs.esf * x3);
+        x -= dT;
+        if (fabsf(dT) <= 2.4e-7f * fabsf(x)) break;
+      }
+      tsn = x;
+      t0n = P + cs.S_topf * tsn;
+    } else {
+      float b0 = 1.f + cs.alpha0f + cs.gamma0f;
+      float r0 = cs.alpha0f * T1 + (1.f - cs.alpha0f - cs.gamma0f) * T0 + cs.gamma0f * (Ts + Qf);
+      r0 -= b0 * T0 - cs.alpha0f * T1;
+      t0n = (r0 - cs.f0f * rho1) / (b0 + cs.f0f * cs.gamma1f) + T0;
+      tsn = Qf;
+    }
+    top = t0n;
+    dtop = t0n - T0;
+    T0n = (double)t0n;
+    Tsn = cs.bc == 2 ? Q : (double)tsn;
+    Fs = (double)(-(t0n - tsn) * cs.kzf);
+  } else {
   double T0 = (double)Ti, T1 = (double)Tip1, rho1 = (double)rho_next;
   double Ts = v.Tsurf[g];
-  double Q = Qnp1[g];
-  double T0n, Tsn;
   if (cs.bc == 0) {
     double Qn = v.Qprev[g];
     double Tr3 = Ts * Ts * Ts;
@@ -258,11 +305,14 @@ k_conduct(StepView v, const double* __restrict__ Qnp1, int upd) {
     if (INC) T0n += T0;
     Tsn = Q;
   }
-  double Fs = -(T0n - Tsn) * cs.kz;
+  Fs = -(T0n - Tsn) * cs.kz;
+  top = (R)T0n;
+  dtop = (R)(T0n - T0);
+  }
   // downward pass
   if (INC) {
-    R dprev = (R)(T0n - T0);
-    T[0] = (R)T0n;
+    R dprev = dtop;
+    T[0] = top;
 #pragma unroll 4
     for (int i = 1; i < nz; ++i) {   // the increments, into the rho slots
       const R* c = tab + (size_t)i * TAB_W;
@@ -280,7 +330,7 @@ k_conduct(StepView v, const double* __restrict__ Qnp1, int upd) {
         if (i0 + j < nz) T[(size_t)(i0 + j) * N] = t[j] + RHO(i0 + j);
     }
   } else {
-    R prev = (R)T0n;
+    R prev = top;
     T[0] = prev;
     for (int i = 1; i < nz; ++i) {
       const R* c = tab + (size_t)i * TAB_W;
@@ -381,6 +431,9 @@ int build_tables(int nz, const double* z, const double* ti, const double* rhoc, 
   cs.kz = k[0] / z[0];
   cs.cgeo = dt / rhoc[nz - 1] * Fgeo / (z[nz - 1] - z[nz - 2]);
   cs.es = emiss * SIGMA_SB;
+  cs.alpha0f = (float)cs.alpha0; cs.gamma0f = (float)cs.gamma0; cs.k1f = (float)cs.k1; cs.f0f = (float)cs.f0;
+  cs.gamma1f = (float)cs.gamma1; cs.esf = (float)cs.es; cs.inv_Apf = (float)cs.inv_Ap;
+  cs.S_topf = (float)cs.S_top; cs.B_topf = (float)cs.B_top; cs.kzf = (float)cs.kz;
   cs.nz = nz;
   cs.bc = bc;
   return ILG_OK;

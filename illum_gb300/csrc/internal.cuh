@@ -41,6 +41,8 @@ struct CondScalars {
   double alpha0, gamma0, k1, f0, gamma1, Ap, k0, z0, cgeo, es;
   double inv_Ap, S_top, B_top, kz;   // 1/Ap, 2 gamma0/Ap, 2 k1 (S_top - 1), k0/z0
   int nz, bc;                        // bc: 0 linearised, 1 Newton, 2 prescribed Ts (conductionT)
+  // the same, rounded to fp32 (the fp32 surface boundary)
+  float alpha0f, gamma0f, k1f, f0f, gamma1f, esf, inv_Apf, S_topf, B_topf, kzf;
 };
 
 // Per sun position, precomputed on the host (direct.cu make_sun_aux).
