@@ -22,7 +22,7 @@ import os
 import numpy as np
 
 __all__ = ["IllumContext", "ThermalModel", "Batch", "IlgError", "fib_spiral", "conductionQ", "conductionQ_batch", "lib",
-           "library_path", "RunOpts", "PREC_FP64", "PREC_MIXED", "BC_LINEARISED", "BC_NEWTON",
+           "library_path", "RunOpts", "Tune", "PREC_FP64", "PREC_MIXED", "BC_LINEARISED", "BC_NEWTON",
            "COUPLE_REFERENCE", "COUPLE_DIRECT"]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
@@ -45,6 +45,15 @@ class IlgError(RuntimeError):
 class RunOpts(C.Structure):
     _fields_ = [("dt", C.c_double), ("tol", C.c_double), ("max_sweeps", C.c_int), ("use_radiosity", C.c_int),
                 ("use_graph", C.c_int), ("precision", C.c_int), ("coupling", C.c_int)]
+
+
+class Tune(C.Structure):
+    """Launch shapes of the step kernels (include/illum_gb300.h ilg_tune)."""
+    _fields_ = [("classify_threads", C.c_int), ("exact_facets", C.c_int), ("conduct_threads", C.c_int),
+                ("direct_us", C.c_double), ("conduct_us", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 _lib = None
@@ -88,6 +97,9 @@ _SIGS = {
                                   C.c_void_p]),
     "ilg_get_outputs": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "ilg_set_timing": (C.c_int, [C.c_void_p, C.c_int]),
+    "ilg_autotune": (C.c_int, [C.c_void_p, C.POINTER(RunOpts), C.c_int, C.POINTER(Tune)]),
+    "ilg_set_tune": (C.c_int, [C.c_void_p, C.POINTER(Tune)]),
+    "ilg_get_tune": (C.c_int, [C.c_void_p, C.POINTER(Tune)]),
     "ilg_get_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double),
                                 C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "ilg_batch_create": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.POINTER(C.c_void_p)]),
@@ -325,6 +337,23 @@ class IllumContext:
 
     def set_timing(self, enable=True):
         _check(lib().ilg_set_timing(self._h, int(enable)))
+
+    def autotune(self, opts, first_sun=0):
+        """Times every launch shape of the step kernels on this context's
+        workload (its state is left as it was) and keeps the fastest;
+        returns the chosen shapes and their measured times."""
+        t = Tune()
+        _check(lib().ilg_autotune(self._h, C.byref(opts), int(first_sun), C.byref(t)))
+        return t.as_dict()
+
+    def set_tune(self, classify_threads=256, exact_facets=8, conduct_threads=64):
+        t = Tune(classify_threads, exact_facets, conduct_threads, 0.0, 0.0)
+        _check(lib().ilg_set_tune(self._h, C.byref(t)))
+
+    def get_tune(self):
+        t = Tune()
+        _check(lib().ilg_get_tune(self._h, C.byref(t)))
+        return {k: v for k, v in t.as_dict().items() if not k.endswith("_us")}
 
     def stats(self):
         a, b, c = C.c_double(), C.c_double(), C.c_double()

@@ -287,6 +287,7 @@ static int build(Batch& b) {
   v.cblocks = b.cblocks.p; v.ncblocks = (int)ncb;
   v.work = b.work.p; v.counters = b.counters.p; v.derr = b.derr.p; v.mesh_flag = b.mesh_flag.p;
   v.barrier = b.barrier.p;
+  v.tune = b.members[0]->c.tune;   // direct-insolation shapes; conduction uses the block table
   b.plan.precision = b.precision;
   b.plan.rad_on = b.ntiles > 0;
   b.plan.rec_on = nrec > 0;

@@ -168,6 +168,7 @@ static StepView solo_view(Context& c, int precision) {
   v.work = c.work.p; v.counters = c.counters.p; v.derr = c.derr.p; v.mesh_flag = c.mesh_flag.p;
   v.barrier = c.barrier.p;
   v.rho64 = nullptr; v.rho32 = nullptr;
+  v.tune = c.tune;
   (void)precision;
   return v;
 }
@@ -367,6 +368,37 @@ static int set_host_sun(Context& c, const double* sun) {
 }  // namespace ilg
 
 using namespace ilg;
+
+// Autotuner helpers (ilg_autotune).
+namespace {
+// Mean device time (us) of `reps` launches after two warm-up launches.
+template <class F>
+int time_launches(Context& c, F&& launch, int reps, double* us) {
+  cudaEvent_t a = nullptr, b = nullptr;
+  ILG_CUDA(cudaEventCreate(&a));
+  ILG_CUDA(cudaEventCreate(&b));
+  int rc = ILG_OK;
+  for (int i = 0; i < 2 && rc == ILG_OK; ++i) rc = launch();
+  if (rc == ILG_OK) rc = cudaEventRecord(a, c.stream) == cudaSuccess ? ILG_OK : ILG_ERR_CUDA;
+  for (int i = 0; i < reps && rc == ILG_OK; ++i) rc = launch();
+  float ms = 0.f;
+  if (rc == ILG_OK && (cudaEventRecord(b, c.stream) != cudaSuccess || cudaEventSynchronize(b) != cudaSuccess ||
+                       cudaEventElapsedTime(&ms, a, b) != cudaSuccess)) {
+    set_error("autotune timing failed");
+    rc = ILG_ERR_CUDA;
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  *us = 1000.0 * ms / reps;
+  return rc;
+}
+
+int scratch_copy(dbuf<double>& d, const double* src, size_t n, cudaStream_t s) {
+  ILG_TRY(d.alloc(n));
+  ILG_CUDA(cudaMemcpyAsync(d.p, src, n * 8, cudaMemcpyDeviceToDevice, s));
+  return ILG_OK;
+}
+}  // namespace
 
 extern "C" {
 
@@ -855,6 +887,98 @@ int ilg_get_thermal_records(ilg_ctx* ctx, double* out, int* count) {
     ILG_CUDA(cudaMemcpyAsync(out, c.rec.p, (size_t)n * REC_W * 8, cudaMemcpyDeviceToHost, c.stream));
     ILG_CUDA(cudaStreamSynchronize(c.stream));
   }
+  return ILG_OK;
+}
+
+// ---- launch-shape autotuner ----------------------------------------------------
+int ilg_autotune(ilg_ctx* ctx, const ilg_run_opts* opts, int first_sun, ilg_tune* chosen) {
+  if (!ctx) { set_error("ctx is NULL"); return ILG_ERR_ARG; }
+  Context& c = ctx->c;
+  ILG_TRY(check_run(c, opts, false));
+  if (first_sun < 0 || first_sun >= c.nsun) { set_error("first_sun out of range"); return ILG_ERR_ARG; }
+  const ilg_run_opts& o = *opts;
+  cudaStream_t s = c.stream;
+  ILG_TRY(upload_desc(c, solo_desc(c, &o, first_sun)));
+  // the step kernels run on copies of everything they write
+  StepView v = solo_view(c, o.precision);
+  const size_t nt = (size_t)c.nt, nl = (size_t)c.nz * nt;
+  dbuf<double> sE, srad, sTs, sFs, sQp, sra, sta, stm;
+  ILG_TRY(scratch_copy(sE, c.E.p, nt, s));
+  ILG_TRY(scratch_copy(srad, c.rad.p, nt, s));
+  ILG_TRY(scratch_copy(sTs, c.Tsurf.p, nt, s));
+  ILG_TRY(scratch_copy(sFs, c.Fsurf.p, nt, s));
+  ILG_TRY(scratch_copy(sQp, c.Qprev.p, nt, s));
+  ILG_TRY(scratch_copy(sra, c.rad_avg.p, nt, s));
+  ILG_TRY(scratch_copy(sta, c.therm_avg.p, nt, s));
+  ILG_TRY(scratch_copy(stm, c.therm_max.p, nt, s));
+  v.E = sE.p; v.rad = srad.p; v.Tsurf = sTs.p; v.Fsurf = sFs.p; v.Qprev = sQp.p;
+  v.rad_avg = sra.p; v.therm_avg = sta.p; v.therm_max = stm.p;
+  dbuf<float> sT32;
+  dbuf<float2> sTdf;
+  if (o.precision == ILG_PREC_MIXED) {
+    ILG_TRY(sT32.alloc(nl));
+    ILG_CUDA(cudaMemcpyAsync(sT32.p, c.T32.p, nl * 4, cudaMemcpyDeviceToDevice, s));
+    v.T32 = sT32.p;
+  } else {
+    ILG_TRY(sTdf.alloc(nl));
+    ILG_CUDA(cudaMemcpyAsync(sTdf.p, c.Tdf.p, nl * 8, cudaMemcpyDeviceToDevice, s));
+    v.Tdf = sTdf.p;
+  }
+  const int mu32 = o.precision == ILG_PREC_MIXED ? 1 : 0;
+  const int reps = 10;
+  TuneCfg best = c.tune;
+  double best_d = 1e300, best_c = 1e300, us = 0.0;
+  for (int cb : {128, 256, 512})
+    for (int nf : {4, 8, 16, 32}) {
+      v.tune.classify_threads = cb;
+      v.tune.exact_facets = nf;
+      ILG_TRY(time_launches(c, [&] { return direct_launch(v, 0, mu32, s); }, reps, &us));
+      if (us < best_d) { best_d = us; best.classify_threads = cb; best.exact_facets = nf; }
+    }
+  v.tune.classify_threads = best.classify_threads;
+  v.tune.exact_facets = best.exact_facets;
+  for (int bs : {32, 64, 128}) {
+    v.tune.conduct_threads = bs;
+    ILG_TRY(time_launches(c, [&] { return conduction_launch(v, v.rad, o.precision, 1, c.nz, s); }, reps, &us));
+    if (us < best_c) { best_c = us; best.conduct_threads = bs; }
+  }
+  ILG_CUDA(cudaStreamSynchronize(s));
+  ILG_TRY(read_device_errors(c));
+  c.tune = best;
+  invalidate_graph(c);   // captured with the previous shapes
+  if (chosen) {
+    chosen->classify_threads = best.classify_threads;
+    chosen->exact_facets = best.exact_facets;
+    chosen->conduct_threads = best.conduct_threads;
+    chosen->direct_us = best_d;
+    chosen->conduct_us = best_c;
+  }
+  return ILG_OK;
+}
+
+int ilg_set_tune(ilg_ctx* ctx, const ilg_tune* t) {
+  if (!ctx || !t) { set_error("invalid arguments"); return ILG_ERR_ARG; }
+  if ((t->classify_threads != 128 && t->classify_threads != 256 && t->classify_threads != 512) ||
+      (t->exact_facets != 4 && t->exact_facets != 8 && t->exact_facets != 16 && t->exact_facets != 32) ||
+      (t->conduct_threads != 32 && t->conduct_threads != 64 && t->conduct_threads != 128)) {
+    set_error("unsupported launch shape");
+    return ILG_ERR_ARG;
+  }
+  Context& c = ctx->c;
+  c.tune.classify_threads = t->classify_threads;
+  c.tune.exact_facets = t->exact_facets;
+  c.tune.conduct_threads = t->conduct_threads;
+  invalidate_graph(c);
+  return ILG_OK;
+}
+
+int ilg_get_tune(const ilg_ctx* ctx, ilg_tune* t) {
+  if (!ctx || !t) { set_error("invalid arguments"); return ILG_ERR_ARG; }
+  t->classify_threads = ctx->c.tune.classify_threads;
+  t->exact_facets = ctx->c.tune.exact_facets;
+  t->conduct_threads = ctx->c.tune.conduct_threads;
+  t->direct_us = 0.0;
+  t->conduct_us = 0.0;
   return ILG_OK;
 }
 

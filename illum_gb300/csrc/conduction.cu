@@ -202,52 +202,34 @@ k_conduct(StepView v, const double* __restrict__ Qnp1, int upd) {
   const double Q = Qnp1[g];
   double T0n, Tsn, Fs;
   R top, dtop;   // T1(n+1) and its increment, in the state's type
+  bool done_top = false;
   if constexpr (std::is_same<R, float>::value) {
-    // fp32 state: the boundary rows in fp32 as well (Newton to ~2 ulp)
-    const float T0 = Ti, T1 = Tip1, rho1 = rho_next;
-    const float Ts = (float)v.Tsurf[g], Qf = (float)Q;
-    float t0n, tsn;
-    if (cs.bc == 0) {
-      const float Qn = (float)v.Qprev[g];
-      float Tr3 = Ts * Ts * Ts;
-      float arad = -3.f * cs.esf * Tr3 * Ts;
-      float brad = 2.f * cs.esf * Tr3;
-      float den = cs.k1f + brad;
-      float ann = (Qn - arad) / den, annp1 = (Qf - arad) / den, bn = (cs.k1f - brad) / den;
-      float b0 = 1.f + cs.alpha0f + cs.gamma0f - cs.gamma0f * bn;
-      float r0 = cs.gamma0f * (annp1 + ann) + (1.f - cs.alpha0f - cs.gamma0f + cs.gamma0f * bn) * T0 +
-                 cs.alpha0f * T1;
-      float piv = b0 + cs.f0f * cs.gamma1f;
-      if (piv == 0.f) { atomicExch(&v.derr[DERR_PIVOT], 1); return; }
-      r0 -= b0 * T0 - cs.alpha0f * T1;
-      t0n = (r0 - cs.f0f * rho1) / piv + T0;
-      tsn = 0.5f * (annp1 + bn * t0n + t0n);
-    } else if (cs.bc == 1) {
-      float R0 = 2.f * cs.alpha0f * (T1 - T0) + 4.f * cs.gamma0f * (Ts - T0) - 2.f * cs.gamma0f * Ts;
-      float P = (R0 - cs.f0f * rho1) * cs.inv_Apf + T0;
-      const float A = Qf + 2.f * cs.k1f * P;
-      float x = Ts;
+    if (cs.bc == 1) {
+      // fp32 state, Newton boundary: P = T1(n+1) - S_top Ts(n+1) is a small
+      // difference of temperature-sized terms when S_top ~ 1, and the root
+      // moves by 2 k1 dP / |g'| (large for conductive materials), so P, A
+      // and T1(n+1) are formed in FP64; the root itself is found in FP32
+      // (to ~2 ulp; A is accurate, and g's rounding is ~ulp(x) |g'|).
+      const double T0 = (double)Ti, T1 = (double)Tip1, Ts = v.Tsurf[g];
+      const double R0 = 2.0 * cs.alpha0 * (T1 - T0) + 4.0 * cs.gamma0 * (Ts - T0) - 2.0 * cs.gamma0 * Ts;
+      const double P = (R0 - cs.f0 * (double)rho_next) * cs.inv_Ap + T0;
+      const float A = (float)(Q + 2.0 * cs.k1 * P);
+      float x = (float)Ts;
       for (int it = 0; it < 30; ++it) {
         float x3 = x * x * x;
         float dT = (A + cs.B_topf * x - cs.esf * x3 * x) / (cs.B_topf - 4.f * cs.esf * x3);
         x -= dT;
         if (fabsf(dT) <= 2.4e-7f * fabsf(x)) break;
       }
-      tsn = x;
-      t0n = P + cs.S_topf * tsn;
-    } else {
-      float b0 = 1.f + cs.alpha0f + cs.gamma0f;
-      float r0 = cs.alpha0f * T1 + (1.f - cs.alpha0f - cs.gamma0f) * T0 + cs.gamma0f * (Ts + Qf);
-      r0 -= b0 * T0 - cs.alpha0f * T1;
-      t0n = (r0 - cs.f0f * rho1) / (b0 + cs.f0f * cs.gamma1f) + T0;
-      tsn = Qf;
+      Tsn = (double)x;
+      T0n = P + cs.S_top * Tsn;
+      top = (float)T0n;
+      dtop = (float)(T0n - T0);
+      Fs = -(T0n - Tsn) * cs.kz;
+      done_top = true;
     }
-    top = t0n;
-    dtop = t0n - T0;
-    T0n = (double)t0n;
-    Tsn = cs.bc == 2 ? Q : (double)tsn;
-    Fs = (double)(-(t0n - tsn) * cs.kzf);
-  } else {
+  }
+  if (!done_top) {
   double T0 = (double)Ti, T1 = (double)Tip1, rho1 = (double)rho_next;
   double Ts = v.Tsurf[g];
   if (cs.bc == 0) {
@@ -431,9 +413,8 @@ int build_tables(int nz, const double* z, const double* ti, const double* rhoc, 
   cs.kz = k[0] / z[0];
   cs.cgeo = dt / rhoc[nz - 1] * Fgeo / (z[nz - 1] - z[nz - 2]);
   cs.es = emiss * SIGMA_SB;
-  cs.alpha0f = (float)cs.alpha0; cs.gamma0f = (float)cs.gamma0; cs.k1f = (float)cs.k1; cs.f0f = (float)cs.f0;
-  cs.gamma1f = (float)cs.gamma1; cs.esf = (float)cs.es; cs.inv_Apf = (float)cs.inv_Ap;
-  cs.S_topf = (float)cs.S_top; cs.B_topf = (float)cs.B_top; cs.kzf = (float)cs.kz;
+  cs.esf = (float)cs.es;
+  cs.B_topf = (float)cs.B_top;
   cs.nz = nz;
   cs.bc = bc;
   return ILG_OK;
@@ -472,6 +453,11 @@ int conduction_setup() {
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_LIMIT));
   ILG_CUDA(cudaFuncSetAttribute(k_conduct<float, true, COND_STEP_THREADS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)SMEM_LIMIT));
+  // the other block sizes ilg_autotune may choose for single-mesh steps
+  ILG_CUDA(cudaFuncSetAttribute(k_conduct<dfloat, true, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_LIMIT));
+  ILG_CUDA(cudaFuncSetAttribute(k_conduct<dfloat, true, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_LIMIT));
+  ILG_CUDA(cudaFuncSetAttribute(k_conduct<float, true, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_LIMIT));
+  ILG_CUDA(cudaFuncSetAttribute(k_conduct<float, true, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_LIMIT));
   done.store(true, std::memory_order_release);
   return ILG_OK;
 }
@@ -516,8 +502,21 @@ int conduction_state_convert(Context& c, int precision) {
   return ILG_OK;
 }
 
+// Threads per block: the view's tuned value for a single mesh (a batch's
+// block table is cut at COND_STEP_THREADS), COND_STEP_THREADS where the
+// tuned size would not fit the column in shared memory.
 int conduction_launch(const StepView& v, const double* Q, int precision, int upd, int nz_max, cudaStream_t s) {
-  if (precision == ILG_PREC_MIXED) return launch_conduct<float, COND_STEP_THREADS>(v, Q, upd, nz_max, s);
+  int bs = v.cblocks ? COND_STEP_THREADS : v.tune.conduct_threads;
+  if (bs != 32 && bs != 64 && bs != 128) { set_error("conduct_threads must be 32, 64 or 128"); return ILG_ERR_ARG; }
+  const size_t elt = precision == ILG_PREC_MIXED ? sizeof(float) : sizeof(dfloat);
+  if ((size_t)nz_max * bs * elt > SMEM_LIMIT) bs = COND_STEP_THREADS;
+  if (precision == ILG_PREC_MIXED) {
+    if (bs == 32) return launch_conduct<float, 32>(v, Q, upd, nz_max, s);
+    if (bs == 128) return launch_conduct<float, 128>(v, Q, upd, nz_max, s);
+    return launch_conduct<float, COND_STEP_THREADS>(v, Q, upd, nz_max, s);
+  }
+  if (bs == 32) return launch_conduct<dfloat, 32>(v, Q, upd, nz_max, s);
+  if (bs == 128) return launch_conduct<dfloat, 128>(v, Q, upd, nz_max, s);
   return launch_conduct<dfloat, COND_STEP_THREADS>(v, Q, upd, nz_max, s);
 }
 

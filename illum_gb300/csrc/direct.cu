@@ -167,7 +167,8 @@ __global__ void k_direct_classify(StepView v, int dropin, int mu32_flux) {
   }
 }
 
-// Pass 2: blocks of DX_FACETS undecided facets. The GPU's FP64 pipe is slow
+// Pass 2: blocks of NF undecided facets (4..32, chosen by ilg_autotune; few
+// per block spread the FP64 work over many SMs). The GPU's FP64 pipe is slow
 // per instruction, so FP64 runs one lane per facet or per ambiguous
 // sample, and the FP64 set-up overlaps the FP32 filter:
 //   warp 0, one lane per facet: the sun frame (T, B) of geom.h sun_frame and
@@ -185,7 +186,6 @@ __global__ void k_direct_classify(StepView v, int dropin, int mu32_flux) {
 // errors; a facet whose sun-frame axis choice is within rounding of a tie
 // lists all its samples. Counts are integer sums, so the result does not
 // depend on the order.
-constexpr int DX_FACETS = 8;    // facets per block: spreads the FP64 work over the SMs
 constexpr int DX_THREADS = 512;
 constexpr int DX_LIST = 4096;   // (facet, sample) pairs per round of the filter
 
@@ -272,15 +272,16 @@ __device__ __forceinline__ void dx_exact_sample(const StepView& v, DxFacet& F, i
   if (sample_lit(p, disk, BTN, hl, M.nphi, M.dphi, M.interp)) atomicAdd(&F.count, 1);
 }
 
+template <int NF>
 __global__ void __launch_bounds__(DX_THREADS) k_direct_exact(StepView v, int dropin, int mu32_flux) {
-  __shared__ DxFacet fs[DX_FACETS];
+  __shared__ DxFacet fs[NF];
   __shared__ int list[DX_LIST];
   __shared__ int nlist;
   const int nw = v.counters[0];
   const int nsamp = v.ndisk - 1;   // samples per facet (the meshes of a view share the disk)
   const int FT = DX_THREADS - 32;  // filter threads (warps 1..)
-  for (int base = blockIdx.x * DX_FACETS; base < nw; base += gridDim.x * DX_FACETS) {
-    const int nf = min(DX_FACETS, nw - base);
+  for (int base = blockIdx.x * NF; base < nw; base += gridDim.x * NF) {
+    const int nf = min(NF, nw - base);
     const int total = nf * nsamp;
     if (threadIdx.x < 32) {
       // FP64 set-up, one lane per facet (overlaps the filter below)
@@ -388,9 +389,17 @@ SunAux make_sun_aux(const double* s, double solar_const, double scene_mag, doubl
 // first.
 int direct_launch(const StepView& v, int dropin, int mu32_flux, cudaStream_t s) {
   ILG_CUDA(cudaMemsetAsync(v.counters, 0, sizeof(int), s));
-  k_direct_classify<<<div_up(v.nt, 256), 256, 0, s>>>(v, dropin, mu32_flux);
+  const int cb = v.tune.classify_threads;
+  if (cb != 128 && cb != 256 && cb != 512) { set_error("classify_threads must be 128, 256 or 512"); return ILG_ERR_ARG; }
+  k_direct_classify<<<div_up(v.nt, cb), cb, 0, s>>>(v, dropin, mu32_flux);
   ILG_CUDA(cudaGetLastError());
-  k_direct_exact<<<152 * 4, DX_THREADS, 0, s>>>(v, dropin, mu32_flux);
+  switch (v.tune.exact_facets) {
+    case 4: k_direct_exact<4><<<152 * 4, DX_THREADS, 0, s>>>(v, dropin, mu32_flux); break;
+    case 8: k_direct_exact<8><<<152 * 4, DX_THREADS, 0, s>>>(v, dropin, mu32_flux); break;
+    case 16: k_direct_exact<16><<<152 * 4, DX_THREADS, 0, s>>>(v, dropin, mu32_flux); break;
+    case 32: k_direct_exact<32><<<152 * 4, DX_THREADS, 0, s>>>(v, dropin, mu32_flux); break;
+    default: set_error("exact_facets must be 4, 8, 16 or 32"); return ILG_ERR_ARG;
+  }
   ILG_CUDA(cudaGetLastError());
   return ILG_OK;
 }

@@ -41,8 +41,7 @@ struct CondScalars {
   double alpha0, gamma0, k1, f0, gamma1, Ap, k0, z0, cgeo, es;
   double inv_Ap, S_top, B_top, kz;   // 1/Ap, 2 gamma0/Ap, 2 k1 (S_top - 1), k0/z0
   int nz, bc;                        // bc: 0 linearised, 1 Newton, 2 prescribed Ts (conductionT)
-  // the same, rounded to fp32 (the fp32 surface boundary)
-  float alpha0f, gamma0f, k1f, f0f, gamma1f, esf, inv_Apf, S_topf, B_topf, kzf;
+  float esf, B_topf;                 // es, B_top rounded to fp32 (the fp32 Newton root)
 };
 
 // Per sun position, precomputed on the host (direct.cu make_sun_aux).
@@ -98,7 +97,16 @@ struct MeshDesc {
 };
 
 // Everything a step kernel touches, as plain device pointers.
+// Launch shapes of the step kernels (ilg_autotune picks them by timing; no
+// result depends on them).
+struct TuneCfg {
+  int classify_threads = 256;   // k_direct_classify threads per block
+  int exact_facets = 8;         // undecided facets per k_direct_exact block
+  int conduct_threads = 64;     // conduction threads per block (single-mesh views)
+};
+
 struct StepView {
+  TuneCfg tune;
   int nt, nmesh;
   MeshDesc* md;
   const int* mesh_of;          // per facet, or nullptr for a single mesh
@@ -144,6 +152,7 @@ struct StepView {
 };
 
 struct Context {
+  TuneCfg tune;
   int nt = 0;
   cudaStream_t stream = nullptr;
   float scene_mag = 1.0f;   // max |coordinate|

@@ -202,6 +202,25 @@ int ilg_get_outputs(ilg_ctx* ctx, double* rad, double* rad_avg, double* therm_av
  * enabled, and per-call counters. */
 int ilg_set_timing(ilg_ctx* ctx, int enable);
 
+/* ---- launch-shape autotuner (no reference counterpart) ------------------------ */
+/* Launch shapes of the step kernels. No result depends on them (every
+ * facet's work is independent of the block it runs in, and the sums are
+ * per facet), only the step's speed. */
+typedef struct ilg_tune {
+  int classify_threads;   /* direct-insolation pass 1, threads per block: 128, 256, 512 */
+  int exact_facets;       /* direct-insolation pass 2, undecided facets per block: 4, 8, 16, 32 */
+  int conduct_threads;    /* conduction, columns per block (single-mesh steps): 32, 64, 128 */
+  double direct_us;       /* ilg_autotune: measured time of the chosen direct shapes (us per step) */
+  double conduct_us;      /* ilg_autotune: measured time of the chosen conduction shape */
+} ilg_tune;
+/* Times every shape on the context's own workload for opts (sun position
+ * first_sun) on scratch copies of the buffers the kernels write (the
+ * context's state is not changed), keeps the fastest and returns it in
+ * *chosen (may be NULL). Requires what ilg_run_steps requires. */
+int ilg_autotune(ilg_ctx* ctx, const ilg_run_opts* opts, int first_sun, ilg_tune* chosen);
+int ilg_set_tune(ilg_ctx* ctx, const ilg_tune* tune);
+int ilg_get_tune(const ilg_ctx* ctx, ilg_tune* tune);
+
 /* ---- thermal records (thermal_model record_stats) ---------------------------- */
 /* Records, for each of the next `capacity` steps (ilg_run_steps,
  * ilg_run_steps_host, or a batch holding the context), 15 FP64 values: the

@@ -318,6 +318,26 @@ def test_mixed_precision_within_tolerance(ilg, oracle_mod, mesh_l4, tol, max_swe
     assert err_s <= TOL_T_MIXED and err_t <= TOL_T_MIXED, (err_s, err_t)
 
 
+def test_mixed_precision_conductive_material(ilg, oracle_mod, mesh_l4):
+    """High thermal inertia (conductive top layer, k1 ~ 1e4 W/m^2 K): the
+    Newton boundary's root is 2 k1 / |g'| times more sensitive to the
+    boundary's P than to the layers, which the fp32 state must not feel."""
+    v, f = mesh_l4
+    nsteps = 300
+    ref = _setup_run(ilg, oracle_mod, v, f, 32, 79, nsteps, precision=0)
+    mix = _setup_run(ilg, oracle_mod, v, f, 32, 79, nsteps, precision=1)
+    out = []
+    for ctx, _, opts, *_ in (ref, mix):
+        tm = ilg.ThermalModel(ctx, meshgen.geometric_depths(79), 1515.0, 1.05e6, 200.0, emissivity=0.95,
+                              bc_mode=1, precision=opts.precision)
+        if opts.precision == 1:
+            opts.tol, opts.max_sweeps = 1e-3, 2
+        ctx.run_steps(opts, 0, nsteps)
+        out.append(tm.T.copy())
+    err = np.abs(out[0] - out[1]).max()
+    assert err <= TOL_T_MIXED, err
+
+
 # ------------------------------------------------------------ edge cases
 def test_single_triangle_and_no_form_factors(ilg, oracle_mod):
     v = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32)
