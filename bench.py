@@ -349,6 +349,8 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=12)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="default launch shapes (profiling runs)")
+    ap.add_argument("--mixed-steps", type=int, default=720, help="steps of the mixed-precision comparison run")
     ap.add_argument("--workload", default="c1", choices=["c1", "batch", "serve", "terrain"],
                     help="c1: one 81,920-facet mesh (default); batch: 64 meshes as one batch; serve: request "
                          "loop; terrain: heightmap patch with a form-factor cutoff, mixed precision")
@@ -420,7 +422,7 @@ def main():
     opts = ig.RunOpts(dt=W["dt"], tol=c["tol"], max_sweeps=200, use_radiosity=1, use_graph=1,
                       precision=ig.PREC_FP64, coupling=ig.COUPLE_DIRECT)
     # launch shapes of the step kernels, timed on this workload (state untouched)
-    tune = ctx.autotune(opts, first_sun=0)
+    tune = None if args.no_autotune else ctx.autotune(opts, first_sun=0)
     # warm-up (graph capture included)
     run_chunks(lambda s, k: ctx.bench_steps(opts, s, k, 256.0), 0, args.warmup, nsun)
     sun_pos = args.warmup
@@ -472,9 +474,9 @@ def main():
         Wf = build_workload(ig, meshgen, precision=ig.PREC_FP64)
         mopts = ig.RunOpts(dt=W["dt"], tol=MIXED_TOL, max_sweeps=MIXED_SWEEPS, use_radiosity=1, use_graph=1,
                            precision=ig.PREC_MIXED, coupling=ig.COUPLE_DIRECT)
-        nchk = 720
+        nchk = args.mixed_steps
         Wf["ctx"].run_steps(opts, 0, nchk)
-        mtune = Wm["ctx"].autotune(mopts, first_sun=0)
+        mtune = None if args.no_autotune else Wm["ctx"].autotune(mopts, first_sun=0)
         mres = Wm["ctx"].bench_steps(mopts, 0, nchk, 256.0)
         err = float(np.abs(Wf["tm"].T - Wm["tm"].T).max())
         mval = N * nchk / (mres[0].sum() / 1000.0)
