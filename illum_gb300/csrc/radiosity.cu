@@ -32,7 +32,12 @@
 // and the running sum is kept as an unevaluated float pair by TwoSum
 // (Dekker 1971; Knuth TAOCP vol. 2, 4.2.2). The relative error of a row sum
 // is ~2^-46 (vs 2^-53 for FP64), orders of magnitude below the solve
-// tolerance; everything per row (residual, iterate, convergence) is FP64.
+// tolerance. The iterate is kept as its scattered part s = x - E, also a
+// double-float, with E in FP64: x = E + s is formed in FP64 only when the
+// solve ends, so the result carries E exactly and s to ~2^-46 of |s|
+// (|s| <= albedo * max x). Per row and sweep the finishing work (s' = F x,
+// the change s' - s, the halo copy x' = E + s') is FP32 arithmetic, and the
+// squared changes are summed in FP32 (a stop decision needs a few digits).
 //
 // The double-float values are stored as two arrays, hi = fl(F) and
 // lo = fl(F - hi).
@@ -341,15 +346,19 @@ __device__ __forceinline__ void tile_rows(const StepView& v, const RowTile& T, i
   __syncthreads();
 }
 
-// Block sum in a fixed order; thread 0 stores it. Ends with a block barrier
-// (the tile's shared arrays are free again).
-__device__ __forceinline__ void block_sum_store(double d, double* red, double* out) {
-  d = warp_sum(d);
+// Block sum in a fixed order (FP32); thread 0 stores it. Ends with a block
+// barrier (the tile's shared arrays are free again).
+__device__ __forceinline__ float warp_sumf(float x) {
+  for (int o = 16; o; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+  return x;
+}
+__device__ __forceinline__ void block_sum_store(float d, float* red, double* out) {
+  d = warp_sumf(d);
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = d;
   __syncthreads();
   if (threadIdx.x < 32) {
-    double t = warp_sum(red[threadIdx.x]);
-    if (threadIdx.x == 0) *out = t;
+    float t = warp_sumf(red[threadIdx.x]);
+    if (threadIdx.x == 0) *out = (double)t;
   }
   __syncthreads();
 }
@@ -405,40 +414,51 @@ __device__ __forceinline__ int decide_meshes(const StepView& v, MeshState& st, i
   return running;
 }
 
-// The solve works on radiosity positions (Morton order within each mesh):
-// EP = E, P0 / P1 = iterates, gathered through rperm at entry, H0 / H1 the
-// iterates' double-float copies (what the halos gather) and EH = E as a
-// double-float (the copies are updated in FP32 arithmetic). Start values:
-// rows without entries are x = E exactly; the others start at E (cold) or
-// at the mesh's previous solution, extrapolated linearly once two solutions
-// exist (warm). The warm start predicts the scattered part S = x - E and
-// takes the step's own E: x0 = E + S(n) + (S(n) - S(n-1)). E jumps where
-// a facet enters or leaves shadow; S = F x varies smoothly, so the start is
-// off by about F dE there instead of dE. sprev holds S(n) and, after it,
-// its last change.
+// The solve works on radiosity positions (Morton order within each mesh),
+// gathered through rperm at entry: EP = E (FP64), S0 / S1 = the iterates'
+// scattered parts s = x - E (double-floats), H0 / H1 = the iterates
+// x = E + s as double-floats (what the halos gather) and EH = E as a
+// double-float. Start values: rows without entries are x = E exactly
+// (s = 0); the others start at s = 0 (cold) or at the mesh's previous
+// solution, extrapolated linearly once two solutions exist (warm). The warm
+// start predicts the scattered part and takes the step's own E:
+// s0 = S(n) + (S(n) - S(n-1)). E jumps where a facet enters or leaves
+// shadow; S = F x varies smoothly, so the start is off by about F dE there
+// instead of dE. sprev holds S(n) and, after it, its last change.
+struct RadBufs {
+  double* EP;
+  float2 *S0, *S1, *H0, *H1, *EH;
+  __device__ __forceinline__ explicit RadBufs(const StepView& v) {
+    EP = v.rbuf;
+    S0 = reinterpret_cast<float2*>(v.rbuf + v.nt);
+    S1 = reinterpret_cast<float2*>(v.rbuf + 2 * (size_t)v.nt);
+    H0 = reinterpret_cast<float2*>(v.rbuf + 3 * (size_t)v.nt);
+    H1 = H0 + v.nt;
+    EH = H1 + v.nt;
+  }
+};
+
 __device__ __forceinline__ void init_x(const StepView& v, const double* x, int warm, int gt, int nthreads) {
-  double* EP = v.rbuf;
-  double* P0 = v.rbuf + v.nt;
-  double* P1 = v.rbuf + 2 * (size_t)v.nt;
-  float2* H0 = reinterpret_cast<float2*>(v.rbuf + 3 * (size_t)v.nt);
-  float2* H1 = H0 + v.nt;
-  float2* EH = H1 + v.nt;
+  const RadBufs B(v);
   for (int p = gt; p < v.nt; p += nthreads) {
     int g = (int)v.rperm[p];
     const MeshDesc& M = v.md[mesh_of_facet(v, g)];
     if (!M.active || M.ntiles == 0) continue;
     double e = v.E[g];
-    double x0 = e;
+    float2 s0 = make_float2(0.f, 0.f);
     if (warm && v.row_act[g] && M.frame >= 1) {
-      x0 = e + v.sprev[g];
-      if (M.frame >= 2) x0 += v.sprev[v.nt + g];
+      double s = v.sprev[g];
+      if (M.frame >= 2) s += v.sprev[v.nt + g];
+      s0 = split_df(s);
     }
-    EP[p] = e;
-    P0[p] = x0;
-    P1[p] = e;
-    H0[p] = split_df(x0);
-    H1[p] = split_df(e);
-    EH[p] = H1[p];
+    const float2 eh = split_df(e);
+    const float2 x0 = df_add(eh, s0);
+    B.EP[p] = e;
+    B.S0[p] = s0;
+    B.S1[p] = make_float2(0.f, 0.f);
+    B.H0[p] = x0;
+    B.H1[p] = x0;
+    B.EH[p] = eh;
     if (v.x32) {
       v.x32[p] = 0.f;
       v.x32[v.nt + p] = 0.f;
@@ -446,22 +466,20 @@ __device__ __forceinline__ void init_x(const StepView& v, const double* x, int w
   }
 }
 
-// Scatter the solved meshes' last iterate back to facet order; warm solves
-// also record S = x - E and its change for the next step's start.
+// Scatter the solved meshes' last iterate x = E + s back to facet order
+// (FP64); warm solves also record s and its change for the next step's
+// start. Rows without entries keep s = 0 in both buffers.
 __device__ __forceinline__ void scatter_x(const StepView& v, const MeshState& st, double* x, int warm, int gt,
                                           int nthreads, bool mixed) {
-  const double* EP = v.rbuf;
-  const double* P0 = v.rbuf + v.nt;
-  const double* P1 = v.rbuf + 2 * (size_t)v.nt;
+  const RadBufs B(v);
   for (int p = gt; p < v.nt; p += nthreads) {
     int g = (int)v.rperm[p];
     int m = mesh_of_facet(v, g);
     const MeshDesc& M = v.md[m];
     if (!M.active || M.ntiles == 0) continue;
-    double xs = (!mixed && (st.sweeps[m] & 1)) ? ld_it(P1 + p) : ld_it(P0 + p);
-    x[g] = xs;
+    const double s = df_value(ld_it(((!mixed && (st.sweeps[m] & 1)) ? B.S1 : B.S0) + p));
+    x[g] = B.EP[p] + s;
     if (warm) {
-      double s = xs - EP[p];
       v.sprev[v.nt + g] = s - v.sprev[g];
       v.sprev[g] = s;
     }
@@ -488,7 +506,7 @@ __device__ __forceinline__ RadSmem rad_smem() {
 // FP64 Jacobi to each mesh's tolerance. x: solution (and warm start).
 __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity64(StepView v, double* x, int warm) {
   __shared__ MeshState st;
-  __shared__ double red[32];
+  __shared__ float red[32];
   const RadSmem sm = rad_smem();
   const int gt = blockIdx.x * RAD_THREADS + threadIdx.x;
   const int nthreads = gridDim.x * RAD_THREADS;
@@ -496,12 +514,8 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity64(StepView v, doub
   init_x(v, x, warm, gt, nthreads);
   if (!grid_barrier(v.barrier, gridDim.x, v.derr)) return;
   const uint64_t pol = l2_keep_policy();
-  const double* EP = v.rbuf;
-  double* cur = v.rbuf + v.nt;
-  double* nxt = v.rbuf + 2 * (size_t)v.nt;
-  float2* curh = reinterpret_cast<float2*>(v.rbuf + 3 * (size_t)v.nt);
-  float2* nxth = curh + v.nt;
-  const float2* EH = nxth + v.nt;
+  const RadBufs B(v);
+  float2 *cur = B.S0, *nxt = B.S1, *curh = B.H0, *nxth = B.H1;
   for (int par = 0;; par ^= 1) {
     for (int t = blockIdx.x; t < v.ntiles; t += gridDim.x) {
       const RowTile T = v.tiles[t];
@@ -509,21 +523,23 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity64(StepView v, doub
       stage_halo(v, T, curh, sm.sx);
       tile_rows<AccDF>(v, T, t, ValsDF{v.t_vhi, v.t_vlo}, sm.sx, sm.tail, sm.tnew, sm.rs, pol);
       const uint32_t* rows = v.t_row + T.r0;
-      double d2 = 0.0;
+      float d2 = 0.f;
       for (int r = threadIdx.x; r < T.nrows; r += RAD_THREADS) {
         uint32_t i = __ldg(rows + r);
-        const float2 sr = sm.rs[r];
-        double xn = __ldg(EP + i) + df_value(sr);
-        double df = xn - ld_it(cur + i);
-        nxt[i] = xn;
-        nxth[i] = df_add(__ldg(EH + i), sr);
-        d2 += df * df;
+        const float2 sn = sm.rs[r];          // s' = F x
+        const float2 sc = ld_it(cur + i);
+        // s' - s: exact high-part difference when the two are within a
+        // factor of two, else rounded relative to the change itself
+        const float df = __fadd_rn(__fsub_rn(sn.x, sc.x), __fsub_rn(sn.y, sc.y));
+        nxt[i] = sn;
+        nxth[i] = df_add(__ldg(B.EH + i), sn);
+        d2 = __fmaf_rn(df, df, d2);
       }
       block_sum_store(d2, red, v.tile_d2 + (size_t)par * v.ntiles + t);
     }
     if (!grid_barrier(v.barrier, gridDim.x, v.derr)) return;
-    double* tmp = cur; cur = nxt; nxt = tmp;
-    float2* tmph = curh; curh = nxth; nxth = tmph;
+    float2* tmp = cur; cur = nxt; nxt = tmp;
+    tmp = curh; curh = nxth; nxth = tmp;
     if (decide_meshes(v, st, 1, 0, par) == 0) break;
   }
   scatter_x(v, st, x, warm, gt, nthreads, false);
@@ -535,7 +551,7 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity64(StepView v, doub
 // update of the round that reaches max_sweeps.
 __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity_mixed(StepView v, double* x, int warm) {
   __shared__ MeshState st;
-  __shared__ double red[32];
+  __shared__ float red[32];
   const RadSmem sm = rad_smem();
   float* sxf = reinterpret_cast<float*>(sm.sx);
   float* tailf = reinterpret_cast<float*>(sm.tail);
@@ -549,9 +565,9 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity_mixed(StepView v, 
   init_x(v, x, warm, gt, nthreads);
   if (!grid_barrier(v.barrier, gridDim.x, v.derr)) return;
   const uint64_t pol = l2_keep_policy();
-  const double* EP = v.rbuf;
-  double* X = v.rbuf + v.nt;          // the fp64 iterate (radiosity positions)
-  float2* XH = reinterpret_cast<float2*>(v.rbuf + 3 * (size_t)v.nt);   // its double-float copy
+  const RadBufs B(v);
+  float2* S = B.S0;     // the iterate's scattered part s = x - E (radiosity positions)
+  float2* XH = B.H0;    // x = E + s, what the halos gather
   int first = 1;
   for (int par = 0;; par ^= 1) {
     for (int t = blockIdx.x; t < v.ntiles; t += gridDim.x) {
@@ -560,13 +576,15 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity_mixed(StepView v, 
       stage_halo(v, T, XH, sm.sx);
       tile_rows<AccDF>(v, T, t, ValsHi{v.t_vhi}, sm.sx, sm.tail, sm.tnew, sm.rs, pol);
       const uint32_t* rows = v.t_row + T.r0;
-      double d2 = 0.0;
+      float d2 = 0.f;
       for (int r = threadIdx.x; r < T.nrows; r += RAD_THREADS) {
         uint32_t i = __ldg(rows + r);
-        double res = __ldg(EP + i) + df_value(sm.rs[r]) - ld_it(X + i);
-        r32[i] = (float)res;
-        xa[i] = (float)res;     // inner start: d0 = r
-        d2 += res * res;
+        // r = E + fl(F) x - x = fl(F) x - s
+        const float2 fx = sm.rs[r], s = ld_it(S + i);
+        const float res = __fadd_rn(__fsub_rn(fx.x, s.x), __fsub_rn(fx.y, s.y));
+        r32[i] = res;
+        xa[i] = res;     // inner start: d0 = r
+        d2 = __fmaf_rn(res, res, d2);
       }
       block_sum_store(d2, red, v.tile_d2 + (size_t)par * v.ntiles + t);
     }
@@ -592,9 +610,9 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity_mixed(StepView v, 
         } else {   // last sweep: nobody reads d again, x += d directly
           for (int r = threadIdx.x; r < T.nrows; r += RAD_THREADS) {
             uint32_t i = __ldg(rows + r);
-            const float d = ld_it(r32 + i) + __ldg(scale + r) * rsf[r];
-            X[i] = ld_it(X + i) + (double)d;
-            XH[i] = df_add(ld_it(XH + i), make_float2(d, 0.f));
+            const float2 d = make_float2(ld_it(r32 + i) + __ldg(scale + r) * rsf[r], 0.f);
+            S[i] = df_add(ld_it(S + i), d);
+            XH[i] = df_add(ld_it(XH + i), d);
           }
         }
         __syncthreads();
