@@ -170,7 +170,7 @@ static int build(Batch& b) {
   ILG_TRY(b.t_halo.alloc(nhal > 0 ? nhal : 1));
   ILG_TRY(b.row_act.alloc(nt));
   ILG_TRY(b.work.alloc(nt)); ILG_TRY(b.counters.alloc(8)); ILG_TRY(b.derr.alloc(DERR_COUNT));
-  ILG_TRY(b.mesh_flag.alloc(n)); ILG_TRY(b.barrier.alloc(2));
+  ILG_TRY(b.mesh_flag.alloc(n)); ILG_TRY(b.barrier.alloc(radiosity_barrier_words(n)));
   // the members' tiles, shifted to the scene's arrays
   std::vector<RowTile> th;
   {

@@ -420,7 +420,7 @@ int ilg_ctx_create(const float* verts, int nv, const int32_t* tris, int nt, cons
   for (auto& e : c.ev)
     if (cudaEventCreate(&e) != cudaSuccess) { set_error("cudaEventCreate failed"); delete h; return ILG_ERR_CUDA; }
   if ((rc = c.derr.alloc(DERR_COUNT)) || (rc = c.counters.alloc(8)) || (rc = c.work.alloc(nt)) ||
-      (rc = c.barrier.alloc(2)) || (rc = c.md.alloc(1)) || (rc = c.mesh_flag.alloc(1))) {
+      (rc = c.barrier.alloc(radiosity_barrier_words(1))) || (rc = c.md.alloc(1)) || (rc = c.mesh_flag.alloc(1))) {
     delete h;
     return rc;
   }

@@ -290,6 +290,9 @@ int radiosity_prepare(Context& c);
 int radiosity_grid(int ntiles, int precision);
 int radiosity_max_meshes();
 int radiosity_threads();
+// unsigned words of a view's barrier buffer: the grid barrier's counter and
+// the per-mesh residual accumulators of the radiosity kernels
+size_t radiosity_barrier_words(int nmesh);
 int radiosity_launch(const StepView& v, double* x, int warm, int precision, int grid, cudaStream_t s);
 
 // ---- capi.cu ----

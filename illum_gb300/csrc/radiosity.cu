@@ -14,9 +14,9 @@
 // tile's entries, row after row, are split into equal runs, one per thread
 // (entries of a row that straddles threads are combined in a fixed order),
 // so every thread of every block does the same amount of work whatever the
-// row lengths. Every block reduces the per-tile residual partials in the
-// same fixed order, so all blocks take the same stop decisions and results
-// are run-to-run deterministic. The residual of iterate x_k is
+// row lengths. The per-tile residual partials meet in integer accumulators
+// (order-independent sums), so all blocks take the same stop decisions and
+// results are run-to-run deterministic. The residual of iterate x_k is
 // E - (I - F) x_k = x_{k+1} - x_k, so it comes for free with the next sweep;
 // iteration stops once its 2-norm is <= tol.
 // With albedo-scaled form factors the iteration matrix has spectral radius
@@ -77,25 +77,25 @@ constexpr int64_t RAD_ROW_COST = 32;     // a row's finishing work, in entries (
 constexpr size_t RAD_SMEM =
     (size_t)RAD_HALO * sizeof(float2) + RAD_THREADS * sizeof(float2) + RAD_ROWS * sizeof(float2) + RAD_THREADS;
 
-// Grid barrier for a cooperative launch (all blocks co-resident). The wait
-// is bounded: after ~2^26 polls it records DERR_BARRIER and returns false.
-// The fences make the iterates written before the barrier visible to the
-// loads after it.
-__device__ bool grid_barrier(unsigned* bar, unsigned nblocks, int* derr) {
+// Grid barrier for a cooperative launch (all blocks co-resident) on an
+// arrival counter that only grows during the launch (zeroed before it):
+// every block counts its barriers in gen, and barrier number gen opens once
+// the counter reaches gen * nblocks, so the last block to arrive releases
+// the others with its own increment (no reset on the critical path). The
+// wait is bounded: after ~2^26 polls it records DERR_BARRIER and returns
+// false. The fences make the iterates written before the barrier visible to
+// the loads after it.
+__device__ bool grid_barrier(unsigned* bar, unsigned nblocks, unsigned& gen, int* derr) {
   __shared__ int ok;
+  ++gen;
   __syncthreads();
   if (threadIdx.x == 0) {
     ok = 1;
-    volatile unsigned* gen = bar + 1;
-    unsigned g = *gen;
+    const unsigned target = gen * nblocks;
     __threadfence();
-    if (atomicAdd(bar, 1u) == nblocks - 1) {
-      atomicExch(bar, 0u);
-      __threadfence();
-      atomicAdd(bar + 1, 1u);
-    } else {
+    if (atomicAdd(bar, 1u) + 1u < target) {
       long long it = 0;
-      while (*gen == g) {
+      while (*(volatile unsigned*)bar < target) {
         if (++it > (1LL << 26) || *(volatile int*)&derr[DERR_BARRIER]) {
           atomicExch(&derr[DERR_BARRIER], 1);
           ok = 0;
@@ -346,72 +346,116 @@ __device__ __forceinline__ void tile_rows(const StepView& v, const RowTile& T, i
   __syncthreads();
 }
 
-// Block sum in a fixed order (FP32); thread 0 stores it. Ends with a block
+// Block sum in a fixed order (FP32), valid in thread 0. Ends with a block
 // barrier (the tile's shared arrays are free again).
 __device__ __forceinline__ float warp_sumf(float x) {
   for (int o = 16; o; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
   return x;
 }
-__device__ __forceinline__ void block_sum_store(float d, float* red, double* out) {
+__device__ __forceinline__ float block_sum(float d, float* red) {
   d = warp_sumf(d);
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = d;
   __syncthreads();
-  if (threadIdx.x < 32) {
-    float t = warp_sumf(red[threadIdx.x]);
-    if (threadIdx.x == 0) *out = (double)t;
-  }
+  float t = 0.f;
+  if (threadIdx.x < 32) t = warp_sumf(red[threadIdx.x]);
   __syncthreads();
+  return t;
 }
 
-// Per-mesh convergence: a mesh's residual is the sum of its tiles' partials
-// (lane-strided over the tiles, then a fixed warp tree), computed by every
-// block for every running mesh, so all blocks take the same decisions
-// without another barrier, and a mesh's decisions are the same alone and in
-// a batch. Tile partials are double-buffered by sweep parity: a block that
-// runs ahead into the next sweep writes the other buffer.
+// Per-mesh convergence. Each tile's squared change (FP32 partial) is
+// recorded in tile_d2 (double-buffered by sweep parity) and added, as an
+// integer, to its mesh's accumulator: the partial in units of tol^2 / 2^20,
+// rounded up and capped at 2^40 (a NaN counts as the cap). Integer sums do
+// not depend on the order of the atomic adds, so every block reads the same
+// total after the grid barrier and takes the same decision with one load,
+// and a mesh's decisions are the same alone and in a batch. A mesh stops
+// when its total is <= 2^20 units, i.e. sum of partials <= tol^2 (at most
+// ntiles units conservative). The accumulators follow the barrier's two
+// counter words, three buffers of nmesh by residual number mod 3: buffer
+// k + 1 is cleared during residual k (its last reader, decision k - 2,
+// finished before the barrier that precedes residual k), and the accumulators
+// of residual 0 are cleared before the first barrier.
+constexpr unsigned long long RES_UNITS = 1ull << 20;
+constexpr unsigned long long RES_CAP = 1ull << 40;
+
+__device__ __forceinline__ unsigned long long* res_acc(const StepView& v, int k) {
+  return reinterpret_cast<unsigned long long*>(v.barrier + 2) + (size_t)(k % 3) * v.nmesh;
+}
+
+// done[m]: 0 running; 1 + (parity of the mesh's last residual) once
+// stopped; 1 for meshes that never ran. unit[m]: residual units per unit of
+// squared change, 2^20 / tol^2 enlarged by 2^-16 so that the FP32 products
+// below never round a partial's units down (+inf when tol is 0).
 struct MeshState {
   int done[RAD_MAX_MESH];
   int sweeps[RAD_MAX_MESH];
+  float unit[RAD_MAX_MESH];
 };
+
+__device__ __forceinline__ unsigned long long res_units(float d2, float unit) {
+  if (isnan(d2)) return RES_CAP;
+  if (!(d2 > 0.f)) return 0ull;
+  const float q = __fmul_ru(d2, unit);
+  return q < (float)RES_CAP ? (unsigned long long)ceilf(q) : RES_CAP;
+}
+
+// Thread 0, after block_sum: record tile t's partial of residual k.
+__device__ __forceinline__ void post_partial(const StepView& v, const MeshState& st, const RowTile& T, int t, int k,
+                                             float d2) {
+  if (threadIdx.x != 0) return;
+  v.tile_d2[(size_t)(k & 1) * v.ntiles + t] = (double)d2;
+  atomicAdd(res_acc(v, k) + T.mesh, res_units(d2, st.unit[T.mesh]));
+  res_acc(v, k + 1)[T.mesh] = 0ull;
+}
 
 __device__ __forceinline__ void init_meshes(const StepView& v, MeshState& st) {
   for (int m = threadIdx.x; m < v.nmesh; m += blockDim.x) {
     const MeshDesc& M = v.md[m];
     st.done[m] = (M.active && M.ntiles > 0) ? 0 : 1;
     st.sweeps[m] = 0;
+    st.unit[m] = M.tol2 > 0.0 ? (float)((double)RES_UNITS / M.tol2 * (1.0 + 1.0 / 65536.0)) : INFINITY;
   }
+  // accumulators of residual 0 (read only after the first barrier)
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+  for (int m = gt; m < v.nmesh; m += gridDim.x * blockDim.x) res_acc(v, 0)[m] = 0ull;
 }
 
-// Every block: totals per running mesh, stop decisions, and the number of
-// meshes still running. Block 0 records the sweep counts and residuals in
-// the mesh table.
-__device__ __forceinline__ int decide_meshes(const StepView& v, MeshState& st, int inc, int first, int par) {
+// Every block, after the barrier that completes residual k: stop decisions
+// and the number of meshes still running. Block 0 records the sweep counts.
+__device__ __forceinline__ int decide_meshes(const StepView& v, MeshState& st, int inc, int first, int k) {
   __syncthreads();
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const double* d2 = v.tile_d2 + (size_t)par * v.ntiles;
-  for (int m = warp; m < v.nmesh; m += RAD_THREADS / 32) {
+  const unsigned long long* acc = res_acc(v, k);
+  for (int m = threadIdx.x; m < v.nmesh; m += blockDim.x) {
     if (st.done[m]) continue;
-    const MeshDesc& M = v.md[m];
-    double t = 0.0;
-    for (int j = lane; j < M.ntiles; j += 32) t += ld_it(d2 + M.tile0 + j);
-    t = warp_sum(t);
-    if (lane == 0) {
-      int sw = st.sweeps[m] + (first ? 0 : inc);
-      st.sweeps[m] = sw;
-      if (t <= M.tol2 || sw >= M.max_sweeps) st.done[m] = 1;
-      if (blockIdx.x == 0) {
-        v.md[m].sweeps = sw;
-        v.md[m].res2 = t;
-      }
-    }
+    const unsigned long long q = __ldcg(acc + m);
+    const int sw = st.sweeps[m] + (first ? 0 : inc);
+    st.sweeps[m] = sw;
+    if (q <= RES_UNITS || sw >= v.md[m].max_sweeps) st.done[m] = 1 + (k & 1);
+    if (blockIdx.x == 0) v.md[m].sweeps = sw;
   }
-  __syncthreads();
   int running = 0;
   for (int m0 = 0; m0 < v.nmesh; m0 += blockDim.x) {
     int m = m0 + threadIdx.x;
     running += __syncthreads_count(m < v.nmesh && !st.done[m]);
   }
   return running;
+}
+
+// Block 0, at the end of the launch: each solved mesh's last residual
+// (sum of its tiles' partials, lane-strided then a fixed warp tree) into
+// the mesh table.
+__device__ __forceinline__ void record_residuals(const StepView& v, const MeshState& st) {
+  if (blockIdx.x != 0) return;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int m = warp; m < v.nmesh; m += RAD_THREADS / 32) {
+    const MeshDesc& M = v.md[m];
+    if (!M.active || M.ntiles == 0) continue;
+    const double* d2 = v.tile_d2 + (size_t)(st.done[m] - 1) * v.ntiles;
+    double t = 0.0;
+    for (int j = lane; j < M.ntiles; j += 32) t += ld_it(d2 + M.tile0 + j);
+    t = warp_sum(t);
+    if (lane == 0) v.md[m].res2 = t;
+  }
 }
 
 // The solve works on radiosity positions (Morton order within each mesh),
@@ -510,19 +554,22 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity64(StepView v, doub
   const RadSmem sm = rad_smem();
   const int gt = blockIdx.x * RAD_THREADS + threadIdx.x;
   const int nthreads = gridDim.x * RAD_THREADS;
+  unsigned gen = 0;
   init_meshes(v, st);
   init_x(v, x, warm, gt, nthreads);
-  if (!grid_barrier(v.barrier, gridDim.x, v.derr)) return;
+  if (!grid_barrier(v.barrier, gridDim.x, gen, v.derr)) return;
   const uint64_t pol = l2_keep_policy();
-  const RadBufs B(v);
-  float2 *cur = B.S0, *nxt = B.S1, *curh = B.H0, *nxth = B.H1;
-  for (int par = 0;; par ^= 1) {
+  for (int it = 0;; ++it) {
     for (int t = blockIdx.x; t < v.ntiles; t += gridDim.x) {
       const RowTile T = v.tiles[t];
       if (st.done[T.mesh]) continue;
-      stage_halo(v, T, curh, sm.sx);
+      const RadBufs B(v);
+      stage_halo(v, T, (it & 1) ? B.H1 : B.H0, sm.sx);
       tile_rows<AccDF>(v, T, t, ValsDF{v.t_vhi, v.t_vlo}, sm.sx, sm.tail, sm.tnew, sm.rs, pol);
       const uint32_t* rows = v.t_row + T.r0;
+      const float2* cur = (it & 1) ? B.S1 : B.S0;
+      float2* nxt = (it & 1) ? B.S0 : B.S1;
+      float2* nxth = (it & 1) ? B.H0 : B.H1;
       float d2 = 0.f;
       for (int r = threadIdx.x; r < T.nrows; r += RAD_THREADS) {
         uint32_t i = __ldg(rows + r);
@@ -535,14 +582,13 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity64(StepView v, doub
         nxth[i] = df_add(__ldg(B.EH + i), sn);
         d2 = __fmaf_rn(df, df, d2);
       }
-      block_sum_store(d2, red, v.tile_d2 + (size_t)par * v.ntiles + t);
+      post_partial(v, st, T, t, it, block_sum(d2, red));
     }
-    if (!grid_barrier(v.barrier, gridDim.x, v.derr)) return;
-    float2* tmp = cur; cur = nxt; nxt = tmp;
-    tmp = curh; curh = nxth; nxth = tmp;
-    if (decide_meshes(v, st, 1, 0, par) == 0) break;
+    if (!grid_barrier(v.barrier, gridDim.x, gen, v.derr)) return;
+    if (decide_meshes(v, st, 1, 0, it) == 0) break;
   }
   scatter_x(v, st, x, warm, gt, nthreads, false);
+  record_residuals(v, st);
 }
 
 // Mixed precision: outer refinement with an fp64 residual r = E - (I - fl(F)) x
@@ -561,15 +607,16 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity_mixed(StepView v, 
   float* xa = v.x32;
   float* xb = v.x32 + v.nt;
   float* r32 = v.x32 + 2 * (size_t)v.nt;
+  unsigned gen = 0;
   init_meshes(v, st);
   init_x(v, x, warm, gt, nthreads);
-  if (!grid_barrier(v.barrier, gridDim.x, v.derr)) return;
+  if (!grid_barrier(v.barrier, gridDim.x, gen, v.derr)) return;
   const uint64_t pol = l2_keep_policy();
   const RadBufs B(v);
   float2* S = B.S0;     // the iterate's scattered part s = x - E (radiosity positions)
   float2* XH = B.H0;    // x = E + s, what the halos gather
   int first = 1;
-  for (int par = 0;; par ^= 1) {
+  for (int round = 0;; ++round) {
     for (int t = blockIdx.x; t < v.ntiles; t += gridDim.x) {
       const RowTile T = v.tiles[t];
       if (st.done[T.mesh]) continue;
@@ -586,10 +633,10 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity_mixed(StepView v, 
         xa[i] = res;     // inner start: d0 = r
         d2 = __fmaf_rn(res, res, d2);
       }
-      block_sum_store(d2, red, v.tile_d2 + (size_t)par * v.ntiles + t);
+      post_partial(v, st, T, t, round, block_sum(d2, red));
     }
-    if (!grid_barrier(v.barrier, gridDim.x, v.derr)) return;
-    int running = decide_meshes(v, st, RAD_INNER, first, par);
+    if (!grid_barrier(v.barrier, gridDim.x, gen, v.derr)) return;
+    int running = decide_meshes(v, st, RAD_INNER, first, round);
     first = 0;
     if (running == 0) break;   // scatter below
     float* cur = xa;
@@ -618,7 +665,7 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity_mixed(StepView v, 
         __syncthreads();
       }
       if (it + 1 < RAD_INNER) {
-        if (!grid_barrier(v.barrier, gridDim.x, v.derr)) return;
+        if (!grid_barrier(v.barrier, gridDim.x, gen, v.derr)) return;
         float* tmp = cur; cur = nxt; nxt = tmp;
       }
     }
@@ -629,17 +676,18 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity_mixed(StepView v, 
       int m = m0 + threadIdx.x;
       bool run = m < v.nmesh && !st.done[m];
       if (run && st.sweeps[m] + RAD_INNER >= v.md[m].max_sweeps) {
-        st.done[m] = 1;
+        st.done[m] = 1 + (round & 1);
         st.sweeps[m] += RAD_INNER;
         if (blockIdx.x == 0) v.md[m].sweeps = st.sweeps[m];
         run = false;
       }
       left += __syncthreads_count(run);
     }
-    if (!grid_barrier(v.barrier, gridDim.x, v.derr)) return;
+    if (!grid_barrier(v.barrier, gridDim.x, gen, v.derr)) return;
     if (left == 0) break;
   }
   scatter_x(v, st, x, warm, gt, nthreads, true);
+  record_residuals(v, st);
 }
 
 // Per-row fp32 scale = max |F_ij| of the row (the bf16 copy stores F/scale).
@@ -939,6 +987,7 @@ int radiosity_prepare(Context& c) {
 
 int radiosity_max_meshes() { return RAD_MAX_MESH; }
 int radiosity_threads() { return RAD_THREADS; }
+size_t radiosity_barrier_words(int nmesh) { return 2 + 2 * 3 * (size_t)(nmesh > 0 ? nmesh : 1); }
 
 // Cooperative grid size for ntiles tiles (at most the co-resident blocks).
 int radiosity_grid(int ntiles, int precision) {
