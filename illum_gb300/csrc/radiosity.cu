@@ -56,6 +56,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <limits>
 #include <mutex>
 #include <thread>
 #include <vector>
@@ -73,7 +74,13 @@ constexpr int RAD_MAX_MESH = 1024;
 constexpr int RAD_INNER = 2;             // fp32 sweeps per refinement of the mixed solve: the bf16 error
                                          // (~4e-3 of the correction) already dominates rho^(k+1), rho ~ 0.013
 constexpr int64_t RAD_MIN_TILE = 16384;  // entries: smaller tiles cost more in staging than they balance
-constexpr int64_t RAD_ROW_COST = 32;     // a row's finishing work, in entries (tile balance)
+// Tile balance, in stored entries: a block's sweep time is about
+// c + 1.35e-4 us per stored entry + 8.8e-4 us per row + 1.5e-4 us per halo
+// facet (per-block timings of the FP64 sweep on GB300, 152 tiles of an
+// 81,920-facet mesh), i.e. a row costs ~7 entries and a halo facet ~1.
+constexpr int64_t RAD_ROW_COST = 7;
+constexpr int64_t RAD_HALO_COST = 1;
+constexpr int64_t RAD_GROUP = 4 * 1024;  // stored entries per group (4 per thread): a tile's stream is whole groups
 constexpr size_t RAD_SMEM =
     (size_t)RAD_HALO * sizeof(float2) + RAD_THREADS * sizeof(float2) + RAD_ROWS * sizeof(float2) + RAD_THREADS;
 
@@ -825,41 +832,67 @@ int radiosity_prepare(Context& c) {
   }
   c.n_active = (int)arow.size();
 
-  // tile cuts: equal shares of the estimated work (entries + RAD_ROW_COST
-  // per row), halo and row caps. Sequential pass: a row is stamped into the
-  // current tile's halo and rolled back if it would overflow it.
+  // Tile cuts. A tile's stream time follows its whole groups (every thread
+  // runs ceil(entries / 4096) groups of four), so tiles get equal group
+  // counts: the smallest ng for which a greedy pass with at most ng * 4096
+  // entries per tile needs no more tiles than co-resident blocks. A second
+  // pass also closes a tile early once its weighed cost (entries + rows +
+  // halo facets) exceeds ng * 4096 plus the first pass's mean row and halo
+  // cost, so row- and halo-heavy tiles carry fewer entries; it is kept if it
+  // still fits the grid. If the halo or row caps force more tiles than
+  // blocks (very large meshes), the cuts are equal shares of the estimated
+  // work (entries + rows), several tiles per block.
   const int G = g_rad_nsm * std::min(g_rad_per_sm64, g_rad_per_smm);
-  int64_t ntarget = std::max<int64_t>(1, std::min<int64_t>(G, (nnz + RAD_MIN_TILE - 1) / RAD_MIN_TILE));
-  const int64_t total_cost = nnz + RAD_ROW_COST * (int64_t)arow.size();
   std::vector<RowTile> tiles;
   std::vector<size_t> tile_a;   // first active row of each tile
-  {
-    std::vector<int> stamp((size_t)nt, -1);
-    std::vector<uint32_t> fresh;
+  std::vector<int> stamp((size_t)nt, -1);
+  std::vector<uint32_t> fresh;
+  const int64_t NOCAP = std::numeric_limits<int64_t>::max() / 4;
+  // One greedy pass. cap > 0: at most cap entries and cap + slack weighed
+  // cost per tile; returns false once more than max_tiles are needed, and
+  // counts the tiles closed by the halo or row caps. cap == 0: cumulative
+  // equal shares of total_cost over ntarget tiles.
+  auto cut = [&](int64_t cap, int64_t slack, int64_t total_cost, int64_t ntarget, size_t max_tiles,
+                 int* capped) -> bool {
+    tiles.clear();
+    tile_a.clear();
+    std::fill(stamp.begin(), stamp.end(), -1);
+    if (capped) *capped = 0;
     int64_t done_cost = 0;
     size_t a = 0;
     while (a < arow.size()) {
+      if (tiles.size() >= max_tiles) return false;
       const int tid = (int)tiles.size();
-      int64_t bound = (int64_t)((double)total_cost * (double)(tid + 1) / (double)ntarget);
+      const int64_t bound = cap > 0 ? 0 : (int64_t)((double)total_cost * (double)(tid + 1) / (double)ntarget);
       int nhalo = 0;
       size_t b = a;
       int64_t ne = 0;
       while (b < arow.size()) {
         int g = (int)order[arow[b]];
-        if (b > a && (int64_t)(b - a) >= RAD_ROWS) break;
+        if (b > a && (int64_t)(b - a) >= RAD_ROWS) {
+          if (capped) ++*capped;
+          break;
+        }
+        const int64_t len = rp[g + 1] - rp[g];
+        if (cap > 0 && b > a && ne + len > cap) break;
         fresh.clear();
         for (int64_t k = rp[g]; k < rp[g + 1]; ++k) {
           uint32_t cpos = (uint32_t)(skey[k] & cmask);
           if (stamp[cpos] != tid) { stamp[cpos] = tid; fresh.push_back(cpos); }
         }
-        if (b > a && nhalo + (int)fresh.size() > RAD_HALO) {
+        const int nh = nhalo + (int)fresh.size();
+        const bool over_halo = nh > RAD_HALO;
+        const bool over_cost =
+            cap > 0 && ne + len + RAD_ROW_COST * (int64_t)(b - a + 1) + RAD_HALO_COST * nh > cap + slack;
+        if (b > a && (over_halo || over_cost)) {
           for (uint32_t cpos : fresh) stamp[cpos] = -1;
+          if (over_halo && capped) ++*capped;
           break;
         }
-        nhalo += (int)fresh.size();
-        ne += rp[g + 1] - rp[g];
+        nhalo = nh;
+        ne += len;
         ++b;
-        if (done_cost + ne + RAD_ROW_COST * (int64_t)(b - a) >= bound && tid + 1 < ntarget) break;
+        if (cap == 0 && done_cost + ne + RAD_ROW_COST * (int64_t)(b - a) >= bound && tid + 1 < ntarget) break;
       }
       RowTile T{};
       T.lam = (int)(((ne + RAD_THREADS - 1) / RAD_THREADS + 3) & ~(int64_t)3);
@@ -870,6 +903,27 @@ int radiosity_prepare(Context& c) {
       tile_a.push_back(a);
       done_cost += ne + RAD_ROW_COST * (int64_t)(b - a);
       a = b;
+    }
+    return true;
+  };
+  {
+    int64_t ng = std::max<int64_t>((RAD_MIN_TILE + RAD_GROUP - 1) / RAD_GROUP,
+                                   (nnz + (int64_t)G * RAD_GROUP - 1) / ((int64_t)G * RAD_GROUP));
+    bool ok = false;
+    int capped = 0;
+    for (int tries = 0; tries < 4; ++tries, ++ng) {
+      ok = cut(ng * RAD_GROUP, NOCAP, 0, 0, (size_t)G, &capped);
+      if (ok || capped > 0) break;   // a larger ng cannot lift the halo / row caps
+    }
+    if (ok && !tiles.empty()) {
+      int64_t extra = 0;
+      for (const RowTile& T : tiles) extra += RAD_ROW_COST * T.nrows + RAD_HALO_COST * T.nhalo;
+      const int64_t slack = extra / (int64_t)tiles.size();
+      if (!cut(ng * RAD_GROUP, slack, 0, 0, (size_t)G, nullptr)) cut(ng * RAD_GROUP, NOCAP, 0, 0, (size_t)G, nullptr);
+    } else if (!ok) {
+      const int64_t ntarget = std::max<int64_t>(1, std::min<int64_t>(G, (nnz + RAD_MIN_TILE - 1) / RAD_MIN_TILE));
+      const int64_t total_cost = nnz + RAD_ROW_COST * (int64_t)arow.size();
+      cut(0, 0, total_cost, ntarget, (size_t)-1, nullptr);
     }
   }
   // offsets of each tile's slots, rows and halo
