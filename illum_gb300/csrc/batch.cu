@@ -44,6 +44,7 @@ struct Batch {
   int nt = 0, precision = 0, nz_max = 0, ntiles = 0;
   int64_t nel = 0;
   cudaStream_t stream = nullptr;
+  StepPipe pipe;
   cudaGraphExec_t graph = nullptr;
   bool graph_broken = false;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -123,7 +124,7 @@ static int build(Batch& b) {
     nH += (int64_t)c.nt * c.nphi;
     nT += (int64_t)c.nt * c.nz;
     ncoef += (int64_t)c.nz * 5;
-    nsun += c.nsun + 1;
+    nsun += c.nsun + 2;   // the table and its two host slots
     ntl += M.ntiles;
     if (M.ntiles) {
       nel += c.tile_elems;
@@ -149,8 +150,9 @@ static int build(Batch& b) {
   ILG_TRY(b.disk.alloc(2 * (size_t)ndisk));
   ILG_TRY(b.disk32.alloc(2 * (size_t)ndisk));
   ILG_TRY(b.suns.alloc(nsun));
-  for (dbuf<double>* d : {&b.Tsurf, &b.Fsurf, &b.Qprev, &b.rad, &b.rad_avg, &b.therm_avg, &b.therm_max, &b.E})
+  for (dbuf<double>* d : {&b.Tsurf, &b.Fsurf, &b.Qprev, &b.rad, &b.rad_avg, &b.therm_avg, &b.therm_max})
     ILG_TRY(d->alloc(nt));
+  ILG_TRY(b.E.alloc(2 * (size_t)nt));   // the direct flux of two consecutive frames
   ILG_TRY(b.sprev.alloc(2 * nt));
   ILG_TRY(b.xtmp.alloc(6 * nt));
   ILG_TRY(b.rperm.alloc(nt));
@@ -212,7 +214,7 @@ static int build(Batch& b) {
     ILG_TRY(cat(b.H, (size_t)M.H0, c.H.p, N * c.nphi, s));
     ILG_TRY(cat(b.H32, (size_t)M.H0, c.H32.p, N * c.nphi, s));
     ILG_TRY(cat(b.hmm32, f0, c.hmm32.p, N, s));
-    ILG_TRY(cat(b.suns, (size_t)M.sun0, c.sun_aux.p, (size_t)c.nsun + 1, s));
+    ILG_TRY(cat(b.suns, (size_t)M.sun0, c.sun_aux.p, (size_t)c.nsun + 2, s));
     ILG_TRY(cat(b.Tsurf, f0, c.Tsurf.p, N, s));
     ILG_TRY(cat(b.Fsurf, f0, c.Fsurf.p, N, s));
     ILG_TRY(cat(b.Qprev, f0, c.Qprev.p, N, s));
@@ -313,7 +315,7 @@ static int batch_graph(Batch& b, cudaGraphExec_t* out) {
   if (b.graph) { *out = b.graph; return ILG_OK; }
   cudaGraph_t g;
   ILG_CUDA(cudaStreamBeginCapture(b.stream, cudaStreamCaptureModeThreadLocal));
-  int rc = enqueue_step(b.v, b.plan, b.stream, nullptr);
+  int rc = enqueue_step_pipe(b.v, b.plan, b.stream, b.pipe);
   cudaError_t e = cudaStreamEndCapture(b.stream, &g);
   if (rc != ILG_OK || e != cudaSuccess) {
     cudaGetLastError();
@@ -359,6 +361,7 @@ int ilg_batch_create(ilg_ctx** members, int n, const ilg_run_opts* opts, ilg_bat
   }
   for (auto& e : b.ev)
     if (cudaEventCreate(&e) != cudaSuccess) { delete h; set_error("cudaEventCreate failed"); return ILG_ERR_CUDA; }
+  if (b.pipe.init() != ILG_OK) { delete h; return ILG_ERR_CUDA; }
   int rc = build(b);
   if (rc != ILG_OK) { delete h; return rc; }
   *out = h;
@@ -376,9 +379,10 @@ int ilg_batch_run(ilg_batch* batch, int nsteps, int use_graph) {
   cudaGraphExec_t g = nullptr;
   if (use_graph && !b.graph_broken)
     if (batch_graph(b, &g) != ILG_OK) { b.graph_broken = true; g = nullptr; cudaGetLastError(); }
+  if (nsteps > 0) ILG_TRY(enqueue_prologue(b.v, b.plan, b.stream));
   for (int s = 0; s < nsteps; ++s) {
     if (g) ILG_CUDA(cudaGraphLaunch(g, b.stream));
-    else ILG_TRY(enqueue_step(b.v, b.plan, b.stream, nullptr));
+    else ILG_TRY(enqueue_step_pipe(b.v, b.plan, b.stream, b.pipe));
   }
   ILG_CUDA(cudaStreamSynchronize(b.stream));
   return batch_errors(b);
@@ -392,11 +396,12 @@ int ilg_batch_bench(ilg_batch* batch, int nsteps, double flush_mb, double* step_
   cudaGraphExec_t g = nullptr;
   if (!b.graph_broken)
     if (batch_graph(b, &g) != ILG_OK) { b.graph_broken = true; g = nullptr; cudaGetLastError(); }
+  if (nsteps > 0) ILG_TRY(enqueue_prologue(b.v, b.plan, b.stream));   // untimed
   for (int s = 0; s < nsteps; ++s) {
     if (nflush) ILG_TRY(flush_launch(b.flush.p, nflush, (unsigned)s, b.stream));
     ILG_CUDA(cudaEventRecord(b.ev[0], b.stream));
     if (g) ILG_CUDA(cudaGraphLaunch(g, b.stream));
-    else ILG_TRY(enqueue_step(b.v, b.plan, b.stream, nullptr));
+    else ILG_TRY(enqueue_step_pipe(b.v, b.plan, b.stream, b.pipe));
     ILG_CUDA(cudaEventRecord(b.ev[3], b.stream));
     ILG_CUDA(cudaEventSynchronize(b.ev[3]));
     float ms = 0.f;

@@ -121,13 +121,48 @@ int flush_launch(float4* buf, size_t n, unsigned salt, cudaStream_t s) {
 // ev (4 events), the phase boundaries are recorded.
 int enqueue_step(const StepView& v, const StepPlan& p, cudaStream_t s, cudaEvent_t* ev) {
   if (ev) ILG_CUDA(cudaEventRecord(ev[0], s));
-  ILG_TRY(direct_launch(v, 0, p.precision == ILG_PREC_MIXED ? 1 : 0, s));
+  ILG_TRY(direct_launch(v, 0, p.precision == ILG_PREC_MIXED ? 1 : 0, 0, s));
   if (ev) ILG_CUDA(cudaEventRecord(ev[1], s));
   if (p.rad_on) ILG_TRY(radiosity_launch(v, v.rad, 1, p.precision, p.rad_grid, s));
   if (ev) ILG_CUDA(cudaEventRecord(ev[2], s));
   ILG_TRY(conduction_launch(v, v.rad, p.precision, 1, p.nz_max, s));
   if (p.rec_on) ILG_TRY(record_launch(v, p.precision, v.cblocks ? v.ncblocks : div_up(v.nt, conduction_step_threads()), s));
   if (ev) ILG_CUDA(cudaEventRecord(ev[3], s));
+  return advance_launch(v, s);
+}
+
+int StepPipe::init() {
+  if (!s2) ILG_CUDA(cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking));
+  if (!fork) ILG_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+  if (!join) ILG_CUDA(cudaEventCreateWithFlags(&join, cudaEventDisableTiming));
+  return ILG_OK;
+}
+
+StepPipe::~StepPipe() {
+  if (fork) cudaEventDestroy(fork);
+  if (join) cudaEventDestroy(join);
+  if (s2) cudaStreamDestroy(s2);
+}
+
+// The current frame's direct flux, before the first pipelined step of a run.
+int enqueue_prologue(const StepView& v, const StepPlan& p, cudaStream_t s) {
+  return direct_launch(v, 0, p.precision == ILG_PREC_MIXED ? 1 : 0, 0, s);
+}
+
+// The step's radiosity reads its frame's E slot; the next frame's direct
+// insolation then writes the other slot on s2 while the conduction runs on
+// s (the two share no array: the conduction reads the radiosity solution,
+// or the current slot for meshes without form factors). Both finish before
+// the advance. Results equal the serial order's bit for bit.
+int enqueue_step_pipe(const StepView& v, const StepPlan& p, cudaStream_t s, const StepPipe& pipe) {
+  if (p.rad_on) ILG_TRY(radiosity_launch(v, v.rad, 1, p.precision, p.rad_grid, s));
+  ILG_CUDA(cudaEventRecord(pipe.fork, s));
+  ILG_CUDA(cudaStreamWaitEvent(pipe.s2, pipe.fork, 0));
+  ILG_TRY(direct_launch(v, 0, p.precision == ILG_PREC_MIXED ? 1 : 0, 1, pipe.s2));
+  ILG_CUDA(cudaEventRecord(pipe.join, pipe.s2));
+  ILG_TRY(conduction_launch(v, v.rad, p.precision, 1, p.nz_max, s));
+  if (p.rec_on) ILG_TRY(record_launch(v, p.precision, v.cblocks ? v.ncblocks : div_up(v.nt, conduction_step_threads()), s));
+  ILG_CUDA(cudaStreamWaitEvent(s, pipe.join, 0));
   return advance_launch(v, s);
 }
 
@@ -219,7 +254,8 @@ static int upload_desc(Context& c, const MeshDesc& M) {
 
 // Per-context scratch of the step kernels, sized before any capture.
 static int ensure_step_buffers(Context& c, int precision) {
-  ILG_TRY(c.E.reserve(c.nt));
+  ILG_TRY(c.pipe.init());
+  ILG_TRY(c.E.reserve(2 * (size_t)c.nt));   // the direct flux of two consecutive frames
   ILG_TRY(c.Q.reserve(c.nt));
   ILG_TRY(c.xtmp.reserve((size_t)6 * c.nt));   // radiosity E, two iterates, double-float copies of both and of E
   if (c.sprev.n < 2 * (size_t)c.nt) {
@@ -262,9 +298,11 @@ static StepPlan solo_plan(Context& c, const ilg_run_opts& o) {
   return p;
 }
 
-// Captures one step; slot >= 0 adds the host sun upload from pinned slot
-// `slot` before and the surface-temperature download into that slot after
-// the step (host-driven steps).
+// Captures one pipelined step; slot >= 0 adds the upload of the next
+// frame's sun from pinned slot `slot` into host slot `slot` before, and the
+// surface-temperature download into pinned slot `slot` after the step
+// (host-driven steps: the graph of slot q runs the steps whose next frame
+// has parity q).
 static int capture_step(Context& c, const ilg_run_opts& o, int slot, cudaGraphExec_t* out) {
   StepView v = solo_view(c, o.precision);
   StepPlan p = solo_plan(c, o);
@@ -272,10 +310,10 @@ static int capture_step(Context& c, const ilg_run_opts& o, int slot, cudaGraphEx
   ILG_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
   int rc = ILG_OK;
   if (slot >= 0)
-    if (cudaMemcpyAsync(c.sun_aux.p + c.nsun, c.pinned_aux + slot * sizeof(SunAux), sizeof(SunAux),
+    if (cudaMemcpyAsync(c.sun_aux.p + c.nsun + slot, c.pinned_aux + slot * sizeof(SunAux), sizeof(SunAux),
                         cudaMemcpyHostToDevice, c.stream) != cudaSuccess)
       rc = ILG_ERR_CUDA;
-  if (rc == ILG_OK) rc = enqueue_step(v, p, c.stream, nullptr);
+  if (rc == ILG_OK) rc = enqueue_step_pipe(v, p, c.stream, c.pipe);
   if (rc == ILG_OK && slot >= 0)
     if (cudaMemcpyAsync(c.pinned_tsurf + (size_t)slot * c.nt, c.Tsurf.p, (size_t)c.nt * 8, cudaMemcpyDeviceToHost,
                         c.stream) != cudaSuccess)
@@ -342,9 +380,9 @@ static int collect_stats(Context& c, bool phases) {
 // Sun positions of the context: a SunAux table of nsun entries plus one
 // host slot (index nsun) for host-driven steps and drop-in calls.
 static int upload_suns(Context& c, const double* suns, int nsun) {
-  std::vector<SunAux> aux((size_t)nsun + 1);
+  std::vector<SunAux> aux((size_t)nsun + 2);   // the table, then the two host slots
   for (int i = 0; i < nsun; ++i) aux[i] = make_sun_aux(suns + 3 * (size_t)i, c.solar_const, c.scene_mag, c.disk_rmax);
-  aux[nsun] = aux[nsun > 0 ? nsun - 1 : 0];
+  aux[nsun] = aux[nsun + 1] = aux[nsun > 0 ? nsun - 1 : 0];
   ILG_TRY(c.sun_aux.alloc(aux.size()));
   ILG_CUDA(cudaMemcpyAsync(c.sun_aux.p, aux.data(), aux.size() * sizeof(SunAux), cudaMemcpyHostToDevice, c.stream));
   ILG_CUDA(cudaStreamSynchronize(c.stream));
@@ -352,16 +390,18 @@ static int upload_suns(Context& c, const double* suns, int nsun) {
   return ILG_OK;
 }
 
-// Put one sun position into the host slot (allocating a one-entry table
-// when no sun table exists yet).
+// Put one sun position into the host slot of frame c.frame_no (allocating
+// the two host slots when no sun table exists yet).
 static int set_host_sun(Context& c, const double* sun) {
   ILG_TRY(ensure_pinned(c));
   if (!c.sun_aux.p) {
-    ILG_TRY(c.sun_aux.alloc(1));
+    ILG_TRY(c.sun_aux.alloc(2));
     c.nsun = 0;
   }
   *(SunAux*)c.pinned_aux = make_sun_aux(sun, c.solar_const, c.scene_mag, c.disk_rmax);
-  ILG_CUDA(cudaMemcpyAsync(c.sun_aux.p + c.nsun, c.pinned_aux, sizeof(SunAux), cudaMemcpyHostToDevice, c.stream));
+  ILG_CUDA(cudaMemcpyAsync(c.sun_aux.p + c.nsun + (c.frame_no & 1), c.pinned_aux, sizeof(SunAux),
+                           cudaMemcpyHostToDevice, c.stream));
+  ILG_CUDA(cudaStreamSynchronize(c.stream));   // the pinned slot is reused at once
   return ILG_OK;
 }
 
@@ -578,7 +618,7 @@ int ilg_direct_radiosity(ilg_ctx* ctx, const double* sun, const double* disk_xy,
   MeshDesc M = solo_desc(c, nullptr, 0);
   M.host_sun = 1;
   ILG_TRY(upload_desc(c, M));
-  ILG_TRY(direct_launch(solo_view(c, ILG_PREC_FP64), 1, 0, c.stream));
+  ILG_TRY(direct_launch(solo_view(c, ILG_PREC_FP64), 1, 0, 0, c.stream));
   ILG_CUDA(cudaMemcpyAsync(out, c.E.p, (size_t)c.nt * 8, cudaMemcpyDeviceToHost, c.stream));
   ILG_CUDA(cudaStreamSynchronize(c.stream));
   return read_device_errors(c);
@@ -599,9 +639,11 @@ int ilg_radiosity_solve(ilg_ctx* ctx, const double* E, double tol, int max_sweep
   o.tol = tol;
   o.max_sweeps = max_sweeps;
   o.use_radiosity = 1;
+  o.coupling = ILG_COUPLE_DIRECT;   // E as given
   MeshDesc M = solo_desc(c, &o, 0);
   ILG_TRY(upload_desc(c, M));
-  ILG_CUDA(cudaMemcpyAsync(c.E.p, E, (size_t)c.nt * 8, cudaMemcpyHostToDevice, c.stream));
+  ILG_CUDA(cudaMemcpyAsync(c.E.p + (size_t)(M.frame & 1) * c.nt, E, (size_t)c.nt * 8, cudaMemcpyHostToDevice,
+                           c.stream));
   StepView v = solo_view(c, ILG_PREC_FP64);
   ILG_TRY(radiosity_launch(v, c.Q.p, 0, ILG_PREC_FP64, radiosity_grid(c.ntiles, ILG_PREC_FP64), c.stream));
   MeshDesc out;
@@ -651,7 +693,7 @@ int ilg_thermal_init(ilg_ctx* ctx, int nz, const double* z, const double* ti, co
   ILG_TRY(c.rad_avg.alloc(nt));
   ILG_TRY(c.therm_avg.alloc(nt));
   ILG_TRY(c.therm_max.alloc(nt));
-  ILG_TRY(c.E.reserve(nt));
+  ILG_TRY(c.E.reserve(2 * (size_t)nt));
   ILG_TRY(c.Q.reserve(nt));
   ILG_CUDA(cudaMemcpyAsync(c.Tdf.p, Tl.data(), n * 8, cudaMemcpyHostToDevice, c.stream));
   ILG_CUDA(cudaMemcpyAsync(c.Tsurf.p, ts.data(), (size_t)nt * 8, cudaMemcpyHostToDevice, c.stream));
@@ -735,9 +777,13 @@ int ilg_run_steps(ilg_ctx* ctx, const ilg_run_opts* opts, int first_sun, int nst
     if (get_graph(c, o, false, &g) != ILG_OK) { c.graph_broken = true; g = nullptr; cudaGetLastError(); }
   StepView v = solo_view(c, o.precision);
   StepPlan p = solo_plan(c, o);
+  // pipelined steps (graph or eager) after a prologue; the phase-timed steps
+  // run in the serial order (same results)
+  if (!timing && nsteps > 0) ILG_TRY(enqueue_prologue(v, p, c.stream));
   for (int s = 0; s < nsteps; ++s) {
     if (g) ILG_CUDA(cudaGraphLaunch(g, c.stream));
-    else ILG_TRY(enqueue_step(v, p, c.stream, timing ? c.ev : nullptr));
+    else if (timing) ILG_TRY(enqueue_step(v, p, c.stream, c.ev));
+    else ILG_TRY(enqueue_step_pipe(v, p, c.stream, c.pipe));
     if (timing) ILG_TRY(collect_stats(c, true));
     if (tsurf_out) {
       ILG_CUDA(cudaMemcpyAsync(c.pinned_tsurf, c.Tsurf.p, (size_t)c.nt * 8, cudaMemcpyDeviceToHost, c.stream));
@@ -755,7 +801,7 @@ int ilg_run_steps_host(ilg_ctx* ctx, const ilg_run_opts* opts, int nsteps, const
   Context& c = ctx->c;
   if (!opts) { set_error("opts is NULL"); return ILG_ERR_ARG; }
   if (c.ndisk < 2) { set_error("sun disk samples are not set (ilg_set_suns)"); return ILG_ERR_ARG; }
-  if (!c.sun_aux.p) { ILG_TRY(c.sun_aux.alloc(1)); c.nsun = 0; }
+  if (!c.sun_aux.p) { ILG_TRY(c.sun_aux.alloc(2)); c.nsun = 0; }
   ILG_TRY(check_run(c, opts, true));
   const ilg_run_opts& o = *opts;
   MeshDesc M = solo_desc(c, &o, 0);
@@ -766,32 +812,46 @@ int ilg_run_steps_host(ilg_ctx* ctx, const ilg_run_opts* opts, int nsteps, const
   if (o.use_graph && !timing && !c.graph_broken)
     if (get_graph(c, o, true, g) != ILG_OK) { c.graph_broken = true; g[0] = g[1] = nullptr; cudaGetLastError(); }
   SunAux* aux = reinterpret_cast<SunAux*>(c.pinned_aux);
-  if (g[0]) {
-    // Pipelined: step s+1 is queued (sun in slot (s+1)&1) before step s's
-    // surface temperatures are copied out of slot s&1, so the GPU runs the
-    // steps back to back. A slot is rewritten only after the step that last
-    // used it has completed.
-    if (nsteps > 0) {
-      aux[0] = make_sun_aux(suns, c.solar_const, c.scene_mag, c.disk_rmax);
-      ILG_CUDA(cudaGraphLaunch(g[0], c.stream));
-      ILG_CUDA(cudaEventRecord(c.slot_ev[0], c.stream));
-    }
+  SunAux* dslot = c.sun_aux.p + c.nsun;   // host slots: frame f uses dslot[f & 1]
+  const int f0 = c.frame_no;
+  auto sun_of = [&](int s) {   // step s's sun (the last one for steps past the call)
+    return make_sun_aux(suns + 3 * (size_t)std::min(s, nsteps - 1), c.solar_const, c.scene_mag, c.disk_rmax);
+  };
+  if (g[0] && nsteps > 0) {
+    // Pipelined: step s runs graph q = (f0 + s + 1) & 1, which uploads step
+    // s+1's sun into host slot q for the next frame's direct insolation and
+    // copies step s's surface temperatures into pinned slot q. Step s+1 is
+    // queued before step s's temperatures are read, so the GPU runs the steps
+    // back to back; a pinned slot is rewritten only after the step that
+    // last used it has completed.
+    StepView v = solo_view(c, o.precision);
+    StepPlan p = solo_plan(c, o);
+    aux[f0 & 1] = sun_of(0);
+    ILG_CUDA(cudaMemcpyAsync(dslot + (f0 & 1), aux + (f0 & 1), sizeof(SunAux), cudaMemcpyHostToDevice, c.stream));
+    ILG_TRY(enqueue_prologue(v, p, c.stream));
+    ILG_CUDA(cudaStreamSynchronize(c.stream));
+    int q = (f0 + 1) & 1;
+    aux[q] = sun_of(1);
+    ILG_CUDA(cudaGraphLaunch(g[q], c.stream));
+    ILG_CUDA(cudaEventRecord(c.slot_ev[q], c.stream));
     for (int s = 0; s < nsteps; ++s) {
-      const int b = s & 1, nb = b ^ 1;
+      q = (f0 + s + 1) & 1;
+      const int nq = q ^ 1;
       if (s + 1 < nsteps) {
-        aux[nb] = make_sun_aux(suns + 3 * (size_t)(s + 1), c.solar_const, c.scene_mag, c.disk_rmax);
-        ILG_CUDA(cudaGraphLaunch(g[nb], c.stream));
-        ILG_CUDA(cudaEventRecord(c.slot_ev[nb], c.stream));
+        aux[nq] = sun_of(s + 2);
+        ILG_CUDA(cudaGraphLaunch(g[nq], c.stream));
+        ILG_CUDA(cudaEventRecord(c.slot_ev[nq], c.stream));
       }
-      ILG_CUDA(cudaEventSynchronize(c.slot_ev[b]));
-      if (tsurf_out) std::memcpy(tsurf_out + (size_t)s * c.nt, c.pinned_tsurf + (size_t)b * c.nt, (size_t)c.nt * 8);
+      ILG_CUDA(cudaEventSynchronize(c.slot_ev[q]));
+      if (tsurf_out) std::memcpy(tsurf_out + (size_t)s * c.nt, c.pinned_tsurf + (size_t)q * c.nt, (size_t)c.nt * 8);
     }
   } else {
     StepView v = solo_view(c, o.precision);
     StepPlan p = solo_plan(c, o);
     for (int s = 0; s < nsteps; ++s) {
-      aux[0] = make_sun_aux(suns + 3 * (size_t)s, c.solar_const, c.scene_mag, c.disk_rmax);
-      ILG_CUDA(cudaMemcpyAsync(c.sun_aux.p + c.nsun, c.pinned_aux, sizeof(SunAux), cudaMemcpyHostToDevice, c.stream));
+      const int q = (f0 + s) & 1;
+      aux[q] = sun_of(s);
+      ILG_CUDA(cudaMemcpyAsync(dslot + q, aux + q, sizeof(SunAux), cudaMemcpyHostToDevice, c.stream));
       ILG_TRY(enqueue_step(v, p, c.stream, timing ? c.ev : nullptr));
       ILG_CUDA(cudaMemcpyAsync(c.pinned_tsurf, c.Tsurf.p, (size_t)c.nt * 8, cudaMemcpyDeviceToHost, c.stream));
       ILG_CUDA(cudaStreamSynchronize(c.stream));
@@ -825,6 +885,9 @@ int ilg_bench_steps(ilg_ctx* ctx, const ilg_run_opts* opts, int first_sun, int n
   StepPlan p = solo_plan(c, o);
   cudaEvent_t a = c.ev[0], b = c.ev[3];
   if (phase_ms) phase_ms[0] = phase_ms[1] = phase_ms[2] = 0.0;
+  // graph steps are pipelined (prologue untimed); eager steps run in the
+  // serial order with their phase boundaries recorded
+  if (g && nsteps > 0) ILG_TRY(enqueue_prologue(v, p, c.stream));
   for (int s = 0; s < nsteps; ++s) {
     if (nflush) ILG_TRY(flush_launch(c.flush.p, nflush, (unsigned)s, c.stream));
     if (g) {
@@ -903,7 +966,7 @@ int ilg_autotune(ilg_ctx* ctx, const ilg_run_opts* opts, int first_sun, ilg_tune
   StepView v = solo_view(c, o.precision);
   const size_t nt = (size_t)c.nt, nl = (size_t)c.nz * nt;
   dbuf<double> sE, srad, sTs, sFs, sQp, sra, sta, stm;
-  ILG_TRY(scratch_copy(sE, c.E.p, nt, s));
+  ILG_TRY(scratch_copy(sE, c.E.p, 2 * nt, s));
   ILG_TRY(scratch_copy(srad, c.rad.p, nt, s));
   ILG_TRY(scratch_copy(sTs, c.Tsurf.p, nt, s));
   ILG_TRY(scratch_copy(sFs, c.Fsurf.p, nt, s));
@@ -932,7 +995,7 @@ int ilg_autotune(ilg_ctx* ctx, const ilg_run_opts* opts, int first_sun, ilg_tune
     for (int nf : {4, 8, 16, 32}) {
       v.tune.classify_threads = cb;
       v.tune.exact_facets = nf;
-      ILG_TRY(time_launches(c, [&] { return direct_launch(v, 0, mu32, s); }, reps, &us));
+      ILG_TRY(time_launches(c, [&] { return direct_launch(v, 0, mu32, 0, s); }, reps, &us));
       if (us < best_d) { best_d = us; best.classify_threads = cb; best.exact_facets = nf; }
     }
   v.tune.classify_threads = best.classify_threads;

@@ -199,7 +199,19 @@ k_conduct(StepView v, const double* __restrict__ Qnp1, int upd) {
   }
   // top row (Ti = T_1, Tip1 = T_2 in the Fortran's numbering). In increment
   // form rho1 is the increment's; T1(n+1) = T0 + (increment) below.
-  const double Q = Qnp1[g];
+  // A scene step's flux: the radiosity solution, or for a mesh without form
+  // factors the frame's direct flux, coupled as src/cpp/illum_cli.cpp:415-421
+  // (rad = -Fsurf_prev + direct) when the mesh follows the reference, and
+  // recorded as the mesh's radiosity. Fsurf is read before this thread
+  // overwrites it below.
+  double Q;
+  if (upd && M.ntiles == 0) {
+    const double d = v.E[(size_t)(M.frame & 1) * v.nt + g];
+    Q = M.coupling == ILG_COUPLE_REFERENCE ? (-v.Fsurf[g] + d) : d;
+    v.rad[g] = Q;
+  } else {
+    Q = Qnp1[g];
+  }
   double T0n, Tsn, Fs;
   R top, dtop;   // T1(n+1) and its increment, in the state's type
   bool done_top = false;

@@ -31,16 +31,24 @@ __device__ __forceinline__ frame3 load_frame(const double* fr) {
   return F;
 }
 
-__device__ __forceinline__ const SunAux* mesh_sun(const StepView& v, const MeshDesc& M) {
-  return v.suns + (M.host_sun ? M.host_slot : M.sun0 + M.sun_idx);
+// The sun of frame M.frame + ahead: from the mesh's table, or from the
+// host slot of that frame's parity (host-driven steps keep two).
+__device__ __forceinline__ const SunAux* mesh_sun(const StepView& v, const MeshDesc& M, int ahead) {
+  return v.suns + (M.host_sun ? M.host_slot + ((M.frame + ahead) & 1) : M.sun0 + M.sun_idx + ahead);
 }
 
-// Where a facet's direct flux goes: the step's E (radiosity follows), rad
-// directly (no radiosity for this mesh), or E alone (drop-in call).
-__device__ __forceinline__ void store_direct(const StepView& v, const MeshDesc& M, int g, double dv, int dropin) {
+// Meshes whose flux this pass computes: active, with a sun for the frame.
+__device__ __forceinline__ bool direct_on(const MeshDesc& M, int ahead) {
+  return M.active && (M.host_sun || M.sun_idx + ahead < M.nsun);
+}
+
+// A facet's direct flux goes into the E slot of its frame (the radiosity
+// solve, or the conduction of a mesh without form factors, reads it and
+// adds the coupling), or into E alone for a drop-in call.
+__device__ __forceinline__ void store_direct(const StepView& v, const MeshDesc& M, int g, double dv, int dropin,
+                                             int ahead) {
   if (dropin) { v.E[g] = dv; return; }
-  double e = M.coupling == ILG_COUPLE_REFERENCE ? (-v.Fsurf[g] + dv) : dv;
-  if (M.ntiles > 0) v.E[g] = e; else v.rad[g] = e;
+  v.E[(size_t)((M.frame + ahead) & 1) * v.nt + g] = dv;
 }
 
 // Range of the horizon threshold of src/cpp/illum.cpp:431-434 over the
@@ -73,17 +81,17 @@ __device__ __forceinline__ bool thr_range(const float* __restrict__ h, int nphi,
 // mu32: the cosine of the sun centre in FP32 (n . u, u the unit sun vector;
 // relative error ~2e-7) instead of the reference's FP64 value; the lit
 // sample count stays exact either way.
-__global__ void k_direct_classify(StepView v, int dropin, int mu32_flux) {
+__global__ void k_direct_classify(StepView v, int dropin, int mu32_flux, int ahead) {
   int f = blockIdx.x * blockDim.x + threadIdx.x;
   bool amb = false;
   const MeshDesc* Mp = nullptr;
   if (f < v.nt) {
     Mp = &v.md[v.mesh_of ? v.mesh_of[f] : 0];
-    if (!Mp->active) Mp = nullptr;
+    if (!direct_on(*Mp, ahead)) Mp = nullptr;
   }
   if (Mp) {
     const MeshDesc& M = *Mp;
-    const SunAux* S = mesh_sun(v, M);
+    const SunAux* S = mesh_sun(v, M, ahead);
     float4 n4 = v.nrm[f];
     float mu32 = (n4.x * S->ux + n4.y * S->uy) + n4.z * S->uz;
     float eps = S->mu_eps;
@@ -151,7 +159,7 @@ __global__ void k_direct_classify(StepView v, int dropin, int mu32_flux) {
         dv *= (mu > 0.0 ? mu : 0.0);
         dv *= S->flux;
       }
-      store_direct(v, M, f, dv, dropin);
+      store_direct(v, M, f, dv, dropin, ahead);
     }
     amb = !decided;
   }
@@ -228,9 +236,9 @@ __device__ __forceinline__ int dx_classify(const StepView& v, const MeshDesc& M,
 
 // FP32 sun direction, frame and kappa of one facet; all_amb when the axis
 // choice of sun_frame is within rounding of a tie.
-__device__ __forceinline__ void dx_setup32(const StepView& v, DxFacet& F, int f) {
+__device__ __forceinline__ void dx_setup32(const StepView& v, DxFacet& F, int f, int ahead) {
   const MeshDesc& M = v.md[v.mesh_of ? v.mesh_of[f] : 0];
-  const SunAux* S = mesh_sun(v, M);
+  const SunAux* S = mesh_sun(v, M, ahead);
   float4 c4 = v.cen[f];
   float sx = (float)S->sx - c4.x, sy = (float)S->sy - c4.y, sz = (float)S->sz - c4.z;
   float dist = sqrtf(sx * sx + sy * sy + sz * sz);
@@ -257,9 +265,9 @@ __device__ __forceinline__ void dx_setup32(const StepView& v, DxFacet& F, int f)
   F.count = 0;
 }
 
-__device__ __forceinline__ void dx_exact_sample(const StepView& v, DxFacet& F, int s) {
+__device__ __forceinline__ void dx_exact_sample(const StepView& v, DxFacet& F, int s, int ahead) {
   const MeshDesc& M = v.md[F.mesh];
-  const SunAux* S = mesh_sun(v, M);
+  const SunAux* S = mesh_sun(v, M, ahead);
   d3 Sv = mkd(S->sx, S->sy, S->sz);
   float4 c4 = v.cen[F.f];
   d3 p = mkd((double)c4.x, (double)c4.y, (double)c4.z);
@@ -273,7 +281,7 @@ __device__ __forceinline__ void dx_exact_sample(const StepView& v, DxFacet& F, i
 }
 
 template <int NF>
-__global__ void __launch_bounds__(DX_THREADS) k_direct_exact(StepView v, int dropin, int mu32_flux) {
+__global__ void __launch_bounds__(DX_THREADS) k_direct_exact(StepView v, int dropin, int mu32_flux, int ahead) {
   __shared__ DxFacet fs[NF];
   __shared__ int list[DX_LIST];
   __shared__ int nlist;
@@ -289,7 +297,7 @@ __global__ void __launch_bounds__(DX_THREADS) k_direct_exact(StepView v, int dro
         DxFacet& F = fs[threadIdx.x];
         int f = v.work[base + threadIdx.x];
         const MeshDesc& M = v.md[v.mesh_of ? v.mesh_of[f] : 0];
-        const SunAux* S = mesh_sun(v, M);
+        const SunAux* S = mesh_sun(v, M, ahead);
         float4 c4 = v.cen[f];
         d3 p = mkd((double)c4.x, (double)c4.y, (double)c4.z);
         d3 Sv = mkd(S->sx, S->sy, S->sz);
@@ -309,7 +317,7 @@ __global__ void __launch_bounds__(DX_THREADS) k_direct_exact(StepView v, int dro
         }
       }
     } else {
-      if (threadIdx.x - 32 < nf) dx_setup32(v, fs[threadIdx.x - 32], v.work[base + threadIdx.x - 32]);
+      if (threadIdx.x - 32 < nf) dx_setup32(v, fs[threadIdx.x - 32], v.work[base + threadIdx.x - 32], ahead);
       if (threadIdx.x == 32) nlist = 0;
       asm volatile("bar.sync 1, %0;" ::"r"(FT));   // the filter warps only
       const int q1 = min(total, DX_LIST);
@@ -326,7 +334,7 @@ __global__ void __launch_bounds__(DX_THREADS) k_direct_exact(StepView v, int dro
       for (int a = threadIdx.x; a < nl; a += DX_THREADS) {
         const int q = list[a];
         const int j = q / nsamp;
-        dx_exact_sample(v, fs[j], q - j * nsamp);
+        dx_exact_sample(v, fs[j], q - j * nsamp, ahead);
       }
       q0 += DX_LIST;
       if (q0 >= total) break;
@@ -348,12 +356,12 @@ __global__ void __launch_bounds__(DX_THREADS) k_direct_exact(StepView v, int dro
     if (threadIdx.x < nf) {
       const DxFacet& F = fs[threadIdx.x];
       const MeshDesc& M = v.md[F.mesh];
-      const SunAux* S = mesh_sun(v, M);
+      const SunAux* S = mesh_sun(v, M, ahead);
       double dv = (double)F.count / M.denom;
       double mu = F.mu;
       dv *= (mu > 0.0 ? mu : 0.0);
       dv *= S->flux;
-      store_direct(v, M, F.f, dv, dropin);
+      store_direct(v, M, F.f, dv, dropin, ahead);
     }
     __syncthreads();
   }
@@ -384,20 +392,20 @@ SunAux make_sun_aux(const double* s, double solar_const, double scene_mag, doubl
   return a;
 }
 
-// Direct insolation for every active mesh of the view (dropin: E = direct
-// only; mu32_flux: FP32 sun cosine in the flux). counters[0] is cleared
-// first.
-int direct_launch(const StepView& v, int dropin, int mu32_flux, cudaStream_t s) {
+// Direct insolation for every active mesh of the view that has a sun for
+// frame M.frame + ahead (dropin: E = direct only; mu32_flux: FP32 sun
+// cosine in the flux). counters[0] is cleared first.
+int direct_launch(const StepView& v, int dropin, int mu32_flux, int ahead, cudaStream_t s) {
   ILG_CUDA(cudaMemsetAsync(v.counters, 0, sizeof(int), s));
   const int cb = v.tune.classify_threads;
   if (cb != 128 && cb != 256 && cb != 512) { set_error("classify_threads must be 128, 256 or 512"); return ILG_ERR_ARG; }
-  k_direct_classify<<<div_up(v.nt, cb), cb, 0, s>>>(v, dropin, mu32_flux);
+  k_direct_classify<<<div_up(v.nt, cb), cb, 0, s>>>(v, dropin, mu32_flux, ahead);
   ILG_CUDA(cudaGetLastError());
   switch (v.tune.exact_facets) {
-    case 4: k_direct_exact<4><<<152 * 4, DX_THREADS, 0, s>>>(v, dropin, mu32_flux); break;
-    case 8: k_direct_exact<8><<<152 * 4, DX_THREADS, 0, s>>>(v, dropin, mu32_flux); break;
-    case 16: k_direct_exact<16><<<152 * 4, DX_THREADS, 0, s>>>(v, dropin, mu32_flux); break;
-    case 32: k_direct_exact<32><<<152 * 4, DX_THREADS, 0, s>>>(v, dropin, mu32_flux); break;
+    case 4: k_direct_exact<4><<<152 * 4, DX_THREADS, 0, s>>>(v, dropin, mu32_flux, ahead); break;
+    case 8: k_direct_exact<8><<<152 * 4, DX_THREADS, 0, s>>>(v, dropin, mu32_flux, ahead); break;
+    case 16: k_direct_exact<16><<<152 * 4, DX_THREADS, 0, s>>>(v, dropin, mu32_flux, ahead); break;
+    case 32: k_direct_exact<32><<<152 * 4, DX_THREADS, 0, s>>>(v, dropin, mu32_flux, ahead); break;
     default: set_error("exact_facets must be 4, 8, 16 or 32"); return ILG_ERR_ARG;
   }
   ILG_CUDA(cudaGetLastError());

@@ -117,7 +117,9 @@ struct StepView {
   const float* disk32;         // fp32 copy of the disk samples
   int ndisk;
   const SunAux* suns;
-  double *Tsurf, *Fsurf, *Qprev, *rad, *rad_avg, *therm_avg, *therm_max, *E;
+  double *Tsurf, *Fsurf, *Qprev, *rad, *rad_avg, *therm_avg, *therm_max;
+  double* E;                   // 2 x nt: the direct flux of frame f in slot f & 1 (before the
+                               // coupling, which its readers apply); a drop-in direct call writes slot 0
   double* sprev;               // 2 x nt: scattered radiosity x - E of the last solve, and its change
   float* x32;                  // 3 x nt (mixed radiosity)
   double* T64;                 // [nz][nt] fp64 layers (standalone column entry points)
@@ -151,10 +153,20 @@ struct StepView {
   float* rho32;
 };
 
+// Second stream and fork/join events of the pipelined step (created on
+// first use; capi.cu).
+struct StepPipe {
+  cudaStream_t s2 = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+  int init();
+  ~StepPipe();
+};
+
 struct Context {
   TuneCfg tune;
   int nt = 0;
   cudaStream_t stream = nullptr;
+  StepPipe pipe;
   float scene_mag = 1.0f;   // max |coordinate|
   float r_max = 0.0f;       // max facet bounding radius
 
@@ -283,7 +295,9 @@ int form_factors_build(Context& c, const double* albedo_h, double albedo_scalar,
 
 // ---- direct.cu ----
 SunAux make_sun_aux(const double* s, double solar_const, double scene_mag, double disk_rmax);
-int direct_launch(const StepView& v, int dropin, int mu32_flux, cudaStream_t s);
+// ahead = 1: the flux of the frame after each mesh's current one (the
+// pipelined step computes it beside the current frame's conduction).
+int direct_launch(const StepView& v, int dropin, int mu32_flux, int ahead, cudaStream_t s);
 
 // ---- radiosity.cu ----
 int radiosity_prepare(Context& c);
@@ -300,6 +314,12 @@ int read_device_errors(Context& c);
 int check_run(Context& c, const ilg_run_opts* o, bool host_driven);
 MeshDesc solo_desc(const Context& c, const ilg_run_opts* o, int first_sun);
 int enqueue_step(const StepView& v, const StepPlan& p, cudaStream_t s, cudaEvent_t* ev);
+// Pipelined step: radiosity of the current frame, then its conduction on s
+// beside the next frame's direct insolation on pipe.s2, then the advance.
+// The current frame's direct flux must be in its E slot already: from the
+// previous pipelined step or from enqueue_prologue at the start of a run.
+int enqueue_step_pipe(const StepView& v, const StepPlan& p, cudaStream_t s, const StepPipe& pipe);
+int enqueue_prologue(const StepView& v, const StepPlan& p, cudaStream_t s);
 int advance_launch(const StepView& v, cudaStream_t s);
 int flush_launch(float4* buf, size_t n, unsigned salt, cudaStream_t s);
 

@@ -495,7 +495,10 @@ __device__ __forceinline__ void init_x(const StepView& v, const double* x, int w
     int g = (int)v.rperm[p];
     const MeshDesc& M = v.md[mesh_of_facet(v, g)];
     if (!M.active || M.ntiles == 0) continue;
-    double e = v.E[g];
+    // the frame's direct flux, coupled as src/cpp/illum_cli.cpp:415-421 when
+    // the mesh follows the reference (rad = -Fsurf_prev + direct)
+    const double d = v.E[(size_t)(M.frame & 1) * v.nt + g];
+    const double e = M.coupling == ILG_COUPLE_REFERENCE ? (-v.Fsurf[g] + d) : d;
     float2 s0 = make_float2(0.f, 0.f);
     if (warm && v.row_act[g] && M.frame >= 1) {
       double s = v.sprev[g];
