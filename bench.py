@@ -51,6 +51,12 @@ MIXED_TOL = 1e-3
 # max_err_K against the FP64 path.
 MIXED_SWEEPS = 2
 
+# DRAM bytes of one k_radiosity64 launch (one step's solve) on the default
+# workload: dram__bytes_read.sum + dram__bytes_write.sum from one ncu
+# capture (--set full, one launch, same workload and build). A profiler's
+# number, reported beside the live timing, never measured inside this run.
+RAD64_DRAM_BYTES_PER_LAUNCH = 198.148096e6 + 8.893696e6
+
 CFG = dict(level=6, seed=1, n_craters=200, dmin_m=30.0, dmax_m=300.0, nphi=64, theta_eps=1e-3, offset=1e-5,
            albedo=0.1, nz=60, ti=300.0, rhoc=1500.0 * 700.0, emiss=0.95, T0=200.0, solar=1361.0, dist_au=1.5,
            period_s=6 * 3600.0, steps_per_rot=720, rotations=10, tol=1e-10, lat_deg=10.0)
@@ -463,8 +469,11 @@ def main():
     dom = max(kern, key=lambda k: kern[k][1])
     b, ms = kern[dom]
     achieved = b / (ms / 1000.0) / 1e9
+    traffic = RAD64_DRAM_BYTES_PER_LAUNCH if dom == "radiosity" else None
     roofline = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+                "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
+                "traffic_unit": "bytes per launch",
+                "traffic_source": "ncu capture of k_radiosity64 on this workload (one launch)" if traffic else None,
                 "algorithmic_bytes": b, "avg_ms": ms}
 
     # mixed precision on a second context from the same initial state
