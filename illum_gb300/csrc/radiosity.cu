@@ -397,6 +397,7 @@ struct MeshState {
   int done[RAD_MAX_MESH];
   int sweeps[RAD_MAX_MESH];
   float unit[RAD_MAX_MESH];
+  unsigned char now[RAD_MAX_MESH];   // stopped at the latest decision
 };
 
 __device__ __forceinline__ unsigned long long res_units(float d2, float unit) {
@@ -433,11 +434,15 @@ __device__ __forceinline__ int decide_meshes(const StepView& v, MeshState& st, i
   __syncthreads();
   const unsigned long long* acc = res_acc(v, k);
   for (int m = threadIdx.x; m < v.nmesh; m += blockDim.x) {
+    st.now[m] = 0;
     if (st.done[m]) continue;
     const unsigned long long q = __ldcg(acc + m);
     const int sw = st.sweeps[m] + (first ? 0 : inc);
     st.sweeps[m] = sw;
-    if (q <= RES_UNITS || sw >= v.md[m].max_sweeps) st.done[m] = 1 + (k & 1);
+    if (q <= RES_UNITS || sw >= v.md[m].max_sweeps) {
+      st.done[m] = 1 + (k & 1);
+      st.now[m] = 1;
+    }
     if (blockIdx.x == 0) v.md[m].sweeps = sw;
   }
   int running = 0;
@@ -489,7 +494,11 @@ struct RadBufs {
   }
 };
 
-__device__ __forceinline__ void init_x(const StepView& v, const double* x, int warm, int gt, int nthreads) {
+// free_rows: also write the result of the rows without entries (x = E,
+// s = 0) and their warm-start record, for a kernel that scatters its tile
+// rows itself.
+__device__ __forceinline__ void init_x(const StepView& v, double* x, int warm, int gt, int nthreads,
+                                       bool free_rows) {
   const RadBufs B(v);
   for (int p = gt; p < v.nt; p += nthreads) {
     int g = (int)v.rperm[p];
@@ -504,6 +513,13 @@ __device__ __forceinline__ void init_x(const StepView& v, const double* x, int w
       double s = v.sprev[g];
       if (M.frame >= 2) s += v.sprev[v.nt + g];
       s0 = split_df(s);
+    }
+    if (free_rows && !v.row_act[g]) {
+      x[g] = e;
+      if (warm) {
+        v.sprev[v.nt + g] = 0.0 - v.sprev[g];
+        v.sprev[g] = 0.0;
+      }
     }
     const float2 eh = split_df(e);
     const float2 x0 = df_add(eh, s0);
@@ -540,6 +556,24 @@ __device__ __forceinline__ void scatter_x(const StepView& v, const MeshState& st
   }
 }
 
+// Tile T's rows (owned by this block): x = E + s into facet order, and the
+// warm-start record, as scatter_x.
+__device__ __forceinline__ void scatter_tile(const StepView& v, const RowTile& T, const float2* S, double* x,
+                                             int warm) {
+  const RadBufs B(v);
+  const uint32_t* rows = v.t_row + T.r0;
+  for (int r = threadIdx.x; r < T.nrows; r += RAD_THREADS) {
+    const uint32_t i = __ldg(rows + r);
+    const int g = (int)v.rperm[i];
+    const double sv = df_value(ld_it(S + i));
+    x[g] = B.EP[i] + sv;
+    if (warm) {
+      v.sprev[v.nt + g] = sv - v.sprev[g];
+      v.sprev[g] = sv;
+    }
+  }
+}
+
 struct RadSmem {
   float2* sx;            // halo values (RAD_HALO double-floats, or floats)
   float2* tail;          // per-thread open-row partials
@@ -566,7 +600,7 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity64(StepView v, doub
   const int nthreads = gridDim.x * RAD_THREADS;
   unsigned gen = 0;
   init_meshes(v, st);
-  init_x(v, x, warm, gt, nthreads);
+  init_x(v, x, warm, gt, nthreads, false);
   if (!grid_barrier(v.barrier, gridDim.x, gen, v.derr)) return;
   const uint64_t pol = l2_keep_policy();
   for (int it = 0;; ++it) {
@@ -619,7 +653,7 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity_mixed(StepView v, 
   float* r32 = v.x32 + 2 * (size_t)v.nt;
   unsigned gen = 0;
   init_meshes(v, st);
-  init_x(v, x, warm, gt, nthreads);
+  init_x(v, x, warm, gt, nthreads, true);
   if (!grid_barrier(v.barrier, gridDim.x, gen, v.derr)) return;
   const uint64_t pol = l2_keep_policy();
   const RadBufs B(v);
@@ -648,7 +682,13 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity_mixed(StepView v, 
     if (!grid_barrier(v.barrier, gridDim.x, gen, v.derr)) return;
     int running = decide_meshes(v, st, RAD_INNER, first, round);
     first = 0;
-    if (running == 0) break;   // scatter below
+    // meshes that stopped on their residual: each block writes its own
+    // tiles' rows (their s was last written by this block)
+    for (int t = blockIdx.x; t < v.ntiles; t += gridDim.x) {
+      const RowTile T = v.tiles[t];
+      if (st.now[T.mesh]) scatter_tile(v, T, S, x, warm);
+    }
+    if (running == 0) break;
     float* cur = xa;
     float* nxt = xb;
     for (int it = 0; it < RAD_INNER; ++it) {
@@ -664,12 +704,25 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity_mixed(StepView v, 
             uint32_t i = __ldg(rows + r);
             nxt[i] = ld_it(r32 + i) + __ldg(scale + r) * rsf[r];
           }
-        } else {   // last sweep: nobody reads d again, x += d directly
+        } else {   // last sweep: nobody reads d again, s += d directly
+          // a mesh whose sweep budget ends with this round takes its result
+          // here (the same test as below)
+          const bool last = st.sweeps[T.mesh] + RAD_INNER >= v.md[T.mesh].max_sweeps;
           for (int r = threadIdx.x; r < T.nrows; r += RAD_THREADS) {
             uint32_t i = __ldg(rows + r);
             const float2 d = make_float2(ld_it(r32 + i) + __ldg(scale + r) * rsf[r], 0.f);
-            S[i] = df_add(ld_it(S + i), d);
+            const float2 sn = df_add(ld_it(S + i), d);
+            S[i] = sn;
             XH[i] = df_add(ld_it(XH + i), d);
+            if (last) {
+              const int g = (int)v.rperm[i];
+              const double sv = df_value(sn);
+              x[g] = B.EP[i] + sv;
+              if (warm) {
+                v.sprev[v.nt + g] = sv - v.sprev[g];
+                v.sprev[g] = sv;
+              }
+            }
           }
         }
         __syncthreads();
@@ -693,10 +746,9 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity_mixed(StepView v, 
       }
       left += __syncthreads_count(run);
     }
+    if (left == 0) break;   // every result is written (by its tile's block)
     if (!grid_barrier(v.barrier, gridDim.x, gen, v.derr)) return;
-    if (left == 0) break;
   }
-  scatter_x(v, st, x, warm, gt, nthreads, true);
   record_residuals(v, st);
 }
 
