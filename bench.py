@@ -46,10 +46,11 @@ UNIT = "facet-steps/s"
 # the mixed path's bar is its temperature error against the FP64 path.
 MIXED_TOL = 1e-3
 # Sweep budget of the mixed path: one refinement round per step (an
-# FP64-accumulated residual, two bf16 sweeps, the update); the next step's
+# FP64-accumulated residual, one bf16 sweep, the update); the next step's
 # first residual includes what the round left. Its error is the measured
-# max_err_K against the FP64 path.
-MIXED_SWEEPS = 2
+# max_err_K against the FP64 path (on C1 the same 0.0011 K as with two or
+# three sweeps per round, which cost 10% and 19% more per step).
+MIXED_SWEEPS = 1
 
 # DRAM bytes of one k_radiosity64 launch (one step's solve) on the default
 # workload: dram__bytes_read.sum + dram__bytes_write.sum from one ncu

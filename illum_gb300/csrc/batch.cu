@@ -294,6 +294,9 @@ static int build(Batch& b) {
   b.plan.rad_on = b.ntiles > 0;
   b.plan.rec_on = nrec > 0;
   b.plan.rad_grid = b.plan.rad_on ? radiosity_grid(b.ntiles, b.precision) : 1;
+  int min_sweeps = b.opts[0].max_sweeps;
+  for (const ilg_run_opts& o : b.opts) min_sweeps = std::min(min_sweeps, o.max_sweeps);
+  b.plan.rad_inner = radiosity_inner(min_sweeps);
   b.plan.nz_max = b.nz_max;
   return ILG_OK;
 }

@@ -123,7 +123,7 @@ int enqueue_step(const StepView& v, const StepPlan& p, cudaStream_t s, cudaEvent
   if (ev) ILG_CUDA(cudaEventRecord(ev[0], s));
   ILG_TRY(direct_launch(v, 0, p.precision == ILG_PREC_MIXED ? 1 : 0, 0, s));
   if (ev) ILG_CUDA(cudaEventRecord(ev[1], s));
-  if (p.rad_on) ILG_TRY(radiosity_launch(v, v.rad, 1, p.precision, p.rad_grid, s));
+  if (p.rad_on) ILG_TRY(radiosity_launch(v, v.rad, 1, p.precision, p.rad_grid, p.rad_inner, s));
   if (ev) ILG_CUDA(cudaEventRecord(ev[2], s));
   ILG_TRY(conduction_launch(v, v.rad, p.precision, 1, p.nz_max, s));
   if (p.rec_on) ILG_TRY(record_launch(v, p.precision, v.cblocks ? v.ncblocks : div_up(v.nt, conduction_step_threads()), s));
@@ -155,7 +155,7 @@ int enqueue_prologue(const StepView& v, const StepPlan& p, cudaStream_t s) {
 // or the current slot for meshes without form factors). Both finish before
 // the advance. Results equal the serial order's bit for bit.
 int enqueue_step_pipe(const StepView& v, const StepPlan& p, cudaStream_t s, const StepPipe& pipe) {
-  if (p.rad_on) ILG_TRY(radiosity_launch(v, v.rad, 1, p.precision, p.rad_grid, s));
+  if (p.rad_on) ILG_TRY(radiosity_launch(v, v.rad, 1, p.precision, p.rad_grid, p.rad_inner, s));
   ILG_CUDA(cudaEventRecord(pipe.fork, s));
   ILG_CUDA(cudaStreamWaitEvent(pipe.s2, pipe.fork, 0));
   ILG_TRY(direct_launch(v, 0, p.precision == ILG_PREC_MIXED ? 1 : 0, 1, pipe.s2));
@@ -293,6 +293,7 @@ static StepPlan solo_plan(Context& c, const ilg_run_opts& o) {
   p.precision = o.precision;
   p.rad_on = o.use_radiosity && c.have_F && c.ntiles > 0;
   p.rad_grid = p.rad_on ? radiosity_grid(c.ntiles, o.precision) : 1;
+  p.rad_inner = radiosity_inner(o.max_sweeps);
   p.nz_max = c.nz;
   p.rec_on = c.rec_cap > 0;
   return p;
@@ -338,7 +339,8 @@ static int capture_step(Context& c, const ilg_run_opts& o, int slot, cudaGraphEx
 // Graph of one step (with_copies: the two host-driven slot graphs, out[0]
 // and out[1]; otherwise out[0] only).
 static int get_graph(Context& c, const ilg_run_opts& o, bool with_copies, cudaGraphExec_t* out) {
-  int key[4] = {o.precision * 4 + o.coupling * 2 + (o.use_radiosity ? 1 : 0), (with_copies ? 1 : 0) + 2 * c.rec_cap,
+  int key[4] = {(o.precision * 4 + o.coupling * 2 + (o.use_radiosity ? 1 : 0)) * 4 + radiosity_inner(o.max_sweeps),
+                (with_copies ? 1 : 0) + 2 * c.rec_cap,
                 c.nz, c.ntiles};
   if (c.graph && std::equal(key, key + 4, c.graph_key)) {
     out[0] = c.graph;
@@ -645,7 +647,7 @@ int ilg_radiosity_solve(ilg_ctx* ctx, const double* E, double tol, int max_sweep
   ILG_CUDA(cudaMemcpyAsync(c.E.p + (size_t)(M.frame & 1) * c.nt, E, (size_t)c.nt * 8, cudaMemcpyHostToDevice,
                            c.stream));
   StepView v = solo_view(c, ILG_PREC_FP64);
-  ILG_TRY(radiosity_launch(v, c.Q.p, 0, ILG_PREC_FP64, radiosity_grid(c.ntiles, ILG_PREC_FP64), c.stream));
+  ILG_TRY(radiosity_launch(v, c.Q.p, 0, ILG_PREC_FP64, radiosity_grid(c.ntiles, ILG_PREC_FP64), 1, c.stream));
   MeshDesc out;
   ILG_CUDA(cudaMemcpyAsync(x, c.Q.p, (size_t)c.nt * 8, cudaMemcpyDeviceToHost, c.stream));
   ILG_CUDA(cudaMemcpyAsync(&out, c.md.p, sizeof(out), cudaMemcpyDeviceToHost, c.stream));

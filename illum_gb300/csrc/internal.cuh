@@ -280,6 +280,7 @@ struct StepPlan {
   bool rad_on;
   bool rec_on;                 // thermal records after conduction
   int rad_grid;
+  int rad_inner;               // mixed solve: bf16 sweeps per refinement round (1..radiosity_max_inner())
   int nz_max;
 };
 
@@ -307,7 +308,10 @@ int radiosity_threads();
 // unsigned words of a view's barrier buffer: the grid barrier's counter and
 // the per-mesh residual accumulators of the radiosity kernels
 size_t radiosity_barrier_words(int nmesh);
-int radiosity_launch(const StepView& v, double* x, int warm, int precision, int grid, cudaStream_t s);
+int radiosity_launch(const StepView& v, double* x, int warm, int precision, int grid, int inner, cudaStream_t s);
+// inner sweeps of a mixed refinement round for a sweep budget (the smallest
+// budget of a view's meshes): the budget, at most radiosity_max_inner()
+int radiosity_inner(int max_sweeps);
 
 // ---- capi.cu ----
 int read_device_errors(Context& c);

@@ -48,9 +48,10 @@
 // E and the residual in FP64): the fixed point is that of (I - fl(F)) x = E,
 // within ~1e-7 of the scattered flux of the fp64 system's. A mesh whose
 // sweep budget runs out in a refinement round stops after the round's update
-// without another residual pass, so max_sweeps = RAD_INNER gives one
-// refinement round per step (the next step's first residual includes what
-// is left).
+// without another residual pass. A round runs min(budget, RAD_INNER) inner
+// sweeps (the smallest budget of the launch's meshes), so max_sweeps = 1 or
+// 2 gives one refinement round per step (the next step's first residual
+// includes what is left).
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -71,7 +72,7 @@ constexpr int RAD_THREADS = 1024;
 constexpr int RAD_HALO = 16384;          // halo values per tile (double-float: 128 KB of shared memory)
 constexpr int RAD_ROWS = 6144;           // rows per tile (their sums: 48 KB of shared memory)
 constexpr int RAD_MAX_MESH = 1024;
-constexpr int RAD_INNER = 2;             // fp32 sweeps per refinement of the mixed solve: the bf16 error
+constexpr int RAD_INNER = 2;             // most fp32 sweeps per refinement of the mixed solve: the bf16 error
                                          // (~4e-3 of the correction) already dominates rho^(k+1), rho ~ 0.013
 constexpr int64_t RAD_MIN_TILE = 16384;  // entries: smaller tiles cost more in staging than they balance
 // Tile balance, in stored entries: a block's sweep time is about
@@ -637,9 +638,9 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity64(StepView v, doub
 
 // Mixed precision: outer refinement with an fp64 residual r = E - (I - fl(F)) x
 // (double-float sums), inner fp32 Jacobi on (I - F~) d = r with bf16 F~
-// (RAD_INNER sweeps), x += d. A mesh stops when ||r||_2 <= tol, or after the
+// (inner sweeps, 1..RAD_INNER), x += d. A mesh stops when ||r||_2 <= tol, or after the
 // update of the round that reaches max_sweeps.
-__global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity_mixed(StepView v, double* x, int warm) {
+__global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity_mixed(StepView v, double* x, int warm, int inner) {
   __shared__ MeshState st;
   __shared__ float red[32];
   const RadSmem sm = rad_smem();
@@ -680,7 +681,7 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity_mixed(StepView v, 
       post_partial(v, st, T, t, round, block_sum(d2, red));
     }
     if (!grid_barrier(v.barrier, gridDim.x, gen, v.derr)) return;
-    int running = decide_meshes(v, st, RAD_INNER, first, round);
+    int running = decide_meshes(v, st, inner, first, round);
     first = 0;
     // meshes that stopped on their residual: each block writes its own
     // tiles' rows (their s was last written by this block)
@@ -691,7 +692,7 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity_mixed(StepView v, 
     if (running == 0) break;
     float* cur = xa;
     float* nxt = xb;
-    for (int it = 0; it < RAD_INNER; ++it) {
+    for (int it = 0; it < inner; ++it) {
       for (int t = blockIdx.x; t < v.ntiles; t += gridDim.x) {
         const RowTile T = v.tiles[t];
         if (st.done[T.mesh]) continue;
@@ -699,7 +700,7 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity_mixed(StepView v, 
         tile_rows<AccF32>(v, T, t, ValsBF{v.t_vbf}, sxf, tailf, sm.tnew, rsf, pol);
         const uint32_t* rows = v.t_row + T.r0;
         const float* scale = v.t_scale + T.r0;
-        if (it + 1 < RAD_INNER) {
+        if (it + 1 < inner) {
           for (int r = threadIdx.x; r < T.nrows; r += RAD_THREADS) {
             uint32_t i = __ldg(rows + r);
             nxt[i] = ld_it(r32 + i) + __ldg(scale + r) * rsf[r];
@@ -707,7 +708,7 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity_mixed(StepView v, 
         } else {   // last sweep: nobody reads d again, s += d directly
           // a mesh whose sweep budget ends with this round takes its result
           // here (the same test as below)
-          const bool last = st.sweeps[T.mesh] + RAD_INNER >= v.md[T.mesh].max_sweeps;
+          const bool last = st.sweeps[T.mesh] + inner >= v.md[T.mesh].max_sweeps;
           for (int r = threadIdx.x; r < T.nrows; r += RAD_THREADS) {
             uint32_t i = __ldg(rows + r);
             const float2 d = make_float2(ld_it(r32 + i) + __ldg(scale + r) * rsf[r], 0.f);
@@ -727,7 +728,7 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity_mixed(StepView v, 
         }
         __syncthreads();
       }
-      if (it + 1 < RAD_INNER) {
+      if (it + 1 < inner) {
         if (!grid_barrier(v.barrier, gridDim.x, gen, v.derr)) return;
         float* tmp = cur; cur = nxt; nxt = tmp;
       }
@@ -738,9 +739,9 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity_mixed(StepView v, 
     for (int m0 = 0; m0 < v.nmesh; m0 += blockDim.x) {
       int m = m0 + threadIdx.x;
       bool run = m < v.nmesh && !st.done[m];
-      if (run && st.sweeps[m] + RAD_INNER >= v.md[m].max_sweeps) {
+      if (run && st.sweeps[m] + inner >= v.md[m].max_sweeps) {
         st.done[m] = 1 + (round & 1);
-        st.sweeps[m] += RAD_INNER;
+        st.sweeps[m] += inner;
         if (blockIdx.x == 0) v.md[m].sweeps = st.sweeps[m];
         run = false;
       }
@@ -1110,7 +1111,9 @@ int radiosity_grid(int ntiles, int precision) {
 // Launches the cooperative solve for every active mesh of the view with
 // tiles. x: result (also the warm start when warm). Per-mesh sweep counts
 // and residuals land in the mesh table.
-int radiosity_launch(const StepView& v, double* x, int warm, int precision, int grid, cudaStream_t s) {
+int radiosity_inner(int max_sweeps) { return max_sweeps < 1 ? 1 : (max_sweeps < RAD_INNER ? max_sweeps : RAD_INNER); }
+
+int radiosity_launch(const StepView& v, double* x, int warm, int precision, int grid, int inner, cudaStream_t s) {
   ILG_TRY(radiosity_setup());
   ILG_CUDA(cudaMemsetAsync(v.barrier, 0, 2 * sizeof(unsigned), s));
   cudaLaunchConfig_t cfg = {};
@@ -1124,7 +1127,7 @@ int radiosity_launch(const StepView& v, double* x, int warm, int precision, int 
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   if (precision == ILG_PREC_MIXED)
-    ILG_CUDA(cudaLaunchKernelEx(&cfg, k_radiosity_mixed, v, x, warm));
+    ILG_CUDA(cudaLaunchKernelEx(&cfg, k_radiosity_mixed, v, x, warm, radiosity_inner(inner)));
   else
     ILG_CUDA(cudaLaunchKernelEx(&cfg, k_radiosity64, v, x, warm));
   return ILG_OK;

@@ -130,8 +130,8 @@ class Server:
         ctx.set_suns(meshgen.spin_sun_positions(r.nsteps, period, dt), ig.fib_spiral(100))
         tm = ig.ThermalModel(ctx, meshgen.geometric_depths(r.nz), r.ti, 1.05e6, 200.0, emissivity=0.95,
                              bc_mode=ig.BC_NEWTON, precision=self.precision)
-        # mixed: one refinement round per step (two bf16 sweeps)
-        opts = ig.RunOpts(dt=dt, tol=self.tol, max_sweeps=2 if self.precision == ig.PREC_MIXED else 200,
+        # mixed: one refinement round per step (one bf16 sweep)
+        opts = ig.RunOpts(dt=dt, tol=self.tol, max_sweeps=1 if self.precision == ig.PREC_MIXED else 200,
                           use_radiosity=1, use_graph=1,
                           precision=self.precision, coupling=ig.COUPLE_DIRECT)
         return Job(req=r, ctx=ctx, tm=tm, opts=opts, nfaces=f.shape[0])

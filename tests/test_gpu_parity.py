@@ -290,6 +290,31 @@ def test_graph_equals_eager_and_host_driven(ilg, oracle_mod, mesh_l3):
         assert np.array_equal(h, runs[0][0]) and np.array_equal(T, runs[0][1])
 
 
+@pytest.mark.parametrize("precision,coupling,use_radiosity", [(0, 0, 1), (1, 1, 1), (0, 0, 0), (1, 1, 0)])
+def test_pipelined_steps_equal_serial_order(ilg, oracle_mod, mesh_l3, precision, coupling, use_radiosity):
+    """Graph and eager steps run the next frame's direct insolation beside
+    the current conduction; phase-timed steps run direct -> radiosity ->
+    conduction in order. Both give the same temperatures and outputs bit for
+    bit, with either coupling and for a mesh stepped without form factors
+    (its conduction reads the direct flux itself)."""
+    v, f = mesh_l3
+    runs = []
+    for mode in ("serial", "graph", "eager"):
+        ctx, tm, opts, _, _, _, _, _ = _setup_run(ilg, oracle_mod, v, f, 16, 30, 24, precision=precision,
+                                                  coupling=coupling, use_graph=0 if mode == "eager" else 1)
+        opts.use_radiosity = use_radiosity
+        if precision == ilg.PREC_MIXED:
+            opts.tol, opts.max_sweeps = 1e-3, 2
+        ctx.set_timing(mode == "serial")
+        h = ctx.run_steps(opts, 0, 24, record_tsurf=True)
+        ctx.set_timing(False)
+        out = ctx.outputs()
+        runs.append((h, tm.T.copy(), out["rad"], out["rad_avg"], out["therm_avg"]))
+    for r in runs[1:]:
+        for a, b in zip(r, runs[0]):
+            assert np.array_equal(a, b)
+
+
 def test_split_runs_equal_one_run(ilg, oracle_mod, mesh_l3):
     v, f = mesh_l3
     a = _setup_run(ilg, oracle_mod, v, f, 16, 30, 30)
@@ -300,11 +325,12 @@ def test_split_runs_equal_one_run(ilg, oracle_mod, mesh_l3):
     assert np.array_equal(a[1].T, b[1].T)
 
 
-@pytest.mark.parametrize("tol,max_sweeps", [(1e-10, 200), (1e-3, 2)])
+@pytest.mark.parametrize("tol,max_sweeps", [(1e-10, 200), (1e-3, 2), (1e-3, 1)])
 def test_mixed_precision_within_tolerance(ilg, oracle_mod, mesh_l4, tol, max_sweeps):
     """Mixed path (bf16 form factors, fp32 conduction) against the FP64 path:
-    solved to tolerance, and with one refinement round per step (the
-    two-sweep budget stops the solve after its first update)."""
+    solved to tolerance, and with one refinement round per step (a budget
+    of two sweeps, or of one, stops the solve after its first update; the
+    round runs that many bf16 sweeps)."""
     v, f = mesh_l4
     nsteps = 360
     ref = _setup_run(ilg, oracle_mod, v, f, 32, 40, nsteps, precision=0)
