@@ -315,6 +315,25 @@ def bench_batch(args, ig, meshgen):
     print(json.dumps(line))
 
 
+def slowest_rank_ms(ms, dist=None):
+    """The timed region's length as the slowest replica saw it: max over
+    ranks (NCCL tensor on the GPU, gloo on the CPU), ms itself for one
+    process."""
+    if dist is None:
+        return float(ms)
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(world, facets, steps, slowest_ms):
+    """Whole-job facet-steps/s of `world` independent replicas, each stepping
+    `facets` facets `steps` times, timed by the slowest one."""
+    return world * facets * steps / (slowest_ms / 1000.0)
+
+
 def run_chunks(fn, first, n, nsun):
     """Call fn(first_sun, count) over [first, first+n) wrapping the sun table."""
     out = []
@@ -442,12 +461,8 @@ def main():
     sun_pos += args.steps
     clk = clocks.stop()
     total_ms = float(step_ms.sum())
-    if dist is not None:
-        import torch
-        t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * N * args.steps / (total_ms / 1000.0)
+    total_ms = slowest_rank_ms(total_ms, dist)
+    value = replica_value(world, N, args.steps, total_ms)
 
     # per-phase breakdown (eager launches with events between phases)
     eager = ig.RunOpts(dt=W["dt"], tol=c["tol"], max_sweeps=200, use_radiosity=1, use_graph=0,
