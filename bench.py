@@ -48,7 +48,7 @@ MIXED_TOL = 1e-3
 # Sweep budget of the mixed path: one refinement round per step (an
 # FP64-accumulated residual, one bf16 sweep, the update); the next step's
 # first residual includes what the round left. Its error is the measured
-# max_err_K against the FP64 path (on C1 the same 0.0011 K as with two or
+# max_err_K against the FP64 path (on the 81,920-facet workload the same 0.0011 K as with two or
 # three sweeps per round, which cost 10% and 19% more per step).
 MIXED_SWEEPS = 1
 
@@ -151,7 +151,7 @@ def build_workload(ig, meshgen, precision=0):
     return dict(v=v, f=f, ctx=ctx, tm=tm, csr=csr, suns=suns, disk=disk, z=z, dt=dt, nsun=nsun, setup=setup)
 
 
-C2 = dict(nmesh=64, seed0=2, levels=(3, 4, 5, 6), crater_rate=0.0025, dmin_m=30.0, dmax_m=300.0, nz=(30, 80),
+BATCH = dict(nmesh=64, seed0=2, levels=(3, 4, 5, 6), crater_rate=0.0025, dmin_m=30.0, dmax_m=300.0, nz=(30, 80),
           ti=(50.0, 2000.0), period_h=(2.0, 12.0), steps_per_rot=(360, 720), nphi=32, albedo=0.1, tol=1e-10)
 
 
@@ -159,40 +159,40 @@ def c2_member_params(seed):
     """Per-mesh draws of the batched workload (seeded, counter-based)."""
     from illum_gb300 import meshgen
     u = meshgen.uniform(seed, 9, 8)
-    level = C2["levels"][min(3, int(u[0] * 4))]
+    level = BATCH["levels"][min(3, int(u[0] * 4))]
     nfaces = 20 * 4 ** level
-    lam = C2["crater_rate"] * nfaces
+    lam = BATCH["crater_rate"] * nfaces
     # Poisson(lam) by inversion of the CDF with one uniform
     k, p, cdf = 0, np.exp(-lam), np.exp(-lam)
     while u[1] > cdf and k < 10 * lam + 20:
         k += 1
         p *= lam / k
         cdf += p
-    nz = C2["nz"][0] + min(C2["nz"][1] - C2["nz"][0], int(u[2] * (C2["nz"][1] - C2["nz"][0] + 1)))
-    ti = float(np.exp(np.log(C2["ti"][0]) + u[3] * (np.log(C2["ti"][1]) - np.log(C2["ti"][0]))))
-    period_h = C2["period_h"][0] + u[4] * (C2["period_h"][1] - C2["period_h"][0])
-    spr = C2["steps_per_rot"][int(u[5] * 2) % 2]
+    nz = BATCH["nz"][0] + min(BATCH["nz"][1] - BATCH["nz"][0], int(u[2] * (BATCH["nz"][1] - BATCH["nz"][0] + 1)))
+    ti = float(np.exp(np.log(BATCH["ti"][0]) + u[3] * (np.log(BATCH["ti"][1]) - np.log(BATCH["ti"][0]))))
+    period_h = BATCH["period_h"][0] + u[4] * (BATCH["period_h"][1] - BATCH["period_h"][0])
+    spr = BATCH["steps_per_rot"][int(u[5] * 2) % 2]
     return dict(level=level, craters=int(k), nz=nz, ti=ti, period_h=period_h, steps_per_rot=spr)
 
 
 def build_c2(ig, meshgen, precision, nmesh=None, nsteps=None):
     members = []
-    nm = nmesh or C2["nmesh"]
-    for seed in range(C2["seed0"], C2["seed0"] + nm):
+    nm = nmesh or BATCH["nmesh"]
+    for seed in range(BATCH["seed0"], BATCH["seed0"] + nm):
         q = c2_member_params(seed)
-        v, f = meshgen.icosphere_craters(q["level"], seed, n_craters=q["craters"], dmin_m=C2["dmin_m"],
-                                         dmax_m=C2["dmax_m"])
+        v, f = meshgen.icosphere_craters(q["level"], seed, n_craters=q["craters"], dmin_m=BATCH["dmin_m"],
+                                         dmax_m=BATCH["dmax_m"])
         ctx = ig.IllumContext(v, f)
-        ctx.make_horizons(nphi=C2["nphi"])
+        ctx.make_horizons(nphi=BATCH["nphi"])
         ctx.set_insolation(1, 0, CFG["solar"])
-        ctx.compute_F(albedo=C2["albedo"])
+        ctx.compute_F(albedo=BATCH["albedo"])
         period = q["period_h"] * 3600.0
         dt = period / q["steps_per_rot"]
         n = nsteps or q["steps_per_rot"]
         ctx.set_suns(meshgen.spin_sun_positions(n, period, dt, CFG["lat_deg"], CFG["dist_au"]), ig.fib_spiral(100))
         tm = ig.ThermalModel(ctx, meshgen.geometric_depths(q["nz"]), q["ti"], CFG["rhoc"], CFG["T0"],
                              emissivity=CFG["emiss"], bc_mode=ig.BC_NEWTON, precision=precision)
-        tol = MIXED_TOL if precision == ig.PREC_MIXED else C2["tol"]
+        tol = MIXED_TOL if precision == ig.PREC_MIXED else BATCH["tol"]
         opts = ig.RunOpts(dt=dt, tol=tol, max_sweeps=MIXED_SWEEPS if precision == ig.PREC_MIXED else 200,
                           use_radiosity=1, use_graph=1, precision=precision,
                           coupling=ig.COUPLE_DIRECT)
@@ -206,10 +206,10 @@ TERRAIN = dict(seed=7, spacing_m=2.0, hurst=0.8, rms_m=25.0, n_bowls=2000, dmin_
 
 
 def bench_terrain(args, ig, meshgen):
-    """C3 shape: fBm heightmap patch with power-law bowls, form factors within
-    a distance cutoff, 128 horizon azimuths, mixed-precision radiosity refined
-    to rel_tol of ||E|| (absolute tolerance rel_tol * ||E|| at noon), C0
-    materials. value = facet-steps/s of the mixed path (device time, L2
+    """Terrain workload: fBm heightmap patch with power-law bowls, form factors
+    within a distance cutoff, 128 horizon azimuths, mixed-precision radiosity refined
+    to rel_tol of ||E|| (absolute tolerance rel_tol * ||E|| at noon), the
+    5,120-facet icosphere workload's materials. value = facet-steps/s of the mixed path (device time, L2
     flushed per step); max_err_K and radiance errors against the same steps
     in FP64."""
     c = TERRAIN
@@ -266,7 +266,7 @@ def bench_terrain(args, ig, meshgen):
             "config": {"workload": f"heightmap {n}x{n} at {c['spacing_m']} m ({N} facets), fBm H {c['hurst']} "
                                    f"RMS {c['rms_m']} m, power-law bowls, form factors within "
                                    f"{args.terrain_cutoff_m} m, nphi {c['nphi']}, radiosity to {c['rel_tol']} of "
-                                   f"||E||, nz {c['nz']} (C3 shape{' at reduced size' if n < 1024 else ''}, cutoff "
+                                   f"||E||, nz {c['nz']} (terrain workload{' at reduced size' if n < 1024 else ''}, cutoff "
                                    f"{args.terrain_cutoff_m} m instead of 2 km)",
                        "facets": N, "l2": "256 MB flush before every timed step"},
             "fp64_value": N * d["K"] / (d["ms"] * 1e-3), "max_err_K_vs_fp64": err_K,
@@ -276,7 +276,7 @@ def bench_terrain(args, ig, meshgen):
 
 
 def bench_batch(args, ig, meshgen):
-    """C2: 64 meshes stepped as one batch (mixed precision, one launch per
+    """Batch workload: 64 meshes stepped as one batch (mixed precision, one launch per
     phase, CUDA graph). value = facet-steps/s over steps where every member
     is active; max_err_K = largest temperature difference of the mixed batch
     against the same batch in FP64 after the timed steps."""
@@ -307,7 +307,7 @@ def bench_batch(args, ig, meshgen):
             "dtype": "bf16 F + fp32 conduction (fp64 residual)", "data": "synthetic",
             "config": {"workload": "64 meshes seeds 2-65, icosphere L3-L6, Poisson craters 0.0025/facet, nz 30-80, "
                                    "ti log-U[50,2000], P U[2,12] h, 360/720 steps per rotation, one batch, "
-                                   "CUDA graph per step (C2)", "facets": nf,
+                                   "CUDA graph per step", "facets": nf,
                        "l2": "256 MB flush before every timed step"},
             "max_err_K_vs_fp64": err, "fp64_batch_value": v64, "mixed_vs_fp64": value / v64,
             "setup_s": t_setup, "clocks": clk, "gpu_launches": 5 * K,
@@ -380,8 +380,8 @@ def main():
     ap.add_argument("--workload", default="c1", choices=["c1", "batch", "serve", "terrain"],
                     help="c1: one 81,920-facet mesh (default); batch: 64 meshes as one batch; serve: request "
                          "loop; terrain: heightmap patch with a form-factor cutoff, mixed precision")
-    ap.add_argument("--terrain-n", type=int, default=1024, help="terrain grid points per side (C3: 1024)")
-    ap.add_argument("--terrain-cutoff-m", type=float, default=30.0, help="form-factor cutoff (C3 states 2000 m)")
+    ap.add_argument("--terrain-n", type=int, default=1024, help="terrain grid points per side (1024: 2,093,058 facets)")
+    ap.add_argument("--terrain-cutoff-m", type=float, default=30.0, help="form-factor cutoff (the terrain configuration states 2000 m)")
     ap.add_argument("--serve-requests", type=int, default=120)
     ap.add_argument("--serve-scale", type=float, default=0.05, help="step-count scale of the serving sample")
     args = ap.parse_args()
@@ -433,7 +433,7 @@ def main():
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                 "data": "synthetic", "impl": "reference",
                 "config": {"workload": "icosphere L6 81,920 facets, 200 craters, nphi 64, nz 60, dt 30 s, "
-                                       "radiosity tol 1e-10, Newton boundary (C1)", "facets": int(W["f"].shape[0])},
+                                       "radiosity tol 1e-10, Newton boundary", "facets": int(W["f"].shape[0])},
                 "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                                  "sample": f"{len(per)} x {args.cpu_steps} time steps of the workload"},
                 "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -542,7 +542,7 @@ def main():
                 "arithmetic": "FP64 state, iterates, residuals and surface boundary; radiosity dot products and "
                               "conduction layer recurrences in double-float (FP32 pairs, ~2^-46 relative)",
                 "config": {"workload": "icosphere L6 81,920 facets, 200 craters 30-300 m, nphi 64, nz 60, "
-                                       "dt 30 s, radiosity tol 1e-10, Newton boundary, E = direct coupling (C1, plain FP64 path)",
+                                       "dt 30 s, radiosity tol 1e-10, Newton boundary, E = direct coupling (plain FP64 path)",
                            "facets": N, "nnz": nnz, "l2": "256 MB flush before every timed step",
                            "parallelism": f"replicas x{world}"},
                 "e2e": e2e, "gpu_launches": 5 * args.steps, "roofline": roofline, "cpu_baseline": cpu,

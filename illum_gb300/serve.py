@@ -250,7 +250,7 @@ class Server:
 
 
 def bench(args) -> dict:
-    """C4-shaped serving run on a bounded sample of the request stream."""
+    """Serving run on a bounded sample of the request stream."""
     n = getattr(args, "serve_requests", 0) or 120
     scale = getattr(args, "serve_scale", 0.0) or 0.05
     reqs = request_stream(n, step_scale=scale)
@@ -265,7 +265,7 @@ def bench(args) -> dict:
             "warmup": 0, "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "bf16 F + fp32 conduction (fp64 residual)", "data": "synthetic",
             "config": {"workload": f"serving: first {n} requests of the seeded stream (Poisson 20/s, icosphere L3-L7, "
-                                   f"craters as C0, 1-20 rotations x 360-1440 steps scaled by {scale}, materials as C2)",
+                                   f"seeded craters, 1-20 rotations x 360-1440 steps scaled by {scale}, materials as the batch workload)",
                        "budget_GB": srv.budget / 1e9, "chunk_steps": srv.chunk},
             "p50_ms": float(np.percentile(lat, 50) * 1000), "p99_ms": float(np.percentile(lat, 99) * 1000),
             "requests": len(done), "wall_s": wall, "batch_rebuilds": srv.rebuilds}

@@ -247,7 +247,7 @@ def _setup_run(ilg, oracle_mod, v, f, nphi, nz, nsteps, period=6 * 3600.0, steps
 
 @pytest.mark.parametrize("coupling,nsteps", [(0, 120), (1, 360)])
 def test_run_steps_vs_oracle_fp64(ilg, oracle_mod, mesh_l4, coupling, nsteps):
-    """C0-shaped run (L4, 32 azimuths, 40 layers, Newton boundary, radiosity
+    """Run on the 5,120-facet icosphere (L4, 32 azimuths, 40 layers, Newton boundary, radiosity
     to 1e-10): surface and subsurface temperatures within 1e-9 K, with the
     reference's E = -Fsurf + direct coupling and with E = direct."""
     v, f = mesh_l4
