@@ -275,6 +275,27 @@ def test_run_steps_reference_boundary(ilg, oracle_mod, mesh_l3):
     assert np.abs(tm.T - st["T"].T).max() <= TOL_T_FP64
 
 
+@pytest.mark.parametrize("coupling", [0, 1])
+def test_run_steps_without_form_factors_vs_oracle(ilg, oracle_mod, mesh_l3, coupling):
+    """Steps without the radiosity solve: the conduction takes the frame's
+    direct flux itself (with the reference's -Fsurf coupling or without) and
+    records it as the radiosity; temperatures and averages as the oracle's
+    loop without form factors."""
+    v, f = mesh_l3
+    nsteps = 60
+    ctx, tm, opts, csr, suns, disk, (z, ti, rhoc), dt = _setup_run(ilg, oracle_mod, v, f, 16, 30, nsteps,
+                                                                   coupling=coupling)
+    opts.use_radiosity = 0
+    hist = ctx.run_steps(opts, 0, nsteps, record_tsurf=True)
+    st = oracle_mod.thermal_run(v, f, ctx.horizons.T, suns, disk, None, z, ti, rhoc, dt=dt, T0=200.0, emiss=0.95,
+                                solar_const=1361.0, norm_mode=1, bc_mode=1, record_tsurf=True, coupling=coupling)
+    assert np.abs(hist - st["tsurf_hist"]).max() <= TOL_T_FP64
+    assert np.abs(tm.T - st["T"].T).max() <= TOL_T_FP64
+    out = ctx.outputs()
+    assert np.abs(out["rad"] - st["rad"]).max() <= 1e-8
+    assert np.abs(out["rad_avg"] - st["rad_avg"]).max() <= 1e-8
+
+
 def test_graph_equals_eager_and_host_driven(ilg, oracle_mod, mesh_l3):
     v, f = mesh_l3
     runs = []
