@@ -267,7 +267,11 @@ k_conduct(StepView v, const double* __restrict__ Qnp1, int upd) {
     // Root of g(x) = Q + 2 k1 (P + (S - 1) x) - es x^4 = A + B x - es x^4
     // (g' = B - 4 es x^3 < 0): Newton in FP32 to ~1e-6, then FP64 steps
     // whose g is exact to FP64 and whose step uses an FP32 reciprocal of
-    // g' (each step gains ~7 digits, so two reach the FP64 tolerance).
+    // g' (relative error ~6e-8, so each step gains ~7 digits). The FP32
+    // stage leaves x within ~1e-7 of the root (its rounding floor), so one
+    // FP64 step that moves x by at most 1e-7 |x| leaves ~6e-8 |dT| +
+    // 2 |dT|^2 / |x| < 1e-11 K and ends the polish; a larger first step
+    // (an FP32 stage that did not converge) continues to the FP64 tolerance.
     const double A = Q + 2.0 * cs.k1 * P;
     float xf = (float)Ts;
     {
@@ -286,7 +290,7 @@ k_conduct(StepView v, const double* __restrict__ Qnp1, int upd) {
       double gx = A + cs.B_top * x - cs.es * x3 * x;
       double dT = gx * (double)__frcp_rn((float)(cs.B_top - 4.0 * cs.es * x3));
       x -= dT;
-      if (fabs(dT) <= tolr * fabs(x)) break;
+      if (fabs(dT) <= (it == 0 ? 1e-7 : tolr) * fabs(x)) break;
     }
     Tsn = x;
     T0n = P + cs.S_top * Tsn;

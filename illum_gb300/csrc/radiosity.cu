@@ -44,8 +44,9 @@
 //
 // Mixed precision: values stored as bf16 with a per-row fp32 scale, fp32
 // accumulation for the inner sweeps, and an outer refinement whose residual
-// is accumulated in double-float from the fp32 values hi (x in double-float,
-// E and the residual in FP64): the fixed point is that of (I - fl(F)) x = E,
+// r = fl(F) x - s is accumulated in double-float from the fp32 values hi (x and
+// s in double-float, E in FP64, r rounded to fp32 for the inner sweeps): the
+// fixed point is that of (I - fl(F)) x = E,
 // within ~1e-7 of the scattered flux of the fp64 system's. A mesh whose
 // sweep budget runs out in a refinement round stops after the round's update
 // without another residual pass. A round runs min(budget, RAD_INNER) inner
@@ -538,17 +539,18 @@ __device__ __forceinline__ void init_x(const StepView& v, double* x, int warm, i
 }
 
 // Scatter the solved meshes' last iterate x = E + s back to facet order
-// (FP64); warm solves also record s and its change for the next step's
-// start. Rows without entries keep s = 0 in both buffers.
+// (FP64; the FP64 solve's result is in S1 after an odd number of sweeps);
+// warm solves also record s and its change for the next step's start. Rows
+// without entries keep s = 0 in both buffers.
 __device__ __forceinline__ void scatter_x(const StepView& v, const MeshState& st, double* x, int warm, int gt,
-                                          int nthreads, bool mixed) {
+                                          int nthreads) {
   const RadBufs B(v);
   for (int p = gt; p < v.nt; p += nthreads) {
     int g = (int)v.rperm[p];
     int m = mesh_of_facet(v, g);
     const MeshDesc& M = v.md[m];
     if (!M.active || M.ntiles == 0) continue;
-    const double s = df_value(ld_it(((!mixed && (st.sweeps[m] & 1)) ? B.S1 : B.S0) + p));
+    const double s = df_value(ld_it(((st.sweeps[m] & 1) ? B.S1 : B.S0) + p));
     x[g] = B.EP[p] + s;
     if (warm) {
       v.sprev[v.nt + g] = s - v.sprev[g];
@@ -632,14 +634,15 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity64(StepView v, doub
     if (!grid_barrier(v.barrier, gridDim.x, gen, v.derr)) return;
     if (decide_meshes(v, st, 1, 0, it) == 0) break;
   }
-  scatter_x(v, st, x, warm, gt, nthreads, false);
+  scatter_x(v, st, x, warm, gt, nthreads);
   record_residuals(v, st);
 }
 
-// Mixed precision: outer refinement with an fp64 residual r = E - (I - fl(F)) x
-// (double-float sums), inner fp32 Jacobi on (I - F~) d = r with bf16 F~
-// (inner sweeps, 1..RAD_INNER), x += d. A mesh stops when ||r||_2 <= tol, or after the
-// update of the round that reaches max_sweeps.
+// Mixed precision: outer refinement with the residual r = E - (I - fl(F)) x
+// = fl(F) x - s (double-float sums), inner fp32 Jacobi on (I - F~) d = r with
+// bf16 F~ (inner sweeps, 1..RAD_INNER), s += d. A mesh stops when
+// ||r||_2 <= tol, or after the update of the round that reaches max_sweeps;
+// each tile's block writes its rows' results.
 __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity_mixed(StepView v, double* x, int warm, int inner) {
   __shared__ MeshState st;
   __shared__ float red[32];
