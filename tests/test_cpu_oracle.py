@@ -143,6 +143,56 @@ def test_gauss_seidel_matches_direct_solve(oracle_mod):
     assert sw1 == 2 and np.abs(x1 - xd).max() < 1.0
 
 
+def test_gauss_seidel_without_form_factors_returns_E(oracle_mod):
+    n = 17
+    E = np.linspace(0.0, 600.0, n)
+    rp = np.zeros(n + 1, np.int64)
+    for mode in (0, 1):
+        x, res, _ = oracle_mod.gauss_seidel(rp, np.zeros(0, np.int32), np.zeros(0), E, mode=mode)
+        assert np.array_equal(x, E) and res == 0.0
+
+
+def test_form_factor_reciprocity(oracle_mod):
+    """F_ij = cos_i cos_j A_j / (pi r^2) (src/cpp/illum.cpp:108-119), so for
+    every pair present both ways F_ij A_i = F_ji A_j."""
+    v, f = meshgen.icosphere_craters(3, 2, n_craters=10, dmin_m=150, dmax_m=450)
+    rows, cols, vals, _ = oracle_mod.form_factors(v, f, albedo_scalar=0.1)
+    _, _, _, area = oracle_mod.facet_geometry(v, f)
+    F = {(int(i), int(j)): float(x) for i, j, x in zip(rows, cols, vals)}
+    both = [(i, j) for (i, j) in F if i < j and (j, i) in F]
+    assert len(both) > 100
+    for i, j in both:
+        a, b = F[(i, j)] * area[i], F[(j, i)] * area[j]
+        assert abs(a - b) <= 1e-12 * max(abs(a), abs(b))
+
+
+# ------------------------------------------------------------ direct insolation
+def test_isolated_facet_direct_known_flux(oracle_mod):
+    """A facet with nothing around it: its horizon is its own plane (rays
+    below it hit the facet itself), every one of the 99 sun-disk samples of
+    a sun above it is lit, and the flux is count / denom * mu * S (AU/d)^2
+    (src/cpp/illum.cpp:441-452); a sun below it gives nothing."""
+    v = np.array([[0, 0, 0], [1e-3, 0, 0], [0, 1e-3, 0]], np.float32)   # 1 m facet, normal +z
+    f = np.array([[0, 1, 2]], np.int32)
+    nphi = 16
+    H = oracle_mod.horizons(v, f, nphi, 1e-3)
+    assert np.all(H > math.pi / 2) and np.all(H < math.pi / 2 + 0.05)
+    disk = oracle_mod.fib_spiral(100)
+    d = np.array([0.3, 0.2, 1.0])
+    d /= np.linalg.norm(d)
+    for dist_au in (1.0, 1.5):
+        sun = meshgen.AU_KM * dist_au * d
+        c, n, _, _ = oracle_mod.facet_geometry(v, f)
+        s = sun - c[0].astype(np.float64)
+        mu = float(n[0].astype(np.float64) @ s / np.linalg.norm(s))
+        for norm_mode, denom in ((0, nphi - 1), (1, 99)):
+            E, cnt = oracle_mod.direct(v, f, H, sun, disk, norm_mode=norm_mode, solar_const=1361.0)
+            assert cnt[0] == 99
+            assert E[0] == pytest.approx(99.0 / denom * mu * 1361.0 / dist_au ** 2, rel=1e-12)
+        E, cnt = oracle_mod.direct(v, f, H, -sun, disk, norm_mode=1, solar_const=1361.0)
+        assert cnt[0] == 0 and E[0] == 0.0
+
+
 # ------------------------------------------------------------ conduction
 def _profile(nz=40):
     z = meshgen.geometric_depths(nz)
