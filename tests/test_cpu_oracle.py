@@ -299,6 +299,14 @@ def test_library_exports_every_declared_symbol(ilg):
     assert ilg.lib().ilg_version() >= 10000
 
 
+def test_python_front_end_binds_every_declared_entry(ilg):
+    """Every C entry point of the header has a ctypes signature in the
+    Python front-end, and nothing else is bound."""
+    hdr = open(os.path.join(ROOT, "include", "illum_gb300.h")).read()
+    declared = set(re.findall(r"\b(ilg_\w+|conduction[qt]_)\s*\(", hdr))
+    assert set(ilg._SIGS) == declared
+
+
 def test_library_has_no_cpu_fallback(ilg):
     """The package exposes no pure-Python compute path: every entry point
     goes through the CUDA library."""
