@@ -66,6 +66,7 @@ _SIGS = {
     "ilg_ctx_destroy": (C.c_int, [C.c_void_p]),
     "ilg_ctx_num_faces": (C.c_int, [C.c_void_p]),
     "ilg_ctx_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int)]),
+    "ilg_ctx_device_bytes": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
     "ilg_trace": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
     "ilg_compute_F": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.POINTER(C.c_int64),
                                 C.POINTER(C.c_int64)]),
@@ -199,6 +200,12 @@ class IllumContext:
         n = C.c_int64(); d = C.c_int()
         _check(lib().ilg_ctx_info(self._h, C.byref(n), C.byref(d)))
         return {"bvh_nodes": n.value, "bvh_depth": d.value}
+
+    def device_bytes(self) -> int:
+        """Device memory the context holds now (bytes)."""
+        n = C.c_int64()
+        _check(lib().ilg_ctx_device_bytes(self._h, C.byref(n)))
+        return n.value
 
     # -- ray queries
     def trace(self, orig, dirs, any_hit=False):

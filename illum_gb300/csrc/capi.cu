@@ -489,6 +489,32 @@ int ilg_ctx_info(const ilg_ctx* ctx, int64_t* bvh_nodes, int* bvh_depth) {
   return ILG_OK;
 }
 
+extern "C++" {
+namespace {
+template <class T>
+int64_t nbytes(const dbuf<T>& b) { return (int64_t)(b.n * sizeof(T)); }
+template <class T, class... R>
+int64_t nbytes(const dbuf<T>& b, const R&... rest) { return nbytes(b) + nbytes(rest...); }
+}  // namespace
+}
+
+int ilg_ctx_device_bytes(const ilg_ctx* ctx, int64_t* bytes) {
+  if (!ctx || !bytes) { set_error("ctx or bytes is NULL"); return ILG_ERR_ARG; }
+  const Context& c = ctx->c;
+  *bytes = nbytes(c.tri_o, c.cen, c.nrm, c.frame32, c.nodes, c.tri_s, c.flush) +
+           nbytes(c.area, c.frame, c.H, c.val, c.tile_d2, c.rho64, c.Tsurf, c.Fsurf, c.Qprev, c.rad, c.rad_avg,
+                  c.therm_avg, c.therm_max, c.E, c.xtmp, c.Q, c.sprev, c.rec, c.rec_part, c.disk) +
+           nbytes(c.H32, c.row_scale, c.t_vhi, c.t_vlo, c.t_scale, c.coef32, c.rho32, c.T32, c.disk32, c.x32) +
+           nbytes(c.hmm32, c.coefdf, c.Tdf) + nbytes(c.rowptr) + nbytes(c.col) + nbytes(c.tiles) +
+           nbytes(c.t_cf) + nbytes(c.t_vbf) + nbytes(c.row_act) +
+           nbytes(c.morton_order, c.t_row, c.t_halo, c.t_start, c.rperm) +
+           nbytes(c.work, c.counters, c.derr, c.mesh_flag) + nbytes(c.barrier) + nbytes(c.sun_aux) + nbytes(c.md) +
+           nbytes(c.scan.a, c.scan.b, c.scan.c, c.sort.keys_alt, c.sort.hist, c.sort.scan.a, c.sort.scan.b,
+                  c.sort.scan.c) +
+           nbytes(c.sort.vals_alt);
+  return ILG_OK;
+}
+
 int ilg_F_info(const ilg_ctx* ctx, int64_t* nnz, int64_t* stored_entries, int* row_tiles, int* active_rows) {
   if (!ctx || !ctx->c.have_F) { set_error("no form factors"); return ILG_ERR_ARG; }
   const Context& c = ctx->c;

@@ -18,12 +18,11 @@ precision).
 """
 from __future__ import annotations
 
-import math
 import queue
 import threading
 import time
 from concurrent.futures import ThreadPoolExecutor
-from dataclasses import dataclass, field
+from dataclasses import dataclass
 
 import numpy as np
 
@@ -88,10 +87,12 @@ def request_stream(n: int, rate_hz: float = 20.0, seed: int = 4242, levels=(3, 4
 
 
 def footprint_bytes(level: int, nz: int, nphi: int, precision: int) -> int:
-    """Device bytes a job holds while it runs (its context plus its copy in a
-    batch): geometry + LBVH + horizons ~ (400 + 8 nphi) B per facet, layer
-    state nz * (4|8) B twice, ~12 facet arrays of 8 B twice, and form factors
-    estimated at 150 entries per facet * 30 B (CSR, row-tile and bf16 copies)."""
+    """A priori estimate of the device bytes a job holds while it runs (its
+    context plus its copy in a batch): geometry + LBVH + horizons ~ (400 +
+    8 nphi) B per facet, layer state nz * (4|8) B twice, ~12 facet arrays of
+    8 B twice, and form factors estimated at 150 entries per facet * 30 B
+    (CSR, row-tile and bf16 copies). The server replaces it by the measured
+    footprint once the job is built (Server._build_one)."""
     n = 20 * 4 ** level
     s_t = 4 if precision == ig.PREC_MIXED else 8
     return int(n * (400 + 8 * nphi + 2 * nz * s_t + 2 * 12 * 8 + 150 * 30))
@@ -114,6 +115,10 @@ class Server:
         self.done: list = []
         self.t0 = 0.0
         self.error = None
+        self.max_used = 0              # largest reserved total (estimates, then measured footprints)
+        self.per_facet = {}            # level -> largest measured bytes per facet of a built job
+        self.est_ratio = []            # measured / reserved per job
+        self.setup_s = []
 
     # -------------------------------------------------------------- setup
     def build_job(self, r: Request) -> Job:
@@ -124,7 +129,7 @@ class Server:
         ctx = ig.IllumContext(v, f)
         ctx.make_horizons(nphi=self.nphi)
         ctx.set_insolation(1, 0, self.solar)
-        ctx.compute_F(albedo=0.1)
+        ctx.compute_F(albedo=0.1, fetch=False)
         period = r.period_h * 3600.0
         dt = period / r.steps_per_rot
         ctx.set_suns(meshgen.spin_sun_positions(r.nsteps, period, dt), ig.fib_spiral(100))
@@ -136,15 +141,46 @@ class Server:
                           precision=self.precision, coupling=ig.COUPLE_DIRECT)
         return Job(req=r, ctx=ctx, tm=tm, opts=opts, nfaces=f.shape[0])
 
+    def _estimate(self, r: Request) -> int:
+        """Bytes to reserve for r: the a priori estimate, or, once a job of
+        the same level has been built, 1.25 x the largest measured bytes per
+        facet at that level (form factors per facet vary with the craters)."""
+        est = footprint_bytes(r.level, r.nz, self.nphi, self.precision)
+        with self.lock:
+            pf = self.per_facet.get(r.level)
+        if pf is not None:
+            est = int(1.25 * pf * 20 * 4 ** r.level)
+        return est
+
     def _build_one(self, r: Request, need: int):
         try:
+            t0 = time.perf_counter()
             job = self.build_job(r)
-            job.footprint = need
+            self.setup_s.append(time.perf_counter() - t0)
+            # the measured footprint: the context, and its copy in a batch
+            actual = 2 * job.ctx.device_bytes()
+            with self.lock:
+                self.used += actual - need
+                self.max_used = max(self.max_used, self.used)
+                self.per_facet[r.level] = max(self.per_facet.get(r.level, 0.0), actual / job.nfaces)
+                self.lock.notify_all()
+            self.est_ratio.append(actual / need)
+            job.footprint = actual
             job.t_ready = time.perf_counter() - self.t0
             self.ready.put(job)
         except Exception as e:   # surfaced by run()
             self.error = e
             self.ready.put(None)
+
+    def stats(self) -> dict:
+        """Admission and set-up figures of the last run."""
+        er = np.array(self.est_ratio) if self.est_ratio else np.zeros(1)
+        st = np.array(self.setup_s) if self.setup_s else np.zeros(1)
+        return {"budget_bytes": self.budget, "max_reserved_bytes": self.max_used,
+                "max_reserved_over_budget": self.max_used / self.budget,
+                "measured_over_reserved": {"max": float(er.max()), "median": float(np.median(er))},
+                "setup_s": {"median": float(np.median(st)), "max": float(st.max()), "sum": float(st.sum())},
+                "setup_workers": self.workers, "batch_rebuilds": getattr(self, "rebuilds", 0)}
 
     def _setup_loop(self, reqs):
         pool = ThreadPoolExecutor(max_workers=self.workers)
@@ -153,11 +189,12 @@ class Server:
                 wait = r.arrival - (time.perf_counter() - self.t0)
                 if wait > 0:
                     time.sleep(wait)
-                need = footprint_bytes(r.level, r.nz, self.nphi, self.precision)
+                need = self._estimate(r)
                 with self.lock:
                     while self.used + need > self.budget and self.used > 0:
                         self.lock.wait()
                     self.used += need
+                    self.max_used = max(self.max_used, self.used)
                 if self.error:
                     break
                 pool.submit(self._build_one, r, need)
@@ -247,25 +284,3 @@ class Server:
     @staticmethod
     def _steps_done(j) -> int:
         return getattr(j, "_done", 0)
-
-
-def bench(args) -> dict:
-    """Serving run on a bounded sample of the request stream."""
-    n = getattr(args, "serve_requests", 0) or 120
-    scale = getattr(args, "serve_scale", 0.0) or 0.05
-    reqs = request_stream(n, step_scale=scale)
-    srv = Server(budget_bytes=int(48e9))
-    t0 = time.perf_counter()
-    done = srv.run(reqs)
-    wall = time.perf_counter() - t0
-    lat = np.array([j.t_done - j.req.arrival for j in done])
-    fs = sum(j.nfaces * j.req.nsteps for j in done)
-    return {"metric": "facet-steps/s at <=0.05 K max err vs FP64; visibility rays/s; serve p50/p99 ms",
-            "value": fs / wall, "unit": "facet-steps/s", "n_gpus": 1, "steps": int(sum(j.req.nsteps for j in done)),
-            "warmup": 0, "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "bf16 F + fp32 conduction (fp64 residual)", "data": "synthetic",
-            "config": {"workload": f"serving: first {n} requests of the seeded stream (Poisson 20/s, icosphere L3-L7, "
-                                   f"seeded craters, 1-20 rotations x 360-1440 steps scaled by {scale}, materials as the batch workload)",
-                       "budget_GB": srv.budget / 1e9, "chunk_steps": srv.chunk},
-            "p50_ms": float(np.percentile(lat, 50) * 1000), "p99_ms": float(np.percentile(lat, 99) * 1000),
-            "requests": len(done), "wall_s": wall, "batch_rebuilds": srv.rebuilds}

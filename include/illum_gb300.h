@@ -77,6 +77,11 @@ int ilg_ctx_create(const float* verts, int nv, const int32_t* tris, int nt,
 int ilg_ctx_destroy(ilg_ctx* ctx);
 int ilg_ctx_num_faces(const ilg_ctx* ctx);
 int ilg_ctx_info(const ilg_ctx* ctx, int64_t* bvh_nodes, int* bvh_depth);
+/* Device bytes the context holds now (every buffer it allocated: geometry,
+ * LBVH, horizons, form factors and their row tiles, thermal state, step
+ * scratch). No reference counterpart: the serving loop admits jobs by this
+ * footprint. */
+int ilg_ctx_device_bytes(const ilg_ctx* ctx, int64_t* bytes);
 
 /* ---- closest / any hit (BVH::getIntersection) ----------------------------- */
 /* hit[r] = index of the closest triangle hit by ray r (or the first found

@@ -162,6 +162,10 @@ struct BVH {
 
   // Closest hit under mt64: smallest t, ties to the smaller index. Returns the
   // triangle index or -1. any_hit = true stops at the first hit.
+  // Children are visited nearer-entry first and a box is skipped once its
+  // entry lies beyond the best hit (with a relative margin). The answer is the
+  // minimum over every triangle whose box the ray enters before the best hit,
+  // so the visiting order changes the running time, never the result.
   int trace(f3 of, f3 df, bool any_hit, double* t_out) const {
     if (nodes.empty()) return -1;
     double o[3] = {of.x, of.y, of.z};
@@ -173,12 +177,14 @@ struct BVH {
     double best = 1e300;
     int besti = -1;
     int stack[128];
+    double tent[128];
     int sp = 0;
-    stack[sp++] = 0;
+    double t_root = slab(nodes[0], o, inv);
+    if (t_root >= 0.0) { stack[sp] = 0; tent[sp++] = t_root; }
     while (sp) {
-      const Node& nd = nodes[stack[--sp]];
-      double te = slab(nd, o, inv);
-      if (te < 0.0 || te > best * (1.0 + 1e-12)) continue;
+      --sp;
+      if (tent[sp] > best * (1.0 + 1e-12)) continue;
+      const Node& nd = nodes[stack[sp]];
       if (nd.count) {
         for (int k = nd.first; k < nd.first + nd.count; ++k) {
           int t = idx[k];
@@ -189,8 +195,15 @@ struct BVH {
           }
         }
       } else {
-        stack[sp++] = nd.left;
-        stack[sp++] = nd.right;
+        double tl = slab(nodes[nd.left], o, inv), tr = slab(nodes[nd.right], o, inv);
+        bool l_ok = tl >= 0.0 && tl <= best * (1.0 + 1e-12);
+        bool r_ok = tr >= 0.0 && tr <= best * (1.0 + 1e-12);
+        // push the farther child first so the nearer one is popped next
+        if (l_ok && r_ok) {
+          if (tl <= tr) { stack[sp] = nd.right; tent[sp++] = tr; stack[sp] = nd.left; tent[sp++] = tl; }
+          else { stack[sp] = nd.left; tent[sp++] = tl; stack[sp] = nd.right; tent[sp++] = tr; }
+        } else if (l_ok) { stack[sp] = nd.left; tent[sp++] = tl; }
+        else if (r_ok) { stack[sp] = nd.right; tent[sp++] = tr; }
       }
     }
     if (t_out) *t_out = best;
