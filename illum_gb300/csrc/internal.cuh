@@ -42,6 +42,10 @@ struct CondScalars {
   double inv_Ap, S_top, B_top, kz;   // 1/Ap, 2 gamma0/Ap, 2 k1 (S_top - 1), k0/z0
   int nz, bc;                        // bc: 0 linearised, 1 Newton, 2 prescribed Ts (conductionT)
   float esf, B_topf;                 // es, B_top rounded to fp32 (the fp32 Newton root)
+  // double-float copies (hi, lo) of the Newton boundary's scalars, for the
+  // segmented step kernels: alpha0, gamma0, f0, inv_Ap, S_top, 2 k1,
+  // B_top, es, kz
+  float2 d_al0, d_g0, d_f0, d_inv_Ap, d_S_top, d_2k1, d_B_top, d_es, d_kz;
 };
 
 // Per sun position, precomputed on the host (direct.cu make_sun_aux).

@@ -173,11 +173,14 @@ typedef struct ilg_run_opts {
 /* What the radiosity solve of a step starts from. ILG_COUPLE_REFERENCE is
  * the reference's E = -Fsurf + direct (src/cpp/illum_cli.cpp:411-421): the
  * conductive surface flux of the previous step is fed back through the
- * radiosity solve. With a thin top layer that loop has a gain above one for
- * mutually visible facets and the run oscillates and diverges (the CPU
- * restatement does the same). ILG_COUPLE_DIRECT starts from the direct
+ * radiosity solve, and with a thin top layer (the millimetre first layer of
+ * the benchmark profiles) the surface temperature then zig-zags from step
+ * to step (the CPU restatement does the same; bounded on the 1,280- and
+ * 5,120-facet crater meshes, with ~26x more sign changes of the step-to-step
+ * change than E = direct). ILG_COUPLE_DIRECT starts from the direct
  * insolation alone (E = direct), so the radiosity solve redistributes
- * scattered sunlight and the conduction step receives it. */
+ * scattered sunlight and the conduction step receives it. Both are tested
+ * against the CPU oracle. */
 #define ILG_COUPLE_REFERENCE 0
 #define ILG_COUPLE_DIRECT 1
 
