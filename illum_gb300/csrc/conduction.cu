@@ -1048,9 +1048,11 @@ int conductiont_host(int nz, const double* z, double dt, double* T, double Tsurf
 //   rho           nz x ncol doubles, only for columns deeper than the
 //                 shared-memory stage holds (nz > 160); written before read
 // Only the error flags must start at zero, and each call clears them itself.
-// All calls share the one array: two calls that overlap on the device would
-// race on it. Calls therefore take a process-wide lock and return only after
-// their work has finished, so calls from one process never overlap.
+// All calls on one device share that device's copy of the array: two calls
+// that overlap on the device would race on it. Calls therefore take a lock
+// per device and return only after their work has finished, so calls from
+// one process never overlap on a device (calls on different devices do not
+// wait for one another).
 
 constexpr size_t NOALLOC_SCRATCH_BYTES = (size_t)ILG_NOALLOC_SCRATCH_MB << 20;
 static __device__ __align__(256) unsigned char g_cond_scratch[NOALLOC_SCRATCH_BYTES];
@@ -1058,8 +1060,7 @@ static __device__ __align__(256) unsigned char g_cond_scratch[NOALLOC_SCRATCH_BY
 namespace {
 
 constexpr int NOALLOC_MAX_DEVICES = 64;
-std::mutex g_noalloc_mu;
-void* g_noalloc_ptr[NOALLOC_MAX_DEVICES];   // scratch address per device (set-up done when non-null)
+std::mutex g_noalloc_mu[NOALLOC_MAX_DEVICES];   // one lock per device's copy of the scratch
 
 size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 
@@ -1078,20 +1079,18 @@ NoallocLayout noalloc_layout(int ncol, int nz, bool deep) {
   return L;
 }
 
-// Once per device, with that device current: the scratch's device address
-// and the shared-memory opt-in of the kernel.
-int noalloc_setup(unsigned char** out) {
-  int dev = 0;
-  ILG_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) { set_error("device %d out of range", dev); return ILG_ERR_ARG; }
-  if (!g_noalloc_ptr[dev]) {
-    void* ptr = nullptr;
-    ILG_CUDA(cudaGetSymbolAddress(&ptr, g_cond_scratch));
-    ILG_CUDA(cudaFuncSetAttribute(k_conduct<double, true, COND_THREADS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)SMEM_LIMIT));
-    g_noalloc_ptr[dev] = ptr;
-  }
-  *out = static_cast<unsigned char*>(g_noalloc_ptr[dev]);
+// On every call, with the caller's device current: the scratch's device
+// address on that device and the shared-memory opt-in of the kernel. Both
+// are taken afresh each time (they are cheap next to the call's stream
+// synchronisation), so a device reset or a new primary context between
+// calls cannot leave a stale address behind.
+int noalloc_setup(int dev, unsigned char** out) {
+  void* ptr = nullptr;
+  ILG_CUDA(cudaGetSymbolAddress(&ptr, g_cond_scratch));
+  ILG_CUDA(cudaFuncSetAttribute(k_conduct<double, true, COND_THREADS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)SMEM_LIMIT));
+  (void)dev;
+  *out = static_cast<unsigned char*>(ptr);
   return ILG_OK;
 }
 
@@ -1121,10 +1120,21 @@ extern "C" int ilg_conductionq_batch_noalloc(int ncol, int nz, const double* z, 
   CondScalars cs;
   ILG_TRY(build_tables(nz, z, ti, rhoc, dt, emiss, Fgeotherm, bc_mode, tab, cs));
   if (ncol == 0) return ILG_OK;
-  std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  unsigned char* base = nullptr;
-  ILG_TRY(noalloc_setup(&base));
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // the call copies from pageable host memory and synchronises the stream,
+  // neither of which a capturing stream allows
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  ILG_CUDA(cudaStreamIsCapturing(s, &cap));
+  if (cap != cudaStreamCaptureStatusNone) {
+    set_error("ilg_conductionq_batch_noalloc cannot run on a stream that is being captured into a graph");
+    return ILG_ERR_ARG;
+  }
+  int dev = 0;
+  ILG_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) { set_error("device %d out of range", dev); return ILG_ERR_ARG; }
+  std::lock_guard<std::mutex> lock(g_noalloc_mu[dev]);
+  unsigned char* base = nullptr;
+  ILG_TRY(noalloc_setup(dev, &base));
   MeshDesc md{};
   md.facet0 = 0; md.nfacet = ncol; md.nz = nz; md.coef0 = 0; md.T0 = 0; md.cs = cs; md.active = 1;
   int* flags = reinterpret_cast<int*>(base + L.flags);

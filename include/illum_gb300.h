@@ -305,10 +305,14 @@ int ilg_conductionq_batch(int ncol, int nz, const double* z, double dt, const do
  * Scratch needed: about 8*ncol + 40*nz bytes, plus 8*nz*ncol for columns
  * deeper than 160 layers; a call needing more than the fixed array returns
  * ILG_ERR_ARG without touching the device (split the columns into smaller
- * calls). The first call on each device sets up the scratch's address for
- * that device; make it before capturing a stream into a graph. Calls share
- * the scratch: overlapping calls would race on it, so calls serialise on a
- * process-wide lock. */
+ * calls). Every call looks up the scratch's address on the current device
+ * (cudaGetSymbolAddress) before it queues anything. The call copies from
+ * pageable host memory and synchronises its stream, so it must not be made
+ * on a stream that is being captured into a graph: it checks, and returns
+ * ILG_ERR_ARG before queuing anything. Calls on one device share that
+ * device's scratch, so overlapping calls would race on it: calls on the same
+ * device serialise on a lock of that device (calls on different devices do
+ * not wait for one another). */
 #define ILG_NOALLOC_SCRATCH_MB 16
 int ilg_conductionq_batch_noalloc(int ncol, int nz, const double* z, double dt,
                                   const double* Qn, const double* Qnp1, double* T,
