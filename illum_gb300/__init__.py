@@ -23,7 +23,7 @@ import numpy as np
 
 __all__ = ["IllumContext", "ThermalModel", "Batch", "IlgError", "fib_spiral", "conductionQ", "conductionQ_batch", "lib",
            "library_path", "RunOpts", "Tune", "PREC_FP64", "PREC_MIXED", "BC_LINEARISED", "BC_NEWTON",
-           "COUPLE_REFERENCE", "COUPLE_DIRECT"]
+           "COUPLE_REFERENCE", "COUPLE_DIRECT", "RAD_TOL", "RAD_GS"]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _SO = os.path.join(_HERE, "libillum_gb300.so")
@@ -31,6 +31,7 @@ _SO = os.path.join(_HERE, "libillum_gb300.so")
 PREC_FP64, PREC_MIXED = 0, 1
 BC_LINEARISED, BC_NEWTON = 0, 1
 COUPLE_REFERENCE, COUPLE_DIRECT = 0, 1
+RAD_TOL, RAD_GS = 0, 1
 
 ERRORS = {-1: "ILG_ERR_ARG", -2: "ILG_ERR_CUDA", -3: "ILG_ERR_NAN", -4: "ILG_ERR_PIVOT", -5: "ILG_ERR_NOMEM",
           -6: "ILG_ERR_DEVICE", -7: "ILG_ERR_NOTCONV"}
@@ -87,6 +88,9 @@ _SIGS = {
     "ilg_direct_radiosity": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     "ilg_radiosity_solve": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_int, C.c_void_p,
                                       C.POINTER(C.c_double), C.POINTER(C.c_int)]),
+    "ilg_radiosity_solve_gs": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.POINTER(C.c_double)]),
+    "ilg_radiosity_levels": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    "ilg_set_radiosity_mode": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "ilg_thermal_init": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_void_p,
                                    C.c_double, C.c_double, C.c_int, C.c_int]),
     "ilg_thermal_step": (C.c_int, [C.c_void_p, C.c_double, C.c_void_p]),
@@ -293,6 +297,25 @@ class IllumContext:
         res = C.c_double(); sw = C.c_int()
         _check(lib().ilg_radiosity_solve(self._h, _p(E), tol, max_sweeps, _p(x), C.byref(res), C.byref(sw)))
         return x, res.value, sw.value
+
+    def radiosity_solve_gs(self, E, gs_steps=1):
+        """The reference's solve: forward solve + gs_steps natural-order
+        Gauss-Seidel sweeps (src/cpp/illum_cli.cpp:425-433). Returns (x, res)."""
+        E = _f64(E)
+        x = np.zeros(self.num_faces, np.float64)
+        res = C.c_double()
+        _check(lib().ilg_radiosity_solve_gs(self._h, _p(E), int(gs_steps), _p(x), C.byref(res)))
+        return x, res.value
+
+    def radiosity_levels(self) -> int:
+        n = C.c_int()
+        _check(lib().ilg_radiosity_levels(self._h, C.byref(n)))
+        return n.value
+
+    def set_radiosity_mode(self, mode, gs_steps=1):
+        """RAD_TOL: fused FP64 steps solve to the run's tolerance; RAD_GS:
+        the reference's fixed sweeps (forward solve + gs_steps sweeps)."""
+        _check(lib().ilg_set_radiosity_mode(self._h, int(mode), int(gs_steps)))
 
     # -- fused loop
     def set_suns(self, suns, disk_xy):

@@ -21,8 +21,9 @@ BUILD = os.path.join(HERE, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off,-fno-fast-math",
                  "-Xptxas", "-warn-spills"]
-EXACT = {"bvh.cu", "direct.cu", "capi.cu"}          # -fmad=false
-SOURCES = ["primitives.cu", "bvh.cu", "direct.cu", "radiosity.cu", "conduction.cu", "capi.cu", "batch.cu"]
+EXACT = {"bvh.cu", "direct.cu", "capi.cu", "gauss_seidel.cu"}   # -fmad=false
+SOURCES = ["primitives.cu", "bvh.cu", "direct.cu", "radiosity.cu", "conduction.cu", "capi.cu", "batch.cu",
+           "gauss_seidel.cu"]
 HEADERS = ["common.cuh", "internal.cuh", "geom.h"]
 
 

@@ -6,11 +6,13 @@ output files (src/cpp/illum_cli.cpp:29-156 config, 268-540 tasks,
     python -m illum_gb300.cli --task form_factors --path shape.obj --albedo 0.12
     python -m illum_gb300.cli --task radiosity --config job.yaml
 
-Differences, by design: the radiosity solve runs to --tol (2-norm of the
-residual) instead of a fixed --gs_steps count of Gauss-Seidel steps; the
-thermal run is the library's fused step (direct -> radiosity -> conduction
-on the GPU), with the reference's coupling rad = -Fsurf + direct.
---precision mixed selects the BF16/FP32 path. A YAML config holds flat
+The radiosity solve is the reference's: a forward solve plus --gs_steps
+natural-order Gauss-Seidel sweeps (default 1, src/cpp/illum_cli.cpp:425-433),
+computed on the GPU in the reference's summation order. Given --tol (2-norm
+of the residual), it instead solves to that tolerance. The thermal run is
+the library's fused step (direct -> radiosity -> conduction on the GPU),
+with the reference's coupling rad = -Fsurf + direct. --precision mixed
+selects the BF16/FP32 path, which solves to --tol. A YAML config holds flat
 `key: value` pairs and lists (inline [a, b] or `- item` lines); command-line
 options given explicitly override it.
 """
@@ -81,8 +83,10 @@ def build_parser() -> argparse.ArgumentParser:
     add("--theta_eps", type=float, default=1e-3)
     add("--nphi", type=int, default=361)
     add("--radiosity", type=_bool, default=False)
-    add("--gs_steps", type=int, default=1, help="accepted for compatibility; the solve runs to --tol")
-    add("--tol", type=float, default=1e-10, help="radiosity residual 2-norm tolerance")
+    add("--gs_steps", type=int, default=1,
+        help="Gauss-Seidel sweeps after the forward solve (the reference's solve, used unless --tol is given)")
+    add("--tol", type=float, default=None,
+        help="radiosity residual 2-norm tolerance: solve to it instead of the fixed sweeps")
     add("--print_residual", type=_bool, default=False)
     add("--thermal", type=_bool, default=False)
     add("--quiet", type=_bool, default=False)
@@ -215,6 +219,11 @@ def task_radiosity(args):
             _timed("- assembling form factor matrix",
                    lambda: ctx.compute_F(albedo=_albedo(args, N), offset=args.offset, fetch=False))
     prec = ig.PREC_MIXED if args.precision == "mixed" else ig.PREC_FP64
+    fixed = args.tol is None          # the reference's forward solve + gs_steps sweeps
+    if fixed and prec == ig.PREC_MIXED:
+        raise SystemExit("--precision mixed solves to a tolerance: give --tol")
+    if args.gs_steps < 0:
+        raise SystemExit("--gs_steps must be >= 0")
     out = {}
     if args.thermal:
         if not args.depths:
@@ -231,8 +240,11 @@ def task_radiosity(args):
                              emissivity=0.999, bc_mode=ig.BC_LINEARISED, precision=prec)
         if args.record_therm_stats:
             ctx.record_thermal(len(suns))
-        opts = ig.RunOpts(dt=args.dt, tol=args.tol, max_sweeps=1000, use_radiosity=int(bool(args.radiosity)),
-                          use_graph=1, precision=prec, coupling=ig.COUPLE_REFERENCE)
+        if fixed:
+            ctx.set_radiosity_mode(ig.RAD_GS, args.gs_steps)
+        opts = ig.RunOpts(dt=args.dt, tol=0.0 if fixed else args.tol, max_sweeps=1000,
+                          use_radiosity=int(bool(args.radiosity)), use_graph=1, precision=prec,
+                          coupling=ig.COUPLE_REFERENCE)
         _timed(f"- {len(suns)} steps (direct, radiosity, conduction)", lambda: ctx.run_steps(opts, 0, len(suns)))
         o = ctx.outputs()
         out = {"rad": o["rad"], "rad_avg": o["rad_avg"], "therm_avg": o["therm_avg"], "therm_max": o["therm_max"],
@@ -247,7 +259,11 @@ def task_radiosity(args):
         for j, s in enumerate(suns):
             rad = ctx.get_direct_radiosity(s, disk)
             if args.radiosity:
-                rad, res, sweeps = ctx.radiosity_solve(rad, tol=args.tol, max_sweeps=1000)
+                if fixed:
+                    rad, res = ctx.radiosity_solve_gs(rad, args.gs_steps)
+                    sweeps = 1 + args.gs_steps
+                else:
+                    rad, res, sweeps = ctx.radiosity_solve(rad, tol=args.tol, max_sweeps=1000)
                 if args.print_residual:
                     print(f"  [{j + 1}/{len(suns)}: res = {res:.3e} after {sweeps} sweeps]")
             rad_avg += (rad - rad_avg) / (j + 1)

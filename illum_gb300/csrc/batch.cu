@@ -101,6 +101,10 @@ static int build(Batch& b) {
   for (int i = 0; i < n; ++i) {
     Context& c = b.members[i]->c;
     const ilg_run_opts& o = b.opts[i];
+    if (c.rad_mode == ILG_RAD_GS && o.use_radiosity) {
+      set_error("batch member %d is in the fixed-sweep Gauss-Seidel mode, which runs on single contexts", i);
+      return ILG_ERR_ARG;
+    }
     ILG_TRY(check_run(c, &o, false));
     ILG_CUDA(cudaStreamSynchronize(c.stream));
     if (ndisk < 0) ndisk = c.ndisk;

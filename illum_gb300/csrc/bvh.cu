@@ -907,6 +907,7 @@ int form_factors_build(Context& c, const double* albedo_h, double albedo_scalar,
     cut.push_back(b);
   }
   c.have_F = false;
+  c.gs_ready = false;
   c.ntiles = 0;
   dbuf<int32_t> ci, cj;
   dbuf<unsigned long long> ukeys, ucount;

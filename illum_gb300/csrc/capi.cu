@@ -117,13 +117,20 @@ int flush_launch(float4* buf, size_t n, unsigned salt, cudaStream_t s) {
   return ILG_OK;
 }
 
+// A step's radiosity solve into v.rad: to the run's tolerance, or the
+// reference's fixed-sweep Gauss-Seidel when the context is in that mode.
+static int radiosity_phase(const StepView& v, const StepPlan& p, cudaStream_t s) {
+  if (p.gs_ctx) return gs_step_launch(*p.gs_ctx, v, p.gs_steps, s);
+  return radiosity_launch(v, v.rad, 1, p.precision, p.rad_grid, p.rad_inner, s);
+}
+
 // One step of a view: direct -> radiosity -> conduction -> advance. With
 // ev (4 events), the phase boundaries are recorded.
 int enqueue_step(const StepView& v, const StepPlan& p, cudaStream_t s, cudaEvent_t* ev) {
   if (ev) ILG_CUDA(cudaEventRecord(ev[0], s));
   ILG_TRY(direct_launch(v, 0, p.precision == ILG_PREC_MIXED ? 1 : 0, 0, s));
   if (ev) ILG_CUDA(cudaEventRecord(ev[1], s));
-  if (p.rad_on) ILG_TRY(radiosity_launch(v, v.rad, 1, p.precision, p.rad_grid, p.rad_inner, s));
+  if (p.rad_on) ILG_TRY(radiosity_phase(v, p, s));
   if (ev) ILG_CUDA(cudaEventRecord(ev[2], s));
   ILG_TRY(conduction_launch(v, v.rad, p.precision, 1, p.nz_max, s));
   if (p.rec_on) ILG_TRY(record_launch(v, p.precision, v.cblocks ? v.ncblocks : div_up(v.nt, conduction_step_threads()), s));
@@ -155,7 +162,7 @@ int enqueue_prologue(const StepView& v, const StepPlan& p, cudaStream_t s) {
 // or the current slot for meshes without form factors). Both finish before
 // the advance. Results equal the serial order's bit for bit.
 int enqueue_step_pipe(const StepView& v, const StepPlan& p, cudaStream_t s, const StepPipe& pipe) {
-  if (p.rad_on) ILG_TRY(radiosity_launch(v, v.rad, 1, p.precision, p.rad_grid, p.rad_inner, s));
+  if (p.rad_on) ILG_TRY(radiosity_phase(v, p, s));
   ILG_CUDA(cudaEventRecord(pipe.fork, s));
   ILG_CUDA(cudaStreamWaitEvent(pipe.s2, pipe.fork, 0));
   ILG_TRY(direct_launch(v, 0, p.precision == ILG_PREC_MIXED ? 1 : 0, 1, pipe.s2));
@@ -281,6 +288,13 @@ int check_run(Context& c, const ilg_run_opts* o, bool host_driven) {
   if (o->coupling != ILG_COUPLE_REFERENCE && o->coupling != ILG_COUPLE_DIRECT) { set_error("bad coupling"); return ILG_ERR_ARG; }
   if (o->use_radiosity && !c.have_F) { set_error("use_radiosity set but no form factors"); return ILG_ERR_ARG; }
   if (o->max_sweeps < 1) { set_error("max_sweeps must be >= 1"); return ILG_ERR_ARG; }
+  if (c.rad_mode == ILG_RAD_GS && o->use_radiosity && c.have_F) {
+    if (o->precision != ILG_PREC_FP64) {
+      set_error("the fixed-sweep Gauss-Seidel mode runs in FP64 precision only");
+      return ILG_ERR_ARG;
+    }
+    ILG_TRY(gs_prepare(c));
+  }
   ILG_TRY(conduction_prepare(c, o->dt, o->precision));
   ILG_TRY(conduction_state_convert(c, o->precision));
   ILG_TRY(ensure_step_buffers(c, o->precision));
@@ -296,6 +310,10 @@ static StepPlan solo_plan(Context& c, const ilg_run_opts& o) {
   p.rad_inner = radiosity_inner(o.max_sweeps);
   p.nz_max = c.nz;
   p.rec_on = c.rec_cap > 0;
+  if (p.rad_on && c.rad_mode == ILG_RAD_GS) {
+    p.gs_ctx = &c;
+    p.gs_steps = c.gs_steps;
+  }
   return p;
 }
 
@@ -339,10 +357,10 @@ static int capture_step(Context& c, const ilg_run_opts& o, int slot, cudaGraphEx
 // Graph of one step (with_copies: the two host-driven slot graphs, out[0]
 // and out[1]; otherwise out[0] only).
 static int get_graph(Context& c, const ilg_run_opts& o, bool with_copies, cudaGraphExec_t* out) {
-  int key[4] = {(o.precision * 4 + o.coupling * 2 + (o.use_radiosity ? 1 : 0)) * 4 + radiosity_inner(o.max_sweeps),
+  int key[5] = {(o.precision * 4 + o.coupling * 2 + (o.use_radiosity ? 1 : 0)) * 4 + radiosity_inner(o.max_sweeps),
                 (with_copies ? 1 : 0) + 2 * c.rec_cap,
-                c.nz, c.ntiles};
-  if (c.graph && std::equal(key, key + 4, c.graph_key)) {
+                c.nz, c.ntiles, c.rad_mode == ILG_RAD_GS ? 1 + c.gs_steps : 0};
+  if (c.graph && std::equal(key, key + 5, c.graph_key)) {
     out[0] = c.graph;
     if (with_copies) out[1] = c.graph_b;
     return ILG_OK;
@@ -354,7 +372,7 @@ static int get_graph(Context& c, const ilg_run_opts& o, bool with_copies, cudaGr
     if (rc != ILG_OK) { invalidate_graph(c); return rc; }
     out[1] = c.graph_b;
   }
-  std::copy(key, key + 4, c.graph_key);
+  std::copy(key, key + 5, c.graph_key);
   out[0] = c.graph;
   return ILG_OK;
 }
@@ -587,6 +605,7 @@ int ilg_set_F(ilg_ctx* ctx, int64_t nnz, const int64_t* rowptr, const int32_t* c
   }
   c.nnz = nnz;
   c.have_F = true;
+  c.gs_ready = false;
   return radiosity_prepare(c);
 }
 
@@ -685,6 +704,49 @@ int ilg_radiosity_solve(ilg_ctx* ctx, const double* E, double tol, int max_sweep
     set_error("radiosity residual %g above tol after %d sweeps", std::sqrt(out.res2), out.sweeps);
     return ILG_ERR_NOTCONV;
   }
+  return ILG_OK;
+}
+
+int ilg_set_radiosity_mode(ilg_ctx* ctx, int mode, int gs_steps) {
+  if (!ctx || (mode != ILG_RAD_TOL && mode != ILG_RAD_GS) || gs_steps < 0) {
+    set_error("invalid radiosity mode (%d, gs_steps %d)", mode, gs_steps);
+    return ILG_ERR_ARG;
+  }
+  Context& c = ctx->c;
+  c.rad_mode = mode;
+  c.gs_steps = gs_steps;
+  invalidate_graph(c);
+  return ILG_OK;
+}
+
+int ilg_radiosity_solve_gs(ilg_ctx* ctx, const double* E, int gs_steps, double* x, double* res) {
+  if (!ctx || !E || !x || gs_steps < 0) { set_error("invalid radiosity arguments"); return ILG_ERR_ARG; }
+  Context& c = ctx->c;
+  if (!c.have_F) { set_error("no form factors"); return ILG_ERR_ARG; }
+  ILG_TRY(gs_prepare(c));
+  ILG_TRY(ensure_step_buffers(c, ILG_PREC_FP64));
+  double* Ed = c.gs_x.p + 2 * (size_t)c.nt;
+  ILG_CUDA(cudaMemcpyAsync(Ed, E, (size_t)c.nt * 8, cudaMemcpyHostToDevice, c.stream));
+  ILG_TRY(gs_solve_launch(c, Ed, c.Q.p, gs_steps, c.stream));
+  std::vector<double> r2;
+  if (res) {
+    ILG_TRY(gs_residual_launch(c, Ed, c.Q.p, c.gs_x.p, c.stream));
+    r2.resize(c.nt);
+    ILG_CUDA(cudaMemcpyAsync(r2.data(), c.gs_x.p, (size_t)c.nt * 8, cudaMemcpyDeviceToHost, c.stream));
+  }
+  ILG_CUDA(cudaMemcpyAsync(x, c.Q.p, (size_t)c.nt * 8, cudaMemcpyDeviceToHost, c.stream));
+  ILG_CUDA(cudaStreamSynchronize(c.stream));
+  if (res) {
+    double acc = 0.0;   // row order, as the CPU oracle sums
+    for (double q : r2) acc += q;
+    *res = std::sqrt(acc);
+  }
+  return ILG_OK;
+}
+
+int ilg_radiosity_levels(const ilg_ctx* ctx, int* levels) {
+  if (!ctx || !levels) { set_error("ctx or levels is NULL"); return ILG_ERR_ARG; }
+  *levels = gs_levels(ctx->c);
   return ILG_OK;
 }
 

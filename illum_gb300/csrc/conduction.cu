@@ -121,6 +121,67 @@ template <> __device__ __forceinline__ double* rho_scratch<double>(const StepVie
 template <> __device__ __forceinline__ float* rho_scratch<float>(const StepView& v) { return v.rho32; }
 template <> __device__ __forceinline__ dfloat* rho_scratch<dfloat>(const StepView&) { return nullptr; }
 
+// Surface boundary of the FP32 and double-float steps: Newton's method for
+// emiss sigma Ts^4 in double-float arithmetic (FP32 iterations, then, for
+// the FP64 step, two double-float polishing steps), so no FP64 arithmetic
+// is on the Newton path.
+__device__ __forceinline__ dfloat to_df(float x) { return dfloat(x, 0.f); }
+__device__ __forceinline__ dfloat to_df(dfloat x) { return x; }
+__device__ __forceinline__ dfloat to_df(float2 x) { return dfloat(x.x, x.y); }
+template <class R> __device__ __forceinline__ R from_df(dfloat x);
+template <> __device__ __forceinline__ float from_df<float>(dfloat x) { return __fadd_rn(x.h, x.l); }
+template <> __device__ __forceinline__ dfloat from_df<dfloat>(dfloat x) { return x; }
+__device__ __forceinline__ double df_to_double(dfloat x) { return (double)x.h + (double)x.l; }
+
+// Newton surface boundary in double-float. T0, T1: the top two layers at
+// time n; rho1: the eliminated right-hand side of layer 1; Ts: the surface
+// temperature at n; Q: the absorbed flux at n+1. Solves
+// g(x) = A + B x - es x^4 = 0 with A = Q + 2 k1 (T0 + P), the top layer's
+// increment being P + S_top x. polish: double-float Newton steps after the
+// FP32 ones (the FP64 step's accuracy).
+struct TopResult { dfloat dtop, top, tsn; };
+__device__ __forceinline__ TopResult newton_top(const CondScalars& cs, dfloat T0, dfloat T1, dfloat rho1, double Ts,
+                                                double Q, bool polish) {
+  const dfloat al0 = to_df(cs.d_al0), g0 = to_df(cs.d_g0), f0 = to_df(cs.d_f0), iAp = to_df(cs.d_inv_Ap);
+  const dfloat Tsd(Ts), Qd(Q);
+  const dfloat two(2.f, 0.f), four(4.f, 0.f);
+  // R0 = 2 al0 (T1 - T0) + 4 g0 (Ts - T0) - 2 g0 Ts; P = (R0 - f0 rho1) / Ap
+  const dfloat R0 = two * al0 * (T1 - T0) + four * g0 * (Tsd - T0) - two * g0 * Tsd;
+  const dfloat P = (R0 - f0 * rho1) * iAp;
+  const dfloat A = Qd + to_df(cs.d_2k1) * (T0 + P);
+  const float Af = __fadd_rn(A.h, A.l), Bf = cs.B_topf, esf = cs.esf;
+  const float tol = polish ? 1e-6f : 2.4e-7f;
+  float xf = __double2float_rn(Ts);
+  // from the previous surface temperature Newton converges in a few steps;
+  // it stops at the tolerance or once a step no longer shrinks (the FP32
+  // rounding floor of g)
+  float prev = INFINITY;
+  for (int it = 0; it < 20; ++it) {
+    const float x3 = xf * xf * xf;
+    const float dT = __fmul_rn(Af + Bf * xf - esf * x3 * xf, __frcp_rn(Bf - 4.f * esf * x3));
+    xf -= dT;
+    const float adt = fabsf(dT);
+    if (adt <= tol * fabsf(xf) || adt >= prev) break;
+    prev = adt;
+  }
+  dfloat x(xf, 0.f);
+  if (polish) {
+    const dfloat B = to_df(cs.d_B_top), es = to_df(cs.d_es);
+    for (int it = 0; it < 2; ++it) {
+      const dfloat x2 = x * x;
+      const dfloat gx = A + B * x - es * (x2 * x2);
+      const float x3 = x.h * x.h * x.h;
+      const float step = __fmul_rn(__fadd_rn(gx.h, gx.l), __frcp_rn(Bf - 4.f * esf * x3));
+      x = x - dfloat(step, 0.f);
+    }
+  }
+  TopResult r;
+  r.dtop = P + to_df(cs.d_S_top) * x;
+  r.top = T0 + r.dtop;
+  r.tsn = x;
+  return r;
+}
+
 // One thread per facet column. Block b covers facets [cb.y, cb.y + BS) of
 // mesh cb.x. Q: the new time level's flux per facet.
 template <class R, bool SMEM, int BS>
@@ -215,29 +276,19 @@ k_conduct(StepView v, const double* __restrict__ Qnp1, int upd) {
   double T0n, Tsn, Fs;
   R top, dtop;   // T1(n+1) and its increment, in the state's type
   bool done_top = false;
-  if constexpr (std::is_same<R, float>::value) {
+  if constexpr (!std::is_same<R, double>::value) {
     if (cs.bc == 1) {
-      // fp32 state, Newton boundary: P = T1(n+1) - S_top Ts(n+1) is a small
-      // difference of temperature-sized terms when S_top ~ 1, and the root
-      // moves by 2 k1 dP / |g'| (large for conductive materials), so P, A
-      // and T1(n+1) are formed in FP64; the root itself is found in FP32
-      // (to ~2 ulp; A is accurate, and g's rounding is ~ulp(x) |g'|).
-      const double T0 = (double)Ti, T1 = (double)Tip1, Ts = v.Tsurf[g];
-      const double R0 = 2.0 * cs.alpha0 * (T1 - T0) + 4.0 * cs.gamma0 * (Ts - T0) - 2.0 * cs.gamma0 * Ts;
-      const double P = (R0 - cs.f0 * (double)rho_next) * cs.inv_Ap + T0;
-      const float A = (float)(Q + 2.0 * cs.k1 * P);
-      float x = (float)Ts;
-      for (int it = 0; it < 30; ++it) {
-        float x3 = x * x * x;
-        float dT = (A + cs.B_topf * x - cs.esf * x3 * x) / (cs.B_topf - 4.f * cs.esf * x3);
-        x -= dT;
-        if (fabsf(dT) <= 2.4e-7f * fabsf(x)) break;
-      }
-      Tsn = (double)x;
-      T0n = P + cs.S_top * Tsn;
-      top = (float)T0n;
-      dtop = (float)(T0n - T0);
-      Fs = -(T0n - Tsn) * cs.kz;
+      // FP32 and double-float states: P, A and the top layer in double-float
+      // (P = T1(n+1) - S_top Ts(n+1) is a small difference of
+      // temperature-sized terms), the root by FP32 Newton steps, polished in
+      // double-float for the FP64 step (no FP64 arithmetic)
+      const TopResult tr = newton_top(cs, to_df(Ti), to_df(Tip1), to_df(rho_next), v.Tsurf[g], Q,
+                                      std::is_same<R, dfloat>::value);
+      Tsn = df_to_double(tr.tsn);
+      top = from_df<R>(tr.top);
+      dtop = from_df<R>(tr.dtop);
+      Fs = -df_to_double((tr.top - tr.tsn) * to_df(cs.d_kz));
+      T0n = 0.0;
       done_top = true;
     }
   }
@@ -343,266 +394,6 @@ k_conduct(StepView v, const double* __restrict__ Qnp1, int upd) {
     v.Tsurf[g] = Tsn;
     v.Qprev[g] = Q;
   }
-  if (upd) {
-    // running means: 1/(frame + 1) by an FP32 reciprocal and two FP64
-    // Newton steps (no FP64 division)
-    const double n = (double)(M.frame + 1);
-    double rn = (double)__frcp_rn((float)n);
-    rn = rn * (2.0 - n * rn);
-    rn = rn * (2.0 - n * rn);
-    v.rad_avg[g] += (Q - v.rad_avg[g]) * rn;
-    v.therm_avg[g] += (Tsn - v.therm_avg[g]) * rn;
-    if (M.frame > 50) v.therm_max[g] = fmax(v.therm_max[g], Tsn);
-  }
-}
-
-// ---- segmented columns (the scene steps) --------------------------------------
-//
-// P lanes of a warp share one facet column: lane s holds layers
-// [s L, s L + L) (L = ceil(nz / P)) in registers, so the column is read
-// once and written once, and each lane's serial chain is L layers long
-// instead of nz. Both Thomas recurrences are first-order and linear:
-//   upward    rho_i = r_i - f_i rho_{i+1}
-//   downward  d_i = (rho_i + g_i d_{i-1}) ib_i        (d_0 = the top increment)
-// so over a segment each is affine in the value that enters it:
-//   rho_i = A_i + B_i rho_in,  B_i = prod_{k=i}^{b-1} (-f_k)
-//   d_i   = C_i + D_i d_in,    D_i = prod_{k=a}^{i} g_k ib_k
-// Every lane computes A (resp. C) with a zero entering value and the
-// products on the fly; P - 1 shuffles then carry the entering values from
-// segment to segment (bottom-up for rho, top-down for d), and each lane adds
-// B rho_in (resp. D d_in). The downward C pass does not depend on the
-// surface boundary, so it runs before lane 0 solves the boundary.
-// The surface boundary (Newton for emiss sigma Ts^4, conductionQ.f:76-98's
-// linearisation otherwise) is lane 0's: in double-float arithmetic for
-// both precisions (FP32 Newton, then, for the FP64 step, two double-float
-// polishing steps), so no FP64 arithmetic is on the Newton path.
-__device__ __forceinline__ float shfl_i(unsigned m, float x, int src, int w) { return __shfl_sync(m, x, src, w); }
-__device__ __forceinline__ dfloat shfl_i(unsigned m, dfloat x, int src, int w) {
-  return dfloat(__shfl_sync(m, x.h, src, w), __shfl_sync(m, x.l, src, w));
-}
-__device__ __forceinline__ float shfl_u(unsigned m, float x, int w) { return __shfl_up_sync(m, x, 1, w); }
-__device__ __forceinline__ dfloat shfl_u(unsigned m, dfloat x, int w) {
-  return dfloat(__shfl_up_sync(m, x.h, 1, w), __shfl_up_sync(m, x.l, 1, w));
-}
-__device__ __forceinline__ float shfl_d(unsigned m, float x, int w) { return __shfl_down_sync(m, x, 1, w); }
-__device__ __forceinline__ dfloat shfl_d(unsigned m, dfloat x, int w) {
-  return dfloat(__shfl_down_sync(m, x.h, 1, w), __shfl_down_sync(m, x.l, 1, w));
-}
-__device__ __forceinline__ dfloat to_df(float x) { return dfloat(x, 0.f); }
-__device__ __forceinline__ dfloat to_df(dfloat x) { return x; }
-__device__ __forceinline__ dfloat to_df(float2 x) { return dfloat(x.x, x.y); }
-template <class R> __device__ __forceinline__ R from_df(dfloat x);
-template <> __device__ __forceinline__ float from_df<float>(dfloat x) { return __fadd_rn(x.h, x.l); }
-template <> __device__ __forceinline__ dfloat from_df<dfloat>(dfloat x) { return x; }
-__device__ __forceinline__ double df_to_double(dfloat x) { return (double)x.h + (double)x.l; }
-template <class R> __device__ __forceinline__ R zero_r() { return R(0); }
-template <> __device__ __forceinline__ dfloat zero_r<dfloat>() { return dfloat(0.f, 0.f); }
-template <class R> __device__ __forceinline__ R one_r() { return R(1); }
-template <> __device__ __forceinline__ dfloat one_r<dfloat>() { return dfloat(1.f, 0.f); }
-__device__ __forceinline__ float ldg_r(const float* p) { return __ldg(p); }
-__device__ __forceinline__ dfloat ldg_r(const dfloat* p) {
-  float2 t = __ldg(reinterpret_cast<const float2*>(p));
-  return dfloat(t.x, t.y);
-}
-
-// Newton surface boundary in double-float. T0, T1: the top two layers at
-// time n; rho1: the eliminated right-hand side of layer 1; Ts: the surface
-// temperature at n; Q: the absorbed flux at n+1. Solves
-// g(x) = A + B x - es x^4 = 0 with A = Q + 2 k1 (T0 + P), the top layer's
-// increment being P + S_top x. polish: double-float Newton steps after the
-// FP32 ones (the FP64 step's accuracy).
-struct TopResult { dfloat dtop, top, tsn; };
-__device__ __forceinline__ TopResult newton_top(const CondScalars& cs, dfloat T0, dfloat T1, dfloat rho1, double Ts,
-                                                double Q, bool polish) {
-  const dfloat al0 = to_df(cs.d_al0), g0 = to_df(cs.d_g0), f0 = to_df(cs.d_f0), iAp = to_df(cs.d_inv_Ap);
-  const dfloat Tsd(Ts), Qd(Q);
-  const dfloat two(2.f, 0.f), four(4.f, 0.f);
-  // R0 = 2 al0 (T1 - T0) + 4 g0 (Ts - T0) - 2 g0 Ts; P = (R0 - f0 rho1) / Ap
-  const dfloat R0 = two * al0 * (T1 - T0) + four * g0 * (Tsd - T0) - two * g0 * Tsd;
-  const dfloat P = (R0 - f0 * rho1) * iAp;
-  const dfloat A = Qd + to_df(cs.d_2k1) * (T0 + P);
-  const float Af = __fadd_rn(A.h, A.l), Bf = cs.B_topf, esf = cs.esf;
-  float xf = __double2float_rn(Ts);
-  for (int it = 0; it < 30; ++it) {
-    const float x3 = xf * xf * xf;
-    const float dT = (Af + Bf * xf - esf * x3 * xf) / (Bf - 4.f * esf * x3);
-    xf -= dT;
-    if (fabsf(dT) <= (polish ? 1e-6f : 2.4e-7f) * fabsf(xf)) break;
-  }
-  dfloat x(xf, 0.f);
-  if (polish) {
-    const dfloat B = to_df(cs.d_B_top), es = to_df(cs.d_es);
-    for (int it = 0; it < 2; ++it) {
-      const dfloat x2 = x * x;
-      const dfloat gx = A + B * x - es * (x2 * x2);
-      const float x3 = x.h * x.h * x.h;
-      const float step = __fmul_rn(__fadd_rn(gx.h, gx.l), __frcp_rn(Bf - 4.f * esf * x3));
-      x = x - dfloat(step, 0.f);
-    }
-  }
-  TopResult r;
-  r.dtop = P + to_df(cs.d_S_top) * x;
-  r.top = T0 + r.dtop;
-  r.tsn = x;
-  return r;
-}
-
-template <class R, int P, int LMAX, int BS>
-__global__ void __launch_bounds__(BS * P)
-k_conduct_seg(StepView v, const double* __restrict__ Qnp1, int upd) {
-  const int2 cb = v.cblocks ? v.cblocks[blockIdx.x] : make_int2(0, blockIdx.x * BS);
-  const MeshDesc& M = v.md[cb.x];
-  if (!M.active) return;
-  const int s = threadIdx.x % P;
-  const int fl = cb.y + threadIdx.x / P;
-  if (fl >= M.nfacet) return;                     // the facet's P lanes leave together
-  const unsigned gm = ((1u << P) - 1u) << ((threadIdx.x & 31) & ~(P - 1));
-  const int g = M.facet0 + fl;
-  const int nz = M.cs.nz;
-  const size_t N = (size_t)M.nfacet;
-  R* __restrict__ T = state_T<R>(v) + M.T0 + fl;
-  const R* __restrict__ tab = coef_tab<R>(v) + M.coef0;
-  const int L = (nz + P - 1) / P;
-  const int a = s * L;
-  const int cnt = max(0, min(L, nz - a));
-  const int k0 = s == 0 ? 1 : 0;                  // first layer of the recurrences (layer 0 is the boundary row)
-  R Tr[LMAX], X[LMAX];
-#pragma unroll
-  for (int k = 0; k < LMAX; ++k) {
-    Tr[k] = zero_r<R>();
-    X[k] = zero_r<R>();
-  }
-#pragma unroll
-  for (int k = 0; k < LMAX; ++k)
-    if (k < cnt) Tr[k] = ld_layer(T + (size_t)(a + k) * N);
-  R Tlast = zero_r<R>();
-#pragma unroll
-  for (int k = 0; k < LMAX; ++k)
-    if (k == cnt - 1) Tlast = Tr[k];
-  const R Tprev = shfl_u(gm, Tlast, P);           // T(a-1): the lane above's last layer
-  const R Tnext = shfl_d(gm, Tr[0], P);           // T(b): the lane below's first layer
-  // upward: A_i with rho_in = 0, and the product B of the segment's -f
-  R acc = zero_r<R>(), Bp = one_r<R>();
-  R dn = zero_r<R>();
-#pragma unroll
-  for (int k = LMAX - 1; k >= 0; --k) {
-    if (k < cnt && k >= k0) {
-      const int i = a + k;
-      const R* c = tab + (size_t)i * TAB_W;
-      const R Ti = Tr[k];
-      const R Tip1 = (k + 1 < cnt) ? Tr[k + 1 < LMAX ? k + 1 : k] : Tnext;
-      const R Tim1 = (k >= 1) ? Tr[k >= 1 ? k - 1 : 0] : Tprev;
-      if (k + 1 >= cnt) dn = (i == nz - 1) ? zero_r<R>() : Ti - Tip1;   // the segment's first layer
-      const R dm = Tim1 - Ti;
-      R r = twice(ldg_r(c) * dm - ldg_r(c + 2) * dn);
-      if (i == nz - 1) r = r + (R)M.cs.cgeo;
-      const R f = ldg_r(c + 3);
-      acc = r - f * acc;
-      Bp = -(f * Bp);
-      X[k] = acc;
-      dn = dm;
-    }
-  }
-  // entering rho, bottom segment to top: rho_in(s) = A_first(s+1) + B_first(s+1) rho_in(s+1)
-  R rin = zero_r<R>();
-#pragma unroll
-  for (int j = P - 2; j >= 0; --j) {
-    const R val = shfl_i(gm, acc + Bp * rin, j + 1, P);
-    if (s == j) rin = val;
-  }
-  // rho_i = A_i + B_i rho_in; then the downward C pass (d_in = 0) and the
-  // segment's product D
-  {
-    R B2 = one_r<R>();
-#pragma unroll
-    for (int k = LMAX - 1; k >= 0; --k) {
-      if (k < cnt && k >= k0) {
-        B2 = -(ldg_r(tab + (size_t)(a + k) * TAB_W + 3) * B2);
-        X[k] = X[k] + B2 * rin;
-      }
-    }
-  }
-  // the boundary row needs T0, T1 and rho1 (layer 1 is lane 0's when L >= 2)
-  const R T1 = shfl_i(gm, L >= 2 ? Tr[1] : Tr[0], L >= 2 ? 0 : 1, P);
-  const R rho1 = shfl_i(gm, L >= 2 ? X[1] : X[0], L >= 2 ? 0 : 1, P);
-  R Cc = zero_r<R>(), Dp = one_r<R>();
-#pragma unroll
-  for (int k = 0; k < LMAX; ++k) {
-    if (k < cnt && k >= k0) {
-      const R* c = tab + (size_t)(a + k) * TAB_W;
-      const R gk = ldg_r(c), ib = ldg_r(c + 4);
-      Cc = (X[k] + gk * Cc) * ib;
-      Dp = (gk * ib) * Dp;
-      X[k] = Cc;
-    }
-  }
-  // surface boundary (lane 0)
-  R dtop = zero_r<R>(), top = zero_r<R>();
-  double Q = 0.0, Tsn = 0.0, Fs = 0.0;
-  if (s == 0) {
-    if (upd && M.ntiles == 0) {
-      // a mesh without form factors takes the frame's direct flux, coupled
-      // as src/cpp/illum_cli.cpp:415-421 when it follows the reference
-      const double d = v.E[(size_t)(M.frame & 1) * v.nt + g];
-      Q = M.coupling == ILG_COUPLE_REFERENCE ? (-v.Fsurf[g] + d) : d;
-      v.rad[g] = Q;
-    } else {
-      Q = Qnp1[g];
-    }
-    const CondScalars& cs = M.cs;
-    const double Ts = v.Tsurf[g];
-    const R T0 = Tr[0];
-    if (cs.bc == 1) {
-      const TopResult tr = newton_top(cs, to_df(T0), to_df(T1), to_df(rho1), Ts, Q,
-                                      std::is_same<R, dfloat>::value);
-      dtop = from_df<R>(tr.dtop);
-      top = from_df<R>(tr.top);
-      Tsn = df_to_double(tr.tsn);
-      Fs = -df_to_double((tr.top - tr.tsn) * to_df(cs.d_kz));
-    } else {
-      // conductionQ.f:76-98, linearised about Ts (FP64; not a benchmark path)
-      const double T0d = df_to_double(to_df(T0)), T1d = df_to_double(to_df(T1)), r1 = df_to_double(to_df(rho1));
-      const double Qn = v.Qprev[g];
-      const double Tr3 = Ts * Ts * Ts;
-      const double arad = -3.0 * cs.es * Tr3 * Ts, brad = 2.0 * cs.es * Tr3, den = cs.k1 + brad;
-      const double ann = (Qn - arad) / den, annp1 = (Q - arad) / den, bn = (cs.k1 - brad) / den;
-      const double b0 = 1.0 + cs.alpha0 + cs.gamma0 - cs.gamma0 * bn;
-      double r0 = cs.gamma0 * (annp1 + ann) + (1.0 - cs.alpha0 - cs.gamma0 + cs.gamma0 * bn) * T0d + cs.alpha0 * T1d;
-      const double piv = b0 + cs.f0 * cs.gamma1;
-      if (piv == 0.0) atomicExch(&v.derr[DERR_PIVOT], 1);
-      r0 -= b0 * T0d - cs.alpha0 * T1d;
-      const double inc = piv != 0.0 ? (r0 - cs.f0 * r1) / piv : 0.0;
-      const double T0n = T0d + inc;
-      Tsn = 0.5 * (annp1 + bn * T0n + T0n);
-      dtop = from_df<R>(dfloat(inc));
-      top = from_df<R>(dfloat(T0n));
-      Fs = -(T0n - Tsn) * cs.kz;
-    }
-  }
-  // entering d, top segment to bottom: d_in(0) = the top increment
-  R din = dtop;
-#pragma unroll
-  for (int j = 0; j <= P - 2; ++j) {
-    const R val = shfl_i(gm, Cc + Dp * din, j, P);
-    if (s == j + 1) din = val;
-  }
-  // T(n+1) = T(n) + C + D d_in
-  {
-    R D2 = one_r<R>();
-#pragma unroll
-    for (int k = 0; k < LMAX; ++k) {
-      if (k < cnt && k >= k0) {
-        const R* c = tab + (size_t)(a + k) * TAB_W;
-        D2 = (ldg_r(c) * ldg_r(c + 4)) * D2;
-        T[(size_t)(a + k) * N] = Tr[k] + (X[k] + D2 * din);
-      }
-    }
-  }
-  if (s != 0) return;
-  T[0] = top;
-  v.Fsurf[g] = Fs;
-  v.Tsurf[g] = Tsn;
-  v.Qprev[g] = Q;
   if (upd) {
     // running means: 1/(frame + 1) by an FP32 reciprocal and two FP64
     // Newton steps (no FP64 division)
@@ -790,37 +581,8 @@ int conduction_state_convert(Context& c, int precision) {
 // Threads per block: the view's tuned value for a single mesh (a batch's
 // block table is cut at COND_STEP_THREADS), COND_STEP_THREADS where the
 // tuned size would not fit the column in shared memory.
-template <class R, int P, int LMAX>
-int launch_seg(const StepView& v, const double* Q, int upd, int bs, cudaStream_t s) {
-  if (P > 4 && bs == 128) bs = 64;   // at most 512 threads per block (register budget)
-  const int grid = v.cblocks ? v.ncblocks : div_up(v.nt, bs);
-  if (grid <= 0) return ILG_OK;
-  if (bs == 32) k_conduct_seg<R, P, LMAX, 32><<<grid, 32 * P, 0, s>>>(v, Q, upd);
-  else if (bs == 128) k_conduct_seg<R, P, LMAX, (P <= 4 ? 128 : 64)><<<grid, (P <= 4 ? 128 : 64) * P, 0, s>>>(v, Q, upd);
-  else k_conduct_seg<R, P, LMAX, COND_STEP_THREADS><<<grid, COND_STEP_THREADS * P, 0, s>>>(v, Q, upd);
-  ILG_CUDA(cudaGetLastError());
-  return ILG_OK;
-}
-
-// Columns of up to SEG_MAX_NZ layers run segmented (P lanes per column);
-// deeper ones stage whole columns (shared memory, or the deep-column
-// scratch).
-constexpr int SEG_MAX_NZ = 128;
-
-template <class R>
-int launch_seg_for(const StepView& v, const double* Q, int upd, int nz_max, int bs, cudaStream_t s) {
-  if (nz_max <= 64) return launch_seg<R, 4, 16>(v, Q, upd, bs, s);
-  if (nz_max <= 96) return launch_seg<R, 8, 12>(v, Q, upd, bs, s);
-  return launch_seg<R, 8, 16>(v, Q, upd, bs, s);
-}
-
 int conduction_launch(const StepView& v, const double* Q, int precision, int upd, int nz_max, cudaStream_t s) {
   int bs = v.cblocks ? COND_STEP_THREADS : v.tune.conduct_threads;
-  if (nz_max <= SEG_MAX_NZ) {
-    if (bs != 32 && bs != 64 && bs != 128) { set_error("conduct_threads must be 32, 64 or 128"); return ILG_ERR_ARG; }
-    if (precision == ILG_PREC_MIXED) return launch_seg_for<float>(v, Q, upd, nz_max, bs, s);
-    return launch_seg_for<dfloat>(v, Q, upd, nz_max, bs, s);
-  }
   if (bs != 32 && bs != 64 && bs != 128) { set_error("conduct_threads must be 32, 64 or 128"); return ILG_ERR_ARG; }
   const size_t elt = precision == ILG_PREC_MIXED ? sizeof(float) : sizeof(dfloat);
   if ((size_t)nz_max * bs * elt > SMEM_LIMIT) bs = COND_STEP_THREADS;

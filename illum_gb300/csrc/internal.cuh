@@ -215,6 +215,13 @@ struct Context {
   dbuf<double> tile_d2;
   dbuf<uint8_t> row_act;
   dbuf<uint32_t> rperm;           // Morton position -> facet (radiosity's internal order)
+  // the reference's fixed-sweep Gauss-Seidel (gauss_seidel.cu)
+  int rad_mode = 0;               // ILG_RAD_TOL / ILG_RAD_GS
+  int gs_steps = 1;
+  bool gs_ready = false;          // gs_rows / gs_lptr describe the current form factors
+  dbuf<uint32_t> gs_rows;         // rows in dependency-level order
+  std::vector<int> gs_lptr;       // level boundaries in gs_rows
+  dbuf<double> gs_x;              // 3 x N: two iterates and the right-hand side
 
   // thermal
   bool have_thermal = false;
@@ -266,7 +273,7 @@ struct Context {
   // CUDA graph of one step
   cudaGraphExec_t graph = nullptr;       // without copies, or with the copies of slot 0
   cudaGraphExec_t graph_b = nullptr;     // with the copies of slot 1
-  int graph_key[4] = {-1, -1, -1, -1};
+  int graph_key[5] = {-1, -1, -1, -1, -1};
   bool graph_broken = false;      // capture failed once: launch eagerly
 
   dbuf<float4> flush;              // L2-eviction buffer of the benchmark loop
@@ -286,6 +293,8 @@ struct StepPlan {
   int rad_grid;
   int rad_inner;               // mixed solve: bf16 sweeps per refinement round (1..radiosity_max_inner())
   int nz_max;
+  const Context* gs_ctx = nullptr;   // fixed-sweep Gauss-Seidel of this context instead of the tolerance solve
+  int gs_steps = 0;
 };
 
 // ---- bvh.cu ----
@@ -316,6 +325,16 @@ int radiosity_launch(const StepView& v, double* x, int warm, int precision, int 
 // inner sweeps of a mixed refinement round for a sweep budget (the smallest
 // budget of a view's meshes): the budget, at most radiosity_max_inner()
 int radiosity_inner(int max_sweeps);
+
+// ---- gauss_seidel.cu ----
+int gs_prepare(Context& c);       // dependency levels of the current form factors (once per F)
+int gs_levels(const Context& c);
+// 1 + gs_steps natural-order sweeps from zero for right-hand side E (device,
+// facet order) into x (device, facet order)
+int gs_solve_launch(const Context& c, const double* E, double* x, int gs_steps, cudaStream_t s);
+// a fused step's solve: the frame's coupled direct flux into v.rad
+int gs_step_launch(const Context& c, const StepView& v, int gs_steps, cudaStream_t s);
+int gs_residual_launch(const Context& c, const double* E, const double* x, double* r2, cudaStream_t s);
 
 // ---- capi.cu ----
 int read_device_errors(Context& c);

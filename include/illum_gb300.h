@@ -145,6 +145,25 @@ int ilg_direct_radiosity(ilg_ctx* ctx, const double* sun, const double* disk_xy,
 int ilg_radiosity_solve(ilg_ctx* ctx, const double* E, double tol, int max_sweeps, double* x,
                         double* res, int* sweeps);
 
+/* The reference's own solve: a forward solve of L x = E with
+ * L = I - tril(F), then gs_steps Gauss-Seidel sweeps x = L^{-1}(E - U x),
+ * U = -triu(F), in natural row order (src/cpp/arma_util.cpp:4-17,
+ * src/cpp/illum_cli.cpp:425-433; its default gs_steps is 1,
+ * illum_cli.cpp:607-610). Each row sums in the reference's order, so x
+ * equals the CPU restatement's bit for bit. *res (may be NULL) receives
+ * ||(I - F) x - E||_2. Rows run level by level (rows whose lower columns
+ * are all final); the levels are found on the first call after F changes. */
+int ilg_radiosity_solve_gs(ilg_ctx* ctx, const double* E, int gs_steps, double* x, double* res);
+/* Number of dependency levels of the fixed-sweep solve (0 before its first
+ * use on the current form factors). */
+int ilg_radiosity_levels(const ilg_ctx* ctx, int* levels);
+/* Which solve the fused FP64 steps run: ILG_RAD_TOL (default) solves to the
+ * run's tolerance; ILG_RAD_GS runs the reference's fixed sweeps as
+ * ilg_radiosity_solve_gs with gs_steps (single contexts, FP64 only). */
+#define ILG_RAD_TOL 0
+#define ILG_RAD_GS 1
+int ilg_set_radiosity_mode(ilg_ctx* ctx, int mode, int gs_steps);
+
 /* ---- thermal model -------------------------------------------------------- */
 /* z, ti, rhoc: nz per-layer values (the reference shares one profile across
  * facets, thermal.hpp:23-42); T0: uniform start temperature, or T0_full

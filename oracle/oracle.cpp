@@ -213,9 +213,15 @@ struct BVH {
 
 }  // namespace
 
+// Face normals that replace the computed ones in the direct insolation
+// (the thermal loop included): the normals of an OBJ as the reference reads
+// them (src/cpp/obj_util.cpp:70-88). nullptr: computed from the vertices.
+static const float* g_normals = nullptr;
+
 extern "C" {
 
 void orc_set_threads(int n) { g_threads = n; }
+void orc_set_normals(const float* normals) { g_normals = normals; }
 
 // Derived per-facet quantities (centroid, normal, bounding radius, area),
 // as the reference's Tri object provides them (src/cpp/obj_util.cpp:70-92).
@@ -377,7 +383,7 @@ void orc_fib_spiral(double* xy, int n) { fib_spiral(xy, n); }
 void orc_direct(const float* verts, const int32_t* tris, int nt, const double* horizons, int nphi,
                 const double* sun, const double* disk_xy, int ndisk, int norm_mode, int interp,
                 double solar_const, double* out, int32_t* counts) {
-  Mesh m = make_mesh(verts, tris, nt, nullptr);
+  Mesh m = make_mesh(verts, tris, nt, g_normals);
   double dphi = TWO_PI / (double)(nphi - 1);
   d3 S = mkd(sun[0], sun[1], sun[2]);
   double scale_au = ONE_AU_KM / norm(S);
@@ -430,11 +436,38 @@ int orc_gauss_seidel(int n, const int64_t* rowptr, const int32_t* col, const dou
   int sweeps = 0;
   int limit = mode == 0 ? 1 + gs_steps : max_sweeps;
   double r = 0.0;
+  std::vector<double> b(mode == 0 ? n : 0);
   while (sweeps < limit) {
-    for (int i = 0; i < n; ++i) {
-      double xi = E[i];
-      for (int64_t k = rowptr[i]; k < rowptr[i + 1]; ++k) xi += val[k] * x[col[k]];
-      x[i] = xi;
+    if (mode == 0) {
+      // the reference's order: b = E - U x with U = -triu(F) (diagonal
+      // included), the product accumulated from zero over each row's
+      // columns in ascending order (Armadillo's sparse product), then the
+      // forward solve of L x = b with L = I - tril(F), adding the lower
+      // terms in ascending column order and dividing by L's diagonal
+      // 1 - F_ii (src/cpp/arma_util.cpp:4-17, src/cpp/illum_cli.cpp:425-433;
+      // -(-a) b terms are exact sign flips of a b). The first solve has no
+      // upper term.
+      for (int i = 0; i < n; ++i) {
+        double u = 0.0;
+        if (sweeps > 0)
+          for (int64_t k = rowptr[i]; k < rowptr[i + 1]; ++k)
+            if (col[k] >= i) u += val[k] * x[col[k]];
+        b[i] = sweeps > 0 ? E[i] + u : E[i];
+      }
+      for (int i = 0; i < n; ++i) {
+        double xi = b[i], fii = 0.0;
+        for (int64_t k = rowptr[i]; k < rowptr[i + 1]; ++k) {
+          if (col[k] < i) xi += val[k] * x[col[k]];
+          else if (col[k] == i) fii = val[k];
+        }
+        x[i] = xi / (1.0 - fii);
+      }
+    } else {
+      for (int i = 0; i < n; ++i) {
+        double xi = E[i];
+        for (int64_t k = rowptr[i]; k < rowptr[i + 1]; ++k) xi += val[k] * x[col[k]];
+        x[i] = xi;
+      }
     }
     ++sweeps;
     if (mode == 1) {

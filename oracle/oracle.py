@@ -108,7 +108,21 @@ def fib_spiral(n=100):
     return xy.T.copy()          # n x 2
 
 
-def direct(verts, faces, hor, sun, disk_xy, norm_mode=0, interp=0, solar_const=1372.0):
+class _normals:
+    """Face normals for the oracle's direct insolation during a call (the
+    OBJ reader's normals), or the computed ones when None."""
+
+    def __init__(self, normals):
+        self.n = None if normals is None else np.ascontiguousarray(normals, np.float32)
+
+    def __enter__(self):
+        lib().orc_set_normals(_p(self.n))
+
+    def __exit__(self, *exc):
+        lib().orc_set_normals(None)
+
+
+def direct(verts, faces, hor, sun, disk_xy, norm_mode=0, interp=0, solar_const=1372.0, normals=None):
     verts = np.ascontiguousarray(verts, np.float32)
     faces = np.ascontiguousarray(faces, np.int32)
     hor = np.ascontiguousarray(hor, np.float64)
@@ -116,9 +130,10 @@ def direct(verts, faces, hor, sun, disk_xy, norm_mode=0, interp=0, solar_const=1
     sun = np.ascontiguousarray(sun, np.float64)
     dxy = np.ascontiguousarray(np.asarray(disk_xy, np.float64).T)   # column-major n x 2
     out = np.zeros(nt, np.float64); cnt = np.zeros(nt, np.int32)
-    lib().orc_direct(_p(verts), _p(faces), C.c_int(nt), _p(hor), C.c_int(nphi), _p(sun), _p(dxy),
-                     C.c_int(disk_xy.shape[0]), C.c_int(norm_mode), C.c_int(interp),
-                     C.c_double(solar_const), _p(out), _p(cnt))
+    with _normals(normals):
+        lib().orc_direct(_p(verts), _p(faces), C.c_int(nt), _p(hor), C.c_int(nphi), _p(sun), _p(dxy),
+                         C.c_int(disk_xy.shape[0]), C.c_int(norm_mode), C.c_int(interp),
+                         C.c_double(solar_const), _p(out), _p(cnt))
     return out, cnt
 
 
@@ -176,9 +191,11 @@ class RunParams(C.Structure):
 def thermal_run(verts, faces, hor, suns, disk_xy, csr, z, ti, rhoc, *, dt, T0, emiss=0.999,
                 solar_const=1372.0, norm_mode=0, interp=0, bc_mode=0, rad_mode=1, gs_steps=1,
                 tol=1e-10, max_sweeps=200, state=None, frame0=0, record_tsurf=False, direct_all=None,
-                coupling=0):
+                coupling=0, normals=None):
     """Time-step loop of src/cpp/illum_cli.cpp:403-468. Returns a dict of the
-    final state (T is (nz+1) x N column-major as a [N, nz+1] array)."""
+    final state (T is (nz+1) x N column-major as a [N, nz+1] array).
+    normals: face normals for the direct insolation (an OBJ's, as read by
+    the reference), or None for the ones computed from the vertices."""
     verts = np.ascontiguousarray(verts, np.float32)
     faces = np.ascontiguousarray(faces, np.int32)
     nt = faces.shape[0]
@@ -202,12 +219,13 @@ def thermal_run(verts, faces, hor, suns, disk_xy, csr, z, ti, rhoc, *, dt, T0, e
         rowptr = col = val = None
     hist = np.zeros((nsteps, nt), np.float64) if record_tsurf else None
     da = None if direct_all is None else np.ascontiguousarray(direct_all, np.float64)
-    rc = lib().orc_thermal_run(C.byref(P), _p(verts), _p(faces), _p(hor), _p(suns), _p(dxy), _p(da), _p(rowptr),
-                               _p(col), _p(val), _p(np.ascontiguousarray(z, np.float64)),
-                               _p(np.ascontiguousarray(ti, np.float64)), _p(np.ascontiguousarray(rhoc, np.float64)),
-                               _p(state["T"]), _p(state["Qprev"]), _p(state["Fsurf"]), _p(state["rad"]),
-                               _p(state["rad_avg"]), _p(state["therm_avg"]), _p(state["therm_max"]),
-                               C.c_int(frame0), _p(hist))
+    with _normals(normals):
+        rc = lib().orc_thermal_run(C.byref(P), _p(verts), _p(faces), _p(hor), _p(suns), _p(dxy), _p(da),
+                                   _p(rowptr), _p(col), _p(val), _p(np.ascontiguousarray(z, np.float64)),
+                                   _p(np.ascontiguousarray(ti, np.float64)),
+                                   _p(np.ascontiguousarray(rhoc, np.float64)), _p(state["T"]), _p(state["Qprev"]),
+                                   _p(state["Fsurf"]), _p(state["rad"]), _p(state["rad_avg"]),
+                                   _p(state["therm_avg"]), _p(state["therm_max"]), C.c_int(frame0), _p(hist))
     if rc:
         raise ZeroDivisionError("zero pivot in conduction")
     if record_tsurf:

@@ -1,6 +1,8 @@
 """The task front-end end to end on a small OBJ: horizons, form factors and
-a radiosity + thermal run write the reference's output files, with the
-values the library's API gives."""
+a radiosity + thermal run write the reference's output files; the values
+match the library's API and, for the thermal run (the reference's
+forward solve + gs_steps sweeps, its coupling and linearised boundary), the
+CPU oracle."""
 import numpy as np
 import pytest
 
@@ -20,7 +22,7 @@ def _write_obj(path, v, f):
             fh.write("f %d//%d %d//%d %d//%d\n" % (t[0], t[0], t[1], t[1], t[2], t[2]))
 
 
-def test_cli_tasks(ilg, tmp_path):
+def test_cli_tasks(ilg, oracle_mod, tmp_path):
     from illum_gb300 import cli
     v, f = meshgen.icosphere_craters(2, seed=3, n_craters=4, dmin_m=150.0, dmax_m=400.0)
     obj = tmp_path / "shape.obj"
@@ -50,3 +52,15 @@ def test_cli_tasks(ilg, tmp_path):
     assert therm.shape == (Fc.shape[0],) and np.all(np.isfinite(therm))
     assert armaio.load(str(out / "therm_stats.bin")).shape == (8, 12)
     assert np.array_equal(res["therm"], therm)
+    # the same job on the CPU oracle: reference solve (gs_steps 1 by
+    # default), rad = -Fsurf + direct, linearised boundary, emissivity 0.999,
+    # lit counts over nphi - 1, 1372 W/m^2 at 1 AU
+    depths = np.array([0.002, 0.005, 0.01, 0.02, 0.05, 0.1])
+    nz = len(depths)
+    st = oracle_mod.thermal_run(V, Fc, H.T, suns / 1000.0, ilg.fib_spiral(100), (rp, c, x), depths,
+                                np.full(nz, 300.0), np.full(nz, 1.05e6), dt=600.0, T0=220.0, emiss=0.999,
+                                solar_const=1372.0, norm_mode=0, bc_mode=0, rad_mode=0, gs_steps=1, coupling=0,
+                                normals=N)
+    assert np.abs(therm - st["T"][:, 0]).max() <= 1e-9
+    assert np.abs(armaio.load(str(out / "rad.bin")).ravel() - st["rad"]).max() <= 1e-9 * np.abs(st["rad"]).max()
+    assert np.abs(armaio.load(str(out / "therm_avg.bin")).ravel() - st["therm_avg"]).max() <= 1e-9
