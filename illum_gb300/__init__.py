@@ -90,6 +90,7 @@ _SIGS = {
                                       C.POINTER(C.c_double), C.POINTER(C.c_int)]),
     "ilg_radiosity_solve_gs": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.POINTER(C.c_double)]),
     "ilg_radiosity_levels": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    "ilg_debug_barrier_timeout": (C.c_int, [C.c_void_p, C.c_int, C.c_longlong, C.c_int]),
     "ilg_set_radiosity_mode": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "ilg_thermal_init": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_void_p,
                                    C.c_double, C.c_double, C.c_int, C.c_int]),
@@ -306,6 +307,11 @@ class IllumContext:
         res = C.c_double()
         _check(lib().ilg_radiosity_solve_gs(self._h, _p(E), int(gs_steps), _p(x), C.byref(res)))
         return x, res.value
+
+    def debug_barrier_timeout(self, blocks=4, polls=4096, unreachable=True):
+        """Status of one grid-barrier wait with a `polls` limit (test entry):
+        0 when the barrier opened, ILG_ERR_DEVICE when the wait ran out."""
+        return lib().ilg_debug_barrier_timeout(self._h, int(blocks), int(polls), int(bool(unreachable)))
 
     def radiosity_levels(self) -> int:
         n = C.c_int()

@@ -744,6 +744,16 @@ int ilg_radiosity_solve_gs(ilg_ctx* ctx, const double* E, int gs_steps, double* 
   return ILG_OK;
 }
 
+int ilg_debug_barrier_timeout(ilg_ctx* ctx, int blocks, long long polls, int unreachable) {
+  if (!ctx) { set_error("ctx is NULL"); return ILG_ERR_ARG; }
+  Context& c = ctx->c;
+  ILG_TRY(c.barrier.reserve(radiosity_barrier_words(1)));
+  ILG_TRY(c.derr.reserve(DERR_COUNT));
+  ILG_CUDA(cudaMemsetAsync(c.derr.p, 0, DERR_COUNT * sizeof(int), c.stream));
+  ILG_TRY(radiosity_barrier_probe(c.barrier.p, c.derr.p, blocks, polls, unreachable, c.stream));
+  return read_device_errors(c);   // ILG_ERR_DEVICE once the wait ran out (the flags are cleared)
+}
+
 int ilg_radiosity_levels(const ilg_ctx* ctx, int* levels) {
   if (!ctx || !levels) { set_error("ctx or levels is NULL"); return ILG_ERR_ARG; }
   *levels = gs_levels(ctx->c);

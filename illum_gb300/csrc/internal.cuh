@@ -322,6 +322,7 @@ int radiosity_threads();
 // the per-mesh residual accumulators of the radiosity kernels
 size_t radiosity_barrier_words(int nmesh);
 int radiosity_launch(const StepView& v, double* x, int warm, int precision, int grid, int inner, cudaStream_t s);
+int radiosity_barrier_probe(unsigned* bar, int* derr, int blocks, long long polls, int unreachable, cudaStream_t s);
 // inner sweeps of a mixed refinement round for a sweep budget (the smallest
 // budget of a view's meshes): the budget, at most radiosity_max_inner()
 int radiosity_inner(int max_sweeps);

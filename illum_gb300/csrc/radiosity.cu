@@ -86,14 +86,21 @@ constexpr int64_t RAD_GROUP = 4 * 1024;  // stored entries per group (4 per thre
 constexpr size_t RAD_SMEM =
     (size_t)RAD_HALO * sizeof(float2) + RAD_THREADS * sizeof(float2) + RAD_ROWS * sizeof(float2) + RAD_THREADS;
 
+// Most polls of one grid-barrier wait (about 2^26 x 32 ns before it gives
+// up). A device variable so that a test can shrink it (ilg_debug_barrier_
+// timeout) and watch a wait run out without a long stall.
+constexpr long long BARRIER_POLLS = 1LL << 26;
+__device__ long long g_barrier_polls = BARRIER_POLLS;
+
 // Grid barrier for a cooperative launch (all blocks co-resident) on an
 // arrival counter that only grows during the launch (zeroed before it):
 // every block counts its barriers in gen, and barrier number gen opens once
 // the counter reaches gen * nblocks, so the last block to arrive releases
 // the others with its own increment (no reset on the critical path). The
-// wait is bounded: after ~2^26 polls it records DERR_BARRIER and returns
-// false. The fences make the iterates written before the barrier visible to
-// the loads after it.
+// wait is bounded: after g_barrier_polls polls it records DERR_BARRIER and
+// returns false (as does every block that sees the flag while waiting).
+// The fences make the iterates written before the barrier visible to the
+// loads after it.
 __device__ bool grid_barrier(unsigned* bar, unsigned nblocks, unsigned& gen, int* derr) {
   __shared__ int ok;
   ++gen;
@@ -101,11 +108,12 @@ __device__ bool grid_barrier(unsigned* bar, unsigned nblocks, unsigned& gen, int
   if (threadIdx.x == 0) {
     ok = 1;
     const unsigned target = gen * nblocks;
+    const long long limit = g_barrier_polls;
     __threadfence();
     if (atomicAdd(bar, 1u) + 1u < target) {
       long long it = 0;
       while (*(volatile unsigned*)bar < target) {
-        if (++it > (1LL << 26) || *(volatile int*)&derr[DERR_BARRIER]) {
+        if (++it > limit || *(volatile int*)&derr[DERR_BARRIER]) {
           atomicExch(&derr[DERR_BARRIER], 1);
           ok = 0;
           break;
@@ -425,9 +433,8 @@ __device__ __forceinline__ void init_meshes(const StepView& v, MeshState& st) {
     st.sweeps[m] = 0;
     st.unit[m] = M.tol2 > 0.0 ? (float)((double)RES_UNITS / M.tol2 * (1.0 + 1.0 / 65536.0)) : INFINITY;
   }
-  // accumulators of residual 0 (read only after the first barrier)
-  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
-  for (int m = gt; m < v.nmesh; m += gridDim.x * blockDim.x) res_acc(v, 0)[m] = 0ull;
+  // the accumulators of residual 0 are cleared with the barrier counter
+  // before the launch (radiosity_launch): residual 0 starts without a barrier
 }
 
 // Every block, after the barrier that completes residual k: stop decisions
@@ -496,44 +503,76 @@ struct RadBufs {
   }
 };
 
-// free_rows: also write the result of the rows without entries (x = E,
-// s = 0) and their warm-start record, for a kernel that scatters its tile
-// rows itself.
-__device__ __forceinline__ void init_x(const StepView& v, double* x, int warm, int gt, int nthreads,
-                                       bool free_rows) {
+// The start of a solve at radiosity position p: the frame's direct flux,
+// coupled as src/cpp/illum_cli.cpp:415-421 when the mesh follows the
+// reference (rad = -Fsurf_prev + direct), in FP64, and the start of the
+// scattered part s = x - E: 0 (cold, or a row without entries) or the
+// mesh's previous solution extrapolated linearly once two exist (warm).
+// Evaluated where it is needed (a tile's own rows, its halo, the rows
+// without entries) instead of in a separate pass behind a grid barrier:
+// the inputs (E, Fsurf, sprev) do not change before the solve's last pass.
+struct SolveStart {
+  double e;
+  float2 s0;
+  int g;
+  bool act;     // the row has entries
+  bool on;      // its mesh is solved in this launch
+};
+__device__ __forceinline__ SolveStart solve_start(const StepView& v, uint32_t p, int warm) {
+  SolveStart r;
+  r.g = (int)v.rperm[p];
+  const MeshDesc& M = v.md[mesh_of_facet(v, r.g)];
+  r.on = M.active && M.ntiles > 0;
+  const double d = v.E[(size_t)(M.frame & 1) * v.nt + r.g];
+  r.e = M.coupling == ILG_COUPLE_REFERENCE ? (-v.Fsurf[r.g] + d) : d;
+  r.act = v.row_act[r.g] != 0;
+  r.s0 = make_float2(0.f, 0.f);
+  if (warm && r.act && M.frame >= 1) {
+    double s = v.sprev[r.g];
+    if (M.frame >= 2) s += v.sprev[v.nt + r.g];
+    r.s0 = split_df(s);
+  }
+  return r;
+}
+
+// Halo of the first pass: x = E + s0 of every halo facet, as a double-float.
+__device__ __forceinline__ void stage_halo_start(const StepView& v, const RowTile& T, int warm, float2* sx) {
+  const uint32_t* hp = v.t_halo + T.h0;
+  for (int h = threadIdx.x; h < T.nhalo; h += RAD_THREADS) {
+    const SolveStart st = solve_start(v, __ldg(hp + h), warm);
+    sx[h] = df_add(split_df(st.e), st.s0);
+  }
+  __syncthreads();
+}
+
+// Rows without entries have x = E exactly (s = 0): during the first pass
+// (grid-stride, before the first grid barrier) write what later passes and
+// the result read for them: the iterates and halo copies (FP64 kernel), or
+// the result itself, the warm-start record and zero corrections (mixed
+// kernel, whose blocks scatter their own tiles' rows).
+__device__ __forceinline__ void start_free_rows(const StepView& v, double* x, int warm, int gt, int nthreads,
+                                                bool mixed) {
   const RadBufs B(v);
   for (int p = gt; p < v.nt; p += nthreads) {
-    int g = (int)v.rperm[p];
-    const MeshDesc& M = v.md[mesh_of_facet(v, g)];
-    if (!M.active || M.ntiles == 0) continue;
-    // the frame's direct flux, coupled as src/cpp/illum_cli.cpp:415-421 when
-    // the mesh follows the reference (rad = -Fsurf_prev + direct)
-    const double d = v.E[(size_t)(M.frame & 1) * v.nt + g];
-    const double e = M.coupling == ILG_COUPLE_REFERENCE ? (-v.Fsurf[g] + d) : d;
-    float2 s0 = make_float2(0.f, 0.f);
-    if (warm && v.row_act[g] && M.frame >= 1) {
-      double s = v.sprev[g];
-      if (M.frame >= 2) s += v.sprev[v.nt + g];
-      s0 = split_df(s);
-    }
-    if (free_rows && !v.row_act[g]) {
-      x[g] = e;
+    const SolveStart st = solve_start(v, (uint32_t)p, warm);
+    if (!st.on || st.act) continue;
+    const float2 eh = split_df(st.e);
+    if (mixed) {
+      x[st.g] = st.e;
       if (warm) {
-        v.sprev[v.nt + g] = 0.0 - v.sprev[g];
-        v.sprev[g] = 0.0;
+        v.sprev[v.nt + st.g] = 0.0 - v.sprev[st.g];
+        v.sprev[st.g] = 0.0;
       }
-    }
-    const float2 eh = split_df(e);
-    const float2 x0 = df_add(eh, s0);
-    B.EP[p] = e;
-    B.S0[p] = s0;
-    B.S1[p] = make_float2(0.f, 0.f);
-    B.H0[p] = x0;
-    B.H1[p] = x0;
-    B.EH[p] = eh;
-    if (v.x32) {
+      B.H0[p] = eh;
       v.x32[p] = 0.f;
       v.x32[v.nt + p] = 0.f;
+    } else {
+      B.EP[p] = st.e;
+      B.S0[p] = make_float2(0.f, 0.f);
+      B.S1[p] = make_float2(0.f, 0.f);
+      B.H0[p] = eh;
+      B.H1[p] = eh;
+      B.EH[p] = eh;
     }
   }
 }
@@ -603,15 +642,16 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity64(StepView v, doub
   const int nthreads = gridDim.x * RAD_THREADS;
   unsigned gen = 0;
   init_meshes(v, st);
-  init_x(v, x, warm, gt, nthreads, false);
-  if (!grid_barrier(v.barrier, gridDim.x, gen, v.derr)) return;
+  __syncthreads();
   const uint64_t pol = l2_keep_policy();
   for (int it = 0;; ++it) {
+    if (it == 0) start_free_rows(v, x, warm, gt, nthreads, false);
     for (int t = blockIdx.x; t < v.ntiles; t += gridDim.x) {
       const RowTile T = v.tiles[t];
       if (st.done[T.mesh]) continue;
       const RadBufs B(v);
-      stage_halo(v, T, (it & 1) ? B.H1 : B.H0, sm.sx);
+      if (it == 0) stage_halo_start(v, T, warm, sm.sx);
+      else stage_halo(v, T, (it & 1) ? B.H1 : B.H0, sm.sx);
       tile_rows<AccDF>(v, T, t, ValsDF{v.t_vhi, v.t_vlo}, sm.sx, sm.tail, sm.tnew, sm.rs, pol);
       const uint32_t* rows = v.t_row + T.r0;
       const float2* cur = (it & 1) ? B.S1 : B.S0;
@@ -621,12 +661,22 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity64(StepView v, doub
       for (int r = threadIdx.x; r < T.nrows; r += RAD_THREADS) {
         uint32_t i = __ldg(rows + r);
         const float2 sn = sm.rs[r];          // s' = F x
-        const float2 sc = ld_it(cur + i);
+        float2 sc, eh;
+        if (it == 0) {                       // the row's start (E, s0), kept for the later passes
+          const SolveStart st0 = solve_start(v, i, warm);
+          sc = st0.s0;
+          eh = split_df(st0.e);
+          B.EP[i] = st0.e;
+          B.EH[i] = eh;
+        } else {
+          sc = ld_it(cur + i);
+          eh = ld_it(B.EH + i);
+        }
         // s' - s: exact high-part difference when the two are within a
         // factor of two, else rounded relative to the change itself
         const float df = __fadd_rn(__fsub_rn(sn.x, sc.x), __fsub_rn(sn.y, sc.y));
         nxt[i] = sn;
-        nxth[i] = df_add(__ldg(B.EH + i), sn);
+        nxth[i] = df_add(eh, sn);
         d2 = __fmaf_rn(df, df, d2);
       }
       post_partial(v, st, T, t, it, block_sum(d2, red));
@@ -657,25 +707,36 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity_mixed(StepView v, 
   float* r32 = v.x32 + 2 * (size_t)v.nt;
   unsigned gen = 0;
   init_meshes(v, st);
-  init_x(v, x, warm, gt, nthreads, true);
-  if (!grid_barrier(v.barrier, gridDim.x, gen, v.derr)) return;
+  __syncthreads();
   const uint64_t pol = l2_keep_policy();
   const RadBufs B(v);
   float2* S = B.S0;     // the iterate's scattered part s = x - E (radiosity positions)
   float2* XH = B.H0;    // x = E + s, what the halos gather
   int first = 1;
   for (int round = 0;; ++round) {
+    if (round == 0) start_free_rows(v, x, warm, gt, nthreads, true);
     for (int t = blockIdx.x; t < v.ntiles; t += gridDim.x) {
       const RowTile T = v.tiles[t];
       if (st.done[T.mesh]) continue;
-      stage_halo(v, T, XH, sm.sx);
+      if (round == 0) stage_halo_start(v, T, warm, sm.sx);
+      else stage_halo(v, T, XH, sm.sx);
       tile_rows<AccDF>(v, T, t, ValsHi{v.t_vhi}, sm.sx, sm.tail, sm.tnew, sm.rs, pol);
       const uint32_t* rows = v.t_row + T.r0;
       float d2 = 0.f;
       for (int r = threadIdx.x; r < T.nrows; r += RAD_THREADS) {
         uint32_t i = __ldg(rows + r);
+        float2 s;
+        if (round == 0) {                    // the row's start, kept for the later passes
+          const SolveStart st0 = solve_start(v, i, warm);
+          s = st0.s0;
+          B.EP[i] = st0.e;
+          S[i] = s;
+          XH[i] = df_add(split_df(st0.e), s);
+        } else {
+          s = ld_it(S + i);
+        }
         // r = E + fl(F) x - x = fl(F) x - s
-        const float2 fx = sm.rs[r], s = ld_it(S + i);
+        const float2 fx = sm.rs[r];
         const float res = __fadd_rn(__fsub_rn(fx.x, s.x), __fsub_rn(fx.y, s.y));
         r32[i] = res;
         xa[i] = res;     // inner start: d0 = r
@@ -1116,9 +1177,48 @@ int radiosity_grid(int ntiles, int precision) {
 // and residuals land in the mesh table.
 int radiosity_inner(int max_sweeps) { return max_sweeps < 1 ? 1 : (max_sweeps < RAD_INNER ? max_sweeps : RAD_INNER); }
 
+namespace {
+// Waits at one grid barrier that expects `expected` arrivals: with
+// expected > gridDim.x nobody can open it and every block's wait runs out.
+__global__ void k_barrier_probe(unsigned* bar, unsigned expected, int* derr) {
+  unsigned gen = 0;
+  grid_barrier(bar, expected, gen, derr);
+}
+}  // namespace
+
+// One cooperative launch of `blocks` blocks waiting at a barrier that
+// `unreachable` keeps shut, with the poll limit set to `polls` for the
+// launch (and restored after it). The wait's outcome is in the view's error
+// flags, read by the caller.
+int radiosity_barrier_probe(unsigned* bar, int* derr, int blocks, long long polls, int unreachable, cudaStream_t s) {
+  if (blocks < 1 || blocks > 8 || polls < 1) { set_error("invalid barrier probe"); return ILG_ERR_ARG; }
+  ILG_CUDA(cudaMemcpyToSymbolAsync(g_barrier_polls, &polls, sizeof(polls), 0, cudaMemcpyHostToDevice, s));
+  ILG_CUDA(cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), s));
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(blocks);
+  cfg.blockDim = dim3(32);
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  const unsigned expected = (unsigned)blocks + (unreachable ? 1u : 0u);
+  const cudaError_t e = cudaLaunchKernelEx(&cfg, k_barrier_probe, bar, expected, derr);
+  const long long standard = BARRIER_POLLS;
+  const cudaError_t e2 = cudaMemcpyToSymbolAsync(g_barrier_polls, &standard, sizeof(standard), 0,
+                                                 cudaMemcpyHostToDevice, s);
+  ILG_CUDA(e);
+  ILG_CUDA(e2);
+  ILG_CUDA(cudaStreamSynchronize(s));
+  return ILG_OK;
+}
+
 int radiosity_launch(const StepView& v, double* x, int warm, int precision, int grid, int inner, cudaStream_t s) {
   ILG_TRY(radiosity_setup());
-  ILG_CUDA(cudaMemsetAsync(v.barrier, 0, 2 * sizeof(unsigned), s));
+  // the barrier counter and the meshes' residual-0 accumulators (buffer 0,
+  // nmesh 64-bit words right after the counter's two words)
+  ILG_CUDA(cudaMemsetAsync(v.barrier, 0, (2 + 2 * (size_t)v.nmesh) * sizeof(unsigned), s));
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(grid);
   cfg.blockDim = dim3(RAD_THREADS);

@@ -88,6 +88,28 @@ def icosphere(level: int):
     return v, f
 
 
+_ICO_CACHE: dict = {}
+
+
+def _icosphere_cached(level: int):
+    """icosphere(level) and the 2-ring smoothing operator of its vertices,
+    built once per level (the generators copy what they modify)."""
+    if level not in _ICO_CACHE:
+        v, f = icosphere(level)
+        _ICO_CACHE[level] = (v, f, None)
+    return _ICO_CACHE[level]
+
+
+def _two_ring(level: int):
+    v, f, A2 = _icosphere_cached(level)
+    if A2 is None:
+        A = _vertex_adjacency(v.shape[0], f)
+        A2 = (A @ A)
+        A2.data[:] = 1.0
+        _ICO_CACHE[level] = (v, f, A2)
+    return A2
+
+
 def _vertex_adjacency(nv: int, f: np.ndarray):
     import scipy.sparse as sp
     e = np.concatenate([f[:, [0, 1]], f[:, [1, 2]], f[:, [2, 0]]])
@@ -104,19 +126,20 @@ def icosphere_craters(level: int, seed: int, radius_m: float = 1000.0, sigma_m: 
     """Icosphere + smoothed Gaussian radial field + spherical-cap craters.
 
     Returns (verts float32 [V,3] in km, faces int32 [F,3])."""
-    v, f = icosphere(level)
+    v, f, _ = _icosphere_cached(level)
     nv = v.shape[0]
-    g = normal(seed, 1, nv)
-    A = _vertex_adjacency(nv, f)
-    A2 = (A @ A)
-    A2.data[:] = 1.0
-    deg = np.asarray(A2.sum(axis=1)).ravel()
-    h = (A2 @ g) / deg
-    h = h - h.mean()
-    sd = h.std()
-    if sd > 0:
-        h *= sigma_m / sd
-    r = radius_m + h
+    if sigma_m != 0.0:
+        g = normal(seed, 1, nv)
+        A2 = _two_ring(level)
+        deg = np.asarray(A2.sum(axis=1)).ravel()
+        h = (A2 @ g) / deg
+        h = h - h.mean()
+        sd = h.std()
+        if sd > 0:
+            h *= sigma_m / sd
+        r = radius_m + h
+    else:
+        r = np.full(nv, radius_m)
     if n_craters > 0:
         cu = uniform(seed, 2, n_craters)
         cv = uniform(seed, 3, n_craters)

@@ -229,6 +229,18 @@ int ilg_get_outputs(ilg_ctx* ctx, double* rad, double* rad_avg, double* therm_av
  * enabled, and per-call counters. */
 int ilg_set_timing(ilg_ctx* ctx, int enable);
 
+/* ---- bounded device waits (no reference counterpart) ------------------------- */
+/* Test entry for the radiosity solver's grid barrier, whose waits are
+ * bounded: one cooperative launch of `blocks` (1..8) blocks waits at a
+ * barrier with the poll limit set to `polls` for that launch. With
+ * unreachable != 0 the barrier expects one more arrival than there are
+ * blocks, so every wait runs out: the call returns ILG_ERR_DEVICE ("grid
+ * barrier wait exceeded its limit") and the context stays usable. With
+ * unreachable == 0 the barrier opens and the call returns ILG_OK. The poll
+ * limit is a per-device setting for the duration of the launch: do not run
+ * radiosity solves on the same device meanwhile. */
+int ilg_debug_barrier_timeout(ilg_ctx* ctx, int blocks, long long polls, int unreachable);
+
 /* ---- launch-shape autotuner (no reference counterpart) ------------------------ */
 /* Launch shapes of the step kernels. No result depends on them (every
  * facet's work is independent of the block it runs in, and the sums are
