@@ -81,6 +81,8 @@ _SIGS = {
     "ilg_F_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int),
                              C.POINTER(C.c_int)]),
     "ilg_make_horizons": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_double]),
+    "ilg_make_horizons_mesh": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_double,
+                                         C.c_double]),
     "ilg_get_horizons": (C.c_int, [C.c_void_p, C.c_void_p]),
     "ilg_set_horizons": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
     "ilg_set_insolation": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_double]),
@@ -261,8 +263,23 @@ class IllumContext:
         self.nnz = val.shape[0]
 
     # -- horizons
+    def set_horizon_mesh(self, verts, faces):
+        """A separate mesh the horizon rays are cast against
+        (illum_context::set_horizon_obj_file, src/cpp/illum.hpp:36-37);
+        None clears it."""
+        if verts is None:
+            self._hmesh = None
+        else:
+            self._hmesh = (np.ascontiguousarray(verts, np.float32), np.ascontiguousarray(faces, np.int32))
+
     def make_horizons(self, nphi=361, theta_eps=1e-3, offset=1e-5):
-        _check(lib().ilg_make_horizons(self._h, nphi, theta_eps, offset))
+        hm = getattr(self, "_hmesh", None)
+        if hm is None:
+            _check(lib().ilg_make_horizons(self._h, nphi, theta_eps, offset))
+        else:
+            v, f = hm
+            _check(lib().ilg_make_horizons_mesh(self._h, _p(v), v.shape[0], _p(f), f.shape[0], nphi, theta_eps,
+                                                offset))
         self.nphi = nphi
 
     @property

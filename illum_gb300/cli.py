@@ -135,8 +135,6 @@ def resolve(argv=None) -> argparse.Namespace:
                 val = val if isinstance(val, list) else [val]
                 val = [float(x) for x in val]
             setattr(args, k, val)
-    if args.horizon_obj_file:
-        raise SystemExit("horizon_obj_file (a separate horizon mesh) is not supported")
     if args.mesh_unit == "m":
         print("mesh_unit m: vertices are taken as given (the reference has not implemented it)")
     return args
@@ -157,6 +155,11 @@ def _context(args):
         raise SystemExit("--path is required")
     v, f, n = _timed(f"- loading {args.path}", lambda: meshgen.load_obj(args.path, args.shape))
     ctx = _timed("- building LBVH", lambda: ig.IllumContext(v, f, n))
+    if args.horizon_obj_file:
+        # a separate mesh for the horizon rays (src/cpp/illum_cli.cpp:899-901)
+        hv, hf, _ = _timed(f"- loading horizon mesh {args.horizon_obj_file}",
+                           lambda: meshgen.load_obj(args.horizon_obj_file, 0))
+        ctx.set_horizon_mesh(hv, hf)
     return ig, ctx
 
 

@@ -285,6 +285,7 @@ static int build(Batch& b) {
   v.therm_avg = b.therm_avg.p; v.therm_max = b.therm_max.p; v.E = b.E.p; v.sprev = b.sprev.p;
   v.x32 = b.x32.p; v.Tdf = b.Tdf.p; v.T32 = b.T32.p; v.coefdf = b.coefdf.p; v.coef32 = b.coef32.p;
   v.tiles = b.tiles.p; v.ntiles = b.ntiles;
+  v.l2_stream = radiosity_l2_stream(b.nel);
   v.t_cf = b.t_cf.p; v.t_vhi = b.t_vhi.p; v.t_vlo = b.t_vlo.p; v.t_vbf = b.t_vbf.p;
   v.t_row = b.t_row.p; v.t_halo = b.t_halo.p; v.t_start = b.t_start.p; v.t_scale = b.t_scale.p;
   v.tile_d2 = b.tile_d2.p;

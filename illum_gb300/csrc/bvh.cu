@@ -813,7 +813,7 @@ static int build_horizon_tree(double theta_eps, std::vector<HorizonNode>& tree) 
   return ILG_OK;
 }
 
-int horizons_build(Context& c, int nphi, double theta_eps, double offset) {
+int horizons_build(Context& c, int nphi, double theta_eps, double offset, const Context* hmesh) {
   if (nphi < 2) { set_error("nphi must be >= 2"); return ILG_ERR_ARG; }
   if (!(theta_eps > 0.0)) { set_error("theta_eps must be > 0"); return ILG_ERR_ARG; }
   cudaStream_t s = c.stream;
@@ -835,7 +835,10 @@ int horizons_build(Context& c, int nphi, double theta_eps, double offset) {
   ILG_CUDA(cudaMemcpyAsync(ds.p, sph.data(), nphi * 8, cudaMemcpyHostToDevice, s));
   ILG_TRY(c.H.alloc((size_t)c.nt * nphi));
   int64_t total = (int64_t)c.nt * nphi;
-  k_horizons<<<div_up(total, 128), 128, 0, s>>>(c.nodes.p, c.tri_s.p, c.root, c.tri_o.p, c.cen.p, c.nrm.p, c.nt,
+  // the rays of a separate horizon mesh's facets-independent BVH, or the
+  // context's own (src/cpp/illum.cpp:333-360)
+  const Context& hb = hmesh ? *hmesh : c;
+  k_horizons<<<div_up(total, 128), 128, 0, s>>>(hb.nodes.p, hb.tri_s.p, hb.root, c.tri_o.p, c.cen.p, c.nrm.p, c.nt,
                                                 nphi, dc.p, ds.p, dtree.p, (int)tree.size(), (float)offset, c.H.p,
                                                 c.derr.p);
   ILG_CUDA(cudaGetLastError());

@@ -201,6 +201,7 @@ static StepView solo_view(Context& c, int precision) {
   v.T64 = nullptr; v.Tdf = c.Tdf.p; v.T32 = c.T32.p;
   v.coef64 = nullptr; v.coefdf = c.coefdf.p; v.coef32 = c.coef32.p;
   v.tiles = c.tiles.p; v.ntiles = c.have_F ? c.ntiles : 0;
+  v.l2_stream = radiosity_l2_stream(c.tile_elems);
   v.t_cf = c.t_cf.p; v.t_vhi = c.t_vhi.p; v.t_vlo = c.t_vlo.p; v.t_vbf = c.t_vbf.p;
   v.t_row = c.t_row.p; v.t_halo = c.t_halo.p; v.t_start = c.t_start.p; v.t_scale = c.t_scale.p;
   v.tile_d2 = c.tile_d2.p;
@@ -613,6 +614,17 @@ int ilg_make_horizons(ilg_ctx* ctx, int nphi, double theta_eps, double offset) {
   if (!ctx) { set_error("ctx is NULL"); return ILG_ERR_ARG; }
   invalidate_graph(ctx->c);
   return horizons_build(ctx->c, nphi, theta_eps, offset);
+}
+
+int ilg_make_horizons_mesh(ilg_ctx* ctx, const float* verts, int nv, const int32_t* tris, int nt, int nphi,
+                           double theta_eps, double offset) {
+  if (!ctx) { set_error("ctx is NULL"); return ILG_ERR_ARG; }
+  ilg_ctx* hm = nullptr;
+  ILG_TRY(ilg_ctx_create(verts, nv, tris, nt, nullptr, &hm));   // the horizon mesh's LBVH (synchronised)
+  invalidate_graph(ctx->c);
+  const int rc = horizons_build(ctx->c, nphi, theta_eps, offset, &hm->c);
+  ilg_ctx_destroy(hm);
+  return rc;
 }
 
 int ilg_get_horizons(ilg_ctx* ctx, double* out) {

@@ -135,6 +135,7 @@ struct StepView {
   // radiosity row tiles
   const RowTile* tiles;
   int ntiles;
+  int l2_stream;               // 1: the stored matrix is much larger than L2 (stream it evict-first)
   const uint16_t* t_cf;        // per stored entry: halo index | row end << 15
   const float* t_vhi;          // double-float values: hi = fl(F)
   const float* t_vlo;          //   and lo = fl(F - hi)
@@ -301,7 +302,9 @@ struct StepPlan {
 int bvh_build(Context& c, const float* verts_h, int nv, const int32_t* tris_h, const float* normals_h);
 int bvh_trace(Context& c, int nrays, const float* orig_h, const float* dir_h, int any_hit, int32_t* hit_h,
               double* t_h);
-int horizons_build(Context& c, int nphi, double theta_eps, double offset);
+// hmesh: the context of a separate horizon mesh whose LBVH the horizon
+// rays are traced against (nullptr: c's own)
+int horizons_build(Context& c, int nphi, double theta_eps, double offset, const Context* hmesh = nullptr);
 int horizons_f32(Context& c);   // H32 and hmm32 from H
 int bvh_render(Context& c, int mode, double az_deg, double el_deg, int width, int height, int32_t* out_h);
 int form_factors_build(Context& c, const double* albedo_h, double albedo_scalar, double offset,
@@ -317,6 +320,8 @@ int direct_launch(const StepView& v, int dropin, int mu32_flux, int ahead, cudaS
 int radiosity_prepare(Context& c);
 int radiosity_grid(int ntiles, int precision);
 int radiosity_max_meshes();
+// whether a matrix of `stored` entries is streamed (larger than ~3/4 of L2)
+int radiosity_l2_stream(int64_t stored);
 int radiosity_threads();
 // unsigned words of a view's barrier buffer: the grid barrier's counter and
 // the per-mesh residual accumulators of the radiosity kernels

@@ -132,12 +132,23 @@ __device__ __forceinline__ int mesh_of_facet(const StepView& v, int g) { return 
 // Matrix loads: read-only for the whole solve, so the non-coherent path, no
 // L1 allocation (each entry is used once per sweep), and an L2 evict-last
 // policy on 3/4 of the lines so that repeated sweeps find most of the
-// matrix in L2 when it is about as large as L2.
-__device__ __forceinline__ uint64_t l2_keep_policy() {
+// matrix in L2 when it is about as large as L2. A matrix much larger than
+// L2 is streamed with evict-first instead (nothing of it survives until the
+// next pass, and evict-last lines would only crowd out the iterates).
+__device__ __forceinline__ uint64_t l2_keep_policy(int stream) {
   uint64_t pol;
-  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 0.75;" : "=l"(pol));
+  if (stream)
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+  else
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 0.75;" : "=l"(pol));
   return pol;
 }
+// L2 prefetch of the entry groups RAD_PF groups ahead of the one being
+// summed: the register pipeline keeps two groups in flight per thread,
+// which at one 1024-thread block per SM is too few bytes in flight to
+// cover DRAM latency; prefetched lines arrive in L2 meanwhile.
+constexpr int RAD_PF = 6;
+__device__ __forceinline__ void pf_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 __device__ __forceinline__ uint2 ld_mat(const uint2* p, uint64_t pol) {
   uint2 r;
   asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v2.u32 {%0, %1}, [%2], %3;"
@@ -168,6 +179,9 @@ __device__ __forceinline__ void ld_vals4(ValsHi s, size_t off, float2 (&w)[4], u
   w[2] = make_float2(h.z, 0.f);
   w[3] = make_float2(h.w, 0.f);
 }
+__device__ __forceinline__ void pf_vals(ValsDF s, size_t off) { pf_l2(s.hi + off); pf_l2(s.lo + off); }
+__device__ __forceinline__ void pf_vals(ValsHi s, size_t off) { pf_l2(s.hi + off); }
+__device__ __forceinline__ void pf_vals(ValsBF s, size_t off) { pf_l2(s.v + off); }
 __device__ __forceinline__ void ld_vals4(ValsBF s, size_t off, float (&w)[4], uint64_t pol) {
   uint2 r = ld_mat(reinterpret_cast<const uint2*>(s.v + off), pol);
   w[0] = __uint_as_float(r.x << 16);
@@ -316,6 +330,10 @@ __device__ __forceinline__ void tile_rows(const StepView& v, const RowTile& T, i
       any = true;
     }
   };
+  for (int q = 2; q < RAD_PF && q < ng; ++q) {
+    pf_l2(cfp + (size_t)q * RAD_THREADS);
+    pf_vals(vals, vo + (size_t)q * 4 * RAD_THREADS);
+  }
   uint2 c0 = ld_mat(cfp, pol), c1 = c0;
   W w0[4], w1[4];
   ld_vals4(vals, vo, w0, pol);
@@ -329,6 +347,10 @@ __device__ __forceinline__ void tile_rows(const StepView& v, const RowTile& T, i
   for (int g = 0; g < ng; ++g) {
     uint2 c2 = c1;
     W w2[4];
+    if (g + RAD_PF < ng) {
+      pf_l2(cfp + (size_t)(g + RAD_PF) * RAD_THREADS);
+      pf_vals(vals, vo + (size_t)(g + RAD_PF) * 4 * RAD_THREADS);
+    }
     if (g + 2 < ng) {
       c2 = ld_mat(cfp + (size_t)(g + 2) * RAD_THREADS, pol);
       ld_vals4(vals, vo + (size_t)(g + 2) * 4 * RAD_THREADS, w2, pol);
@@ -433,8 +455,9 @@ __device__ __forceinline__ void init_meshes(const StepView& v, MeshState& st) {
     st.sweeps[m] = 0;
     st.unit[m] = M.tol2 > 0.0 ? (float)((double)RES_UNITS / M.tol2 * (1.0 + 1.0 / 65536.0)) : INFINITY;
   }
-  // the accumulators of residual 0 are cleared with the barrier counter
-  // before the launch (radiosity_launch): residual 0 starts without a barrier
+  // accumulators of residual 0 (read only after the first barrier)
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+  for (int m = gt; m < v.nmesh; m += gridDim.x * blockDim.x) res_acc(v, 0)[m] = 0ull;
 }
 
 // Every block, after the barrier that completes residual k: stop decisions
@@ -503,76 +526,44 @@ struct RadBufs {
   }
 };
 
-// The start of a solve at radiosity position p: the frame's direct flux,
-// coupled as src/cpp/illum_cli.cpp:415-421 when the mesh follows the
-// reference (rad = -Fsurf_prev + direct), in FP64, and the start of the
-// scattered part s = x - E: 0 (cold, or a row without entries) or the
-// mesh's previous solution extrapolated linearly once two exist (warm).
-// Evaluated where it is needed (a tile's own rows, its halo, the rows
-// without entries) instead of in a separate pass behind a grid barrier:
-// the inputs (E, Fsurf, sprev) do not change before the solve's last pass.
-struct SolveStart {
-  double e;
-  float2 s0;
-  int g;
-  bool act;     // the row has entries
-  bool on;      // its mesh is solved in this launch
-};
-__device__ __forceinline__ SolveStart solve_start(const StepView& v, uint32_t p, int warm) {
-  SolveStart r;
-  r.g = (int)v.rperm[p];
-  const MeshDesc& M = v.md[mesh_of_facet(v, r.g)];
-  r.on = M.active && M.ntiles > 0;
-  const double d = v.E[(size_t)(M.frame & 1) * v.nt + r.g];
-  r.e = M.coupling == ILG_COUPLE_REFERENCE ? (-v.Fsurf[r.g] + d) : d;
-  r.act = v.row_act[r.g] != 0;
-  r.s0 = make_float2(0.f, 0.f);
-  if (warm && r.act && M.frame >= 1) {
-    double s = v.sprev[r.g];
-    if (M.frame >= 2) s += v.sprev[v.nt + r.g];
-    r.s0 = split_df(s);
-  }
-  return r;
-}
-
-// Halo of the first pass: x = E + s0 of every halo facet, as a double-float.
-__device__ __forceinline__ void stage_halo_start(const StepView& v, const RowTile& T, int warm, float2* sx) {
-  const uint32_t* hp = v.t_halo + T.h0;
-  for (int h = threadIdx.x; h < T.nhalo; h += RAD_THREADS) {
-    const SolveStart st = solve_start(v, __ldg(hp + h), warm);
-    sx[h] = df_add(split_df(st.e), st.s0);
-  }
-  __syncthreads();
-}
-
-// Rows without entries have x = E exactly (s = 0): during the first pass
-// (grid-stride, before the first grid barrier) write what later passes and
-// the result read for them: the iterates and halo copies (FP64 kernel), or
-// the result itself, the warm-start record and zero corrections (mixed
-// kernel, whose blocks scatter their own tiles' rows).
-__device__ __forceinline__ void start_free_rows(const StepView& v, double* x, int warm, int gt, int nthreads,
-                                                bool mixed) {
+// free_rows: also write the result of the rows without entries (x = E,
+// s = 0) and their warm-start record, for a kernel that scatters its tile
+// rows itself.
+__device__ __forceinline__ void init_x(const StepView& v, double* x, int warm, int gt, int nthreads,
+                                       bool free_rows) {
   const RadBufs B(v);
   for (int p = gt; p < v.nt; p += nthreads) {
-    const SolveStart st = solve_start(v, (uint32_t)p, warm);
-    if (!st.on || st.act) continue;
-    const float2 eh = split_df(st.e);
-    if (mixed) {
-      x[st.g] = st.e;
+    int g = (int)v.rperm[p];
+    const MeshDesc& M = v.md[mesh_of_facet(v, g)];
+    if (!M.active || M.ntiles == 0) continue;
+    // the frame's direct flux, coupled as src/cpp/illum_cli.cpp:415-421 when
+    // the mesh follows the reference (rad = -Fsurf_prev + direct)
+    const double d = v.E[(size_t)(M.frame & 1) * v.nt + g];
+    const double e = M.coupling == ILG_COUPLE_REFERENCE ? (-v.Fsurf[g] + d) : d;
+    float2 s0 = make_float2(0.f, 0.f);
+    if (warm && v.row_act[g] && M.frame >= 1) {
+      double s = v.sprev[g];
+      if (M.frame >= 2) s += v.sprev[v.nt + g];
+      s0 = split_df(s);
+    }
+    if (free_rows && !v.row_act[g]) {
+      x[g] = e;
       if (warm) {
-        v.sprev[v.nt + st.g] = 0.0 - v.sprev[st.g];
-        v.sprev[st.g] = 0.0;
+        v.sprev[v.nt + g] = 0.0 - v.sprev[g];
+        v.sprev[g] = 0.0;
       }
-      B.H0[p] = eh;
+    }
+    const float2 eh = split_df(e);
+    const float2 x0 = df_add(eh, s0);
+    B.EP[p] = e;
+    B.S0[p] = s0;
+    B.S1[p] = make_float2(0.f, 0.f);
+    B.H0[p] = x0;
+    B.H1[p] = x0;
+    B.EH[p] = eh;
+    if (v.x32) {
       v.x32[p] = 0.f;
       v.x32[v.nt + p] = 0.f;
-    } else {
-      B.EP[p] = st.e;
-      B.S0[p] = make_float2(0.f, 0.f);
-      B.S1[p] = make_float2(0.f, 0.f);
-      B.H0[p] = eh;
-      B.H1[p] = eh;
-      B.EH[p] = eh;
     }
   }
 }
@@ -642,16 +633,15 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity64(StepView v, doub
   const int nthreads = gridDim.x * RAD_THREADS;
   unsigned gen = 0;
   init_meshes(v, st);
-  __syncthreads();
-  const uint64_t pol = l2_keep_policy();
+  init_x(v, x, warm, gt, nthreads, false);
+  if (!grid_barrier(v.barrier, gridDim.x, gen, v.derr)) return;
+  const uint64_t pol = l2_keep_policy(v.l2_stream);
   for (int it = 0;; ++it) {
-    if (it == 0) start_free_rows(v, x, warm, gt, nthreads, false);
     for (int t = blockIdx.x; t < v.ntiles; t += gridDim.x) {
       const RowTile T = v.tiles[t];
       if (st.done[T.mesh]) continue;
       const RadBufs B(v);
-      if (it == 0) stage_halo_start(v, T, warm, sm.sx);
-      else stage_halo(v, T, (it & 1) ? B.H1 : B.H0, sm.sx);
+      stage_halo(v, T, (it & 1) ? B.H1 : B.H0, sm.sx);
       tile_rows<AccDF>(v, T, t, ValsDF{v.t_vhi, v.t_vlo}, sm.sx, sm.tail, sm.tnew, sm.rs, pol);
       const uint32_t* rows = v.t_row + T.r0;
       const float2* cur = (it & 1) ? B.S1 : B.S0;
@@ -661,22 +651,12 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity64(StepView v, doub
       for (int r = threadIdx.x; r < T.nrows; r += RAD_THREADS) {
         uint32_t i = __ldg(rows + r);
         const float2 sn = sm.rs[r];          // s' = F x
-        float2 sc, eh;
-        if (it == 0) {                       // the row's start (E, s0), kept for the later passes
-          const SolveStart st0 = solve_start(v, i, warm);
-          sc = st0.s0;
-          eh = split_df(st0.e);
-          B.EP[i] = st0.e;
-          B.EH[i] = eh;
-        } else {
-          sc = ld_it(cur + i);
-          eh = ld_it(B.EH + i);
-        }
+        const float2 sc = ld_it(cur + i);
         // s' - s: exact high-part difference when the two are within a
         // factor of two, else rounded relative to the change itself
         const float df = __fadd_rn(__fsub_rn(sn.x, sc.x), __fsub_rn(sn.y, sc.y));
         nxt[i] = sn;
-        nxth[i] = df_add(eh, sn);
+        nxth[i] = df_add(__ldg(B.EH + i), sn);
         d2 = __fmaf_rn(df, df, d2);
       }
       post_partial(v, st, T, t, it, block_sum(d2, red));
@@ -707,36 +687,25 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity_mixed(StepView v, 
   float* r32 = v.x32 + 2 * (size_t)v.nt;
   unsigned gen = 0;
   init_meshes(v, st);
-  __syncthreads();
-  const uint64_t pol = l2_keep_policy();
+  init_x(v, x, warm, gt, nthreads, true);
+  if (!grid_barrier(v.barrier, gridDim.x, gen, v.derr)) return;
+  const uint64_t pol = l2_keep_policy(v.l2_stream);
   const RadBufs B(v);
   float2* S = B.S0;     // the iterate's scattered part s = x - E (radiosity positions)
   float2* XH = B.H0;    // x = E + s, what the halos gather
   int first = 1;
   for (int round = 0;; ++round) {
-    if (round == 0) start_free_rows(v, x, warm, gt, nthreads, true);
     for (int t = blockIdx.x; t < v.ntiles; t += gridDim.x) {
       const RowTile T = v.tiles[t];
       if (st.done[T.mesh]) continue;
-      if (round == 0) stage_halo_start(v, T, warm, sm.sx);
-      else stage_halo(v, T, XH, sm.sx);
+      stage_halo(v, T, XH, sm.sx);
       tile_rows<AccDF>(v, T, t, ValsHi{v.t_vhi}, sm.sx, sm.tail, sm.tnew, sm.rs, pol);
       const uint32_t* rows = v.t_row + T.r0;
       float d2 = 0.f;
       for (int r = threadIdx.x; r < T.nrows; r += RAD_THREADS) {
         uint32_t i = __ldg(rows + r);
-        float2 s;
-        if (round == 0) {                    // the row's start, kept for the later passes
-          const SolveStart st0 = solve_start(v, i, warm);
-          s = st0.s0;
-          B.EP[i] = st0.e;
-          S[i] = s;
-          XH[i] = df_add(split_df(st0.e), s);
-        } else {
-          s = ld_it(S + i);
-        }
         // r = E + fl(F) x - x = fl(F) x - s
-        const float2 fx = sm.rs[r];
+        const float2 fx = sm.rs[r], s = ld_it(S + i);
         const float res = __fadd_rn(__fsub_rn(fx.x, s.x), __fsub_rn(fx.y, s.y));
         r32[i] = res;
         xa[i] = res;     // inner start: d0 = r
@@ -1161,6 +1130,10 @@ int radiosity_prepare(Context& c) {
 
 int radiosity_max_meshes() { return RAD_MAX_MESH; }
 int radiosity_threads() { return RAD_THREADS; }
+// 10 bytes per stored entry (u16 column, f32 hi, f32 lo or bf16): streamed
+// when it would not stay in the 126 MB L2 between passes.
+int radiosity_l2_stream(int64_t stored) { return stored * 10 > (int64_t)96 << 20 ? 1 : 0; }
+
 size_t radiosity_barrier_words(int nmesh) { return 2 + 2 * 3 * (size_t)(nmesh > 0 ? nmesh : 1); }
 
 // Cooperative grid size for ntiles tiles (at most the co-resident blocks).
@@ -1216,9 +1189,7 @@ int radiosity_barrier_probe(unsigned* bar, int* derr, int blocks, long long poll
 
 int radiosity_launch(const StepView& v, double* x, int warm, int precision, int grid, int inner, cudaStream_t s) {
   ILG_TRY(radiosity_setup());
-  // the barrier counter and the meshes' residual-0 accumulators (buffer 0,
-  // nmesh 64-bit words right after the counter's two words)
-  ILG_CUDA(cudaMemsetAsync(v.barrier, 0, (2 + 2 * (size_t)v.nmesh) * sizeof(unsigned), s));
+  ILG_CUDA(cudaMemsetAsync(v.barrier, 0, 2 * sizeof(unsigned), s));
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(grid);
   cfg.blockDim = dim3(RAD_THREADS);

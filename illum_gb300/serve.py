@@ -119,22 +119,31 @@ class Server:
         self.per_facet = {}            # level -> largest measured bytes per facet of a built job
         self.est_ratio = []            # measured / reserved per job
         self.setup_s = []
+        self.phase_s = []              # per job: mesh, LBVH, horizons, form factors, suns + thermal (s)
+        self.first_building = set()    # levels whose first job is being built
 
     # -------------------------------------------------------------- setup
     def build_job(self, r: Request) -> Job:
         # craters as in the CPU-runnable configuration (20 caps, 80-300 m), no
         # extra radial roughness
+        t = [time.perf_counter()]
         v, f = meshgen.icosphere_craters(r.level, r.seed, sigma_m=0.0, n_craters=r.n_craters, dmin_m=80.0,
                                          dmax_m=300.0)
+        t.append(time.perf_counter())
         ctx = ig.IllumContext(v, f)
+        t.append(time.perf_counter())
         ctx.make_horizons(nphi=self.nphi)
+        t.append(time.perf_counter())
         ctx.set_insolation(1, 0, self.solar)
         ctx.compute_F(albedo=0.1, fetch=False)
+        t.append(time.perf_counter())
         period = r.period_h * 3600.0
         dt = period / r.steps_per_rot
         ctx.set_suns(meshgen.spin_sun_positions(r.nsteps, period, dt), ig.fib_spiral(100))
         tm = ig.ThermalModel(ctx, meshgen.geometric_depths(r.nz), r.ti, 1.05e6, 200.0, emissivity=0.95,
                              bc_mode=ig.BC_NEWTON, precision=self.precision)
+        t.append(time.perf_counter())
+        self.phase_s.append(np.diff(t))
         # mixed: one refinement round per step (one bf16 sweep)
         opts = ig.RunOpts(dt=dt, tol=self.tol, max_sweeps=1 if self.precision == ig.PREC_MIXED else 200,
                           use_radiosity=1, use_graph=1,
@@ -142,15 +151,14 @@ class Server:
         return Job(req=r, ctx=ctx, tm=tm, opts=opts, nfaces=f.shape[0])
 
     def _estimate(self, r: Request) -> int:
-        """Bytes to reserve for r: the a priori estimate, or, once a job of
+        """Bytes to reserve for r (called with the lock held): once a job of
         the same level has been built, 1.25 x the largest measured bytes per
-        facet at that level (form factors per facet vary with the craters)."""
-        est = footprint_bytes(r.level, r.nz, self.nphi, self.precision)
-        with self.lock:
-            pf = self.per_facet.get(r.level)
+        facet at that level (form factors per facet vary with the craters);
+        before that, 3 x the a priori estimate."""
+        pf = self.per_facet.get(r.level)
         if pf is not None:
-            est = int(1.25 * pf * 20 * 4 ** r.level)
-        return est
+            return int(1.25 * pf * 20 * 4 ** r.level)
+        return 3 * footprint_bytes(r.level, r.nz, self.nphi, self.precision)
 
     def _build_one(self, r: Request, need: int):
         try:
@@ -163,6 +171,7 @@ class Server:
                 self.used += actual - need
                 self.max_used = max(self.max_used, self.used)
                 self.per_facet[r.level] = max(self.per_facet.get(r.level, 0.0), actual / job.nfaces)
+                self.first_building.discard(r.level)
                 self.lock.notify_all()
             self.est_ratio.append(actual / need)
             job.footprint = actual
@@ -170,13 +179,19 @@ class Server:
             self.ready.put(job)
         except Exception as e:   # surfaced by run()
             self.error = e
+            with self.lock:
+                self.first_building.discard(r.level)
+                self.lock.notify_all()
             self.ready.put(None)
 
     def stats(self) -> dict:
         """Admission and set-up figures of the last run."""
         er = np.array(self.est_ratio) if self.est_ratio else np.zeros(1)
         st = np.array(self.setup_s) if self.setup_s else np.zeros(1)
-        return {"budget_bytes": self.budget, "max_reserved_bytes": self.max_used,
+        ph = np.array(self.phase_s) if self.phase_s else np.zeros((1, 5))
+        names = ("mesh", "lbvh", "horizons", "form_factors", "suns_thermal")
+        return {"setup_phase_sum_s": {n: float(x) for n, x in zip(names, ph.sum(0))},
+                "budget_bytes": self.budget, "max_reserved_bytes": self.max_used,
                 "max_reserved_over_budget": self.max_used / self.budget,
                 "measured_over_reserved": {"max": float(er.max()), "median": float(np.median(er))},
                 "setup_s": {"median": float(np.median(st)), "max": float(st.max()), "sum": float(st.sum())},
@@ -189,12 +204,18 @@ class Server:
                 wait = r.arrival - (time.perf_counter() - self.t0)
                 if wait > 0:
                     time.sleep(wait)
-                need = self._estimate(r)
                 with self.lock:
-                    while self.used + need > self.budget and self.used > 0:
+                    # a level's first job is built alone: the jobs after it
+                    # reserve what it measured
+                    while r.level in self.first_building and not self.error:
+                        self.lock.wait()
+                    need = self._estimate(r)
+                    while self.used + need > self.budget and self.used > 0 and not self.error:
                         self.lock.wait()
                     self.used += need
                     self.max_used = max(self.max_used, self.used)
+                    if r.level not in self.per_facet:
+                        self.first_building.add(r.level)
                 if self.error:
                     break
                 pool.submit(self._build_one, r, need)

@@ -121,6 +121,14 @@ int ilg_F_info(const ilg_ctx* ctx, int64_t* nnz, int64_t* stored_entries, int* r
 
 /* ---- horizons ----------------------------------------------------------- */
 int ilg_make_horizons(ilg_ctx* ctx, int nphi, double theta_eps, double offset);
+/* make_horizons with a separate horizon mesh (illum_context::
+ * set_horizon_obj_file, src/cpp/illum.hpp:36-37, used at
+ * src/cpp/illum.cpp:333-349): every facet of the context keeps its own
+ * centroid, normal and frame, and its horizon rays are cast against the
+ * triangles verts / tris (nv x 3 float, nt x 3 int32), e.g. a larger patch
+ * of terrain around the mesh. The horizon mesh's LBVH lives for the call. */
+int ilg_make_horizons_mesh(ilg_ctx* ctx, const float* verts, int nv, const int32_t* tris, int nt, int nphi,
+                           double theta_eps, double offset);
 /* out: nphi x nt column-major (nphi zenith angles per facet) */
 int ilg_get_horizons(ilg_ctx* ctx, double* out);
 int ilg_set_horizons(ilg_ctx* ctx, int nphi, const double* h);

@@ -342,11 +342,23 @@ int64_t orc_last_visibility_rays() { return s_rays; }
 // Horizon bisection: src/cpp/illum.cpp:274-324 for every facet (:326-363).
 // phi = linspace(0, 2 pi, nphi) with the endpoint (:329). Output nphi x nt,
 // column-major (one column of nphi zenith angles per facet).
+void orc_horizons_mesh(const float* verts, const int32_t* tris, int nt, const float* hverts,
+                       const int32_t* htris, int hnt, int nphi, double theta_eps, double offset, double* out);
+
 void orc_horizons(const float* verts, const int32_t* tris, int nt, int nphi,
                   double theta_eps, double offset, double* out) {
+  orc_horizons_mesh(verts, tris, nt, nullptr, nullptr, 0, nphi, theta_eps, offset, out);
+}
+
+// The same with a separate horizon mesh (src/cpp/illum.cpp:333-349): rays
+// from the facets of (verts, tris), traced against (hverts, htris); hverts
+// NULL traces against the mesh itself.
+void orc_horizons_mesh(const float* verts, const int32_t* tris, int nt, const float* hverts,
+                       const int32_t* htris, int hnt, int nphi, double theta_eps, double offset, double* out) {
   Mesh m = make_mesh(verts, tris, nt, nullptr);
+  Mesh hmesh = hverts ? make_mesh(hverts, htris, hnt, nullptr) : Mesh{};
   BVH bvh;
-  bvh.build(m);
+  bvh.build(hverts ? hmesh : m);
   std::vector<double> cph(nphi), sph(nphi);
   double dphi = nphi > 1 ? TWO_PI / (double)(nphi - 1) : 0.0;
   for (int k = 0; k < nphi; ++k) {

@@ -92,13 +92,21 @@ def coo_to_csr(n, rows, cols, vals):
     return rowptr, c, v
 
 
-def horizons(verts, faces, nphi, theta_eps=1e-3, offset=1e-5):
+def horizons(verts, faces, nphi, theta_eps=1e-3, offset=1e-5, horizon_mesh=None):
+    """nt x nphi zenith angles; horizon_mesh = (verts, faces) of a separate
+    mesh the rays are traced against (src/cpp/illum.cpp:333-349)."""
     verts = np.ascontiguousarray(verts, np.float32)
     faces = np.ascontiguousarray(faces, np.int32)
     nt = faces.shape[0]
     out = np.zeros((nt, nphi), np.float64)   # row f = column f of the nphi x N matrix
-    lib().orc_horizons(_p(verts), _p(faces), C.c_int(nt), C.c_int(nphi), C.c_double(theta_eps),
-                       C.c_double(offset), _p(out))
+    if horizon_mesh is None:
+        lib().orc_horizons(_p(verts), _p(faces), C.c_int(nt), C.c_int(nphi), C.c_double(theta_eps),
+                           C.c_double(offset), _p(out))
+    else:
+        hv = np.ascontiguousarray(horizon_mesh[0], np.float32)
+        hf = np.ascontiguousarray(horizon_mesh[1], np.int32)
+        lib().orc_horizons_mesh(_p(verts), _p(faces), C.c_int(nt), _p(hv), _p(hf), C.c_int(hf.shape[0]),
+                                C.c_int(nphi), C.c_double(theta_eps), C.c_double(offset), _p(out))
     return out
 
 

@@ -64,3 +64,22 @@ def test_cli_tasks(ilg, oracle_mod, tmp_path):
     assert np.abs(therm - st["T"][:, 0]).max() <= 1e-9
     assert np.abs(armaio.load(str(out / "rad.bin")).ravel() - st["rad"]).max() <= 1e-9 * np.abs(st["rad"]).max()
     assert np.abs(armaio.load(str(out / "therm_avg.bin")).ravel() - st["therm_avg"]).max() <= 1e-9
+
+
+def test_cli_horizon_obj_file(ilg, oracle_mod, tmp_path):
+    """horizon_obj_file: the horizons of the shape's facets traced against a
+    second OBJ (src/cpp/illum_cli.cpp:899-901), as the oracle traces them."""
+    from illum_gb300 import cli
+    v, f = meshgen.icosphere_craters(2, seed=3, n_craters=4, dmin_m=150.0, dmax_m=400.0)
+    hv, hf = meshgen.icosphere_craters(3, seed=9, n_craters=30, dmin_m=150.0, dmax_m=500.0)
+    obj, hobj = tmp_path / "shape.obj", tmp_path / "horizon.obj"
+    _write_obj(str(obj), v.astype(np.float64), f)
+    _write_obj(str(hobj), hv.astype(np.float64), hf)
+    out = tmp_path / "out"
+    cli.main(["--task", "horizons", "--path", str(obj), "--horizon_obj_file", str(hobj), "--nphi", "16",
+              "--output_dir", str(out)])
+    H = armaio.load(str(out / "horizons.bin"))
+    V, Fc, _ = meshgen.load_obj(str(obj))
+    HV, HF, _ = meshgen.load_obj(str(hobj))
+    assert np.array_equal(H, oracle_mod.horizons(V, Fc, 16, horizon_mesh=(HV, HF)).T)
+

@@ -419,3 +419,31 @@ def test_errors_are_reported(ilg):
     with pytest.raises(ilg.IlgError):
         ilg.conductionQ_batch(np.array([0.1]), 1.0, None, np.zeros(1), np.zeros((1, 1)), np.ones(1), np.ones(1),
                               1.0, np.zeros(1))   # nz < 2
+
+
+def _grid_faces(n):
+    idx = np.arange(n * n).reshape(n, n)
+    a = idx[:-1, :-1].ravel(); b = idx[1:, :-1].ravel(); c = idx[1:, 1:].ravel(); d = idx[:-1, 1:].ravel()
+    return np.concatenate([np.stack([a, b, c], 1), np.stack([a, c, d], 1)]).astype(np.int32)
+
+
+def test_horizons_with_separate_mesh_bit_exact(ilg, oracle_mod):
+    """A separate horizon mesh (src/cpp/illum.cpp:333-349): the facets of a
+    33 x 33 patch cut from the middle of a 97 x 97 terrain take their
+    horizons from the whole terrain. Bit for bit against the oracle, and
+    different from the patch's own horizons (the surroundings rise above
+    them)."""
+    n, m0, m = 97, 32, 33
+    hv, hf = meshgen.heightmap_terrain(n=n, spacing_m=2.0, seed=4, rms_m=8.0, n_bowls=12, dmin_m=10.0, dmax_m=60.0)
+    sub = (np.arange(m0, m0 + m)[:, None] * n + np.arange(m0, m0 + m)[None, :]).ravel()
+    v = np.ascontiguousarray(hv[sub])
+    f = _grid_faces(m)
+    ctx = ilg.IllumContext(v, f)
+    ctx.set_horizon_mesh(hv, hf)
+    ctx.make_horizons(nphi=24)
+    Ho = oracle_mod.horizons(v, f, 24, horizon_mesh=(hv, hf))
+    assert np.array_equal(ctx.horizons.T, Ho)
+    own = ilg.IllumContext(v, f)
+    own.make_horizons(nphi=24)
+    assert np.array_equal(own.horizons.T, oracle_mod.horizons(v, f, 24))
+    assert (own.horizons > ctx.horizons + 1e-3).mean() > 0.2

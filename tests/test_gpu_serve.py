@@ -24,16 +24,18 @@ def test_serving_results_equal_alone(ilg, workers, min_rebuild_s):
 
 
 def test_admission_respects_budget(ilg):
+    """Jobs reserve device memory before their set-up: a level's first job
+    3x the a priori estimate (built alone), the later ones 1.25x the largest
+    footprint measured at that level; each reservation is replaced by the
+    measured footprint (context + batch copy) once the job is built. The
+    reserved total never exceeds the budget."""
     from illum_gb300 import serve
-    reqs = serve.request_stream(4, rate_hz=1000.0, levels=(3,), rotations=(1, 1), steps_per_rot=(30, 31))
-    one = serve.footprint_bytes(3, 80, 32, ilg.PREC_MIXED)
-    srv = serve.Server(budget_bytes=int(1.5 * one), chunk_steps=10, setup_workers=4)
-    seen = []
-    orig = srv.build_job
-
-    def spy(r):
-        seen.append(srv.used)
-        return orig(r)
-    srv.build_job = spy
+    reqs = serve.request_stream(6, rate_hz=1000.0, levels=(3,), rotations=(1, 1), steps_per_rot=(30, 31))
+    first = 3 * serve.footprint_bytes(3, 80, 32, ilg.PREC_MIXED)
+    srv = serve.Server(budget_bytes=int(1.5 * first), chunk_steps=10, setup_workers=4)
     done = srv.run(reqs)
-    assert len(done) == 4 and max(seen) <= srv.budget
+    st = srv.stats()
+    assert len(done) == 6
+    assert 3 in srv.per_facet                      # calibrated from a measured footprint
+    assert st["max_reserved_bytes"] <= srv.budget
+    assert st["measured_over_reserved"]["max"] <= 1.0
