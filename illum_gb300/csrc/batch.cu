@@ -38,6 +38,7 @@ __global__ void k_iota(uint32_t* a, int64_t n, int off) {
 }  // namespace
 
 struct Batch {
+  OwnedStream owned_stream;   // destroyed after every buffer (they are freed on it)
   std::vector<ilg_ctx*> members;
   std::vector<ilg_run_opts> opts;
   std::vector<MeshDesc> mh;
@@ -79,7 +80,6 @@ struct Batch {
     if (graph) cudaGraphExecDestroy(graph);
     for (auto& e : ev)
       if (e) cudaEventDestroy(e);
-    if (stream) cudaStreamDestroy(stream);
   }
 };
 
@@ -105,7 +105,10 @@ static int build(Batch& b) {
       set_error("batch member %d is in the fixed-sweep Gauss-Seidel mode, which runs on single contexts", i);
       return ILG_ERR_ARG;
     }
-    ILG_TRY(check_run(c, &o, false));
+    {
+      AllocOn onm(c.stream);   // the member's own buffers live (and are freed) on its stream
+      ILG_TRY(check_run(c, &o, false));
+    }
     ILG_CUDA(cudaStreamSynchronize(c.stream));
     if (ndisk < 0) ndisk = c.ndisk;
     if (c.ndisk != ndisk) { set_error("batch members must share the sun-disk samples"); return ILG_ERR_ARG; }
@@ -362,11 +365,13 @@ int ilg_batch_create(ilg_ctx** members, int n, const ilg_run_opts* opts, ilg_bat
   b.members.assign(members, members + n);
   b.opts.assign(opts, opts + n);
   b.precision = opts[0].precision;
-  if (cudaStreamCreateWithFlags(&b.stream, cudaStreamNonBlocking) != cudaSuccess) {
+  if (cudaStreamCreateWithFlags(&b.owned_stream.s, cudaStreamNonBlocking) != cudaSuccess) {
     delete h;
     set_error("cudaStreamCreate failed");
     return ILG_ERR_CUDA;
   }
+  b.stream = b.owned_stream.s;
+  AllocOn on(b.stream);
   for (auto& e : b.ev)
     if (cudaEventCreate(&e) != cudaSuccess) { delete h; set_error("cudaEventCreate failed"); return ILG_ERR_CUDA; }
   if (b.pipe.init() != ILG_OK) { delete h; return ILG_ERR_CUDA; }
@@ -399,6 +404,7 @@ int ilg_batch_run(ilg_batch* batch, int nsteps, int use_graph) {
 int ilg_batch_bench(ilg_batch* batch, int nsteps, double flush_mb, double* step_ms) {
   if (!batch || nsteps < 0 || !step_ms) { set_error("invalid arguments"); return ILG_ERR_ARG; }
   Batch& b = batch->b;
+  AllocOn on_(b.stream);
   size_t nflush = flush_mb > 0 ? (size_t)(flush_mb * 1048576.0 / 16.0) : 0;
   if (nflush) ILG_TRY(b.flush.reserve(nflush));
   cudaGraphExec_t g = nullptr;

@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -34,7 +35,24 @@ Context::~Context() {
   if (pinned_tsurf) cudaFreeHost(pinned_tsurf);
   for (cudaEvent_t e : slot_ev)
     if (e) cudaEventDestroy(e);
-  if (stream) cudaStreamDestroy(stream);
+  // the stream itself goes last (owned_stream), after the buffers' frees
+}
+
+thread_local cudaStream_t t_alloc_stream = nullptr;
+
+int alloc_pool_setup() {
+  static std::mutex mu;
+  static std::vector<int> done;
+  int dev = 0;
+  ILG_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lock(mu);
+  if (std::find(done.begin(), done.end(), dev) != done.end()) return ILG_OK;
+  cudaMemPool_t pool;
+  ILG_CUDA(cudaDeviceGetDefaultMemPool(&pool, dev));
+  uint64_t keep = UINT64_MAX;   // keep freed memory in the process's pool
+  ILG_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+  done.push_back(dev);
+  return ILG_OK;
 }
 
 int read_device_errors(Context& c) {
@@ -299,7 +317,6 @@ int check_run(Context& c, const ilg_run_opts* o, bool host_driven) {
   ILG_TRY(conduction_prepare(c, o->dt, o->precision));
   ILG_TRY(conduction_state_convert(c, o->precision));
   ILG_TRY(ensure_step_buffers(c, o->precision));
-  ILG_TRY(ensure_pinned(c));
   return ILG_OK;
 }
 
@@ -469,15 +486,18 @@ int ilg_version(void) { return 10000; }
 int ilg_ctx_create(const float* verts, int nv, const int32_t* tris, int nt, const float* normals, ilg_ctx** out) {
   if (!out || !verts || !tris || nv < 3 || nt < 1) { set_error("invalid mesh arguments"); return ILG_ERR_ARG; }
   *out = nullptr;
+  ILG_TRY(alloc_pool_setup());
   ilg_ctx* h = new ilg_ctx();
   Context& c = h->c;
   c.nt = nt;
   int rc = ILG_OK;
-  if (cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) != cudaSuccess) {
+  if (cudaStreamCreateWithFlags(&c.owned_stream.s, cudaStreamNonBlocking) != cudaSuccess) {
     set_error("cudaStreamCreate failed");
     delete h;
     return ILG_ERR_CUDA;
   }
+  c.stream = c.owned_stream.s;
+  AllocOn on(c.stream);
   for (auto& e : c.ev)
     if (cudaEventCreate(&e) != cudaSuccess) { set_error("cudaEventCreate failed"); delete h; return ILG_ERR_CUDA; }
   if ((rc = c.derr.alloc(DERR_COUNT)) || (rc = c.counters.alloc(8)) || (rc = c.work.alloc(nt)) ||
@@ -578,6 +598,7 @@ int ilg_compute_F_cutoff(ilg_ctx* ctx, const double* albedo, double albedo_scala
 int ilg_get_F(ilg_ctx* ctx, int64_t* rowptr, int32_t* col, double* val) {
   if (!ctx || !ctx->c.have_F) { set_error("no form factors"); return ILG_ERR_ARG; }
   Context& c = ctx->c;
+  AllocOn on_(c.stream);
   if (rowptr) ILG_CUDA(cudaMemcpyAsync(rowptr, c.rowptr.p, ((size_t)c.nt + 1) * 8, cudaMemcpyDeviceToHost, c.stream));
   if (c.nnz > 0) {
     if (col) ILG_CUDA(cudaMemcpyAsync(col, c.col.p, (size_t)c.nnz * 4, cudaMemcpyDeviceToHost, c.stream));
@@ -590,6 +611,7 @@ int ilg_get_F(ilg_ctx* ctx, int64_t* rowptr, int32_t* col, double* val) {
 int ilg_set_F(ilg_ctx* ctx, int64_t nnz, const int64_t* rowptr, const int32_t* col, const double* val) {
   if (!ctx || nnz < 0 || !rowptr || (nnz > 0 && (!col || !val))) { set_error("invalid F arguments"); return ILG_ERR_ARG; }
   Context& c = ctx->c;
+  AllocOn on_(c.stream);
   if (rowptr[0] != 0 || rowptr[c.nt] != nnz) { set_error("rowptr does not span nnz"); return ILG_ERR_ARG; }
   for (int i = 0; i < c.nt; ++i)
     if (rowptr[i + 1] < rowptr[i]) { set_error("rowptr decreases at row %d", i); return ILG_ERR_ARG; }
@@ -612,6 +634,7 @@ int ilg_set_F(ilg_ctx* ctx, int64_t nnz, const int64_t* rowptr, const int32_t* c
 
 int ilg_make_horizons(ilg_ctx* ctx, int nphi, double theta_eps, double offset) {
   if (!ctx) { set_error("ctx is NULL"); return ILG_ERR_ARG; }
+  AllocOn on_(ctx->c.stream);
   invalidate_graph(ctx->c);
   return horizons_build(ctx->c, nphi, theta_eps, offset);
 }
@@ -621,6 +644,7 @@ int ilg_make_horizons_mesh(ilg_ctx* ctx, const float* verts, int nv, const int32
   if (!ctx) { set_error("ctx is NULL"); return ILG_ERR_ARG; }
   ilg_ctx* hm = nullptr;
   ILG_TRY(ilg_ctx_create(verts, nv, tris, nt, nullptr, &hm));   // the horizon mesh's LBVH (synchronised)
+  AllocOn on_(ctx->c.stream);
   invalidate_graph(ctx->c);
   const int rc = horizons_build(ctx->c, nphi, theta_eps, offset, &hm->c);
   ilg_ctx_destroy(hm);
@@ -630,6 +654,7 @@ int ilg_make_horizons_mesh(ilg_ctx* ctx, const float* verts, int nv, const int32
 int ilg_get_horizons(ilg_ctx* ctx, double* out) {
   if (!ctx || !ctx->c.H.p || !out) { set_error("no horizons"); return ILG_ERR_ARG; }
   Context& c = ctx->c;
+  AllocOn on_(c.stream);
   ILG_CUDA(cudaMemcpyAsync(out, c.H.p, (size_t)c.nt * c.nphi * 8, cudaMemcpyDeviceToHost, c.stream));
   ILG_CUDA(cudaStreamSynchronize(c.stream));
   return ILG_OK;
@@ -638,6 +663,7 @@ int ilg_get_horizons(ilg_ctx* ctx, double* out) {
 int ilg_set_horizons(ilg_ctx* ctx, int nphi, const double* h) {
   if (!ctx || nphi < 2 || !h) { set_error("invalid horizon arguments"); return ILG_ERR_ARG; }
   Context& c = ctx->c;
+  AllocOn on_(c.stream);
   invalidate_graph(c);
   size_t n = (size_t)c.nt * nphi;
   for (size_t k = 0; k < n; ++k)
@@ -655,6 +681,7 @@ int ilg_set_insolation(ilg_ctx* ctx, int norm_mode, int interp, double solar_con
     return ILG_ERR_ARG;
   }
   Context& c = ctx->c;
+  AllocOn on_(c.stream);
   invalidate_graph(c);
   c.norm_mode = norm_mode;
   c.interp = interp;
@@ -670,6 +697,7 @@ void ilg_fib_spiral(double* xy, int n) {
 int ilg_direct_radiosity(ilg_ctx* ctx, const double* sun, const double* disk_xy, int ndisk, double* out) {
   if (!ctx || !sun || !out) { set_error("invalid direct arguments"); return ILG_ERR_ARG; }
   Context& c = ctx->c;
+  AllocOn on_(c.stream);
   if (!c.H.p || c.nphi < 2) { set_error("horizons are not set"); return ILG_ERR_ARG; }
   ILG_TRY(set_disk(c, disk_xy, ndisk));
   ILG_TRY(ensure_step_buffers(c, ILG_PREC_FP64));
@@ -686,6 +714,7 @@ int ilg_direct_radiosity(ilg_ctx* ctx, const double* sun, const double* disk_xy,
 int ilg_radiosity_solve(ilg_ctx* ctx, const double* E, double tol, int max_sweeps, double* x, double* res, int* sweeps) {
   if (!ctx || !E || !x || max_sweeps < 1 || !(tol >= 0.0)) { set_error("invalid radiosity arguments"); return ILG_ERR_ARG; }
   Context& c = ctx->c;
+  AllocOn on_(c.stream);
   if (!c.have_F) { set_error("no form factors"); return ILG_ERR_ARG; }
   if (c.ntiles == 0) {
     std::memcpy(x, E, (size_t)c.nt * 8);
@@ -725,6 +754,7 @@ int ilg_set_radiosity_mode(ilg_ctx* ctx, int mode, int gs_steps) {
     return ILG_ERR_ARG;
   }
   Context& c = ctx->c;
+  AllocOn on_(c.stream);
   c.rad_mode = mode;
   c.gs_steps = gs_steps;
   invalidate_graph(c);
@@ -734,6 +764,7 @@ int ilg_set_radiosity_mode(ilg_ctx* ctx, int mode, int gs_steps) {
 int ilg_radiosity_solve_gs(ilg_ctx* ctx, const double* E, int gs_steps, double* x, double* res) {
   if (!ctx || !E || !x || gs_steps < 0) { set_error("invalid radiosity arguments"); return ILG_ERR_ARG; }
   Context& c = ctx->c;
+  AllocOn on_(c.stream);
   if (!c.have_F) { set_error("no form factors"); return ILG_ERR_ARG; }
   ILG_TRY(gs_prepare(c));
   ILG_TRY(ensure_step_buffers(c, ILG_PREC_FP64));
@@ -759,6 +790,7 @@ int ilg_radiosity_solve_gs(ilg_ctx* ctx, const double* E, int gs_steps, double* 
 int ilg_debug_barrier_timeout(ilg_ctx* ctx, int blocks, long long polls, int unreachable) {
   if (!ctx) { set_error("ctx is NULL"); return ILG_ERR_ARG; }
   Context& c = ctx->c;
+  AllocOn on_(c.stream);
   ILG_TRY(c.barrier.reserve(radiosity_barrier_words(1)));
   ILG_TRY(c.derr.reserve(DERR_COUNT));
   ILG_CUDA(cudaMemsetAsync(c.derr.p, 0, DERR_COUNT * sizeof(int), c.stream));
@@ -778,6 +810,7 @@ int ilg_thermal_init(ilg_ctx* ctx, int nz, const double* z, const double* ti, co
   if (bc_mode != ILG_BC_LINEARISED && bc_mode != ILG_BC_NEWTON) { set_error("bad bc_mode"); return ILG_ERR_ARG; }
   if (precision != ILG_PREC_FP64 && precision != ILG_PREC_MIXED) { set_error("bad precision"); return ILG_ERR_ARG; }
   Context& c = ctx->c;
+  AllocOn on_(c.stream);
   invalidate_graph(c);
   int nt = c.nt;
   c.nz = nz;
@@ -824,6 +857,7 @@ int ilg_thermal_init(ilg_ctx* ctx, int nz, const double* z, const double* ti, co
 int ilg_thermal_step(ilg_ctx* ctx, double dt, const double* Q) {
   if (!ctx || !Q || !(dt > 0.0)) { set_error("invalid thermal step arguments"); return ILG_ERR_ARG; }
   Context& c = ctx->c;
+  AllocOn on_(c.stream);
   if (!c.have_thermal) { set_error("ilg_thermal_init has not been called"); return ILG_ERR_ARG; }
   ILG_TRY(conduction_prepare(c, dt, c.state_prec));
   ILG_TRY(ensure_step_buffers(c, c.state_prec));
@@ -838,6 +872,7 @@ int ilg_thermal_step(ilg_ctx* ctx, double dt, const double* Q) {
 int ilg_thermal_get(ilg_ctx* ctx, double* T, double* Fsurf, double* Qprev) {
   if (!ctx) { set_error("ctx is NULL"); return ILG_ERR_ARG; }
   Context& c = ctx->c;
+  AllocOn on_(c.stream);
   if (!c.have_thermal) { set_error("ilg_thermal_init has not been called"); return ILG_ERR_ARG; }
   int nt = c.nt, nz = c.nz;
   if (T) {
@@ -870,6 +905,7 @@ int ilg_thermal_get(ilg_ctx* ctx, double* T, double* Fsurf, double* Qprev) {
 int ilg_set_suns(ilg_ctx* ctx, int nsun, const double* suns, const double* disk_xy, int ndisk) {
   if (!ctx || nsun < 1 || !suns) { set_error("invalid sun arguments"); return ILG_ERR_ARG; }
   Context& c = ctx->c;
+  AllocOn on_(c.stream);
   invalidate_graph(c);
   ILG_TRY(set_disk(c, disk_xy, ndisk));
   c.suns_h.assign(suns, suns + 3 * (size_t)nsun);
@@ -879,8 +915,10 @@ int ilg_set_suns(ilg_ctx* ctx, int nsun, const double* suns, const double* disk_
 int ilg_run_steps(ilg_ctx* ctx, const ilg_run_opts* opts, int first_sun, int nsteps, double* tsurf_out) {
   if (!ctx) { set_error("ctx is NULL"); return ILG_ERR_ARG; }
   Context& c = ctx->c;
+  AllocOn on_(c.stream);
   ILG_TRY(check_run(c, opts, false));
   if (nsteps < 0 || first_sun < 0 || first_sun + nsteps > c.nsun) { set_error("sun range out of bounds"); return ILG_ERR_ARG; }
+  if (tsurf_out) ILG_TRY(ensure_pinned(c));   // page-locked staging, only where host copies are made
   const ilg_run_opts& o = *opts;
   ILG_TRY(upload_desc(c, solo_desc(c, &o, first_sun)));
   bool timing = c.timing;
@@ -911,10 +949,12 @@ int ilg_run_steps(ilg_ctx* ctx, const ilg_run_opts* opts, int first_sun, int nst
 int ilg_run_steps_host(ilg_ctx* ctx, const ilg_run_opts* opts, int nsteps, const double* suns, double* tsurf_out) {
   if (!ctx || (nsteps > 0 && !suns)) { set_error("invalid arguments"); return ILG_ERR_ARG; }
   Context& c = ctx->c;
+  AllocOn on_(c.stream);
   if (!opts) { set_error("opts is NULL"); return ILG_ERR_ARG; }
   if (c.ndisk < 2) { set_error("sun disk samples are not set (ilg_set_suns)"); return ILG_ERR_ARG; }
   if (!c.sun_aux.p) { ILG_TRY(c.sun_aux.alloc(2)); c.nsun = 0; }
   ILG_TRY(check_run(c, opts, true));
+  ILG_TRY(ensure_pinned(c));
   const ilg_run_opts& o = *opts;
   MeshDesc M = solo_desc(c, &o, 0);
   M.host_sun = 1;
@@ -984,6 +1024,7 @@ int ilg_bench_steps(ilg_ctx* ctx, const ilg_run_opts* opts, int first_sun, int n
                     double* step_ms, double* phase_ms) {
   if (!ctx || !step_ms) { set_error("invalid arguments"); return ILG_ERR_ARG; }
   Context& c = ctx->c;
+  AllocOn on_(c.stream);
   ILG_TRY(check_run(c, opts, false));
   if (nsteps < 0 || first_sun < 0 || first_sun + nsteps > c.nsun) { set_error("sun range out of bounds"); return ILG_ERR_ARG; }
   const ilg_run_opts& o = *opts;
@@ -1030,6 +1071,7 @@ int ilg_bench_steps(ilg_ctx* ctx, const ilg_run_opts* opts, int first_sun, int n
 int ilg_get_outputs(ilg_ctx* ctx, double* rad, double* rad_avg, double* therm_avg, double* therm_max) {
   if (!ctx) { set_error("ctx is NULL"); return ILG_ERR_ARG; }
   Context& c = ctx->c;
+  AllocOn on_(c.stream);
   if (!c.have_thermal) { set_error("ilg_thermal_init has not been called"); return ILG_ERR_ARG; }
   size_t b = (size_t)c.nt * 8;
   if (rad) ILG_CUDA(cudaMemcpyAsync(rad, c.rad.p, b, cudaMemcpyDeviceToHost, c.stream));
@@ -1043,6 +1085,7 @@ int ilg_get_outputs(ilg_ctx* ctx, double* rad, double* rad_avg, double* therm_av
 int ilg_record_thermal(ilg_ctx* ctx, int capacity) {
   if (!ctx || capacity < 0) { set_error("invalid arguments"); return ILG_ERR_ARG; }
   Context& c = ctx->c;
+  AllocOn on_(c.stream);
   invalidate_graph(c);
   if (capacity == 0) { c.rec_cap = 0; return ILG_OK; }
   ILG_TRY(c.rec.alloc((size_t)capacity * REC_W));
@@ -1056,6 +1099,7 @@ int ilg_record_thermal(ilg_ctx* ctx, int capacity) {
 int ilg_get_thermal_records(ilg_ctx* ctx, double* out, int* count) {
   if (!ctx || !count) { set_error("invalid arguments"); return ILG_ERR_ARG; }
   Context& c = ctx->c;
+  AllocOn on_(c.stream);
   int n = std::max(0, std::min(c.rec_cap, c.frame_no - c.rec_frame0));
   *count = n;
   if (out && n > 0) {
@@ -1069,6 +1113,7 @@ int ilg_get_thermal_records(ilg_ctx* ctx, double* out, int* count) {
 int ilg_autotune(ilg_ctx* ctx, const ilg_run_opts* opts, int first_sun, ilg_tune* chosen) {
   if (!ctx) { set_error("ctx is NULL"); return ILG_ERR_ARG; }
   Context& c = ctx->c;
+  AllocOn on_(c.stream);
   ILG_TRY(check_run(c, opts, false));
   if (first_sun < 0 || first_sun >= c.nsun) { set_error("first_sun out of range"); return ILG_ERR_ARG; }
   const ilg_run_opts& o = *opts;
@@ -1140,6 +1185,7 @@ int ilg_set_tune(ilg_ctx* ctx, const ilg_tune* t) {
     return ILG_ERR_ARG;
   }
   Context& c = ctx->c;
+  AllocOn on_(c.stream);
   c.tune.classify_threads = t->classify_threads;
   c.tune.exact_facets = t->exact_facets;
   c.tune.conduct_threads = t->conduct_threads;
@@ -1160,6 +1206,7 @@ int ilg_get_tune(const ilg_ctx* ctx, ilg_tune* t) {
 int ilg_set_timing(ilg_ctx* ctx, int enable) {
   if (!ctx) { set_error("ctx is NULL"); return ILG_ERR_ARG; }
   Context& c = ctx->c;
+  AllocOn on_(c.stream);
   c.timing = enable != 0;
   c.ms_direct = c.ms_rad = c.ms_cond = 0.f;
   c.stats_ambiguous = c.stats_sweeps = 0;
@@ -1170,6 +1217,7 @@ int ilg_get_stats(ilg_ctx* ctx, double* ms_direct, double* ms_radiosity, double*
                   int64_t* sweeps) {
   if (!ctx) { set_error("ctx is NULL"); return ILG_ERR_ARG; }
   Context& c = ctx->c;
+  AllocOn on_(c.stream);
   if (ms_direct) *ms_direct = c.ms_direct;
   if (ms_radiosity) *ms_radiosity = c.ms_rad;
   if (ms_conduction) *ms_conduction = c.ms_cond;

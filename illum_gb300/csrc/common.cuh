@@ -37,36 +37,76 @@ struct Status {
     if (rc_ != ILG_OK) return rc_; \
   } while (0)
 
-// Owning device buffer (cudaMalloc / cudaFree). Not copyable.
+// Stream that orders the calling thread's device allocations: set, for the
+// duration of an API call, to the stream of the context (or batch) it works
+// on. With one, dbuf allocates from the device's stream-ordered pool and
+// frees on that stream, so neither waits for work that other streams have
+// queued (cudaFree synchronises the whole device, which stalls a context's
+// set-up behind every other context's steps); without one it uses
+// cudaMalloc / cudaFree.
+extern thread_local cudaStream_t t_alloc_stream;
+struct AllocOn {
+  cudaStream_t prev;
+  explicit AllocOn(cudaStream_t s) : prev(t_alloc_stream) { t_alloc_stream = s; }
+  ~AllocOn() { t_alloc_stream = prev; }
+  AllocOn(const AllocOn&) = delete;
+  AllocOn& operator=(const AllocOn&) = delete;
+};
+// Keeps freed pool memory cached in the process (set once per device).
+int alloc_pool_setup();
+
+// A stream destroyed last: the first member of an object whose buffers
+// are freed on it, so their stream-ordered frees are queued before the
+// stream goes (its pending work still completes after cudaStreamDestroy).
+struct OwnedStream {
+  cudaStream_t s = nullptr;
+  OwnedStream() = default;
+  OwnedStream(const OwnedStream&) = delete;
+  OwnedStream& operator=(const OwnedStream&) = delete;
+  ~OwnedStream() { if (s) cudaStreamDestroy(s); }
+};
+
+// Owning device buffer. Not copyable.
 template <class T>
 struct dbuf {
   T* p = nullptr;
   size_t n = 0;
+  cudaStream_t s = nullptr;   // the stream it was allocated on (and is freed on), or none
   dbuf() = default;
   dbuf(const dbuf&) = delete;
   dbuf& operator=(const dbuf&) = delete;
-  dbuf(dbuf&& o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+  dbuf(dbuf&& o) noexcept : p(o.p), n(o.n), s(o.s) { o.p = nullptr; o.n = 0; o.s = nullptr; }
   dbuf& operator=(dbuf&& o) noexcept {
-    if (this != &o) { release(); p = o.p; n = o.n; o.p = nullptr; o.n = 0; }
+    if (this != &o) { release(); p = o.p; n = o.n; s = o.s; o.p = nullptr; o.n = 0; o.s = nullptr; }
     return *this;
   }
   ~dbuf() { release(); }
   void release() {
-    if (p) cudaFree(p);
+    if (p) {
+      if (s) cudaFreeAsync(p, s);
+      else cudaFree(p);
+    }
     p = nullptr;
     n = 0;
+    s = nullptr;
   }
   int alloc(size_t count) {
     if (count == n && p) return ILG_OK;
     release();
     if (count == 0) return ILG_OK;
-    cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+    const cudaStream_t st = t_alloc_stream;
+    cudaError_t e = st ? cudaMallocAsync(&p, count * sizeof(T), st) : cudaMalloc(&p, count * sizeof(T));
+    // the memory is used at once from the host and other streams: wait for
+    // the allocation in its own stream (that stream only)
+    if (e == cudaSuccess && st) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) {
+      if (p && st) cudaFreeAsync(p, st);
       p = nullptr;
-      set_error("cudaMalloc of %zu bytes failed: %s", count * sizeof(T), cudaGetErrorString(e));
+      set_error("device allocation of %zu bytes failed: %s", count * sizeof(T), cudaGetErrorString(e));
       return ILG_ERR_NOMEM;
     }
     n = count;
+    s = st;
     return ILG_OK;
   }
   // grow-only reallocation (contents not preserved)

@@ -168,9 +168,10 @@ struct StepPipe {
 };
 
 struct Context {
+  OwnedStream owned_stream;   // destroyed after every buffer (they are freed on it)
   TuneCfg tune;
   int nt = 0;
-  cudaStream_t stream = nullptr;
+  cudaStream_t stream = nullptr;   // = owned_stream.s
   StepPipe pipe;
   float scene_mag = 1.0f;   // max |coordinate|
   float r_max = 0.0f;       // max facet bounding radius

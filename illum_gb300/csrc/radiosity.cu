@@ -144,9 +144,10 @@ __device__ __forceinline__ uint64_t l2_keep_policy(int stream) {
   return pol;
 }
 // L2 prefetch of the entry groups RAD_PF groups ahead of the one being
-// summed: the register pipeline keeps two groups in flight per thread,
-// which at one 1024-thread block per SM is too few bytes in flight to
-// cover DRAM latency; prefetched lines arrive in L2 meanwhile.
+// summed, for a matrix streamed from HBM: the register pipeline keeps two
+// groups in flight per thread, which at one 1024-thread block per SM is too
+// few bytes in flight to cover DRAM latency; prefetched lines arrive in L2
+// meanwhile.
 constexpr int RAD_PF = 6;
 __device__ __forceinline__ void pf_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 __device__ __forceinline__ uint2 ld_mat(const uint2* p, uint64_t pol) {
@@ -330,10 +331,12 @@ __device__ __forceinline__ void tile_rows(const StepView& v, const RowTile& T, i
       any = true;
     }
   };
-  for (int q = 2; q < RAD_PF && q < ng; ++q) {
-    pf_l2(cfp + (size_t)q * RAD_THREADS);
-    pf_vals(vals, vo + (size_t)q * 4 * RAD_THREADS);
-  }
+  const bool pf = v.l2_stream != 0;   // an L2-resident matrix gains nothing from prefetching
+  if (pf)
+    for (int q = 2; q < RAD_PF && q < ng; ++q) {
+      pf_l2(cfp + (size_t)q * RAD_THREADS);
+      pf_vals(vals, vo + (size_t)q * 4 * RAD_THREADS);
+    }
   uint2 c0 = ld_mat(cfp, pol), c1 = c0;
   W w0[4], w1[4];
   ld_vals4(vals, vo, w0, pol);
@@ -347,7 +350,7 @@ __device__ __forceinline__ void tile_rows(const StepView& v, const RowTile& T, i
   for (int g = 0; g < ng; ++g) {
     uint2 c2 = c1;
     W w2[4];
-    if (g + RAD_PF < ng) {
+    if (pf && g + RAD_PF < ng) {
       pf_l2(cfp + (size_t)(g + RAD_PF) * RAD_THREADS);
       pf_vals(vals, vo + (size_t)(g + RAD_PF) * 4 * RAD_THREADS);
     }
