@@ -73,6 +73,8 @@ _SIGS = {
                                 C.POINTER(C.c_int64)]),
     "ilg_compute_F_cutoff": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_double,
                                        C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    "ilg_visibility_sample": (C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_void_p, C.c_int, C.c_void_p, C.c_int,
+                                        C.c_void_p, C.c_void_p, C.POINTER(C.c_int64)]),
     "ilg_get_F": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "ilg_record_thermal": (C.c_int, [C.c_void_p, C.c_int]),
     "ilg_render": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_int, C.c_int, C.c_void_p]),
@@ -244,6 +246,19 @@ class IllumContext:
         if not fetch:
             return None
         return self.get_F()
+
+    def visibility_sample(self, sources, cutoff=None, radii=(), offset=1e-5):
+        """Nonzero form-factor entries of the listed source columns (and of
+        the sample within each radius) without building F; cutoff None: none."""
+        src = np.ascontiguousarray(sources, np.int32)
+        rad = np.ascontiguousarray(radii, np.float64)
+        per = np.zeros(src.shape[0], np.int64)
+        within = np.zeros(max(1, rad.shape[0]), np.int64)
+        rays = C.c_int64()
+        _check(lib().ilg_visibility_sample(self._h, 0.0 if cutoff is None else float(cutoff), offset, _p(src),
+                                           src.shape[0], _p(rad) if rad.shape[0] else None, rad.shape[0], _p(per),
+                                           _p(within), C.byref(rays)))
+        return {"per_source": per, "within_radius": within[:rad.shape[0]], "rays": rays.value}
 
     def get_F(self):
         rowptr = np.zeros(self.num_faces + 1, np.int64)
@@ -449,6 +464,19 @@ class ThermalModel:
         out = np.zeros((self.ctx.num_faces, self.nz + 1), np.float64)
         _check(lib().ilg_thermal_get(self.ctx._h, _p(out), None, None))
         return out.T
+
+    def visibility_sample(self, sources, cutoff=None, radii=(), offset=1e-5):
+        """Nonzero form-factor entries of the listed source columns (and of
+        the sample within each radius) without building F; cutoff None: none."""
+        src = np.ascontiguousarray(sources, np.int32)
+        rad = np.ascontiguousarray(radii, np.float64)
+        per = np.zeros(src.shape[0], np.int64)
+        within = np.zeros(max(1, rad.shape[0]), np.int64)
+        rays = C.c_int64()
+        _check(lib().ilg_visibility_sample(self._h, 0.0 if cutoff is None else float(cutoff), offset, _p(src),
+                                           src.shape[0], _p(rad) if rad.shape[0] else None, rad.shape[0], _p(per),
+                                           _p(within), C.byref(rays)))
+        return {"per_source": per, "within_radius": within[:rad.shape[0]], "rays": rays.value}
 
     def get_F(self):
         F = np.zeros(self.ctx.num_faces)

@@ -439,23 +439,25 @@ __global__ void k_frontier(const float4* __restrict__ nodes, int root, int* fron
   *nfront = n;
 }
 
-// Work item (source j, subtree sub), stored at t = (j - j0) FF_SPLIT + sub
-// so that a source's candidates are contiguous. Threads run subtree-major:
-// a warp holds consecutive sources on the same subtree (similar queries).
-// Counting writes count[t]; FILL writes the item's candidates from
-// offs[t] - base0 on.
+// Work item (source number q in [j0, j1), subtree sub), stored at
+// t = (q - j0) FF_SPLIT + sub so that a source's candidates are contiguous;
+// the source facet is q, or src[q] for a list of sources. Threads run
+// subtree-major: a warp holds consecutive sources on the same subtree
+// (similar queries). Counting writes count[t]; FILL writes the item's
+// candidates from offs[t] - base0 on.
 template <bool FILL>
 __global__ void k_candidates(const float4* __restrict__ nodes, const float4* __restrict__ tri_s,
                              const int* __restrict__ front, const int* __restrict__ nfront,
                              const float4* __restrict__ cen, const float4* __restrict__ nrm, int j0, int j1,
-                             float r_max, float slack, float cut2, float box_cut2, uint32_t* count,
-                             const unsigned long long* __restrict__ offs, unsigned long long base0, int32_t* cand_i,
-                             int32_t* cand_j, int* derr) {
+                             const int* __restrict__ src, float r_max, float slack, float cut2, float box_cut2,
+                             uint32_t* count, const unsigned long long* __restrict__ offs, unsigned long long base0,
+                             int32_t* cand_i, int32_t* cand_j, int* derr) {
   const int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int nsrc = j1 - j0;
-  const int sub = (int)(u / nsrc), j = j0 + (int)(u % nsrc);
+  const int sub = (int)(u / nsrc), q = j0 + (int)(u % nsrc);
   if (sub >= FF_SPLIT) return;
-  const int64_t t = (int64_t)(j - j0) * FF_SPLIT + sub;
+  const int j = src ? src[q] : q;
+  const int64_t t = (int64_t)(q - j0) * FF_SPLIT + sub;
   uint32_t cnt = 0;
   if (sub >= *nfront) {
     if (!FILL) count[t] = 0;
@@ -568,6 +570,30 @@ __global__ void k_ff_values(const unsigned long long* __restrict__ keys, int64_t
   }
   keep[k] = kp;
   fval[k] = F;
+}
+
+// Sampled visibility: every distinct (hit i, source j) key with a nonzero
+// form factor counts for its source's sample slot, and for every radius its
+// centroid distance does not exceed.
+__global__ void k_sample_count(const unsigned long long* __restrict__ keys, int64_t n, int bits,
+                               const float4* __restrict__ cen, const float4* __restrict__ nrm,
+                               const double* __restrict__ area, const int* __restrict__ slot,
+                               const double* __restrict__ radii, int nradii, unsigned long long* per_src,
+                               unsigned long long* within) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const unsigned long long key = keys[k];
+  if (k > 0 && keys[k - 1] == key) return;
+  const unsigned long long mask = (1ull << bits) - 1ull;
+  const int i = (int)(key >> bits), j = (int)(key & mask);
+  const double F = form_factor(f3of(cen[i]), f3of(nrm[i]), f3of(cen[j]), f3of(nrm[j]), area[j]);
+  if (!(F > 0.0)) return;
+  atomicAdd(&per_src[slot[j]], 1ull);
+  const float4 a = cen[i], b = cen[j];
+  const double dx = (double)a.x - b.x, dy = (double)a.y - b.y, dz = (double)a.z - b.z;
+  const double d = sqrt(dx * dx + dy * dy + dz * dz);
+  for (int q = 0; q < nradii; ++q)
+    if (d <= radii[q]) atomicAdd(&within[q], 1ull);
 }
 
 __global__ void k_ff_compact(const unsigned long long* __restrict__ keys, int64_t n, int bits,
@@ -881,8 +907,8 @@ int form_factors_build(Context& c, const double* albedo_h, double albedo_scalar,
   k_frontier<<<1, 1, 0, s>>>(c.nodes.p, c.root, front.p, front.p + FF_SPLIT);
   ILG_CUDA(cudaGetLastError());
   k_candidates<false><<<div_up(nitems, 128), 128, 0, s>>>(c.nodes.p, c.tri_s.p, front.p, front.p + FF_SPLIT, c.cen.p,
-                                                          c.nrm.p, 0, nt, c.r_max, slack, cut2, box_cut2, cnt.p,
-                                                          nullptr, 0ull, nullptr, nullptr, c.derr.p);
+                                                          c.nrm.p, 0, nt, nullptr, c.r_max, slack, cut2, box_cut2,
+                                                          cnt.p, nullptr, 0ull, nullptr, nullptr, c.derr.p);
   ILG_CUDA(cudaGetLastError());
   ILG_TRY(scan_exclusive_u32_to_u64(cnt.p, offs.p, nitems, c.scan, s));
   // per-source offsets: every FF_SPLIT-th item offset, and the total
@@ -934,8 +960,8 @@ int form_factors_build(Context& c, const double* albedo_h, double albedo_scalar,
       ucap = want;
     }
     k_candidates<true><<<div_up((int64_t)(b - a) * FF_SPLIT, 128), 128, 0, s>>>(
-        c.nodes.p, c.tri_s.p, front.p, front.p + FF_SPLIT, c.cen.p, c.nrm.p, a, b, c.r_max, slack, cut2, box_cut2,
-        nullptr, offs.p + (size_t)a * FF_SPLIT, offs_h[a], ci.p, cj.p, c.derr.p);
+        c.nodes.p, c.tri_s.p, front.p, front.p + FF_SPLIT, c.cen.p, c.nrm.p, a, b, nullptr, c.r_max, slack, cut2,
+        box_cut2, nullptr, offs.p + (size_t)a * FF_SPLIT, offs_h[a], ci.p, cj.p, c.derr.p);
     ILG_CUDA(cudaGetLastError());
     k_vis_rays<<<div_up(np, 128), 128, 0, s>>>(c.nodes.p, c.tri_s.p, c.root, c.cen.p, c.nrm.p, np, ci.p, cj.p,
                                                (float)offset, bits, ukeys.p, ucount.p, c.derr.p);
@@ -988,6 +1014,100 @@ int form_factors_build(Context& c, const double* albedo_h, double albedo_scalar,
   c.nnz = nnz;
   c.have_F = true;
   ILG_TRY(radiosity_prepare(c));
+  return read_device_errors(c);
+}
+
+int visibility_sample(Context& c, double cutoff, double offset, const int* src_h, int nsrc, const double* radii_h,
+                      int nradii, int64_t* per_src_h, int64_t* within_h, int64_t* rays_out) {
+  if (nsrc < 1 || !src_h || nradii < 0 || (nradii > 0 && !radii_h)) { set_error("invalid sample"); return ILG_ERR_ARG; }
+  cudaStream_t s = c.stream;
+  const int nt = c.nt;
+  std::vector<int> slot_h((size_t)nt, -1);
+  for (int q = 0; q < nsrc; ++q) {
+    if (src_h[q] < 0 || src_h[q] >= nt) { set_error("source %d out of range", src_h[q]); return ILG_ERR_ARG; }
+    if (slot_h[src_h[q]] >= 0) { set_error("source %d listed twice", src_h[q]); return ILG_ERR_ARG; }
+    slot_h[src_h[q]] = q;
+  }
+  dbuf<int> dsrc, dslot, front;
+  dbuf<double> dradii;
+  dbuf<unsigned long long> per_src, within, offs, ukeys, ucount;
+  dbuf<uint32_t> cnt;
+  ILG_TRY(dsrc.alloc(nsrc));
+  ILG_TRY(dslot.alloc(nt));
+  ILG_TRY(dradii.alloc(std::max(nradii, 1)));
+  ILG_TRY(per_src.alloc(nsrc));
+  ILG_TRY(within.alloc(std::max(nradii, 1)));
+  ILG_TRY(front.alloc(FF_SPLIT + 1));
+  const int64_t nitems = (int64_t)nsrc * FF_SPLIT;
+  ILG_TRY(cnt.alloc(nitems));
+  ILG_TRY(offs.alloc(nitems));
+  ILG_TRY(ucount.alloc(1));
+  ILG_CUDA(cudaMemcpyAsync(dsrc.p, src_h, (size_t)nsrc * 4, cudaMemcpyHostToDevice, s));
+  ILG_CUDA(cudaMemcpyAsync(dslot.p, slot_h.data(), (size_t)nt * 4, cudaMemcpyHostToDevice, s));
+  if (nradii > 0) ILG_CUDA(cudaMemcpyAsync(dradii.p, radii_h, (size_t)nradii * 8, cudaMemcpyHostToDevice, s));
+  ILG_CUDA(cudaMemsetAsync(per_src.p, 0, (size_t)nsrc * 8, s));
+  ILG_CUDA(cudaMemsetAsync(within.p, 0, (size_t)std::max(nradii, 1) * 8, s));
+  ILG_CUDA(cudaMemsetAsync(ucount.p, 0, 8, s));
+  const float slack = 1e-5f * c.scene_mag;
+  const float cut2 = cutoff > 0.0 ? (float)(cutoff * cutoff) : -1.0f;
+  const float box_cut2 = cutoff > 0.0 ? (float)((cutoff + 1e-5 * c.scene_mag) * (cutoff + 1e-5 * c.scene_mag)) * 1.0001f
+                                      : -1.0f;
+  k_frontier<<<1, 1, 0, s>>>(c.nodes.p, c.root, front.p, front.p + FF_SPLIT);
+  k_candidates<false><<<div_up(nitems, 128), 128, 0, s>>>(c.nodes.p, c.tri_s.p, front.p, front.p + FF_SPLIT, c.cen.p,
+                                                          c.nrm.p, 0, nsrc, dsrc.p, c.r_max, slack, cut2, box_cut2,
+                                                          cnt.p, nullptr, 0ull, nullptr, nullptr, c.derr.p);
+  ILG_CUDA(cudaGetLastError());
+  ILG_TRY(scan_exclusive_u32_to_u64(cnt.p, offs.p, nitems, c.scan, s));
+  std::vector<unsigned long long> offs_h((size_t)nsrc + 1);
+  uint32_t last_cnt = 0;
+  unsigned long long last_off = 0;
+  ILG_CUDA(cudaMemcpy2DAsync(offs_h.data(), 8, offs.p, 8 * FF_SPLIT, 8, nsrc, cudaMemcpyDeviceToHost, s));
+  ILG_CUDA(cudaMemcpyAsync(&last_off, offs.p + (nitems - 1), 8, cudaMemcpyDeviceToHost, s));
+  ILG_CUDA(cudaMemcpyAsync(&last_cnt, cnt.p + (nitems - 1), 4, cudaMemcpyDeviceToHost, s));
+  ILG_CUDA(cudaStreamSynchronize(s));
+  offs_h[nsrc] = last_off + last_cnt;
+  if (rays_out) *rays_out = (int64_t)offs_h[nsrc];
+  int bits = 1;
+  while ((1LL << bits) < nt) ++bits;
+  // chunks of at most FF_CHUNK candidate pairs; each chunk's distinct hit
+  // keys are sorted, counted and dropped (the sample's keys never coexist)
+  std::vector<int> cutq{0};
+  int64_t cap = 1;
+  while (cutq.back() < nsrc) {
+    int a = cutq.back(), b = a + 1;
+    while (b < nsrc && (int64_t)(offs_h[b + 1] - offs_h[a]) <= FF_CHUNK) ++b;
+    cap = std::max<int64_t>(cap, (int64_t)(offs_h[b] - offs_h[a]));
+    cutq.push_back(b);
+  }
+  dbuf<int32_t> ci, cj;
+  ILG_TRY(ci.alloc(cap));
+  ILG_TRY(cj.alloc(cap));
+  ILG_TRY(ukeys.alloc(cap));
+  for (size_t q = 0; q + 1 < cutq.size(); ++q) {
+    const int a = cutq[q], b = cutq[q + 1];
+    const int64_t np = (int64_t)(offs_h[b] - offs_h[a]);
+    if (np == 0) continue;
+    ILG_CUDA(cudaMemsetAsync(ucount.p, 0, 8, s));
+    k_candidates<true><<<div_up((int64_t)(b - a) * FF_SPLIT, 128), 128, 0, s>>>(
+        c.nodes.p, c.tri_s.p, front.p, front.p + FF_SPLIT, c.cen.p, c.nrm.p, a, b, dsrc.p, c.r_max, slack, cut2,
+        box_cut2, nullptr, offs.p + (size_t)a * FF_SPLIT, offs_h[a], ci.p, cj.p, c.derr.p);
+    ILG_CUDA(cudaGetLastError());
+    k_vis_rays<<<div_up(np, 128), 128, 0, s>>>(c.nodes.p, c.tri_s.p, c.root, c.cen.p, c.nrm.p, np, ci.p, cj.p,
+                                               (float)offset, bits, ukeys.p, ucount.p, c.derr.p);
+    ILG_CUDA(cudaGetLastError());
+    unsigned long long nk = 0;
+    ILG_CUDA(cudaMemcpyAsync(&nk, ucount.p, 8, cudaMemcpyDeviceToHost, s));
+    ILG_CUDA(cudaStreamSynchronize(s));
+    if (nk > 1) ILG_TRY(radix_sort_u64(ukeys.p, nullptr, (int64_t)nk, 2 * bits, c.sort, s));
+    if (nk > 0) {
+      k_sample_count<<<div_up((int64_t)nk, 256), 256, 0, s>>>(ukeys.p, (int64_t)nk, bits, c.cen.p, c.nrm.p, c.area.p,
+                                                             dslot.p, dradii.p, nradii, per_src.p, within.p);
+      ILG_CUDA(cudaGetLastError());
+    }
+  }
+  ILG_CUDA(cudaMemcpyAsync(per_src_h, per_src.p, (size_t)nsrc * 8, cudaMemcpyDeviceToHost, s));
+  if (nradii > 0 && within_h) ILG_CUDA(cudaMemcpyAsync(within_h, within.p, (size_t)nradii * 8, cudaMemcpyDeviceToHost, s));
+  ILG_CUDA(cudaStreamSynchronize(s));
   return read_device_errors(c);
 }
 

@@ -595,6 +595,15 @@ int ilg_compute_F_cutoff(ilg_ctx* ctx, const double* albedo, double albedo_scala
   return ILG_OK;
 }
 
+int ilg_visibility_sample(ilg_ctx* ctx, double cutoff, double offset, const int32_t* sources, int nsrc,
+                          const double* radii, int nradii, int64_t* per_source, int64_t* within_radius,
+                          int64_t* rays) {
+  if (!ctx || !per_source) { set_error("ctx or per_source is NULL"); return ILG_ERR_ARG; }
+  Context& c = ctx->c;
+  AllocOn on_(c.stream);
+  return visibility_sample(c, cutoff, offset, sources, nsrc, radii, nradii, per_source, within_radius, rays);
+}
+
 int ilg_get_F(ilg_ctx* ctx, int64_t* rowptr, int32_t* col, double* val) {
   if (!ctx || !ctx->c.have_F) { set_error("no form factors"); return ILG_ERR_ARG; }
   Context& c = ctx->c;

@@ -310,6 +310,8 @@ int horizons_f32(Context& c);   // H32 and hmm32 from H
 int bvh_render(Context& c, int mode, double az_deg, double el_deg, int width, int height, int32_t* out_h);
 int form_factors_build(Context& c, const double* albedo_h, double albedo_scalar, double offset,
                        double cutoff, int64_t* rays_out);
+int visibility_sample(Context& c, double cutoff, double offset, const int* src_h, int nsrc, const double* radii_h,
+                      int nradii, int64_t* per_src_h, int64_t* within_h, int64_t* rays_out);
 
 // ---- direct.cu ----
 SunAux make_sun_aux(const double* s, double solar_const, double scene_mag, double disk_rmax);

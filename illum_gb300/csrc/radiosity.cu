@@ -817,6 +817,111 @@ __global__ void k_row_keys(const int64_t* __restrict__ rowptr, const int32_t* __
   }
 }
 
+// Tile build on the device. Per Morton position p: an upper bound on the
+// halo facets row order[p] adds to a tile that already holds row
+// order[p - 1], i.e. its columns not among that row's (both column lists
+// ascending in Morton rank; an empty previous row bounds it by the row's
+// length). The host cuts tiles with these bounds, so a tile's exact halo
+// is never larger than its bound.
+__global__ void k_halo_inc(const int64_t* __restrict__ rowptr, const uint32_t* __restrict__ order,
+                           const unsigned long long* __restrict__ skey, unsigned long long cmask, int nt, int* inc) {
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= nt) return;
+  const int g = (int)order[p];
+  const int64_t a0 = rowptr[g], a1 = rowptr[g + 1];
+  if (p == 0) { inc[p] = (int)(a1 - a0); return; }
+  const int h = (int)order[p - 1];
+  int64_t j = rowptr[h];
+  const int64_t b1 = rowptr[h + 1];
+  int cnt = 0;
+  for (int64_t k = a0; k < a1; ++k) {
+    const unsigned long long c = skey[k] & cmask;
+    while (j < b1 && (skey[j] & cmask) < c) ++j;
+    if (j >= b1 || (skey[j] & cmask) != c) ++cnt;
+  }
+  inc[p] = cnt;
+}
+
+// key = (tile of the entry's row) << rb | Morton rank of its column; value =
+// the entry's index in the row-sorted order.
+__global__ void k_tile_keys(const unsigned long long* __restrict__ skey, int64_t n, int rb,
+                            const int* __restrict__ tile_of, unsigned long long* key, uint32_t* idx) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const unsigned long long cm = (1ull << rb) - 1;
+  const int g = (int)(skey[k] >> rb);
+  key[k] = ((unsigned long long)tile_of[g] << rb) | (skey[k] & cm);
+  idx[k] = (uint32_t)k;
+}
+
+// 1 where a (tile, column) run starts in the sorted keys.
+__global__ void k_run_flags(const unsigned long long* __restrict__ key, int64_t n, uint32_t* flag) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  flag[i] = (i == 0 || key[i] != key[i - 1]) ? 1u : 0u;
+}
+
+// Runs are the tiles' halo facets, in (tile, Morton rank) order: the run
+// index is the facet's slot in t_halo, and a tile's first run is its h0.
+__global__ void k_halo_runs(const unsigned long long* __restrict__ key, const uint32_t* __restrict__ flag,
+                            const unsigned long long* __restrict__ before, int64_t n, int rb, uint32_t* t_halo,
+                            int* tile_first) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || !flag[i]) return;
+  const unsigned long long cm = (1ull << rb) - 1;
+  const int64_t r = (int64_t)before[i];
+  t_halo[r] = (uint32_t)(key[i] & cm);
+  const int t = (int)(key[i] >> rb);
+  if (i == 0 || (int)(key[i - 1] >> rb) != t) tile_first[t] = (int)r;
+}
+
+// Each entry to its stored slot: entry j of a tile (rows in Morton order,
+// each row's entries in column order) belongs to thread t = j / lam as its
+// kk = j % lam-th, stored at e0 + (kk / 4) 4096 + 4 t + kk % 4; the slot
+// holds the entry's halo index (run - h0) with the row-end bit, the CSR
+// entry it takes its value from, and its row (for the row scale).
+__global__ void k_tile_slots(const unsigned long long* __restrict__ key, const uint32_t* __restrict__ idx,
+                             const uint32_t* __restrict__ flag, const unsigned long long* __restrict__ before,
+                             int64_t n, int rb, const unsigned long long* __restrict__ skey,
+                             const uint32_t* __restrict__ ssrc, const int64_t* __restrict__ rowptr,
+                             const int* __restrict__ rowoff, const RowTile* __restrict__ tiles, uint16_t* cf,
+                             uint32_t* esrc, uint32_t* efac) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int t = (int)(key[i] >> rb);
+  const RowTile T = tiles[t];
+  const int64_t run = (int64_t)before[i] + flag[i] - 1;
+  const uint32_t loc = (uint32_t)(run - T.h0);
+  const int64_t k = idx[i];
+  const int g = (int)(skey[k] >> rb);
+  const int64_t j = rowoff[g] + (k - rowptr[g]);
+  const int64_t th = j / T.lam, kk = j - th * T.lam;
+  const int64_t off = T.e0 + (kk >> 2) * 4 * RAD_THREADS + 4 * th + (kk & 3);
+  cf[off] = (uint16_t)(loc | (k + 1 == rowptr[g + 1] ? 0x8000u : 0u));
+  esrc[off] = ssrc[k];
+  efac[off] = (uint32_t)g;
+}
+
+// Each thread's first row (with a continuation bit when its run starts
+// inside the row): rowj0 holds each tile row's first entry index within the
+// tile, tile rows in order.
+__global__ void k_tile_starts(const RowTile* __restrict__ tiles, int ntiles, const int64_t* __restrict__ ne,
+                              const int* __restrict__ rowj0, uint32_t* tstart) {
+  int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= (int64_t)ntiles * RAD_THREADS) return;
+  const int tid = (int)(q / RAD_THREADS), t = (int)(q % RAD_THREADS);
+  const RowTile T = tiles[tid];
+  const int64_t j0 = (int64_t)t * T.lam;
+  if (j0 >= ne[tid]) { tstart[q] = (uint32_t)T.nrows; return; }
+  const int* rj = rowj0 + T.r0;
+  int lo = 0, hi = T.nrows;   // last row with rj <= j0
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if ((int64_t)rj[mid] <= j0) lo = mid; else hi = mid;
+  }
+  tstart[q] = (uint32_t)lo | ((int64_t)rj[lo] != j0 ? 0x80000000u : 0u);
+}
+
 // Stored entry e takes CSR entry src[e] (value as a double-float, and its
 // bf16 copy scaled by its row's scale), or zero for padding (src = ~0).
 __global__ void k_tile_fill(const uint32_t* __restrict__ src, const uint32_t* __restrict__ fac, int64_t n,
@@ -880,31 +985,36 @@ int radiosity_prepare(Context& c) {
 
   // Each row's entries in Morton order of their columns, sorted on the
   // device: key = (row, Morton position of the column), value = CSR entry.
+  // Only N-sized data (row pointers, the Morton order, per-row halo bounds)
+  // comes to the host, which cuts the tiles; everything per entry stays on
+  // the device.
   int rb = 1;
   while ((1 << rb) < nt) ++rb;
   std::vector<int64_t> rp((size_t)nt + 1);
-  std::vector<unsigned long long> skey((size_t)(nnz > 0 ? nnz : 1));
-  std::vector<uint32_t> ssrc((size_t)(nnz > 0 ? nnz : 1));
   std::vector<uint32_t> order((size_t)nt);
+  std::vector<int> hinc((size_t)nt, 0);
   ILG_CUDA(cudaMemcpyAsync(rp.data(), c.rowptr.p, rp.size() * 8, cudaMemcpyDeviceToHost, s));
   ILG_CUDA(cudaMemcpyAsync(order.data(), c.morton_order.p, (size_t)nt * 4, cudaMemcpyDeviceToHost, s));
+  dbuf<unsigned long long> dkey;
+  dbuf<uint32_t> dsv;
+  const unsigned long long cmask = (1ull << rb) - 1;
   if (nnz > 0) {
-    dbuf<uint32_t> drank, dsv;
-    dbuf<unsigned long long> dkey;
+    dbuf<uint32_t> drank;
+    dbuf<int> dinc;
     ILG_TRY(drank.alloc(nt));
     ILG_TRY(dkey.alloc(nnz));
     ILG_TRY(dsv.alloc(nnz));
+    ILG_TRY(dinc.alloc(nt));
     k_rank<<<div_up(nt, 256), 256, 0, s>>>(c.morton_order.p, nt, drank.p);
     ILG_CUDA(cudaGetLastError());
     k_row_keys<<<div_up(nt, 256), 256, 0, s>>>(c.rowptr.p, c.col.p, drank.p, nt, rb, dkey.p, dsv.p);
     ILG_CUDA(cudaGetLastError());
     ILG_TRY(radix_sort_u64(dkey.p, dsv.p, nnz, 2 * rb, c.sort, s));
-    ILG_CUDA(cudaMemcpyAsync(skey.data(), dkey.p, (size_t)nnz * 8, cudaMemcpyDeviceToHost, s));
-    ILG_CUDA(cudaMemcpyAsync(ssrc.data(), dsv.p, (size_t)nnz * 4, cudaMemcpyDeviceToHost, s));
-    ILG_CUDA(cudaStreamSynchronize(s));
+    k_halo_inc<<<div_up(nt, 256), 256, 0, s>>>(c.rowptr.p, c.morton_order.p, dkey.p, cmask, nt, dinc.p);
+    ILG_CUDA(cudaGetLastError());
+    ILG_CUDA(cudaMemcpyAsync(hinc.data(), dinc.p, (size_t)nt * 4, cudaMemcpyDeviceToHost, s));
   }
   ILG_CUDA(cudaStreamSynchronize(s));
-  const unsigned long long cmask = (1ull << rb) - 1;
 
   // active rows (with entries) in Morton order
   std::vector<uint8_t> act((size_t)nt, 0);
@@ -933,12 +1043,13 @@ int radiosity_prepare(Context& c) {
   // cost, so row- and halo-heavy tiles carry fewer entries; it is kept if it
   // still fits the grid. If the halo or row caps force more tiles than
   // blocks (very large meshes), the cuts are equal shares of the estimated
-  // work (entries + rows), several tiles per block.
+  // work (entries + rows), several tiles per block. A tile's halo is counted
+  // with the per-row bounds (a tile's first row adds all its columns), so it
+  // never exceeds the exact halo found on the device afterwards.
   const int G = g_rad_nsm * std::min(g_rad_per_sm64, g_rad_per_smm);
   std::vector<RowTile> tiles;
   std::vector<size_t> tile_a;   // first active row of each tile
-  std::vector<int> stamp((size_t)nt, -1);
-  std::vector<uint32_t> fresh;
+  std::vector<int64_t> tile_ne;  // entries of each tile
   const int64_t NOCAP = std::numeric_limits<int64_t>::max() / 4;
   // One greedy pass. cap > 0: at most cap entries and cap + slack weighed
   // cost per tile; returns false once more than max_tiles are needed, and
@@ -948,7 +1059,7 @@ int radiosity_prepare(Context& c) {
                  int* capped) -> bool {
     tiles.clear();
     tile_a.clear();
-    std::fill(stamp.begin(), stamp.end(), -1);
+    tile_ne.clear();
     if (capped) *capped = 0;
     int64_t done_cost = 0;
     size_t a = 0;
@@ -956,7 +1067,7 @@ int radiosity_prepare(Context& c) {
       if (tiles.size() >= max_tiles) return false;
       const int tid = (int)tiles.size();
       const int64_t bound = cap > 0 ? 0 : (int64_t)((double)total_cost * (double)(tid + 1) / (double)ntarget);
-      int nhalo = 0;
+      int64_t nhalo = 0;
       size_t b = a;
       int64_t ne = 0;
       while (b < arow.size()) {
@@ -967,17 +1078,11 @@ int radiosity_prepare(Context& c) {
         }
         const int64_t len = rp[g + 1] - rp[g];
         if (cap > 0 && b > a && ne + len > cap) break;
-        fresh.clear();
-        for (int64_t k = rp[g]; k < rp[g + 1]; ++k) {
-          uint32_t cpos = (uint32_t)(skey[k] & cmask);
-          if (stamp[cpos] != tid) { stamp[cpos] = tid; fresh.push_back(cpos); }
-        }
-        const int nh = nhalo + (int)fresh.size();
+        const int64_t nh = nhalo + (b == a ? len : (int64_t)hinc[arow[b]]);
         const bool over_halo = nh > RAD_HALO;
         const bool over_cost =
             cap > 0 && ne + len + RAD_ROW_COST * (int64_t)(b - a + 1) + RAD_HALO_COST * nh > cap + slack;
         if (b > a && (over_halo || over_cost)) {
-          for (uint32_t cpos : fresh) stamp[cpos] = -1;
           if (over_halo && capped) ++*capped;
           break;
         }
@@ -989,10 +1094,11 @@ int radiosity_prepare(Context& c) {
       RowTile T{};
       T.lam = (int)(((ne + RAD_THREADS - 1) / RAD_THREADS + 3) & ~(int64_t)3);
       T.nrows = (int)(b - a);
-      T.nhalo = nhalo;
+      T.nhalo = (int)nhalo;
       T.mesh = 0;
       tiles.push_back(T);
       tile_a.push_back(a);
+      tile_ne.push_back(ne);
       done_cost += ne + RAD_ROW_COST * (int64_t)(b - a);
       a = b;
     }
@@ -1018,105 +1124,107 @@ int radiosity_prepare(Context& c) {
       cut(0, 0, total_cost, ntarget, (size_t)-1, nullptr);
     }
   }
-  // offsets of each tile's slots, rows and halo
-  int64_t stored_total = 0, rows_total = 0, halo_total = 0;
-  for (RowTile& T : tiles) {
+  // per row: its tile and first entry within the tile; per tile: stored
+  // offset and rows
+  const int ntile = (int)tiles.size();
+  std::vector<int> tile_of((size_t)nt, 0), rowoff((size_t)nt, 0);
+  std::vector<uint32_t> trow(arow.size());
+  std::vector<int> rowj0(arow.size());
+  int64_t stored_total = 0, rows_total = 0;
+  for (int tid = 0; tid < ntile; ++tid) {
+    RowTile& T = tiles[tid];
     T.e0 = stored_total;
     T.r0 = (int)rows_total;
-    T.h0 = (int)halo_total;
     stored_total += (int64_t)T.lam * RAD_THREADS;
-    rows_total += T.nrows;
-    halo_total += T.nhalo;
-  }
-  std::vector<uint16_t> cf((size_t)stored_total, 0);
-  std::vector<uint32_t> esrc((size_t)stored_total, 0xffffffffu), efac((size_t)stored_total, 0);
-  std::vector<uint32_t> trow((size_t)rows_total), thalo((size_t)halo_total);
-  std::vector<uint32_t> tstart(tiles.size() * RAD_THREADS);
-  // Per tile, independently (host threads): sorted halo, entry slots
-  // (thread t holds entries [t lam, (t+1) lam) of the tile, interleaved by
-  // 4) and each thread's first row with its continuation bit.
-  std::atomic<int> next{0};
-  std::atomic<int> bad{0};
-  auto fill = [&]() {
-    std::vector<int> loc((size_t)nt, 0);
-    std::vector<int> seen((size_t)nt, -1);
-    std::vector<uint32_t> halo;
-    std::vector<int64_t> row_first;
-    for (int tid; (tid = next.fetch_add(1)) < (int)tiles.size();) {
-      const RowTile& T = tiles[tid];
-      const size_t a = tile_a[tid], b = a + T.nrows;
-      halo.clear();
-      int64_t ne = 0;
-      for (size_t q = a; q < b; ++q) {
-        int g = (int)order[arow[q]];
-        ne += rp[g + 1] - rp[g];
-        for (int64_t k = rp[g]; k < rp[g + 1]; ++k) {
-          uint32_t cpos = (uint32_t)(skey[k] & cmask);
-          if (seen[cpos] != tid) { seen[cpos] = tid; halo.push_back(cpos); }
-        }
-      }
-      if ((int)halo.size() != T.nhalo) { bad = 1; continue; }
-      std::sort(halo.begin(), halo.end());
-      for (int h = 0; h < (int)halo.size(); ++h) loc[halo[h]] = h;
-      std::copy(halo.begin(), halo.end(), thalo.begin() + T.h0);
-      row_first.clear();
-      int64_t j = 0;
-      for (size_t q = a; q < b; ++q) {
-        int p = arow[q];
-        int g = (int)order[p];
-        row_first.push_back(j);
-        trow[(size_t)T.r0 + (q - a)] = (uint32_t)p;
-        for (int64_t k = rp[g]; k < rp[g + 1]; ++k, ++j) {
-          int64_t t = j / T.lam, kk = j % T.lam;
-          int64_t off = T.e0 + (kk >> 2) * 4 * RAD_THREADS + 4 * t + (kk & 3);
-          cf[off] = (uint16_t)(loc[skey[k] & cmask] | (k + 1 == rp[g + 1] ? 0x8000 : 0));
-          esrc[off] = ssrc[k];
-          efac[off] = (uint32_t)g;
-        }
-      }
-      uint32_t* ts = tstart.data() + (size_t)tid * RAD_THREADS;
-      for (int t = 0; t < RAD_THREADS; ++t) {
-        int64_t j0 = (int64_t)t * T.lam;
-        if (j0 >= ne) { ts[t] = (uint32_t)T.nrows; continue; }
-        int r = (int)(std::upper_bound(row_first.begin(), row_first.end(), j0) - row_first.begin()) - 1;
-        ts[t] = (uint32_t)r | (row_first[r] != j0 ? 0x80000000u : 0u);
-      }
+    int64_t j = 0;
+    for (int q = 0; q < T.nrows; ++q) {
+      const int p = arow[tile_a[tid] + q];
+      const int g = (int)order[p];
+      tile_of[g] = tid;
+      rowoff[g] = (int)j;
+      trow[(size_t)rows_total + q] = (uint32_t)p;
+      rowj0[(size_t)rows_total + q] = (int)j;
+      j += rp[g + 1] - rp[g];
     }
-  };
-  {
-    int nth = (int)std::min<size_t>(tiles.size(), std::max(1u, std::min(16u, std::thread::hardware_concurrency())));
-    std::vector<std::thread> pool;
-    for (int t = 1; t < nth; ++t) pool.emplace_back(fill);
-    fill();
-    for (auto& th : pool) th.join();
+    rows_total += T.nrows;
   }
-  if (bad) { set_error("row tile halo mismatch"); return ILG_ERR_CUDA; }
-  c.ntiles = (int)tiles.size();
-  c.tile_elems = (int64_t)cf.size();
-  c.tiles_h = tiles;
-  const int64_t ns = c.tile_elems > 0 ? c.tile_elems : 1;
-  const int ntl = c.ntiles > 0 ? c.ntiles : 1;
-  ILG_TRY(c.tiles.alloc(ntl));
-  ILG_TRY(c.t_cf.alloc(ns));
-  ILG_TRY(c.t_vhi.alloc(ns));
-  ILG_TRY(c.t_vlo.alloc(ns));
-  ILG_TRY(c.t_vbf.alloc(ns));
-  ILG_TRY(c.t_row.alloc(trow.empty() ? 1 : trow.size()));
-  ILG_TRY(c.t_scale.alloc(trow.empty() ? 1 : trow.size()));
-  ILG_TRY(c.t_halo.alloc(thalo.empty() ? 1 : thalo.size()));
-  ILG_TRY(c.t_start.alloc((size_t)ntl * RAD_THREADS));
-  ILG_TRY(c.tile_d2.alloc(2 * (size_t)ntl));
-  if (c.ntiles > 0) {
+  // exact halos on the device: the entries sorted by (tile, column), runs =
+  // halo facets
+  std::vector<int> tfirst((size_t)ntile + 1, 0);
+  dbuf<uint32_t> t_halo_tmp;
+  if (ntile > 0) {
+    dbuf<int> dtile_of, drowoff, dtfirst;
+    dbuf<unsigned long long> key2, before;
+    dbuf<uint32_t> idx2, flag;
+    ILG_TRY(dtile_of.alloc(nt));
+    ILG_TRY(drowoff.alloc(nt));
+    ILG_TRY(key2.alloc(nnz));
+    ILG_TRY(idx2.alloc(nnz));
+    ILG_TRY(flag.alloc(nnz));
+    ILG_TRY(before.alloc(nnz));
+    ILG_TRY(dtfirst.alloc(ntile + 1));
+    ILG_TRY(t_halo_tmp.alloc(nnz));
+    ILG_CUDA(cudaMemcpyAsync(dtile_of.p, tile_of.data(), (size_t)nt * 4, cudaMemcpyHostToDevice, s));
+    ILG_CUDA(cudaMemcpyAsync(drowoff.p, rowoff.data(), (size_t)nt * 4, cudaMemcpyHostToDevice, s));
+    k_tile_keys<<<div_up(nnz, 256), 256, 0, s>>>(dkey.p, nnz, rb, dtile_of.p, key2.p, idx2.p);
+    ILG_CUDA(cudaGetLastError());
+    int tb = 1;
+    while ((1 << tb) < ntile) ++tb;
+    ILG_TRY(radix_sort_u64(key2.p, idx2.p, nnz, tb + rb, c.sort, s));
+    k_run_flags<<<div_up(nnz, 256), 256, 0, s>>>(key2.p, nnz, flag.p);
+    ILG_CUDA(cudaGetLastError());
+    ILG_TRY(scan_exclusive_u32_to_u64(flag.p, before.p, nnz, c.scan, s));
+    k_halo_runs<<<div_up(nnz, 256), 256, 0, s>>>(key2.p, flag.p, before.p, nnz, rb, t_halo_tmp.p, dtfirst.p);
+    ILG_CUDA(cudaGetLastError());
+    unsigned long long last_before = 0;
+    uint32_t last_flag = 0;
+    ILG_CUDA(cudaMemcpyAsync(tfirst.data(), dtfirst.p, (size_t)ntile * 4, cudaMemcpyDeviceToHost, s));
+    ILG_CUDA(cudaMemcpyAsync(&last_before, before.p + nnz - 1, 8, cudaMemcpyDeviceToHost, s));
+    ILG_CUDA(cudaMemcpyAsync(&last_flag, flag.p + nnz - 1, 4, cudaMemcpyDeviceToHost, s));
+    ILG_CUDA(cudaStreamSynchronize(s));
+    tfirst[ntile] = (int)(last_before + last_flag);
+    for (int tid = 0; tid < ntile; ++tid) {
+      RowTile& T = tiles[tid];
+      T.h0 = tfirst[tid];
+      T.nhalo = tfirst[tid + 1] - tfirst[tid];
+      if (T.nhalo > RAD_HALO || T.nhalo < 1) { set_error("row tile halo of %d facets", T.nhalo); return ILG_ERR_CUDA; }
+    }
+    c.ntiles = ntile;
+    c.tile_elems = stored_total;
+    c.tiles_h = tiles;
+    const int64_t ns = stored_total;
+    ILG_TRY(c.tiles.alloc(ntile));
+    ILG_TRY(c.t_cf.alloc(ns));
+    ILG_TRY(c.t_vhi.alloc(ns));
+    ILG_TRY(c.t_vlo.alloc(ns));
+    ILG_TRY(c.t_vbf.alloc(ns));
+    ILG_TRY(c.t_row.alloc(trow.size()));
+    ILG_TRY(c.t_scale.alloc(trow.size()));
+    ILG_TRY(c.t_halo.alloc(tfirst[ntile]));
+    ILG_TRY(c.t_start.alloc((size_t)ntile * RAD_THREADS));
+    ILG_TRY(c.tile_d2.alloc(2 * (size_t)ntile));
     dbuf<uint32_t> dsrc, dfac;
+    dbuf<int> drowj0;
+    dbuf<int64_t> dne;
     ILG_TRY(dsrc.alloc(ns));
     ILG_TRY(dfac.alloc(ns));
+    ILG_TRY(drowj0.alloc(rowj0.size()));
+    ILG_TRY(dne.alloc(ntile));
     ILG_CUDA(cudaMemcpyAsync(c.tiles.p, tiles.data(), tiles.size() * sizeof(RowTile), cudaMemcpyHostToDevice, s));
-    ILG_CUDA(cudaMemcpyAsync(c.t_cf.p, cf.data(), cf.size() * 2, cudaMemcpyHostToDevice, s));
     ILG_CUDA(cudaMemcpyAsync(c.t_row.p, trow.data(), trow.size() * 4, cudaMemcpyHostToDevice, s));
-    ILG_CUDA(cudaMemcpyAsync(c.t_halo.p, thalo.data(), thalo.size() * 4, cudaMemcpyHostToDevice, s));
-    ILG_CUDA(cudaMemcpyAsync(c.t_start.p, tstart.data(), tstart.size() * 4, cudaMemcpyHostToDevice, s));
-    ILG_CUDA(cudaMemcpyAsync(dsrc.p, esrc.data(), esrc.size() * 4, cudaMemcpyHostToDevice, s));
-    ILG_CUDA(cudaMemcpyAsync(dfac.p, efac.data(), efac.size() * 4, cudaMemcpyHostToDevice, s));
+    ILG_CUDA(cudaMemcpyAsync(drowj0.p, rowj0.data(), rowj0.size() * 4, cudaMemcpyHostToDevice, s));
+    ILG_CUDA(cudaMemcpyAsync(dne.p, tile_ne.data(), (size_t)ntile * 8, cudaMemcpyHostToDevice, s));
+    ILG_CUDA(cudaMemcpyAsync(c.t_halo.p, t_halo_tmp.p, (size_t)tfirst[ntile] * 4, cudaMemcpyDeviceToDevice, s));
+    // padding slots: no entry (zero halo index, no source)
+    ILG_CUDA(cudaMemsetAsync(c.t_cf.p, 0, (size_t)ns * 2, s));
+    ILG_CUDA(cudaMemsetAsync(dsrc.p, 0xff, (size_t)ns * 4, s));
+    ILG_CUDA(cudaMemsetAsync(dfac.p, 0, (size_t)ns * 4, s));
+    k_tile_slots<<<div_up(nnz, 256), 256, 0, s>>>(key2.p, idx2.p, flag.p, before.p, nnz, rb, dkey.p, dsv.p,
+                                                  c.rowptr.p, drowoff.p, c.tiles.p, c.t_cf.p, dsrc.p, dfac.p);
+    ILG_CUDA(cudaGetLastError());
+    k_tile_starts<<<div_up((int64_t)ntile * RAD_THREADS, 256), 256, 0, s>>>(c.tiles.p, ntile, dne.p, drowj0.p,
+                                                                            c.t_start.p);
+    ILG_CUDA(cudaGetLastError());
     k_tile_fill<<<div_up(ns, 256), 256, 0, s>>>(dsrc.p, dfac.p, ns, c.val.p, c.row_scale.p, c.t_vhi.p, c.t_vlo.p,
                                                 c.t_vbf.p);
     ILG_CUDA(cudaGetLastError());
@@ -1124,6 +1232,20 @@ int radiosity_prepare(Context& c) {
                                                                   c.row_scale.p, c.t_scale.p);
     ILG_CUDA(cudaGetLastError());
     ILG_CUDA(cudaStreamSynchronize(s));
+  } else {
+    c.ntiles = 0;
+    c.tile_elems = 0;
+    c.tiles_h.clear();
+    ILG_TRY(c.tiles.alloc(1));
+    ILG_TRY(c.t_cf.alloc(1));
+    ILG_TRY(c.t_vhi.alloc(1));
+    ILG_TRY(c.t_vlo.alloc(1));
+    ILG_TRY(c.t_vbf.alloc(1));
+    ILG_TRY(c.t_row.alloc(1));
+    ILG_TRY(c.t_scale.alloc(1));
+    ILG_TRY(c.t_halo.alloc(1));
+    ILG_TRY(c.t_start.alloc(RAD_THREADS));
+    ILG_TRY(c.tile_d2.alloc(2));
   }
   ILG_TRY(c.row_act.alloc(nt));
   ILG_CUDA(cudaMemcpyAsync(c.row_act.p, act.data(), (size_t)nt, cudaMemcpyHostToDevice, s));

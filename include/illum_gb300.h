@@ -109,6 +109,17 @@ int ilg_compute_F(ilg_ctx* ctx, const double* albedo, double albedo_scalar, doub
  * patches tractable (a facet then sees O(cutoff^2) facets, not O(N)). */
 int ilg_compute_F_cutoff(ilg_ctx* ctx, const double* albedo, double albedo_scalar, double offset,
                          double cutoff, int64_t* nnz, int64_t* rays);
+/* Size of F from a sample of source facets, without building it (no
+ * reference counterpart; it sizes a cutoff before committing memory):
+ * visibility and form factors of the listed sources only (distinct, in
+ * [0, nt)) with the given cutoff (0: none). per_source[q] receives the
+ * nonzero entries of column sources[q] (what compute_F would store for that
+ * source); within_radius[k] (may be NULL) the sample's nonzero entries whose
+ * centroid distance is at most radii[k] (mesh units); *rays (may be NULL)
+ * the visibility rays cast. */
+int ilg_visibility_sample(ilg_ctx* ctx, double cutoff, double offset, const int32_t* sources, int nsrc,
+                          const double* radii, int nradii, int64_t* per_source, int64_t* within_radius,
+                          int64_t* rays);
 /* rowptr: nt+1, col: nnz, val: nnz */
 int ilg_get_F(ilg_ctx* ctx, int64_t* rowptr, int32_t* col, double* val);
 int ilg_set_F(ilg_ctx* ctx, int64_t nnz, const int64_t* rowptr, const int32_t* col,

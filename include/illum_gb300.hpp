@@ -64,8 +64,19 @@ class illum_context {
     return compute_F_(albedo.data(), 1.0, offset);
   }
 
+  // A separate mesh the horizon rays are traced against (the reference's
+  // set_horizon_obj_file, illum.hpp:36-37; here the loaded triangles:
+  // vertices nv x 3 row-major float, faces nt x 3).
+  void set_horizon_mesh(const std::vector<float>& verts, const std::vector<int32_t>& faces) {
+    hverts_ = verts;
+    hfaces_ = faces;
+  }
   void make_horizons(int nphi = 361, double theta_eps = 1e-3, double offset = 1e-5) {
-    check(ilg_make_horizons(h_, nphi, theta_eps, offset));
+    if (hfaces_.empty())
+      check(ilg_make_horizons(h_, nphi, theta_eps, offset));
+    else
+      check(ilg_make_horizons_mesh(h_, hverts_.data(), (int)(hverts_.size() / 3), hfaces_.data(),
+                                   (int)(hfaces_.size() / 3), nphi, theta_eps, offset));
     nphi_ = nphi;
   }
   // nphi x N column-major, as the reference's arma::mat horizons.
@@ -94,6 +105,14 @@ class illum_context {
     return x;
   }
 
+  // The reference's own solve (illum_cli.cpp:425-433): forward solve plus
+  // gs_steps natural-order Gauss-Seidel sweeps.
+  std::vector<double> radiosity_gs(const std::vector<double>& E, int gs_steps = 1, double* res = nullptr) {
+    std::vector<double> x(num_faces);
+    check(ilg_radiosity_solve_gs(h_, E.data(), gs_steps, x.data(), res));
+    return x;
+  }
+
   ilg_ctx* handle() { return h_; }
   const int num_faces;
 
@@ -111,6 +130,8 @@ class illum_context {
   }
   ilg_ctx* h_ = nullptr;
   int nphi_ = 0;
+  std::vector<float> hverts_;
+  std::vector<int32_t> hfaces_;
 };
 
 class thermal_model {

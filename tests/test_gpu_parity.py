@@ -447,3 +447,27 @@ def test_horizons_with_separate_mesh_bit_exact(ilg, oracle_mod):
     own.make_horizons(nphi=24)
     assert np.array_equal(own.horizons.T, oracle_mod.horizons(v, f, 24))
     assert (own.horizons > ctx.horizons + 1e-3).mean() > 0.2
+
+
+def test_visibility_sample_counts_match_F(ilg):
+    """Sampled visibility (no F built): every source listed gives exactly the
+    column counts of the form factors computed with the same cutoff, and the
+    within-radius counts follow the entries' centroid distances."""
+    v, f = meshgen.heightmap_terrain(n=65, spacing_m=2.0, seed=5, rms_m=6.0, n_bowls=8, dmin_m=10.0, dmax_m=50.0)
+    ctx = ilg.IllumContext(v, f)
+    cut = 0.04
+    rp, col, val = ctx.compute_F(albedo=0.1, cutoff=cut)
+    n = f.shape[0]
+    colcount = np.bincount(col, minlength=n)
+    allsrc = ctx.visibility_sample(np.arange(n), cutoff=cut, radii=[0.01, 0.02, cut])
+    assert np.array_equal(allsrc["per_source"], colcount)
+    assert allsrc["within_radius"][-1] == len(val)
+    assert allsrc["rays"] == ctx.visibility_rays
+    rows = np.repeat(np.arange(n), np.diff(rp))
+    cen = v[f].astype(np.float64).mean(axis=1)
+    d = np.linalg.norm(cen[rows] - cen[col], axis=1)
+    for r, w in zip([0.01, 0.02], allsrc["within_radius"][:2]):
+        assert abs(int(w) - int(np.count_nonzero(d <= r))) <= 2     # float centroids vs the float64 recomputation
+    sub = np.random.default_rng(3).choice(n, 300, replace=False).astype(np.int32)
+    part = ctx.visibility_sample(sub, cutoff=cut)
+    assert np.array_equal(part["per_source"], colcount[sub])
