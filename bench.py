@@ -436,7 +436,43 @@ def mixed_radiosity_bytes(F, rounds, sweeps, N):
     return rounds * (se * 6 + N * 32) + sweeps * (se * 4 + F["active_rows"] * 4 + N * 16)
 
 
-def nested_terrain(ig, meshgen, n, cutoff_m, K, W):
+# Device bytes per stored form-factor entry: resident (CSR 4 + 8, row tiles
+# 2 + 4 + 4 + 2) and at the peak of the build (candidate keys, values,
+# compaction and the device tile build's sort buffers on top).
+F_BYTES_RESIDENT = 24
+F_BYTES_PEAK = 80
+TERRAIN_RADII_M = (30.0, 45.0, 60.0, 90.0, 120.0, 200.0, 400.0, 1000.0, 2000.0)
+
+
+def terrain_cutoff_sizing(ctx, N, F, cutoff_m, frac, hbm_bytes=250e9):
+    """The configured 2 km cutoff, sized without building F: visibility of a
+    seeded sample of source facets with the 2 km cutoff, giving per source
+    the entries its column would hold (nnz estimate N x mean, standard error
+    N x std / sqrt(n)) and the sample's entries within each radius. The
+    largest listed radius whose estimated matrix fits the device at the
+    build's peak is reported beside the cutoff the run used."""
+    if frac <= 0:
+        return None
+    import numpy as np
+    from illum_gb300 import meshgen
+    n = max(16, int(round(frac * N)))
+    order = np.argsort(meshgen.uniform(77, 1, N))
+    src = np.sort(order[:n]).astype(np.int32)
+    t0 = time.perf_counter()
+    r = ctx.visibility_sample(src, cutoff=2.0, radii=[x / 1000.0 for x in TERRAIN_RADII_M])
+    el = time.perf_counter() - t0
+    per = r["per_source"].astype(np.float64)
+    est = {f"{int(x)} m": float(w) * N / n for x, w in zip(TERRAIN_RADII_M, r["within_radius"])}
+    fit = [x for x, w in zip(TERRAIN_RADII_M, r["within_radius"]) if float(w) * N / n * F_BYTES_PEAK <= hbm_bytes]
+    return {"sample_sources": n, "sample_seed": 77, "rays": r["rays"], "seconds": el,
+            "nnz_2km_estimate": float(per.mean() * N), "nnz_2km_stderr": float(per.std(ddof=1) * N / np.sqrt(n)),
+            "nnz_estimate_by_cutoff": est, "bytes_per_entry_peak": F_BYTES_PEAK,
+            "bytes_per_entry_resident": F_BYTES_RESIDENT, "device_budget_bytes": hbm_bytes,
+            "largest_listed_cutoff_fitting_m": max(fit) if fit else None, "run_cutoff_m": cutoff_m,
+            "run_nnz": F["nnz"], "run_nnz_estimate_from_sample": est.get(f"{int(cutoff_m)} m")}
+
+
+def nested_terrain(ig, meshgen, n, cutoff_m, K, W, sample_frac=0.0025):
     """Heightmap terrain patch (fBm + power-law bowls) with form factors
     within a distance cutoff, 128 horizon azimuths, radiosity refined to
     rel_tol of ||E|| at noon: mixed precision, then FP64 on the same context
@@ -465,6 +501,7 @@ def nested_terrain(ig, meshgen, n, cutoff_m, K, W):
     t_ff = time.perf_counter() - t0
     rays = int(ctx.visibility_rays)
     F = ctx.F_info()
+    sizing = terrain_cutoff_sizing(ctx, N, F, cutoff_m, sample_frac)
     ctx.set_insolation(1, 0, CFG["solar"])
     ctx.set_suns(suns, disk)
     E = ctx.get_direct_radiosity(suns[0], disk)
@@ -521,6 +558,7 @@ def nested_terrain(ig, meshgen, n, cutoff_m, K, W):
             "visibility_rays": rays, "phases_ms_per_step": res["phases"], "roofline_radiosity": roof,
             "setup_s": {"mesh_s": t_mesh, "bvh_s": t_bvh, "horizons_s": t_hor, "form_factors_s": t_ff},
             "horizon_rays_per_s": N * c["nphi"] * 11 / t_hor, "visibility_rays_per_s": rays / t_ff,
+            "cutoff_sizing": sizing,
             "clocks": m["clocks"], "fp64_clocks": d["clocks"], "gpu_launches": 5 * K}
 
 
@@ -621,7 +659,8 @@ def standalone(args, ig, meshgen):
     if args.workload == "batch":
         d = nested_batch(ig, meshgen, args.nested_steps, max(3, args.warmup))
     elif args.workload == "terrain":
-        d = nested_terrain(ig, meshgen, args.terrain_n, args.terrain_cutoff_m, args.nested_steps, max(3, args.warmup))
+        d = nested_terrain(ig, meshgen, args.terrain_n, args.terrain_cutoff_m, args.nested_steps, max(3, args.warmup),
+                           args.terrain_sample)
     else:
         d = nested_serve(ig, args.serve_requests, args.serve_scale, args.serve_rate)
     line = {"metric": METRIC, "n_gpus": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -647,6 +686,8 @@ def main():
                     help="c1: the default line; batch / terrain / serve: that nested object alone as the line")
     ap.add_argument("--terrain-n", type=int, default=1024, help="terrain grid points per side (1024: 2,093,058 facets)")
     ap.add_argument("--terrain-cutoff-m", type=float, default=30.0, help="form-factor cutoff (the terrain configuration states 2000 m)")
+    ap.add_argument("--terrain-sample", type=float, default=0.0025,
+                    help="fraction of source facets whose visibility at the configured 2 km cutoff sizes F (0: skip)")
     ap.add_argument("--serve-requests", type=int, default=500)
     ap.add_argument("--serve-scale", type=float, default=0.02, help="step-count scale of the serving sample")
     ap.add_argument("--serve-rate", type=float, default=20.0, help="Poisson arrival rate of the serving stream (1/s)")
@@ -772,7 +813,7 @@ def main():
                 nested[name] = nested_batch(ig, meshgen, args.nested_steps, max(3, min(args.warmup, 10)))
             elif name == "terrain":
                 nested[name] = nested_terrain(ig, meshgen, args.terrain_n, args.terrain_cutoff_m, args.nested_steps,
-                                              max(3, min(args.warmup, 10)))
+                                              max(3, min(args.warmup, 10)), args.terrain_sample)
             elif name == "serve":
                 nested[name] = nested_serve(ig, args.serve_requests, args.serve_scale, args.serve_rate)
         except Exception as e:  # reported, not hidden

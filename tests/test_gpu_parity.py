@@ -461,7 +461,9 @@ def test_visibility_sample_counts_match_F(ilg):
     colcount = np.bincount(col, minlength=n)
     allsrc = ctx.visibility_sample(np.arange(n), cutoff=cut, radii=[0.01, 0.02, cut])
     assert np.array_equal(allsrc["per_source"], colcount)
-    assert allsrc["within_radius"][-1] == len(val)
+    # the cutoff compares float squared distances, the radii double distances:
+    # pairs within rounding of the cutoff may fall on either side
+    assert abs(int(allsrc["within_radius"][-1]) - len(val)) <= 2
     assert allsrc["rays"] == ctx.visibility_rays
     rows = np.repeat(np.arange(n), np.diff(rp))
     cen = v[f].astype(np.float64).mean(axis=1)
