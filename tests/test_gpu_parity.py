@@ -469,7 +469,8 @@ def test_visibility_sample_counts_match_F(ilg):
     cen = v[f].astype(np.float64).mean(axis=1)
     d = np.linalg.norm(cen[rows] - cen[col], axis=1)
     for r, w in zip([0.01, 0.02], allsrc["within_radius"][:2]):
-        assert abs(int(w) - int(np.count_nonzero(d <= r))) <= 2     # float centroids vs the float64 recomputation
+        exp = int(np.count_nonzero(d <= r))
+        assert abs(int(w) - exp) <= 2 + 1e-4 * exp     # float centroids vs the float64 recomputation
     sub = np.random.default_rng(3).choice(n, 300, replace=False).astype(np.int32)
     part = ctx.visibility_sample(sub, cutoff=cut)
     assert np.array_equal(part["per_source"], colcount[sub])
