@@ -817,31 +817,7 @@ __global__ void k_row_keys(const int64_t* __restrict__ rowptr, const int32_t* __
   }
 }
 
-// Tile build on the device. Per Morton position p: an upper bound on the
-// halo facets row order[p] adds to a tile that already holds row
-// order[p - 1], i.e. its columns not among that row's (both column lists
-// ascending in Morton rank; an empty previous row bounds it by the row's
-// length). The host cuts tiles with these bounds, so a tile's exact halo
-// is never larger than its bound.
-__global__ void k_halo_inc(const int64_t* __restrict__ rowptr, const uint32_t* __restrict__ order,
-                           const unsigned long long* __restrict__ skey, unsigned long long cmask, int nt, int* inc) {
-  int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= nt) return;
-  const int g = (int)order[p];
-  const int64_t a0 = rowptr[g], a1 = rowptr[g + 1];
-  if (p == 0) { inc[p] = (int)(a1 - a0); return; }
-  const int h = (int)order[p - 1];
-  int64_t j = rowptr[h];
-  const int64_t b1 = rowptr[h + 1];
-  int cnt = 0;
-  for (int64_t k = a0; k < a1; ++k) {
-    const unsigned long long c = skey[k] & cmask;
-    while (j < b1 && (skey[j] & cmask) < c) ++j;
-    if (j >= b1 || (skey[j] & cmask) != c) ++cnt;
-  }
-  inc[p] = cnt;
-}
-
+// Tile build on the device.
 // key = (tile of the entry's row) << rb | Morton rank of its column; value =
 // the entry's index in the row-sorted order.
 __global__ void k_tile_keys(const unsigned long long* __restrict__ skey, int64_t n, int rb,
@@ -992,7 +968,6 @@ int radiosity_prepare(Context& c) {
   while ((1 << rb) < nt) ++rb;
   std::vector<int64_t> rp((size_t)nt + 1);
   std::vector<uint32_t> order((size_t)nt);
-  std::vector<int> hinc((size_t)nt, 0);
   ILG_CUDA(cudaMemcpyAsync(rp.data(), c.rowptr.p, rp.size() * 8, cudaMemcpyDeviceToHost, s));
   ILG_CUDA(cudaMemcpyAsync(order.data(), c.morton_order.p, (size_t)nt * 4, cudaMemcpyDeviceToHost, s));
   dbuf<unsigned long long> dkey;
@@ -1000,19 +975,14 @@ int radiosity_prepare(Context& c) {
   const unsigned long long cmask = (1ull << rb) - 1;
   if (nnz > 0) {
     dbuf<uint32_t> drank;
-    dbuf<int> dinc;
     ILG_TRY(drank.alloc(nt));
     ILG_TRY(dkey.alloc(nnz));
     ILG_TRY(dsv.alloc(nnz));
-    ILG_TRY(dinc.alloc(nt));
     k_rank<<<div_up(nt, 256), 256, 0, s>>>(c.morton_order.p, nt, drank.p);
     ILG_CUDA(cudaGetLastError());
     k_row_keys<<<div_up(nt, 256), 256, 0, s>>>(c.rowptr.p, c.col.p, drank.p, nt, rb, dkey.p, dsv.p);
     ILG_CUDA(cudaGetLastError());
     ILG_TRY(radix_sort_u64(dkey.p, dsv.p, nnz, 2 * rb, c.sort, s));
-    k_halo_inc<<<div_up(nt, 256), 256, 0, s>>>(c.rowptr.p, c.morton_order.p, dkey.p, cmask, nt, dinc.p);
-    ILG_CUDA(cudaGetLastError());
-    ILG_CUDA(cudaMemcpyAsync(hinc.data(), dinc.p, (size_t)nt * 4, cudaMemcpyDeviceToHost, s));
   }
   ILG_CUDA(cudaStreamSynchronize(s));
 
@@ -1038,23 +1008,33 @@ int radiosity_prepare(Context& c) {
   // runs ceil(entries / 4096) groups of four), so tiles get equal group
   // counts: the smallest ng for which a greedy pass with at most ng * 4096
   // entries per tile needs no more tiles than co-resident blocks. A second
-  // pass also closes a tile early once its weighed cost (entries + rows +
-  // halo facets) exceeds ng * 4096 plus the first pass's mean row and halo
-  // cost, so row- and halo-heavy tiles carry fewer entries; it is kept if it
-  // still fits the grid. If the halo or row caps force more tiles than
-  // blocks (very large meshes), the cuts are equal shares of the estimated
-  // work (entries + rows), several tiles per block. A tile's halo is counted
-  // with the per-row bounds (a tile's first row adds all its columns), so it
-  // never exceeds the exact halo found on the device afterwards.
+  // pass also closes a tile early once its weighed cost (entries + rows)
+  // exceeds ng * 4096 plus the first pass's mean row cost, so row-heavy
+  // tiles carry fewer entries; it is kept if it still fits the grid. If the
+  // row cap forces more tiles than blocks (very large meshes), the cuts are
+  // equal shares of the estimated work (entries + rows), several tiles per
+  // block. Halos are then counted exactly on the device and a tile whose
+  // halo exceeds the shared-memory capacity is split in two, until none
+  // does.
   const int G = g_rad_nsm * std::min(g_rad_per_sm64, g_rad_per_smm);
   std::vector<RowTile> tiles;
   std::vector<size_t> tile_a;   // first active row of each tile
   std::vector<int64_t> tile_ne;  // entries of each tile
   const int64_t NOCAP = std::numeric_limits<int64_t>::max() / 4;
+  auto rlen = [&](size_t q) { const int g = (int)order[arow[q]]; return rp[g + 1] - rp[g]; };
+  auto push_tile = [&](size_t a, size_t b, int64_t ne) {
+    RowTile T{};
+    T.lam = (int)(((ne + RAD_THREADS - 1) / RAD_THREADS + 3) & ~(int64_t)3);
+    T.nrows = (int)(b - a);
+    T.mesh = 0;
+    tiles.push_back(T);
+    tile_a.push_back(a);
+    tile_ne.push_back(ne);
+  };
   // One greedy pass. cap > 0: at most cap entries and cap + slack weighed
   // cost per tile; returns false once more than max_tiles are needed, and
-  // counts the tiles closed by the halo or row caps. cap == 0: cumulative
-  // equal shares of total_cost over ntarget tiles.
+  // counts the tiles closed by the row cap. cap == 0: cumulative equal
+  // shares of total_cost over ntarget tiles.
   auto cut = [&](int64_t cap, int64_t slack, int64_t total_cost, int64_t ntarget, size_t max_tiles,
                  int* capped) -> bool {
     tiles.clear();
@@ -1067,38 +1047,21 @@ int radiosity_prepare(Context& c) {
       if (tiles.size() >= max_tiles) return false;
       const int tid = (int)tiles.size();
       const int64_t bound = cap > 0 ? 0 : (int64_t)((double)total_cost * (double)(tid + 1) / (double)ntarget);
-      int64_t nhalo = 0;
       size_t b = a;
       int64_t ne = 0;
       while (b < arow.size()) {
-        int g = (int)order[arow[b]];
         if (b > a && (int64_t)(b - a) >= RAD_ROWS) {
           if (capped) ++*capped;
           break;
         }
-        const int64_t len = rp[g + 1] - rp[g];
+        const int64_t len = rlen(b);
         if (cap > 0 && b > a && ne + len > cap) break;
-        const int64_t nh = nhalo + (b == a ? len : (int64_t)hinc[arow[b]]);
-        const bool over_halo = nh > RAD_HALO;
-        const bool over_cost =
-            cap > 0 && ne + len + RAD_ROW_COST * (int64_t)(b - a + 1) + RAD_HALO_COST * nh > cap + slack;
-        if (b > a && (over_halo || over_cost)) {
-          if (over_halo && capped) ++*capped;
-          break;
-        }
-        nhalo = nh;
+        if (cap > 0 && b > a && ne + len + RAD_ROW_COST * (int64_t)(b - a + 1) > cap + slack) break;
         ne += len;
         ++b;
         if (cap == 0 && done_cost + ne + RAD_ROW_COST * (int64_t)(b - a) >= bound && tid + 1 < ntarget) break;
       }
-      RowTile T{};
-      T.lam = (int)(((ne + RAD_THREADS - 1) / RAD_THREADS + 3) & ~(int64_t)3);
-      T.nrows = (int)(b - a);
-      T.nhalo = (int)nhalo;
-      T.mesh = 0;
-      tiles.push_back(T);
-      tile_a.push_back(a);
-      tile_ne.push_back(ne);
+      push_tile(a, b, ne);
       done_cost += ne + RAD_ROW_COST * (int64_t)(b - a);
       a = b;
     }
@@ -1111,11 +1074,11 @@ int radiosity_prepare(Context& c) {
     int capped = 0;
     for (int tries = 0; tries < 4; ++tries, ++ng) {
       ok = cut(ng * RAD_GROUP, NOCAP, 0, 0, (size_t)G, &capped);
-      if (ok || capped > 0) break;   // a larger ng cannot lift the halo / row caps
+      if (ok || capped > 0) break;   // a larger ng cannot lift the row cap
     }
     if (ok && !tiles.empty()) {
       int64_t extra = 0;
-      for (const RowTile& T : tiles) extra += RAD_ROW_COST * T.nrows + RAD_HALO_COST * T.nhalo;
+      for (const RowTile& T : tiles) extra += RAD_ROW_COST * T.nrows;
       const int64_t slack = extra / (int64_t)tiles.size();
       if (!cut(ng * RAD_GROUP, slack, 0, 0, (size_t)G, nullptr)) cut(ng * RAD_GROUP, NOCAP, 0, 0, (size_t)G, nullptr);
     } else if (!ok) {
@@ -1125,45 +1088,49 @@ int radiosity_prepare(Context& c) {
     }
   }
   // per row: its tile and first entry within the tile; per tile: stored
-  // offset and rows
-  const int ntile = (int)tiles.size();
+  // offset and rows; then the exact halos on the device (the entries
+  // sorted by (tile, column): runs = halo facets), splitting over-full tiles
   std::vector<int> tile_of((size_t)nt, 0), rowoff((size_t)nt, 0);
   std::vector<uint32_t> trow(arow.size());
   std::vector<int> rowj0(arow.size());
-  int64_t stored_total = 0, rows_total = 0;
-  for (int tid = 0; tid < ntile; ++tid) {
-    RowTile& T = tiles[tid];
-    T.e0 = stored_total;
-    T.r0 = (int)rows_total;
-    stored_total += (int64_t)T.lam * RAD_THREADS;
-    int64_t j = 0;
-    for (int q = 0; q < T.nrows; ++q) {
-      const int p = arow[tile_a[tid] + q];
-      const int g = (int)order[p];
-      tile_of[g] = tid;
-      rowoff[g] = (int)j;
-      trow[(size_t)rows_total + q] = (uint32_t)p;
-      rowj0[(size_t)rows_total + q] = (int)j;
-      j += rp[g + 1] - rp[g];
-    }
-    rows_total += T.nrows;
-  }
-  // exact halos on the device: the entries sorted by (tile, column), runs =
-  // halo facets
-  std::vector<int> tfirst((size_t)ntile + 1, 0);
+  std::vector<int> tfirst;
+  int64_t stored_total = 0;
+  int ntile = 0;
   dbuf<uint32_t> t_halo_tmp;
-  if (ntile > 0) {
-    dbuf<int> dtile_of, drowoff, dtfirst;
-    dbuf<unsigned long long> key2, before;
-    dbuf<uint32_t> idx2, flag;
+  dbuf<int> dtile_of, drowoff, dtfirst;
+  dbuf<unsigned long long> key2, before;
+  dbuf<uint32_t> idx2, flag;
+  if (!tiles.empty()) {
     ILG_TRY(dtile_of.alloc(nt));
     ILG_TRY(drowoff.alloc(nt));
     ILG_TRY(key2.alloc(nnz));
     ILG_TRY(idx2.alloc(nnz));
     ILG_TRY(flag.alloc(nnz));
     ILG_TRY(before.alloc(nnz));
-    ILG_TRY(dtfirst.alloc(ntile + 1));
     ILG_TRY(t_halo_tmp.alloc(nnz));
+  }
+  for (int iter = 0; !tiles.empty(); ++iter) {
+    ntile = (int)tiles.size();
+    stored_total = 0;
+    int64_t rows_total = 0;
+    for (int tid = 0; tid < ntile; ++tid) {
+      RowTile& T = tiles[tid];
+      T.e0 = stored_total;
+      T.r0 = (int)rows_total;
+      stored_total += (int64_t)T.lam * RAD_THREADS;
+      int64_t j = 0;
+      for (int q = 0; q < T.nrows; ++q) {
+        const int p = arow[tile_a[tid] + q];
+        const int g = (int)order[p];
+        tile_of[g] = tid;
+        rowoff[g] = (int)j;
+        trow[(size_t)rows_total + q] = (uint32_t)p;
+        rowj0[(size_t)rows_total + q] = (int)j;
+        j += rp[g + 1] - rp[g];
+      }
+      rows_total += T.nrows;
+    }
+    ILG_TRY(dtfirst.reserve(ntile + 1));
     ILG_CUDA(cudaMemcpyAsync(dtile_of.p, tile_of.data(), (size_t)nt * 4, cudaMemcpyHostToDevice, s));
     ILG_CUDA(cudaMemcpyAsync(drowoff.p, rowoff.data(), (size_t)nt * 4, cudaMemcpyHostToDevice, s));
     k_tile_keys<<<div_up(nnz, 256), 256, 0, s>>>(dkey.p, nnz, rb, dtile_of.p, key2.p, idx2.p);
@@ -1176,6 +1143,7 @@ int radiosity_prepare(Context& c) {
     ILG_TRY(scan_exclusive_u32_to_u64(flag.p, before.p, nnz, c.scan, s));
     k_halo_runs<<<div_up(nnz, 256), 256, 0, s>>>(key2.p, flag.p, before.p, nnz, rb, t_halo_tmp.p, dtfirst.p);
     ILG_CUDA(cudaGetLastError());
+    tfirst.assign((size_t)ntile + 1, 0);
     unsigned long long last_before = 0;
     uint32_t last_flag = 0;
     ILG_CUDA(cudaMemcpyAsync(tfirst.data(), dtfirst.p, (size_t)ntile * 4, cudaMemcpyDeviceToHost, s));
@@ -1183,12 +1151,48 @@ int radiosity_prepare(Context& c) {
     ILG_CUDA(cudaMemcpyAsync(&last_flag, flag.p + nnz - 1, 4, cudaMemcpyDeviceToHost, s));
     ILG_CUDA(cudaStreamSynchronize(s));
     tfirst[ntile] = (int)(last_before + last_flag);
+    bool split = false;
+    std::vector<RowTile> nt_tiles;
+    std::vector<size_t> nt_a;
+    std::vector<int64_t> nt_ne;
     for (int tid = 0; tid < ntile; ++tid) {
-      RowTile& T = tiles[tid];
+      RowTile T = tiles[tid];
       T.h0 = tfirst[tid];
       T.nhalo = tfirst[tid + 1] - tfirst[tid];
-      if (T.nhalo > RAD_HALO || T.nhalo < 1) { set_error("row tile halo of %d facets", T.nhalo); return ILG_ERR_CUDA; }
+      if (T.nhalo < 1) { set_error("row tile without a halo"); return ILG_ERR_CUDA; }
+      if (T.nhalo <= RAD_HALO || T.nrows < 2) {
+        if (T.nhalo > RAD_HALO) { set_error("row tile halo of %d facets", T.nhalo); return ILG_ERR_CUDA; }
+        nt_tiles.push_back(T);
+        nt_a.push_back(tile_a[tid]);
+        nt_ne.push_back(tile_ne[tid]);
+        continue;
+      }
+      // split at the row where the entries reach half
+      split = true;
+      const size_t a = tile_a[tid], b = a + T.nrows;
+      size_t m = a;
+      int64_t ne0 = 0;
+      while (m + 1 < b && 2 * (ne0 + rlen(m)) <= tile_ne[tid]) ne0 += rlen(m++);
+      if (m == a) ne0 += rlen(m++);
+      for (int half = 0; half < 2; ++half) {
+        const size_t ha = half ? m : a, hb = half ? b : m;
+        const int64_t hne = half ? tile_ne[tid] - ne0 : ne0;
+        RowTile H{};
+        H.lam = (int)(((hne + RAD_THREADS - 1) / RAD_THREADS + 3) & ~(int64_t)3);
+        H.nrows = (int)(hb - ha);
+        H.mesh = 0;
+        nt_tiles.push_back(H);
+        nt_a.push_back(ha);
+        nt_ne.push_back(hne);
+      }
     }
+    tiles.swap(nt_tiles);
+    tile_a.swap(nt_a);
+    tile_ne.swap(nt_ne);
+    if (!split) break;
+    if (iter > 40) { set_error("row tiles: halos do not fit after %d splits", iter); return ILG_ERR_CUDA; }
+  }
+  if (ntile > 0) {
     c.ntiles = ntile;
     c.tile_elems = stored_total;
     c.tiles_h = tiles;
