@@ -116,6 +116,7 @@ _SIGS = {
     "ilg_batch_destroy": (C.c_int, [C.c_void_p]),
     "ilg_batch_run": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "ilg_batch_bench": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_void_p]),
+    "ilg_batch_bench_phases": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_void_p, C.c_void_p]),
     "ilg_batch_status": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "ilg_batch_set_active": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "ilg_batch_get_tsurf": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
@@ -519,6 +520,13 @@ class Batch:
         ms = np.zeros(nsteps)
         _check(lib().ilg_batch_bench(self._h, nsteps, flush_mb, _p(ms)))
         return ms
+
+    def bench_phases(self, nsteps, flush_mb=256.0):
+        """Eager serial steps; returns (step_ms, [direct, radiosity, conduction] ms summed)."""
+        ms = np.zeros(nsteps)
+        ph = np.zeros(3)
+        _check(lib().ilg_batch_bench_phases(self._h, nsteps, flush_mb, _p(ms), _p(ph)))
+        return ms, ph
 
     def status(self):
         a = np.zeros(self.n, np.int32); d = np.zeros(self.n, np.int32); w = np.zeros(self.n, np.int32)

@@ -425,6 +425,33 @@ int ilg_batch_bench(ilg_batch* batch, int nsteps, double flush_mb, double* step_
   return batch_errors(b);
 }
 
+// Eager steps in the serial order (no graph, no pipelining) with their
+// phase boundaries recorded: phase_ms[0..2] accumulates the direct,
+// radiosity and conduction phases of all members.
+int ilg_batch_bench_phases(ilg_batch* batch, int nsteps, double flush_mb, double* step_ms, double* phase_ms) {
+  if (!batch || nsteps < 0 || !step_ms || !phase_ms) { set_error("invalid arguments"); return ILG_ERR_ARG; }
+  Batch& b = batch->b;
+  AllocOn on_(b.stream);
+  size_t nflush = flush_mb > 0 ? (size_t)(flush_mb * 1048576.0 / 16.0) : 0;
+  if (nflush) ILG_TRY(b.flush.reserve(nflush));
+  phase_ms[0] = phase_ms[1] = phase_ms[2] = 0.0;
+  for (int s = 0; s < nsteps; ++s) {
+    if (nflush) ILG_TRY(flush_launch(b.flush.p, nflush, (unsigned)s, b.stream));
+    ILG_TRY(enqueue_step(b.v, b.plan, b.stream, b.ev));
+    ILG_CUDA(cudaEventSynchronize(b.ev[3]));
+    float p0, p1, p2;
+    ILG_CUDA(cudaEventElapsedTime(&p0, b.ev[0], b.ev[1]));
+    ILG_CUDA(cudaEventElapsedTime(&p1, b.ev[1], b.ev[2]));
+    ILG_CUDA(cudaEventElapsedTime(&p2, b.ev[2], b.ev[3]));
+    step_ms[s] = (double)p0 + p1 + p2;
+    phase_ms[0] += p0;
+    phase_ms[1] += p1;
+    phase_ms[2] += p2;
+  }
+  ILG_CUDA(cudaStreamSynchronize(b.stream));
+  return batch_errors(b);
+}
+
 int ilg_batch_status(ilg_batch* batch, int* active, int* steps_done, int* sweeps) {
   if (!batch) { set_error("batch is NULL"); return ILG_ERR_ARG; }
   Batch& b = batch->b;

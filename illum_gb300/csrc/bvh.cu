@@ -1013,7 +1013,15 @@ int form_factors_build(Context& c, const double* albedo_h, double albedo_scalar,
   ILG_CUDA(cudaStreamSynchronize(s));
   c.nnz = nnz;
   c.have_F = true;
+  keys.release();
+  keep.release();
+  fval.release();
+  pos.release();
+  rows.release();
   ILG_TRY(radiosity_prepare(c));
+  // the sort and scan scratch grew to the entry count: not kept resident
+  c.sort.release();
+  c.scan.release();
   return read_device_errors(c);
 }
 

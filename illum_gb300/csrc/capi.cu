@@ -638,7 +638,10 @@ int ilg_set_F(ilg_ctx* ctx, int64_t nnz, const int64_t* rowptr, const int32_t* c
   c.nnz = nnz;
   c.have_F = true;
   c.gs_ready = false;
-  return radiosity_prepare(c);
+  ILG_TRY(radiosity_prepare(c));
+  c.sort.release();
+  c.scan.release();
+  return ILG_OK;
 }
 
 int ilg_make_horizons(ilg_ctx* ctx, int nphi, double theta_eps, double offset) {

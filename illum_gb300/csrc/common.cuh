@@ -136,7 +136,10 @@ enum DevErr : int {
 // Exclusive prefix sum of n 64-bit counts; out may alias in. Uses tmp
 // scratch grown on demand. *total receives the sum when non-null (device->host
 // copy, synchronising the stream).
-struct ScanScratch { dbuf<unsigned long long> a, b, c; };
+struct ScanScratch {
+  dbuf<unsigned long long> a, b, c;
+  void release() { a.release(); b.release(); c.release(); }
+};
 int scan_exclusive_u64(const unsigned long long* in, unsigned long long* out, int64_t n,
                        ScanScratch& tmp, cudaStream_t s);
 int scan_exclusive_u32_to_u64(const uint32_t* in, unsigned long long* out, int64_t n,
@@ -149,6 +152,7 @@ struct SortScratch {
   dbuf<uint32_t> vals_alt;
   dbuf<unsigned long long> hist;
   ScanScratch scan;
+  void release() { keys_alt.release(); vals_alt.release(); hist.release(); scan.release(); }
 };
 int radix_sort_u64(unsigned long long* keys, uint32_t* vals, int64_t n, int bits, SortScratch& tmp,
                    cudaStream_t s);

@@ -314,6 +314,9 @@ int ilg_batch_run(ilg_batch* batch, int nsteps, int use_graph);
 int ilg_batch_bench(ilg_batch* batch, int nsteps, double flush_mb, double* step_ms);
 /* per member (arrays of n, any may be NULL): still active, steps done in
  * total (including before this batch), radiosity sweeps of the last step */
+/* Eager steps in the serial order with per-phase device times summed into
+ * phase_ms[0..2] (direct, radiosity, conduction); step_ms[s] = their sum. */
+int ilg_batch_bench_phases(ilg_batch* batch, int nsteps, double flush_mb, double* step_ms, double* phase_ms);
 int ilg_batch_status(ilg_batch* batch, int* active, int* steps_done, int* sweeps);
 int ilg_batch_set_active(ilg_batch* batch, int member, int active);
 int ilg_batch_get_tsurf(ilg_batch* batch, int member, double* out);
