@@ -82,6 +82,7 @@ _SIGS = {
     "ilg_set_F": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]),
     "ilg_F_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int),
                              C.POINTER(C.c_int)]),
+    "ilg_F_tiles": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_int)]),
     "ilg_make_horizons": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_double]),
     "ilg_make_horizons_mesh": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_double,
                                          C.c_double]),
@@ -272,6 +273,14 @@ class IllumContext:
         c, d = C.c_int(), C.c_int()
         _check(lib().ilg_F_info(self._h, C.byref(a), C.byref(b), C.byref(c), C.byref(d)))
         return {"nnz": a.value, "stored_entries": b.value, "row_tiles": c.value, "active_rows": d.value}
+
+    def F_tiles(self):
+        """Per radiosity row tile: entries per thread, rows, halo facets."""
+        n = C.c_int()
+        _check(lib().ilg_F_tiles(self._h, 0, None, None, None, C.byref(n)))
+        lam, rows, halo = (np.zeros(n.value, np.int32) for _ in range(3))
+        _check(lib().ilg_F_tiles(self._h, n.value, _p(lam), _p(rows), _p(halo), C.byref(n)))
+        return {"entries_per_thread": lam, "rows": rows, "halo": halo}
 
     def set_F(self, rowptr, col, val):
         rowptr = np.ascontiguousarray(rowptr, np.int64); col = np.ascontiguousarray(col, np.int32); val = _f64(val)

@@ -69,6 +69,7 @@ int read_device_errors(Context& c) {
   if (h[DERR_STACK]) { set_error("BVH traversal stack overflow"); return ILG_ERR_DEVICE; }
   if (h[DERR_BARRIER]) { set_error("radiosity grid barrier wait exceeded its limit"); return ILG_ERR_DEVICE; }
   if (h[DERR_HORIZON]) { set_error("horizon bisection deeper than its table"); return ILG_ERR_DEVICE; }
+  if (h[DERR_STREAM]) { set_error("radiosity entry-stream copy wait exceeded its limit"); return ILG_ERR_DEVICE; }
   set_error("device error flags set");
   return ILG_ERR_DEVICE;
 }
@@ -561,6 +562,19 @@ int ilg_F_info(const ilg_ctx* ctx, int64_t* nnz, int64_t* stored_entries, int* r
   if (stored_entries) *stored_entries = c.tile_elems;
   if (row_tiles) *row_tiles = c.ntiles;
   if (active_rows) *active_rows = c.n_active;
+  return ILG_OK;
+}
+
+int ilg_F_tiles(const ilg_ctx* ctx, int cap, int* entries_per_thread, int* rows, int* halo, int* ntiles) {
+  if (!ctx || !ctx->c.have_F || !ntiles || cap < 0) { set_error("invalid arguments"); return ILG_ERR_ARG; }
+  const Context& c = ctx->c;
+  *ntiles = c.ntiles;
+  for (int t = 0; t < c.ntiles && t < cap; ++t) {
+    const RowTile& T = c.tiles_h[t];
+    if (entries_per_thread) entries_per_thread[t] = T.lam;
+    if (rows) rows[t] = T.nrows;
+    if (halo) halo[t] = T.nhalo;
+  }
   return ILG_OK;
 }
 

@@ -129,6 +129,7 @@ enum DevErr : int {
   DERR_BARRIER = 2,    // grid barrier wait exceeded its iteration limit
   DERR_HORIZON = 3,    // horizon bisection deeper than the precomputed tree
   DERR_PIVOT = 4,      // zero pivot in a conduction column
+  DERR_STREAM = 5,     // radiosity entry-stream copy wait exceeded its iteration limit
   DERR_COUNT = 8
 };
 

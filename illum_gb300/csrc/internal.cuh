@@ -124,7 +124,7 @@ struct StepView {
   double *Tsurf, *Fsurf, *Qprev, *rad, *rad_avg, *therm_avg, *therm_max;
   double* E;                   // 2 x nt: the direct flux of frame f in slot f & 1 (before the
                                // coupling, which its readers apply); a drop-in direct call writes slot 0
-  double* sprev;               // 2 x nt: scattered radiosity x - E of the last solve, and its change
+  double* sprev;               // 2 x nt by radiosity position: scattered radiosity x - E of the last solve, and its change
   float* x32;                  // 3 x nt (mixed radiosity)
   double* T64;                 // [nz][nt] fp64 layers (standalone column entry points)
   float2* Tdf;                 // [nz][nt] double-float layers (the FP64 step)
@@ -143,7 +143,7 @@ struct StepView {
   const uint32_t *t_row, *t_halo, *t_start;   // tile rows and halos (positions); per-thread first row
   const float* t_scale;        // per tile row: bf16 scale
   double* tile_d2;             // 2 x ntiles residual partials
-  const uint8_t* row_act;      // per facet: its row has entries
+  const uint8_t* row_act;      // per radiosity position: its row has entries
   const uint32_t* rperm;       // radiosity position -> facet (Morton order within each mesh)
   double* rbuf;                // 6 x nt: E, two iterates, double-float copies of both and of E (radiosity positions)
   // conduction blocks: (mesh, first local facet), or nullptr for a single mesh
@@ -243,7 +243,7 @@ struct Context {
   int state_prec = 0;             // which of Tdf / T32 holds the state
   dbuf<double> Tsurf, Fsurf, Qprev;
   dbuf<double> rad, rad_avg, therm_avg, therm_max, E, xtmp, Q;
-  dbuf<double> sprev;             // 2 x N: x - E of the last radiosity solve, and its change
+  dbuf<double> sprev;             // 2 x N by radiosity position: x - E of the last radiosity solve, and its change
   int frame_no = 0;
   int rec_cap = 0, rec_frame0 = 0;  // thermal records (ilg_record_thermal)
   dbuf<double> rec, rec_part;

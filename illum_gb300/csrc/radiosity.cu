@@ -11,6 +11,10 @@
 // A tile's rows see a compact set of facets (its halo), so a block first
 // gathers the halo's x values into shared memory and then streams the tile's
 // entries, each a 16-bit halo index (plus a row-end bit) and a value. The
+// stream reaches shared memory by bulk copies (cp.async.bulk with mbarrier
+// completion) that one producer warp issues ahead of the 31 consumer warps,
+// so DRAM keeps working while the consumers gather the next tile's halo or
+// finish a tile's rows. The
 // tile's entries, row after row, are split into equal runs, one per thread
 // (entries of a row that straddles threads are combined in a fixed order),
 // so every thread of every block does the same amount of work whatever the
@@ -69,9 +73,10 @@ namespace ilg {
 
 namespace {
 
-constexpr int RAD_THREADS = 1024;
-constexpr int RAD_HALO = 16384;          // halo values per tile (double-float: 128 KB of shared memory)
-constexpr int RAD_ROWS = 6144;           // rows per tile (their sums: 48 KB of shared memory)
+constexpr int RAD_THREADS = 992;             // consumer threads (31 warps): one entry run each
+constexpr int RAD_BLOCK = RAD_THREADS + 32;  // and one producer warp that issues the entry-stream copies
+constexpr int RAD_HALO = 6144;           // halo values per tile (double-float: 48 KB of shared memory)
+constexpr int RAD_ROWS = 3072;           // rows per tile (their sums: 24 KB of shared memory)
 constexpr int RAD_MAX_MESH = 1024;
 constexpr int RAD_INNER = 2;             // most fp32 sweeps per refinement of the mixed solve: the bf16 error
                                          // (~4e-3 of the correction) already dominates rho^(k+1), rho ~ 0.013
@@ -82,9 +87,24 @@ constexpr int64_t RAD_MIN_TILE = 16384;  // entries: smaller tiles cost more in 
 // 81,920-facet mesh), i.e. a row costs ~7 entries and a halo facet ~1.
 constexpr int64_t RAD_ROW_COST = 7;
 constexpr int64_t RAD_HALO_COST = 1;
-constexpr int64_t RAD_GROUP = 4 * 1024;  // stored entries per group (4 per thread): a tile's stream is whole groups
-constexpr size_t RAD_SMEM =
-    (size_t)RAD_HALO * sizeof(float2) + RAD_THREADS * sizeof(float2) + RAD_ROWS * sizeof(float2) + RAD_THREADS;
+constexpr int64_t RAD_GROUP = 4 * RAD_THREADS;  // stored entries per group (4 per thread): a tile's stream is whole groups
+// One group in shared memory: its columns (u16), then its values (f32 hi,
+// f32 lo for the FP64 sweeps; f32 hi for the mixed residual; bf16 for the
+// mixed inner sweeps). Every piece is a multiple of 16 bytes, and a group
+// starts at a multiple of RAD_GROUP entries, so each is one bulk copy.
+constexpr int RAD_CF_BYTES = (int)RAD_GROUP * 2;
+constexpr int RAD_F32_BYTES = (int)RAD_GROUP * 4;
+constexpr int RAD_STAGE64 = RAD_CF_BYTES + 2 * RAD_F32_BYTES;   // FP64 sweeps: 3 stages
+constexpr int RAD_STAGEM = RAD_CF_BYTES + RAD_F32_BYTES;        // mixed solve: 5 stages
+constexpr int RAD_NST64 = 3;
+constexpr int RAD_NSTM = 5;
+constexpr int RAD_NST_MAX = 8;
+constexpr size_t RAD_RING = (size_t)(RAD_NST64 * RAD_STAGE64 > RAD_NSTM * RAD_STAGEM ? RAD_NST64 * RAD_STAGE64
+                                                                                        : RAD_NSTM * RAD_STAGEM);
+static_assert(RAD_CF_BYTES % 16 == 0 && RAD_F32_BYTES % 16 == 0, "bulk copies move multiples of 16 bytes");
+static_assert(RAD_NST64 <= RAD_NST_MAX && RAD_NSTM <= RAD_NST_MAX, "stage barriers");
+constexpr size_t RAD_SMEM = RAD_RING + (size_t)RAD_HALO * sizeof(float2) + RAD_THREADS * sizeof(float2) +
+                            RAD_ROWS * sizeof(float2) + RAD_THREADS + 2 * RAD_NST_MAX * sizeof(unsigned long long);
 
 // Most polls of one grid-barrier wait (about 2^26 x 32 ns before it gives
 // up). A device variable so that a test can shrink it (ilg_debug_barrier_
@@ -143,53 +163,150 @@ __device__ __forceinline__ uint64_t l2_keep_policy(int stream) {
     asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 0.75;" : "=l"(pol));
   return pol;
 }
-// L2 prefetch of the entry groups RAD_PF groups ahead of the one being
-// summed, for a matrix streamed from HBM: the register pipeline keeps two
-// groups in flight per thread, which at one 1024-thread block per SM is too
-// few bytes in flight to cover DRAM latency; prefetched lines arrive in L2
-// meanwhile.
-constexpr int RAD_PF = 6;
-__device__ __forceinline__ void pf_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
-__device__ __forceinline__ uint2 ld_mat(const uint2* p, uint64_t pol) {
-  uint2 r;
-  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v2.u32 {%0, %1}, [%2], %3;"
-               : "=r"(r.x), "=r"(r.y) : "l"(p), "l"(pol));
-  return r;
+// The entry stream of a block's tiles reaches shared memory by 1-D bulk
+// copies (cp.async.bulk) into a ring of stages: the producer warp's lane 0
+// waits until a stage is free (its empty barrier), announces the bytes on the
+// stage's full barrier and issues the copies; consumers wait on the full
+// barrier, read their four entries and arrive on the empty barrier. Both
+// sides walk the same sequence of (tile, group) pairs, numbered q from the
+// start of the launch: stage q % nst, use number q / nst, so each wait is on
+// the parity of that use. Every wait is bounded: after RAD_MBAR_POLLS polls
+// it records DERR_STREAM, and from then on the block's waits return at once
+// and its consumers treat the stream as empty (all-zero entries, which index
+// no halo value beyond slot 0 and end no row).
+constexpr long long RAD_MBAR_POLLS = 1LL << 22;
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
 }
-__device__ __forceinline__ float4 ld_mat_f4(const float* p, uint64_t pol) {
-  float4 r;
-  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
-               : "=f"(r.x), "=f"(r.y), "=f"(r.z), "=f"(r.w) : "l"(p), "l"(pol));
-  return r;
+__device__ __forceinline__ void mbar_arrive(unsigned long long* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
-// Value sources of tile_rows: four consecutive entries from offset off.
+__device__ __forceinline__ void mbar_expect(unsigned long long* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+// true once the use with this parity has completed; false after the poll
+// limit (flagged) or when the block's stream has already failed
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity, int* bad, int* derr) {
+  if (*(volatile int*)bad) return false;
+  const unsigned a = smem_u32(bar);
+  for (long long it = 0; it < RAD_MBAR_POLLS; ++it) {
+    unsigned done;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(done) : "r"(a), "r"(parity) : "memory");
+    if (done) return true;
+    if (*(volatile int*)bad) return false;
+  }
+  *(volatile int*)bad = 1;
+  atomicExch(&derr[DERR_STREAM], 1);
+  return false;
+}
+__device__ __forceinline__ void bulk_copy(unsigned dst, const void* src, unsigned bytes, unsigned long long* bar,
+                                          uint64_t pol) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;"
+      ::"r"(dst), "l"(src), "r"(bytes), "r"(smem_u32(bar)), "l"(pol) : "memory");
+}
+
+// Value sources of tile_rows: how a group's values are copied into a stage
+// (after its columns) and read back, four consecutive entries per thread.
 struct ValsDF { const float* hi; const float* lo; };   // double-float (hi, lo)
 struct ValsHi { const float* hi; };                    // fl(F) as a double-float with lo = 0
 struct ValsBF { const __nv_bfloat16* v; };             // bf16, scaled per row
-__device__ __forceinline__ void ld_vals4(ValsDF s, size_t off, float2 (&w)[4], uint64_t pol) {
-  float4 h = ld_mat_f4(s.hi + off, pol), l = ld_mat_f4(s.lo + off, pol);
+__device__ __forceinline__ unsigned vals_bytes(ValsDF) { return 2 * RAD_F32_BYTES; }
+__device__ __forceinline__ unsigned vals_bytes(ValsHi) { return RAD_F32_BYTES; }
+__device__ __forceinline__ unsigned vals_bytes(ValsBF) { return RAD_CF_BYTES; }
+__device__ __forceinline__ void copy_vals(ValsDF s, unsigned dst, size_t e, unsigned long long* bar, uint64_t pol) {
+  bulk_copy(dst, s.hi + e, RAD_F32_BYTES, bar, pol);
+  bulk_copy(dst + RAD_F32_BYTES, s.lo + e, RAD_F32_BYTES, bar, pol);
+}
+__device__ __forceinline__ void copy_vals(ValsHi s, unsigned dst, size_t e, unsigned long long* bar, uint64_t pol) {
+  bulk_copy(dst, s.hi + e, RAD_F32_BYTES, bar, pol);
+}
+__device__ __forceinline__ void copy_vals(ValsBF s, unsigned dst, size_t e, unsigned long long* bar, uint64_t pol) {
+  bulk_copy(dst, s.v + e, RAD_CF_BYTES, bar, pol);
+}
+__device__ __forceinline__ void read_vals(ValsDF, const unsigned char* st, int tid, float2 (&w)[4]) {
+  const float4 h = *reinterpret_cast<const float4*>(st + 16 * tid);
+  const float4 l = *reinterpret_cast<const float4*>(st + RAD_F32_BYTES + 16 * tid);
   w[0] = make_float2(h.x, l.x);
   w[1] = make_float2(h.y, l.y);
   w[2] = make_float2(h.z, l.z);
   w[3] = make_float2(h.w, l.w);
 }
-__device__ __forceinline__ void ld_vals4(ValsHi s, size_t off, float2 (&w)[4], uint64_t pol) {
-  float4 h = ld_mat_f4(s.hi + off, pol);
+__device__ __forceinline__ void read_vals(ValsHi, const unsigned char* st, int tid, float2 (&w)[4]) {
+  const float4 h = *reinterpret_cast<const float4*>(st + 16 * tid);
   w[0] = make_float2(h.x, 0.f);
   w[1] = make_float2(h.y, 0.f);
   w[2] = make_float2(h.z, 0.f);
   w[3] = make_float2(h.w, 0.f);
 }
-__device__ __forceinline__ void pf_vals(ValsDF s, size_t off) { pf_l2(s.hi + off); pf_l2(s.lo + off); }
-__device__ __forceinline__ void pf_vals(ValsHi s, size_t off) { pf_l2(s.hi + off); }
-__device__ __forceinline__ void pf_vals(ValsBF s, size_t off) { pf_l2(s.v + off); }
-__device__ __forceinline__ void ld_vals4(ValsBF s, size_t off, float (&w)[4], uint64_t pol) {
-  uint2 r = ld_mat(reinterpret_cast<const uint2*>(s.v + off), pol);
+__device__ __forceinline__ void read_vals(ValsBF, const unsigned char* st, int tid, float (&w)[4]) {
+  const uint2 r = *reinterpret_cast<const uint2*>(st + 8 * tid);
   w[0] = __uint_as_float(r.x << 16);
   w[1] = __uint_as_float(r.x & 0xffff0000u);
   w[2] = __uint_as_float(r.y << 16);
   w[3] = __uint_as_float(r.y & 0xffff0000u);
 }
+template <class W> __device__ __forceinline__ void zero_vals(W (&w)[4]);
+template <> __device__ __forceinline__ void zero_vals(float2 (&w)[4]) {
+  for (int j = 0; j < 4; ++j) w[j] = make_float2(0.f, 0.f);
+}
+template <> __device__ __forceinline__ void zero_vals(float (&w)[4]) {
+  for (int j = 0; j < 4; ++j) w[j] = 0.f;
+}
+
+// The block's stream ring and its sequence position (per thread; every
+// consumer and the producer lane advance it identically).
+struct Pipe {
+  unsigned char* ring;
+  unsigned long long* full;
+  unsigned long long* empty;
+  int* bad;
+  int nst;
+  int stage_bytes;
+  unsigned q;
+};
+
+// Producer (lane 0 of the producer warp): the copies of every group of tile T.
+template <class V>
+__device__ __forceinline__ void produce_tile(Pipe& p, const StepView& v, const RowTile& T, V vals, uint64_t pol) {
+  const int ng = T.lam >> 2;
+  const unsigned bytes = (unsigned)RAD_CF_BYTES + vals_bytes(vals);
+  for (int g = 0; g < ng; ++g, ++p.q) {
+    const unsigned s = p.q % (unsigned)p.nst, n = p.q / (unsigned)p.nst;
+    if (n > 0 && !mbar_wait(p.empty + s, (n - 1) & 1u, p.bad, v.derr)) continue;
+    if (*(volatile int*)p.bad) continue;
+    const unsigned dst = smem_u32(p.ring + (size_t)s * p.stage_bytes);
+    const size_t e = (size_t)T.e0 + (size_t)g * RAD_GROUP;
+    mbar_expect(p.full + s, bytes);
+    bulk_copy(dst, v.t_cf + e, RAD_CF_BYTES, p.full + s, pol);
+    copy_vals(vals, dst + RAD_CF_BYTES, e, p.full + s, pol);
+  }
+}
+
+// Consumer: the next group's four entries of this thread (columns and
+// values), then the stage is released.
+template <class V, class W>
+__device__ __forceinline__ void take_group(Pipe& p, const StepView& v, V vals, uint2& c, W (&w)[4]) {
+  const unsigned s = p.q % (unsigned)p.nst, n = p.q / (unsigned)p.nst;
+  ++p.q;
+  const unsigned char* st = p.ring + (size_t)s * p.stage_bytes;
+  if (mbar_wait(p.full + s, n & 1u, p.bad, v.derr)) {
+    c = *reinterpret_cast<const uint2*>(st + 8 * threadIdx.x);
+    read_vals(vals, st + RAD_CF_BYTES, threadIdx.x, w);
+  } else {
+    c = make_uint2(0u, 0u);
+    zero_vals(w);
+  }
+  mbar_arrive(p.empty + s);
+}
+
+// Barrier of the consumer threads only (the producer warp does not take
+// part in the tile work).
+__device__ __forceinline__ void cbar() { asm volatile("bar.sync 1, %0;" ::"n"(RAD_THREADS) : "memory"); }
 
 __device__ __forceinline__ double warp_sum(double x) {
   for (int o = 16; o; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
@@ -287,22 +404,23 @@ __device__ __forceinline__ void stage_halo(const StepView& v, const RowTile& T, 
     sx[h + 3 * RAD_THREADS] = to_halo(xd, sx);
   }
   for (; h < T.nhalo; h += RAD_THREADS) sx[h] = to_halo(ld_it(xg + __ldg(hp + h)), sx);
-  __syncthreads();
+  cbar();
 }
 
 // One tile: thread t owns entries [t*lam, (t+1)*lam) of the tile's entry
 // stream (rows in order, each row's entries in column order), stored so that
-// a warp's loads are contiguous: entry k of thread t at e0 + (k/4)*4096 +
-// 4t + k%4. Each thread accumulates sequentially (two groups of four
-// entries in flight ahead of the one being summed) and stores the sum of
-// every row that starts and ends in its run in rs[row] (shared memory). A
-// row that began in an earlier thread is completed by the thread where it
-// ends: the partial sums of the threads it spans, in thread order, then its
-// own part. Ends with a block barrier: rs holds every row sum of the tile.
+// a group of 4 RAD_THREADS entries is contiguous: entry k of thread t at
+// e0 + (k/4)*RAD_GROUP + 4t + k%4. The groups arrive in shared memory by
+// bulk copies (the block's Pipe). Each thread accumulates sequentially and
+// stores the sum of every row that starts and ends in its run in rs[row]
+// (shared memory). A row that began in an earlier thread is completed by the
+// thread where it ends: the partial sums of the threads it spans, in thread
+// order, then its own part. Ends with a consumer barrier: rs holds every
+// row sum of the tile.
 template <class Acc, class V>
-__device__ __forceinline__ void tile_rows(const StepView& v, const RowTile& T, int t, V vals,
+__device__ __forceinline__ void tile_rows(const StepView& v, const RowTile& T, int t, Pipe& p, V vals,
                                           const typename Acc::X* sx, typename Acc::Part* tail, unsigned char* tnew,
-                                          typename Acc::Sum* rs, uint64_t pol) {
+                                          typename Acc::Sum* rs) {
   typedef typename Acc::W W;
   const int tid = threadIdx.x;
   const uint32_t s0 = __ldg(v.t_start + (size_t)t * RAD_THREADS + tid);
@@ -313,8 +431,6 @@ __device__ __forceinline__ void tile_rows(const StepView& v, const RowTile& T, i
   Acc acc, head;
   acc.zero();
   head.zero();
-  const uint2* cfp = reinterpret_cast<const uint2*>(v.t_cf + T.e0) + tid;
-  const size_t vo = (size_t)T.e0 + 4 * tid;
   const int ng = T.lam >> 2;
   auto elem = [&](uint32_t c, W w) {
     acc.add(w, sx[c & 0x7fffu]);
@@ -331,51 +447,18 @@ __device__ __forceinline__ void tile_rows(const StepView& v, const RowTile& T, i
       any = true;
     }
   };
-  const bool pf = v.l2_stream != 0;   // an L2-resident matrix gains nothing from prefetching
-  if (pf)
-    for (int q = 2; q < RAD_PF && q < ng; ++q) {
-      pf_l2(cfp + (size_t)q * RAD_THREADS);
-      pf_vals(vals, vo + (size_t)q * 4 * RAD_THREADS);
-    }
-  uint2 c0 = ld_mat(cfp, pol), c1 = c0;
-  W w0[4], w1[4];
-  ld_vals4(vals, vo, w0, pol);
-  if (ng > 1) {
-    c1 = ld_mat(cfp + RAD_THREADS, pol);
-    ld_vals4(vals, vo + 4 * RAD_THREADS, w1, pol);
-  } else {
-#pragma unroll
-    for (int j = 0; j < 4; ++j) w1[j] = w0[j];
-  }
   for (int g = 0; g < ng; ++g) {
-    uint2 c2 = c1;
-    W w2[4];
-    if (pf && g + RAD_PF < ng) {
-      pf_l2(cfp + (size_t)(g + RAD_PF) * RAD_THREADS);
-      pf_vals(vals, vo + (size_t)(g + RAD_PF) * 4 * RAD_THREADS);
-    }
-    if (g + 2 < ng) {
-      c2 = ld_mat(cfp + (size_t)(g + 2) * RAD_THREADS, pol);
-      ld_vals4(vals, vo + (size_t)(g + 2) * 4 * RAD_THREADS, w2, pol);
-    } else {
-#pragma unroll
-      for (int j = 0; j < 4; ++j) w2[j] = w1[j];
-    }
-    elem(c0.x & 0xffffu, w0[0]);
-    elem(c0.x >> 16, w0[1]);
-    elem(c0.y & 0xffffu, w0[2]);
-    elem(c0.y >> 16, w0[3]);
-    c0 = c1;
-    c1 = c2;
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      w0[j] = w1[j];
-      w1[j] = w2[j];
-    }
+    uint2 c;
+    W w[4];
+    take_group(p, v, vals, c, w);
+    elem(c.x & 0xffffu, w[0]);
+    elem(c.x >> 16, w[1]);
+    elem(c.y & 0xffffu, w[2]);
+    elem(c.y >> 16, w[3]);
   }
   tail[tid] = acc.part();
   tnew[tid] = (any || !cont) ? 1 : 0;
-  __syncthreads();
+  cbar();
   if (has_head) {
     int u = tid - 1;
     while (!tnew[u]) --u;   // thread 0 starts a row, so this stops
@@ -385,11 +468,11 @@ __device__ __forceinline__ void tile_rows(const StepView& v, const RowTile& T, i
     s.merge(head.part());
     rs[head_row] = s.get();
   }
-  __syncthreads();
+  cbar();
 }
 
-// Block sum in a fixed order (FP32), valid in thread 0. Ends with a block
-// barrier (the tile's shared arrays are free again).
+// Sum over the consumer threads in a fixed order (FP32), valid in thread 0.
+// Ends with a consumer barrier (the tile's shared arrays are free again).
 __device__ __forceinline__ float warp_sumf(float x) {
   for (int o = 16; o; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
   return x;
@@ -397,10 +480,10 @@ __device__ __forceinline__ float warp_sumf(float x) {
 __device__ __forceinline__ float block_sum(float d, float* red) {
   d = warp_sumf(d);
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = d;
-  __syncthreads();
+  cbar();
   float t = 0.f;
-  if (threadIdx.x < 32) t = warp_sumf(red[threadIdx.x]);
-  __syncthreads();
+  if (threadIdx.x < 32) t = warp_sumf(threadIdx.x < RAD_THREADS / 32 ? red[threadIdx.x] : 0.f);
+  cbar();
   return t;
 }
 
@@ -492,7 +575,7 @@ __device__ __forceinline__ int decide_meshes(const StepView& v, MeshState& st, i
 // (sum of its tiles' partials, lane-strided then a fixed warp tree) into
 // the mesh table.
 __device__ __forceinline__ void record_residuals(const StepView& v, const MeshState& st) {
-  if (blockIdx.x != 0) return;
+  if (blockIdx.x != 0 || threadIdx.x >= RAD_THREADS) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int m = warp; m < v.nmesh; m += RAD_THREADS / 32) {
     const MeshDesc& M = v.md[m];
@@ -529,44 +612,76 @@ struct RadBufs {
   }
 };
 
-// free_rows: also write the result of the rows without entries (x = E,
-// s = 0) and their warm-start record, for a kernel that scatters its tile
-// rows itself.
+// The solve's own per-row state is kept by radiosity position p (Morton
+// order): the warm-start record sprev, row_act, and the mesh of a position
+// (a mesh's positions and facets occupy the same range, so mesh_of serves
+// both). Only E (read) and x (written) are in facet order: one gather and
+// one scatter through rperm per row and solve. Each thread takes
+// RAD_ILP positions at once so that their loads are in flight together.
+constexpr int RAD_ILP = 4;
+
+// free_rows (the mixed solve): also write the result of the rows without
+// entries (x = E, s = 0) and their warm-start record, for a kernel that
+// scatters its tile rows itself; that solve reads only EP, S0 and H0 (and
+// x32), the FP64 sweeps also S1, H1 and EH.
 __device__ __forceinline__ void init_x(const StepView& v, double* x, int warm, int gt, int nthreads,
                                        bool free_rows) {
   const RadBufs B(v);
-  for (int p = gt; p < v.nt; p += nthreads) {
-    int g = (int)v.rperm[p];
-    const MeshDesc& M = v.md[mesh_of_facet(v, g)];
-    if (!M.active || M.ntiles == 0) continue;
-    // the frame's direct flux, coupled as src/cpp/illum_cli.cpp:415-421 when
-    // the mesh follows the reference (rad = -Fsurf_prev + direct)
-    const double d = v.E[(size_t)(M.frame & 1) * v.nt + g];
-    const double e = M.coupling == ILG_COUPLE_REFERENCE ? (-v.Fsurf[g] + d) : d;
-    float2 s0 = make_float2(0.f, 0.f);
-    if (warm && v.row_act[g] && M.frame >= 1) {
-      double s = v.sprev[g];
-      if (M.frame >= 2) s += v.sprev[v.nt + g];
-      s0 = split_df(s);
+  for (int p0 = gt; p0 < v.nt; p0 += RAD_ILP * nthreads) {
+    int g[RAD_ILP];
+    const MeshDesc* M[RAD_ILP];
+    double d[RAD_ILP], sp0[RAD_ILP], sp1[RAD_ILP], fs[RAD_ILP];
+    uint8_t act[RAD_ILP];
+#pragma unroll
+    for (int k = 0; k < RAD_ILP; ++k) {
+      const int p = p0 + k * nthreads;
+      g[k] = 0;
+      M[k] = nullptr;
+      if (p >= v.nt) continue;
+      const MeshDesc* m = v.md + mesh_of_facet(v, p);
+      if (!m->active || m->ntiles == 0) continue;
+      M[k] = m;
+      g[k] = (int)v.rperm[p];
+      act[k] = v.row_act[p];
+      sp0[k] = warm ? v.sprev[p] : 0.0;
+      sp1[k] = warm ? v.sprev[v.nt + p] : 0.0;
     }
-    if (free_rows && !v.row_act[g]) {
-      x[g] = e;
-      if (warm) {
-        v.sprev[v.nt + g] = 0.0 - v.sprev[g];
-        v.sprev[g] = 0.0;
+#pragma unroll
+    for (int k = 0; k < RAD_ILP; ++k) {
+      if (!M[k]) continue;
+      d[k] = v.E[(size_t)(M[k]->frame & 1) * v.nt + g[k]];
+      fs[k] = M[k]->coupling == ILG_COUPLE_REFERENCE ? v.Fsurf[g[k]] : 0.0;
+    }
+#pragma unroll
+    for (int k = 0; k < RAD_ILP; ++k) {
+      if (!M[k]) continue;
+      const int p = p0 + k * nthreads;
+      const MeshDesc& Mk = *M[k];
+      // the frame's direct flux, coupled as src/cpp/illum_cli.cpp:415-421
+      // when the mesh follows the reference (rad = -Fsurf_prev + direct)
+      const double e = Mk.coupling == ILG_COUPLE_REFERENCE ? (-fs[k] + d[k]) : d[k];
+      float2 s0 = make_float2(0.f, 0.f);
+      if (warm && act[k] && Mk.frame >= 1) s0 = split_df(Mk.frame >= 2 ? sp0[k] + sp1[k] : sp0[k]);
+      if (free_rows && !act[k]) {
+        x[g[k]] = e;
+        if (warm) {
+          v.sprev[v.nt + p] = 0.0 - sp0[k];
+          v.sprev[p] = 0.0;
+        }
       }
-    }
-    const float2 eh = split_df(e);
-    const float2 x0 = df_add(eh, s0);
-    B.EP[p] = e;
-    B.S0[p] = s0;
-    B.S1[p] = make_float2(0.f, 0.f);
-    B.H0[p] = x0;
-    B.H1[p] = x0;
-    B.EH[p] = eh;
-    if (v.x32) {
-      v.x32[p] = 0.f;
-      v.x32[v.nt + p] = 0.f;
+      const float2 eh = split_df(e);
+      const float2 x0 = df_add(eh, s0);
+      B.EP[p] = e;
+      B.S0[p] = s0;
+      B.H0[p] = x0;
+      if (free_rows) {
+        v.x32[p] = 0.f;
+        v.x32[v.nt + p] = 0.f;
+      } else {
+        B.S1[p] = make_float2(0.f, 0.f);
+        B.H1[p] = x0;
+        B.EH[p] = eh;
+      }
     }
   }
 }
@@ -578,96 +693,176 @@ __device__ __forceinline__ void init_x(const StepView& v, double* x, int warm, i
 __device__ __forceinline__ void scatter_x(const StepView& v, const MeshState& st, double* x, int warm, int gt,
                                           int nthreads) {
   const RadBufs B(v);
-  for (int p = gt; p < v.nt; p += nthreads) {
-    int g = (int)v.rperm[p];
-    int m = mesh_of_facet(v, g);
-    const MeshDesc& M = v.md[m];
-    if (!M.active || M.ntiles == 0) continue;
-    const double s = df_value(ld_it(((st.sweeps[m] & 1) ? B.S1 : B.S0) + p));
-    x[g] = B.EP[p] + s;
-    if (warm) {
-      v.sprev[v.nt + g] = s - v.sprev[g];
-      v.sprev[g] = s;
+  for (int p0 = gt; p0 < v.nt; p0 += RAD_ILP * nthreads) {
+    int g[RAD_ILP];
+    bool ok[RAD_ILP];
+    double s[RAD_ILP], e[RAD_ILP], sp[RAD_ILP];
+#pragma unroll
+    for (int k = 0; k < RAD_ILP; ++k) {
+      const int p = p0 + k * nthreads;
+      ok[k] = false;
+      if (p >= v.nt) continue;
+      const int m = mesh_of_facet(v, p);
+      const MeshDesc& M = v.md[m];
+      if (!M.active || M.ntiles == 0) continue;
+      ok[k] = true;
+      g[k] = (int)v.rperm[p];
+      s[k] = df_value(ld_it(((st.sweeps[m] & 1) ? B.S1 : B.S0) + p));
+      e[k] = B.EP[p];
+      sp[k] = warm ? v.sprev[p] : 0.0;
+    }
+#pragma unroll
+    for (int k = 0; k < RAD_ILP; ++k) {
+      if (!ok[k]) continue;
+      const int p = p0 + k * nthreads;
+      x[g[k]] = e[k] + s[k];
+      if (warm) {
+        v.sprev[v.nt + p] = s[k] - sp[k];
+        v.sprev[p] = s[k];
+      }
     }
   }
 }
 
-// Tile T's rows (owned by this block): x = E + s into facet order, and the
-// warm-start record, as scatter_x.
-__device__ __forceinline__ void scatter_tile(const StepView& v, const RowTile& T, const float2* S, double* x,
-                                             int warm) {
+// The rows of this block's tiles whose mesh stopped at the latest decision
+// (st.now): x = E + s into facet order, and the warm-start record, as
+// scatter_x. The block's rows are dealt to its consumer threads in one run
+// over all its tiles (a thread takes every RAD_THREADS-th row of the
+// concatenation), so each thread has a few rows in a row instead of a
+// fraction of one per tile.
+__device__ __forceinline__ void scatter_block(const StepView& v, const MeshState& st, const float2* S, double* x,
+                                              int warm) {
   const RadBufs B(v);
-  const uint32_t* rows = v.t_row + T.r0;
-  for (int r = threadIdx.x; r < T.nrows; r += RAD_THREADS) {
-    const uint32_t i = __ldg(rows + r);
-    const int g = (int)v.rperm[i];
-    const double sv = df_value(ld_it(S + i));
-    x[g] = B.EP[i] + sv;
-    if (warm) {
-      v.sprev[v.nt + g] = sv - v.sprev[g];
-      v.sprev[g] = sv;
+  int r = threadIdx.x;
+  for (int t = blockIdx.x; t < v.ntiles; t += gridDim.x) {
+    const RowTile T = v.tiles[t];
+    if (!st.now[T.mesh]) continue;
+    const uint32_t* rows = v.t_row + T.r0;
+    for (; r < T.nrows; r += RAD_THREADS) {
+      const uint32_t i = __ldg(rows + r);
+      const int g = (int)v.rperm[i];
+      const double sv = df_value(ld_it(S + i));
+      x[g] = B.EP[i] + sv;
+      if (warm) {
+        v.sprev[v.nt + i] = sv - v.sprev[i];
+        v.sprev[i] = sv;
+      }
     }
+    r -= T.nrows;
   }
 }
 
 struct RadSmem {
-  float2* sx;            // halo values (RAD_HALO double-floats, or floats)
-  float2* tail;          // per-thread open-row partials
-  float2* rs;            // row sums of the tile (RAD_ROWS double-floats, or floats)
-  unsigned char* tnew;   // per thread: its last open row began in its run
+  unsigned char* ring;       // entry-stream stages (RAD_RING bytes)
+  float2* sx;                // halo values (RAD_HALO double-floats, or floats)
+  float2* tail;              // per-thread open-row partials
+  float2* rs;                // row sums of the tile (RAD_ROWS double-floats, or floats)
+  unsigned char* tnew;       // per thread: its last open row began in its run
+  unsigned long long* full;  // per stage: its copies have landed
+  unsigned long long* empty; // per stage: every consumer has read it
 };
 
 __device__ __forceinline__ RadSmem rad_smem() {
-  extern __shared__ __align__(16) unsigned char rad_dyn[];
+  extern __shared__ __align__(128) unsigned char rad_dyn[];
   RadSmem m;
-  m.sx = reinterpret_cast<float2*>(rad_dyn);
+  m.ring = rad_dyn;
+  m.sx = reinterpret_cast<float2*>(rad_dyn + RAD_RING);
   m.tail = m.sx + RAD_HALO;
   m.rs = m.tail + RAD_THREADS;
   m.tnew = reinterpret_cast<unsigned char*>(m.rs + RAD_ROWS);
+  m.full = reinterpret_cast<unsigned long long*>(m.tnew + RAD_THREADS);
+  m.empty = m.full + RAD_NST_MAX;
   return m;
+}
+static_assert((RAD_RING + (size_t)(RAD_HALO + RAD_THREADS + RAD_ROWS) * 8 + RAD_THREADS) % 8 == 0,
+              "stage barriers are 8-byte aligned");
+
+// The ring's barriers, set up by thread 0 before the launch's first block
+// barrier (inside init_meshes' caller): full counts the producer's one
+// arrival plus the copied bytes, empty one arrival per consumer thread.
+__device__ __forceinline__ Pipe make_pipe(const RadSmem& m, int nst, int stage_bytes, int* bad) {
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < nst; ++s) {
+      mbar_init(m.full + s, 1);
+      mbar_init(m.empty + s, RAD_THREADS);
+    }
+    *bad = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  Pipe p;
+  p.ring = m.ring;
+  p.full = m.full;
+  p.empty = m.empty;
+  p.bad = bad;
+  p.nst = nst;
+  p.stage_bytes = stage_bytes;
+  p.q = 0;
+  return p;
+}
+
+// Producer warp: the copies of one pass over the block's tiles (lane 0
+// issues; the other lanes only follow the launch's block barriers).
+template <class V>
+__device__ __forceinline__ void produce_pass(Pipe& p, const StepView& v, const MeshState& st, V vals, uint64_t pol) {
+  if ((threadIdx.x & 31) != 0) return;
+  for (int t = blockIdx.x; t < v.ntiles; t += gridDim.x) {
+    const RowTile T = v.tiles[t];
+    if (st.done[T.mesh]) continue;
+    produce_tile(p, v, T, vals, pol);
+  }
 }
 
 // FP64 Jacobi to each mesh's tolerance. x: solution (and warm start).
-__global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity64(StepView v, double* x, int warm) {
+__global__ void __launch_bounds__(RAD_BLOCK, 1) k_radiosity64(StepView v, double* x, int warm) {
   __shared__ MeshState st;
   __shared__ float red[32];
+  __shared__ int bad;
   const RadSmem sm = rad_smem();
+  const bool producer = threadIdx.x >= RAD_THREADS;
   const int gt = blockIdx.x * RAD_THREADS + threadIdx.x;
   const int nthreads = gridDim.x * RAD_THREADS;
   unsigned gen = 0;
+  Pipe pipe = make_pipe(sm, RAD_NST64, RAD_STAGE64, &bad);
   init_meshes(v, st);
-  init_x(v, x, warm, gt, nthreads, false);
+  if (!producer) init_x(v, x, warm, gt, nthreads, false);
   if (!grid_barrier(v.barrier, gridDim.x, gen, v.derr)) return;
   const uint64_t pol = l2_keep_policy(v.l2_stream);
+  const ValsDF vals{v.t_vhi, v.t_vlo};
   for (int it = 0;; ++it) {
-    for (int t = blockIdx.x; t < v.ntiles; t += gridDim.x) {
-      const RowTile T = v.tiles[t];
-      if (st.done[T.mesh]) continue;
-      const RadBufs B(v);
-      stage_halo(v, T, (it & 1) ? B.H1 : B.H0, sm.sx);
-      tile_rows<AccDF>(v, T, t, ValsDF{v.t_vhi, v.t_vlo}, sm.sx, sm.tail, sm.tnew, sm.rs, pol);
-      const uint32_t* rows = v.t_row + T.r0;
-      const float2* cur = (it & 1) ? B.S1 : B.S0;
-      float2* nxt = (it & 1) ? B.S0 : B.S1;
-      float2* nxth = (it & 1) ? B.H0 : B.H1;
-      float d2 = 0.f;
-      for (int r = threadIdx.x; r < T.nrows; r += RAD_THREADS) {
-        uint32_t i = __ldg(rows + r);
-        const float2 sn = sm.rs[r];          // s' = F x
-        const float2 sc = ld_it(cur + i);
-        // s' - s: exact high-part difference when the two are within a
-        // factor of two, else rounded relative to the change itself
-        const float df = __fadd_rn(__fsub_rn(sn.x, sc.x), __fsub_rn(sn.y, sc.y));
-        nxt[i] = sn;
-        nxth[i] = df_add(__ldg(B.EH + i), sn);
-        d2 = __fmaf_rn(df, df, d2);
+    if (producer) {
+      produce_pass(pipe, v, st, vals, pol);
+      __syncwarp();
+    } else {
+      for (int t = blockIdx.x; t < v.ntiles; t += gridDim.x) {
+        const RowTile T = v.tiles[t];
+        if (st.done[T.mesh]) continue;
+        const RadBufs B(v);
+        stage_halo(v, T, (it & 1) ? B.H1 : B.H0, sm.sx);
+        tile_rows<AccDF>(v, T, t, pipe, vals, sm.sx, sm.tail, sm.tnew, sm.rs);
+        const uint32_t* rows = v.t_row + T.r0;
+        const float2* cur = (it & 1) ? B.S1 : B.S0;
+        float2* nxt = (it & 1) ? B.S0 : B.S1;
+        float2* nxth = (it & 1) ? B.H0 : B.H1;
+        float d2 = 0.f;
+        for (int r = threadIdx.x; r < T.nrows; r += RAD_THREADS) {
+          uint32_t i = __ldg(rows + r);
+          const float2 sn = sm.rs[r];          // s' = F x
+          const float2 sc = ld_it(cur + i);
+          // s' - s: exact high-part difference when the two are within a
+          // factor of two, else rounded relative to the change itself
+          const float df = __fadd_rn(__fsub_rn(sn.x, sc.x), __fsub_rn(sn.y, sc.y));
+          nxt[i] = sn;
+          nxth[i] = df_add(__ldg(B.EH + i), sn);
+          d2 = __fmaf_rn(df, df, d2);
+        }
+        post_partial(v, st, T, t, it, block_sum(d2, red));
       }
-      post_partial(v, st, T, t, it, block_sum(d2, red));
     }
     if (!grid_barrier(v.barrier, gridDim.x, gen, v.derr)) return;
     if (decide_meshes(v, st, 1, 0, it) == 0) break;
   }
-  scatter_x(v, st, x, warm, gt, nthreads);
+  if (!producer) scatter_x(v, st, x, warm, gt, nthreads);
   record_residuals(v, st);
 }
 
@@ -676,10 +871,12 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity64(StepView v, doub
 // bf16 F~ (inner sweeps, 1..RAD_INNER), s += d. A mesh stops when
 // ||r||_2 <= tol, or after the update of the round that reaches max_sweeps;
 // each tile's block writes its rows' results.
-__global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity_mixed(StepView v, double* x, int warm, int inner) {
+__global__ void __launch_bounds__(RAD_BLOCK, 1) k_radiosity_mixed(StepView v, double* x, int warm, int inner) {
   __shared__ MeshState st;
   __shared__ float red[32];
+  __shared__ int bad;
   const RadSmem sm = rad_smem();
+  const bool producer = threadIdx.x >= RAD_THREADS;
   float* sxf = reinterpret_cast<float*>(sm.sx);
   float* tailf = reinterpret_cast<float*>(sm.tail);
   float* rsf = reinterpret_cast<float*>(sm.rs);
@@ -689,80 +886,77 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity_mixed(StepView v, 
   float* xb = v.x32 + v.nt;
   float* r32 = v.x32 + 2 * (size_t)v.nt;
   unsigned gen = 0;
+  Pipe pipe = make_pipe(sm, RAD_NSTM, RAD_STAGEM, &bad);
   init_meshes(v, st);
-  init_x(v, x, warm, gt, nthreads, true);
+  if (!producer) init_x(v, x, warm, gt, nthreads, true);
   if (!grid_barrier(v.barrier, gridDim.x, gen, v.derr)) return;
   const uint64_t pol = l2_keep_policy(v.l2_stream);
   const RadBufs B(v);
+  const ValsHi vhi{v.t_vhi};
+  const ValsBF vbf{v.t_vbf};
   float2* S = B.S0;     // the iterate's scattered part s = x - E (radiosity positions)
   float2* XH = B.H0;    // x = E + s, what the halos gather
   int first = 1;
   for (int round = 0;; ++round) {
-    for (int t = blockIdx.x; t < v.ntiles; t += gridDim.x) {
-      const RowTile T = v.tiles[t];
-      if (st.done[T.mesh]) continue;
-      stage_halo(v, T, XH, sm.sx);
-      tile_rows<AccDF>(v, T, t, ValsHi{v.t_vhi}, sm.sx, sm.tail, sm.tnew, sm.rs, pol);
-      const uint32_t* rows = v.t_row + T.r0;
-      float d2 = 0.f;
-      for (int r = threadIdx.x; r < T.nrows; r += RAD_THREADS) {
-        uint32_t i = __ldg(rows + r);
-        // r = E + fl(F) x - x = fl(F) x - s
-        const float2 fx = sm.rs[r], s = ld_it(S + i);
-        const float res = __fadd_rn(__fsub_rn(fx.x, s.x), __fsub_rn(fx.y, s.y));
-        r32[i] = res;
-        xa[i] = res;     // inner start: d0 = r
-        d2 = __fmaf_rn(res, res, d2);
+    if (producer) {
+      produce_pass(pipe, v, st, vhi, pol);
+      __syncwarp();
+    } else {
+      for (int t = blockIdx.x; t < v.ntiles; t += gridDim.x) {
+        const RowTile T = v.tiles[t];
+        if (st.done[T.mesh]) continue;
+        stage_halo(v, T, XH, sm.sx);
+        tile_rows<AccDF>(v, T, t, pipe, vhi, sm.sx, sm.tail, sm.tnew, sm.rs);
+        const uint32_t* rows = v.t_row + T.r0;
+        float d2 = 0.f;
+        for (int r = threadIdx.x; r < T.nrows; r += RAD_THREADS) {
+          uint32_t i = __ldg(rows + r);
+          // r = E + fl(F) x - x = fl(F) x - s
+          const float2 fx = sm.rs[r], s = ld_it(S + i);
+          const float res = __fadd_rn(__fsub_rn(fx.x, s.x), __fsub_rn(fx.y, s.y));
+          r32[i] = res;
+          xa[i] = res;     // inner start: d0 = r
+          d2 = __fmaf_rn(res, res, d2);
+        }
+        post_partial(v, st, T, t, round, block_sum(d2, red));
       }
-      post_partial(v, st, T, t, round, block_sum(d2, red));
     }
     if (!grid_barrier(v.barrier, gridDim.x, gen, v.derr)) return;
     int running = decide_meshes(v, st, inner, first, round);
     first = 0;
     // meshes that stopped on their residual: each block writes its own
     // tiles' rows (their s was last written by this block)
-    for (int t = blockIdx.x; t < v.ntiles; t += gridDim.x) {
-      const RowTile T = v.tiles[t];
-      if (st.now[T.mesh]) scatter_tile(v, T, S, x, warm);
-    }
+    if (!producer) scatter_block(v, st, S, x, warm);
     if (running == 0) break;
     float* cur = xa;
     float* nxt = xb;
     for (int it = 0; it < inner; ++it) {
-      for (int t = blockIdx.x; t < v.ntiles; t += gridDim.x) {
-        const RowTile T = v.tiles[t];
-        if (st.done[T.mesh]) continue;
-        stage_halo(v, T, cur, sxf);
-        tile_rows<AccF32>(v, T, t, ValsBF{v.t_vbf}, sxf, tailf, sm.tnew, rsf, pol);
-        const uint32_t* rows = v.t_row + T.r0;
-        const float* scale = v.t_scale + T.r0;
-        if (it + 1 < inner) {
-          for (int r = threadIdx.x; r < T.nrows; r += RAD_THREADS) {
-            uint32_t i = __ldg(rows + r);
-            nxt[i] = ld_it(r32 + i) + __ldg(scale + r) * rsf[r];
-          }
-        } else {   // last sweep: nobody reads d again, s += d directly
-          // a mesh whose sweep budget ends with this round takes its result
-          // here (the same test as below)
-          const bool last = st.sweeps[T.mesh] + inner >= v.md[T.mesh].max_sweeps;
-          for (int r = threadIdx.x; r < T.nrows; r += RAD_THREADS) {
-            uint32_t i = __ldg(rows + r);
-            const float2 d = make_float2(ld_it(r32 + i) + __ldg(scale + r) * rsf[r], 0.f);
-            const float2 sn = df_add(ld_it(S + i), d);
-            S[i] = sn;
-            XH[i] = df_add(ld_it(XH + i), d);
-            if (last) {
-              const int g = (int)v.rperm[i];
-              const double sv = df_value(sn);
-              x[g] = B.EP[i] + sv;
-              if (warm) {
-                v.sprev[v.nt + g] = sv - v.sprev[g];
-                v.sprev[g] = sv;
-              }
+      if (producer) {
+        produce_pass(pipe, v, st, vbf, pol);
+        __syncwarp();
+      } else {
+        for (int t = blockIdx.x; t < v.ntiles; t += gridDim.x) {
+          const RowTile T = v.tiles[t];
+          if (st.done[T.mesh]) continue;
+          stage_halo(v, T, cur, sxf);
+          tile_rows<AccF32>(v, T, t, pipe, vbf, sxf, tailf, sm.tnew, rsf);
+          const uint32_t* rows = v.t_row + T.r0;
+          const float* scale = v.t_scale + T.r0;
+          if (it + 1 < inner) {
+            for (int r = threadIdx.x; r < T.nrows; r += RAD_THREADS) {
+              uint32_t i = __ldg(rows + r);
+              nxt[i] = ld_it(r32 + i) + __ldg(scale + r) * rsf[r];
+            }
+          } else {   // last sweep: nobody reads d again, s += d directly
+            for (int r = threadIdx.x; r < T.nrows; r += RAD_THREADS) {
+              uint32_t i = __ldg(rows + r);
+              const float2 d = make_float2(ld_it(r32 + i) + __ldg(scale + r) * rsf[r], 0.f);
+              S[i] = df_add(ld_it(S + i), d);
+              XH[i] = df_add(ld_it(XH + i), d);
             }
           }
+          cbar();
         }
-        __syncthreads();
       }
       if (it + 1 < inner) {
         if (!grid_barrier(v.barrier, gridDim.x, gen, v.derr)) return;
@@ -770,19 +964,23 @@ __global__ void __launch_bounds__(RAD_THREADS, 1) k_radiosity_mixed(StepView v, 
       }
     }
     // meshes whose budget this round used up stop here (same decision in
-    // every block: it depends on the counts only)
+    // every block: it depends on the counts only) and take their results
+    // (each block its own tiles' rows, whose s it wrote)
     int left = 0;
     for (int m0 = 0; m0 < v.nmesh; m0 += blockDim.x) {
       int m = m0 + threadIdx.x;
       bool run = m < v.nmesh && !st.done[m];
+      if (m < v.nmesh) st.now[m] = 0;
       if (run && st.sweeps[m] + inner >= v.md[m].max_sweeps) {
         st.done[m] = 1 + (round & 1);
         st.sweeps[m] += inner;
+        st.now[m] = 1;
         if (blockIdx.x == 0) v.md[m].sweeps = st.sweeps[m];
         run = false;
       }
       left += __syncthreads_count(run);
     }
+    if (!producer) scatter_block(v, st, S, x, warm);
     if (left == 0) break;   // every result is written (by its tile's block)
     if (!grid_barrier(v.barrier, gridDim.x, gen, v.derr)) return;
   }
@@ -853,7 +1051,7 @@ __global__ void k_halo_runs(const unsigned long long* __restrict__ key, const ui
 
 // Each entry to its stored slot: entry j of a tile (rows in Morton order,
 // each row's entries in column order) belongs to thread t = j / lam as its
-// kk = j % lam-th, stored at e0 + (kk / 4) 4096 + 4 t + kk % 4; the slot
+// kk = j % lam-th, stored at e0 + (kk / 4) RAD_GROUP + 4 t + kk % 4; the slot
 // holds the entry's halo index (run - h0) with the row-end bit, the CSR
 // entry it takes its value from, and its row (for the row scale).
 __global__ void k_tile_slots(const unsigned long long* __restrict__ key, const uint32_t* __restrict__ idx,
@@ -934,8 +1132,8 @@ int radiosity_setup() {
   ILG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   ILG_CUDA(cudaFuncSetAttribute(k_radiosity64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RAD_SMEM));
   ILG_CUDA(cudaFuncSetAttribute(k_radiosity_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RAD_SMEM));
-  ILG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_rad_per_sm64, k_radiosity64, RAD_THREADS, RAD_SMEM));
-  ILG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_rad_per_smm, k_radiosity_mixed, RAD_THREADS, RAD_SMEM));
+  ILG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_rad_per_sm64, k_radiosity64, RAD_BLOCK, RAD_SMEM));
+  ILG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_rad_per_smm, k_radiosity_mixed, RAD_BLOCK, RAD_SMEM));
   if (g_rad_per_sm64 < 1 || g_rad_per_smm < 1) { set_error("radiosity kernel cannot be resident"); return ILG_ERR_CUDA; }
   g_rad_nsm = nsm;
   g_rad_ready.store(true, std::memory_order_release);
@@ -998,18 +1196,18 @@ int radiosity_prepare(Context& c) {
                   (long long)len, RAD_HALO);
         return ILG_ERR_ARG;
       }
-      act[g] = 1;
+      act[p] = 1;
       arow.push_back(p);
     }
   }
   c.n_active = (int)arow.size();
 
   // Tile cuts. A tile's stream time follows its whole groups (every thread
-  // runs ceil(entries / 4096) groups of four), so tiles get equal group
-  // counts: the smallest ng for which a greedy pass with at most ng * 4096
+  // runs ceil(entries / RAD_GROUP) groups of four), so tiles get equal group
+  // counts: the smallest ng for which a greedy pass with at most ng * RAD_GROUP
   // entries per tile needs no more tiles than co-resident blocks. A second
   // pass also closes a tile early once its weighed cost (entries + rows)
-  // exceeds ng * 4096 plus the first pass's mean row cost, so row-heavy
+  // exceeds ng * RAD_GROUP plus the first pass's mean row cost, so row-heavy
   // tiles carry fewer entries; it is kept if it still fits the grid. If the
   // row cap forces more tiles than blocks (very large meshes), the cuts are
   // equal shares of the estimated work (entries + rows), several tiles per
@@ -1321,7 +1519,7 @@ int radiosity_launch(const StepView& v, double* x, int warm, int precision, int 
   ILG_CUDA(cudaMemsetAsync(v.barrier, 0, 2 * sizeof(unsigned), s));
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(grid);
-  cfg.blockDim = dim3(RAD_THREADS);
+  cfg.blockDim = dim3(RAD_BLOCK);
   cfg.dynamicSmemBytes = RAD_SMEM;
   cfg.stream = s;
   cudaLaunchAttribute attr[1];

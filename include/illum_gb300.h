@@ -129,6 +129,11 @@ int ilg_set_F(ilg_ctx* ctx, int64_t nnz, const int64_t* rowptr, const int32_t* c
  * entries (any may be NULL). */
 int ilg_F_info(const ilg_ctx* ctx, int64_t* nnz, int64_t* stored_entries, int* row_tiles,
                int* active_rows);
+/* The radiosity row tiles of the context's form factors (a diagnostic of
+ * the GPU layout, no counterpart in the reference): per tile, the entries
+ * each of its threads streams per sweep, its rows and its halo facets. The
+ * first min(cap, *ntiles) tiles are written; *ntiles receives the count. */
+int ilg_F_tiles(const ilg_ctx* ctx, int cap, int* entries_per_thread, int* rows, int* halo, int* ntiles);
 
 /* ---- horizons ----------------------------------------------------------- */
 int ilg_make_horizons(ilg_ctx* ctx, int nphi, double theta_eps, double offset);
