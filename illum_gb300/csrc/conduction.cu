@@ -208,6 +208,16 @@ k_conduct(StepView v, const double* __restrict__ Qnp1, int upd) {
   // carries no large cancellation when the diffusion numbers alpha, gamma
   // are large.
   constexpr bool INC = !std::is_same<R, double>::value;
+  // The facet's scalars, loaded before the column work so that their
+  // latency overlaps it. A scene step's flux: the radiosity solution, or for
+  // a mesh without form factors the frame's direct flux, coupled as
+  // src/cpp/illum_cli.cpp:415-421 (rad = -Fsurf_prev + direct) when the mesh
+  // follows the reference, and recorded as the mesh's radiosity. Fsurf is
+  // read before this thread overwrites it below.
+  const bool direct_only = upd && M.ntiles == 0;
+  const double Qsrc = direct_only ? v.E[(size_t)(M.frame & 1) * v.nt + g] : Qnp1[g];
+  const double Fs_prev = (direct_only && M.coupling == ILG_COUPLE_REFERENCE) ? v.Fsurf[g] : 0.0;
+  const double Ts_prev = v.Tsurf[g];
   // Stage the column in the rho slots (slot i <- T_i): the upward pass then
   // reads T from shared memory and overwrites slot i with rho_i once T_i is
   // in registers. In shared memory the copies are asynchronous (cp.async,
@@ -260,18 +270,10 @@ k_conduct(StepView v, const double* __restrict__ Qnp1, int upd) {
   }
   // top row (Ti = T_1, Tip1 = T_2 in the Fortran's numbering). In increment
   // form rho1 is the increment's; T1(n+1) = T0 + (increment) below.
-  // A scene step's flux: the radiosity solution, or for a mesh without form
-  // factors the frame's direct flux, coupled as src/cpp/illum_cli.cpp:415-421
-  // (rad = -Fsurf_prev + direct) when the mesh follows the reference, and
-  // recorded as the mesh's radiosity. Fsurf is read before this thread
-  // overwrites it below.
-  double Q;
-  if (upd && M.ntiles == 0) {
-    const double d = v.E[(size_t)(M.frame & 1) * v.nt + g];
-    Q = M.coupling == ILG_COUPLE_REFERENCE ? (-v.Fsurf[g] + d) : d;
+  double Q = Qsrc;
+  if (direct_only) {
+    if (M.coupling == ILG_COUPLE_REFERENCE) Q = -Fs_prev + Qsrc;
     v.rad[g] = Q;
-  } else {
-    Q = Qnp1[g];
   }
   double T0n, Tsn, Fs;
   R top, dtop;   // T1(n+1) and its increment, in the state's type
@@ -282,7 +284,7 @@ k_conduct(StepView v, const double* __restrict__ Qnp1, int upd) {
       // (P = T1(n+1) - S_top Ts(n+1) is a small difference of
       // temperature-sized terms), the root by FP32 Newton steps, polished in
       // double-float for the FP64 step (no FP64 arithmetic)
-      const TopResult tr = newton_top(cs, to_df(Ti), to_df(Tip1), to_df(rho_next), v.Tsurf[g], Q,
+      const TopResult tr = newton_top(cs, to_df(Ti), to_df(Tip1), to_df(rho_next), Ts_prev, Q,
                                       std::is_same<R, dfloat>::value);
       Tsn = df_to_double(tr.tsn);
       top = from_df<R>(tr.top);
@@ -294,7 +296,7 @@ k_conduct(StepView v, const double* __restrict__ Qnp1, int upd) {
   }
   if (!done_top) {
   double T0 = (double)Ti, T1 = (double)Tip1, rho1 = (double)rho_next;
-  double Ts = v.Tsurf[g];
+  double Ts = Ts_prev;
   if (cs.bc == 0) {
     double Qn = v.Qprev[g];
     double Tr3 = Ts * Ts * Ts;
