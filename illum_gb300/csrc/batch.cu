@@ -68,6 +68,8 @@ struct Batch {
   dbuf<uint16_t> t_cf;
   dbuf<float> t_vhi, t_vlo;
   dbuf<double> tile_d2;
+  dbuf<int> sched_start, sched_tile;   // per-block tile schedule of the batch's radiosity grid
+  int sched_grid = 0;
   dbuf<__nv_bfloat16> t_vbf;
   dbuf<uint32_t> t_row, t_halo, t_start;
   dbuf<float> t_scale;
@@ -202,6 +204,8 @@ static int build(Batch& b) {
   }
   if (!th.empty())
     ILG_CUDA(cudaMemcpyAsync(b.tiles.p, th.data(), th.size() * sizeof(RowTile), cudaMemcpyHostToDevice, s));
+  b.sched_grid = radiosity_grid((int)th.size(), b.precision);
+  ILG_TRY(radiosity_schedule(th, b.sched_grid, b.sched_start, b.sched_tile, s));
   ILG_CUDA(cudaMemsetAsync(b.row_act.p, 0, nt, s));
   ILG_CUDA(cudaMemsetAsync(b.counters.p, 0, 8 * sizeof(int), s));
   ILG_CUDA(cudaMemsetAsync(b.derr.p, 0, DERR_COUNT * sizeof(int), s));
@@ -288,6 +292,7 @@ static int build(Batch& b) {
   v.therm_avg = b.therm_avg.p; v.therm_max = b.therm_max.p; v.E = b.E.p; v.sprev = b.sprev.p;
   v.x32 = b.x32.p; v.Tdf = b.Tdf.p; v.T32 = b.T32.p; v.coefdf = b.coefdf.p; v.coef32 = b.coef32.p;
   v.tiles = b.tiles.p; v.ntiles = b.ntiles;
+  v.blk_start = b.sched_start.p; v.blk_tile = b.sched_tile.p; v.sched_grid = b.sched_grid;
   v.l2_stream = radiosity_l2_stream(b.nel);
   v.t_cf = b.t_cf.p; v.t_vhi = b.t_vhi.p; v.t_vlo = b.t_vlo.p; v.t_vbf = b.t_vbf.p;
   v.t_row = b.t_row.p; v.t_halo = b.t_halo.p; v.t_start = b.t_start.p; v.t_scale = b.t_scale.p;

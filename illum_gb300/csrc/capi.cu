@@ -220,6 +220,7 @@ static StepView solo_view(Context& c, int precision) {
   v.T64 = nullptr; v.Tdf = c.Tdf.p; v.T32 = c.T32.p;
   v.coef64 = nullptr; v.coefdf = c.coefdf.p; v.coef32 = c.coef32.p;
   v.tiles = c.tiles.p; v.ntiles = c.have_F ? c.ntiles : 0;
+  v.blk_start = c.sched_start.p; v.blk_tile = c.sched_tile.p; v.sched_grid = c.sched_grid;
   v.l2_stream = radiosity_l2_stream(c.tile_elems);
   v.t_cf = c.t_cf.p; v.t_vhi = c.t_vhi.p; v.t_vlo = c.t_vlo.p; v.t_vbf = c.t_vbf.p;
   v.t_row = c.t_row.p; v.t_halo = c.t_halo.p; v.t_start = c.t_start.p; v.t_scale = c.t_scale.p;

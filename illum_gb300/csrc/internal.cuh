@@ -135,6 +135,9 @@ struct StepView {
   // radiosity row tiles
   const RowTile* tiles;
   int ntiles;
+  const int* blk_start;        // per radiosity block b: its tiles are blk_tile[blk_start[b] .. blk_start[b + 1])
+  const int* blk_tile;
+  int sched_grid;              // the radiosity grid the schedule was made for
   int l2_stream;               // 1: the stored matrix is much larger than L2 (stream it evict-first)
   const uint16_t* t_cf;        // per stored entry: halo index | row end << 15
   const float* t_vhi;          // double-float values: hi = fl(F)
@@ -215,6 +218,8 @@ struct Context {
   dbuf<uint32_t> t_row, t_halo, t_start;
   dbuf<float> t_scale;
   dbuf<double> tile_d2;
+  dbuf<int> sched_start, sched_tile;   // per-block tile schedule (radiosity_schedule)
+  int sched_grid = 0;
   dbuf<uint8_t> row_act;
   dbuf<uint32_t> rperm;           // Morton position -> facet (radiosity's internal order)
   // the reference's fixed-sweep Gauss-Seidel (gauss_seidel.cu)
@@ -322,6 +327,10 @@ int direct_launch(const StepView& v, int dropin, int mu32_flux, int ahead, cudaS
 // ---- radiosity.cu ----
 int radiosity_prepare(Context& c);
 int radiosity_grid(int ntiles, int precision);
+// Balanced assignment of row tiles to the grid's blocks (longest tiles
+// first, each to the least loaded block); uploads it to start/order.
+int radiosity_schedule(const std::vector<RowTile>& tiles, int grid, dbuf<int>& start, dbuf<int>& order,
+                       cudaStream_t s);
 int radiosity_max_meshes();
 // whether a matrix of `stored` entries is streamed (larger than ~3/4 of L2)
 int radiosity_l2_stream(int64_t stored);

@@ -734,7 +734,8 @@ __device__ __forceinline__ void scatter_block(const StepView& v, const MeshState
                                               int warm) {
   const RadBufs B(v);
   int r = threadIdx.x;
-  for (int t = blockIdx.x; t < v.ntiles; t += gridDim.x) {
+  for (int k = v.blk_start[blockIdx.x]; k < v.blk_start[blockIdx.x + 1]; ++k) {
+    const int t = v.blk_tile[k];
     const RowTile T = v.tiles[t];
     if (!st.now[T.mesh]) continue;
     const uint32_t* rows = v.t_row + T.r0;
@@ -806,7 +807,8 @@ __device__ __forceinline__ Pipe make_pipe(const RadSmem& m, int nst, int stage_b
 template <class V>
 __device__ __forceinline__ void produce_pass(Pipe& p, const StepView& v, const MeshState& st, V vals, uint64_t pol) {
   if ((threadIdx.x & 31) != 0) return;
-  for (int t = blockIdx.x; t < v.ntiles; t += gridDim.x) {
+  for (int k = v.blk_start[blockIdx.x]; k < v.blk_start[blockIdx.x + 1]; ++k) {
+    const int t = v.blk_tile[k];
     const RowTile T = v.tiles[t];
     if (st.done[T.mesh]) continue;
     produce_tile(p, v, T, vals, pol);
@@ -834,7 +836,8 @@ __global__ void __launch_bounds__(RAD_BLOCK, 1) k_radiosity64(StepView v, double
       produce_pass(pipe, v, st, vals, pol);
       __syncwarp();
     } else {
-      for (int t = blockIdx.x; t < v.ntiles; t += gridDim.x) {
+      for (int k = v.blk_start[blockIdx.x]; k < v.blk_start[blockIdx.x + 1]; ++k) {
+    const int t = v.blk_tile[k];
         const RowTile T = v.tiles[t];
         if (st.done[T.mesh]) continue;
         const RadBufs B(v);
@@ -902,7 +905,8 @@ __global__ void __launch_bounds__(RAD_BLOCK, 1) k_radiosity_mixed(StepView v, do
       produce_pass(pipe, v, st, vhi, pol);
       __syncwarp();
     } else {
-      for (int t = blockIdx.x; t < v.ntiles; t += gridDim.x) {
+      for (int k = v.blk_start[blockIdx.x]; k < v.blk_start[blockIdx.x + 1]; ++k) {
+    const int t = v.blk_tile[k];
         const RowTile T = v.tiles[t];
         if (st.done[T.mesh]) continue;
         stage_halo(v, T, XH, sm.sx);
@@ -935,7 +939,8 @@ __global__ void __launch_bounds__(RAD_BLOCK, 1) k_radiosity_mixed(StepView v, do
         produce_pass(pipe, v, st, vbf, pol);
         __syncwarp();
       } else {
-        for (int t = blockIdx.x; t < v.ntiles; t += gridDim.x) {
+        for (int k = v.blk_start[blockIdx.x]; k < v.blk_start[blockIdx.x + 1]; ++k) {
+    const int t = v.blk_tile[k];
           const RowTile T = v.tiles[t];
           if (st.done[T.mesh]) continue;
           stage_halo(v, T, cur, sxf);
@@ -1434,7 +1439,11 @@ int radiosity_prepare(Context& c) {
                                                                   c.row_scale.p, c.t_scale.p);
     ILG_CUDA(cudaGetLastError());
     ILG_CUDA(cudaStreamSynchronize(s));
+    c.sched_grid = radiosity_grid(ntile, ILG_PREC_FP64);
+    ILG_TRY(radiosity_schedule(tiles, c.sched_grid, c.sched_start, c.sched_tile, s));
   } else {
+    c.sched_grid = radiosity_grid(0, ILG_PREC_FP64);
+    ILG_TRY(radiosity_schedule({}, c.sched_grid, c.sched_start, c.sched_tile, s));
     c.ntiles = 0;
     c.tile_elems = 0;
     c.tiles_h.clear();
@@ -1464,12 +1473,60 @@ int radiosity_l2_stream(int64_t stored) { return stored * 10 > (int64_t)96 << 20
 size_t radiosity_barrier_words(int nmesh) { return 2 + 2 * 3 * (size_t)(nmesh > 0 ? nmesh : 1); }
 
 // Cooperative grid size for ntiles tiles (at most the co-resident blocks).
+// Both solves launch the same block shape and shared memory, so one grid
+// (and one tile schedule) serves either precision.
 int radiosity_grid(int ntiles, int precision) {
+  (void)precision;
   if (radiosity_setup() != ILG_OK) return 1;
-  int per_sm = precision == ILG_PREC_MIXED ? g_rad_per_smm : g_rad_per_sm64;
+  int per_sm = std::min(g_rad_per_smm, g_rad_per_sm64);
   int grid = per_sm * g_rad_nsm;
   if (ntiles < grid) grid = ntiles;
   return grid < 1 ? 1 : grid;
+}
+
+// Tile cost in stored entries (RAD_ROW_COST per row, RAD_HALO_COST per halo
+// facet, plus a fixed cost of one group for the tile's set-up).
+int radiosity_schedule(const std::vector<RowTile>& tiles, int grid, dbuf<int>& start, dbuf<int>& order,
+                       cudaStream_t s) {
+  const int n = (int)tiles.size();
+  if (grid < 1) grid = 1;
+  std::vector<int> idx(n);
+  std::vector<int64_t> cost(n);
+  for (int t = 0; t < n; ++t) {
+    const RowTile& T = tiles[t];
+    idx[t] = t;
+    cost[t] = (int64_t)T.lam * RAD_THREADS + RAD_ROW_COST * T.nrows + RAD_HALO_COST * T.nhalo + RAD_GROUP;
+  }
+  std::sort(idx.begin(), idx.end(), [&](int a, int b) { return cost[a] != cost[b] ? cost[a] > cost[b] : a < b; });
+  std::vector<int64_t> load((size_t)grid, 0);
+  std::vector<std::vector<int>> lists((size_t)grid);
+  // least loaded block: a binary heap of (load, block)
+  std::vector<std::pair<int64_t, int>> heap;
+  for (int b = 0; b < grid; ++b) heap.push_back({0, b});
+  auto cmp = [](const std::pair<int64_t, int>& a, const std::pair<int64_t, int>& b) {
+    return a.first != b.first ? a.first > b.first : a.second > b.second;
+  };
+  std::make_heap(heap.begin(), heap.end(), cmp);
+  for (int t : idx) {
+    std::pop_heap(heap.begin(), heap.end(), cmp);
+    auto& top = heap.back();
+    lists[(size_t)top.second].push_back(t);
+    top.first += cost[t];
+    std::push_heap(heap.begin(), heap.end(), cmp);
+  }
+  std::vector<int> st((size_t)grid + 1, 0), ord;
+  ord.reserve(n);
+  for (int b = 0; b < grid; ++b) {
+    std::sort(lists[(size_t)b].begin(), lists[(size_t)b].end());
+    for (int t : lists[(size_t)b]) ord.push_back(t);
+    st[(size_t)b + 1] = (int)ord.size();
+  }
+  ILG_TRY(start.alloc((size_t)grid + 1));
+  ILG_TRY(order.alloc(n > 0 ? (size_t)n : 1));
+  ILG_CUDA(cudaMemcpyAsync(start.p, st.data(), st.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+  if (n > 0) ILG_CUDA(cudaMemcpyAsync(order.p, ord.data(), ord.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+  ILG_CUDA(cudaStreamSynchronize(s));
+  return ILG_OK;
 }
 
 // Launches the cooperative solve for every active mesh of the view with
@@ -1516,6 +1573,10 @@ int radiosity_barrier_probe(unsigned* bar, int* derr, int blocks, long long poll
 
 int radiosity_launch(const StepView& v, double* x, int warm, int precision, int grid, int inner, cudaStream_t s) {
   ILG_TRY(radiosity_setup());
+  if (!v.blk_start || grid != v.sched_grid) {
+    set_error("radiosity grid %d has no tile schedule (made for %d blocks)", grid, v.sched_grid);
+    return ILG_ERR_ARG;
+  }
   ILG_CUDA(cudaMemsetAsync(v.barrier, 0, 2 * sizeof(unsigned), s));
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(grid);
