@@ -440,23 +440,34 @@ def mixed_radiosity_bytes(F, rounds, sweeps, N):
     return rounds * (se * 6 + N * 32) + sweeps * (se * 4 + F["active_rows"] * 4 + N * 16)
 
 
-# Device bytes per stored form-factor entry: resident (CSR 4 + 8, row tiles
-# 2 + 4 + 4 + 2) and at the peak of the build (candidate keys, values,
-# compaction and the device tile build's sort buffers on top).
+# Device bytes per stored form-factor entry once built: CSR 4 + 8, row
+# tiles 2 + 4 + 4 + 2. The build's peak per entry is measured (allocation
+# pool high-water mark) on the base cutoff.
 F_BYTES_RESIDENT = 24
-F_BYTES_PEAK = 80
 TERRAIN_RADII_M = (30.0, 45.0, 60.0, 90.0, 120.0, 200.0, 400.0, 1000.0, 2000.0)
+TERRAIN_BASE_CUTOFF_M = 30.0   # first build: measures the peak bytes per entry
+F_BYTES_PEAK_FLOOR = 48.0      # per entry: kept keys and values, sort buffers, CSR, row tiles
+TERRAIN_BUILD_CAP_S = 90.0     # longest form-factor build the bench attempts
 
 
-def terrain_cutoff_sizing(ctx, N, F, cutoff_m, frac, hbm_bytes=250e9):
+def device_memory_bytes():
+    """(total, used) bytes of GPU 0 as nvidia-smi reports them, or None."""
+    try:
+        out = subprocess.run(["nvidia-smi", "--query-gpu=memory.total,memory.used", "--format=csv,noheader,nounits",
+                              "-i", "0"], capture_output=True, text=True, timeout=20).stdout.strip().split(",")
+        return float(out[0]) * 1048576.0, float(out[1]) * 1048576.0
+    except Exception:
+        return None
+
+
+def terrain_cutoff_sizing(ctx, N, frac, peak_per_entry, budget_bytes, max_radius_m):
     """The configured 2 km cutoff, sized without building F: visibility of a
     seeded sample of source facets with the 2 km cutoff, giving per source
     the entries its column would hold (nnz estimate N x mean, standard error
-    N x std / sqrt(n)) and the sample's entries within each radius. The
-    largest listed radius whose estimated matrix fits the device at the
-    build's peak is reported beside the cutoff the run used."""
-    if frac <= 0:
-        return None
+    N x std / sqrt(n)) and the sample's entries within each listed radius.
+    A radius fits when its estimated entries times the build's peak bytes
+    per entry stay within the budget (device memory free for it) and it
+    does not exceed max_radius_m (the build-time cap)."""
     import numpy as np
     from illum_gb300 import meshgen
     n = max(16, int(round(frac * N)))
@@ -467,13 +478,15 @@ def terrain_cutoff_sizing(ctx, N, F, cutoff_m, frac, hbm_bytes=250e9):
     el = time.perf_counter() - t0
     per = r["per_source"].astype(np.float64)
     est = {f"{int(x)} m": float(w) * N / n for x, w in zip(TERRAIN_RADII_M, r["within_radius"])}
-    fit = [x for x, w in zip(TERRAIN_RADII_M, r["within_radius"]) if float(w) * N / n * F_BYTES_PEAK <= hbm_bytes]
+    fit = [x for x, w in zip(TERRAIN_RADII_M, r["within_radius"])
+           if float(w) * N / n * peak_per_entry <= budget_bytes and x <= max_radius_m]
+    nnz2k = float(per.mean() * N)
     return {"sample_sources": n, "sample_seed": 77, "rays": r["rays"], "seconds": el,
-            "nnz_2km_estimate": float(per.mean() * N), "nnz_2km_stderr": float(per.std(ddof=1) * N / np.sqrt(n)),
-            "nnz_estimate_by_cutoff": est, "bytes_per_entry_peak": F_BYTES_PEAK,
-            "bytes_per_entry_resident": F_BYTES_RESIDENT, "device_budget_bytes": hbm_bytes,
-            "largest_listed_cutoff_fitting_m": max(fit) if fit else None, "run_cutoff_m": cutoff_m,
-            "run_nnz": F["nnz"], "run_nnz_estimate_from_sample": est.get(f"{int(cutoff_m)} m")}
+            "nnz_2km_estimate": nnz2k, "nnz_2km_stderr": float(per.std(ddof=1) * N / np.sqrt(n)),
+            "bytes_2km_bf16_u16": nnz2k * 4.0, "nnz_estimate_by_cutoff": est,
+            "build_peak_bytes_per_entry": peak_per_entry, "bytes_per_entry_resident": F_BYTES_RESIDENT,
+            "budget_bytes": budget_bytes, "build_time_cap_radius_m": max_radius_m,
+            "largest_listed_cutoff_fitting_m": max(fit) if fit else None}
 
 
 def nested_terrain(ig, meshgen, n, cutoff_m, K, W, sample_frac=0.0025):
@@ -500,12 +513,53 @@ def nested_terrain(ig, meshgen, n, cutoff_m, K, W, sample_frac=0.0025):
     t0 = time.perf_counter()
     ctx.make_horizons(nphi=c["nphi"])
     t_hor = time.perf_counter() - t0
+    # F at the base cutoff, with the allocation pool's high-water mark: the
+    # build's peak device bytes per stored entry
+    ig.device_pool_high(reset=True)
+    used0, _ = ig.device_pool_high()
     t0 = time.perf_counter()
-    ctx.compute_F(albedo=c["albedo"], cutoff=cutoff_m / 1000.0, fetch=False)
+    ctx.compute_F(albedo=c["albedo"], cutoff=TERRAIN_BASE_CUTOFF_M / 1000.0, fetch=False)
     t_ff = time.perf_counter() - t0
+    used1, _ = ig.device_pool_high()
+    F = ctx.F_info()
+    measured = (used1 - used0) / max(1, F["nnz"])
+    peak_per_entry = max(measured, F_BYTES_PEAK_FLOOR)
+    base = {"cutoff_m": TERRAIN_BASE_CUTOFF_M, "nnz": F["nnz"], "form_factors_s": t_ff,
+            "visibility_rays": int(ctx.visibility_rays), "build_peak_bytes": used1 - used0,
+            "build_peak_bytes_per_entry_measured": measured}
+    # candidate pairs grow as the radius squared: the radius whose build
+    # would take TERRAIN_BUILD_CAP_S at the base build's rate
+    max_radius = TERRAIN_BASE_CUTOFF_M * float(np.sqrt(TERRAIN_BUILD_CAP_S / max(t_ff, 1e-3)))
+    sizing = None
+    run_cut = TERRAIN_BASE_CUTOFF_M if cutoff_m is None else cutoff_m
+    if sample_frac > 0:
+        mem = device_memory_bytes()
+        budget = 0.85 * (mem[0] - mem[1]) if mem else 150e9
+        sizing = terrain_cutoff_sizing(ctx, N, sample_frac, peak_per_entry, budget, max_radius)
+        if cutoff_m is None and sizing["largest_listed_cutoff_fitting_m"]:
+            run_cut = sizing["largest_listed_cutoff_fitting_m"]
+    # the chosen radius, else the next smaller listed ones (a build can still
+    # fail: device memory, or a facet seeing more facets than a row tile's
+    # halo holds), down to the base cutoff, whose F is rebuilt last
+    fallback = []
+    tries = [run_cut] + [x for x in sorted(TERRAIN_RADII_M, reverse=True) if TERRAIN_BASE_CUTOFF_M < x < run_cut]
+    if cutoff_m is not None:
+        tries = [run_cut]
+    for cut in tries + [TERRAIN_BASE_CUTOFF_M]:
+        if cut == TERRAIN_BASE_CUTOFF_M and not fallback and run_cut == TERRAIN_BASE_CUTOFF_M:
+            break   # the base F is in place
+        try:
+            t0 = time.perf_counter()
+            ctx.compute_F(albedo=c["albedo"], cutoff=cut / 1000.0, fetch=False)
+            t_ff = time.perf_counter() - t0
+            run_cut = cut
+            break
+        except ig.IlgError as e:
+            fallback.append(f"{cut:g} m failed ({e})")
+    fallback = "; ".join(fallback) if fallback else None
+    cutoff_m = run_cut
     rays = int(ctx.visibility_rays)
     F = ctx.F_info()
-    sizing = terrain_cutoff_sizing(ctx, N, F, cutoff_m, sample_frac)
     ctx.set_insolation(1, 0, CFG["solar"])
     ctx.set_suns(suns, disk)
     E = ctx.get_direct_radiosity(suns[0], disk)
@@ -551,8 +605,16 @@ def nested_terrain(ig, meshgen, n, cutoff_m, K, W, sample_frac=0.0025):
             "frac": ach / peak, "peak_kind": peak_kind, "algorithmic_bytes": b, "avg_ms": ms_rad,
             "sweeps_per_step": sw, "residual_passes_per_step": rounds,
             "traffic": profile_traffic("k_radiosity_mixed_terrain"), "traffic_unit": "bytes per launch (ncu)"}
+    why = "the configuration states 2 km"
+    if sizing:
+        why += (f": estimated {sizing['nnz_2km_estimate']:.3g} entries, {sizing['bytes_2km_bf16_u16'] / 1e9:.0f} GB "
+                f"as bf16 + u16 alone, beyond the device")
+        if fallback:
+            why += f"; {fallback}; ran {cutoff_m:g} m"
+        elif cutoff_m == sizing["largest_listed_cutoff_fitting_m"]:
+            why += f"; {cutoff_m:g} m is the largest listed radius whose build fits"
     label = (f"heightmap {n}x{n} at {c['spacing_m']} m ({N} facets), fBm H {c['hurst']} RMS {c['rms_m']} m, "
-             f"power-law bowls, form factors within {cutoff_m:g} m (the configuration states 2 km), nphi {c['nphi']}, "
+             f"power-law bowls, form factors within {cutoff_m:g} m ({why}), nphi {c['nphi']}, "
              f"radiosity to {c['rel_tol']} of ||E||, nz {c['nz']}, equatorial site, 360 steps per rotation")
     return {"value": N * K / (m["ms"] * 1e-3), "unit": UNIT, "steps": K, "warmup": W, "ms_per_step": m["ms"] / K,
             "dtype": "bf16 F + fp32 conduction (fp64 residual)",
@@ -562,7 +624,7 @@ def nested_terrain(ig, meshgen, n, cutoff_m, K, W, sample_frac=0.0025):
             "visibility_rays": rays, "phases_ms_per_step": res["phases"], "roofline_radiosity": roof,
             "setup_s": {"mesh_s": t_mesh, "bvh_s": t_bvh, "horizons_s": t_hor, "form_factors_s": t_ff},
             "horizon_rays_per_s": N * c["nphi"] * 11 / t_hor, "visibility_rays_per_s": rays / t_ff,
-            "cutoff_sizing": sizing,
+            "cutoff_sizing": sizing, "base_build": base, "cutoff_fallback": fallback,
             "clocks": m["clocks"], "fp64_clocks": d["clocks"], "gpu_launches": 5 * K}
 
 
@@ -689,7 +751,9 @@ def main():
     ap.add_argument("--workload", default="c1", choices=["c1", "batch", "serve", "terrain"],
                     help="c1: the default line; batch / terrain / serve: that nested object alone as the line")
     ap.add_argument("--terrain-n", type=int, default=1024, help="terrain grid points per side (1024: 2,093,058 facets)")
-    ap.add_argument("--terrain-cutoff-m", type=float, default=30.0, help="form-factor cutoff (the terrain configuration states 2000 m)")
+    ap.add_argument("--terrain-cutoff-m", type=float, default=None,
+                    help="form-factor cutoff in m (default: the largest listed radius whose build fits the device; "
+                         "the terrain configuration states 2000 m)")
     ap.add_argument("--terrain-sample", type=float, default=0.0025,
                     help="fraction of source facets whose visibility at the configured 2 km cutoff sizes F (0: skip)")
     ap.add_argument("--serve-requests", type=int, default=500)

@@ -82,6 +82,7 @@ _SIGS = {
     "ilg_set_F": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]),
     "ilg_F_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int),
                              C.POINTER(C.c_int)]),
+    "ilg_device_pool_high": (C.c_int, [C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.c_int]),
     "ilg_F_tiles": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_int)]),
     "ilg_make_horizons": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_double]),
     "ilg_make_horizons_mesh": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_double,
@@ -96,6 +97,7 @@ _SIGS = {
     "ilg_radiosity_solve_gs": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.POINTER(C.c_double)]),
     "ilg_radiosity_levels": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     "ilg_debug_barrier_timeout": (C.c_int, [C.c_void_p, C.c_int, C.c_longlong, C.c_int]),
+    "ilg_debug_ff_chunk": (C.c_int, [C.c_longlong]),
     "ilg_set_radiosity_mode": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "ilg_thermal_init": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_void_p,
                                    C.c_double, C.c_double, C.c_int, C.c_int]),
@@ -552,6 +554,18 @@ class Batch:
 
     def sync(self):
         _check(lib().ilg_batch_sync(self._h))
+
+
+def debug_ff_chunk(pairs):
+    """Candidate pairs per form-factor build chunk (test entry; 0: default)."""
+    _check(lib().ilg_debug_ff_chunk(int(pairs)))
+
+
+def device_pool_high(reset=False):
+    """(used, reserved) high-water bytes of the device's allocation pool."""
+    u, r = C.c_int64(), C.c_int64()
+    _check(lib().ilg_device_pool_high(C.byref(u), C.byref(r), int(reset)))
+    return u.value, r.value
 
 
 def conductionQ(z, dt, Qn, Qnp1, T, ti, rhoc, emiss, Tsurf, Fgeotherm=0.0):

@@ -4,6 +4,7 @@
 // (src/cpp/illum.cpp:31-237). Compiled with -fmad=false: the ray origins,
 // directions and the mt64 predicate must round exactly as geom.h specifies.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <vector>
 
@@ -608,6 +609,37 @@ __global__ void k_ff_compact(const unsigned long long* __restrict__ keys, int64_
   val[p] = fval[k];
 }
 
+// A chunk's kept entries (first occurrence, nonzero form factor): key and
+// value at their scan position.
+__global__ void k_ff_pack(const unsigned long long* __restrict__ keys, int64_t n, const uint32_t* __restrict__ keep,
+                          const unsigned long long* __restrict__ pos, const double* __restrict__ fval,
+                          unsigned long long* okey, double* oval) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n || !keep[k]) return;
+  const int64_t p = (int64_t)pos[k];
+  okey[p] = keys[k];
+  oval[p] = fval[k];
+}
+
+// The entries in (row, column) order: row and column from the sorted key,
+// the value through the sort's permutation (idx == nullptr: no
+// permutation).
+__global__ void k_ff_unpack(const unsigned long long* __restrict__ keys, const uint32_t* __restrict__ idx,
+                            const double* __restrict__ vals, int64_t n, int bits, int32_t* rows, int32_t* col,
+                            double* val) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const unsigned long long key = keys[k];
+  rows[k] = (int32_t)(key >> bits);
+  col[k] = (int32_t)(key & ((1ull << bits) - 1ull));
+  val[k] = vals[idx ? idx[k] : k];
+}
+
+__global__ void k_iota_u32(uint32_t* a, int64_t n) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) a[k] = (uint32_t)k;
+}
+
 __global__ void k_rowptr(const int32_t* __restrict__ rows, int64_t nnz, int nt, int64_t* rowptr) {
   int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r > nt) return;
@@ -885,6 +917,14 @@ int horizons_f32(Context& c) {
 
 // Candidate pairs held on the device at once (8 bytes each).
 constexpr int64_t FF_CHUNK = int64_t(1) << 29;
+// The chunk size in force (a test entry may lower it to exercise the
+// several-chunk path on a small mesh).
+std::atomic<int64_t> g_ff_chunk{FF_CHUNK};
+
+int ff_set_chunk(int64_t pairs) {
+  g_ff_chunk.store(pairs > 0 ? pairs : FF_CHUNK);
+  return ILG_OK;
+}
 
 int form_factors_build(Context& c, const double* albedo_h, double albedo_scalar, double offset, double cutoff,
                        int64_t* rays_out) {
@@ -927,85 +967,122 @@ int form_factors_build(Context& c, const double* albedo_h, double albedo_scalar,
 
   // Sources in chunks of at most FF_CHUNK pairs (a source with more pairs is
   // a chunk of its own): candidate pairs exist for one chunk at a time.
+  const int64_t chunk = g_ff_chunk.load();
   std::vector<int> cut{0};
   int64_t cap = 1;
   while (cut.back() < nt) {
     int a = cut.back(), b = a + 1;
-    while (b < nt && (int64_t)(offs_h[b + 1] - offs_h[a]) <= FF_CHUNK) ++b;
+    while (b < nt && (int64_t)(offs_h[b + 1] - offs_h[a]) <= chunk) ++b;
     cap = std::max<int64_t>(cap, (int64_t)(offs_h[b] - offs_h[a]));
     cut.push_back(b);
   }
   c.have_F = false;
   c.gs_ready = false;
   c.ntiles = 0;
-  dbuf<int32_t> ci, cj;
-  dbuf<unsigned long long> ukeys, ucount;
-  ILG_TRY(ci.alloc(cap));
-  ILG_TRY(cj.alloc(cap));
-  ILG_TRY(ucount.alloc(1));
-  ILG_CUDA(cudaMemsetAsync(ucount.p, 0, 8, s));
-  int64_t ucap = 0;   // ukeys capacity; kept >= keys so far + the next chunk's pairs
-  unsigned long long nkeys = 0;
-  for (size_t q = 0; q + 1 < cut.size(); ++q) {
-    const int a = cut[q], b = cut[q + 1];
-    const int64_t np = (int64_t)(offs_h[b] - offs_h[a]);
-    if (np == 0) continue;
-    if ((int64_t)nkeys + np > ucap) {
-      int64_t want = std::min<int64_t>(npairs, std::max<int64_t>(2 * ucap, (int64_t)nkeys + np));
-      dbuf<unsigned long long> grown;
-      ILG_TRY(grown.alloc(want));
-      if (nkeys > 0) ILG_CUDA(cudaMemcpyAsync(grown.p, ukeys.p, nkeys * 8, cudaMemcpyDeviceToDevice, s));
-      ILG_CUDA(cudaStreamSynchronize(s));
-      std::swap(ukeys, grown);
-      ucap = want;
+  // Per chunk: its rays' distinct hit keys (sorted), their form factors, and
+  // the kept entries (first occurrence, nonzero) packed into the chunk's own
+  // arrays. Chunks own disjoint sources, so no key repeats across chunks and
+  // only the kept entries outlive their chunk.
+  std::vector<dbuf<unsigned long long>> ck;
+  std::vector<dbuf<double>> cv;
+  std::vector<int64_t> cn;
+  {
+    dbuf<int32_t> ci, cj;
+    dbuf<unsigned long long> ukeys, ucount, pos;
+    dbuf<uint32_t> keep;
+    dbuf<double> fval, alb;
+    ILG_TRY(ci.alloc(cap));
+    ILG_TRY(cj.alloc(cap));
+    ILG_TRY(ukeys.alloc(cap));
+    ILG_TRY(keep.alloc(cap));
+    ILG_TRY(fval.alloc(cap));
+    ILG_TRY(pos.alloc(cap));
+    ILG_TRY(ucount.alloc(1));
+    if (albedo_h) {
+      ILG_TRY(alb.alloc(nt));
+      ILG_CUDA(cudaMemcpyAsync(alb.p, albedo_h, (size_t)nt * 8, cudaMemcpyHostToDevice, s));
     }
-    k_candidates<true><<<div_up((int64_t)(b - a) * FF_SPLIT, 128), 128, 0, s>>>(
-        c.nodes.p, c.tri_s.p, front.p, front.p + FF_SPLIT, c.cen.p, c.nrm.p, a, b, nullptr, c.r_max, slack, cut2,
-        box_cut2, nullptr, offs.p + (size_t)a * FF_SPLIT, offs_h[a], ci.p, cj.p, c.derr.p);
-    ILG_CUDA(cudaGetLastError());
-    k_vis_rays<<<div_up(np, 128), 128, 0, s>>>(c.nodes.p, c.tri_s.p, c.root, c.cen.p, c.nrm.p, np, ci.p, cj.p,
-                                               (float)offset, bits, ukeys.p, ucount.p, c.derr.p);
-    ILG_CUDA(cudaGetLastError());
-    ILG_CUDA(cudaMemcpyAsync(&nkeys, ucount.p, 8, cudaMemcpyDeviceToHost, s));
-    ILG_CUDA(cudaStreamSynchronize(s));
-  }
-  ci.release();
-  cj.release();
-  const int64_t n = (int64_t)nkeys;
-  if (n > 1) ILG_TRY(radix_sort_u64(ukeys.p, nullptr, n, 2 * bits, c.sort, s));
-  dbuf<unsigned long long>& keys = ukeys;
-  dbuf<uint32_t> keep;
-  dbuf<double> fval;
-  dbuf<unsigned long long> pos;
-  dbuf<double> alb;
-  ILG_TRY(keep.alloc(n > 0 ? n : 1));
-  ILG_TRY(fval.alloc(n > 0 ? n : 1));
-  ILG_TRY(pos.alloc(n > 0 ? n : 1));
-  if (albedo_h) {
-    ILG_TRY(alb.alloc(nt));
-    ILG_CUDA(cudaMemcpyAsync(alb.p, albedo_h, (size_t)nt * 8, cudaMemcpyHostToDevice, s));
+    for (size_t q = 0; q + 1 < cut.size(); ++q) {
+      const int a = cut[q], b = cut[q + 1];
+      const int64_t np = (int64_t)(offs_h[b] - offs_h[a]);
+      if (np == 0) continue;
+      ILG_CUDA(cudaMemsetAsync(ucount.p, 0, 8, s));
+      k_candidates<true><<<div_up((int64_t)(b - a) * FF_SPLIT, 128), 128, 0, s>>>(
+          c.nodes.p, c.tri_s.p, front.p, front.p + FF_SPLIT, c.cen.p, c.nrm.p, a, b, nullptr, c.r_max, slack, cut2,
+          box_cut2, nullptr, offs.p + (size_t)a * FF_SPLIT, offs_h[a], ci.p, cj.p, c.derr.p);
+      ILG_CUDA(cudaGetLastError());
+      k_vis_rays<<<div_up(np, 128), 128, 0, s>>>(c.nodes.p, c.tri_s.p, c.root, c.cen.p, c.nrm.p, np, ci.p, cj.p,
+                                                 (float)offset, bits, ukeys.p, ucount.p, c.derr.p);
+      ILG_CUDA(cudaGetLastError());
+      unsigned long long nk = 0;
+      ILG_CUDA(cudaMemcpyAsync(&nk, ucount.p, 8, cudaMemcpyDeviceToHost, s));
+      ILG_CUDA(cudaStreamSynchronize(s));
+      if (nk == 0) continue;
+      if (nk > 1) ILG_TRY(radix_sort_u64(ukeys.p, nullptr, (int64_t)nk, 2 * bits, c.sort, s));
+      k_ff_values<<<div_up((int64_t)nk, 256), 256, 0, s>>>(ukeys.p, (int64_t)nk, bits, nt, c.cen.p, c.nrm.p,
+                                                          c.area.p, alb.p, albedo_scalar, keep.p, fval.p, c.derr.p);
+      ILG_CUDA(cudaGetLastError());
+      ILG_TRY(scan_exclusive_u32_to_u64(keep.p, pos.p, (int64_t)nk, c.scan, s));
+      unsigned long long lp = 0;
+      uint32_t lk = 0;
+      ILG_CUDA(cudaMemcpyAsync(&lp, pos.p + (nk - 1), 8, cudaMemcpyDeviceToHost, s));
+      ILG_CUDA(cudaMemcpyAsync(&lk, keep.p + (nk - 1), 4, cudaMemcpyDeviceToHost, s));
+      ILG_CUDA(cudaStreamSynchronize(s));
+      const int64_t nkeep = (int64_t)lp + lk;
+      if (nkeep == 0) continue;
+      ck.emplace_back();
+      cv.emplace_back();
+      ILG_TRY(ck.back().alloc(nkeep));
+      ILG_TRY(cv.back().alloc(nkeep));
+      cn.push_back(nkeep);
+      k_ff_pack<<<div_up((int64_t)nk, 256), 256, 0, s>>>(ukeys.p, (int64_t)nk, keep.p, pos.p, fval.p,
+                                                         ck.back().p, cv.back().p);
+      ILG_CUDA(cudaGetLastError());
+    }
   }
   int64_t nnz = 0;
-  if (n > 0) {
-    k_ff_values<<<div_up(n, 256), 256, 0, s>>>(keys.p, n, bits, nt, c.cen.p, c.nrm.p, c.area.p, alb.p,
-                                               albedo_scalar, keep.p, fval.p, c.derr.p);
-    ILG_CUDA(cudaGetLastError());
-    ILG_TRY(scan_exclusive_u32_to_u64(keep.p, pos.p, n, c.scan, s));
-    unsigned long long lp = 0;
-    uint32_t lk = 0;
-    ILG_CUDA(cudaMemcpyAsync(&lp, pos.p + (n - 1), 8, cudaMemcpyDeviceToHost, s));
-    ILG_CUDA(cudaMemcpyAsync(&lk, keep.p + (n - 1), 4, cudaMemcpyDeviceToHost, s));
-    ILG_CUDA(cudaStreamSynchronize(s));
-    nnz = (int64_t)lp + lk;
-  }
+  for (int64_t x : cn) nnz += x;
+  if (nnz > (int64_t)0xffffffffLL) { set_error("%lld form-factor entries exceed the 32-bit entry index", (long long)nnz); return ILG_ERR_ARG; }
   ILG_TRY(read_device_errors(c));
+  // all entries in (row, column) order: one chunk is sorted already; several
+  // are concatenated and sorted by key, the values following the permutation
   dbuf<int32_t> rows;
-  ILG_TRY(rows.alloc(nnz > 0 ? nnz : 1));
-  ILG_TRY(c.col.alloc(nnz > 0 ? nnz : 1));
-  ILG_TRY(c.val.alloc(nnz > 0 ? nnz : 1));
+  auto alloc_csr = [&]() -> int {
+    ILG_TRY(rows.alloc(nnz > 0 ? nnz : 1));
+    ILG_TRY(c.col.alloc(nnz > 0 ? nnz : 1));
+    ILG_TRY(c.val.alloc(nnz > 0 ? nnz : 1));
+    return ILG_OK;
+  };
   ILG_TRY(c.rowptr.alloc((size_t)nt + 1));
-  if (n > 0) {
-    k_ff_compact<<<div_up(n, 256), 256, 0, s>>>(keys.p, n, bits, keep.p, pos.p, fval.p, rows.p, c.col.p, c.val.p);
+  if (ck.size() <= 1) ILG_TRY(alloc_csr());
+  if (ck.size() == 1) {
+    k_ff_unpack<<<div_up(nnz, 256), 256, 0, s>>>(ck[0].p, nullptr, cv[0].p, nnz, bits, rows.p, c.col.p, c.val.p);
+    ILG_CUDA(cudaGetLastError());
+    ck.clear();
+    cv.clear();
+  } else if (ck.size() > 1) {
+    dbuf<unsigned long long> ekeys;
+    dbuf<double> evals;
+    dbuf<uint32_t> eidx;
+    ILG_TRY(ekeys.alloc(nnz));
+    ILG_TRY(evals.alloc(nnz));
+    int64_t off = 0;
+    for (size_t q = 0; q < ck.size(); ++q) {
+      ILG_CUDA(cudaMemcpyAsync(ekeys.p + off, ck[q].p, (size_t)cn[q] * 8, cudaMemcpyDeviceToDevice, s));
+      ILG_CUDA(cudaMemcpyAsync(evals.p + off, cv[q].p, (size_t)cn[q] * 8, cudaMemcpyDeviceToDevice, s));
+      off += cn[q];
+      ck[q].release();
+      cv[q].release();
+    }
+    ck.clear();
+    cv.clear();
+    ILG_TRY(eidx.alloc(nnz));
+    k_iota_u32<<<div_up(nnz, 256), 256, 0, s>>>(eidx.p, nnz);
+    ILG_CUDA(cudaGetLastError());
+    ILG_TRY(radix_sort_u64(ekeys.p, eidx.p, nnz, 2 * bits, c.sort, s));
+    c.sort.release();
+    ILG_TRY(alloc_csr());
+    k_ff_unpack<<<div_up(nnz, 256), 256, 0, s>>>(ekeys.p, eidx.p, evals.p, nnz, bits, rows.p, c.col.p, c.val.p);
     ILG_CUDA(cudaGetLastError());
   }
   k_rowptr<<<div_up(nt + 1, 256), 256, 0, s>>>(rows.p, nnz, nt, c.rowptr.p);
@@ -1013,15 +1090,12 @@ int form_factors_build(Context& c, const double* albedo_h, double albedo_scalar,
   ILG_CUDA(cudaStreamSynchronize(s));
   c.nnz = nnz;
   c.have_F = true;
-  keys.release();
-  keep.release();
-  fval.release();
-  pos.release();
   rows.release();
   ILG_TRY(radiosity_prepare(c));
   // the sort and scan scratch grew to the entry count: not kept resident
   c.sort.release();
   c.scan.release();
+  if (nnz > (int64_t(1) << 26)) ILG_TRY(pool_trim(s));
   return read_device_errors(c);
 }
 

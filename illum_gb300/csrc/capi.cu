@@ -55,6 +55,19 @@ int alloc_pool_setup() {
   return ILG_OK;
 }
 
+// Return the pool's unused reserved memory to the device (after a build
+// whose scratch was large, so that a later allocation outside the pool
+// finds the memory free).
+int pool_trim(cudaStream_t s) {
+  int dev = 0;
+  ILG_CUDA(cudaGetDevice(&dev));
+  cudaMemPool_t pool;
+  ILG_CUDA(cudaDeviceGetDefaultMemPool(&pool, dev));
+  ILG_CUDA(cudaStreamSynchronize(s));
+  ILG_CUDA(cudaMemPoolTrimTo(pool, 0));
+  return ILG_OK;
+}
+
 int read_device_errors(Context& c) {
   int h[DERR_COUNT];
   ILG_CUDA(cudaMemcpyAsync(h, c.derr.p, sizeof(h), cudaMemcpyDeviceToHost, c.stream));
@@ -566,6 +579,25 @@ int ilg_F_info(const ilg_ctx* ctx, int64_t* nnz, int64_t* stored_entries, int* r
   return ILG_OK;
 }
 
+int ilg_device_pool_high(int64_t* used_high, int64_t* reserved_high, int reset) {
+  ILG_TRY(alloc_pool_setup());
+  int dev = 0;
+  ILG_CUDA(cudaGetDevice(&dev));
+  cudaMemPool_t pool;
+  ILG_CUDA(cudaDeviceGetDefaultMemPool(&pool, dev));
+  uint64_t u = 0, r = 0;
+  ILG_CUDA(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemHigh, &u));
+  ILG_CUDA(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemHigh, &r));
+  if (used_high) *used_high = (int64_t)u;
+  if (reserved_high) *reserved_high = (int64_t)r;
+  if (reset) {
+    uint64_t z = 0;
+    ILG_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrUsedMemHigh, &z));
+    ILG_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReservedMemHigh, &z));
+  }
+  return ILG_OK;
+}
+
 int ilg_F_tiles(const ilg_ctx* ctx, int cap, int* entries_per_thread, int* rows, int* halo, int* ntiles) {
   if (!ctx || !ctx->c.have_F || !ntiles || cap < 0) { set_error("invalid arguments"); return ILG_ERR_ARG; }
   const Context& c = ctx->c;
@@ -581,6 +613,7 @@ int ilg_F_tiles(const ilg_ctx* ctx, int cap, int* entries_per_thread, int* rows,
 
 int ilg_trace(ilg_ctx* ctx, int nrays, const float* orig, const float* dir, int any_hit, int32_t* hit, double* t) {
   if (!ctx || nrays < 0 || (nrays > 0 && (!orig || !dir || !hit))) { set_error("invalid trace arguments"); return ILG_ERR_ARG; }
+  AllocOn on_(ctx->c.stream);
   return bvh_trace(ctx->c, nrays, orig, dir, any_hit, hit, t);
 }
 
@@ -589,11 +622,13 @@ int ilg_render(ilg_ctx* ctx, int mode, double az_deg, double el_deg, int width, 
     set_error("invalid render arguments");
     return ILG_ERR_ARG;
   }
+  AllocOn on_(ctx->c.stream);
   return bvh_render(ctx->c, mode, az_deg, el_deg, width, height, facet_out);
 }
 
 int ilg_compute_F(ilg_ctx* ctx, const double* albedo, double albedo_scalar, double offset, int64_t* nnz, int64_t* rays) {
   if (!ctx) { set_error("ctx is NULL"); return ILG_ERR_ARG; }
+  AllocOn on_(ctx->c.stream);
   invalidate_graph(ctx->c);
   ILG_TRY(form_factors_build(ctx->c, albedo, albedo_scalar, offset, 0.0, rays));
   if (nnz) *nnz = ctx->c.nnz;
@@ -604,6 +639,7 @@ int ilg_compute_F_cutoff(ilg_ctx* ctx, const double* albedo, double albedo_scala
                          int64_t* nnz, int64_t* rays) {
   if (!ctx) { set_error("ctx is NULL"); return ILG_ERR_ARG; }
   if (!(cutoff > 0.0)) { set_error("cutoff must be > 0"); return ILG_ERR_ARG; }
+  AllocOn on_(ctx->c.stream);
   invalidate_graph(ctx->c);
   ILG_TRY(form_factors_build(ctx->c, albedo, albedo_scalar, offset, cutoff, rays));
   if (nnz) *nnz = ctx->c.nnz;
@@ -813,6 +849,8 @@ int ilg_radiosity_solve_gs(ilg_ctx* ctx, const double* E, int gs_steps, double* 
   }
   return ILG_OK;
 }
+
+int ilg_debug_ff_chunk(long long pairs) { return ff_set_chunk((int64_t)pairs); }
 
 int ilg_debug_barrier_timeout(ilg_ctx* ctx, int blocks, long long polls, int unreachable) {
   if (!ctx) { set_error("ctx is NULL"); return ILG_ERR_ARG; }

@@ -54,6 +54,7 @@ struct AllocOn {
 };
 // Keeps freed pool memory cached in the process (set once per device).
 int alloc_pool_setup();
+int pool_trim(cudaStream_t s);
 
 // A stream destroyed last: the first member of an object whose buffers
 // are freed on it, so their stream-ordered frees are queued before the
@@ -102,6 +103,7 @@ struct dbuf {
     if (e != cudaSuccess) {
       if (p && st) cudaFreeAsync(p, st);
       p = nullptr;
+      cudaGetLastError();   // an allocation failure is not sticky: clear it for the caller's later checks
       set_error("device allocation of %zu bytes failed: %s", count * sizeof(T), cudaGetErrorString(e));
       return ILG_ERR_NOMEM;
     }

@@ -327,6 +327,7 @@ int direct_launch(const StepView& v, int dropin, int mu32_flux, int ahead, cudaS
 // ---- radiosity.cu ----
 int radiosity_prepare(Context& c);
 int radiosity_grid(int ntiles, int precision);
+int ff_set_chunk(int64_t pairs);   // candidate pairs per form-factor chunk (<= 0: the default)
 // Balanced assignment of row tiles to the grid's blocks (longest tiles
 // first, each to the least loaded block); uploads it to start/order.
 int radiosity_schedule(const std::vector<RowTile>& tiles, int grid, dbuf<int>& start, dbuf<int>& order,

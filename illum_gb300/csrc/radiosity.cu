@@ -75,7 +75,7 @@ namespace {
 
 constexpr int RAD_THREADS = 992;             // consumer threads (31 warps): one entry run each
 constexpr int RAD_BLOCK = RAD_THREADS + 32;  // and one producer warp that issues the entry-stream copies
-constexpr int RAD_HALO = 6144;           // halo values per tile (double-float: 48 KB of shared memory)
+constexpr int RAD_HALO = 8192;           // halo values per tile (double-float: 64 KB of shared memory)
 constexpr int RAD_ROWS = 3072;           // rows per tile (their sums: 24 KB of shared memory)
 constexpr int RAD_MAX_MESH = 1024;
 constexpr int RAD_INNER = 2;             // most fp32 sweeps per refinement of the mixed solve: the bf16 error

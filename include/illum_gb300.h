@@ -82,6 +82,11 @@ int ilg_ctx_info(const ilg_ctx* ctx, int64_t* bvh_nodes, int* bvh_depth);
  * scratch). No reference counterpart: the serving loop admits jobs by this
  * footprint. */
 int ilg_ctx_device_bytes(const ilg_ctx* ctx, int64_t* bytes);
+/* High-water marks of the current device's stream-ordered allocation pool,
+ * which every context allocates from: bytes in use and bytes reserved, since
+ * the last reset (reset != 0 clears both after reading). No reference
+ * counterpart: sizing aid for builds that approach the device's memory. */
+int ilg_device_pool_high(int64_t* used_high, int64_t* reserved_high, int reset);
 
 /* ---- closest / any hit (BVH::getIntersection) ----------------------------- */
 /* hit[r] = index of the closest triangle hit by ray r (or the first found
@@ -264,6 +269,11 @@ int ilg_set_timing(ilg_ctx* ctx, int enable);
  * limit is a per-device setting for the duration of the launch: do not run
  * radiosity solves on the same device meanwhile. */
 int ilg_debug_barrier_timeout(ilg_ctx* ctx, int blocks, long long polls, int unreachable);
+/* Test entry for the form-factor build: candidate pairs per source chunk
+ * (process-wide; <= 0 restores the default of 2^29). A small value runs a
+ * small mesh through the several-chunk path, whose matrix must equal the
+ * one-chunk build's. Not for concurrent use with other builds. */
+int ilg_debug_ff_chunk(long long pairs);
 
 /* ---- launch-shape autotuner (no reference counterpart) ------------------------ */
 /* Launch shapes of the step kernels. No result depends on them (every

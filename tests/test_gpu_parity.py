@@ -101,6 +101,29 @@ def test_form_factors_bit_exact(ilg, oracle_mod, mesh_l4):
     assert np.array_equal(rowptr, rp) and np.array_equal(col, c) and np.array_equal(val, x)
 
 
+@pytest.mark.parametrize("chunk", [997, 20000])
+def test_form_factors_several_chunks_bit_exact(ilg, oracle_mod, mesh_l4, chunk):
+    """The build in source chunks of `chunk` candidate pairs (many chunks,
+    each deduplicated on its own, then merged by a global sort) gives the
+    one-chunk build's matrix and the oracle's, bit for bit, and the radiosity
+    tiles built from it solve the same system."""
+    v, f = mesh_l4
+    ctx = ilg.IllumContext(v, f)
+    try:
+        ilg.debug_ff_chunk(chunk)
+        rowptr, col, val = ctx.compute_F(albedo=0.1)
+    finally:
+        ilg.debug_ff_chunk(0)
+    ro, co, vo, rays = oracle_mod.form_factors(v, f, albedo_scalar=0.1)
+    rp, c, x = oracle_mod.coo_to_csr(f.shape[0], ro, co, vo)
+    assert ctx.visibility_rays == rays
+    assert np.array_equal(rowptr, rp) and np.array_equal(col, c) and np.array_equal(val, x)
+    ref = ilg.IllumContext(v, f)
+    ref.compute_F(albedo=0.1)
+    E = np.random.default_rng(5).uniform(0.0, 800.0, f.shape[0])
+    assert np.array_equal(ctx.radiosity_solve(E, tol=1e-10)[0], ref.radiosity_solve(E, tol=1e-10)[0])
+
+
 def test_form_factors_per_facet_albedo(ilg, oracle_mod, mesh_l3):
     v, f = mesh_l3
     alb = np.random.default_rng(2).uniform(0.05, 0.3, f.shape[0])
