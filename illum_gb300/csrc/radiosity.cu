@@ -81,6 +81,7 @@ constexpr int RAD_MAX_MESH = 1024;
 constexpr int RAD_INNER = 2;             // most fp32 sweeps per refinement of the mixed solve: the bf16 error
                                          // (~4e-3 of the correction) already dominates rho^(k+1), rho ~ 0.013
 constexpr int64_t RAD_MIN_TILE = 16384;  // entries: smaller tiles cost more in staging than they balance
+constexpr int64_t RAD_SPLIT_MIN = 131072;  // entries: tiles above twice the split target are halved
 // Tile balance, in stored entries: a block's sweep time is about
 // c + 1.35e-4 us per stored entry + 8.8e-4 us per row + 1.5e-4 us per halo
 // facet (per-block timings of the FP64 sweep on GB300, 152 tiles of an
@@ -1312,6 +1313,11 @@ int radiosity_prepare(Context& c) {
     ILG_TRY(before.alloc(nnz));
     ILG_TRY(t_halo_tmp.alloc(nnz));
   }
+  // Tiles much larger than nnz / (4 x blocks) entries are halved as well
+  // (when that is above RAD_SPLIT_MIN): with a few tiles per block the
+  // longest-first schedule keeps the blocks' loads within a tile of each
+  // other.
+  const int64_t split_target = std::max<int64_t>(RAD_SPLIT_MIN, nnz / (4 * (int64_t)G));
   for (int iter = 0; !tiles.empty(); ++iter) {
     ntile = (int)tiles.size();
     stored_total = 0;
@@ -1363,7 +1369,8 @@ int radiosity_prepare(Context& c) {
       T.h0 = tfirst[tid];
       T.nhalo = tfirst[tid + 1] - tfirst[tid];
       if (T.nhalo < 1) { set_error("row tile without a halo"); return ILG_ERR_CUDA; }
-      if (T.nhalo <= RAD_HALO || T.nrows < 2) {
+      const bool big = tile_ne[tid] > 2 * split_target;
+      if ((T.nhalo <= RAD_HALO && !big) || T.nrows < 2) {
         if (T.nhalo > RAD_HALO) { set_error("row tile halo of %d facets", T.nhalo); return ILG_ERR_CUDA; }
         nt_tiles.push_back(T);
         nt_a.push_back(tile_a[tid]);
