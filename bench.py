@@ -90,12 +90,12 @@ def _peaks():
         return 6800.0, "fallback"
 
 
-def profile_traffic(name: str):
-    """DRAM bytes per launch recorded in profiles/<name>.md (the line
-    `dram_bytes_per_launch: <bytes>` of an ncu capture summary), or None."""
+def profile_traffic(name: str, key: str = "dram_bytes_per_launch"):
+    """A figure recorded in profiles/<name>.md (the line `<key>: <value>` of
+    an ncu capture summary), or None."""
     try:
         with open(os.path.join(ROOT, "profiles", name + ".md")) as f:
-            m = re.search(r"^dram_bytes_per_launch:\s*([0-9.eE+]+)", f.read(), re.M)
+            m = re.search(r"^" + key + r":\s*([0-9.eE+]+)", f.read(), re.M)
         return float(m.group(1)) if m else None
     except OSError:
         return None
@@ -604,7 +604,15 @@ def nested_terrain(ig, meshgen, n, cutoff_m, K, W, sample_frac=0.0025):
     roof = {"kernel": "k_radiosity_mixed", "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
             "frac": ach / peak, "peak_kind": peak_kind, "algorithmic_bytes": b, "avg_ms": ms_rad,
             "sweeps_per_step": sw, "residual_passes_per_step": rounds,
-            "traffic": profile_traffic("k_radiosity_mixed_terrain"), "traffic_unit": "bytes per launch (ncu)"}
+            "traffic": None, "traffic_unit": "bytes per launch"}
+    # ncu's DRAM bytes of the captured 512 x 512 launch per algorithmic byte,
+    # scaled to this launch's algorithmic bytes (traffic grows with them)
+    cap_t = profile_traffic("k_radiosity_mixed_terrain512")
+    cap_a = profile_traffic("k_radiosity_mixed_terrain512", "algorithmic_bytes_per_launch")
+    if cap_t and cap_a:
+        roof["traffic"] = b * cap_t / cap_a
+        roof["traffic_source"] = ("profiles/k_radiosity_mixed_terrain512.md (ncu, 512 x 512 terrain), "
+                                  "scaled by algorithmic bytes")
     why = "the configuration states 2 km"
     if sizing:
         why += (f": estimated {sizing['nnz_2km_estimate']:.3g} entries, {sizing['bytes_2km_bf16_u16'] / 1e9:.0f} GB "
