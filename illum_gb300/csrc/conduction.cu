@@ -140,10 +140,9 @@ __device__ __forceinline__ double df_to_double(dfloat x) { return (double)x.h + 
 // increment being P + S_top x. polish: double-float Newton steps after the
 // FP32 ones (the FP64 step's accuracy).
 struct TopResult { dfloat dtop, top, tsn; };
-__device__ __forceinline__ TopResult newton_top(const CondScalars& cs, dfloat T0, dfloat T1, dfloat rho1, double Ts,
-                                                double Q, bool polish) {
+__device__ __forceinline__ TopResult newton_top(const CondScalars& cs, dfloat T0, dfloat T1, dfloat rho1, dfloat Tsd,
+                                                dfloat Qd, bool polish) {
   const dfloat al0 = to_df(cs.d_al0), g0 = to_df(cs.d_g0), f0 = to_df(cs.d_f0), iAp = to_df(cs.d_inv_Ap);
-  const dfloat Tsd(Ts), Qd(Q);
   const dfloat two(2.f, 0.f), four(4.f, 0.f);
   // R0 = 2 al0 (T1 - T0) + 4 g0 (Ts - T0) - 2 g0 Ts; P = (R0 - f0 rho1) / Ap
   const dfloat R0 = two * al0 * (T1 - T0) + four * g0 * (Tsd - T0) - two * g0 * Tsd;
@@ -151,7 +150,7 @@ __device__ __forceinline__ TopResult newton_top(const CondScalars& cs, dfloat T0
   const dfloat A = Qd + to_df(cs.d_2k1) * (T0 + P);
   const float Af = __fadd_rn(A.h, A.l), Bf = cs.B_topf, esf = cs.esf;
   const float tol = polish ? 1e-6f : 2.4e-7f;
-  float xf = __double2float_rn(Ts);
+  float xf = __fadd_rn(Tsd.h, Tsd.l);
   // from the previous surface temperature Newton converges in a few steps;
   // it stops at the tolerance or once a step no longer shrinks (the FP32
   // rounding floor of g)
@@ -284,12 +283,17 @@ k_conduct(StepView v, const double* __restrict__ Qnp1, int upd) {
       // (P = T1(n+1) - S_top Ts(n+1) is a small difference of
       // temperature-sized terms), the root by FP32 Newton steps, polished in
       // double-float for the FP64 step (no FP64 arithmetic)
-      const TopResult tr = newton_top(cs, to_df(Ti), to_df(Tip1), to_df(rho_next), Ts_prev, Q,
-                                      std::is_same<R, dfloat>::value);
-      Tsn = df_to_double(tr.tsn);
+      // the double-float step takes Ts and Q to 48 bits; the FP32 step in
+      // FP32 (its layers are FP32), converting each once
+      constexpr bool DF = std::is_same<R, dfloat>::value;
+      const dfloat Tsd = DF ? dfloat(Ts_prev) : dfloat(__double2float_rn(Ts_prev), 0.f);
+      const dfloat Qd = DF ? dfloat(Q) : dfloat(__double2float_rn(Q), 0.f);
+      const TopResult tr = newton_top(cs, to_df(Ti), to_df(Tip1), to_df(rho_next), Tsd, Qd, DF);
+      const dfloat fsd = (tr.top - tr.tsn) * to_df(cs.d_kz);
+      Tsn = DF ? df_to_double(tr.tsn) : (double)__fadd_rn(tr.tsn.h, tr.tsn.l);
       top = from_df<R>(tr.top);
       dtop = from_df<R>(tr.dtop);
-      Fs = -df_to_double((tr.top - tr.tsn) * to_df(cs.d_kz));
+      Fs = DF ? -df_to_double(fsd) : -(double)__fadd_rn(fsd.h, fsd.l);
       T0n = 0.0;
       done_top = true;
     }
@@ -398,7 +402,8 @@ k_conduct(StepView v, const double* __restrict__ Qnp1, int upd) {
   }
   if (upd) {
     // running means: 1/(frame + 1) by an FP32 reciprocal and two FP64
-    // Newton steps (no FP64 division)
+    // Newton steps (no FP64 division; computing it here is cheaper than
+    // loading a per-mesh value at the end of the column)
     const double n = (double)(M.frame + 1);
     double rn = (double)__frcp_rn((float)n);
     rn = rn * (2.0 - n * rn);

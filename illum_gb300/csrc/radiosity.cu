@@ -954,11 +954,13 @@ __global__ void __launch_bounds__(RAD_BLOCK, 1) k_radiosity_mixed(StepView v, do
               nxt[i] = ld_it(r32 + i) + __ldg(scale + r) * rsf[r];
             }
           } else {   // last sweep: nobody reads d again, s += d directly
+            // (x for the halos only if the mesh runs another round)
+            const bool more = st.sweeps[T.mesh] + inner < v.md[T.mesh].max_sweeps;
             for (int r = threadIdx.x; r < T.nrows; r += RAD_THREADS) {
               uint32_t i = __ldg(rows + r);
               const float2 d = make_float2(ld_it(r32 + i) + __ldg(scale + r) * rsf[r], 0.f);
               S[i] = df_add(ld_it(S + i), d);
-              XH[i] = df_add(ld_it(XH + i), d);
+              if (more) XH[i] = df_add(ld_it(XH + i), d);
             }
           }
           cbar();
