@@ -94,6 +94,7 @@ _SIGS = {
     "ilg_direct_radiosity": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     "ilg_radiosity_solve": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_int, C.c_void_p,
                                       C.POINTER(C.c_double), C.POINTER(C.c_int)]),
+    "ilg_set_radiosity_blocks": (C.c_int, [C.c_void_p, C.c_int]),
     "ilg_radiosity_solve_gs": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.POINTER(C.c_double)]),
     "ilg_radiosity_levels": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     "ilg_debug_barrier_timeout": (C.c_int, [C.c_void_p, C.c_int, C.c_longlong, C.c_int]),
@@ -343,6 +344,10 @@ class IllumContext:
         _check(lib().ilg_radiosity_solve(self._h, _p(E), tol, max_sweeps, _p(x), C.byref(res), C.byref(sw)))
         return x, res.value, sw.value
 
+    def set_radiosity_blocks(self, blocks: int):
+        """Cut the radiosity row tiles for `blocks` blocks (0: all the device holds)."""
+        _check(lib().ilg_set_radiosity_blocks(self._h, int(blocks)))
+
     def radiosity_solve_gs(self, E, gs_steps=1):
         """The reference's solve: forward solve + gs_steps natural-order
         Gauss-Seidel sweeps (src/cpp/illum_cli.cpp:425-433). Returns (x, res)."""
@@ -554,6 +559,12 @@ class Batch:
 
     def sync(self):
         _check(lib().ilg_batch_sync(self._h))
+
+
+def radiosity_blocks_for(nnz: int, entries_per_tile: int = 200_000) -> int:
+    """A block count that gives tiles of about `entries_per_tile` entries
+    (at least one block): for meshes solved beside others."""
+    return max(1, -(-int(nnz) // entries_per_tile))
 
 
 def debug_ff_chunk(pairs):

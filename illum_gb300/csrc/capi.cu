@@ -824,6 +824,20 @@ int ilg_set_radiosity_mode(ilg_ctx* ctx, int mode, int gs_steps) {
   return ILG_OK;
 }
 
+int ilg_set_radiosity_blocks(ilg_ctx* ctx, int blocks) {
+  if (!ctx || blocks < 0) { set_error("invalid radiosity block count %d", blocks); return ILG_ERR_ARG; }
+  Context& c = ctx->c;
+  AllocOn on_(c.stream);
+  if (c.tile_blocks == blocks) return ILG_OK;
+  c.tile_blocks = blocks;
+  if (!c.have_F) return ILG_OK;
+  invalidate_graph(c);
+  ILG_TRY(radiosity_prepare(c));
+  c.sort.release();
+  c.scan.release();
+  return ILG_OK;
+}
+
 int ilg_radiosity_solve_gs(ilg_ctx* ctx, const double* E, int gs_steps, double* x, double* res) {
   if (!ctx || !E || !x || gs_steps < 0) { set_error("invalid radiosity arguments"); return ILG_ERR_ARG; }
   Context& c = ctx->c;

@@ -220,6 +220,7 @@ struct Context {
   dbuf<double> tile_d2;
   dbuf<int> sched_start, sched_tile;   // per-block tile schedule (radiosity_schedule)
   int sched_grid = 0;
+  int tile_blocks = 0;                 // row tiles cut for this many blocks (0: every co-resident block)
   dbuf<uint8_t> row_act;
   dbuf<uint32_t> rperm;           // Morton position -> facet (radiosity's internal order)
   // the reference's fixed-sweep Gauss-Seidel (gauss_seidel.cu)

@@ -1222,7 +1222,8 @@ int radiosity_prepare(Context& c) {
   // block. Halos are then counted exactly on the device and a tile whose
   // halo exceeds the shared-memory capacity is split in two, until none
   // does.
-  const int G = g_rad_nsm * std::min(g_rad_per_sm64, g_rad_per_smm);
+  const int Gdev = g_rad_nsm * std::min(g_rad_per_sm64, g_rad_per_smm);
+  const int G = c.tile_blocks > 0 ? std::min(Gdev, c.tile_blocks) : Gdev;
   std::vector<RowTile> tiles;
   std::vector<size_t> tile_a;   // first active row of each tile
   std::vector<int64_t> tile_ne;  // entries of each tile

@@ -136,6 +136,8 @@ class Server:
         t.append(time.perf_counter())
         ctx.set_insolation(1, 0, self.solar)
         ctx.compute_F(albedo=0.1, fetch=False)
+        # row tiles of ~200k entries: the batch, not one job, fills the GPU
+        ctx.set_radiosity_blocks(ig.radiosity_blocks_for(ctx.F_info()["nnz"]))
         t.append(time.perf_counter())
         period = r.period_h * 3600.0
         dt = period / r.steps_per_rot

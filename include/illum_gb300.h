@@ -174,6 +174,14 @@ int ilg_direct_radiosity(ilg_ctx* ctx, const double* sun, const double* disk_xy,
 int ilg_radiosity_solve(ilg_ctx* ctx, const double* E, double tol, int max_sweeps, double* x,
                         double* res, int* sweeps);
 
+/* Cut the context's radiosity row tiles for `blocks` blocks (0: every block
+ * the device holds at once, the default), rebuilding them if form factors
+ * exist. Fewer, larger tiles suit a mesh that is solved beside others (a
+ * batch or the serving loop): each tile costs a fixed set-up besides its
+ * entries. A context's results depend on its tiling in the last bits only,
+ * and are the same alone and in a batch for a given setting. No reference
+ * counterpart. */
+int ilg_set_radiosity_blocks(ilg_ctx* ctx, int blocks);
 /* The reference's own solve: a forward solve of L x = E with
  * L = I - tril(F), then gs_steps Gauss-Seidel sweeps x = L^{-1}(E - U x),
  * U = -triu(F), in natural row order (src/cpp/arma_util.cpp:4-17,

@@ -44,6 +44,36 @@ def test_batch_members_equal_alone(ilg, precision):
             assert np.array_equal(o[k], outs[k]), k
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+def test_batch_members_equal_alone_coarse_tiles(ilg, precision):
+    """Members whose row tiles are cut for few blocks (the batch workloads'
+    setting): the same bitwise alone and in the batch, and the solve agrees
+    with the default tiling to the tolerance."""
+    specs = [(3, 31, 20, 4.0, 16), (3, 32, 40, 6.0, 12)]
+    alone = []
+    for sp in specs:
+        ctx, tm, opts, n = _member(ilg, *sp, precision)
+        ctx.set_radiosity_blocks(2)
+        h = ctx.run_steps(opts, 0, n, record_tsurf=True)
+        alone.append((tm.T, ctx.outputs()))
+    mem = [_member(ilg, *sp, precision) for sp in specs]
+    for m in mem:
+        m[0].set_radiosity_blocks(2)
+        assert m[0].F_info()["row_tiles"] <= 2 * 2 + 2
+    b = ilg.Batch([m[0] for m in mem], [m[2] for m in mem])
+    b.run(max(sp[4] for sp in specs))
+    b.sync()
+    for (ctx, tm, opts, n), (T, outs) in zip(mem, alone):
+        assert np.array_equal(tm.T, T)
+        assert np.array_equal(ctx.outputs()["rad"], outs["rad"])
+    ctx, _, _, _ = _member(ilg, *specs[0], 0)
+    E = np.random.default_rng(3).uniform(0.0, 900.0, ctx.num_faces)
+    x0 = ctx.radiosity_solve(E, tol=1e-10)[0]
+    ctx.set_radiosity_blocks(1)
+    x1 = ctx.radiosity_solve(E, tol=1e-10)[0]
+    assert np.abs(x1 - x0).max() <= 1e-9 * max(1.0, np.abs(x0).max())
+
+
 def test_batch_member_switched_off(ilg):
     specs = [(2, 21, 20, 4.0, 20), (2, 22, 20, 4.0, 20)]
     mem = [_member(ilg, *sp, 0) for sp in specs]
