@@ -67,6 +67,11 @@ MIXED_TOL = 1e-3
 # FP64-accumulated residual, one bf16 sweep, the update); the next step's
 # first residual includes what the round left.
 MIXED_SWEEPS = 1
+# Refinement spacing of the mixed path's per-step solve (RunOpts.refine_every):
+# 0 = a refinement round every step (residual pass + bf16 sweep); K >= 1 =
+# one pass over the matrix per step, with the f32 form factors every K-th
+# step and the bf16 copy applied to the change since then in between.
+MIXED_REFINE = 0
 
 CFG = dict(level=6, seed=1, n_craters=200, dmin_m=30.0, dmax_m=300.0, nphi=64, theta_eps=1e-3, offset=1e-5,
            albedo=0.1, nz=60, ti=300.0, rhoc=1500.0 * 700.0, emiss=0.95, T0=200.0, solar=1361.0, dist_au=1.5,
@@ -202,7 +207,7 @@ def new_thermal(ig, ctx, z, precision):
 def c1_opts(ig, dt, precision, use_graph=1):
     if precision == ig.PREC_MIXED:
         return ig.RunOpts(dt=dt, tol=MIXED_TOL, max_sweeps=MIXED_SWEEPS, use_radiosity=1, use_graph=use_graph,
-                          precision=precision, coupling=ig.COUPLE_DIRECT)
+                          precision=precision, coupling=ig.COUPLE_DIRECT, refine_every=MIXED_REFINE)
     return ig.RunOpts(dt=dt, tol=CFG["tol"], max_sweeps=200, use_radiosity=1, use_graph=use_graph,
                       precision=precision, coupling=ig.COUPLE_DIRECT)
 
@@ -353,7 +358,8 @@ def c2_thermal(ig, m, precision):
                          bc_mode=ig.BC_NEWTON, precision=precision)
     mixed = precision == ig.PREC_MIXED
     opts = ig.RunOpts(dt=m["dt"], tol=MIXED_TOL if mixed else BATCH["tol"], max_sweeps=MIXED_SWEEPS if mixed else 200,
-                      use_radiosity=1, use_graph=1, precision=precision, coupling=ig.COUPLE_DIRECT)
+                      use_radiosity=1, use_graph=1, precision=precision, coupling=ig.COUPLE_DIRECT,
+                      refine_every=MIXED_REFINE if mixed else 0)
     return tm, opts
 
 
@@ -651,7 +657,8 @@ def nested_serve(ig, nreq, scale, rate):
     out = {}
     for prec in (ig.PREC_MIXED, ig.PREC_FP64):
         srv = serve.Server(budget_bytes=int(48e9), precision=prec,
-                           tol=MIXED_TOL if prec == ig.PREC_MIXED else 1e-10)
+                           tol=MIXED_TOL if prec == ig.PREC_MIXED else 1e-10,
+                           refine_every=MIXED_REFINE if prec == ig.PREC_MIXED else 0)
         clk = ClockSampler(0).start()
         t0 = time.perf_counter()
         done = srv.run(reqs)
@@ -728,6 +735,7 @@ def mixed_vs_fp64_c1(ig, W, nchk, autotune):
     err = float(np.abs(T64 - tm.T).max())
     return {"value": N * nchk / (ms.sum() / 1000.0), "unit": UNIT, "steps": nchk, "max_err_K": err,
             "ms_per_step": float(ms.mean()), "radiosity_tol": MIXED_TOL, "radiosity_max_sweeps": MIXED_SWEEPS,
+            "radiosity_refine_every": MIXED_REFINE,
             "autotune": mtune, "clocks": cl}
 
 
@@ -770,7 +778,11 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=500)
     ap.add_argument("--serve-scale", type=float, default=0.02, help="step-count scale of the serving sample")
     ap.add_argument("--serve-rate", type=float, default=20.0, help="Poisson arrival rate of the serving stream (1/s)")
+    ap.add_argument("--refine-every", type=int, default=0,
+                    help="mixed path: RunOpts.refine_every (0: a refinement round per step; K: one pass per step)")
     args = ap.parse_args()
+    global MIXED_REFINE
+    MIXED_REFINE = args.refine_every
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

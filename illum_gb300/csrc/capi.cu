@@ -153,7 +153,7 @@ int flush_launch(float4* buf, size_t n, unsigned salt, cudaStream_t s) {
 // reference's fixed-sweep Gauss-Seidel when the context is in that mode.
 static int radiosity_phase(const StepView& v, const StepPlan& p, cudaStream_t s) {
   if (p.gs_ctx) return gs_step_launch(*p.gs_ctx, v, p.gs_steps, s);
-  return radiosity_launch(v, v.rad, 1, p.precision, p.rad_grid, p.rad_inner, s);
+  return radiosity_launch(v, v.rad, 1, p.precision, p.rad_grid, p.rad_inner, p.rad_lagged, s);
 }
 
 // One step of a view: direct -> radiosity -> conduction -> advance. With
@@ -282,6 +282,8 @@ MeshDesc solo_desc(const Context& c, const ilg_run_opts* o, int first_sun) {
   M.rec_frame0 = c.rec_frame0;
   M.tol2 = o ? o->tol * o->tol : 0.0;
   M.max_sweeps = o ? o->max_sweeps : 1;
+  M.refine_every = o ? o->refine_every : 0;
+  M.ref_age = -1;
   M.active = 1;
   return M;
 }
@@ -322,6 +324,11 @@ int check_run(Context& c, const ilg_run_opts* o, bool host_driven) {
   if (o->coupling != ILG_COUPLE_REFERENCE && o->coupling != ILG_COUPLE_DIRECT) { set_error("bad coupling"); return ILG_ERR_ARG; }
   if (o->use_radiosity && !c.have_F) { set_error("use_radiosity set but no form factors"); return ILG_ERR_ARG; }
   if (o->max_sweeps < 1) { set_error("max_sweeps must be >= 1"); return ILG_ERR_ARG; }
+  if (o->refine_every < 0) { set_error("refine_every must be >= 0"); return ILG_ERR_ARG; }
+  if (o->refine_every > 0 && o->precision != ILG_PREC_MIXED) {
+    set_error("refine_every applies to the mixed precision only");
+    return ILG_ERR_ARG;
+  }
   if (c.rad_mode == ILG_RAD_GS && o->use_radiosity && c.have_F) {
     if (o->precision != ILG_PREC_FP64) {
       set_error("the fixed-sweep Gauss-Seidel mode runs in FP64 precision only");
@@ -341,6 +348,7 @@ static StepPlan solo_plan(Context& c, const ilg_run_opts& o) {
   p.rad_on = o.use_radiosity && c.have_F && c.ntiles > 0;
   p.rad_grid = p.rad_on ? radiosity_grid(c.ntiles, o.precision) : 1;
   p.rad_inner = radiosity_inner(o.max_sweeps);
+  p.rad_lagged = o.precision == ILG_PREC_MIXED && o.refine_every > 0;
   p.nz_max = c.nz;
   p.rec_on = c.rec_cap > 0;
   if (p.rad_on && c.rad_mode == ILG_RAD_GS) {
@@ -390,10 +398,10 @@ static int capture_step(Context& c, const ilg_run_opts& o, int slot, cudaGraphEx
 // Graph of one step (with_copies: the two host-driven slot graphs, out[0]
 // and out[1]; otherwise out[0] only).
 static int get_graph(Context& c, const ilg_run_opts& o, bool with_copies, cudaGraphExec_t* out) {
-  int key[5] = {(o.precision * 4 + o.coupling * 2 + (o.use_radiosity ? 1 : 0)) * 4 + radiosity_inner(o.max_sweeps),
+  int key[6] = {(o.precision * 4 + o.coupling * 2 + (o.use_radiosity ? 1 : 0)) * 4 + radiosity_inner(o.max_sweeps),
                 (with_copies ? 1 : 0) + 2 * c.rec_cap,
-                c.nz, c.ntiles, c.rad_mode == ILG_RAD_GS ? 1 + c.gs_steps : 0};
-  if (c.graph && std::equal(key, key + 5, c.graph_key)) {
+                c.nz, c.ntiles, c.rad_mode == ILG_RAD_GS ? 1 + c.gs_steps : 0, o.refine_every > 0 ? 1 : 0};
+  if (c.graph && std::equal(key, key + 6, c.graph_key)) {
     out[0] = c.graph;
     if (with_copies) out[1] = c.graph_b;
     return ILG_OK;
@@ -405,7 +413,7 @@ static int get_graph(Context& c, const ilg_run_opts& o, bool with_copies, cudaGr
     if (rc != ILG_OK) { invalidate_graph(c); return rc; }
     out[1] = c.graph_b;
   }
-  std::copy(key, key + 5, c.graph_key);
+  std::copy(key, key + 6, c.graph_key);
   out[0] = c.graph;
   return ILG_OK;
 }
@@ -796,7 +804,7 @@ int ilg_radiosity_solve(ilg_ctx* ctx, const double* E, double tol, int max_sweep
   ILG_CUDA(cudaMemcpyAsync(c.E.p + (size_t)(M.frame & 1) * c.nt, E, (size_t)c.nt * 8, cudaMemcpyHostToDevice,
                            c.stream));
   StepView v = solo_view(c, ILG_PREC_FP64);
-  ILG_TRY(radiosity_launch(v, c.Q.p, 0, ILG_PREC_FP64, radiosity_grid(c.ntiles, ILG_PREC_FP64), 1, c.stream));
+  ILG_TRY(radiosity_launch(v, c.Q.p, 0, ILG_PREC_FP64, radiosity_grid(c.ntiles, ILG_PREC_FP64), 1, false, c.stream));
   MeshDesc out;
   ILG_CUDA(cudaMemcpyAsync(x, c.Q.p, (size_t)c.nt * 8, cudaMemcpyDeviceToHost, c.stream));
   ILG_CUDA(cudaMemcpyAsync(&out, c.md.p, sizeof(out), cudaMemcpyDeviceToHost, c.stream));

@@ -91,6 +91,9 @@ struct MeshDesc {
   int tile0, ntiles;           // radiosity row tiles (0: no radiosity)
   double tol2;                 // squared residual tolerance
   int max_sweeps;
+  int refine_every;            // mixed solve: 0 = refinement rounds to tol each step; K >= 1 = one
+                               // pass per step, with fl(F) every K-th step (k_radiosity_lagged)
+  int ref_age;                 // that solve: steps since its reference pass (-1: none yet)
   int sweeps;                  // out: sweeps of the last solve
   double res2;                 // out: squared residual bound of the last solve
   int active;                  // 0: skipped by the step kernels
@@ -281,7 +284,7 @@ struct Context {
   // CUDA graph of one step
   cudaGraphExec_t graph = nullptr;       // without copies, or with the copies of slot 0
   cudaGraphExec_t graph_b = nullptr;     // with the copies of slot 1
-  int graph_key[5] = {-1, -1, -1, -1, -1};
+  int graph_key[6] = {-1, -1, -1, -1, -1, -1};
   bool graph_broken = false;      // capture failed once: launch eagerly
 
   dbuf<float4> flush;              // L2-eviction buffer of the benchmark loop
@@ -300,6 +303,7 @@ struct StepPlan {
   bool rec_on;                 // thermal records after conduction
   int rad_grid;
   int rad_inner;               // mixed solve: bf16 sweeps per refinement round (1..radiosity_max_inner())
+  bool rad_lagged = false;     // mixed solve: one pass per step, refinement every refine_every steps
   int nz_max;
   const Context* gs_ctx = nullptr;   // fixed-sweep Gauss-Seidel of this context instead of the tolerance solve
   int gs_steps = 0;
@@ -340,7 +344,8 @@ int radiosity_threads();
 // unsigned words of a view's barrier buffer: the grid barrier's counter and
 // the per-mesh residual accumulators of the radiosity kernels
 size_t radiosity_barrier_words(int nmesh);
-int radiosity_launch(const StepView& v, double* x, int warm, int precision, int grid, int inner, cudaStream_t s);
+int radiosity_launch(const StepView& v, double* x, int warm, int precision, int grid, int inner, bool lagged,
+                     cudaStream_t s);
 int radiosity_barrier_probe(unsigned* bar, int* derr, int blocks, long long polls, int unreachable, cudaStream_t s);
 // inner sweeps of a mixed refinement round for a sweep budget (the smallest
 // budget of a view's meshes): the budget, at most radiosity_max_inner()

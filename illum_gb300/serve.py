@@ -100,7 +100,8 @@ def footprint_bytes(level: int, nz: int, nphi: int, precision: int) -> int:
 
 class Server:
     def __init__(self, budget_bytes: int, precision: int = ig.PREC_MIXED, chunk_steps: int = 30, nphi: int = 32,
-                 tol: float = 1e-3, solar: float = 1361.0, setup_workers: int = 4, min_rebuild_s: float = 0.25):
+                 tol: float = 1e-3, solar: float = 1361.0, setup_workers: int = 4, min_rebuild_s: float = 0.25,
+                 refine_every: int = 0):
         self.budget = budget_bytes
         self.workers = max(1, setup_workers)
         self.min_rebuild_s = min_rebuild_s
@@ -108,6 +109,7 @@ class Server:
         self.chunk = chunk_steps
         self.nphi = nphi
         self.tol = tol
+        self.refine_every = refine_every if precision == ig.PREC_MIXED else 0
         self.solar = solar
         self.used = 0
         self.lock = threading.Condition()
@@ -146,10 +148,11 @@ class Server:
                              bc_mode=ig.BC_NEWTON, precision=self.precision)
         t.append(time.perf_counter())
         self.phase_s.append(np.diff(t))
-        # mixed: one refinement round per step (one bf16 sweep)
+        # mixed: one refinement round per step (one bf16 sweep), or with
+        # refine_every = K one pass per step (f32 form factors every K-th)
         opts = ig.RunOpts(dt=dt, tol=self.tol, max_sweeps=1 if self.precision == ig.PREC_MIXED else 200,
                           use_radiosity=1, use_graph=1,
-                          precision=self.precision, coupling=ig.COUPLE_DIRECT)
+                          precision=self.precision, coupling=ig.COUPLE_DIRECT, refine_every=self.refine_every)
         return Job(req=r, ctx=ctx, tm=tm, opts=opts, nfaces=f.shape[0])
 
     def _estimate(self, r: Request) -> int:

@@ -224,6 +224,13 @@ typedef struct ilg_run_opts {
   int use_graph;           /* capture the step in a CUDA graph */
   int precision;           /* ILG_PREC_FP64 / ILG_PREC_MIXED */
   int coupling;            /* ILG_COUPLE_REFERENCE / ILG_COUPLE_DIRECT */
+  int refine_every;        /* mixed precision only. 0: each step's solve runs refinement rounds
+                              (residual with the f32 form factors, bf16 sweeps) until tol or
+                              max_sweeps. K >= 1: one pass over the matrix per step, warm
+                              started; every K-th step of a mesh (and its first of a run) applies
+                              the f32 form factors, s = F x, and keeps (s, x) as the reference;
+                              the steps between apply the bf16 copy to the change since then,
+                              s = s_ref + F~ (x - x_ref) (tol and max_sweeps unused) */
 } ilg_run_opts;
 
 /* What the radiosity solve of a step starts from. ILG_COUPLE_REFERENCE is

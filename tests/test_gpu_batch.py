@@ -23,15 +23,20 @@ def _member(ilg, level, seed, nz, period_h, nsteps, precision, coupling=1, ti=30
     return ctx, tm, opts, nsteps
 
 
-@pytest.mark.parametrize("precision", [0, 1])
-def test_batch_members_equal_alone(ilg, precision):
+@pytest.mark.parametrize("precision,refine_every", [(0, 0), (1, 0), (1, 3)])
+def test_batch_members_equal_alone(ilg, precision, refine_every):
+    """refine_every = 3: one pass per step, the f32 form factors on every
+    third step of each member (its own count, from its first step)."""
     specs = [(3, 11, 20, 4.0, 30), (2, 12, 35, 7.0, 18), (3, 13, 50, 2.5, 24)]
     alone = []
     for sp in specs:
         ctx, tm, opts, n = _member(ilg, *sp, precision)
+        opts.refine_every = refine_every
         h = ctx.run_steps(opts, 0, n, record_tsurf=True)
         alone.append((h[-1], tm.T, ctx.outputs()))
     mem = [_member(ilg, *sp, precision) for sp in specs]
+    for m in mem:
+        m[2].refine_every = refine_every
     b = ilg.Batch([m[0] for m in mem], [m[2] for m in mem])
     b.run(max(sp[4] for sp in specs))
     act, done, _ = b.status()

@@ -359,6 +359,40 @@ def test_pipelined_steps_equal_serial_order(ilg, oracle_mod, mesh_l3, precision,
             assert np.array_equal(a, b)
 
 
+def test_refine_every_graph_equals_eager(ilg, oracle_mod, mesh_l3):
+    """The one-pass mixed solve (refine_every = 3): graph, eager and
+    phase-timed steps give the same results bit for bit, with one sweep
+    per step."""
+    v, f = mesh_l3
+    runs = []
+    for mode in ("serial", "graph", "eager"):
+        ctx, tm, opts, _, _, _, _, _ = _setup_run(ilg, oracle_mod, v, f, 16, 30, 24, precision=1,
+                                                  use_graph=0 if mode == "eager" else 1)
+        opts.tol, opts.max_sweeps, opts.refine_every = 1e-3, 1, 3
+        ctx.set_timing(mode == "serial")
+        h = ctx.run_steps(opts, 0, 24, record_tsurf=True)
+        if mode == "serial":   # phase-timed steps record their sweep counts
+            assert ctx.stats()["radiosity_sweeps"] == 24
+        ctx.set_timing(False)
+        runs.append((h, tm.T.copy(), ctx.outputs()["rad"]))
+    for r in runs[1:]:
+        for a, b in zip(r, runs[0]):
+            assert np.array_equal(a, b)
+
+
+def test_refine_every_is_checked(ilg, oracle_mod, mesh_l3):
+    """refine_every belongs to the mixed precision, and is >= 0."""
+    v, f = mesh_l3
+    ctx, tm, opts, _, _, _, _, _ = _setup_run(ilg, oracle_mod, v, f, 16, 30, 4, precision=0)
+    opts.refine_every = 2
+    with pytest.raises(ilg.IlgError):
+        ctx.run_steps(opts, 0, 2)
+    ctx, tm, opts, _, _, _, _, _ = _setup_run(ilg, oracle_mod, v, f, 16, 30, 4, precision=1)
+    opts.refine_every = -1
+    with pytest.raises(ilg.IlgError):
+        ctx.run_steps(opts, 0, 2)
+
+
 def test_split_runs_equal_one_run(ilg, oracle_mod, mesh_l3):
     v, f = mesh_l3
     a = _setup_run(ilg, oracle_mod, v, f, 16, 30, 30)
@@ -369,18 +403,21 @@ def test_split_runs_equal_one_run(ilg, oracle_mod, mesh_l3):
     assert np.array_equal(a[1].T, b[1].T)
 
 
-@pytest.mark.parametrize("tol,max_sweeps", [(1e-10, 200), (1e-3, 2), (1e-3, 1)])
-def test_mixed_precision_within_tolerance(ilg, oracle_mod, mesh_l4, tol, max_sweeps):
+@pytest.mark.parametrize("tol,max_sweeps,refine_every", [(1e-10, 200, 0), (1e-3, 2, 0), (1e-3, 1, 0),
+                                                         (1e-3, 1, 1), (1e-3, 1, 4), (1e-3, 1, 16)])
+def test_mixed_precision_within_tolerance(ilg, oracle_mod, mesh_l4, tol, max_sweeps, refine_every):
     """Mixed path (bf16 form factors, fp32 conduction) against the FP64 path:
-    solved to tolerance, and with one refinement round per step (a budget
-    of two sweeps, or of one, stops the solve after its first update; the
-    round runs that many bf16 sweeps)."""
+    solved to tolerance, with one refinement round per step (a budget of
+    two sweeps, or of one, stops the solve after its first update; the
+    round runs that many bf16 sweeps), and with one pass per step whose
+    f32 reference pass comes every refine_every steps."""
     v, f = mesh_l4
     nsteps = 360
     ref = _setup_run(ilg, oracle_mod, v, f, 32, 40, nsteps, precision=0)
     mix = _setup_run(ilg, oracle_mod, v, f, 32, 40, nsteps, precision=1)
     mix[2].tol = tol
     mix[2].max_sweeps = max_sweeps
+    mix[2].refine_every = refine_every
     ha = ref[0].run_steps(ref[2], 0, nsteps, record_tsurf=True)
     hb = mix[0].run_steps(mix[2], 0, nsteps, record_tsurf=True)
     err_s = np.abs(ha - hb).max()
