@@ -69,9 +69,10 @@ MIXED_TOL = 1e-3
 MIXED_SWEEPS = 1
 # Refinement spacing of the mixed path's per-step solve (RunOpts.refine_every):
 # 0 = a refinement round every step (residual pass + bf16 sweep); K >= 1 =
-# one pass over the matrix per step, with the f32 form factors every K-th
-# step and the bf16 copy applied to the change since then in between.
-MIXED_REFINE = 0
+# one pass over the matrix per step from a predicted warm start, with the
+# f32 form factors every K-th step and the bf16 copy applied to the change
+# since then in between.
+MIXED_REFINE = 4
 
 CFG = dict(level=6, seed=1, n_craters=200, dmin_m=30.0, dmax_m=300.0, nphi=64, theta_eps=1e-3, offset=1e-5,
            albedo=0.1, nz=60, ti=300.0, rhoc=1500.0 * 700.0, emiss=0.95, T0=200.0, solar=1361.0, dist_au=1.5,
@@ -202,6 +203,19 @@ def new_thermal(ig, ctx, z, precision):
     c = CFG
     return ig.ThermalModel(ctx, z, c["ti"], c["rhoc"], c["T0"], emissivity=c["emiss"], bc_mode=ig.BC_NEWTON,
                            precision=precision)
+
+
+def mixed_dtype():
+    if MIXED_REFINE > 0:
+        return "bf16 F + f32 reference passes + fp32 conduction"
+    return "bf16 F + fp32 conduction (fp64 residual)"
+
+
+def mixed_solve_label():
+    if MIXED_REFINE > 0:
+        return (f"one matrix pass per step from a predicted warm start, f32 form factors every {MIXED_REFINE}th "
+                "step, bf16 between")
+    return "one refinement round per step (f32 residual pass, one bf16 sweep)"
 
 
 def c1_opts(ig, dt, precision, use_graph=1):
@@ -421,11 +435,12 @@ def nested_batch(ig, meshgen, K, W):
         m["ctx"].close()
     mx, d = out[ig.PREC_MIXED], out[ig.PREC_FP64]
     return {"value": mx["value"], "unit": UNIT, "steps": K, "warmup": W, "ms_per_step": mx["ms"],
-            "dtype": "bf16 F + fp32 conduction (fp64 residual)",
+            "dtype": mixed_dtype(),
             "config": {"workload": "64 meshes seeds 2-65, icosphere L3-L6, Poisson craters 0.0025/facet, nz 30-80, "
                                    "ti log-U[50,2000], P U[2,12] h, 360/720 steps per rotation, nphi 32, albedo 0.1, "
                                    "one batch, one launch per phase, CUDA graph per step, radiosity row tiles of ~200k "
-                                   "entries per member; FP64 arm radiosity tol 1e-10",
+                                   "entries per member; FP64 arm radiosity tol 1e-10; mixed arm "
+                                   + mixed_solve_label(),
                        "facets": nf, "l2": "256 MB flush before every timed step"},
             "fp64_value": d["value"], "fp64_ms_per_step": d["ms"], "mixed_vs_fp64": mx["value"] / d["value"],
             "phases_ms_per_step": mx["phases"], "fp64_phases_ms_per_step": d["phases"],
@@ -673,11 +688,12 @@ def nested_serve(ig, nreq, scale, rate):
     m, d = out[ig.PREC_MIXED], out[ig.PREC_FP64]
     err = max(float(np.abs(m["tsurf"][k] - d["tsurf"][k]).max()) for k in m["tsurf"])
     return {"value": m["value"], "unit": UNIT, "steps": m["steps"], "p50_ms": m["p50"], "p99_ms": m["p99"],
-            "dtype": "bf16 F + fp32 conduction (fp64 residual)",
+            "dtype": mixed_dtype(),
             "config": {"workload": f"serving: the first {nreq} requests of the seeded stream (Poisson {rate:g}/s, "
                                    f"icosphere L3-L7, 20 craters 80-300 m, 1-20 rotations x 360-1440 steps per "
                                    f"rotation scaled by {scale:g}, materials as the batch workload), 48 GB admission "
-                                   f"budget", "requests": nreq, "step_scale": scale},
+                                   f"budget; FP64 arm radiosity tol 1e-10; mixed arm " + mixed_solve_label(),
+                       "requests": nreq, "step_scale": scale},
             "requests_done": m["n"], "wall_s": m["wall"], "batch_rebuilds": m["rebuilds"],
             "fp64_value": d["value"], "fp64_p50_ms": d["p50"], "fp64_p99_ms": d["p99"], "fp64_wall_s": d["wall"],
             "mixed_vs_fp64": m["value"] / d["value"], "max_err_K_vs_fp64": err,
@@ -755,6 +771,7 @@ def standalone(args, ig, meshgen):
 
 
 def main():
+    global MIXED_REFINE
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=1440)
@@ -778,10 +795,9 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=500)
     ap.add_argument("--serve-scale", type=float, default=0.02, help="step-count scale of the serving sample")
     ap.add_argument("--serve-rate", type=float, default=20.0, help="Poisson arrival rate of the serving stream (1/s)")
-    ap.add_argument("--refine-every", type=int, default=0,
+    ap.add_argument("--refine-every", type=int, default=MIXED_REFINE,
                     help="mixed path: RunOpts.refine_every (0: a refinement round per step; K: one pass per step)")
     args = ap.parse_args()
-    global MIXED_REFINE
     MIXED_REFINE = args.refine_every
 
     rank = int(os.environ.get("RANK", "0"))

@@ -161,7 +161,7 @@ static int build(Batch& b) {
   ILG_TRY(b.suns.alloc(nsun));
   for (dbuf<double>* d : {&b.Tsurf, &b.Fsurf, &b.Qprev, &b.rad, &b.rad_avg, &b.therm_avg, &b.therm_max})
     ILG_TRY(d->alloc(nt));
-  ILG_TRY(b.E.alloc(2 * (size_t)nt));   // the direct flux of two consecutive frames
+  ILG_TRY(b.E.alloc(E_SLOTS * (size_t)nt));   // the direct flux of consecutive frames
   ILG_TRY(b.sprev.alloc(2 * nt));
   ILG_TRY(b.xtmp.alloc(6 * nt));
   ILG_TRY(b.rperm.alloc(nt));
@@ -235,6 +235,11 @@ static int build(Batch& b) {
     ILG_TRY(cat(b.therm_max, f0, c.therm_max.p, N, s));
     ILG_TRY(cat(b.sprev, f0, c.sprev.p, N, s));
     ILG_TRY(cat(b.sprev, (size_t)nt + f0, c.sprev.p + N, N, s));
+    if (M.refine_every > 0 && M.ref_age >= 0) {
+      // the one-pass solve's reference (s_ref, x_ref by position: xtmp's S1, H1)
+      ILG_TRY(cat(b.xtmp, 2 * (size_t)nt + f0, c.xtmp.p + 2 * N, N, s));
+      ILG_TRY(cat(b.xtmp, 4 * (size_t)nt + f0, c.xtmp.p + 4 * N, N, s));
+    }
     if (mixed) {
       ILG_TRY(cat(b.T32, (size_t)M.T0, c.T32.p, N * c.nz, s));
       ILG_TRY(cat(b.coef32, (size_t)M.coef0, c.coef32.p, (size_t)c.nz * 5, s));
@@ -446,6 +451,7 @@ int ilg_batch_bench_phases(ilg_batch* batch, int nsteps, double flush_mb, double
   size_t nflush = flush_mb > 0 ? (size_t)(flush_mb * 1048576.0 / 16.0) : 0;
   if (nflush) ILG_TRY(b.flush.reserve(nflush));
   phase_ms[0] = phase_ms[1] = phase_ms[2] = 0.0;
+  if (nsteps > 0) ILG_TRY(enqueue_serial_prologue(b.v, b.plan, b.stream));
   for (int s = 0; s < nsteps; ++s) {
     if (nflush) ILG_TRY(flush_launch(b.flush.p, nflush, (unsigned)s, b.stream));
     ILG_TRY(enqueue_step(b.v, b.plan, b.stream, b.ev));
@@ -521,6 +527,15 @@ int ilg_batch_sync(ilg_batch* batch) {
     ILG_CUDA(cudaMemcpyAsync(c.therm_max.p, b.therm_max.p + f0, bytes, cudaMemcpyDeviceToDevice, s));
     ILG_CUDA(cudaMemcpyAsync(c.sprev.p, b.sprev.p + f0, bytes, cudaMemcpyDeviceToDevice, s));
     ILG_CUDA(cudaMemcpyAsync(c.sprev.p + N, b.sprev.p + (size_t)b.nt + f0, bytes, cudaMemcpyDeviceToDevice, s));
+    if (b.plan.rad_lagged && M.ntiles > 0) {
+      c.ref_age = m[i].ref_age;
+      if (c.ref_age >= 0) {
+        ILG_CUDA(cudaMemcpyAsync(c.xtmp.p + 2 * N, b.xtmp.p + 2 * (size_t)b.nt + f0, bytes, cudaMemcpyDeviceToDevice, s));
+        ILG_CUDA(cudaMemcpyAsync(c.xtmp.p + 4 * N, b.xtmp.p + 4 * (size_t)b.nt + f0, bytes, cudaMemcpyDeviceToDevice, s));
+      }
+    } else if (M.ntiles > 0) {
+      c.ref_age = -1;
+    }
     if (mixed)
       ILG_CUDA(cudaMemcpyAsync(c.T32.p, b.T32.p + M.T0, N * c.nz * 4, cudaMemcpyDeviceToDevice, s));
     else

@@ -157,10 +157,12 @@ static int radiosity_phase(const StepView& v, const StepPlan& p, cudaStream_t s)
 }
 
 // One step of a view: direct -> radiosity -> conduction -> advance. With
-// ev (4 events), the phase boundaries are recorded.
+// ev (4 events), the phase boundaries are recorded. The one-pass mixed
+// solve also reads the next frame's direct flux: its steps compute that one
+// (the current frame's came from the previous step or the serial prologue).
 int enqueue_step(const StepView& v, const StepPlan& p, cudaStream_t s, cudaEvent_t* ev) {
   if (ev) ILG_CUDA(cudaEventRecord(ev[0], s));
-  ILG_TRY(direct_launch(v, 0, p.precision == ILG_PREC_MIXED ? 1 : 0, 0, s));
+  ILG_TRY(direct_launch(v, 0, p.precision == ILG_PREC_MIXED ? 1 : 0, p.rad_lagged ? 1 : 0, s));
   if (ev) ILG_CUDA(cudaEventRecord(ev[1], s));
   if (p.rad_on) ILG_TRY(radiosity_phase(v, p, s));
   if (ev) ILG_CUDA(cudaEventRecord(ev[2], s));
@@ -183,21 +185,29 @@ StepPipe::~StepPipe() {
   if (s2) cudaStreamDestroy(s2);
 }
 
-// The current frame's direct flux, before the first pipelined step of a run.
+// The current frame's direct flux (and the next frame's for the one-pass
+// mixed solve), before the first pipelined step of a run.
 int enqueue_prologue(const StepView& v, const StepPlan& p, cudaStream_t s) {
-  return direct_launch(v, 0, p.precision == ILG_PREC_MIXED ? 1 : 0, 0, s);
+  ILG_TRY(direct_launch(v, 0, p.precision == ILG_PREC_MIXED ? 1 : 0, 0, s));
+  if (p.rad_lagged) ILG_TRY(direct_launch(v, 0, 1, 1, s));
+  return ILG_OK;
 }
 
-// The step's radiosity reads its frame's E slot; the next frame's direct
-// insolation then writes the other slot on s2 while the conduction runs on
-// s (the two share no array: the conduction reads the radiosity solution,
-// or the current slot for meshes without form factors). Both finish before
-// the advance. Results equal the serial order's bit for bit.
+int enqueue_serial_prologue(const StepView& v, const StepPlan& p, cudaStream_t s) {
+  return p.rad_lagged ? direct_launch(v, 0, 1, 0, s) : ILG_OK;
+}
+
+// The step's radiosity reads its frame's E slot (the one-pass mixed solve
+// also the next frame's); the direct insolation of the frame after those
+// then writes its own slot on s2 while the conduction runs on s (the two
+// share no array: the conduction reads the radiosity solution, or the
+// current slot for meshes without form factors). Both finish before the
+// advance. Results equal the serial order's bit for bit.
 int enqueue_step_pipe(const StepView& v, const StepPlan& p, cudaStream_t s, const StepPipe& pipe) {
   if (p.rad_on) ILG_TRY(radiosity_phase(v, p, s));
   ILG_CUDA(cudaEventRecord(pipe.fork, s));
   ILG_CUDA(cudaStreamWaitEvent(pipe.s2, pipe.fork, 0));
-  ILG_TRY(direct_launch(v, 0, p.precision == ILG_PREC_MIXED ? 1 : 0, 1, pipe.s2));
+  ILG_TRY(direct_launch(v, 0, p.precision == ILG_PREC_MIXED ? 1 : 0, p.rad_lagged ? 2 : 1, pipe.s2));
   ILG_CUDA(cudaEventRecord(pipe.join, pipe.s2));
   ILG_TRY(conduction_launch(v, v.rad, p.precision, 1, p.nz_max, s));
   if (p.rec_on) ILG_TRY(record_launch(v, p.precision, v.cblocks ? v.ncblocks : div_up(v.nt, conduction_step_threads()), s));
@@ -283,9 +293,26 @@ MeshDesc solo_desc(const Context& c, const ilg_run_opts* o, int first_sun) {
   M.tol2 = o ? o->tol * o->tol : 0.0;
   M.max_sweeps = o ? o->max_sweeps : 1;
   M.refine_every = o ? o->refine_every : 0;
-  M.ref_age = -1;
+  M.ref_age = c.ref_age;
   M.active = 1;
   return M;
+}
+
+// After a run's steps: the one-pass mixed solve's reference carries over to
+// the context's next run (its age from the mesh table, s_ref and x_ref stay
+// in xtmp); any other radiosity solve reuses those buffers, so it ends the
+// reference.
+static int keep_reference(Context& c, const StepPlan& p) {
+  if (!p.rad_on) return ILG_OK;
+  if (!p.rad_lagged) {
+    c.ref_age = -1;
+    return ILG_OK;
+  }
+  MeshDesc M;
+  ILG_CUDA(cudaMemcpyAsync(&M, c.md.p, sizeof(MeshDesc), cudaMemcpyDeviceToHost, c.stream));
+  ILG_CUDA(cudaStreamSynchronize(c.stream));
+  c.ref_age = M.ref_age;
+  return ILG_OK;
 }
 
 static int upload_desc(Context& c, const MeshDesc& M) {
@@ -298,7 +325,7 @@ static int upload_desc(Context& c, const MeshDesc& M) {
 // Per-context scratch of the step kernels, sized before any capture.
 static int ensure_step_buffers(Context& c, int precision) {
   ILG_TRY(c.pipe.init());
-  ILG_TRY(c.E.reserve(2 * (size_t)c.nt));   // the direct flux of two consecutive frames
+  ILG_TRY(c.E.reserve(E_SLOTS * (size_t)c.nt));   // the direct flux of consecutive frames
   ILG_TRY(c.Q.reserve(c.nt));
   ILG_TRY(c.xtmp.reserve((size_t)6 * c.nt));   // radiosity E, two iterates, double-float copies of both and of E
   if (c.sprev.n < 2 * (size_t)c.nt) {
@@ -327,6 +354,10 @@ int check_run(Context& c, const ilg_run_opts* o, bool host_driven) {
   if (o->refine_every < 0) { set_error("refine_every must be >= 0"); return ILG_ERR_ARG; }
   if (o->refine_every > 0 && o->precision != ILG_PREC_MIXED) {
     set_error("refine_every applies to the mixed precision only");
+    return ILG_ERR_ARG;
+  }
+  if (o->refine_every > 0 && host_driven) {
+    set_error("refine_every needs the sun positions on the device (ilg_run_steps): its solve reads the next frame's flux");
     return ILG_ERR_ARG;
   }
   if (c.rad_mode == ILG_RAD_GS && o->use_radiosity && c.have_F) {
@@ -787,6 +818,7 @@ int ilg_radiosity_solve(ilg_ctx* ctx, const double* E, double tol, int max_sweep
   Context& c = ctx->c;
   AllocOn on_(c.stream);
   if (!c.have_F) { set_error("no form factors"); return ILG_ERR_ARG; }
+  c.ref_age = -1;   // the solve below reuses the buffers of a one-pass reference
   if (c.ntiles == 0) {
     std::memcpy(x, E, (size_t)c.nt * 8);
     if (res) *res = 0.0;
@@ -801,7 +833,7 @@ int ilg_radiosity_solve(ilg_ctx* ctx, const double* E, double tol, int max_sweep
   o.coupling = ILG_COUPLE_DIRECT;   // E as given
   MeshDesc M = solo_desc(c, &o, 0);
   ILG_TRY(upload_desc(c, M));
-  ILG_CUDA(cudaMemcpyAsync(c.E.p + (size_t)(M.frame & 1) * c.nt, E, (size_t)c.nt * 8, cudaMemcpyHostToDevice,
+  ILG_CUDA(cudaMemcpyAsync(c.E.p + e_slot(M.frame) * c.nt, E, (size_t)c.nt * 8, cudaMemcpyHostToDevice,
                            c.stream));
   StepView v = solo_view(c, ILG_PREC_FP64);
   ILG_TRY(radiosity_launch(v, c.Q.p, 0, ILG_PREC_FP64, radiosity_grid(c.ntiles, ILG_PREC_FP64), 1, false, c.stream));
@@ -925,7 +957,7 @@ int ilg_thermal_init(ilg_ctx* ctx, int nz, const double* z, const double* ti, co
   ILG_TRY(c.rad_avg.alloc(nt));
   ILG_TRY(c.therm_avg.alloc(nt));
   ILG_TRY(c.therm_max.alloc(nt));
-  ILG_TRY(c.E.reserve(2 * (size_t)nt));
+  ILG_TRY(c.E.reserve(E_SLOTS * (size_t)nt));
   ILG_TRY(c.Q.reserve(nt));
   ILG_CUDA(cudaMemcpyAsync(c.Tdf.p, Tl.data(), n * 8, cudaMemcpyHostToDevice, c.stream));
   ILG_CUDA(cudaMemcpyAsync(c.Tsurf.p, ts.data(), (size_t)nt * 8, cudaMemcpyHostToDevice, c.stream));
@@ -1017,6 +1049,7 @@ int ilg_run_steps(ilg_ctx* ctx, const ilg_run_opts* opts, int first_sun, int nst
   // pipelined steps (graph or eager) after a prologue; the phase-timed steps
   // run in the serial order (same results)
   if (!timing && nsteps > 0) ILG_TRY(enqueue_prologue(v, p, c.stream));
+  if (timing && nsteps > 0) ILG_TRY(enqueue_serial_prologue(v, p, c.stream));
   for (int s = 0; s < nsteps; ++s) {
     if (g) ILG_CUDA(cudaGraphLaunch(g, c.stream));
     else if (timing) ILG_TRY(enqueue_step(v, p, c.stream, c.ev));
@@ -1029,6 +1062,7 @@ int ilg_run_steps(ilg_ctx* ctx, const ilg_run_opts* opts, int first_sun, int nst
     }
   }
   ILG_CUDA(cudaStreamSynchronize(c.stream));
+  ILG_TRY(keep_reference(c, solo_plan(c, o)));
   c.frame_no += nsteps;
   return read_device_errors(c);
 }
@@ -1098,6 +1132,7 @@ int ilg_run_steps_host(ilg_ctx* ctx, const ilg_run_opts* opts, int nsteps, const
       if (tsurf_out) std::memcpy(tsurf_out + (size_t)s * c.nt, c.pinned_tsurf, (size_t)c.nt * 8);
     }
   }
+  ILG_TRY(keep_reference(c, solo_plan(c, o)));
   c.frame_no += nsteps;
   return read_device_errors(c);
 }
@@ -1128,6 +1163,7 @@ int ilg_bench_steps(ilg_ctx* ctx, const ilg_run_opts* opts, int first_sun, int n
   // graph steps are pipelined (prologue untimed); eager steps run in the
   // serial order with their phase boundaries recorded
   if (g && nsteps > 0) ILG_TRY(enqueue_prologue(v, p, c.stream));
+  if (!g && nsteps > 0) ILG_TRY(enqueue_serial_prologue(v, p, c.stream));
   for (int s = 0; s < nsteps; ++s) {
     if (nflush) ILG_TRY(flush_launch(c.flush.p, nflush, (unsigned)s, c.stream));
     if (g) {
@@ -1151,6 +1187,7 @@ int ilg_bench_steps(ilg_ctx* ctx, const ilg_run_opts* opts, int first_sun, int n
     ILG_TRY(collect_stats(c, false));
   }
   ILG_CUDA(cudaStreamSynchronize(c.stream));
+  ILG_TRY(keep_reference(c, solo_plan(c, o)));
   c.frame_no += nsteps;
   return read_device_errors(c);
 }
@@ -1210,7 +1247,7 @@ int ilg_autotune(ilg_ctx* ctx, const ilg_run_opts* opts, int first_sun, ilg_tune
   StepView v = solo_view(c, o.precision);
   const size_t nt = (size_t)c.nt, nl = (size_t)c.nz * nt;
   dbuf<double> sE, srad, sTs, sFs, sQp, sra, sta, stm;
-  ILG_TRY(scratch_copy(sE, c.E.p, 2 * nt, s));
+  ILG_TRY(scratch_copy(sE, c.E.p, E_SLOTS * nt, s));
   ILG_TRY(scratch_copy(srad, c.rad.p, nt, s));
   ILG_TRY(scratch_copy(sTs, c.Tsurf.p, nt, s));
   ILG_TRY(scratch_copy(sFs, c.Fsurf.p, nt, s));

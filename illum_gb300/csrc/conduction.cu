@@ -214,7 +214,7 @@ k_conduct(StepView v, const double* __restrict__ Qnp1, int upd) {
   // follows the reference, and recorded as the mesh's radiosity. Fsurf is
   // read before this thread overwrites it below.
   const bool direct_only = upd && M.ntiles == 0;
-  const double Qsrc = direct_only ? v.E[(size_t)(M.frame & 1) * v.nt + g] : Qnp1[g];
+  const double Qsrc = direct_only ? v.E[e_slot(M.frame) * v.nt + g] : Qnp1[g];
   const double Fs_prev = (direct_only && M.coupling == ILG_COUPLE_REFERENCE) ? v.Fsurf[g] : 0.0;
   const double Ts_prev = v.Tsurf[g];
   // Stage the column in the rho slots (slot i <- T_i): the upward pass then

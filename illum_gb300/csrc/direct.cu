@@ -48,7 +48,7 @@ __device__ __forceinline__ bool direct_on(const MeshDesc& M, int ahead) {
 __device__ __forceinline__ void store_direct(const StepView& v, const MeshDesc& M, int g, double dv, int dropin,
                                              int ahead) {
   if (dropin) { v.E[g] = dv; return; }
-  v.E[(size_t)((M.frame + ahead) & 1) * v.nt + g] = dv;
+  v.E[e_slot(M.frame + ahead) * v.nt + g] = dv;
 }
 
 // Range of the horizon threshold of src/cpp/illum.cpp:431-434 over the

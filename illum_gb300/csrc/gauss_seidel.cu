@@ -51,7 +51,7 @@ __global__ void k_gs_rhs(StepView v, double* Eg) {
   int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= v.nt) return;
   const MeshDesc& M = v.md[0];
-  const double d = v.E[(size_t)(M.frame & 1) * v.nt + g];
+  const double d = v.E[e_slot(M.frame) * v.nt + g];
   Eg[g] = M.coupling == ILG_COUPLE_REFERENCE ? (-v.Fsurf[g] + d) : d;
 }
 

@@ -74,6 +74,12 @@ struct RowTile {
 // radiosity tiles live in the scene's arrays, and its run state. The step
 // kernels read it from device memory, so a captured step graph stays valid
 // while meshes advance, finish or are switched off.
+// Slots of the direct-flux buffer: frames f, f + 1 and f + 2 (the one-pass
+// mixed solve of frame f reads the next frame's flux, computed two frames
+// ahead beside the conduction).
+constexpr int E_SLOTS = 3;
+__host__ __device__ __forceinline__ size_t e_slot(int frame) { return (size_t)(frame % E_SLOTS); }
+
 struct MeshDesc {
   int facet0, nfacet;          // facet range in the scene
   int nphi, interp;
@@ -125,9 +131,10 @@ struct StepView {
   int ndisk;
   const SunAux* suns;
   double *Tsurf, *Fsurf, *Qprev, *rad, *rad_avg, *therm_avg, *therm_max;
-  double* E;                   // 2 x nt: the direct flux of frame f in slot f & 1 (before the
-                               // coupling, which its readers apply); a drop-in direct call writes slot 0
-  double* sprev;               // 2 x nt by radiosity position: scattered radiosity x - E of the last solve, and its change
+  double* E;                   // E_SLOTS x nt: the direct flux of frame f in slot e_slot(f) (before
+                               // the coupling, which its readers apply); a drop-in direct call writes slot 0
+  double* sprev;               // 2 x nt by radiosity position: scattered radiosity x - E of the last solve, and its
+                               // change (the one-pass mixed solve: its predicted change for the next step)
   float* x32;                  // 3 x nt (mixed radiosity)
   double* T64;                 // [nz][nt] fp64 layers (standalone column entry points)
   float2* Tdf;                 // [nz][nt] double-float layers (the FP64 step)
@@ -254,6 +261,8 @@ struct Context {
   dbuf<double> rad, rad_avg, therm_avg, therm_max, E, xtmp, Q;
   dbuf<double> sprev;             // 2 x N by radiosity position: x - E of the last radiosity solve, and its change
   int frame_no = 0;
+  int ref_age = -1;               // the one-pass mixed solve: steps since its reference step, whose
+                                  // s_ref and x_ref (by position) stay in xtmp's S1 and H1; -1: none
   int rec_cap = 0, rec_frame0 = 0;  // thermal records (ilg_record_thermal)
   dbuf<double> rec, rec_part;
 
@@ -372,6 +381,8 @@ int enqueue_step(const StepView& v, const StepPlan& p, cudaStream_t s, cudaEvent
 // previous pipelined step or from enqueue_prologue at the start of a run.
 int enqueue_step_pipe(const StepView& v, const StepPlan& p, cudaStream_t s, const StepPipe& pipe);
 int enqueue_prologue(const StepView& v, const StepPlan& p, cudaStream_t s);
+// Before the first of a run's serial (phase-timed) steps.
+int enqueue_serial_prologue(const StepView& v, const StepPlan& p, cudaStream_t s);
 int advance_launch(const StepView& v, cudaStream_t s);
 int flush_launch(float4* buf, size_t n, unsigned salt, cudaStream_t s);
 

@@ -216,14 +216,19 @@ __device__ __forceinline__ void bulk_copy(unsigned dst, const void* src, unsigne
 struct ValsDF { const float* hi; const float* lo; };   // double-float (hi, lo)
 struct ValsHi { const float* hi; };                    // fl(F) as a double-float with lo = 0
 struct ValsBF { const __nv_bfloat16* v; };             // bf16, scaled per row
+struct ValsHiF { const float* hi; };                   // fl(F) as a float
 __device__ __forceinline__ unsigned vals_bytes(ValsDF) { return 2 * RAD_F32_BYTES; }
 __device__ __forceinline__ unsigned vals_bytes(ValsHi) { return RAD_F32_BYTES; }
+__device__ __forceinline__ unsigned vals_bytes(ValsHiF) { return RAD_F32_BYTES; }
 __device__ __forceinline__ unsigned vals_bytes(ValsBF) { return RAD_CF_BYTES; }
 __device__ __forceinline__ void copy_vals(ValsDF s, unsigned dst, size_t e, unsigned long long* bar, uint64_t pol) {
   bulk_copy(dst, s.hi + e, RAD_F32_BYTES, bar, pol);
   bulk_copy(dst + RAD_F32_BYTES, s.lo + e, RAD_F32_BYTES, bar, pol);
 }
 __device__ __forceinline__ void copy_vals(ValsHi s, unsigned dst, size_t e, unsigned long long* bar, uint64_t pol) {
+  bulk_copy(dst, s.hi + e, RAD_F32_BYTES, bar, pol);
+}
+__device__ __forceinline__ void copy_vals(ValsHiF s, unsigned dst, size_t e, unsigned long long* bar, uint64_t pol) {
   bulk_copy(dst, s.hi + e, RAD_F32_BYTES, bar, pol);
 }
 __device__ __forceinline__ void copy_vals(ValsBF s, unsigned dst, size_t e, unsigned long long* bar, uint64_t pol) {
@@ -243,6 +248,13 @@ __device__ __forceinline__ void read_vals(ValsHi, const unsigned char* st, int t
   w[1] = make_float2(h.y, 0.f);
   w[2] = make_float2(h.z, 0.f);
   w[3] = make_float2(h.w, 0.f);
+}
+__device__ __forceinline__ void read_vals(ValsHiF, const unsigned char* st, int tid, float (&w)[4]) {
+  const float4 h = *reinterpret_cast<const float4*>(st + 16 * tid);
+  w[0] = h.x;
+  w[1] = h.y;
+  w[2] = h.z;
+  w[3] = h.w;
 }
 __device__ __forceinline__ void read_vals(ValsBF, const unsigned char* st, int tid, float (&w)[4]) {
   const uint2 r = *reinterpret_cast<const uint2*>(st + 8 * tid);
@@ -379,6 +391,27 @@ struct AccF32 {
   __device__ __forceinline__ Part part() const { return s; }
   __device__ __forceinline__ void merge(Part q) { s += q; }
   __device__ __forceinline__ float get() const { return s; }
+};
+
+// Two fp32 sums over the same entries (the one-pass mixed solve: the
+// iterate's change and the next frame's change of the direct flux).
+struct AccF2 {
+  typedef float W;
+  typedef float2 X;
+  typedef float2 Part;
+  typedef float2 Sum;
+  float a, b;
+  __device__ __forceinline__ void zero() { a = 0.f; b = 0.f; }
+  __device__ __forceinline__ void add(float w, float2 x) {
+    a = fmaf(w, x.x, a);
+    b = fmaf(w, x.y, b);
+  }
+  __device__ __forceinline__ Part part() const { return make_float2(a, b); }
+  __device__ __forceinline__ void merge(Part q) {
+    a += q.x;
+    b += q.y;
+  }
+  __device__ __forceinline__ float2 get() const { return make_float2(a, b); }
 };
 
 __device__ __forceinline__ float2 to_halo(float2 x, float2*) { return x; }
@@ -599,7 +632,9 @@ __device__ __forceinline__ void record_residuals(const StepView& v, const MeshSt
 // start predicts the scattered part and takes the step's own E:
 // s0 = S(n) + (S(n) - S(n-1)). E jumps where a facet enters or leaves
 // shadow; S = F x varies smoothly, so the start is off by about F dE there
-// instead of dE. sprev holds S(n) and, after it, its last change.
+// instead of dE. sprev holds S(n) and, after it, its last change; for the
+// one-pass mixed solve (predicted) the predicted change F (E(n+1) - E(n))
+// instead, so that s0 = S(n) + P from the second step on.
 struct RadBufs {
   double* EP;
   float2 *S0, *S1, *H0, *H1, *EH;
@@ -625,23 +660,29 @@ constexpr int RAD_ILP = 4;
 // entries (x = E, s = 0) and their warm-start record, for a kernel that
 // scatters its tile rows itself; that solve reads only EP, S0 and H0 (and
 // x32), the FP64 sweeps also S1, H1 and EH.
+// kind (the one-pass mixed solve, per mesh: 0 bf16 step, 1 reference step, 2
+// first reference step): the warm start is S(n) + P, and the pass's halo
+// vector EH = (x - x_ref, E(n+1) - E(n)) and the reference iterate H1 are
+// written here too; x32 then holds only P (zero for rows without entries).
 __device__ __forceinline__ void init_x(const StepView& v, double* x, int warm, int gt, int nthreads,
-                                       bool free_rows) {
+                                       bool free_rows, const unsigned char* kind = nullptr) {
   const RadBufs B(v);
+  const bool predicted = kind != nullptr;
   for (int p0 = gt; p0 < v.nt; p0 += RAD_ILP * nthreads) {
-    int g[RAD_ILP];
-    const MeshDesc* M[RAD_ILP];
-    double d[RAD_ILP], sp0[RAD_ILP], sp1[RAD_ILP], fs[RAD_ILP];
+    int g[RAD_ILP], mi[RAD_ILP];   // facet and mesh of each position (mesh -1: none)
+    double d[RAD_ILP], sp0[RAD_ILP], sp1[RAD_ILP];
+    float de[RAD_ILP];
     uint8_t act[RAD_ILP];
 #pragma unroll
     for (int k = 0; k < RAD_ILP; ++k) {
       const int p = p0 + k * nthreads;
       g[k] = 0;
-      M[k] = nullptr;
+      mi[k] = -1;
       if (p >= v.nt) continue;
-      const MeshDesc* m = v.md + mesh_of_facet(v, p);
+      const int mk = mesh_of_facet(v, p);
+      const MeshDesc* m = v.md + mk;
       if (!m->active || m->ntiles == 0) continue;
-      M[k] = m;
+      mi[k] = mk;
       g[k] = (int)v.rperm[p];
       act[k] = v.row_act[p];
       sp0[k] = warm ? v.sprev[p] : 0.0;
@@ -649,20 +690,30 @@ __device__ __forceinline__ void init_x(const StepView& v, double* x, int warm, i
     }
 #pragma unroll
     for (int k = 0; k < RAD_ILP; ++k) {
-      if (!M[k]) continue;
-      d[k] = v.E[(size_t)(M[k]->frame & 1) * v.nt + g[k]];
-      fs[k] = M[k]->coupling == ILG_COUPLE_REFERENCE ? v.Fsurf[g[k]] : 0.0;
+      if (mi[k] < 0) continue;
+      const MeshDesc& Mk = v.md[mi[k]];
+      const double dk = v.E[e_slot(Mk.frame) * v.nt + g[k]];
+      const bool ref = Mk.coupling == ILG_COUPLE_REFERENCE;
+      const double fs = ref ? v.Fsurf[g[k]] : 0.0;
+      // the change of the direct flux to the next frame (none after the
+      // table's last sun)
+      if (predicted)
+        de[k] = (!Mk.host_sun && Mk.sun_idx + 1 < Mk.nsun)
+                    ? (float)(v.E[e_slot(Mk.frame + 1) * v.nt + g[k]] - dk)
+                    : 0.f;
+      // the frame's direct flux, coupled as src/cpp/illum_cli.cpp:415-421
+      // when the mesh follows the reference (rad = -Fsurf_prev + direct)
+      d[k] = ref ? (-fs + dk) : dk;
     }
 #pragma unroll
     for (int k = 0; k < RAD_ILP; ++k) {
-      if (!M[k]) continue;
+      if (mi[k] < 0) continue;
       const int p = p0 + k * nthreads;
-      const MeshDesc& Mk = *M[k];
-      // the frame's direct flux, coupled as src/cpp/illum_cli.cpp:415-421
-      // when the mesh follows the reference (rad = -Fsurf_prev + direct)
-      const double e = Mk.coupling == ILG_COUPLE_REFERENCE ? (-fs[k] + d[k]) : d[k];
+      const MeshDesc& Mk = v.md[mi[k]];
+      const double e = d[k];
       float2 s0 = make_float2(0.f, 0.f);
-      if (warm && act[k] && Mk.frame >= 1) s0 = split_df(Mk.frame >= 2 ? sp0[k] + sp1[k] : sp0[k]);
+      if (warm && act[k] && Mk.frame >= 1)
+        s0 = split_df(Mk.frame >= 2 || predicted ? sp0[k] + sp1[k] : sp0[k]);
       if (free_rows && !act[k]) {
         x[g[k]] = e;
         if (warm) {
@@ -675,7 +726,20 @@ __device__ __forceinline__ void init_x(const StepView& v, double* x, int warm, i
       B.EP[p] = e;
       B.S0[p] = s0;
       B.H0[p] = x0;
-      if (free_rows) {
+      if (predicted) {
+        // x - x_ref, high parts first (exact when within a factor of 2)
+        const int kd = kind[mi[k]];
+        float dx;
+        if (kd == 2) {
+          dx = __fadd_rn(x0.x, x0.y);
+        } else {
+          const float2 xr = B.H1[p];
+          dx = __fadd_rn(__fsub_rn(x0.x, xr.x), __fsub_rn(x0.y, xr.y));
+        }
+        if (kd) B.H1[p] = x0;
+        B.EH[p] = make_float2(dx, de[k]);
+        if (!act[k]) v.x32[v.nt + p] = 0.f;
+      } else if (free_rows) {
         v.x32[p] = 0.f;
         v.x32[v.nt + p] = 0.f;
       } else {
@@ -732,7 +796,7 @@ __device__ __forceinline__ void scatter_x(const StepView& v, const MeshState& st
 // concatenation), so each thread has a few rows in a row instead of a
 // fraction of one per tile.
 __device__ __forceinline__ void scatter_block(const StepView& v, const MeshState& st, const float2* S, double* x,
-                                              int warm) {
+                                              int warm, const float* pred = nullptr) {
   const RadBufs B(v);
   int r = threadIdx.x;
   for (int k = v.blk_start[blockIdx.x]; k < v.blk_start[blockIdx.x + 1]; ++k) {
@@ -746,7 +810,7 @@ __device__ __forceinline__ void scatter_block(const StepView& v, const MeshState
       const double sv = df_value(ld_it(S + i));
       x[g] = B.EP[i] + sv;
       if (warm) {
-        v.sprev[v.nt + i] = sv - v.sprev[i];
+        v.sprev[v.nt + i] = pred ? (double)ld_it(pred + i) : sv - v.sprev[i];
         v.sprev[i] = sv;
       }
     }
@@ -995,73 +1059,61 @@ __global__ void __launch_bounds__(RAD_BLOCK, 1) k_radiosity_mixed(StepView v, do
   record_residuals(v, st);
 }
 
-// Mixed precision with the refinement spread over the steps (refine_every =
-// K >= 1): one pass over the matrix per step, from the warm start s0 (x =
-// E + s0). A mesh's reference step (its first of the run, then every K-th)
-// applies fl(F) in double-float, s = fl(F) x, and keeps s_ref = s (S1) and
-// x_ref = x (H1, every position of the mesh). The steps between apply the
-// bf16 copy F~ (FP32 sums) to the change since then:
-//   s = s_ref + F~ (x - x_ref) = fl(F) x - (fl(F) - F~)(x - x_ref),
-// so the bf16 error (~2^-9 of each entry) multiplies only the change of x
-// since the reference pass, not x. A step is one Jacobi sweep from the warm
-// start (iteration matrix of spectral radius ~ albedo times the visible
-// fraction, ~0.01-0.03 on the crater meshes), in place of a refinement round
-// (a residual pass plus bf16 sweeps) that reads the matrix twice. The
-// step's squared change |s - s0|^2 is recorded as its residual.
+// Mixed precision, one pass over the matrix per step (refine_every = K >=
+// 1). The pass applies F to x - x_ref, where x = E + s0 is the step's
+// iterate and x_ref the iterate of the mesh's last reference step:
+//   s = s_ref + F (x - x_ref),
+// with the f32 values on a reference step (every K-th step of a mesh, and
+// its first of a run, where x_ref = 0 and s_ref = 0), which then keeps
+// (s, x) as the new reference, and the bf16 copy F~ on the steps between:
+// s = F x - (F - F~)(x - x_ref), the bf16 error confined to the change
+// since the reference step. Sums in FP32 (the terms are changes); s and
+// s_ref stay double-float. A single sweep from the previous solution would
+// leave the multiple scattering of a change of E one order behind (F^2 dE
+// for a facet that crosses the terminator), so the warm start predicts it:
+// the same pass also forms P = F (E(n+1) - E(n)) with the next frame's
+// direct flux (a second right-hand side on the same matrix entries, 8 B
+// halos of (x - x_ref, dE)), and the next step starts from s0 = s + P, off by
+// F^2 dE instead of F dE. The step's squared change |s - s0|^2 is recorded
+// as its residual.
 __global__ void __launch_bounds__(RAD_BLOCK, 1) k_radiosity_lagged(StepView v, double* x, int warm) {
   __shared__ MeshState st;
   __shared__ float red[32];
   __shared__ int bad;
-  // the pass's reference flags live in st.now until the pass is over (the
+  // each mesh's kind of pass (0: bf16 step, 1: reference step, 2: first
+  // reference step of the run) lives in st.now until the pass is over (the
   // static shared memory has no room for another array beside the ring)
-  unsigned char* refine = st.now;
+  unsigned char* kind = st.now;
   const RadSmem sm = rad_smem();
   const bool producer = threadIdx.x >= RAD_THREADS;
-  float* sxf = reinterpret_cast<float*>(sm.sx);
-  float* tailf = reinterpret_cast<float*>(sm.tail);
-  float* rsf = reinterpret_cast<float*>(sm.rs);
   const int gt = blockIdx.x * RAD_THREADS + threadIdx.x;
   const int nthreads = gridDim.x * RAD_THREADS;
-  float* dx = v.x32;   // x - x_ref by position (steps between reference passes)
+  const RadBufs B(v);
+  float2* XD = B.EH;            // by position: (x - x_ref, E(n+1) - E(n))
+  float* pred = v.x32 + v.nt;   // by position: P, the predicted change of s
   unsigned gen = 0;
   Pipe pipe = make_pipe(sm, RAD_NSTM, RAD_STAGEM, &bad);
   init_meshes(v, st);
   for (int m = threadIdx.x; m < v.nmesh; m += blockDim.x) {
     const MeshDesc& M = v.md[m];
-    refine[m] = (M.ref_age < 0 || M.ref_age + 1 >= M.refine_every) ? 1 : 0;
+    kind[m] = M.ref_age < 0 ? 2 : (M.ref_age + 1 >= M.refine_every ? 1 : 0);
   }
   __syncthreads();
-  const RadBufs B(v);
-  if (!producer) {
-    init_x(v, x, warm, gt, nthreads, true);
-    // the positions init_x gave this thread (p = gt mod nthreads): x_ref, or
-    // x - x_ref (high parts subtracted first: exact when within a factor of 2)
-    for (int p = gt; p < v.nt; p += nthreads) {
-      const MeshDesc& M = v.md[mesh_of_facet(v, p)];
-      if (!M.active || M.ntiles == 0) continue;
-      const float2 xp = B.H0[p];
-      if (refine[mesh_of_facet(v, p)]) {
-        B.H1[p] = xp;
-      } else {
-        const float2 xr = B.H1[p];
-        dx[p] = __fadd_rn(__fsub_rn(xp.x, xr.x), __fsub_rn(xp.y, xr.y));
-      }
-    }
-  }
+  if (!producer) init_x(v, x, warm, gt, nthreads, true, kind);
   if (!grid_barrier(v.barrier, gridDim.x, gen, v.derr)) return;
   // every block has read the ages: block 0 advances them
   if (blockIdx.x == 0)
     for (int m = threadIdx.x; m < v.nmesh; m += blockDim.x)
-      if (!st.done[m]) v.md[m].ref_age = refine[m] ? 0 : v.md[m].ref_age + 1;
+      if (!st.done[m]) v.md[m].ref_age = kind[m] ? 0 : v.md[m].ref_age + 1;
   const uint64_t pol = l2_keep_policy(v.l2_stream);
-  const ValsHi vhi{v.t_vhi};
+  const ValsHiF vhi{v.t_vhi};
   const ValsBF vbf{v.t_vbf};
   if (producer) {
     if ((threadIdx.x & 31) == 0)
       for (int k = v.blk_start[blockIdx.x]; k < v.blk_start[blockIdx.x + 1]; ++k) {
         const RowTile T = v.tiles[v.blk_tile[k]];
         if (st.done[T.mesh]) continue;
-        if (refine[T.mesh]) produce_tile(pipe, v, T, vhi, pol);
+        if (kind[T.mesh]) produce_tile(pipe, v, T, vhi, pol);
         else produce_tile(pipe, v, T, vbf, pol);
       }
     __syncwarp();
@@ -1070,37 +1122,32 @@ __global__ void __launch_bounds__(RAD_BLOCK, 1) k_radiosity_lagged(StepView v, d
       const int t = v.blk_tile[k];
       const RowTile T = v.tiles[t];
       if (st.done[T.mesh]) continue;
+      const int kd = kind[T.mesh];
+      stage_halo(v, T, XD, sm.sx);
+      if (kd) tile_rows<AccF2>(v, T, t, pipe, vhi, sm.sx, sm.tail, sm.tnew, sm.rs);
+      else tile_rows<AccF2>(v, T, t, pipe, vbf, sm.sx, sm.tail, sm.tnew, sm.rs);
       const uint32_t* rows = v.t_row + T.r0;
+      const float* scale = v.t_scale + T.r0;
       float d2 = 0.f;
-      if (refine[T.mesh]) {
-        stage_halo(v, T, B.H0, sm.sx);
-        tile_rows<AccDF>(v, T, t, pipe, vhi, sm.sx, sm.tail, sm.tnew, sm.rs);
-        for (int r = threadIdx.x; r < T.nrows; r += RAD_THREADS) {
-          const uint32_t i = __ldg(rows + r);
-          const float2 sn = sm.rs[r], s0 = ld_it(B.S0 + i);
-          const float df = __fadd_rn(__fsub_rn(sn.x, s0.x), __fsub_rn(sn.y, s0.y));
-          B.S0[i] = sn;
-          B.S1[i] = sn;
-          d2 = __fmaf_rn(df, df, d2);
-        }
-      } else {
-        stage_halo(v, T, dx, sxf);
-        tile_rows<AccF32>(v, T, t, pipe, vbf, sxf, tailf, sm.tnew, rsf);
-        const float* scale = v.t_scale + T.r0;
-        for (int r = threadIdx.x; r < T.nrows; r += RAD_THREADS) {
-          const uint32_t i = __ldg(rows + r);
-          const float2 sn = df_add(ld_it(B.S1 + i), make_float2(__ldg(scale + r) * rsf[r], 0.f));
-          const float2 s0 = ld_it(B.S0 + i);
-          const float df = __fadd_rn(__fsub_rn(sn.x, s0.x), __fsub_rn(sn.y, s0.y));
-          B.S0[i] = sn;
-          d2 = __fmaf_rn(df, df, d2);
-        }
+      for (int r = threadIdx.x; r < T.nrows; r += RAD_THREADS) {
+        const uint32_t i = __ldg(rows + r);
+        const float2 a = sm.rs[r];   // F (x - x_ref), F dE of the row
+        const float sc = kd ? 1.f : __ldg(scale + r);
+        const float2 sref = kd == 2 ? make_float2(0.f, 0.f) : ld_it(B.S1 + i);
+        const float2 sn = df_add(sref, make_float2(sc * a.x, 0.f));
+        const float2 s0 = ld_it(B.S0 + i);
+        const float df = __fadd_rn(__fsub_rn(sn.x, s0.x), __fsub_rn(sn.y, s0.y));
+        if (kd) B.S1[i] = sn;
+        B.S0[i] = sn;
+        pred[i] = sc * a.y;
+        d2 = __fmaf_rn(df, df, d2);
       }
       post_partial(v, st, T, t, 0, block_sum(d2, red));
     }
   }
   // every solved mesh stops after this pass: each block writes its own
-  // tiles' rows (whose s it wrote); the residual record waits for all tiles
+  // tiles' rows (whose s and P it wrote); the residual record waits for all
+  // tiles
   __syncthreads();
   for (int m = threadIdx.x; m < v.nmesh; m += blockDim.x) {
     st.now[m] = st.done[m] ? 0 : 1;
@@ -1111,7 +1158,7 @@ __global__ void __launch_bounds__(RAD_BLOCK, 1) k_radiosity_lagged(StepView v, d
     }
   }
   __syncthreads();
-  if (!producer) scatter_block(v, st, B.S0, x, warm);
+  if (!producer) scatter_block(v, st, B.S0, x, warm, pred);
   if (!grid_barrier(v.barrier, gridDim.x, gen, v.derr)) return;
   record_residuals(v, st);
 }
@@ -1281,6 +1328,7 @@ int radiosity_setup() {
 // or its rows RAD_ROWS.
 int radiosity_prepare(Context& c) {
   ILG_TRY(radiosity_setup());
+  c.ref_age = -1;   // a new matrix or layout: no one-pass reference
   cudaStream_t s = c.stream;
   const int nt = c.nt;
   const int64_t nnz = c.nnz;

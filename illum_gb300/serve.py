@@ -101,7 +101,7 @@ def footprint_bytes(level: int, nz: int, nphi: int, precision: int) -> int:
 class Server:
     def __init__(self, budget_bytes: int, precision: int = ig.PREC_MIXED, chunk_steps: int = 30, nphi: int = 32,
                  tol: float = 1e-3, solar: float = 1361.0, setup_workers: int = 4, min_rebuild_s: float = 0.25,
-                 refine_every: int = 0):
+                 refine_every: int = 4):
         self.budget = budget_bytes
         self.workers = max(1, setup_workers)
         self.min_rebuild_s = min_rebuild_s

@@ -393,14 +393,23 @@ def test_refine_every_is_checked(ilg, oracle_mod, mesh_l3):
         ctx.run_steps(opts, 0, 2)
 
 
-def test_split_runs_equal_one_run(ilg, oracle_mod, mesh_l3):
+@pytest.mark.parametrize("precision,refine_every", [(0, 0), (1, 4)])
+def test_split_runs_equal_one_run(ilg, oracle_mod, mesh_l3, precision, refine_every):
+    """Runs continue where the last one stopped (warm start, and the
+    one-pass mixed solve's reference step schedule and reference)."""
     v, f = mesh_l3
-    a = _setup_run(ilg, oracle_mod, v, f, 16, 30, 30)
-    a[0].run_steps(a[2], 0, 30)
-    b = _setup_run(ilg, oracle_mod, v, f, 16, 30, 30)
-    b[0].run_steps(b[2], 0, 10)
-    b[0].run_steps(b[2], 10, 20)
-    assert np.array_equal(a[1].T, b[1].T)
+    runs = []
+    for split in ((30,), (10, 11, 9)):
+        ctx, tm, opts, *_ = _setup_run(ilg, oracle_mod, v, f, 16, 30, 30, precision=precision)
+        if precision:
+            opts.tol, opts.max_sweeps, opts.refine_every = 1e-3, 1, refine_every
+        s0 = 0
+        for n in split:
+            ctx.run_steps(opts, s0, n)
+            s0 += n
+        runs.append((tm.T.copy(), ctx.outputs()["rad"]))
+    assert np.array_equal(runs[0][0], runs[1][0])
+    assert np.array_equal(runs[0][1], runs[1][1])
 
 
 @pytest.mark.parametrize("tol,max_sweeps,refine_every", [(1e-10, 200, 0), (1e-3, 2, 0), (1e-3, 1, 0),

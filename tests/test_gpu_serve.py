@@ -6,14 +6,16 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("workers,min_rebuild_s", [(1, 0.0), (4, 0.25)])
-def test_serving_results_equal_alone(ilg, workers, min_rebuild_s):
+@pytest.mark.parametrize("workers,min_rebuild_s,refine_every", [(1, 0.0, 4), (4, 0.25, 4), (4, 0.0, 0)])
+def test_serving_results_equal_alone(ilg, workers, min_rebuild_s, refine_every):
     """Jobs built concurrently, finished members switched off in place and
     batches re-formed: every job's final surface temperature equals the
-    job run alone, bitwise."""
+    job run alone, bitwise (the one-pass solve's reference travels with the
+    job from batch to batch)."""
     from illum_gb300 import serve
     reqs = serve.request_stream(8, rate_hz=200.0, levels=(2, 3), rotations=(1, 2), steps_per_rot=(40, 60))
-    srv = serve.Server(budget_bytes=int(2e9), chunk_steps=7, setup_workers=workers, min_rebuild_s=min_rebuild_s)
+    srv = serve.Server(budget_bytes=int(2e9), chunk_steps=7, setup_workers=workers, min_rebuild_s=min_rebuild_s,
+                       refine_every=refine_every)
     done = srv.run(reqs)
     assert len(done) == len(reqs) and srv.rebuilds >= 2
     assert sorted(j.req.rid for j in done) == list(range(len(reqs)))
