@@ -226,11 +226,15 @@ typedef struct ilg_run_opts {
   int coupling;            /* ILG_COUPLE_REFERENCE / ILG_COUPLE_DIRECT */
   int refine_every;        /* mixed precision only. 0: each step's solve runs refinement rounds
                               (residual with the f32 form factors, bf16 sweeps) until tol or
-                              max_sweeps. K >= 1: one pass over the matrix per step, warm
-                              started; every K-th step of a mesh (and its first of a run) applies
-                              the f32 form factors, s = F x, and keeps (s, x) as the reference;
+                              max_sweeps. K >= 1: one pass over the matrix per step from the
+                              warm start s0 = s(n) + F (E(n+1) - E(n)) (the next frame's direct
+                              flux is computed ahead; needs device-resident suns, not
+                              ilg_run_steps_host); every K-th step of a mesh (and its first)
+                              applies the f32 form factors and keeps (s, x) as the reference,
                               the steps between apply the bf16 copy to the change since then,
-                              s = s_ref + F~ (x - x_ref) (tol and max_sweeps unused) */
+                              s = s_ref + F~ (x - x_ref). The reference carries over to the
+                              context's next run and through batches (tol and max_sweeps
+                              unused) */
 } ilg_run_opts;
 
 /* What the radiosity solve of a step starts from. ILG_COUPLE_REFERENCE is
