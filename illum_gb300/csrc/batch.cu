@@ -60,7 +60,8 @@ struct Batch {
   dbuf<float> H32, disk32;
   dbuf<float2> hmm32;
   dbuf<SunAux> suns;
-  dbuf<double> Tsurf, Fsurf, Qprev, rad, rad_avg, therm_avg, therm_max, E, xtmp, sprev;
+  dbuf<double> Tsurf, Fsurf, Qprev, rad, rad_avg, therm_avg, therm_max, E, xtmp;
+  dbuf<float2> sprev;
   dbuf<float> x32;
   dbuf<float2> Tdf, coefdf;
   dbuf<float> T32, coef32;

@@ -330,7 +330,7 @@ static int ensure_step_buffers(Context& c, int precision) {
   ILG_TRY(c.xtmp.reserve((size_t)6 * c.nt));   // radiosity E, two iterates, double-float copies of both and of E
   if (c.sprev.n < 2 * (size_t)c.nt) {
     ILG_TRY(c.sprev.alloc(2 * (size_t)c.nt));
-    ILG_CUDA(cudaMemset(c.sprev.p, 0, 2 * (size_t)c.nt * 8));
+    ILG_CUDA(cudaMemset(c.sprev.p, 0, 2 * (size_t)c.nt * sizeof(float2)));
   }
   if (precision == ILG_PREC_MIXED) ILG_TRY(c.x32.reserve((size_t)3 * c.nt));
   ILG_TRY(c.md.reserve(1));
@@ -964,7 +964,7 @@ int ilg_thermal_init(ilg_ctx* ctx, int nz, const double* z, const double* ti, co
   for (double* p : {c.Fsurf.p, c.Qprev.p, c.rad.p, c.rad_avg.p, c.therm_avg.p, c.therm_max.p})
     ILG_CUDA(cudaMemsetAsync(p, 0, (size_t)nt * 8, c.stream));
   ILG_CUDA(cudaMemsetAsync(c.counters.p, 0, 8 * sizeof(int), c.stream));
-  if (c.sprev.p) ILG_CUDA(cudaMemsetAsync(c.sprev.p, 0, c.sprev.n * 8, c.stream));
+  if (c.sprev.p) ILG_CUDA(cudaMemsetAsync(c.sprev.p, 0, c.sprev.n * sizeof(float2), c.stream));
   invalidate_graph(c);
   ILG_CUDA(cudaStreamSynchronize(c.stream));
   c.state_prec = ILG_PREC_FP64;

@@ -133,8 +133,9 @@ struct StepView {
   double *Tsurf, *Fsurf, *Qprev, *rad, *rad_avg, *therm_avg, *therm_max;
   double* E;                   // E_SLOTS x nt: the direct flux of frame f in slot e_slot(f) (before
                                // the coupling, which its readers apply); a drop-in direct call writes slot 0
-  double* sprev;               // 2 x nt by radiosity position: scattered radiosity x - E of the last solve, and its
-                               // change (the one-pass mixed solve: its predicted change for the next step)
+  float2* sprev;               // 2 x nt by radiosity position, double-floats: scattered radiosity x - E of the last
+                               // solve, and its change (the one-pass mixed solve: its predicted change for the
+                               // next step)
   float* x32;                  // 3 x nt (mixed radiosity)
   double* T64;                 // [nz][nt] fp64 layers (standalone column entry points)
   float2* Tdf;                 // [nz][nt] double-float layers (the FP64 step)
@@ -259,7 +260,8 @@ struct Context {
   int state_prec = 0;             // which of Tdf / T32 holds the state
   dbuf<double> Tsurf, Fsurf, Qprev;
   dbuf<double> rad, rad_avg, therm_avg, therm_max, E, xtmp, Q;
-  dbuf<double> sprev;             // 2 x N by radiosity position: x - E of the last radiosity solve, and its change
+  dbuf<float2> sprev;             // 2 x N by radiosity position (double-floats): x - E of the last radiosity solve,
+                                  // and its change
   int frame_no = 0;
   int ref_age = -1;               // the one-pass mixed solve: steps since its reference step, whose
                                   // s_ref and x_ref (by position) stay in xtmp's S1 and H1; -1: none

@@ -379,6 +379,8 @@ __device__ __forceinline__ float2 df_add(float2 a, float2 b) {
   return make_float2(t, __fsub_rn(e, __fsub_rn(t, s)));
 }
 
+__device__ __forceinline__ float2 df_neg(float2 a) { return make_float2(-a.x, -a.y); }
+
 // Plain fp32 sum (mixed inner sweeps: bf16 values, fp32 iterates).
 struct AccF32 {
   typedef float W;
@@ -670,7 +672,8 @@ __device__ __forceinline__ void init_x(const StepView& v, double* x, int warm, i
   const bool predicted = kind != nullptr;
   for (int p0 = gt; p0 < v.nt; p0 += RAD_ILP * nthreads) {
     int g[RAD_ILP], mi[RAD_ILP];   // facet and mesh of each position (mesh -1: none)
-    double d[RAD_ILP], sp0[RAD_ILP], sp1[RAD_ILP];
+    double d[RAD_ILP];
+    float2 sp0[RAD_ILP], sp1[RAD_ILP];
     float de[RAD_ILP];
     uint8_t act[RAD_ILP];
 #pragma unroll
@@ -685,8 +688,8 @@ __device__ __forceinline__ void init_x(const StepView& v, double* x, int warm, i
       mi[k] = mk;
       g[k] = (int)v.rperm[p];
       act[k] = v.row_act[p];
-      sp0[k] = warm ? v.sprev[p] : 0.0;
-      sp1[k] = warm ? v.sprev[v.nt + p] : 0.0;
+      sp0[k] = warm ? v.sprev[p] : make_float2(0.f, 0.f);
+      sp1[k] = warm ? v.sprev[v.nt + p] : make_float2(0.f, 0.f);
     }
 #pragma unroll
     for (int k = 0; k < RAD_ILP; ++k) {
@@ -712,13 +715,12 @@ __device__ __forceinline__ void init_x(const StepView& v, double* x, int warm, i
       const MeshDesc& Mk = v.md[mi[k]];
       const double e = d[k];
       float2 s0 = make_float2(0.f, 0.f);
-      if (warm && act[k] && Mk.frame >= 1)
-        s0 = split_df(Mk.frame >= 2 || predicted ? sp0[k] + sp1[k] : sp0[k]);
+      if (warm && act[k] && Mk.frame >= 1) s0 = Mk.frame >= 2 || predicted ? df_add(sp0[k], sp1[k]) : sp0[k];
       if (free_rows && !act[k]) {
         x[g[k]] = e;
         if (warm) {
-          v.sprev[v.nt + p] = 0.0 - sp0[k];
-          v.sprev[p] = 0.0;
+          v.sprev[v.nt + p] = df_neg(sp0[k]);
+          v.sprev[p] = make_float2(0.f, 0.f);
         }
       }
       const float2 eh = split_df(e);
@@ -761,7 +763,8 @@ __device__ __forceinline__ void scatter_x(const StepView& v, const MeshState& st
   for (int p0 = gt; p0 < v.nt; p0 += RAD_ILP * nthreads) {
     int g[RAD_ILP];
     bool ok[RAD_ILP];
-    double s[RAD_ILP], e[RAD_ILP], sp[RAD_ILP];
+    double e[RAD_ILP];
+    float2 s[RAD_ILP], sp[RAD_ILP];
 #pragma unroll
     for (int k = 0; k < RAD_ILP; ++k) {
       const int p = p0 + k * nthreads;
@@ -772,17 +775,17 @@ __device__ __forceinline__ void scatter_x(const StepView& v, const MeshState& st
       if (!M.active || M.ntiles == 0) continue;
       ok[k] = true;
       g[k] = (int)v.rperm[p];
-      s[k] = df_value(ld_it(((st.sweeps[m] & 1) ? B.S1 : B.S0) + p));
+      s[k] = ld_it(((st.sweeps[m] & 1) ? B.S1 : B.S0) + p);
       e[k] = B.EP[p];
-      sp[k] = warm ? v.sprev[p] : 0.0;
+      sp[k] = warm ? v.sprev[p] : make_float2(0.f, 0.f);
     }
 #pragma unroll
     for (int k = 0; k < RAD_ILP; ++k) {
       if (!ok[k]) continue;
       const int p = p0 + k * nthreads;
-      x[g[k]] = e[k] + s[k];
+      x[g[k]] = e[k] + df_value(s[k]);
       if (warm) {
-        v.sprev[v.nt + p] = s[k] - sp[k];
+        v.sprev[v.nt + p] = df_add(s[k], df_neg(sp[k]));
         v.sprev[p] = s[k];
       }
     }
@@ -807,10 +810,10 @@ __device__ __forceinline__ void scatter_block(const StepView& v, const MeshState
     for (; r < T.nrows; r += RAD_THREADS) {
       const uint32_t i = __ldg(rows + r);
       const int g = (int)v.rperm[i];
-      const double sv = df_value(ld_it(S + i));
-      x[g] = B.EP[i] + sv;
+      const float2 sv = ld_it(S + i);
+      x[g] = B.EP[i] + df_value(sv);
       if (warm) {
-        v.sprev[v.nt + i] = pred ? (double)ld_it(pred + i) : sv - v.sprev[i];
+        v.sprev[v.nt + i] = pred ? make_float2(ld_it(pred + i), 0.f) : df_add(sv, df_neg(v.sprev[i]));
         v.sprev[i] = sv;
       }
     }
