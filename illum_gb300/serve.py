@@ -157,12 +157,13 @@ class Server:
 
     def _estimate(self, r: Request) -> int:
         """Bytes to reserve for r (called with the lock held): once a job of
-        the same level has been built, 1.25 x the largest measured bytes per
-        facet at that level (form factors per facet vary with the craters);
+        the same level has been built, 1.5 x the largest measured bytes per
+        facet at that level (form factors per facet vary with the craters:
+        up to 1.43 x a level's earlier maximum in the 500-request sample);
         before that, 3 x the a priori estimate."""
         pf = self.per_facet.get(r.level)
         if pf is not None:
-            return int(1.25 * pf * 20 * 4 ** r.level)
+            return int(1.5 * pf * 20 * 4 ** r.level)
         return 3 * footprint_bytes(r.level, r.nz, self.nphi, self.precision)
 
     def _build_one(self, r: Request, need: int):

@@ -27,7 +27,7 @@ def test_serving_results_equal_alone(ilg, workers, min_rebuild_s, refine_every):
 
 def test_admission_respects_budget(ilg):
     """Jobs reserve device memory before their set-up: a level's first job
-    3x the a priori estimate (built alone), the later ones 1.25x the largest
+    3x the a priori estimate (built alone), the later ones 1.5x the largest
     footprint measured at that level; each reservation is replaced by the
     measured footprint (context + batch copy) once the job is built. The
     reserved total never exceeds the budget."""
