@@ -400,6 +400,40 @@ def build_c2(ig, meshgen, precision, nmesh=None, nsteps=None):
     return members
 
 
+# Vector bytes per facet of one one-pass mixed solve (k_radiosity_lagged):
+# start pass 16 (warm-start record) + 16 (direct flux of two frames) + 9
+# (permutation, row flag, mesh) + 8 (reference iterate) + 32 written (E,
+# s0, x, halo vector); the halo vector gathered once, 8; row finishing 16
+# read + 12 written; result pass 16 + 4 + 8 read, 8 + 16 written.
+LAGGED_VEC_BYTES = 176
+
+
+def batch_roofline(stored, nf, ms_rad):
+    """HBM roofline of the batch's mixed radiosity launch: algorithmic bytes
+    per step (entry stream + vectors) over its CUDA-event time; traffic from
+    the ncu capture of a bf16 step and a reference step, weighted as the
+    steps come."""
+    peak, peak_kind = _peaks()
+    if MIXED_REFINE > 0:
+        k = MIXED_REFINE
+        b = stored * (4.0 * (k - 1) + 6.0) / k + nf * LAGGED_VEC_BYTES
+        t_bf = profile_traffic("k_radiosity_lagged_batch64")
+        t_rf = profile_traffic("k_radiosity_lagged_batch64", "dram_bytes_per_ref_launch")
+        traffic = (t_bf * (k - 1) + t_rf) / k if t_bf and t_rf else None
+        kernel = "k_radiosity_lagged"
+    else:
+        b = stored * 10.0 + nf * LAGGED_VEC_BYTES
+        traffic = None
+        kernel = "k_radiosity_mixed"
+    ach = b / (ms_rad * 1e-3) / 1e9
+    out = {"kernel": kernel, "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+           "peak_kind": peak_kind, "algorithmic_bytes": b, "avg_ms": ms_rad, "traffic": traffic,
+           "traffic_unit": "bytes per launch"}
+    if traffic:
+        out["traffic_source"] = "profiles/k_radiosity_lagged_batch64.md (ncu, one bf16 and one reference step)"
+    return out
+
+
 def nested_batch(ig, meshgen, K, W):
     """64 meshes stepped as one batch (one launch per phase, CUDA graph per
     step): mixed precision, then FP64 on the same meshes from the same
@@ -431,9 +465,11 @@ def nested_batch(ig, meshgen, K, W):
         if prec == ig.PREC_MIXED:
             Tm = [m["tm"].T for m in mem]
     err = max(float(np.abs(m["tm"].T - t).max()) for m, t in zip(mem, Tm))
+    stored = sum(m["ctx"].F_info()["stored_entries"] for m in mem)
     for m in mem:
         m["ctx"].close()
     mx, d = out[ig.PREC_MIXED], out[ig.PREC_FP64]
+    roof = batch_roofline(stored, nf, mx["phases"]["radiosity"])
     return {"value": mx["value"], "unit": UNIT, "steps": K, "warmup": W, "ms_per_step": mx["ms"],
             "dtype": mixed_dtype(),
             "config": {"workload": "64 meshes seeds 2-65, icosphere L3-L6, Poisson craters 0.0025/facet, nz 30-80, "
@@ -444,7 +480,7 @@ def nested_batch(ig, meshgen, K, W):
                        "facets": nf, "l2": "256 MB flush before every timed step"},
             "fp64_value": d["value"], "fp64_ms_per_step": d["ms"], "mixed_vs_fp64": mx["value"] / d["value"],
             "phases_ms_per_step": mx["phases"], "fp64_phases_ms_per_step": d["phases"],
-            "max_err_K_vs_fp64": err, "err_after_steps": W + K + P, "setup_s": t_setup,
+            "max_err_K_vs_fp64": err, "err_after_steps": W + K + P, "setup_s": t_setup, "roofline_radiosity": roof,
             "clocks": mx["clocks"], "fp64_clocks": d["clocks"], "gpu_launches": 5 * K}
 
 
