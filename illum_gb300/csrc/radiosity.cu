@@ -1067,8 +1067,10 @@ __global__ void __launch_bounds__(RAD_BLOCK, 1) k_radiosity_mixed(StepView v, do
 // iterate and x_ref the iterate of the mesh's last reference step:
 //   s = s_ref + F (x - x_ref),
 // with the f32 values on a reference step (every K-th step of a mesh, and
-// its first of a run, where x_ref = 0 and s_ref = 0), which then keeps
-// (s, x) as the new reference, and the bf16 copy F~ on the steps between:
+// a step without an earlier reference, where x_ref = 0 and s_ref = 0: the
+// mesh's first, or its first after a new matrix or another solve on its
+// buffers), which then keeps (s, x) as the new reference, and the bf16 copy
+// F~ on the steps between:
 // s = F x - (F - F~)(x - x_ref), the bf16 error confined to the change
 // since the reference step. Sums in FP32 (the terms are changes); s and
 // s_ref stay double-float. A single sweep from the previous solution would
@@ -1083,9 +1085,10 @@ __global__ void __launch_bounds__(RAD_BLOCK, 1) k_radiosity_lagged(StepView v, d
   __shared__ MeshState st;
   __shared__ float red[32];
   __shared__ int bad;
-  // each mesh's kind of pass (0: bf16 step, 1: reference step, 2: first
-  // reference step of the run) lives in st.now until the pass is over (the
-  // static shared memory has no room for another array beside the ring)
+  // each mesh's kind of pass (0: bf16 step, 1: reference step, 2: reference
+  // step without an earlier reference) lives in st.now until the pass is
+  // over (the static shared memory has no room for another array beside the
+  // ring)
   unsigned char* kind = st.now;
   const RadSmem sm = rad_smem();
   const bool producer = threadIdx.x >= RAD_THREADS;
