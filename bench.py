@@ -453,6 +453,7 @@ def nested_batch(ig, meshgen, K, W):
             for m in mem:
                 m["tm"], m["opts"] = c2_thermal(ig, m, prec)
         b = ig.Batch([m["ctx"] for m in mem], [m["opts"] for m in mem])
+        tune = b.autotune()   # the batch's own direct-insolation shapes (untimed)
         b.run(W)
         clk = ClockSampler(0).start()
         ms = b.bench(K, 256.0)
@@ -460,7 +461,7 @@ def nested_batch(ig, meshgen, K, W):
         _, ph = b.bench_phases(P, 256.0)
         b.sync()
         b.close()
-        out[prec] = dict(value=nf * K / (ms.sum() / 1000.0), ms=float(ms.mean()), clocks=cl,
+        out[prec] = dict(value=nf * K / (ms.sum() / 1000.0), ms=float(ms.mean()), clocks=cl, autotune=tune,
                          phases={k: float(v) / P for k, v in zip(("direct", "radiosity", "conduction"), ph)})
         if prec == ig.PREC_MIXED:
             Tm = [m["tm"].T for m in mem]
@@ -481,6 +482,7 @@ def nested_batch(ig, meshgen, K, W):
             "fp64_value": d["value"], "fp64_ms_per_step": d["ms"], "mixed_vs_fp64": mx["value"] / d["value"],
             "phases_ms_per_step": mx["phases"], "fp64_phases_ms_per_step": d["phases"],
             "max_err_K_vs_fp64": err, "err_after_steps": W + K + P, "setup_s": t_setup, "roofline_radiosity": roof,
+            "autotune": mx["autotune"], "fp64_autotune": d["autotune"],
             "clocks": mx["clocks"], "fp64_clocks": d["clocks"], "gpu_launches": 5 * K}
 
 

@@ -121,6 +121,7 @@ _SIGS = {
     "ilg_batch_run": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "ilg_batch_bench": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_void_p]),
     "ilg_batch_bench_phases": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_void_p, C.c_void_p]),
+    "ilg_batch_autotune": (C.c_int, [C.c_void_p, C.POINTER(Tune)]),
     "ilg_batch_status": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "ilg_batch_set_active": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "ilg_batch_get_tsurf": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
@@ -543,6 +544,13 @@ class Batch:
         ph = np.zeros(3)
         _check(lib().ilg_batch_bench_phases(self._h, nsteps, flush_mb, _p(ms), _p(ph)))
         return ms, ph
+
+    def autotune(self):
+        """Times every direct-insolation launch shape on the batch's own
+        workload and keeps the fastest; returns the shapes and their time."""
+        t = Tune()
+        _check(lib().ilg_batch_autotune(self._h, C.byref(t)))
+        return {k: v for k, v in t.as_dict().items() if k != "conduct_us"}
 
     def status(self):
         a = np.zeros(self.n, np.int32); d = np.zeros(self.n, np.int32); w = np.zeros(self.n, np.int32)

@@ -470,6 +470,54 @@ int ilg_batch_bench_phases(ilg_batch* batch, int nsteps, double flush_mb, double
   return batch_errors(b);
 }
 
+int ilg_batch_autotune(ilg_batch* batch, ilg_tune* chosen) {
+  if (!batch) { set_error("batch is NULL"); return ILG_ERR_ARG; }
+  Batch& b = batch->b;
+  AllocOn on_(b.stream);
+  cudaStream_t s = b.stream;
+  // the direct passes write the flux slots (timed on a copy) and the
+  // undecided-facet list and count (scratch of the pass itself)
+  dbuf<double> sE;
+  ILG_TRY(sE.alloc(b.E.n));
+  ILG_CUDA(cudaMemcpyAsync(sE.p, b.E.p, b.E.n * 8, cudaMemcpyDeviceToDevice, s));
+  StepView v = b.v;
+  v.E = sE.p;
+  const int mu32 = b.precision == ILG_PREC_MIXED ? 1 : 0;
+  cudaEvent_t e0 = b.ev[0], e1 = b.ev[3];
+  const int reps = 10;
+  double best = 1e300;
+  int best_cb = v.tune.classify_threads, best_nf = v.tune.exact_facets;
+  for (int cb : {128, 256, 512})
+    for (int nf : {4, 8, 16, 32}) {
+      v.tune.classify_threads = cb;
+      v.tune.exact_facets = nf;
+      for (int i = 0; i < 2; ++i) ILG_TRY(direct_launch(v, 0, mu32, 0, s));
+      ILG_CUDA(cudaEventRecord(e0, s));
+      for (int i = 0; i < reps; ++i) ILG_TRY(direct_launch(v, 0, mu32, 0, s));
+      ILG_CUDA(cudaEventRecord(e1, s));
+      ILG_CUDA(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      ILG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      const double us = 1000.0 * ms / reps;
+      if (us < best) { best = us; best_cb = cb; best_nf = nf; }
+    }
+  ILG_TRY(batch_errors(b));
+  b.v.tune.classify_threads = best_cb;
+  b.v.tune.exact_facets = best_nf;
+  if (b.graph) {   // captured with the previous shapes
+    cudaGraphExecDestroy(b.graph);
+    b.graph = nullptr;
+  }
+  if (chosen) {
+    chosen->classify_threads = best_cb;
+    chosen->exact_facets = best_nf;
+    chosen->conduct_threads = conduction_step_threads();
+    chosen->direct_us = best;
+    chosen->conduct_us = 0.0;
+  }
+  return ILG_OK;
+}
+
 int ilg_batch_status(ilg_batch* batch, int* active, int* steps_done, int* sweeps) {
   if (!batch) { set_error("batch is NULL"); return ILG_ERR_ARG; }
   Batch& b = batch->b;

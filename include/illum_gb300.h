@@ -346,11 +346,18 @@ int ilg_batch_run(ilg_batch* batch, int nsteps, int use_graph);
 /* nsteps timed steps (L2 flushed by a flush_mb write before each);
  * step_ms: nsteps device times. */
 int ilg_batch_bench(ilg_batch* batch, int nsteps, double flush_mb, double* step_ms);
-/* per member (arrays of n, any may be NULL): still active, steps done in
- * total (including before this batch), radiosity sweeps of the last step */
 /* Eager steps in the serial order with per-phase device times summed into
  * phase_ms[0..2] (direct, radiosity, conduction); step_ms[s] = their sum. */
 int ilg_batch_bench_phases(ilg_batch* batch, int nsteps, double flush_mb, double* step_ms, double* phase_ms);
+/* The direct-insolation launch shapes of the batch's steps (a batch starts
+ * with its first member's; its conduction runs on the batch's own block
+ * table): every supported shape timed on the batch's own workload (no state
+ * changes), the fastest kept for the batch's later steps; *chosen (may be
+ * NULL) receives the shapes and their time per step (direct_us). No result
+ * depends on the shapes. */
+int ilg_batch_autotune(ilg_batch* batch, ilg_tune* chosen);
+/* per member (arrays of n, any may be NULL): still active, steps done in
+ * total (including before this batch), radiosity sweeps of the last step */
 int ilg_batch_status(ilg_batch* batch, int* active, int* steps_done, int* sweeps);
 int ilg_batch_set_active(ilg_batch* batch, int member, int active);
 int ilg_batch_get_tsurf(ilg_batch* batch, int member, double* out);

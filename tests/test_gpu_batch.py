@@ -91,3 +91,24 @@ def test_batch_member_switched_off(ilg):
     ctx, tm, opts, n = _member(ilg, *specs[1], 0)
     h = ctx.run_steps(opts, 0, 5, record_tsurf=True)
     assert np.array_equal(b.tsurf(1), h[-1])
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_batch_autotune_keeps_results(ilg, precision):
+    """The batch's own direct-insolation shapes: supported ones, timed, and
+    the members' results the same bit for bit with and without them."""
+    specs = [(3, 41, 20, 4.0, 20), (2, 42, 35, 7.0, 14)]
+    out = []
+    for tune in (False, True):
+        mem = [_member(ilg, *sp, precision) for sp in specs]
+        b = ilg.Batch([m[0] for m in mem], [m[2] for m in mem])
+        if tune:
+            t = b.autotune()
+            assert t["classify_threads"] in (128, 256, 512) and t["exact_facets"] in (4, 8, 16, 32)
+            assert t["direct_us"] > 0
+        b.run(max(sp[4] for sp in specs))
+        b.sync()
+        out.append([(m[1].T.copy(), m[0].outputs()["rad"].copy()) for m in mem])
+        b.close()
+    for (ta, ra), (tb, rb) in zip(*out):
+        assert np.array_equal(ta, tb) and np.array_equal(ra, rb)
