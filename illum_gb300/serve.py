@@ -160,11 +160,12 @@ class Server:
         the same level has been built, 1.5 x the largest measured bytes per
         facet at that level (form factors per facet vary with the craters:
         up to 1.43 x a level's earlier maximum in the 500-request sample);
-        before that, 3 x the a priori estimate."""
+        before that, 4 x the a priori estimate (a level-7 job measured up
+        to 3.45 x it at full step counts)."""
         pf = self.per_facet.get(r.level)
         if pf is not None:
             return int(1.5 * pf * 20 * 4 ** r.level)
-        return 3 * footprint_bytes(r.level, r.nz, self.nphi, self.precision)
+        return 4 * footprint_bytes(r.level, r.nz, self.nphi, self.precision)
 
     def _build_one(self, r: Request, need: int):
         try:

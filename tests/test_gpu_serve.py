@@ -27,13 +27,13 @@ def test_serving_results_equal_alone(ilg, workers, min_rebuild_s, refine_every):
 
 def test_admission_respects_budget(ilg):
     """Jobs reserve device memory before their set-up: a level's first job
-    3x the a priori estimate (built alone), the later ones 1.5x the largest
+    4x the a priori estimate (built alone), the later ones 1.5x the largest
     footprint measured at that level; each reservation is replaced by the
     measured footprint (context + batch copy) once the job is built. The
     reserved total never exceeds the budget."""
     from illum_gb300 import serve
     reqs = serve.request_stream(6, rate_hz=1000.0, levels=(3,), rotations=(1, 1), steps_per_rot=(30, 31))
-    first = 3 * serve.footprint_bytes(3, 80, 32, ilg.PREC_MIXED)
+    first = 4 * serve.footprint_bytes(3, 80, 32, ilg.PREC_MIXED)
     srv = serve.Server(budget_bytes=int(1.5 * first), chunk_steps=10, setup_workers=4)
     done = srv.run(reqs)
     st = srv.stats()
