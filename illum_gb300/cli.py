@@ -12,7 +12,9 @@ computed on the GPU in the reference's summation order. Given --tol (2-norm
 of the residual), it instead solves to that tolerance. The thermal run is
 the library's fused step (direct -> radiosity -> conduction on the GPU),
 with the reference's coupling rad = -Fsurf + direct. --precision mixed
-selects the BF16/FP32 path, which solves to --tol. A YAML config holds flat
+selects the BF16/FP32 path, which solves to --tol, or with --refine_every K
+makes one pass over the form factors per step (the f32 values every K-th
+step; RunOpts.refine_every). A YAML config holds flat
 `key: value` pairs and lists (inline [a, b] or `- item` lines); command-line
 options given explicitly override it.
 """
@@ -108,6 +110,8 @@ def build_parser() -> argparse.ArgumentParser:
     add("--repeat", type=int)
     add("--print_config", type=_bool, default=False)
     add("--precision", default="fp64", choices=["fp64", "mixed"])
+    add("--refine_every", type=int, default=0,
+        help="mixed precision: one radiosity pass per step, the f32 form factors every K-th step (0: solve to --tol)")
     add("--seed", type=int, default=0, help="seed of the random sun direction when no sun file is given")
     return ap
 
@@ -223,8 +227,12 @@ def task_radiosity(args):
                    lambda: ctx.compute_F(albedo=_albedo(args, N), offset=args.offset, fetch=False))
     prec = ig.PREC_MIXED if args.precision == "mixed" else ig.PREC_FP64
     fixed = args.tol is None          # the reference's forward solve + gs_steps sweeps
-    if fixed and prec == ig.PREC_MIXED:
-        raise SystemExit("--precision mixed solves to a tolerance: give --tol")
+    if args.refine_every < 0 or (args.refine_every > 0 and (prec != ig.PREC_MIXED or not args.thermal)):
+        raise SystemExit("--refine_every K >= 1 goes with --precision mixed and --thermal")
+    if fixed and prec == ig.PREC_MIXED and args.refine_every == 0:
+        raise SystemExit("--precision mixed solves to a tolerance: give --tol (or --refine_every K)")
+    if args.refine_every > 0:
+        fixed = False
     if args.gs_steps < 0:
         raise SystemExit("--gs_steps must be >= 0")
     out = {}
@@ -245,9 +253,9 @@ def task_radiosity(args):
             ctx.record_thermal(len(suns))
         if fixed:
             ctx.set_radiosity_mode(ig.RAD_GS, args.gs_steps)
-        opts = ig.RunOpts(dt=args.dt, tol=0.0 if fixed else args.tol, max_sweeps=1000,
+        opts = ig.RunOpts(dt=args.dt, tol=0.0 if fixed or args.tol is None else args.tol, max_sweeps=1000,
                           use_radiosity=int(bool(args.radiosity)), use_graph=1, precision=prec,
-                          coupling=ig.COUPLE_REFERENCE)
+                          coupling=ig.COUPLE_REFERENCE, refine_every=args.refine_every)
         _timed(f"- {len(suns)} steps (direct, radiosity, conduction)", lambda: ctx.run_steps(opts, 0, len(suns)))
         o = ctx.outputs()
         out = {"rad": o["rad"], "rad_avg": o["rad_avg"], "therm_avg": o["therm_avg"], "therm_max": o["therm_max"],

@@ -83,3 +83,26 @@ def test_cli_horizon_obj_file(ilg, oracle_mod, tmp_path):
     HV, HF, _ = meshgen.load_obj(str(hobj))
     assert np.array_equal(H, oracle_mod.horizons(V, Fc, 16, horizon_mesh=(HV, HF)).T)
 
+
+
+def test_cli_mixed_one_pass(ilg, tmp_path):
+    """--precision mixed --refine_every 4 (one radiosity pass per step): the
+    thermal job's surface temperatures within the mixed path's 0.05 K of the
+    same job in FP64 solved to --tol 1e-10; the option needs the mixed
+    precision and a thermal run."""
+    from illum_gb300 import cli
+    v, f = meshgen.icosphere_craters(2, seed=3, n_craters=4, dmin_m=150.0, dmax_m=400.0)
+    obj = tmp_path / "shape.obj"
+    _write_obj(str(obj), v.astype(np.float64), f)
+    suns = meshgen.spin_sun_positions(24, 6 * 3600.0, 600.0) * 1000.0
+    np.savetxt(str(tmp_path / "sun.txt"), suns)
+    cfg = tmp_path / "job.yaml"
+    cfg.write_text("radiosity: true\nthermal: true\nnphi: 16\ndt: 600\nti: 300\nrhoc: 1.05e6\nT0: 220\n"
+                   "albedo: 0.1\ndepths: [0.002, 0.005, 0.01, 0.02, 0.05, 0.1]\n"
+                   f"sun_pos_file: {tmp_path / 'sun.txt'}\n")
+    base = ["--task", "radiosity", "--path", str(obj), "--config", str(cfg)]
+    r64 = cli.main(base + ["--tol", "1e-10", "--output_dir", str(tmp_path / "o64")])
+    rmx = cli.main(base + ["--precision", "mixed", "--refine_every", "4", "--output_dir", str(tmp_path / "omx")])
+    assert np.abs(rmx["therm"] - r64["therm"]).max() <= 0.05
+    with pytest.raises(SystemExit):
+        cli.main(base + ["--refine_every", "4", "--output_dir", str(tmp_path / "bad")])
