@@ -45,7 +45,8 @@ class IlgError(RuntimeError):
 
 class RunOpts(C.Structure):
     _fields_ = [("dt", C.c_double), ("tol", C.c_double), ("max_sweeps", C.c_int), ("use_radiosity", C.c_int),
-                ("use_graph", C.c_int), ("precision", C.c_int), ("coupling", C.c_int), ("refine_every", C.c_int)]
+                ("use_graph", C.c_int), ("precision", C.c_int), ("coupling", C.c_int), ("refine_every", C.c_int),
+                ("layer_rounding", C.c_int)]
 
 
 class Tune(C.Structure):

@@ -317,6 +317,7 @@ static int build(Batch& b) {
   for (const ilg_run_opts& o : b.opts) min_sweeps = std::min(min_sweeps, o.max_sweeps);
   b.plan.rad_inner = radiosity_inner(min_sweeps);
   b.plan.rad_lagged = b.precision == ILG_PREC_MIXED && b.opts[0].refine_every > 0;
+  b.plan.layer_sr = b.precision == ILG_PREC_MIXED && b.opts[0].layer_rounding == 1;
   b.plan.nz_max = b.nz_max;
   return ILG_OK;
 }
@@ -368,6 +369,11 @@ int ilg_batch_create(ilg_ctx** members, int n, const ilg_run_opts* opts, ilg_bat
   if (n > radiosity_max_meshes()) { set_error("a batch holds at most %d meshes", radiosity_max_meshes()); return ILG_ERR_ARG; }
   for (int i = 1; i < n; ++i)
     if (opts[i].precision != opts[0].precision) { set_error("batch members must share one precision"); return ILG_ERR_ARG; }
+  for (int i = 1; i < n; ++i)
+    if (opts[i].layer_rounding != opts[0].layer_rounding) {
+      set_error("batch members must share one layer_rounding");
+      return ILG_ERR_ARG;
+    }
   for (int i = 1; i < n; ++i)
     if ((opts[i].refine_every > 0) != (opts[0].refine_every > 0)) {
       set_error("batch members must all use refine_every > 0 or all 0");

@@ -166,7 +166,7 @@ int enqueue_step(const StepView& v, const StepPlan& p, cudaStream_t s, cudaEvent
   if (ev) ILG_CUDA(cudaEventRecord(ev[1], s));
   if (p.rad_on) ILG_TRY(radiosity_phase(v, p, s));
   if (ev) ILG_CUDA(cudaEventRecord(ev[2], s));
-  ILG_TRY(conduction_launch(v, v.rad, p.precision, 1, p.nz_max, s));
+  ILG_TRY(conduction_launch(v, v.rad, p.precision, 1, p.nz_max, s, p.layer_sr));
   if (p.rec_on) ILG_TRY(record_launch(v, p.precision, v.cblocks ? v.ncblocks : div_up(v.nt, conduction_step_threads()), s));
   if (ev) ILG_CUDA(cudaEventRecord(ev[3], s));
   return advance_launch(v, s);
@@ -209,7 +209,7 @@ int enqueue_step_pipe(const StepView& v, const StepPlan& p, cudaStream_t s, cons
   ILG_CUDA(cudaStreamWaitEvent(pipe.s2, pipe.fork, 0));
   ILG_TRY(direct_launch(v, 0, p.precision == ILG_PREC_MIXED ? 1 : 0, p.rad_lagged ? 2 : 1, pipe.s2));
   ILG_CUDA(cudaEventRecord(pipe.join, pipe.s2));
-  ILG_TRY(conduction_launch(v, v.rad, p.precision, 1, p.nz_max, s));
+  ILG_TRY(conduction_launch(v, v.rad, p.precision, 1, p.nz_max, s, p.layer_sr));
   if (p.rec_on) ILG_TRY(record_launch(v, p.precision, v.cblocks ? v.ncblocks : div_up(v.nt, conduction_step_threads()), s));
   ILG_CUDA(cudaStreamWaitEvent(s, pipe.join, 0));
   return advance_launch(v, s);
@@ -356,6 +356,11 @@ int check_run(Context& c, const ilg_run_opts* o, bool host_driven) {
     set_error("refine_every applies to the mixed precision only");
     return ILG_ERR_ARG;
   }
+  if (o->layer_rounding != 0 && o->layer_rounding != 1) { set_error("layer_rounding must be 0 or 1"); return ILG_ERR_ARG; }
+  if (o->layer_rounding && o->precision != ILG_PREC_MIXED) {
+    set_error("layer_rounding applies to the mixed precision's FP32 layers only");
+    return ILG_ERR_ARG;
+  }
   if (o->refine_every > 0 && host_driven) {
     set_error("refine_every needs the sun positions on the device (ilg_run_steps): its solve reads the next frame's flux");
     return ILG_ERR_ARG;
@@ -380,6 +385,7 @@ static StepPlan solo_plan(Context& c, const ilg_run_opts& o) {
   p.rad_grid = p.rad_on ? radiosity_grid(c.ntiles, o.precision) : 1;
   p.rad_inner = radiosity_inner(o.max_sweeps);
   p.rad_lagged = o.precision == ILG_PREC_MIXED && o.refine_every > 0;
+  p.layer_sr = o.precision == ILG_PREC_MIXED && o.layer_rounding == 1;
   p.nz_max = c.nz;
   p.rec_on = c.rec_cap > 0;
   if (p.rad_on && c.rad_mode == ILG_RAD_GS) {
@@ -431,7 +437,7 @@ static int capture_step(Context& c, const ilg_run_opts& o, int slot, cudaGraphEx
 static int get_graph(Context& c, const ilg_run_opts& o, bool with_copies, cudaGraphExec_t* out) {
   int key[6] = {(o.precision * 4 + o.coupling * 2 + (o.use_radiosity ? 1 : 0)) * 4 + radiosity_inner(o.max_sweeps),
                 (with_copies ? 1 : 0) + 2 * c.rec_cap,
-                c.nz, c.ntiles, c.rad_mode == ILG_RAD_GS ? 1 + c.gs_steps : 0, o.refine_every > 0 ? 1 : 0};
+                c.nz, c.ntiles, c.rad_mode == ILG_RAD_GS ? 1 + c.gs_steps : 0, (o.refine_every > 0 ? 1 : 0) + 2 * (o.layer_rounding ? 1 : 0)};
   if (c.graph && std::equal(key, key + 6, c.graph_key)) {
     out[0] = c.graph;
     if (with_copies) out[1] = c.graph_b;

@@ -181,9 +181,35 @@ __device__ __forceinline__ TopResult newton_top(const CondScalars& cs, dfloat T0
   return r;
 }
 
+// Unbiased rounding of an FP32 layer update a + b: the exact sum is
+// s + e (TwoSum, s = fl(a + b)); s moves one ulp toward e with probability
+// |e| / ulp, so the expected stored value is a + b and increments smaller
+// than half an ulp are not lost on average. The uniform draw is a hash of
+// (facet within its mesh, layer, frame): reproducible, and the same alone
+// and in a batch. The hash is the lowbias32 integer finaliser (C. Wellons,
+// "Prospecting for hash functions", 2018).
+__device__ __forceinline__ uint32_t sr_hash(uint32_t x) {
+  x ^= x >> 16;
+  x *= 0x7feb352dU;
+  x ^= x >> 15;
+  x *= 0x846ca68bU;
+  x ^= x >> 16;
+  return x;
+}
+__device__ __forceinline__ float sr_add(float a, float b, uint32_t key) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  if (e == 0.f || s == 0.f) return s;
+  const float n = __int_as_float(__float_as_int(s) + (((e > 0.f) == (s > 0.f)) ? 1 : -1));
+  const float u = (float)(sr_hash(key) >> 8) * 5.9604644775390625e-8f;   // [0, 1) in steps of 2^-24
+  return fabsf(e) > u * fabsf(__fsub_rn(n, s)) ? n : s;
+}
+
 // One thread per facet column. Block b covers facets [cb.y, cb.y + BS) of
-// mesh cb.x. Q: the new time level's flux per facet.
-template <class R, bool SMEM, int BS>
+// mesh cb.x. Q: the new time level's flux per facet. SR: the FP32 layers'
+// updates rounded without bias (sr_add).
+template <class R, bool SMEM, int BS, bool SR = false>
 __global__ void __launch_bounds__(BS)
 k_conduct(StepView v, const double* __restrict__ Qnp1, int upd) {
   extern __shared__ unsigned char smem_raw[];
@@ -382,7 +408,14 @@ k_conduct(StepView v, const double* __restrict__ Qnp1, int upd) {
         if (i0 + j < nz) t[j] = ld_layer(T + (size_t)(i0 + j) * N);
 #pragma unroll
       for (int j = 0; j < 16; ++j)
-        if (i0 + j < nz) T[(size_t)(i0 + j) * N] = t[j] + RHO(i0 + j);
+        if (i0 + j < nz) {
+          if constexpr (SR && std::is_same<R, float>::value)
+            T[(size_t)(i0 + j) * N] = sr_add(t[j], RHO(i0 + j),
+                                             (uint32_t)fl * 0x9E3779B9u + (uint32_t)(i0 + j) * 0x85EBCA6Bu +
+                                                 (uint32_t)M.frame * 0xC2B2AE35u);
+          else
+            T[(size_t)(i0 + j) * N] = t[j] + RHO(i0 + j);
+        }
     }
   } else {
     R prev = top;
@@ -504,10 +537,18 @@ int build_tables(int nz, const double* z, const double* ti, const double* rhoc, 
 }
 
 template <class R, int BS>
-int launch_conduct(const StepView& v, const double* Q, int upd, int nz_max, cudaStream_t s) {
+int launch_conduct(const StepView& v, const double* Q, int upd, int nz_max, cudaStream_t s, bool sr = false) {
   size_t smem = (size_t)nz_max * BS * sizeof(R);
   int grid = v.cblocks ? v.ncblocks : div_up(v.nt, BS);
   if (grid <= 0) return ILG_OK;
+  if constexpr (std::is_same<R, float>::value) {
+    if (sr) {   // unbiased layer rounding (FP32 layers, shared-memory columns)
+      if (smem > SMEM_LIMIT) { set_error("unbiased layer rounding: %d layers do not fit a column block", nz_max); return ILG_ERR_ARG; }
+      k_conduct<R, true, BS, true><<<grid, BS, smem, s>>>(v, Q, upd);
+      ILG_CUDA(cudaGetLastError());
+      return ILG_OK;
+    }
+  }
   if (smem <= SMEM_LIMIT) {
     k_conduct<R, true, BS><<<grid, BS, smem, s>>>(v, Q, upd);
   } else {
@@ -541,6 +582,13 @@ int conduction_setup() {
   ILG_CUDA(cudaFuncSetAttribute(k_conduct<dfloat, true, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_LIMIT));
   ILG_CUDA(cudaFuncSetAttribute(k_conduct<float, true, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_LIMIT));
   ILG_CUDA(cudaFuncSetAttribute(k_conduct<float, true, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_LIMIT));
+  // the unbiased-rounding variants of the FP32 kernels
+  ILG_CUDA(cudaFuncSetAttribute(k_conduct<float, true, 32, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)SMEM_LIMIT));
+  ILG_CUDA(cudaFuncSetAttribute(k_conduct<float, true, COND_STEP_THREADS, true>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_LIMIT));
+  ILG_CUDA(cudaFuncSetAttribute(k_conduct<float, true, 128, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)SMEM_LIMIT));
   done.store(true, std::memory_order_release);
   return ILG_OK;
 }
@@ -587,16 +635,18 @@ int conduction_state_convert(Context& c, int precision) {
 
 // Threads per block: the view's tuned value for a single mesh (a batch's
 // block table is cut at COND_STEP_THREADS), COND_STEP_THREADS where the
-// tuned size would not fit the column in shared memory.
-int conduction_launch(const StepView& v, const double* Q, int precision, int upd, int nz_max, cudaStream_t s) {
+// tuned size would not fit the column in shared memory. sr: the FP32
+// layers' updates rounded without bias (mixed precision).
+int conduction_launch(const StepView& v, const double* Q, int precision, int upd, int nz_max, cudaStream_t s,
+                      bool sr) {
   int bs = v.cblocks ? COND_STEP_THREADS : v.tune.conduct_threads;
   if (bs != 32 && bs != 64 && bs != 128) { set_error("conduct_threads must be 32, 64 or 128"); return ILG_ERR_ARG; }
   const size_t elt = precision == ILG_PREC_MIXED ? sizeof(float) : sizeof(dfloat);
   if ((size_t)nz_max * bs * elt > SMEM_LIMIT) bs = COND_STEP_THREADS;
   if (precision == ILG_PREC_MIXED) {
-    if (bs == 32) return launch_conduct<float, 32>(v, Q, upd, nz_max, s);
-    if (bs == 128) return launch_conduct<float, 128>(v, Q, upd, nz_max, s);
-    return launch_conduct<float, COND_STEP_THREADS>(v, Q, upd, nz_max, s);
+    if (bs == 32) return launch_conduct<float, 32>(v, Q, upd, nz_max, s, sr);
+    if (bs == 128) return launch_conduct<float, 128>(v, Q, upd, nz_max, s, sr);
+    return launch_conduct<float, COND_STEP_THREADS>(v, Q, upd, nz_max, s, sr);
   }
   if (bs == 32) return launch_conduct<dfloat, 32>(v, Q, upd, nz_max, s);
   if (bs == 128) return launch_conduct<dfloat, 128>(v, Q, upd, nz_max, s);

@@ -315,6 +315,7 @@ struct StepPlan {
   int rad_grid;
   int rad_inner;               // mixed solve: bf16 sweeps per refinement round (1..radiosity_max_inner())
   bool rad_lagged = false;     // mixed solve: one pass per step, refinement every refine_every steps
+  bool layer_sr = false;       // mixed conduction: FP32 layer updates rounded without bias
   int nz_max;
   const Context* gs_ctx = nullptr;   // fixed-sweep Gauss-Seidel of this context instead of the tolerance solve
   int gs_steps = 0;
@@ -402,7 +403,8 @@ int record_launch(const StepView& v, int precision, int ncblocks, cudaStream_t s
 int conduction_step_threads();   // facets per conduction block of a scene step
 // Q: heat flux at the new time level per facet (global index); upd: also
 // update rad_avg / therm_avg / therm_max; nz_max: deepest mesh of the view.
-int conduction_launch(const StepView& v, const double* Q, int precision, int upd, int nz_max, cudaStream_t s);
+int conduction_launch(const StepView& v, const double* Q, int precision, int upd, int nz_max, cudaStream_t s,
+                      bool sr = false);
 int conduction_state_convert(Context& c, int precision);
 int conduction_batch_host(int ncol, int nz, const double* z, double dt, const double* Qn, const double* Qnp1,
                           double* T, const double* ti, const double* rhoc, double emiss, double* Tsurf,

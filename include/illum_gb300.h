@@ -235,6 +235,10 @@ typedef struct ilg_run_opts {
                               s = s_ref + F~ (x - x_ref). The reference carries over to the
                               context's next run and through batches (tol and max_sweeps
                               unused) */
+  int layer_rounding;      /* mixed precision only. 0: the FP32 layers' updates T + dT round to
+                              nearest; 1: without bias (up one ulp with probability remainder /
+                              ulp, from a hash of facet, layer and frame), so that increments
+                              below half an ulp at depth are not lost over long runs */
 } ilg_run_opts;
 
 /* What the radiosity solve of a step starts from. ILG_COUPLE_REFERENCE is
